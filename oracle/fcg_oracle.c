@@ -1,0 +1,820 @@
+/*
+ * fcg_oracle.c -- CPU restatement of freeCappuccino's pressure-correction path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for libfcgpu.so, never part of the
+ * product.  See fcg_oracle.h for the conventions.  Build with
+ *   gcc -O2 -ffp-contract=off -fPIC -shared
+ * (no fused multiply-add, no reassociation) so that every expression below is
+ * evaluated in the order the Fortran source writes it.
+ *
+ * All citations are paths inside the freeCappuccino source tree.
+ */
+#include "fcg_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* Default-REAL (single precision) literals promoted to real(dp). */
+double orc_const_small_src(void) { return (double)1e-20f; }  /* modules_allocatable.f90:27 */
+double orc_const_small_test(void) { return (double)1e-30f; } /* tests/test_sparse_solvers.f90:36 */
+double orc_const_tol(void) { return (double)1e-13f; }        /* dpcg.f90:37, iccg.f90:191 */
+static double s0_init(void) { return (double)1.e20f; }        /* dpcg.f90:76 */
+static double geo_tiny(void) { return (double)1e-30f; }       /* mesh_geometry_and_topology.f90:57 */
+
+/* Fortran 1-based accessors. */
+#define F(arr, i) ((arr)[(i)-1])
+#define G3(arr, c, i) ((arr)[3 * ((i)-1) + ((c)-1)]) /* dPhidxi(c,i), component fastest */
+
+/* ------------------------------------------------------------------------- */
+/* Geometry: mesh_geometry_and_topology.f90:859-1079                          */
+/* ------------------------------------------------------------------------- */
+
+/* find_intersection_point, mesh_geometry_and_topology.f90:201-274: the same
+ * determinant-ratio expression, term for term, evaluated left to right. */
+static void intersection_point(double x1, double y1, double z1, double x2, double y2, double z2,
+                               double x3, double y3, double z3, double x4, double y4, double z4,
+                               double x5, double y5, double z5, double *xj, double *yj,
+                               double *zj) {
+  double num = x2 * (y3 * z4 - y4 * z3) - x1 * (y3 * z4 - y4 * z3) - x3 * (y2 * z4 - y4 * z2) +
+               x1 * (y2 * z4 - y4 * z2) + x3 * (y1 * z4 - y4 * z1) - x2 * (y1 * z4 - y4 * z1) +
+               x4 * (y2 * z3 - y3 * z2) - x1 * (y2 * z3 - y3 * z2) - x4 * (y1 * z3 - y3 * z1) +
+               x2 * (y1 * z3 - y3 * z1) + x4 * (y1 * z2 - y2 * z1) - x3 * (y1 * z2 - y2 * z1);
+  double den = x2 * (y3 * (z5 - z4) - (y5 - y4) * z3) - x1 * (y3 * (z5 - z4) - (y5 - y4) * z3) -
+               x3 * (y2 * (z5 - z4) - (y5 - y4) * z2) + x1 * (y2 * (z5 - z4) - (y5 - y4) * z2) +
+               x3 * (y1 * (z5 - z4) - (y5 - y4) * z1) - x2 * (y1 * (z5 - z4) - (y5 - y4) * z1) +
+               (x5 - x4) * (y2 * z3 - y3 * z2) - (x5 - x4) * (y1 * z3 - y3 * z1) +
+               (x5 - x4) * (y1 * z2 - y2 * z1) + geo_tiny();
+  double t = -num / den;
+  *xj = x4 + (x5 - x4) * t;
+  *yj = y4 + (y5 - y4) * t;
+  *zj = z4 + (z5 - z4) * t;
+}
+
+/* centroid_component_part_polymesh, :162-183:
+ *   1./(2*vol) * 1./24._dp*nx * ((a+b)**2 + (b+c)**2 + (c+a)**2), left to right. */
+static double cc_part(double a, double b, double c, double nx, double vol) {
+  double t = 1.0 / (2.0 * vol);
+  t = t * 1.0;
+  t = t / 24.0;
+  t = t * nx;
+  return t * ((a + b) * (a + b) + (b + c) * (b + c) + (c + a) * (c + a));
+}
+
+int orc_geometry(int numNodes, const double *x, const double *y, const double *z, int numCells,
+                 int numFaces, int numInnerFaces, const int *face_ptr, const int *face_nodes,
+                 const int *owner, const int *neighbour, double *arx, double *ary, double *arz,
+                 double *xf, double *yf, double *zf, double *xc, double *yc, double *zc,
+                 double *vol, double *facint) {
+  const double half = 0.5;
+  const double one_third = 1.0 / 3.0; /* 1./3._dp */
+  const double sixth = 1.0 / 6.0;     /* 1./6._dp, cell_volume_part_polymesh :155 */
+  (void)numNodes;
+  memset(arx, 0, sizeof(double) * numFaces);
+  memset(ary, 0, sizeof(double) * numFaces);
+  memset(arz, 0, sizeof(double) * numFaces);
+  memset(vol, 0, sizeof(double) * numCells);
+  memset(xc, 0, sizeof(double) * numCells);
+  memset(yc, 0, sizeof(double) * numCells);
+  memset(zc, 0, sizeof(double) * numCells);
+
+  /* Pass 1 (:866-950): face area vectors, cell volumes, face centres. */
+  for (int iface = 1; iface <= numFaces; ++iface) {
+    const int *node = face_nodes + face_ptr[iface - 1]; /* node[0] is node(1) */
+    int nnodes = face_ptr[iface] - face_ptr[iface - 1];
+    int inp = F(owner, iface);
+#define NX(k) F(x, node[(k)-1])
+#define NY(k) F(y, node[(k)-1])
+#define NZ(k) F(z, node[(k)-1])
+    for (int i = 1; i <= nnodes - 2; ++i) {
+      double px = NX(i + 1) - NX(1), py = NY(i + 1) - NY(1), pz = NZ(i + 1) - NZ(1);
+      double qx = NX(i + 2) - NX(1), qy = NY(i + 2) - NY(1), qz = NZ(i + 2) - NZ(1);
+      double nx = py * qz - pz * qy; /* triangular_face_area_components_polymesh :128-130 */
+      double ny = pz * qx - px * qz;
+      double nz = px * qy - py * qx;
+      F(arx, iface) = F(arx, iface) + half * nx;
+      F(ary, iface) = F(ary, iface) + half * ny;
+      F(arz, iface) = F(arz, iface) + half * nz;
+      double cx = one_third * (NX(i + 2) + NX(i + 1) + NX(1));
+      double cy = one_third * (NY(i + 2) + NY(i + 1) + NY(1));
+      double cz = one_third * (NZ(i + 2) + NZ(i + 1) + NZ(1));
+      F(vol, inp) = F(vol, inp) + sixth * (cx * nx + cy * ny + cz * nz);
+      if (iface <= numInnerFaces) {
+        int inn = F(neighbour, iface);
+        F(vol, inn) = F(vol, inn) + sixth * (cx * -nx + cy * -ny + cz * -nz);
+      }
+    }
+    /* Arithmetic-mean face centre (:936-948). */
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    for (int k = 1; k <= nnodes; ++k) {
+      sx = sx + NX(k);
+      sy = sy + NY(k);
+      sz = sz + NZ(k);
+    }
+    F(xf, iface) = sx / (double)nnodes;
+    F(yf, iface) = sy / (double)nnodes;
+    F(zf, iface) = sz / (double)nnodes;
+  }
+
+  /* Pass 2 (:972-1008): cell centroids. */
+  for (int iface = 1; iface <= numFaces; ++iface) {
+    const int *node = face_nodes + face_ptr[iface - 1];
+    int nnodes = face_ptr[iface] - face_ptr[iface - 1];
+    int inp = F(owner, iface);
+    for (int i = 1; i <= nnodes - 2; ++i) {
+      double px = NX(i + 1) - NX(1), py = NY(i + 1) - NY(1), pz = NZ(i + 1) - NZ(1);
+      double qx = NX(i + 2) - NX(1), qy = NY(i + 2) - NY(1), qz = NZ(i + 2) - NZ(1);
+      double nx = py * qz - pz * qy;
+      double ny = pz * qx - px * qz;
+      double nz = px * qy - py * qx;
+      F(xc, inp) = F(xc, inp) + cc_part(NX(1), NX(i + 1), NX(i + 2), nx, F(vol, inp));
+      F(yc, inp) = F(yc, inp) + cc_part(NY(1), NY(i + 1), NY(i + 2), ny, F(vol, inp));
+      F(zc, inp) = F(zc, inp) + cc_part(NZ(1), NZ(i + 1), NZ(i + 2), nz, F(vol, inp));
+      if (iface <= numInnerFaces) {
+        int inn = F(neighbour, iface);
+        F(xc, inn) = F(xc, inn) + cc_part(NX(1), NX(i + 2), NX(i + 1), -nx, F(vol, inn));
+        F(yc, inn) = F(yc, inn) + cc_part(NY(1), NY(i + 2), NY(i + 1), -ny, F(vol, inn));
+        F(zc, inn) = F(zc, inn) + cc_part(NZ(1), NZ(i + 2), NZ(i + 1), -nz, F(vol, inn));
+      }
+    }
+  }
+
+  /* Pass 3 (:1030-1079): interpolation factor through the plane of nodes 1..3. */
+  for (int iface = 1; iface <= numInnerFaces; ++iface) {
+    const int *node = face_nodes + face_ptr[iface - 1];
+    int inp = F(owner, iface), inn = F(neighbour, iface);
+    double xpn = F(xc, inn) - F(xc, inp);
+    double ypn = F(yc, inn) - F(yc, inp);
+    double zpn = F(zc, inn) - F(zc, inp);
+    double dpn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
+    double xjp, yjp, zjp;
+    intersection_point(NX(1), NY(1), NZ(1), NX(2), NY(2), NZ(2), NX(3), NY(3), NZ(3),
+                       F(xc, inp), F(yc, inp), F(zc, inp), F(xc, inn), F(yc, inn), F(zc, inn),
+                       &xjp, &yjp, &zjp);
+    xpn = xjp - F(xc, inp);
+    ypn = yjp - F(yc, inp);
+    zpn = zjp - F(zc, inp);
+    double djn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
+    F(facint, iface) = djn / dpn;
+  }
+#undef NX
+#undef NY
+#undef NZ
+  return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* a1: CSR pattern, sparse_matrix.f90:42-172                                  */
+/* ------------------------------------------------------------------------- */
+
+typedef struct {
+  int i, j;
+} ij_pair;
+
+static int ij_compare(const void *pa, const void *pb) {
+  const ij_pair *a = (const ij_pair *)pa, *b = (const ij_pair *)pb;
+  if (a->i != b->i) return a->i < b->i ? -1 : 1;
+  if (a->j != b->j) return a->j < b->j ? -1 : 1;
+  return 0;
+}
+
+/* csr_to_k, utils.f90:76-128: linear scan of row icell for column jcell (0 if absent). */
+static int csr_to_k(int icell, int jcell, const int *ioffset, const int *ja) {
+  for (int l = F(ioffset, icell); l <= F(ioffset, icell + 1) - 1; ++l)
+    if (F(ja, l) == jcell) return l;
+  return 0;
+}
+
+int orc_create_csr(int numCells, int numInnerFaces, const int *owner, const int *neighbour,
+                   int *ioffset, int *ja, int *diag, int *slot_pn, int *slot_np) {
+  long nnz = (long)numCells + 2L * numInnerFaces;
+  ij_pair *coo = (ij_pair *)malloc(sizeof(ij_pair) * (size_t)(nnz > 0 ? nnz : 1));
+  if (!coo) return -1;
+  /* COO fill (:61-72). */
+  for (int icell = 1; icell <= numCells; ++icell) coo[icell - 1] = (ij_pair){icell, icell};
+  for (int i = 1; i <= numInnerFaces; ++i)
+    coo[numCells + i - 1] = (ij_pair){F(owner, i), F(neighbour, i)};
+  for (int i = 1; i <= numInnerFaces; ++i)
+    coo[numCells + numInnerFaces + i - 1] = (ij_pair){F(neighbour, i), F(owner, i)};
+  /* Lexical sort (:77, i4vec2_sort_a). Pairs are unique, so any correct sort gives
+   * the same order as the reference's heap sort. */
+  qsort(coo, (size_t)nnz, sizeof(ij_pair), ij_compare);
+  for (long k = 0; k < nnz; ++k) ja[k] = coo[k].j;
+  /* Diagonal positions (:87, find_main_diag_element_positions utils.f90:130-148). */
+  int id = 1;
+  for (long indx = 1; indx <= nnz; ++indx)
+    if (coo[indx - 1].i == coo[indx - 1].j) F(diag, id++) = (int)indx;
+  /* Row starts (:97-104, find_index_position utils.f90:151-170). */
+  long istart = 1, iend = 1;
+  for (int icell = 1; icell <= numCells; ++icell) {
+    for (long i = istart; i <= iend; ++i)
+      if (coo[i - 1].i == icell) {
+        F(ioffset, icell) = (int)i;
+        break;
+      }
+    istart = F(ioffset, icell) + 1;
+    iend = nnz;
+  }
+  F(ioffset, numCells + 1) = (int)(nnz + 1);
+  free(coo);
+  /* Face -> slot maps (:159-168). */
+  for (int i = 1; i <= numInnerFaces; ++i) {
+    int ijp = F(owner, i), ijn = F(neighbour, i);
+    F(slot_pn, i) = csr_to_k(ijp, ijn, ioffset, ja);
+    F(slot_np, i) = csr_to_k(ijn, ijp, ioffset, ja);
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Boundary slot offsets, mesh_geometry_and_topology.f90:593-605              */
+/* ------------------------------------------------------------------------- */
+static int iInletStart(const orc_mesh *m) { return m->numCells; }
+static int iOutletStart(const orc_mesh *m) { return m->numCells + m->ninl; }
+static int iSymmetryStart(const orc_mesh *m) { return m->numCells + m->ninl + m->nout; }
+static int iWallStart(const orc_mesh *m) { return m->numCells + m->ninl + m->nout + m->nsym; }
+static int iPressOutletStart(const orc_mesh *m) {
+  return m->numCells + m->ninl + m->nout + m->nsym + m->nwal;
+}
+
+/* ------------------------------------------------------------------------- */
+/* a2: fvm_laplacian.f90                                                      */
+/* ------------------------------------------------------------------------- */
+
+int orc_laplacian(const orc_mesh *m, const int *ioffset, const int *diag, const int *slot_pn,
+                  const int *slot_np, const double *mu, const double *phi, double *a,
+                  double *su) {
+  long nnz = (long)F(ioffset, m->numCells + 1) - 1;
+  for (long k = 0; k < nnz; ++k) a[k] = 0.0; /* :33 */
+  for (int i = 1; i <= m->numInnerFaces; ++i) { /* :38-65 */
+    int ijp = F(m->owner, i), ijn = F(m->neighbour, i);
+    double arx = F(m->arx, i), ary = F(m->ary, i), arz = F(m->arz, i);
+    /* facefluxlaplacian :171-221 */
+    double fxn = F(m->facint, i);
+    double fxp = 1.0 - fxn;
+    double xpn = F(m->xc, ijn) - F(m->xc, ijp);
+    double ypn = F(m->yc, ijn) - F(m->yc, ijp);
+    double zpn = F(m->zc, ijn) - F(m->zc, ijp);
+    double smdpn = (arx * arx + ary * ary + arz * arz) / (arx * xpn + ary * ypn + arz * zpn);
+    double cap = (fxp * F(mu, ijp) + fxn * F(mu, ijn)) * smdpn;
+    double can = cap;
+    F(a, F(slot_pn, i)) = can;
+    F(a, F(slot_np, i)) = cap;
+    F(a, F(diag, ijp)) = F(a, F(diag, ijp)) - can;
+    F(a, F(diag, ijn)) = F(a, F(diag, ijn)) - cap;
+  }
+  /* Wall faces (:140-154); inlet/outlet/symmetry add nothing (their loops are commented out). */
+  for (int i = 1; i <= m->nwal; ++i) {
+    int iface = m->iWallFacesStart + i;
+    int ijp = F(m->owner, iface);
+    int ijb = iWallStart(m) + i;
+    int k = F(diag, ijp);
+    double are = sqrt(F(m->arx, iface) * F(m->arx, iface) + F(m->ary, iface) * F(m->ary, iface) +
+                      F(m->arz, iface) * F(m->arz, iface));
+    double dx = F(m->xc, ijp) - F(m->xf, iface);
+    double dy = F(m->yc, ijp) - F(m->yf, iface);
+    double dz = F(m->zc, ijp) - F(m->zf, iface);
+    double dpw = sqrt(dx * dx + dy * dy + dz * dz);
+    F(a, k) = F(a, k) - F(mu, ijp) * are / dpw;
+    F(su, ijp) = F(su, ijp) + F(a, k) * F(phi, ijb);
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* a3: facefluxmass.f90:34-199 inside calcp-multiple_correction_SIMPLE.f90:34-77 */
+/* ------------------------------------------------------------------------- */
+
+/* face_value_central, interpolation.f90:145-199 */
+static double face_value_central(const orc_mesh *m, int inp, int inn, double xf, double yf,
+                                 double zf, const double *fi, const double *gradfi) {
+  double gradfidr = G3(gradfi, 1, inp) * (xf - F(m->xc, inp)) +
+                    G3(gradfi, 2, inp) * (yf - F(m->yc, inp)) +
+                    G3(gradfi, 3, inp) * (zf - F(m->zc, inp)) +
+                    G3(gradfi, 1, inn) * (xf - F(m->xc, inn)) +
+                    G3(gradfi, 2, inn) * (yf - F(m->yc, inn)) +
+                    G3(gradfi, 3, inn) * (zf - F(m->zc, inn));
+  return 0.5 * (F(fi, inp) + F(fi, inn) + gradfidr);
+}
+
+int orc_facefluxmass(const orc_mesh *m, const int *diag, const int *slot_pn, const int *slot_np,
+                     const double *u, const double *v, const double *w, const double *p,
+                     const double *dUdxi, const double *dVdxi, const double *dWdxi,
+                     const double *dPdxi, const double *apu, const double *apv,
+                     const double *apw, const double *den, int nnz, double *a, double *su,
+                     double *flmass) {
+  for (int k = 0; k < nnz; ++k) a[k] = 0.0;              /* calcp :34 */
+  for (int i = 0; i < m->numCells; ++i) su[i] = 0.0;     /* calcp :35 */
+  for (int i = 1; i <= m->numInnerFaces; ++i) {
+    int ijp = F(m->owner, i), ijn = F(m->neighbour, i);
+    double xf = F(m->xf, i), yf = F(m->yf, i), zf = F(m->zf, i);
+    double arx = F(m->arx, i), ary = F(m->ary, i), arz = F(m->arz, i);
+    double fxn = F(m->facint, i);
+    double fxp = 1.0 - fxn;
+    double xpn = F(m->xc, ijn) - F(m->xc, ijp);
+    double ypn = F(m->yc, ijn) - F(m->yc, ijp);
+    double zpn = F(m->zc, ijn) - F(m->zc, ijp);
+    double are = sqrt(arx * arx + ary * ary + arz * arz);
+    double nxx = arx / are, nyy = ary / are, nzz = arz / are;
+    double Dpu = fxn * F(m->vol, ijn) * F(apu, ijn) + fxp * F(m->vol, ijp) * F(apu, ijp);
+    double Dpv = fxn * F(m->vol, ijn) * F(apv, ijn) + fxp * F(m->vol, ijp) * F(apv, ijp);
+    double Dpw = fxn * F(m->vol, ijn) * F(apw, ijn) + fxp * F(m->vol, ijp) * F(apw, ijp);
+    double dene = F(den, ijp) * fxp + F(den, ijn) * fxn;
+    double sfdpnr = 1.0 / (arx * xpn * nxx + ary * ypn * nyy + arz * zpn * nzz);
+    double smdpn = (arx * arx + ary * ary + arz * arz) * sfdpnr;
+    double cap = -(dene * Dpu * smdpn);
+    double can = cap;
+    double ui = face_value_central(m, ijp, ijn, xf, yf, zf, u, dUdxi);
+    double vi = face_value_central(m, ijp, ijn, xf, yf, zf, v, dVdxi);
+    double wi = face_value_central(m, ijp, ijn, xf, yf, zf, w, dWdxi);
+    double dpxi = Dpu * (fxn * G3(dPdxi, 1, ijn) + fxp * G3(dPdxi, 1, ijp)) * xpn * nxx;
+    double dpyi = Dpv * (fxn * G3(dPdxi, 2, ijn) + fxp * G3(dPdxi, 2, ijp)) * ypn * nyy;
+    double dpzi = Dpw * (fxn * G3(dPdxi, 3, ijn) + fxp * G3(dPdxi, 3, ijp)) * zpn * nzz;
+    double xpp = xf - (xf - F(m->xc, ijp)) * nxx;
+    double ypp = yf - (yf - F(m->yc, ijp)) * nyy;
+    double zpp = zf - (zf - F(m->zc, ijp)) * nzz;
+    double xep = xf - (xf - F(m->xc, ijn)) * nxx;
+    double yep = yf - (yf - F(m->yc, ijn)) * nyy;
+    double zep = zf - (zf - F(m->zc, ijn)) * nzz;
+    xpp = xpp - F(m->xc, ijp);
+    ypp = ypp - F(m->yc, ijp);
+    zpp = zpp - F(m->zc, ijp);
+    xep = xep - F(m->xc, ijn);
+    yep = yep - F(m->yc, ijn);
+    zep = zep - F(m->zc, ijn);
+    double dpe = F(p, ijn) - F(p, ijp);
+    /* :174-175, including the reference's sign pattern (only the first P term is subtracted). */
+    double dpecorr = G3(dPdxi, 1, ijn) * xep + G3(dPdxi, 2, ijn) * yep + G3(dPdxi, 3, ijn) * zep -
+                     G3(dPdxi, 1, ijp) * xpp + G3(dPdxi, 2, ijp) * ypp + G3(dPdxi, 3, ijp) * zpp;
+    dpe = dpe + dpecorr;
+    double dpex = Dpu * dpe * sfdpnr * arx;
+    double dpey = Dpv * dpe * sfdpnr * ary;
+    double dpez = Dpw * dpe * sfdpnr * arz;
+    double ue = ui - dpex + dpxi;
+    double ve = vi - dpey + dpyi;
+    double we = wi - dpez + dpzi;
+    double fm = dene * (ue * arx + ve * ary + we * arz);
+    F(flmass, i) = fm;
+    F(a, F(slot_pn, i)) = can;
+    F(a, F(slot_np, i)) = cap;
+    F(a, F(diag, ijp)) = F(a, F(diag, ijp)) - can;
+    F(a, F(diag, ijn)) = F(a, F(diag, ijn)) - cap;
+    F(su, ijp) = F(su, ijp) - fm;
+    F(su, ijn) = F(su, ijn) + fm;
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* a4: fluxmc, facefluxmass.f90:520-607, driven by calcp :193-206             */
+/* ------------------------------------------------------------------------- */
+
+int orc_fluxmc(const orc_mesh *m, const double *dPdxi, const double *apu, const double *den,
+               double *su, double *flmass) {
+  for (int i = 0; i < m->numCells; ++i) su[i] = 0.0; /* calcp :193 */
+  for (int i = 1; i <= m->numInnerFaces; ++i) {
+    int ijp = F(m->owner, i), ijn = F(m->neighbour, i);
+    double xf = F(m->xf, i), yf = F(m->yf, i), zf = F(m->zf, i);
+    double arx = F(m->arx, i), ary = F(m->ary, i), arz = F(m->arz, i);
+    double fxn = F(m->facint, i);
+    double fxp = 1.0 - fxn;
+    double xpn = F(m->xc, ijn) - F(m->xc, ijp);
+    double ypn = F(m->yc, ijn) - F(m->yc, ijp);
+    double zpn = F(m->zc, ijn) - F(m->zc, ijp);
+    double are = sqrt(arx * arx + ary * ary + arz * arz);
+    double nxx = arx / are, nyy = ary / are, nzz = arz / are;
+    double dppnnr = 1.0 / ((xpn * nxx) + (ypn * nyy) + (zpn * nzz));
+    double xpp = xf - (xf - F(m->xc, ijp)) * nxx;
+    double ypp = yf - (yf - F(m->yc, ijp)) * nyy;
+    double zpp = zf - (zf - F(m->zc, ijp)) * nzz;
+    double xep = xf - (xf - F(m->xc, ijn)) * nxx;
+    double yep = yf - (yf - F(m->yc, ijn)) * nyy;
+    double zep = zf - (zf - F(m->zc, ijn)) * nzz;
+    xpp = xpp - F(m->xc, ijp);
+    ypp = ypp - F(m->yc, ijp);
+    zpp = zpp - F(m->zc, ijp);
+    xep = xep - F(m->xc, ijn);
+    yep = yep - F(m->yc, ijn);
+    zep = zep - F(m->zc, ijn);
+    double rapr = F(apu, ijp) * F(den, ijp) * F(m->vol, ijp) * fxp +
+                  F(apu, ijn) * F(den, ijn) * F(m->vol, ijn) * fxn;
+    double fmcor = rapr * are *
+                   ((G3(dPdxi, 1, ijn) * xep - G3(dPdxi, 1, ijp) * xpp) +
+                    (G3(dPdxi, 2, ijn) * yep - G3(dPdxi, 2, ijp) * ypp) +
+                    (G3(dPdxi, 3, ijn) * zep - G3(dPdxi, 3, ijp) * zpp)) *
+                   dppnnr;
+    F(flmass, i) = F(flmass, i) + fmcor;
+    F(su, ijp) = F(su, ijp) - fmcor;
+    F(su, ijn) = F(su, ijn) + fmcor;
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* a5/a6: grad_gauss.f90, grad_gauss_corrected.f90                           */
+/* ------------------------------------------------------------------------- */
+
+/* One pass of grad_gauss.f90:46-113 with old gradient (dfxo,dfyo,dfzo). */
+static void gauss_pass(const orc_mesh *m, const double *fi, const double *dfxo,
+                       const double *dfyo, const double *dfzo, double *dfx, double *dfy,
+                       double *dfz) {
+  int n = m->numCells;
+  for (int i = 0; i < n; ++i) dfx[i] = dfy[i] = dfz[i] = 0.0;
+  for (int i = 1; i <= m->numInnerFaces; ++i) { /* gradco :128-190 */
+    int ijp = F(m->owner, i), ijn = F(m->neighbour, i);
+    double fxn = F(m->facint, i);
+    double fxp = 1.0 - fxn;
+    double xi = F(m->xc, ijp) * fxp + F(m->xc, ijn) * fxn;
+    double yi = F(m->yc, ijp) * fxp + F(m->yc, ijn) * fxn;
+    double zi = F(m->zc, ijp) * fxp + F(m->zc, ijn) * fxn;
+    double dfxi = F(dfxo, ijp) * fxp + F(dfxo, ijn) * fxn;
+    double dfyi = F(dfyo, ijp) * fxp + F(dfyo, ijn) * fxn;
+    double dfzi = F(dfzo, ijp) * fxp + F(dfzo, ijn) * fxn;
+    double fie = F(fi, ijp) * fxp + F(fi, ijn) * fxn + dfxi * (F(m->xf, i) - xi) +
+                 dfyi * (F(m->yf, i) - yi) + dfzi * (F(m->zf, i) - zi);
+    double dfxe = fie * F(m->arx, i), dfye = fie * F(m->ary, i), dfze = fie * F(m->arz, i);
+    F(dfx, ijp) = F(dfx, ijp) + dfxe;
+    F(dfy, ijp) = F(dfy, ijp) + dfye;
+    F(dfz, ijp) = F(dfz, ijp) + dfze;
+    F(dfx, ijn) = F(dfx, ijn) - dfxe;
+    F(dfy, ijn) = F(dfy, ijn) - dfye;
+    F(dfz, ijn) = F(dfz, ijn) - dfze;
+  }
+  /* Boundary loops :70-103 in patch-type order; gradbc :194-211. */
+  const int cnt[5] = {m->ninl, m->nout, m->nsym, m->nwal, m->npru};
+  const int fst[5] = {m->iInletFacesStart, m->iOutletFacesStart, m->iSymmetryFacesStart,
+                      m->iWallFacesStart, m->iPressOutletFacesStart};
+  const int bst[5] = {iInletStart(m), iOutletStart(m), iSymmetryStart(m), iWallStart(m),
+                      iPressOutletStart(m)};
+  for (int t = 0; t < 5; ++t)
+    for (int i = 1; i <= cnt[t]; ++i) {
+      int iface = fst[t] + i;
+      int ijp = F(m->owner, iface);
+      int ijb = bst[t] + i;
+      F(dfx, ijp) = F(dfx, ijp) + F(fi, ijb) * F(m->arx, iface);
+      F(dfy, ijp) = F(dfy, ijp) + F(fi, ijb) * F(m->ary, iface);
+      F(dfz, ijp) = F(dfz, ijp) + F(fi, ijb) * F(m->arz, iface);
+    }
+  for (int ijp = 1; ijp <= n; ++ijp) { /* :108-113 */
+    double volr = 1.0 / F(m->vol, ijp);
+    F(dfx, ijp) = F(dfx, ijp) * volr;
+    F(dfy, ijp) = F(dfy, ijp) * volr;
+    F(dfz, ijp) = F(dfz, ijp) * volr;
+  }
+}
+
+int orc_grad_gauss(const orc_mesh *m, const double *phi, int nigrad, int corrected,
+                   double *dPhidxi) {
+  int n = m->numCells;
+  double *o = (double *)calloc((size_t)3 * n + 3, sizeof(double));
+  double *g = (double *)calloc((size_t)3 * n + 3, sizeof(double));
+  if (!o || !g) return -1;
+  double *dfxo = o, *dfyo = o + n, *dfzo = o + 2 * n;
+  double *dfx = g, *dfy = g + n, *dfz = g + 2 * n;
+  int passes = nigrad;
+  if (corrected) { /* grad_gauss_corrected.f90:38-40: old gradient = incoming */
+    for (int i = 0; i < n; ++i) {
+      dfxo[i] = dPhidxi[3 * i];
+      dfyo[i] = dPhidxi[3 * i + 1];
+      dfzo[i] = dPhidxi[3 * i + 2];
+    }
+    passes = 1;
+  }
+  for (int lc = 1; lc <= passes; ++lc) {
+    gauss_pass(m, phi, dfxo, dfyo, dfzo, dfx, dfy, dfz);
+    if (lc != passes) { /* :116-120 */
+      memcpy(dfxo, dfx, sizeof(double) * n);
+      memcpy(dfyo, dfy, sizeof(double) * n);
+      memcpy(dfzo, dfz, sizeof(double) * n);
+    }
+  }
+  for (int i = 0; i < n; ++i) {
+    dPhidxi[3 * i] = dfx[i];
+    dPhidxi[3 * i + 1] = dfy[i];
+    dPhidxi[3 * i + 2] = dfz[i];
+  }
+  free(o);
+  free(g);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* a7: grad_lsq.f90                                                           */
+/* ------------------------------------------------------------------------- */
+
+#define DM(c, i) dmat[9 * ((i)-1) + ((c)-1)]
+
+int orc_grad_lsq_matrix(const orc_mesh *m, double *dmat) {
+  int n = m->numCells;
+  for (long k = 0; k < 9L * n; ++k) dmat[k] = 0.0; /* :54 */
+  for (int i = 1; i <= m->numInnerFaces; ++i) {    /* :57-82 */
+    int ijp = F(m->owner, i), ijn = F(m->neighbour, i);
+    double Dx = F(m->xc, ijn) - F(m->xc, ijp);
+    double Dy = F(m->yc, ijn) - F(m->yc, ijp);
+    double Dz = F(m->zc, ijn) - F(m->zc, ijp);
+    DM(1, ijp) += Dx * Dx;
+    DM(1, ijn) += Dx * Dx;
+    DM(4, ijp) += Dy * Dy;
+    DM(4, ijn) += Dy * Dy;
+    DM(6, ijp) += Dz * Dz;
+    DM(6, ijn) += Dz * Dz;
+    DM(2, ijp) += Dx * Dy;
+    DM(2, ijn) += Dx * Dy;
+    DM(3, ijp) += Dx * Dz;
+    DM(3, ijn) += Dx * Dz;
+    DM(5, ijp) += Dy * Dz;
+    DM(5, ijn) += Dy * Dz;
+  }
+  int nbf = m->numFaces - m->numInnerFaces;
+  for (int i = 1; i <= nbf; ++i) { /* :116-130 */
+    int iface = m->numInnerFaces + i;
+    int ijp = F(m->owner, iface);
+    double Dx = F(m->xf, iface) - F(m->xc, ijp);
+    double Dy = F(m->yf, iface) - F(m->yc, ijp);
+    double Dz = F(m->zf, iface) - F(m->zc, ijp);
+    DM(1, ijp) += Dx * Dx;
+    DM(4, ijp) += Dy * Dy;
+    DM(6, ijp) += Dz * Dz;
+    DM(2, ijp) += Dx * Dy;
+    DM(3, ijp) += Dx * Dz;
+    DM(5, ijp) += Dy * Dz;
+  }
+  for (int inp = 1; inp <= n; ++inp) { /* :134-165 */
+    double d11 = DM(1, inp), d12 = DM(2, inp), d13 = DM(3, inp);
+    double d22 = DM(4, inp), d23 = DM(5, inp), d33 = DM(6, inp);
+    double d21 = d12, d31 = d13, d32 = d23;
+    double tmp = 1.0 / (d11 * d22 * d33 - d11 * d23 * d32 - d12 * d21 * d33 + d12 * d23 * d31 +
+                        d13 * d21 * d32 - d13 * d22 * d31);
+    DM(1, inp) = (d22 * d33 - d23 * d32) * tmp;
+    DM(2, inp) = (d21 * d33 - d23 * d31) * tmp;
+    DM(3, inp) = (d21 * d32 - d22 * d31) * tmp;
+    DM(4, inp) = (d11 * d33 - d13 * d31) * tmp;
+    DM(5, inp) = (d12 * d33 - d13 * d32) * tmp;
+    DM(6, inp) = (d11 * d32 - d12 * d31) * tmp;
+    DM(7, inp) = (d12 * d23 - d13 * d22) * tmp;
+    DM(8, inp) = (d11 * d23 - d13 * d21) * tmp;
+    DM(9, inp) = (d11 * d22 - d12 * d21) * tmp;
+  }
+  return 0;
+}
+
+int orc_grad_lsq(const orc_mesh *m, const double *fi, const double *dmat, double *dFidxi) {
+  int n = m->numCells;
+  double *b = (double *)calloc((size_t)3 * n + 3, sizeof(double));
+  if (!b) return -1;
+  double *b1 = b, *b2 = b + n, *b3 = b + 2 * n;
+  for (int i = 1; i <= m->numInnerFaces; ++i) { /* :179-196 */
+    int ijp = F(m->owner, i), ijn = F(m->neighbour, i);
+    double Dx = (F(m->xc, ijn) - F(m->xc, ijp)) * (F(fi, ijn) - F(fi, ijp));
+    double Dy = (F(m->yc, ijn) - F(m->yc, ijp)) * (F(fi, ijn) - F(fi, ijp));
+    double Dz = (F(m->zc, ijn) - F(m->zc, ijp)) * (F(fi, ijn) - F(fi, ijp));
+    F(b1, ijp) += Dx;
+    F(b1, ijn) += Dx;
+    F(b2, ijp) += Dy;
+    F(b2, ijn) += Dy;
+    F(b3, ijp) += Dz;
+    F(b3, ijn) += Dz;
+  }
+  const int cnt[5] = {m->ninl, m->nout, m->nsym, m->nwal, m->npru};
+  const int fst[5] = {m->iInletFacesStart, m->iOutletFacesStart, m->iSymmetryFacesStart,
+                      m->iWallFacesStart, m->iPressOutletFacesStart};
+  const int bst[5] = {iInletStart(m), iOutletStart(m), iSymmetryStart(m), iWallStart(m),
+                      iPressOutletStart(m)};
+  for (int t = 0; t < 5; ++t) /* :220-293 */
+    for (int i = 1; i <= cnt[t]; ++i) {
+      int iface = fst[t] + i;
+      int ijp = F(m->owner, iface);
+      int ijn = bst[t] + i;
+      double Dx = (F(fi, ijn) - F(fi, ijp)) * (F(m->xf, iface) - F(m->xc, ijp));
+      double Dy = (F(fi, ijn) - F(fi, ijp)) * (F(m->yf, iface) - F(m->yc, ijp));
+      double Dz = (F(fi, ijn) - F(fi, ijp)) * (F(m->zf, iface) - F(m->zc, ijp));
+      F(b1, ijp) += Dx;
+      F(b2, ijp) += Dy;
+      F(b3, ijp) += Dz;
+    }
+  for (int inp = 1; inp <= n; ++inp) { /* :300-306 */
+    G3(dFidxi, 1, inp) = F(b1, inp) * DM(1, inp) - F(b2, inp) * DM(2, inp) + F(b3, inp) * DM(3, inp);
+    G3(dFidxi, 2, inp) = F(b1, inp) * DM(4, inp) - F(b2, inp) * DM(5, inp) - F(b3, inp) * DM(6, inp);
+    G3(dFidxi, 3, inp) = F(b1, inp) * DM(7, inp) - F(b2, inp) * DM(8, inp) + F(b3, inp) * DM(9, inp);
+  }
+  free(b);
+  return 0;
+}
+#undef DM
+
+/* ------------------------------------------------------------------------- */
+/* a8: bpres.f90                                                              */
+/* ------------------------------------------------------------------------- */
+
+int orc_bpres(const orc_mesh *m, double *p, const double *dPdxi, int istage) {
+  const int cnt[5] = {m->ninl, m->nout, m->nsym, m->nwal, m->npru};
+  const int fst[5] = {m->iInletFacesStart, m->iOutletFacesStart, m->iSymmetryFacesStart,
+                      m->iWallFacesStart, m->iPressOutletFacesStart};
+  const int bst[5] = {iInletStart(m), iOutletStart(m), iSymmetryStart(m), iWallStart(m),
+                      iPressOutletStart(m)};
+  if (istage == 1) { /* :37-96: every boundary slot takes its owner value */
+    for (int t = 0; t < 5; ++t)
+      for (int i = 1; i <= cnt[t]; ++i) F(p, bst[t] + i) = F(p, F(m->owner, fst[t] + i));
+  } else { /* :98-148: wall and pressure-outlet slots are extrapolated */
+    for (int t = 3; t < 5; ++t)
+      for (int i = 1; i <= cnt[t]; ++i) {
+        int iface = fst[t] + i;
+        int ijp = F(m->owner, iface);
+        double xpb = F(m->xf, iface) - F(m->xc, ijp);
+        double ypb = F(m->yf, iface) - F(m->yc, ijp);
+        double zpb = F(m->zf, iface) - F(m->zc, ijp);
+        F(p, bst[t] + i) = F(p, ijp) + G3(dPdxi, 1, ijp) * xpb + G3(dPdxi, 2, ijp) * ypb +
+                           G3(dPdxi, 3, ijp) * zpb;
+      }
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* a9-a11: Krylov solvers                                                     */
+/* ------------------------------------------------------------------------- */
+
+int orc_spmv(int n, const int *ioffset, const int *ja, const double *a, const double *x,
+             double *y) {
+  for (int i = 1; i <= n; ++i) {
+    double s = 0.0;
+    for (int k = F(ioffset, i); k <= F(ioffset, i + 1) - 1; ++k) s = s + F(a, k) * F(x, F(ja, k));
+    F(y, i) = s;
+  }
+  return 0;
+}
+
+/* res = su - A fi and its L1 norm (dpcg.f90:51-64). */
+static double initial_residual(int n, const int *ioffset, const int *ja, const double *a,
+                               const double *su, const double *fi, double *res) {
+  for (int i = 1; i <= n; ++i) {
+    double r = F(su, i);
+    for (int k = F(ioffset, i); k <= F(ioffset, i + 1) - 1; ++k) r = r - F(a, k) * F(fi, F(ja, k));
+    F(res, i) = r;
+  }
+  double res0 = 0.0;
+  for (int i = 0; i < n; ++i) res0 = res0 + fabs(res[i]);
+  return res0;
+}
+
+/* M^-1 r with M = (D+L) D^-1 (D+U), d = 1/D (iccg.f90:94-111, bicgstab.f90:117-136). */
+static void dic_apply(int n, const int *ioffset, const int *ja, const int *diag, const double *a,
+                      const double *d, double small, const double *r, double *zk) {
+  for (int i = 1; i <= n; ++i) {
+    double z = F(r, i);
+    for (int k = F(ioffset, i); k <= F(diag, i) - 1; ++k) z = z - F(a, k) * F(zk, F(ja, k));
+    F(zk, i) = z * F(d, i);
+  }
+  for (int i = 0; i < n; ++i) zk[i] = zk[i] / (d[i] + small);
+  for (int i = n; i >= 1; --i) {
+    double z = F(zk, i);
+    for (int k = F(diag, i) + 1; k <= F(ioffset, i + 1) - 1; ++k) z = z - F(a, k) * F(zk, F(ja, k));
+    F(zk, i) = z * F(d, i);
+  }
+}
+
+static void fill_out(orc_solver_out *out, double res0, double resl, int iters, int written) {
+  if (!out) return;
+  out->res0 = res0;
+  out->resl = resl;
+  out->iters = iters;
+  out->resor_written = written;
+  if (written) out->resor = res0;
+}
+
+/* Shared PCG body of dpcg.f90:80-147 / iccg.f90:244-325; dic != NULL selects DIC. */
+static int pcg(int n, const int *ioffset, const int *ja, const int *diag, const double *a,
+               const double *su, double *fi, double *res, const orc_solver_opts *o,
+               orc_solver_out *out, int use_dic) {
+  double *pk = (double *)calloc((size_t)n + 1, sizeof(double));
+  double *zk = (double *)calloc((size_t)n + 1, sizeof(double));
+  double *d = (double *)calloc((size_t)n + 1, sizeof(double));
+  if (!pk || !zk || !d) return -1;
+  double res0 = initial_residual(n, ioffset, ja, a, su, fi, res);
+  if (o->early_exit && res0 < orc_const_tol()) { /* dpcg.f90:66-70 */
+    fill_out(out, res0, res0, 0, 0);
+    free(pk), free(zk), free(d);
+    return 0;
+  }
+  if (use_dic) { /* iccg.f90:231-237 */
+    for (int i = 1; i <= n; ++i) {
+      double di = F(a, F(diag, i));
+      for (int k = F(ioffset, i); k <= F(diag, i) - 1; ++k)
+        di = di - F(a, k) * F(a, k) * F(d, F(ja, k));
+      F(d, i) = 1.0 / di;
+    }
+  }
+  double s0 = s0_init(), resl = res0, resor = 0.0;
+  int itr = 0;
+  for (int l = 1; l <= o->nsw; ++l) {
+    if (use_dic) {
+      dic_apply(n, ioffset, ja, diag, a, d, o->small, res, zk);
+    } else {
+      for (int i = 1; i <= n; ++i) F(zk, i) = F(res, i) / F(a, F(diag, i));
+    }
+    double sk = 0.0;
+    for (int i = 0; i < n; ++i) sk = sk + res[i] * zk[i];
+    double bet = sk / s0;
+    for (int i = 0; i < n; ++i) pk[i] = zk[i] + bet * pk[i];
+    orc_spmv(n, ioffset, ja, a, pk, zk);
+    double pkapk = 0.0;
+    for (int i = 0; i < n; ++i) pkapk = pkapk + pk[i] * zk[i];
+    double alf = sk / pkapk;
+    for (int i = 0; i < n; ++i) fi[i] = fi[i] + alf * pk[i];
+    for (int i = 0; i < n; ++i) res[i] = res[i] - alf * zk[i];
+    resl = 0.0;
+    for (int i = 0; i < n; ++i) resl = resl + fabs(res[i]);
+    s0 = sk;
+    ++itr;
+    if (l == 1) resor = res0;
+    double rsm = resl / (resor + o->small);
+    if (o->trace) {
+      o->trace[2 * (l - 1)] = resl;
+      o->trace[2 * (l - 1) + 1] = rsm;
+    }
+    if (rsm < o->resmax) break;
+  }
+  fill_out(out, res0, resl, itr, itr > 0);
+  free(pk), free(zk), free(d);
+  return 0;
+}
+
+int orc_dpcg(int n, const int *ioffset, const int *ja, const int *diag, const double *a,
+             const double *su, double *fi, double *res, const orc_solver_opts *o,
+             orc_solver_out *out) {
+  return pcg(n, ioffset, ja, diag, a, su, fi, res, o, out, 0);
+}
+
+int orc_iccg(int n, const int *ioffset, const int *ja, const int *diag, const double *a,
+             const double *su, double *fi, double *res, const orc_solver_opts *o,
+             orc_solver_out *out) {
+  return pcg(n, ioffset, ja, diag, a, su, fi, res, o, out, 1);
+}
+
+/* bicgstab.f90:1-231 (right-preconditioned, DILU). */
+int orc_bicgstab(int n, const int *ioffset, const int *ja, const int *diag, const double *a,
+                 const double *su, double *fi, double *res, const orc_solver_opts *o,
+                 orc_solver_out *out) {
+  size_t sz = (size_t)n + 1;
+  double *reso = calloc(sz, sizeof(double)), *pk = calloc(sz, sizeof(double));
+  double *uk = calloc(sz, sizeof(double)), *zk = calloc(sz, sizeof(double));
+  double *vk = calloc(sz, sizeof(double)), *d = calloc(sz, sizeof(double));
+  if (!reso || !pk || !uk || !zk || !vk || !d) return -1;
+  double res0 = initial_residual(n, ioffset, ja, a, su, fi, res);
+  if (o->early_exit && res0 < orc_const_tol()) {
+    fill_out(out, res0, res0, 0, 0);
+    free(reso), free(pk), free(uk), free(zk), free(vk), free(d);
+    return 0;
+  }
+  /* DILU diagonal (:68-79): the transpose entry a(l) is found by a scan of row ja(k)
+   * from its diagonal; when the scan finds nothing l ends one past the row. */
+  for (int i = 1; i <= n; ++i) {
+    double di = F(a, F(diag, i));
+    for (int k = F(ioffset, i); k <= F(diag, i) - 1; ++k) {
+      int jr = F(ja, k);
+      int l;
+      for (l = F(diag, jr); l <= F(ioffset, jr + 1) - 1; ++l)
+        if (F(ja, l) == i) break;
+      di = di - F(a, k) * F(d, jr) * F(a, l);
+    }
+    F(d, i) = 1.0 / di;
+  }
+  memcpy(reso, res, sizeof(double) * n);
+  double alf = 1.0, beto = 1.0, gam = 1.0, resl = res0, resor = 0.0;
+  int itr = 0;
+  for (int l = 1; l <= o->nsw; ++l) {
+    double bet = 0.0;
+    for (int i = 0; i < n; ++i) bet = bet + res[i] * reso[i];
+    double om = bet * gam / (alf * beto + o->small);
+    beto = bet;
+    for (int i = 0; i < n; ++i) pk[i] = res[i] + om * (pk[i] - alf * uk[i]);
+    dic_apply(n, ioffset, ja, diag, a, d, o->small, pk, zk);
+    orc_spmv(n, ioffset, ja, a, zk, uk);
+    double ukreso = 0.0;
+    for (int i = 0; i < n; ++i) ukreso = ukreso + uk[i] * reso[i];
+    gam = bet / ukreso;
+    for (int i = 0; i < n; ++i) fi[i] = fi[i] + gam * zk[i];
+    for (int i = 0; i < n; ++i) res[i] = res[i] - gam * uk[i];
+    dic_apply(n, ioffset, ja, diag, a, d, o->small, res, zk);
+    orc_spmv(n, ioffset, ja, a, zk, vk);
+    double vr = 0.0, vv = 0.0;
+    for (int i = 0; i < n; ++i) vr = vr + vk[i] * res[i];
+    for (int i = 0; i < n; ++i) vv = vv + vk[i] * vk[i];
+    alf = vr / (vv + o->small);
+    for (int i = 0; i < n; ++i) fi[i] = fi[i] + alf * zk[i];
+    for (int i = 0; i < n; ++i) res[i] = res[i] - alf * vk[i];
+    resl = 0.0;
+    for (int i = 0; i < n; ++i) resl = resl + fabs(res[i]);
+    ++itr;
+    if (l == 1) resor = res0;
+    double rsm = resl / (resor + o->small);
+    if (o->trace) {
+      o->trace[2 * (l - 1)] = resl;
+      o->trace[2 * (l - 1) + 1] = rsm;
+    }
+    if (rsm < o->resmax) break;
+  }
+  fill_out(out, res0, resl, itr, itr > 0);
+  free(reso), free(pk), free(uk), free(zk), free(vk), free(d);
+  return 0;
+}

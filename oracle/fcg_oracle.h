@@ -1,0 +1,123 @@
+/*
+ * fcg_oracle.h -- CPU restatement of freeCappuccino's pressure-correction path.
+ *
+ * TEST INFRASTRUCTURE ONLY. This library is the checker for the CUDA library
+ * (libfcgpu.so). Only the test-suite, the smoke check and the CPU-baseline leg of
+ * the benchmark may load it. The product never links or calls it.
+ *
+ * Every routine restates one reference subroutine, loop for loop, in the
+ * reference's evaluation order (Fortran left-to-right, no fused multiply-add:
+ * the library is compiled with -O2 -ffp-contract=off).  Index VALUES stay 1-based
+ * exactly as the Fortran arrays hold them (owner, neighbour, ioffset, ja, diag,
+ * slot maps); the C arrays themselves are 0-based, so ref(i) is c[i-1].
+ *
+ * Parity pin: the three Krylov solvers reproduce the reference's own golden
+ * traces (tests/test_sparse_solvers.f90 + tests/output.txt).  Geometry, assembly
+ * and gradient routines have no stored reference outputs; they are pinned only by
+ * this restatement.
+ */
+#ifndef FCG_ORACLE_H
+#define FCG_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Mesh description (module `geometry`, src/mesh_geometry_and_topology.f90:12-98). */
+typedef struct orc_mesh {
+  int numCells, numFaces, numInnerFaces;
+  int ninl, nout, nsym, nwal, npru;
+  /* 0-based starts as read from the boundary file (face iface = start + i, i 1-based). */
+  int iInletFacesStart, iOutletFacesStart, iSymmetryFacesStart, iWallFacesStart,
+      iPressOutletFacesStart;
+  const int *owner;     /* [numFaces]      1-based */
+  const int *neighbour; /* [numInnerFaces] 1-based */
+  const double *arx, *ary, *arz, *xf, *yf, *zf; /* [numFaces] */
+  const double *xc, *yc, *zc, *vol;             /* [numCells] */
+  const double *facint;                         /* [numInnerFaces] */
+} orc_mesh;
+
+/* Float-literal constants of the reference: default-REAL literals promoted to real(dp). */
+double orc_const_small_src(void);  /* parameters::small = 1e-20 (modules_allocatable.f90:27) */
+double orc_const_small_test(void); /* small = 1e-30 (tests/test_sparse_solvers.f90:36) */
+double orc_const_tol(void);        /* tol = 1e-13 (dpcg.f90:37) */
+
+/* --- geometry: mesh_geometry_and_topology.f90:859-1079 (triangle fans from node 1) --- */
+int orc_geometry(int numNodes, const double *x, const double *y, const double *z,
+                 int numCells, int numFaces, int numInnerFaces,
+                 const int *face_ptr,   /* [numFaces+1] 0-based offsets into face_nodes */
+                 const int *face_nodes, /* 1-based node ids */
+                 const int *owner, const int *neighbour,
+                 double *arx, double *ary, double *arz, double *xf, double *yf, double *zf,
+                 double *xc, double *yc, double *zc, double *vol, double *facint);
+
+/* --- a1: sparse_matrix.f90:42-172 --- */
+int orc_create_csr(int numCells, int numInnerFaces, const int *owner, const int *neighbour,
+                   int *ioffset /*[n+1]*/, int *ja /*[nnz]*/, int *diag /*[n]*/,
+                   int *slot_pn /*[nin]*/, int *slot_np /*[nin]*/);
+
+/* --- a2: fvm_laplacian.f90:1-163 (+ facefluxlaplacian :171-221) --- */
+int orc_laplacian(const orc_mesh *m, const int *ioffset, const int *diag,
+                  const int *slot_pn, const int *slot_np,
+                  const double *mu /*[n]*/, const double *phi /*[numTotal]*/,
+                  double *a /*[nnz] out*/, double *su /*[n] in/out*/);
+
+/* --- a3: calcp-multiple_correction_SIMPLE.f90:34-77 + facefluxmass.f90:34-199 --- */
+int orc_facefluxmass(const orc_mesh *m, const int *diag, const int *slot_pn, const int *slot_np,
+                     const double *u, const double *v, const double *w, const double *p,
+                     const double *dUdxi, const double *dVdxi, const double *dWdxi,
+                     const double *dPdxi, /* (3,n) component fastest */
+                     const double *apu, const double *apv, const double *apw, /* [n] */
+                     const double *den, /* [numTotal] */
+                     int nnz, double *a, double *su, double *flmass);
+
+/* --- a4: calcp-multiple_correction_SIMPLE.f90:193-206 + facefluxmass.f90:520-607 --- */
+int orc_fluxmc(const orc_mesh *m, const double *dPdxi, const double *apu, const double *den,
+               double *su, double *flmass);
+
+/* --- a5/a6: grad_gauss.f90:1-211, grad_gauss_corrected.f90:1-112 ---
+ * Writes dPhidxi(3,n) the way gradients.f90:95-151 / :197-259 do (zeroed first).
+ * corrected != 0 selects grad_gauss_corrected (one pass, old gradient = incoming). */
+int orc_grad_gauss(const orc_mesh *m, const double *phi, int nigrad, int corrected,
+                   double *dPhidxi);
+
+/* --- a7: grad_lsq.f90 stage 1 (:50-165) and stage 2 (:168-306) --- */
+int orc_grad_lsq_matrix(const orc_mesh *m, double *dmat /*(9,n)*/);
+int orc_grad_lsq(const orc_mesh *m, const double *phi, const double *dmat, double *dPhidxi);
+
+/* --- a8: bpres.f90:3-152 --- */
+int orc_bpres(const orc_mesh *m, double *p /*[numTotal]*/, const double *dPdxi, int istage);
+
+/* --- a9-a11: dpcg.f90, iccg.f90, bicgstab.f90 --- */
+typedef struct orc_solver_opts {
+  double resmax;   /* sor(ifi) */
+  int nsw;         /* nsw(ifi) */
+  double small;    /* parameters::small (1e-20) or the test copies' 1e-30 */
+  int early_exit;  /* 1: src/ variant returns when res0 < tol; 0: test copies never do */
+  double *trace;   /* optional [2*nsw]: per sweep (resl, rsm) */
+} orc_solver_opts;
+
+typedef struct orc_solver_out {
+  double res0, resl, resor; /* resor is written only when at least one sweep ran */
+  int iters;
+  int resor_written;
+} orc_solver_out;
+
+int orc_dpcg(int n, const int *ioffset, const int *ja, const int *diag, const double *a,
+             const double *su, double *fi, double *res, const orc_solver_opts *o,
+             orc_solver_out *out);
+int orc_iccg(int n, const int *ioffset, const int *ja, const int *diag, const double *a,
+             const double *su, double *fi, double *res, const orc_solver_opts *o,
+             orc_solver_out *out);
+int orc_bicgstab(int n, const int *ioffset, const int *ja, const int *diag, const double *a,
+                 const double *su, double *fi, double *res, const orc_solver_opts *o,
+                 orc_solver_out *out);
+
+/* Plain CSR matrix-vector product y = A x (the loop of dpcg.f90:105-110). */
+int orc_spmv(int n, const int *ioffset, const int *ja, const double *a, const double *x,
+             double *y);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
