@@ -1,0 +1,132 @@
+"""ctypes binding of libfcgpu.so (the C ABI declared in include/fcgpu.h and
+include/fcgpu_meshgen.h).  Loading fails loudly when the library has not been built:
+there is no Python or CPU fallback for any compute entry point."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import _build
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_vp = C.c_void_p
+
+FCG_OK = 0
+FCG_ERR_ARG = -1
+FCG_ERR_STATE = -2
+FCG_ERR_CUDA = -3
+FCG_ERR_INDEX = -4
+FCG_ERR_PIVOT = -5
+FCG_ERR_STALL = -6
+FCG_ERR_TIMEOUT = -7
+FCG_ERR_UNSUPPORTED = -8
+FCG_ERR_NOMEM = -9
+FCG_ERR_NONFINITE = -10
+
+FCG_GRAD_GAUSS = 1
+FCG_GRAD_GAUSS_CORRECTED = 2
+FCG_GRAD_LSQ = 3
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [
+        ("numCells", C.c_int), ("numFaces", C.c_int), ("numInnerFaces", C.c_int),
+        ("ninl", C.c_int), ("nout", C.c_int), ("nsym", C.c_int), ("nwal", C.c_int),
+        ("npru", C.c_int),
+        ("iInletFacesStart", C.c_int), ("iOutletFacesStart", C.c_int),
+        ("iSymmetryFacesStart", C.c_int), ("iWallFacesStart", C.c_int),
+        ("iPressOutletFacesStart", C.c_int), ("noc", C.c_int),
+        ("owner", _vp), ("neighbour", _vp),
+        ("arx", _vp), ("ary", _vp), ("arz", _vp), ("xf", _vp), ("yf", _vp), ("zf", _vp),
+        ("xc", _vp), ("yc", _vp), ("zc", _vp), ("vol", _vp), ("facint", _vp),
+    ]
+
+
+class FlowFields(C.Structure):
+    _fields_ = [(k, _vp) for k in ("u", "v", "w", "p", "dUdxi", "dVdxi", "dWdxi", "dPdxi",
+                                   "apu", "apv", "apw", "den")]
+
+
+class SolveReport(C.Structure):
+    _fields_ = [("res0", C.c_double), ("resl", C.c_double), ("iters", C.c_int),
+                ("converged", C.c_int), ("l2_rel", C.c_double), ("seconds", C.c_double)]
+
+
+_CTX = C.c_void_p
+
+# name -> (restype, argtypes)
+_PROTOS = {
+    "fcg_abi_version": (C.c_int, []),
+    "fcg_status_string": (C.c_char_p, [C.c_int]),
+    "fcg_last_error": (C.c_char_p, [_CTX]),
+    "fcg_create": (C.c_int, [C.POINTER(_CTX), C.c_int]),
+    "fcg_destroy": (C.c_int, [_CTX]),
+    "fcg_set_stream": (C.c_int, [_CTX, _vp]),
+    "fcg_synchronize": (C.c_int, [_CTX]),
+    "fcg_bind_mesh": (C.c_int, [_CTX, C.POINTER(MeshDesc)]),
+    "fcg_mesh_sizes": (C.c_int, [_CTX, _ip, _ip, _ip, C.POINTER(C.c_longlong), _ip]),
+    "fcg_create_csr": (C.c_int, [_CTX, _vp, _vp, _vp, _vp, _vp]),
+    "fcg_csr_build": (C.c_int, [C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "fcg_laplacian": (C.c_int, [_CTX, _vp, _vp, _vp, _vp]),
+    "fcg_facefluxmass": (C.c_int, [_CTX, C.POINTER(FlowFields), _vp, _vp, _vp]),
+    "fcg_fluxmc": (C.c_int, [_CTX, _vp, _vp, _vp, _vp, _vp]),
+    "fcg_grad": (C.c_int, [_CTX, _vp, _vp, C.c_int, C.c_int]),
+    "fcg_grad_lsq_matrix": (C.c_int, [_CTX, _vp]),
+    "fcg_bpres": (C.c_int, [_CTX, _vp, _vp, C.c_int]),
+    "fcg_dpcg": (C.c_int, [_CTX, _vp, _vp, _vp, _vp, C.c_double, C.c_int, _dp,
+                           C.POINTER(SolveReport)]),
+    "fcg_iccg": (C.c_int, [_CTX, _vp, _vp, _vp, _vp, C.c_double, C.c_int, _dp,
+                           C.POINTER(SolveReport)]),
+    "fcg_bicgstab": (C.c_int, [_CTX, _vp, _vp, _vp, _vp, C.c_double, C.c_int, _dp,
+                               C.POINTER(SolveReport)]),
+    "fcg_set_solver_options": (C.c_int, [_CTX, C.c_double, C.c_int]),
+    "fcg_get_solver_trace": (C.c_int, [_CTX, _vp, C.c_int, _ip]),
+    "fcg_spmv": (C.c_int, [_CTX, _vp, _vp, _vp]),
+    # synthetic inputs (include/fcgpu_meshgen.h)
+    "fcg_hex_mesh_sizes": (C.c_int, [C.c_int, _ip, _ip, _ip, _ip]),
+    "fcg_hex_mesh_build": (C.c_int, [C.c_int, C.c_double, C.c_ulonglong, _vp, _vp, _vp, _vp,
+                                     _vp, _vp, _vp, _vp]),
+    "fcg_mesh_geometry": (C.c_int, [C.c_int, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp,
+                                    _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                    _vp, _vp, _vp]),
+    "fcg_uniform_fill": (C.c_int, [C.c_ulonglong, C.c_ulonglong, C.c_longlong, C.c_double,
+                                   C.c_double, _vp]),
+}
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True) -> C.CDLL:
+    """Loads libfcgpu.so (building it first if asked).  Raises if it cannot be loaded."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if build_if_missing:
+        path = _build.build()
+    if not os.path.exists(path):
+        raise RuntimeError(f"libfcgpu.so is not built ({path}); run __graft_entry__.build()")
+    lib = C.CDLL(path)
+    for name, (res, args) in _PROTOS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    return list(_PROTOS)
+
+
+class FcgError(RuntimeError):
+    def __init__(self, status: int, where: str, detail: str = ""):
+        lib = load(build_if_missing=False)
+        name = lib.fcg_status_string(status).decode()
+        super().__init__(f"{where}: status {status} ({name}){': ' + detail if detail else ''}")
+        self.status = status

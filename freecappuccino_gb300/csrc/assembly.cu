@@ -1,0 +1,294 @@
+// Face-loop assembly kernels: laplacian (fvm_laplacian.f90), the pressure-correction
+// coefficients and Rhie-Chow fluxes of calcp/facefluxmass (facefluxmass.f90:34-199)
+// and the non-orthogonal corrector source of fluxmc (facefluxmass.f90:520-607).
+//
+// Each assembly is two kernels and uses no atomics:
+//   1. one thread per inner face computes the face's coefficient and flux and writes
+//      the two off-diagonal CSR slots (each slot belongs to exactly one face) and, where
+//      a per-cell sum follows, a face array;
+//   2. one thread per cell gathers its faces through the cell->face incidence list,
+//      which holds the faces in the Fortran loop's order, so the diagonal and the
+//      source are summed term by term exactly as the reference sums them.
+// This file is compiled with --fmad=false: every a*b+c below is a rounded multiply
+// followed by a rounded add, as gfortran evaluates it, so the coefficients are
+// bit-identical to the reference's loop on the same inputs.
+#include "fcg_internal.h"
+#include "launch.h"
+
+using namespace fcg;
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// laplacian(mu,phi)
+// ---------------------------------------------------------------------------
+__global__ void k_lap_faces(MeshView m, const double *__restrict__ mu, double *__restrict__ a) {
+  FCG_GRID_STRIDE(f, m.nin) {
+    int p = m.owner[f], q = m.neighbour[f];
+    double arx = m.arx[f], ary = m.ary[f], arz = m.arz[f];
+    double fxn = m.facint[f];  // facefluxlaplacian :195-196
+    double fxp = 1.0 - fxn;
+    double xpn = m.xc[q] - m.xc[p], ypn = m.yc[q] - m.yc[p], zpn = m.zc[q] - m.zc[p];
+    double smdpn = (arx * arx + ary * ary + arz * arz) / (arx * xpn + ary * ypn + arz * zpn);
+    double cap = (fxp * mu[p] + fxn * mu[q]) * smdpn;  // :218, can = cap
+    a[m.slot_pn[f]] = cap;                              // :48-49
+    a[m.slot_np[f]] = cap;                              // :52-53
+  }
+}
+
+__global__ void k_lap_cells(MeshView m, const double *__restrict__ mu,
+                            const double *__restrict__ phi, double *__restrict__ a,
+                            double *__restrict__ su) {
+  FCG_GRID_STRIDE(c, m.n) {
+    double acc = 0.0;  // a = 0 (:33), then a(diag) -= can/cap in face order (:58-63)
+    for (int e = m.cf_ptr[c]; e < m.cf_ptr[c + 1]; ++e) acc = acc - a[m.cf_slot[e]];
+    double s = su[c];
+    for (int e = m.cb_ptr[c]; e < m.cb_ptr[c + 1]; ++e) {  // wall faces :140-154
+      if (m.cb_type[e] != B_WALL) continue;
+      int f = m.cb_face[e];
+      double are = sqrt(m.arx[f] * m.arx[f] + m.ary[f] * m.ary[f] + m.arz[f] * m.arz[f]);
+      double dx = m.xc[c] - m.xf[f], dy = m.yc[c] - m.yf[f], dz = m.zc[c] - m.zf[f];
+      double dpw = sqrt(dx * dx + dy * dy + dz * dz);
+      acc = acc - mu[c] * are / dpw;
+      s = s + acc * phi[m.cb_slot[e]];
+    }
+    a[m.diag[c]] = acc;
+    su[c] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// facefluxmass inside calcp :45-77
+// ---------------------------------------------------------------------------
+struct FlowView {
+  const double *u, *v, *w, *p, *dU, *dV, *dW, *dP, *apu, *apv, *apw, *den;
+};
+
+// face_value_central, interpolation.f90:145-199
+__device__ __forceinline__ double face_value_central(const MeshView &m, int p, int q, double xf,
+                                                     double yf, double zf,
+                                                     const double *__restrict__ fi,
+                                                     const double *__restrict__ g) {
+  double gradfidr = g[3 * p] * (xf - m.xc[p]) + g[3 * p + 1] * (yf - m.yc[p]) +
+                    g[3 * p + 2] * (zf - m.zc[p]) + g[3 * q] * (xf - m.xc[q]) +
+                    g[3 * q + 1] * (yf - m.yc[q]) + g[3 * q + 2] * (zf - m.zc[q]);
+  return 0.5 * (fi[p] + fi[q] + gradfidr);
+}
+
+__global__ void k_ffm_faces(MeshView m, FlowView fl, double *__restrict__ a,
+                            double *__restrict__ flmass) {
+  FCG_GRID_STRIDE(f, m.nin) {
+    int p = m.owner[f], q = m.neighbour[f];
+    double xf = m.xf[f], yf = m.yf[f], zf = m.zf[f];
+    double arx = m.arx[f], ary = m.ary[f], arz = m.arz[f];
+    double fxn = m.facint[f];
+    double fxp = 1.0 - fxn;
+    double xpn = m.xc[q] - m.xc[p], ypn = m.yc[q] - m.yc[p], zpn = m.zc[q] - m.zc[p];
+    double are = sqrt(arx * arx + ary * ary + arz * arz);
+    double nxx = arx / are, nyy = ary / are, nzz = arz / are;
+    double Dpu = fxn * m.vol[q] * fl.apu[q] + fxp * m.vol[p] * fl.apu[p];  // :86-88
+    double Dpv = fxn * m.vol[q] * fl.apv[q] + fxp * m.vol[p] * fl.apv[p];
+    double Dpw = fxn * m.vol[q] * fl.apw[q] + fxp * m.vol[p] * fl.apw[p];
+    double dene = fl.den[p] * fxp + fl.den[q] * fxn;
+    double sfdpnr = 1.0 / (arx * xpn * nxx + ary * ypn * nyy + arz * zpn * nzz);  // :94
+    double smdpn = (arx * arx + ary * ary + arz * arz) * sfdpnr;
+    double cap = -(dene * Dpu * smdpn);  // :96, can = cap
+    double ui = face_value_central(m, p, q, xf, yf, zf, fl.u, fl.dU);
+    double vi = face_value_central(m, p, q, xf, yf, zf, fl.v, fl.dV);
+    double wi = face_value_central(m, p, q, xf, yf, zf, fl.w, fl.dW);
+    const double *dP = fl.dP;
+    double dpxi = Dpu * (fxn * dP[3 * q] + fxp * dP[3 * p]) * xpn * nxx;  // :145-147
+    double dpyi = Dpv * (fxn * dP[3 * q + 1] + fxp * dP[3 * p + 1]) * ypn * nyy;
+    double dpzi = Dpw * (fxn * dP[3 * q + 2] + fxp * dP[3 * p + 2]) * zpn * nzz;
+    double xpp = xf - (xf - m.xc[p]) * nxx, ypp = yf - (yf - m.yc[p]) * nyy,
+           zpp = zf - (zf - m.zc[p]) * nzz;
+    double xep = xf - (xf - m.xc[q]) * nxx, yep = yf - (yf - m.yc[q]) * nyy,
+           zep = zf - (zf - m.zc[q]) * nzz;
+    xpp = xpp - m.xc[p];
+    ypp = ypp - m.yc[p];
+    zpp = zpp - m.zc[p];
+    xep = xep - m.xc[q];
+    yep = yep - m.yc[q];
+    zep = zep - m.zc[q];
+    double dpe = fl.p[q] - fl.p[p];
+    // :174-175 as written: only the first owner term carries the minus sign.
+    double dpecorr = dP[3 * q] * xep + dP[3 * q + 1] * yep + dP[3 * q + 2] * zep - dP[3 * p] * xpp +
+                     dP[3 * p + 1] * ypp + dP[3 * p + 2] * zpp;
+    dpe = dpe + dpecorr;
+    double dpex = Dpu * dpe * sfdpnr * arx, dpey = Dpv * dpe * sfdpnr * ary,
+           dpez = Dpw * dpe * sfdpnr * arz;
+    double ue = ui - dpex + dpxi, ve = vi - dpey + dpyi, we = wi - dpez + dpzi;
+    flmass[f] = dene * (ue * arx + ve * ary + we * arz);  // :185
+    a[m.slot_pn[f]] = cap;
+    a[m.slot_np[f]] = cap;
+  }
+}
+
+// Diagonal from the cell's own off-diagonal slots and su from the face fluxes, both in
+// face order (calcp :65-75).
+__global__ void k_ffm_cells(MeshView m, const double *__restrict__ flmass, double *__restrict__ a,
+                            double *__restrict__ su) {
+  FCG_GRID_STRIDE(c, m.n) {
+    double acc = 0.0, s = 0.0;
+    for (int e = m.cf_ptr[c]; e < m.cf_ptr[c + 1]; ++e) {
+      int ent = m.cf_ent[e];
+      acc = acc - a[m.cf_slot[e]];
+      double fm = flmass[(ent > 0 ? ent : -ent) - 1];
+      s = ent > 0 ? s - fm : s + fm;
+    }
+    a[m.diag[c]] = acc;
+    su[c] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// fluxmc inside calcp :193-206
+// ---------------------------------------------------------------------------
+__global__ void k_fmc_faces(MeshView m, const double *__restrict__ dP,
+                            const double *__restrict__ apu, const double *__restrict__ den,
+                            double *__restrict__ flmass, double *__restrict__ fmcor_out) {
+  FCG_GRID_STRIDE(f, m.nin) {
+    int p = m.owner[f], q = m.neighbour[f];
+    double xf = m.xf[f], yf = m.yf[f], zf = m.zf[f];
+    double arx = m.arx[f], ary = m.ary[f], arz = m.arz[f];
+    double fxn = m.facint[f];
+    double fxp = 1.0 - fxn;
+    double xpn = m.xc[q] - m.xc[p], ypn = m.yc[q] - m.yc[p], zpn = m.zc[q] - m.zc[p];
+    double are = sqrt(arx * arx + ary * ary + arz * arz);
+    double nxx = arx / are, nyy = ary / are, nzz = arz / are;
+    double dppnnr = 1.0 / ((xpn * nxx) + (ypn * nyy) + (zpn * nzz));  // :578
+    double xpp = xf - (xf - m.xc[p]) * nxx, ypp = yf - (yf - m.yc[p]) * nyy,
+           zpp = zf - (zf - m.zc[p]) * nzz;
+    double xep = xf - (xf - m.xc[q]) * nxx, yep = yf - (yf - m.yc[q]) * nyy,
+           zep = zf - (zf - m.zc[q]) * nzz;
+    xpp = xpp - m.xc[p];
+    ypp = ypp - m.yc[p];
+    zpp = zpp - m.zc[p];
+    xep = xep - m.xc[q];
+    yep = yep - m.yc[q];
+    zep = zep - m.zc[q];
+    double rapr = apu[p] * den[p] * m.vol[p] * fxp + apu[q] * den[q] * m.vol[q] * fxn;  // :599
+    double fmcor = rapr * are *
+                   ((dP[3 * q] * xep - dP[3 * p] * xpp) + (dP[3 * q + 1] * yep - dP[3 * p + 1] * ypp) +
+                    (dP[3 * q + 2] * zep - dP[3 * p + 2] * zpp)) *
+                   dppnnr;  // :603-605
+    flmass[f] = flmass[f] + fmcor;  // calcp :201
+    fmcor_out[f] = fmcor;
+  }
+}
+
+__global__ void k_fmc_cells(MeshView m, const double *__restrict__ fmcor, double *__restrict__ su) {
+  FCG_GRID_STRIDE(c, m.n) {
+    double s = 0.0;  // su = 0 (:193), then -= / += fmcor in face order (:203-204)
+    for (int e = m.cf_ptr[c]; e < m.cf_ptr[c + 1]; ++e) {
+      int ent = m.cf_ent[e];
+      double fm = fmcor[(ent > 0 ? ent : -ent) - 1];
+      s = ent > 0 ? s - fm : s + fm;
+    }
+    su[c] = s;
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" int fcg_laplacian(fcg_context *c, const double *mu, const double *phi, double *a,
+                             double *su) {
+  if (!c) return FCG_ERR_ARG;
+  if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_laplacian before fcg_bind_mesh");
+  FCG_CUDA_TRY(c, cudaSetDevice(c->device));
+  void *dmu, *dphi, *da, *dsu;
+  bool hmu, hphi, ha, hsu;
+  int rc;
+  if ((rc = stage_in(c, mu, sizeof(double) * c->n, 0, true, &dmu, &hmu))) return rc;
+  if ((rc = stage_in(c, phi, sizeof(double) * c->ntot, 1, true, &dphi, &hphi))) return rc;
+  if ((rc = stage_in(c, a, sizeof(double) * c->nnz, 2, false, &da, &ha))) return rc;
+  if ((rc = stage_in(c, su, sizeof(double) * c->n, 3, true, &dsu, &hsu))) return rc;
+  const MeshView &m = c->mv;
+  if (m.nin > 0) {
+    k_lap_faces<<<grid_for(m.nin, c->num_sms), kTPB, 0, c->stream>>>(m, (const double *)dmu,
+                                                                        (double *)da);
+    FCG_CHECK_LAUNCH(c, "k_lap_faces");
+  }
+  k_lap_cells<<<grid_for(m.n, c->num_sms), kTPB, 0, c->stream>>>(
+      m, (const double *)dmu, (const double *)dphi, (double *)da, (double *)dsu);
+  FCG_CHECK_LAUNCH(c, "k_lap_cells");
+  if ((rc = stage_out(c, a, da, sizeof(double) * c->nnz, ha))) return rc;
+  if ((rc = stage_out(c, su, dsu, sizeof(double) * c->n, hsu))) return rc;
+  if (ha || hsu) FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return FCG_OK;
+}
+
+extern "C" int fcg_facefluxmass(fcg_context *c, const fcg_flow_fields *f, double *a, double *su,
+                                double *flmass) {
+  if (!c || !f) return FCG_ERR_ARG;
+  if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_facefluxmass before fcg_bind_mesh");
+  FCG_CUDA_TRY(c, cudaSetDevice(c->device));
+  const size_t nt = sizeof(double) * c->ntot, n1 = sizeof(double) * c->n, n3 = 3 * n1;
+  const double *src[12] = {f->u, f->v, f->w, f->p, f->dUdxi, f->dVdxi, f->dWdxi, f->dPdxi,
+                           f->apu, f->apv, f->apw, f->den};
+  const size_t bytes[12] = {nt, nt, nt, nt, n3, n3, n3, n3, n1, n1, n1, nt};
+  void *dev[12];
+  bool host[12];
+  int rc;
+  for (int i = 0; i < 12; ++i)
+    if ((rc = stage_in(c, src[i], bytes[i], i, true, &dev[i], &host[i]))) return rc;
+  void *da, *dsu, *dfm;
+  bool ha, hsu, hfm;
+  if ((rc = stage_in(c, a, sizeof(double) * c->nnz, 12, false, &da, &ha))) return rc;
+  if ((rc = stage_in(c, su, n1, 13, false, &dsu, &hsu))) return rc;
+  if ((rc = stage_in(c, flmass, sizeof(double) * (c->nin > 0 ? c->nin : 1), 14, false, &dfm, &hfm)))
+    return rc;
+  FlowView fl{(const double *)dev[0], (const double *)dev[1], (const double *)dev[2],
+              (const double *)dev[3], (const double *)dev[4], (const double *)dev[5],
+              (const double *)dev[6], (const double *)dev[7], (const double *)dev[8],
+              (const double *)dev[9], (const double *)dev[10], (const double *)dev[11]};
+  const MeshView &m = c->mv;
+  if (m.nin > 0) {
+    k_ffm_faces<<<grid_for(m.nin, c->num_sms), kTPB, 0, c->stream>>>(m, fl, (double *)da,
+                                                                        (double *)dfm);
+    FCG_CHECK_LAUNCH(c, "k_ffm_faces");
+  }
+  k_ffm_cells<<<grid_for(m.n, c->num_sms), kTPB, 0, c->stream>>>(m, (const double *)dfm,
+                                                                    (double *)da, (double *)dsu);
+  FCG_CHECK_LAUNCH(c, "k_ffm_cells");
+  if ((rc = stage_out(c, a, da, sizeof(double) * c->nnz, ha))) return rc;
+  if ((rc = stage_out(c, su, dsu, n1, hsu))) return rc;
+  if ((rc = stage_out(c, flmass, dfm, sizeof(double) * c->nin, hfm))) return rc;
+  if (ha || hsu || hfm) FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return FCG_OK;
+}
+
+extern "C" int fcg_fluxmc(fcg_context *c, const double *dPdxi, const double *apu,
+                          const double *den, double *su, double *flmass) {
+  if (!c) return FCG_ERR_ARG;
+  if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_fluxmc before fcg_bind_mesh");
+  FCG_CUDA_TRY(c, cudaSetDevice(c->device));
+  void *dP, *dapu, *dden, *dsu, *dfm;
+  bool h0, h1, h2, hsu, hfm;
+  int rc;
+  const size_t n1 = sizeof(double) * c->n;
+  if ((rc = stage_in(c, dPdxi, 3 * n1, 0, true, &dP, &h0))) return rc;
+  if ((rc = stage_in(c, apu, n1, 1, true, &dapu, &h1))) return rc;
+  if ((rc = stage_in(c, den, sizeof(double) * c->ntot, 2, true, &dden, &h2))) return rc;
+  if ((rc = stage_in(c, su, n1, 3, false, &dsu, &hsu))) return rc;
+  if ((rc = stage_in(c, flmass, sizeof(double) * (c->nin > 0 ? c->nin : 1), 4, true, &dfm, &hfm)))
+    return rc;
+  FCG_CUDA_TRY(c, c->scratch.ensure(sizeof(double) * (c->nin > 0 ? c->nin : 1)));
+  const MeshView &m = c->mv;
+  if (m.nin > 0) {
+    k_fmc_faces<<<grid_for(m.nin, c->num_sms), kTPB, 0, c->stream>>>(
+        m, (const double *)dP, (const double *)dapu, (const double *)dden, (double *)dfm,
+        c->scratch.as<double>());
+    FCG_CHECK_LAUNCH(c, "k_fmc_faces");
+  }
+  k_fmc_cells<<<grid_for(m.n, c->num_sms), kTPB, 0, c->stream>>>(m, c->scratch.as<double>(),
+                                                                    (double *)dsu);
+  FCG_CHECK_LAUNCH(c, "k_fmc_cells");
+  if ((rc = stage_out(c, su, dsu, n1, hsu))) return rc;
+  if ((rc = stage_out(c, flmass, dfm, sizeof(double) * c->nin, hfm))) return rc;
+  if (hsu || hfm) FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return FCG_OK;
+}

@@ -1,0 +1,159 @@
+// Internal state of an fcg_context and the views the kernels receive.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/fcgpu.h"
+
+namespace fcg {
+
+// Boundary types in the reference's loop order (grad_gauss.f90:70-103, bpres.f90:41-96).
+enum BType { B_INLET = 0, B_OUTLET = 1, B_SYMMETRY = 2, B_WALL = 3, B_PRESSOUT = 4, B_NTYPES = 5 };
+
+// A growable device allocation owned by the context.
+struct DBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t need) {
+    if (need <= bytes && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, need ? need : 16);
+    if (e == cudaSuccess) bytes = need ? need : 16;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <class T>
+  T *as() const { return (T *)p; }
+};
+
+// Device-side mesh and pattern, passed by value to kernels.  All indices 0-based.
+struct MeshView {
+  int n, nf, nin, ntot;
+  long long nnz;
+  const int *owner, *neighbour;
+  const double *arx, *ary, *arz, *xf, *yf, *zf;
+  const double *xc, *yc, *zc, *vol, *facint;
+  const int *ioffset, *ja, *diag, *slot_pn, *slot_np;
+  // inner-face incidence per cell, ascending face order: ent = f+1 (owner) or -(f+1)
+  // (neighbour); slot = CSR position of this cell's row entry for that face.
+  const int *cf_ptr, *cf_ent, *cf_slot;
+  // boundary faces per cell in the reference's boundary loop order (type, then index)
+  const int *cb_ptr, *cb_face, *cb_slot, *cb_type;
+  // boundary faces per cell in face order (grad_lsq.f90:116-130)
+  const int *cbf_ptr, *cbf_face;
+};
+
+// Sliced-ELL copy of the CSR pattern used by the solvers: slices of 32 rows, each
+// slice as wide as its longest row, stored column-major inside the slice so that a
+// warp reads one entry of 32 consecutive rows per load.
+struct SellView {
+  int nslices;
+  const long long *ptr; // [nslices+1] element offset of each slice
+  const int *width;     // [nslices]
+  const int *col;       // [len] 0-based column (pads: the row itself)
+  const int *src;       // [len] CSR position of the entry (pads: -1)
+};
+
+struct Level {
+  std::vector<int> ptr;  // host: level offsets into rows
+  int *rows = nullptr;   // device: rows sorted by level, ascending inside a level
+  int count = 0;
+};
+
+}  // namespace fcg
+
+namespace fcg {
+struct KrylovState;
+void destroy_krylov(KrylovState *k);
+}  // namespace fcg
+
+struct fcg_context {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  std::string err;
+  bool bound = false;
+  unsigned bind_gen = 0;  // bumped by every fcg_bind_mesh; captured graphs depend on it
+
+  // sizes
+  int n = 0, nf = 0, nin = 0, nb = 0, ntot = 0;
+  long long nnz = 0;
+  int cnt[fcg::B_NTYPES] = {0}, fst[fcg::B_NTYPES] = {0}, bst[fcg::B_NTYPES] = {0};
+
+  // host copies of the 1-based CSR (fcg_create_csr hands them back)
+  std::vector<int> h_ioffset, h_ja, h_diag, h_slot_pn, h_slot_np;
+
+  // device allocations made by fcg_bind_mesh (mesh arrays and topology)
+  std::vector<fcg::DBuf> bound_allocs;
+  fcg::MeshView mv{};
+  fcg::SellView sv{};
+  int sell_maxw = 0;
+  long long sell_len = 0;
+  fcg::Level lf, lb;  // forward (lower) and backward (upper) level schedules
+  const int *tpos = nullptr;  // CSR position of the transpose entry of every entry
+
+  // lazily built lsq matrices dmat(9,n)
+  fcg::DBuf dmat;
+  bool dmat_ready = false;
+
+  // per-call staging of host arrays and kernel scratch
+  std::vector<fcg::DBuf> stage;
+  fcg::DBuf scratch;
+  fcg::KrylovState *ks = nullptr;  // solver workspaces and captured graphs (krylov.cu)
+
+  ~fcg_context();
+};
+
+namespace fcg {
+
+int set_error(fcg_context *c, int status, const std::string &msg);
+int cuda_fail(fcg_context *c, cudaError_t e, const char *where);
+
+// Host-side construction of the topology (topology.cpp).  Returns a status code.
+struct HostTopology {
+  std::vector<int> ioffset, ja, diag, slot_pn, slot_np;  // 1-based (reference form)
+  std::vector<int> cf_ptr, cf_ent, cf_slot;              // 0-based
+  std::vector<int> cb_ptr, cb_face, cb_slot, cb_type;
+  std::vector<int> cbf_ptr, cbf_face;
+  std::vector<long long> sell_ptr;
+  std::vector<int> sell_width, sell_col, sell_src;
+  int sell_maxw = 0;
+  std::vector<int> lf_ptr, lf_rows, lb_ptr, lb_rows;
+  std::vector<int> tpos;
+};
+
+int build_topology(const fcg_mesh_desc &m, const int cnt[B_NTYPES], const int fst[B_NTYPES],
+                   const int bst[B_NTYPES], HostTopology &t, std::string &err);
+
+// Pointer staging: returns a device pointer for a user array of `bytes` bytes.  A
+// device pointer is returned as is; a host array is copied into staging slot `slot`
+// when `copy_in` is set.  `was_host` tells the caller to copy results back.
+int stage_in(fcg_context *c, const void *user, size_t bytes, int slot, bool copy_in, void **dev,
+             bool *was_host);
+int stage_out(fcg_context *c, void *user, const void *dev, size_t bytes, bool was_host);
+bool is_device_pointer(const void *p);
+
+}  // namespace fcg
+
+#define FCG_CUDA_TRY(ctx, expr)                                   \
+  do {                                                            \
+    cudaError_t _e = (expr);                                      \
+    if (_e != cudaSuccess) return fcg::cuda_fail((ctx), _e, #expr); \
+  } while (0)
+
+#define FCG_CHECK_LAUNCH(ctx, name)                                   \
+  do {                                                                \
+    cudaError_t _e = cudaGetLastError();                              \
+    if (_e != cudaSuccess) return fcg::cuda_fail((ctx), _e, name);    \
+  } while (0)

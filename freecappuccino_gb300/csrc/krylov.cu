@@ -1,0 +1,858 @@
+// Krylov solvers of the pressure-correction path: dpcg (src/dpcg.f90), iccg with the
+// diagonal incomplete-Cholesky factor (src/iccg.f90) and bicgstab with the diagonal
+// ILU factor (src/bicgstab.f90), plus the standalone SpMV.
+//
+// Design (one GPU, everything device-resident):
+//  * The caller's CSR values are gathered once per solve into a sliced-ELL copy
+//    (32-row slices, column-major inside a slice): a warp reads one entry of 32
+//    consecutive rows per load, so the matrix streams from HBM fully coalesced.
+//    Entries keep the CSR column order, so each row is summed in the reference's order.
+//  * Every global sum (L1 norms, dot products) is a deterministic two-level reduction:
+//    per-block partials, then the last block to finish (ticket counter) adds the
+//    partials in index order and computes the solver scalars (alpha, beta, omega,
+//    the stop test) on the device.  No host round trip per sweep.
+//  * One sweep is a fixed chain of kernels captured once into the body of a CUDA-graph
+//    WHILE node; the kernel that evaluates the stop test clears the node's condition.
+//    A whole solve is one graph launch.
+//  * The DIC/DILU triangular solves run level by level (rows of one level depend only
+//    on rows of earlier levels), one kernel per level inside the same graph; each row
+//    is computed with the reference's operand order, so the preconditioner is the
+//    reference's M = (D+L) D^-1 (D+U) exactly.
+// Deviation kept on purpose: DPCG's z = r / a(diag) is computed as r * (1/a(diag))
+// (FP64 division is slow on this part); the difference is at most one ulp per entry.
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "fcg_internal.h"
+#include "launch.h"
+
+namespace fcg {
+
+enum SolverKind { SK_DPCG = 0, SK_ICCG = 1, SK_BICG = 2, SK_N = 3 };
+
+// Device-resident solver scalars.  Written by the last block of a reduction kernel,
+// read by the following kernels (stream order makes the writes visible).
+struct Scal {
+  double res0, resl, resor, rsm;
+  double s0, sk, bet, pkapk, alf;  // CG; alf is also BiCGStab's alpha
+  double gam, om, beto, bbet;      // BiCGStab
+  double l2r, l2b;                 // final recomputed ||su - A x||^2 and ||su||^2
+  double small, resmax, tol;
+  int iter, nsw, done, converged, status, early, trace_cap, pad;
+  unsigned int ticket[8];
+  unsigned int body_count;  // executions of the loop body, counted independently of iter
+};
+
+struct KrylovState {
+  int n = 0, G = 0, nsw_cap = 0;
+  unsigned bind_gen = 0;
+  long long nnz = 0, sell_len = 0;
+  DBuf vec;  // all vectors
+  double *x = nullptr, *res = nullptr, *su = nullptr, *pk = nullptr, *zk = nullptr,
+         *qk = nullptr, *invd = nullptr, *d = nullptr, *reso = nullptr, *uk = nullptr,
+         *vk = nullptr, *a = nullptr, *sval = nullptr, *partials = nullptr, *rtmp = nullptr;
+  DBuf trace;
+  Scal *S = nullptr;  // device
+  Scal *hS = nullptr; // pinned host copy
+  cudaStream_t cap = nullptr;
+  cudaGraphExec_t exec[SK_N] = {nullptr, nullptr, nullptr};
+  cudaGraph_t graph[SK_N] = {nullptr, nullptr, nullptr};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool matrix_loaded = false;
+  double small = (double)1e-20f;  // parameters::small (modules_allocatable.f90:27)
+  int early_exit = 1;
+};
+
+void destroy_krylov(KrylovState *k) {
+  if (!k) return;
+  for (int i = 0; i < SK_N; ++i) {
+    if (k->exec[i]) cudaGraphExecDestroy(k->exec[i]);
+    if (k->graph[i]) cudaGraphDestroy(k->graph[i]);
+  }
+  if (k->cap) cudaStreamDestroy(k->cap);
+  if (k->ev0) cudaEventDestroy(k->ev0);
+  if (k->ev1) cudaEventDestroy(k->ev1);
+  if (k->hS) cudaFreeHost(k->hS);
+  if (k->S) cudaFree(k->S);
+  k->vec.release();
+  k->trace.release();
+  delete k;
+}
+
+namespace {
+
+constexpr int kWarps = kTPB / 32;
+
+// ---------------------------------------------------------------------------
+// Deterministic reductions
+// ---------------------------------------------------------------------------
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double (*sh)[kWarps]) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) sh[k][w] = v[k];
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = lane < kWarps ? sh[k][lane] : 0.0;
+#pragma unroll
+    for (int o = kWarps / 2; o > 0; o >>= 1)
+#pragma unroll
+      for (int k = 0; k < NV; ++k) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+  }
+  __syncthreads();
+}
+
+// Stores this block's sums; returns true in the last block to arrive, whose thread 0
+// then holds the grid-wide sums in v (partials added in block-index order).
+template <int NV>
+__device__ bool reduce_commit(double (&v)[NV], double *partials, unsigned int *ticket) {
+  __shared__ double sh[NV][kWarps];
+  __shared__ bool am_last;
+  block_sum<NV>(v, sh);
+  const int G = gridDim.x;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) partials[k * G + blockIdx.x] = v[k];
+    __threadfence();
+    unsigned int t = atomicAdd(ticket, 1u);
+    am_last = (t == (unsigned int)G - 1);
+  }
+  __syncthreads();
+  if (!am_last) return false;
+  __threadfence();
+  double s[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) s[k] = 0.0;
+  for (int i = threadIdx.x; i < G; i += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) s[k] += __ldcg(&partials[k * G + i]);
+  block_sum<NV>(s, sh);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = s[k];
+    *ticket = 0u;
+  }
+  return true;
+}
+
+__device__ __forceinline__ bool solve_done(const Scal *S) { return __ldcg(&S->done) != 0; }
+
+__device__ __forceinline__ void stop_loop(cudaGraphConditionalHandle h, int use_cond) {
+  if (use_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(h, 0);
+}
+
+// Bound on the WHILE loop that does not depend on the reductions: the closing kernel of
+// the body counts its executions and ends the loop after nsw + 2 of them whatever the
+// solver scalars say (status FCG_ERR_TIMEOUT).
+__device__ __forceinline__ void loop_guard(Scal *S, cudaGraphConditionalHandle h, int use_cond) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    unsigned int c = atomicAdd(&S->body_count, 1u) + 1u;
+    if (c > (unsigned int)S->nsw + 2u) {
+      S->status = FCG_ERR_TIMEOUT;
+      S->done = 1;
+      if (use_cond) cudaGraphSetConditional(h, 0);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Matrix preparation
+// ---------------------------------------------------------------------------
+// CSR values -> sliced ELL (one thread per row, writes coalesced along the slice);
+// also 1/a(diag) for the Jacobi preconditioner.
+__global__ void k_sell_fill(SellView s, int n, const int *__restrict__ diag,
+                            const double *__restrict__ a, double *__restrict__ sval,
+                            double *__restrict__ invd) {
+  FCG_GRID_STRIDE(r, (long long)s.nslices * 32) {
+    int slice = (int)(r >> 5), lane = (int)(r & 31);
+    long long base = s.ptr[slice];
+    int w = s.width[slice];
+    int dpos = r < n ? diag[r] : -2;
+    for (int j = 0; j < w; ++j) {
+      long long p = base + (long long)j * 32 + lane;
+      int src = s.src[p];
+      double v = src >= 0 ? a[src] : 0.0;
+      sval[p] = v;
+      if (src == dpos && invd) invd[r] = 1.0 / v;
+    }
+  }
+}
+
+// y = A x for the rows of one warp's slice; returns the row's sum.
+__device__ __forceinline__ double sell_row(const SellView &s, const double *__restrict__ val,
+                                           const double *__restrict__ x, int slice, int lane) {
+  long long base = s.ptr[slice] + lane;
+  int w = s.width[slice];
+  double acc = 0.0;
+#pragma unroll 4
+  for (int j = 0; j < w; ++j) {
+    long long p = base + (long long)j * 32;
+    acc += __ldg(&val[p]) * __ldg(&x[__ldg(&s.col[p])]);
+  }
+  return acc;
+}
+
+#define FCG_SLICE_LOOP(slice, lane, s)                                                      \
+  const int lane = threadIdx.x & 31;                                                       \
+  for (int slice = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);        \
+       slice < (s).nslices; slice += (int)(((long long)gridDim.x * blockDim.x) >> 5))
+
+__global__ void k_spmv(SellView s, int n, const double *__restrict__ val,
+                       const double *__restrict__ x, double *__restrict__ y) {
+  FCG_SLICE_LOOP(slice, lane, s) {
+    int r = slice * 32 + lane;
+    double acc = sell_row(s, val, x, slice, lane);
+    if (r < n) y[r] = acc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Solver kernels
+// ---------------------------------------------------------------------------
+// res = su - A x, res0 = sum|res| (dpcg.f90:51-64); DPCG also sk = sum res^2/a(diag).
+__global__ void k_init(SellView s, int n, const double *__restrict__ val,
+                       const double *__restrict__ su, const double *__restrict__ x,
+                       double *__restrict__ res, const double *__restrict__ invd, Scal *S,
+                       double *partials, int kind) {
+  double v[2] = {0.0, 0.0};
+  FCG_SLICE_LOOP(slice, lane, s) {
+    int r = slice * 32 + lane;
+    double ax = sell_row(s, val, x, slice, lane);
+    if (r < n) {
+      double rr = su[r] - ax;
+      res[r] = rr;
+      v[0] += fabs(rr);
+      if (kind == SK_DPCG) v[1] += rr * (rr * invd[r]);
+    }
+  }
+  if (reduce_commit<2>(v, partials, &S->ticket[0]) && threadIdx.x == 0) {
+    S->res0 = v[0];
+    S->resl = v[0];
+    S->iter = 0;
+    S->converged = 0;
+    S->status = 0;
+    S->s0 = (double)1.e20f;  // dpcg.f90:76
+    S->sk = v[1];
+    S->bet = v[1] / S->s0;
+    S->alf = 1.0;  // bicgstab.f90:90-92
+    S->beto = 1.0;
+    S->gam = 1.0;
+    S->done = (S->nsw <= 0 || (S->early && v[0] < S->tol)) ? 1 : 0;  // dpcg.f90:66-70
+    if (!isfinite(v[0])) {
+      S->status = FCG_ERR_NONFINITE;
+      S->done = 1;
+    }
+  }
+}
+
+// Stop test shared by all solvers (dpcg.f90:130-142); thread 0 of the last block.
+__device__ void finish_sweep(Scal *S, double resl, double *trace, cudaGraphConditionalHandle h,
+                             int use_cond) {
+  int it = S->iter + 1;
+  S->iter = it;
+  S->resl = resl;
+  if (it == 1) S->resor = S->res0;
+  double rsm = resl / (S->resor + S->small);
+  S->rsm = rsm;
+  if (trace && it <= S->trace_cap) {
+    trace[2 * (it - 1)] = resl;
+    trace[2 * (it - 1) + 1] = rsm;
+  }
+  if (rsm < S->resmax) S->converged = 1;
+  if (!isfinite(resl)) S->status = FCG_ERR_NONFINITE;
+  if (S->converged || it >= S->nsw || S->status) {
+    S->done = 1;
+    if (use_cond) cudaGraphSetConditional(h, 0);
+  }
+}
+
+// pk = M^-1 res + bet*pk: Jacobi (dpcg.f90:85-100) or z from the sweeps (iccg.f90:278).
+__global__ void k_cg_p(int n, const double *__restrict__ res, const double *__restrict__ invd,
+                       const double *__restrict__ z, double *__restrict__ pk, const Scal *S,
+                       int kind) {
+  if (solve_done(S)) return;
+  const double bet = __ldcg(&S->bet);
+  FCG_GRID_STRIDE(i, n) {
+    double zi = kind == SK_DPCG ? res[i] * invd[i] : z[i];
+    pk[i] = zi + bet * pk[i];
+  }
+}
+
+// qk = A pk, pkapk = sum pk*qk, alf = sk/pkapk (dpcg.f90:105-121).
+__global__ void k_cg_spmv(SellView s, int n, const double *__restrict__ val,
+                          const double *__restrict__ pk, double *__restrict__ qk, Scal *S,
+                          double *partials) {
+  if (solve_done(S)) return;
+  double v[1] = {0.0};
+  FCG_SLICE_LOOP(slice, lane, s) {
+    int r = slice * 32 + lane;
+    double q = sell_row(s, val, pk, slice, lane);
+    if (r < n) {
+      qk[r] = q;
+      v[0] += pk[r] * q;
+    }
+  }
+  if (reduce_commit<1>(v, partials, &S->ticket[1]) && threadIdx.x == 0) {
+    S->pkapk = v[0];
+    S->alf = S->sk / v[0];
+    if (!isfinite(S->alf)) S->status = FCG_ERR_NONFINITE;
+  }
+}
+
+// fi += alf*pk, res -= alf*qk, resl = sum|res| (dpcg.f90:124-142); DPCG also forms
+// the next sk and beta in the same pass.
+__global__ void k_cg_update(int n, double *__restrict__ x, double *__restrict__ res,
+                            const double *__restrict__ pk, const double *__restrict__ qk,
+                            const double *__restrict__ invd, Scal *S, double *partials,
+                            double *trace, cudaGraphConditionalHandle h, int use_cond, int kind) {
+  if (solve_done(S)) {
+    stop_loop(h, use_cond);
+    return;
+  }
+  loop_guard(S, h, use_cond);
+  const double alf = __ldcg(&S->alf);
+  double v[2] = {0.0, 0.0};
+  FCG_GRID_STRIDE(i, n) {
+    x[i] = x[i] + alf * pk[i];
+    double r = res[i] - alf * qk[i];
+    res[i] = r;
+    v[0] += fabs(r);
+    if (kind == SK_DPCG) v[1] += r * (r * invd[i]);
+  }
+  if (reduce_commit<2>(v, partials, &S->ticket[2]) && threadIdx.x == 0) {
+    S->s0 = S->sk;  // dpcg.f90:132
+    if (kind == SK_DPCG) {
+      S->sk = v[1];
+      S->bet = v[1] / S->s0;  // next sweep's beta (dpcg.f90:95)
+    }
+    if (S->status) {
+      S->done = 1;
+      if (use_cond) cudaGraphSetConditional(h, 0);
+      return;
+    }
+    finish_sweep(S, v[0], trace, h, use_cond);
+  }
+}
+
+// ICCG: sk = sum res*z, bet = sk/s0 (iccg.f90:268-273).
+__global__ void k_cg_dot(int n, const double *__restrict__ res, const double *__restrict__ z,
+                         Scal *S, double *partials) {
+  if (solve_done(S)) return;
+  double v[1] = {0.0};
+  FCG_GRID_STRIDE(i, n) v[0] += res[i] * z[i];
+  if (reduce_commit<1>(v, partials, &S->ticket[3]) && threadIdx.x == 0) {
+    S->sk = v[0];
+    S->bet = v[0] / S->s0;
+  }
+}
+
+// --- triangular sweeps, one launch per level -----------------------------------
+// forward: z_i = (b_i - sum_{k<diag} a_k z_{ja_k}) * d_i        (iccg.f90:248-254)
+__global__ void k_fwd_level(const int *__restrict__ rows, int count,
+                            const int *__restrict__ ioffset, const int *__restrict__ ja,
+                            const int *__restrict__ diag, const double *__restrict__ a,
+                            const double *__restrict__ d, const double *__restrict__ b,
+                            double *__restrict__ z, const Scal *S) {
+  if (solve_done(S)) return;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  int i = rows[t];
+  double zi = b[i];
+  for (int k = ioffset[i]; k < diag[i]; ++k) zi = zi - a[k] * z[ja[k]];
+  z[i] = zi * d[i];
+}
+
+// backward with the reference's rescale zk/(d+small) folded in (iccg.f90:256-265).
+__global__ void k_bwd_level(const int *__restrict__ rows, int count,
+                            const int *__restrict__ ioffset, const int *__restrict__ ja,
+                            const int *__restrict__ diag, const double *__restrict__ a,
+                            const double *__restrict__ d, double *__restrict__ z,
+                            const Scal *S) {
+  if (solve_done(S)) return;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  int i = rows[t];
+  double di = d[i];
+  double zi = z[i] / (di + S->small);
+  for (int k = diag[i] + 1; k < ioffset[i + 1]; ++k) zi = zi - a[k] * z[ja[k]];
+  z[i] = zi * di;
+}
+
+// Factor diagonals, level by level: DIC d_i = 1/(a_ii - sum a_ik^2 d_k) (iccg.f90:
+// 231-237); DILU d_i = 1/(a_ii - sum a_ik d_k a_ki) (bicgstab.f90:68-79).
+__global__ void k_factor_level(const int *__restrict__ rows, int count,
+                               const int *__restrict__ ioffset, const int *__restrict__ ja,
+                               const int *__restrict__ diag, const int *__restrict__ tpos,
+                               const double *__restrict__ a, double *__restrict__ d, Scal *S,
+                               int dilu) {
+  if (solve_done(S)) return;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  int i = rows[t];
+  double di = a[diag[i]];
+  for (int k = ioffset[i]; k < diag[i]; ++k) {
+    int j = ja[k];
+    if (dilu)
+      di = di - a[k] * d[j] * a[tpos[k]];
+    else
+      di = di - a[k] * a[k] * d[j];
+  }
+  double inv = 1.0 / di;
+  d[i] = inv;
+  if (!isfinite(inv) || di == 0.0) S->status = FCG_ERR_PIVOT;
+}
+
+// --- BiCGStab sweep (bicgstab.f90:99-224) -------------------------------------
+// bet = sum res*reso; om = bet*gam/(alf*beto+small); beto = bet
+__global__ void k_bi_dot1(int n, const double *__restrict__ res, const double *__restrict__ reso,
+                          Scal *S, double *partials) {
+  if (solve_done(S)) return;
+  double v[1] = {0.0};
+  FCG_GRID_STRIDE(i, n) v[0] += res[i] * reso[i];
+  if (reduce_commit<1>(v, partials, &S->ticket[3]) && threadIdx.x == 0) {
+    double bet = v[0];
+    S->bbet = bet;
+    S->om = bet * S->gam / (S->alf * S->beto + S->small);
+    S->beto = bet;
+  }
+}
+
+// pk = res + om*(pk - alf*uk)
+__global__ void k_bi_p(int n, const double *__restrict__ res, const double *__restrict__ uk,
+                       double *__restrict__ pk, const Scal *S) {
+  if (solve_done(S)) return;
+  const double om = __ldcg(&S->om), alf = __ldcg(&S->alf);
+  FCG_GRID_STRIDE(i, n) pk[i] = res[i] + om * (pk[i] - alf * uk[i]);
+}
+
+// uk = A zk; gam = bet / sum uk*reso
+__global__ void k_bi_spmv1(SellView s, int n, const double *__restrict__ val,
+                           const double *__restrict__ zk, const double *__restrict__ reso,
+                           double *__restrict__ uk, Scal *S, double *partials) {
+  if (solve_done(S)) return;
+  double v[1] = {0.0};
+  FCG_SLICE_LOOP(slice, lane, s) {
+    int r = slice * 32 + lane;
+    double u = sell_row(s, val, zk, slice, lane);
+    if (r < n) {
+      uk[r] = u;
+      v[0] += u * reso[r];
+    }
+  }
+  if (reduce_commit<1>(v, partials, &S->ticket[4]) && threadIdx.x == 0) {
+    S->gam = S->bbet / v[0];
+    if (!isfinite(S->gam)) S->status = FCG_ERR_NONFINITE;
+  }
+}
+
+// fi += gam*zk; res -= gam*uk
+__global__ void k_bi_upd1(int n, double *__restrict__ x, double *__restrict__ res,
+                          const double *__restrict__ zk, const double *__restrict__ uk,
+                          const Scal *S) {
+  if (solve_done(S)) return;
+  const double gam = __ldcg(&S->gam);
+  FCG_GRID_STRIDE(i, n) {
+    x[i] = x[i] + gam * zk[i];
+    res[i] = res[i] - gam * uk[i];
+  }
+}
+
+// vk = A zk; alf = sum vk*res / (sum vk*vk + small)
+__global__ void k_bi_spmv2(SellView s, int n, const double *__restrict__ val,
+                           const double *__restrict__ zk, const double *__restrict__ res,
+                           double *__restrict__ vk, Scal *S, double *partials) {
+  if (solve_done(S)) return;
+  double v[2] = {0.0, 0.0};
+  FCG_SLICE_LOOP(slice, lane, s) {
+    int r = slice * 32 + lane;
+    double q = sell_row(s, val, zk, slice, lane);
+    if (r < n) {
+      vk[r] = q;
+      v[0] += q * res[r];
+      v[1] += q * q;
+    }
+  }
+  if (reduce_commit<2>(v, partials, &S->ticket[5]) && threadIdx.x == 0) {
+    S->alf = v[0] / (v[1] + S->small);
+    if (!isfinite(S->alf)) S->status = FCG_ERR_NONFINITE;
+  }
+}
+
+// fi += alf*zk; res -= alf*vk; resl = sum|res|; stop test
+__global__ void k_bi_upd2(int n, double *__restrict__ x, double *__restrict__ res,
+                          const double *__restrict__ zk, const double *__restrict__ vk, Scal *S,
+                          double *partials, double *trace, cudaGraphConditionalHandle h,
+                          int use_cond) {
+  if (solve_done(S)) {
+    stop_loop(h, use_cond);
+    return;
+  }
+  loop_guard(S, h, use_cond);
+  const double alf = __ldcg(&S->alf);
+  double v[1] = {0.0};
+  FCG_GRID_STRIDE(i, n) {
+    x[i] = x[i] + alf * zk[i];
+    double r = res[i] - alf * vk[i];
+    res[i] = r;
+    v[0] += fabs(r);
+  }
+  if (reduce_commit<1>(v, partials, &S->ticket[6]) && threadIdx.x == 0) {
+    if (S->status) {
+      S->done = 1;
+      if (use_cond) cudaGraphSetConditional(h, 0);
+      return;
+    }
+    finish_sweep(S, v[0], trace, h, use_cond);
+  }
+}
+
+// Final FP64 check: ||su - A x||^2 and ||su||^2.
+__global__ void k_final(SellView s, int n, const double *__restrict__ val,
+                        const double *__restrict__ su, const double *__restrict__ x, Scal *S,
+                        double *partials) {
+  double v[2] = {0.0, 0.0};
+  FCG_SLICE_LOOP(slice, lane, s) {
+    int r = slice * 32 + lane;
+    double ax = sell_row(s, val, x, slice, lane);
+    if (r < n) {
+      double rr = su[r] - ax;
+      v[0] += rr * rr;
+      v[1] += su[r] * su[r];
+    }
+  }
+  if (reduce_commit<2>(v, partials, &S->ticket[7]) && threadIdx.x == 0) {
+    S->l2r = v[0];
+    S->l2b = v[1];
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+static int ensure_state(fcg_context *c, int nsw) {
+  KrylovState *k = c->ks;
+  if (!k) {
+    k = c->ks = new KrylovState();
+    FCG_CUDA_TRY(c, cudaMalloc(&k->S, sizeof(Scal)));
+    FCG_CUDA_TRY(c, cudaMallocHost(&k->hS, sizeof(Scal)));
+    FCG_CUDA_TRY(c, cudaMemset(k->S, 0, sizeof(Scal)));
+    FCG_CUDA_TRY(c, cudaStreamCreateWithFlags(&k->cap, cudaStreamNonBlocking));
+    FCG_CUDA_TRY(c, cudaEventCreate(&k->ev0));
+    FCG_CUDA_TRY(c, cudaEventCreate(&k->ev1));
+  }
+  const int G = c->num_sms * 8;
+  if (k->n != c->n || k->nnz != c->nnz || k->sell_len != c->sell_len || k->G != G ||
+      k->bind_gen != c->bind_gen) {
+    for (int i = 0; i < SK_N; ++i) {
+      if (k->exec[i]) cudaGraphExecDestroy(k->exec[i]);
+      if (k->graph[i]) cudaGraphDestroy(k->graph[i]);
+      k->exec[i] = nullptr;
+      k->graph[i] = nullptr;
+    }
+    const size_t n = c->n;
+    size_t total = 13 * n + (size_t)c->nnz + (size_t)c->sell_len + 8 * (size_t)G + 64;
+    FCG_CUDA_TRY(c, k->vec.ensure(total * sizeof(double)));
+    FCG_CUDA_TRY(c, cudaMemset(k->vec.p, 0, total * sizeof(double)));
+    double *p = k->vec.as<double>();
+    double **vecs[] = {&k->x, &k->res, &k->su, &k->pk, &k->zk, &k->qk, &k->invd,
+                       &k->d, &k->reso, &k->uk, &k->vk, &k->rtmp};
+    for (double **v : vecs) {
+      *v = p;
+      p += n;
+    }
+    p += n;  // guard
+    k->a = p;
+    p += c->nnz;
+    k->sval = p;
+    p += c->sell_len;
+    k->partials = p;
+    k->n = c->n;
+    k->nnz = c->nnz;
+    k->sell_len = c->sell_len;
+    k->G = G;
+    k->bind_gen = c->bind_gen;
+    k->matrix_loaded = false;
+  }
+  if (nsw > k->nsw_cap) {
+    FCG_CUDA_TRY(c, k->trace.ensure(sizeof(double) * 2 * (size_t)nsw));
+    k->nsw_cap = nsw;
+    for (int i = 0; i < SK_N; ++i) {  // the trace pointer is baked into the graphs
+      if (k->exec[i]) cudaGraphExecDestroy(k->exec[i]);
+      if (k->graph[i]) cudaGraphDestroy(k->graph[i]);
+      k->exec[i] = nullptr;
+      k->graph[i] = nullptr;
+    }
+  }
+  return FCG_OK;
+}
+
+// Loads CSR values a (device pointer) into the solver copies.
+static int load_matrix(fcg_context *c, const double *da) {
+  KrylovState *k = c->ks;
+  FCG_CUDA_TRY(c, cudaMemcpyAsync(k->a, da, sizeof(double) * c->nnz, cudaMemcpyDeviceToDevice,
+                                  c->stream));
+  k_sell_fill<<<grid_for((long long)c->sv.nslices * 32, c->num_sms), kTPB, 0, c->stream>>>(
+      c->sv, c->n, c->mv.diag, k->a, k->sval, k->invd);
+  FCG_CHECK_LAUNCH(c, "k_sell_fill");
+  k->matrix_loaded = true;
+  return FCG_OK;
+}
+
+static void launch_sweeps(fcg_context *c, cudaStream_t st, const Level &lv, bool forward,
+                          const double *b, double *z) {
+  KrylovState *k = c->ks;
+  for (int l = 0; l < lv.count; ++l) {
+    int start = lv.ptr[l], cnt = lv.ptr[l + 1] - lv.ptr[l];
+    int g = (cnt + kTPB - 1) / kTPB;
+    if (forward)
+      k_fwd_level<<<g, kTPB, 0, st>>>(lv.rows + start, cnt, c->mv.ioffset, c->mv.ja, c->mv.diag,
+                                      k->a, k->d, b, z, k->S);
+    else
+      k_bwd_level<<<g, kTPB, 0, st>>>(lv.rows + start, cnt, c->mv.ioffset, c->mv.ja, c->mv.diag,
+                                      k->a, k->d, z, k->S);
+  }
+}
+
+// Enqueues one sweep of solver `kind` on stream st.
+static void enqueue_sweep(fcg_context *c, cudaStream_t st, int kind, cudaGraphConditionalHandle h,
+                          int use_cond) {
+  KrylovState *k = c->ks;
+  const int n = c->n, G = k->G;
+  const SellView &s = c->sv;
+  double *tr = k->trace.as<double>();
+  if (kind == SK_DPCG || kind == SK_ICCG) {
+    if (kind == SK_ICCG) {
+      launch_sweeps(c, st, c->lf, true, k->res, k->zk);
+      launch_sweeps(c, st, c->lb, false, nullptr, k->zk);
+      k_cg_dot<<<G, kTPB, 0, st>>>(n, k->res, k->zk, k->S, k->partials);
+    }
+    k_cg_p<<<G, kTPB, 0, st>>>(n, k->res, k->invd, k->zk, k->pk, k->S, kind);
+    k_cg_spmv<<<G, kTPB, 0, st>>>(s, n, k->sval, k->pk, k->qk, k->S, k->partials);
+    k_cg_update<<<G, kTPB, 0, st>>>(n, k->x, k->res, k->pk, k->qk, k->invd, k->S, k->partials,
+                                     tr, h, use_cond, kind);
+  } else {
+    k_bi_dot1<<<G, kTPB, 0, st>>>(n, k->res, k->reso, k->S, k->partials);
+    k_bi_p<<<G, kTPB, 0, st>>>(n, k->res, k->uk, k->pk, k->S);
+    launch_sweeps(c, st, c->lf, true, k->pk, k->zk);
+    launch_sweeps(c, st, c->lb, false, nullptr, k->zk);
+    k_bi_spmv1<<<G, kTPB, 0, st>>>(s, n, k->sval, k->zk, k->reso, k->uk, k->S, k->partials);
+    k_bi_upd1<<<G, kTPB, 0, st>>>(n, k->x, k->res, k->zk, k->uk, k->S);
+    launch_sweeps(c, st, c->lf, true, k->res, k->zk);
+    launch_sweeps(c, st, c->lb, false, nullptr, k->zk);
+    k_bi_spmv2<<<G, kTPB, 0, st>>>(s, n, k->sval, k->zk, k->res, k->vk, k->S, k->partials);
+    k_bi_upd2<<<G, kTPB, 0, st>>>(n, k->x, k->res, k->zk, k->vk, k->S, k->partials, tr, h,
+                                   use_cond);
+  }
+}
+
+static bool graphs_disabled() {
+  const char *e = std::getenv("FCG_NO_GRAPH");
+  return e && e[0] == '1';
+}
+
+// Captures the WHILE-node graph of one solver kind.
+static int build_graph(fcg_context *c, int kind) {
+  KrylovState *k = c->ks;
+  if (k->exec[kind]) return FCG_OK;
+  cudaGraph_t g;
+  FCG_CUDA_TRY(c, cudaGraphCreate(&g, 0));
+  cudaGraphConditionalHandle h;
+  FCG_CUDA_TRY(c, cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};  // aggregate: rest zeroed
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  FCG_CUDA_TRY(c, cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np));
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  FCG_CUDA_TRY(c, cudaStreamBeginCaptureToGraph(k->cap, body, nullptr, nullptr, 0,
+                                                cudaStreamCaptureModeThreadLocal));
+  enqueue_sweep(c, k->cap, kind, h, 1);
+  cudaGraph_t captured = nullptr;
+  cudaError_t e = cudaStreamEndCapture(k->cap, &captured);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return cuda_fail(c, e, "capture of the solver sweep");
+  }
+  e = cudaGraphInstantiate(&k->exec[kind], g, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return cuda_fail(c, e, "cudaGraphInstantiate (solver)");
+  }
+  k->graph[kind] = g;
+  return FCG_OK;
+}
+
+static int run_solver(fcg_context *c, int kind, const double *a, const double *su, double *fi,
+                      double *res, double sor, int nsw, double *resor, fcg_solve_report *rep) {
+  if (!c) return FCG_ERR_ARG;
+  if (!c->bound) return set_error(c, FCG_ERR_STATE, "solver called before fcg_bind_mesh");
+  if (!a || !su || !fi) return set_error(c, FCG_ERR_ARG, "NULL a, su or fi");
+  if (nsw < 0) return set_error(c, FCG_ERR_ARG, "nsw must be >= 0");
+  FCG_CUDA_TRY(c, cudaSetDevice(c->device));
+  int rc = ensure_state(c, nsw > 0 ? nsw : 1);
+  if (rc) return rc;
+  KrylovState *k = c->ks;
+  const size_t n1 = sizeof(double) * c->n;
+  void *da, *dsu, *dfi;
+  bool ha, hsu, hfi;
+  if ((rc = stage_in(c, a, sizeof(double) * c->nnz, 0, true, &da, &ha))) return rc;
+  if ((rc = stage_in(c, su, n1, 1, true, &dsu, &hsu))) return rc;
+  if ((rc = stage_in(c, fi, n1, 2, true, &dfi, &hfi))) return rc;
+  FCG_CUDA_TRY(c, cudaEventRecord(k->ev0, c->stream));
+  if ((rc = load_matrix(c, (const double *)da))) return rc;
+  FCG_CUDA_TRY(c, cudaMemcpyAsync(k->su, dsu, n1, cudaMemcpyDeviceToDevice, c->stream));
+  FCG_CUDA_TRY(c, cudaMemcpyAsync(k->x, dfi, n1, cudaMemcpyDeviceToDevice, c->stream));
+  FCG_CUDA_TRY(c, cudaMemsetAsync(k->pk, 0, n1, c->stream));
+  FCG_CUDA_TRY(c, cudaMemsetAsync(k->uk, 0, n1, c->stream));
+  // Scalars for this solve.
+  Scal init;
+  std::memset(&init, 0, sizeof init);
+  init.nsw = nsw;
+  init.small = k->small;
+  init.early = k->early_exit;
+  init.resmax = sor;
+  init.tol = (double)1e-13f;  // dpcg.f90:37
+  init.trace_cap = k->nsw_cap;
+  *k->hS = init;
+  FCG_CUDA_TRY(c, cudaMemcpyAsync(k->S, k->hS, sizeof(Scal), cudaMemcpyHostToDevice, c->stream));
+  const int G = k->G;
+  k_init<<<G, kTPB, 0, c->stream>>>(c->sv, c->n, k->sval, k->su, k->x, k->res, k->invd, k->S,
+                                    k->partials, kind);
+  FCG_CHECK_LAUNCH(c, "k_init");
+  if (kind == SK_BICG)
+    FCG_CUDA_TRY(c, cudaMemcpyAsync(k->reso, k->res, n1, cudaMemcpyDeviceToDevice, c->stream));
+  if (kind != SK_DPCG) {  // factor diagonal, level by level
+    for (int l = 0; l < c->lf.count; ++l) {
+      int start = c->lf.ptr[l], cnt = c->lf.ptr[l + 1] - c->lf.ptr[l];
+      k_factor_level<<<(cnt + kTPB - 1) / kTPB, kTPB, 0, c->stream>>>(
+          c->lf.rows + start, cnt, c->mv.ioffset, c->mv.ja, c->mv.diag, c->tpos, k->a, k->d, k->S,
+          kind == SK_BICG);
+    }
+    FCG_CHECK_LAUNCH(c, "k_factor_level");
+  }
+  if (!graphs_disabled()) {
+    if ((rc = build_graph(c, kind))) return rc;
+    FCG_CUDA_TRY(c, cudaGraphLaunch(k->exec[kind], c->stream));
+  } else {
+    // Host-driven loop: chunks of sweeps, stop flag read back between chunks.
+    for (int done = 0, it = 0; !done && it <= nsw; it += 16) {
+      for (int j = 0; j < 16; ++j) enqueue_sweep(c, c->stream, kind, 0, 0);
+      FCG_CHECK_LAUNCH(c, "solver sweep");
+      FCG_CUDA_TRY(c, cudaMemcpyAsync(k->hS, k->S, sizeof(Scal), cudaMemcpyDeviceToHost, c->stream));
+      FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+      done = k->hS->done;
+    }
+  }
+  k_final<<<G, kTPB, 0, c->stream>>>(c->sv, c->n, k->sval, k->su, k->x, k->S, k->partials);
+  FCG_CHECK_LAUNCH(c, "k_final");
+  FCG_CUDA_TRY(c, cudaEventRecord(k->ev1, c->stream));
+  FCG_CUDA_TRY(c, cudaMemcpyAsync(dfi, k->x, n1, cudaMemcpyDeviceToDevice, c->stream));
+  if ((rc = stage_out(c, fi, dfi, n1, hfi))) return rc;
+  if (res) {
+    void *dres;
+    bool hres;
+    if ((rc = stage_in(c, res, n1, 3, false, &dres, &hres))) return rc;
+    FCG_CUDA_TRY(c, cudaMemcpyAsync(dres, k->res, n1, cudaMemcpyDeviceToDevice, c->stream));
+    if ((rc = stage_out(c, res, dres, n1, hres))) return rc;
+  }
+  FCG_CUDA_TRY(c, cudaMemcpyAsync(k->hS, k->S, sizeof(Scal), cudaMemcpyDeviceToHost, c->stream));
+  FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  const Scal &S = *k->hS;
+  if (resor && S.iter > 0) *resor = S.res0;  // dpcg.f90:139
+  if (rep) {
+    rep->res0 = S.res0;
+    rep->resl = S.resl;
+    rep->iters = S.iter;
+    rep->converged = S.converged;
+    rep->l2_rel = S.l2b > 0 ? std::sqrt(S.l2r / S.l2b) : std::sqrt(S.l2r);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, k->ev0, k->ev1);
+    rep->seconds = ms * 1e-3;
+  }
+  if (S.status) {
+    const char *what = S.status == FCG_ERR_PIVOT     ? "zero or non-finite pivot in the factor"
+                       : S.status == FCG_ERR_TIMEOUT ? "solver loop exceeded nsw + 2 sweeps"
+                                                     : "non-finite value in a reduction";
+    return set_error(c, S.status, what);
+  }
+  return FCG_OK;
+}
+
+}  // namespace fcg
+
+using namespace fcg;
+
+extern "C" int fcg_dpcg(fcg_context *c, const double *a, const double *su, double *fi,
+                        double *res, double sor, int nsw, double *resor, fcg_solve_report *rep) {
+  return run_solver(c, SK_DPCG, a, su, fi, res, sor, nsw, resor, rep);
+}
+
+extern "C" int fcg_iccg(fcg_context *c, const double *a, const double *su, double *fi,
+                        double *res, double sor, int nsw, double *resor, fcg_solve_report *rep) {
+  return run_solver(c, SK_ICCG, a, su, fi, res, sor, nsw, resor, rep);
+}
+
+extern "C" int fcg_bicgstab(fcg_context *c, const double *a, const double *su, double *fi,
+                            double *res, double sor, int nsw, double *resor,
+                            fcg_solve_report *rep) {
+  return run_solver(c, SK_BICG, a, su, fi, res, sor, nsw, resor, rep);
+}
+
+extern "C" int fcg_set_solver_options(fcg_context *c, double small, int early_exit) {
+  if (!c) return FCG_ERR_ARG;
+  FCG_CUDA_TRY(c, cudaSetDevice(c->device));
+  int rc = ensure_state(c, 1);
+  if (rc) return rc;
+  c->ks->small = small;
+  c->ks->early_exit = early_exit ? 1 : 0;
+  return FCG_OK;
+}
+
+extern "C" int fcg_get_solver_trace(fcg_context *c, double *out, int max_count, int *count) {
+  if (!c || !c->ks) return FCG_ERR_STATE;
+  int it = c->ks->hS->iter;
+  int m = std::min(std::min(it, max_count), c->ks->nsw_cap);
+  if (count) *count = m;
+  if (out && m > 0)
+    FCG_CUDA_TRY(c, cudaMemcpy(out, c->ks->trace.p, sizeof(double) * 2 * m, cudaMemcpyDeviceToHost));
+  return FCG_OK;
+}
+
+extern "C" int fcg_spmv(fcg_context *c, const double *a, const double *x, double *y) {
+  if (!c) return FCG_ERR_ARG;
+  if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_spmv before fcg_bind_mesh");
+  FCG_CUDA_TRY(c, cudaSetDevice(c->device));
+  int rc = ensure_state(c, 1);
+  if (rc) return rc;
+  KrylovState *k = c->ks;
+  const size_t n1 = sizeof(double) * c->n;
+  if (a) {
+    void *da;
+    bool ha;
+    if ((rc = stage_in(c, a, sizeof(double) * c->nnz, 0, true, &da, &ha))) return rc;
+    if ((rc = load_matrix(c, (const double *)da))) return rc;
+  } else if (!k->matrix_loaded) {
+    return set_error(c, FCG_ERR_STATE, "fcg_spmv with a == NULL before any matrix was loaded");
+  }
+  void *dx, *dy;
+  bool hx, hy;
+  if ((rc = stage_in(c, x, n1, 1, true, &dx, &hx))) return rc;
+  if ((rc = stage_in(c, y, n1, 2, false, &dy, &hy))) return rc;
+  k_spmv<<<k->G, kTPB, 0, c->stream>>>(c->sv, c->n, k->sval, (const double *)dx, (double *)dy);
+  FCG_CHECK_LAUNCH(c, "k_spmv");
+  if ((rc = stage_out(c, y, dy, n1, hy))) return rc;
+  if (hy) FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return FCG_OK;
+}

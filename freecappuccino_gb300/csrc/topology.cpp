@@ -1,0 +1,252 @@
+// Bind-time topology of libfcgpu.so, built on the host once per mesh.
+//
+// * The CSR pattern of create_CSR_matrix_from_mesh_data (src/sparse_matrix.f90:42-172):
+//   the reference fills a COO list and heap-sorts it lexically; since the (row, col)
+//   pairs are unique the result is the canonical row-sorted, column-ascending CSR, so
+//   it is built here directly by counting rows and sorting each (<= 7 entry) row.
+//   diag and the two face->slot maps (:153-167) follow.  Bit-exact with the reference.
+// * Cell->face incidence lists in the reference's face-loop order, used by the
+//   cell-gather kernels so that every per-cell sum adds its terms in the order of the
+//   Fortran loops (inner faces ascending, then boundary faces by type).
+// * A sliced-ELL (32-row slices) copy of the pattern for the solvers.
+// * Level schedules of the lower and upper triangles (row i waits for the rows its
+//   lower/upper entries name) for the DIC/DILU sweeps of iccg.f90 / bicgstab.f90.
+#include <algorithm>
+#include <string>
+
+#include "fcg_internal.h"
+#include "host_util.h"
+
+namespace fcg {
+
+int build_topology(const fcg_mesh_desc &m, const int cnt[B_NTYPES], const int fst[B_NTYPES],
+                   const int bst[B_NTYPES], HostTopology &t, std::string &err) {
+  const int n = m.numCells, nf = m.numFaces, nin = m.numInnerFaces;
+  // --- validation ----------------------------------------------------------
+  for (int f = 0; f < nf; ++f) {
+    int o = m.owner[f];
+    if (o < 1 || o > n) {
+      err = "owner(" + std::to_string(f + 1) + ") = " + std::to_string(o) + " is out of 1.." +
+            std::to_string(n);
+      return FCG_ERR_INDEX;
+    }
+  }
+  for (int f = 0; f < nin; ++f) {
+    int nb = m.neighbour[f];
+    if (nb < 1 || nb > n || nb == m.owner[f]) {
+      err = "neighbour(" + std::to_string(f + 1) + ") = " + std::to_string(nb) + " is invalid";
+      return FCG_ERR_INDEX;
+    }
+  }
+  for (int ty = 0; ty < B_NTYPES; ++ty) {
+    if (cnt[ty] < 0 || (cnt[ty] > 0 && (fst[ty] < nin || (long long)fst[ty] + cnt[ty] > nf))) {
+      err = "boundary type " + std::to_string(ty) + " face range is outside the boundary faces";
+      return FCG_ERR_INDEX;
+    }
+  }
+  // --- CSR -------------------------------------------------------------------
+  t.ioffset.assign(n + 1, 0);
+  std::vector<int> rowcnt(n, 1);
+  for (int f = 0; f < nin; ++f) {
+    rowcnt[m.owner[f] - 1]++;
+    rowcnt[m.neighbour[f] - 1]++;
+  }
+  t.ioffset[0] = 1;
+  for (int i = 0; i < n; ++i) {
+    long long next = (long long)t.ioffset[i] + rowcnt[i];
+    if (next > 0x7fffffffLL) {
+      err = "nnz does not fit a 32-bit CSR index";
+      return FCG_ERR_ARG;
+    }
+    t.ioffset[i + 1] = (int)next;
+  }
+  const long long nnz = (long long)t.ioffset[n] - 1;
+  t.ja.assign(nnz, 0);
+  {
+    std::vector<int> fill(n);
+    for (int i = 0; i < n; ++i) {
+      fill[i] = t.ioffset[i] - 1;
+      t.ja[fill[i]++] = i + 1;
+    }
+    for (int f = 0; f < nin; ++f) {
+      int o = m.owner[f] - 1, nb = m.neighbour[f] - 1;
+      t.ja[fill[o]++] = nb + 1;
+      t.ja[fill[nb]++] = o + 1;
+    }
+  }
+  bool dup = false;
+  parallel_for(n, [&](long long i) {
+    int b = t.ioffset[i] - 1, e = t.ioffset[i + 1] - 1;
+    std::sort(t.ja.begin() + b, t.ja.begin() + e);
+    for (int k = b + 1; k < e; ++k)
+      if (t.ja[k] == t.ja[k - 1]) dup = true;
+  });
+  if (dup) {
+    err = "two faces connect the same pair of cells";
+    return FCG_ERR_INDEX;
+  }
+  t.diag.assign(n, 0);
+  parallel_for(n, [&](long long i) {
+    for (int k = t.ioffset[i] - 1; k < t.ioffset[i + 1] - 1; ++k)
+      if (t.ja[k] == i + 1) t.diag[i] = k + 1;
+  });
+  auto find = [&](int row1, int col1) {  // 1-based position of (row, col), 0 if absent
+    int b = t.ioffset[row1 - 1] - 1, e = t.ioffset[row1] - 1;
+    auto it = std::lower_bound(t.ja.begin() + b, t.ja.begin() + e, col1);
+    return (it != t.ja.begin() + e && *it == col1) ? (int)(it - t.ja.begin()) + 1 : 0;
+  };
+  t.slot_pn.assign(nin, 0);
+  t.slot_np.assign(nin, 0);
+  parallel_for(nin, [&](long long f) {
+    t.slot_pn[f] = find(m.owner[f], m.neighbour[f]);
+    t.slot_np[f] = find(m.neighbour[f], m.owner[f]);
+  });
+  t.tpos.assign(nnz, 0);
+  parallel_for(n, [&](long long i) {
+    for (int k = t.ioffset[i] - 1; k < t.ioffset[i + 1] - 1; ++k)
+      t.tpos[k] = find(t.ja[k], (int)i + 1) - 1;
+  });
+
+  // --- incidence lists ---------------------------------------------------------
+  t.cf_ptr.assign(n + 1, 0);
+  for (int f = 0; f < nin; ++f) {
+    t.cf_ptr[m.owner[f]]++;
+    t.cf_ptr[m.neighbour[f]]++;
+  }
+  for (int i = 0; i < n; ++i) t.cf_ptr[i + 1] += t.cf_ptr[i];
+  t.cf_ent.assign(t.cf_ptr[n], 0);
+  t.cf_slot.assign(t.cf_ptr[n], 0);
+  {
+    std::vector<int> fill(t.cf_ptr.begin(), t.cf_ptr.end() - 1);
+    for (int f = 0; f < nin; ++f) {
+      int o = m.owner[f] - 1, nb = m.neighbour[f] - 1;
+      int e = fill[o]++;
+      t.cf_ent[e] = f + 1;
+      t.cf_slot[e] = t.slot_pn[f] - 1;
+      e = fill[nb]++;
+      t.cf_ent[e] = -(f + 1);
+      t.cf_slot[e] = t.slot_np[f] - 1;
+    }
+  }
+  t.cb_ptr.assign(n + 1, 0);
+  for (int ty = 0; ty < B_NTYPES; ++ty)
+    for (int i = 0; i < cnt[ty]; ++i) t.cb_ptr[m.owner[fst[ty] + i]]++;
+  for (int i = 0; i < n; ++i) t.cb_ptr[i + 1] += t.cb_ptr[i];
+  t.cb_face.assign(t.cb_ptr[n], 0);
+  t.cb_slot.assign(t.cb_ptr[n], 0);
+  t.cb_type.assign(t.cb_ptr[n], 0);
+  {
+    std::vector<int> fill(t.cb_ptr.begin(), t.cb_ptr.end() - 1);
+    for (int ty = 0; ty < B_NTYPES; ++ty)
+      for (int i = 0; i < cnt[ty]; ++i) {
+        int face = fst[ty] + i, c = m.owner[face] - 1;
+        int e = fill[c]++;
+        t.cb_face[e] = face;
+        t.cb_slot[e] = bst[ty] + i;
+        t.cb_type[e] = ty;
+      }
+  }
+  t.cbf_ptr.assign(n + 1, 0);
+  for (int f = nin; f < nf; ++f) t.cbf_ptr[m.owner[f]]++;
+  for (int i = 0; i < n; ++i) t.cbf_ptr[i + 1] += t.cbf_ptr[i];
+  t.cbf_face.assign(t.cbf_ptr[n], 0);
+  {
+    std::vector<int> fill(t.cbf_ptr.begin(), t.cbf_ptr.end() - 1);
+    for (int f = nin; f < nf; ++f) t.cbf_face[fill[m.owner[f] - 1]++] = f;
+  }
+
+  // --- sliced ELL --------------------------------------------------------------
+  const int ns = (n + 31) / 32;
+  t.sell_ptr.assign(ns + 1, 0);
+  t.sell_width.assign(ns, 0);
+  t.sell_maxw = 0;
+  for (int s = 0; s < ns; ++s) {
+    int w = 0;
+    for (int r = 32 * s; r < std::min(n, 32 * s + 32); ++r)
+      w = std::max(w, t.ioffset[r + 1] - t.ioffset[r]);
+    t.sell_width[s] = w;
+    t.sell_maxw = std::max(t.sell_maxw, w);
+    t.sell_ptr[s + 1] = t.sell_ptr[s] + 32LL * w;
+  }
+  t.sell_col.assign(t.sell_ptr[ns], 0);
+  t.sell_src.assign(t.sell_ptr[ns], -1);
+  parallel_for(ns, [&](long long s) {
+    int w = t.sell_width[s];
+    for (int lane = 0; lane < 32; ++lane) {
+      long long r = 32 * s + lane;
+      int len = r < n ? t.ioffset[r + 1] - t.ioffset[r] : 0;
+      for (int j = 0; j < w; ++j) {
+        long long pos = t.sell_ptr[s] + (long long)j * 32 + lane;
+        if (j < len) {
+          int k = t.ioffset[r] - 1 + j;
+          t.sell_col[pos] = t.ja[k] - 1;
+          t.sell_src[pos] = k;
+        } else {
+          t.sell_col[pos] = (int)std::min<long long>(r, n - 1);
+          t.sell_src[pos] = -1;
+        }
+      }
+    }
+  });
+
+  // --- level schedules -----------------------------------------------------------
+  std::vector<int> lev(n, 0);
+  int nlev = 0;
+  for (int i = 0; i < n; ++i) {
+    int l = 0;
+    for (int k = t.ioffset[i] - 1; k < t.diag[i] - 1; ++k) l = std::max(l, lev[t.ja[k] - 1] + 1);
+    lev[i] = l;
+    nlev = std::max(nlev, l + 1);
+  }
+  t.lf_ptr.assign(nlev + 1, 0);
+  for (int i = 0; i < n; ++i) t.lf_ptr[lev[i] + 1]++;
+  for (int l = 0; l < nlev; ++l) t.lf_ptr[l + 1] += t.lf_ptr[l];
+  t.lf_rows.assign(n, 0);
+  {
+    std::vector<int> fill(t.lf_ptr.begin(), t.lf_ptr.end() - 1);
+    for (int i = 0; i < n; ++i) t.lf_rows[fill[lev[i]]++] = i;
+  }
+  nlev = 0;
+  for (int i = n - 1; i >= 0; --i) {
+    int l = 0;
+    for (int k = t.diag[i]; k < t.ioffset[i + 1] - 1; ++k) l = std::max(l, lev[t.ja[k] - 1] + 1);
+    lev[i] = l;
+    nlev = std::max(nlev, l + 1);
+  }
+  t.lb_ptr.assign(nlev + 1, 0);
+  for (int i = 0; i < n; ++i) t.lb_ptr[lev[i] + 1]++;
+  for (int l = 0; l < nlev; ++l) t.lb_ptr[l + 1] += t.lb_ptr[l];
+  t.lb_rows.assign(n, 0);
+  {
+    std::vector<int> fill(t.lb_ptr.begin(), t.lb_ptr.end() - 1);
+    for (int i = 0; i < n; ++i) t.lb_rows[fill[lev[i]]++] = i;
+  }
+  return FCG_OK;
+}
+
+}  // namespace fcg
+
+extern "C" int fcg_csr_build(int numCells, int numInnerFaces, const int *owner,
+                             const int *neighbour, int *ioffset, int *ja, int *diag, int *slot_pn,
+                             int *slot_np) {
+  if (numCells <= 0 || numInnerFaces < 0 || (numInnerFaces > 0 && (!owner || !neighbour)) ||
+      !ioffset || !ja || !diag || (numInnerFaces > 0 && (!slot_pn || !slot_np)))
+    return FCG_ERR_ARG;
+  fcg_mesh_desc m{};
+  m.numCells = numCells;
+  m.numFaces = numInnerFaces;
+  m.numInnerFaces = numInnerFaces;
+  m.owner = owner;
+  m.neighbour = neighbour;
+  const int zero[fcg::B_NTYPES] = {0, 0, 0, 0, 0};
+  fcg::HostTopology t;
+  std::string err;
+  int rc = fcg::build_topology(m, zero, zero, zero, t, err);
+  if (rc) return rc;
+  std::copy(t.ioffset.begin(), t.ioffset.end(), ioffset);
+  std::copy(t.ja.begin(), t.ja.end(), ja);
+  std::copy(t.diag.begin(), t.diag.end(), diag);
+  std::copy(t.slot_pn.begin(), t.slot_pn.end(), slot_pn);
+  std::copy(t.slot_np.begin(), t.slot_np.end(), slot_np);
+  return FCG_OK;
+}

@@ -1,0 +1,176 @@
+"""Meshes for the pressure-correction path: the arrays of the reference's module
+``geometry`` (src/mesh_geometry_and_topology.f90:12-98).
+
+Two sources:
+  * ``hex_mesh(N, jitter, seed)`` -- the N^3 jittered hex mesh of the unit cube made
+    by libfcgpu.so (host code, every thread), with its geometry computed the way
+    ``mesh_geometry`` computes it;
+  * ``polymesh_mesh(points, face_ptr, face_nodes, owner, neighbour, patches)`` -- a mesh
+    read from polyMesh files (the test fixtures), with the boundary patches mapped to
+    the reference's boundary types as mesh_geometry_and_topology.f90:409-472 does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+
+BOUNDARY_TYPES = ("inlet", "outlet", "symmetry", "wall", "prOutlet")
+_WALL_ALIASES = ("wall", "wallIsoth", "wallAdiab", "wallQFlux")
+
+
+@dataclass
+class Mesh:
+    numCells: int
+    numFaces: int
+    numInnerFaces: int
+    owner: np.ndarray
+    neighbour: np.ndarray
+    arx: np.ndarray
+    ary: np.ndarray
+    arz: np.ndarray
+    xf: np.ndarray
+    yf: np.ndarray
+    zf: np.ndarray
+    xc: np.ndarray
+    yc: np.ndarray
+    zc: np.ndarray
+    vol: np.ndarray
+    facint: np.ndarray
+    counts: dict = field(default_factory=dict)  # ninl, nout, nsym, nwal, npru
+    starts: dict = field(default_factory=dict)  # i*FacesStart (0-based)
+    points: np.ndarray | None = None
+    face_ptr: np.ndarray | None = None
+    face_nodes: np.ndarray | None = None
+
+    @property
+    def numTotal(self) -> int:
+        return self.numCells + self.numFaces - self.numInnerFaces
+
+    @property
+    def nnz(self) -> int:
+        return self.numCells + 2 * self.numInnerFaces
+
+    def boundary_slot_start(self, btype: str) -> int:
+        """0-based offset of a boundary type's slots in a numTotal field (:593-605)."""
+        off = self.numCells
+        for t, key in zip(BOUNDARY_TYPES, ("ninl", "nout", "nsym", "nwal", "npru")):
+            if t == btype:
+                return off
+            off += self.counts.get(key, 0)
+        raise KeyError(btype)
+
+    def desc(self) -> _lib.MeshDesc:
+        d = _lib.MeshDesc()
+        d.numCells, d.numFaces, d.numInnerFaces = self.numCells, self.numFaces, self.numInnerFaces
+        for k in ("ninl", "nout", "nsym", "nwal", "npru"):
+            setattr(d, k, int(self.counts.get(k, 0)))
+        for k in ("iInletFacesStart", "iOutletFacesStart", "iSymmetryFacesStart",
+                  "iWallFacesStart", "iPressOutletFacesStart"):
+            setattr(d, k, int(self.starts.get(k, 0)))
+        d.noc = 0
+        for k in ("owner", "neighbour", "arx", "ary", "arz", "xf", "yf", "zf", "xc", "yc", "zc",
+                  "vol", "facint"):
+            setattr(d, k, getattr(self, k).ctypes.data)
+        return d
+
+    def oracle_kwargs(self) -> dict:
+        """Keyword arguments for the oracle's mesh wrapper (tests only)."""
+        kw = {k: getattr(self, k) for k in ("numCells", "numFaces", "numInnerFaces", "owner",
+                                             "neighbour", "arx", "ary", "arz", "xf", "yf", "zf",
+                                             "xc", "yc", "zc", "vol", "facint")}
+        kw.update(self.counts)
+        kw.update(self.starts)
+        return kw
+
+
+def _p(a):
+    return a.ctypes.data
+
+
+def compute_geometry(points, face_ptr, face_nodes, owner, neighbour, numCells):
+    """mesh_geometry's geometric part (:859-1079), run by libfcgpu.so on the host."""
+    lib = _lib.load()
+    x, y, z = (np.ascontiguousarray(points[:, i], dtype=np.float64) for i in range(3))
+    face_ptr = np.ascontiguousarray(face_ptr, dtype=np.int32)
+    face_nodes = np.ascontiguousarray(face_nodes, dtype=np.int32)
+    owner = np.ascontiguousarray(owner, dtype=np.int32)
+    neighbour = np.ascontiguousarray(neighbour, dtype=np.int32)
+    nf, nin = len(face_ptr) - 1, len(neighbour)
+    g = {k: np.zeros(nf) for k in ("arx", "ary", "arz", "xf", "yf", "zf")}
+    g.update({k: np.zeros(numCells) for k in ("xc", "yc", "zc", "vol")})
+    g["facint"] = np.zeros(max(nin, 1))
+    rc = lib.fcg_mesh_geometry(len(x), _p(x), _p(y), _p(z), numCells, nf, nin, _p(face_ptr),
+                               _p(face_nodes), _p(owner), _p(neighbour if nin else g["facint"]),
+                               *[_p(g[k]) for k in ("arx", "ary", "arz", "xf", "yf", "zf", "xc",
+                                                    "yc", "zc", "vol", "facint")])
+    if rc != 0:
+        raise _lib.FcgError(rc, "fcg_mesh_geometry")
+    g["facint"] = g["facint"][:nin]
+    return g
+
+
+def hex_mesh(N: int, jitter: float = 0.0, seed: int = 0, keep_topology: bool = False) -> Mesh:
+    """N^3 hex mesh of the unit cube: wall at x=0, symmetry on the other five faces."""
+    lib = _lib.load()
+    nn, nc, nf, nin = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    rc = lib.fcg_hex_mesh_sizes(N, C.byref(nn), C.byref(nc), C.byref(nf), C.byref(nin))
+    if rc != 0:
+        raise _lib.FcgError(rc, "fcg_hex_mesh_sizes")
+    nn, nc, nf, nin = nn.value, nc.value, nf.value, nin.value
+    pts = np.zeros((3, nn))
+    face_ptr = np.zeros(nf + 1, np.int32)
+    face_nodes = np.zeros(4 * nf, np.int32)
+    owner = np.zeros(nf, np.int32)
+    neighbour = np.zeros(max(nin, 1), np.int32)
+    patches = np.zeros(4, np.int32)
+    rc = lib.fcg_hex_mesh_build(N, float(jitter), int(seed), _p(pts[0]), _p(pts[1]), _p(pts[2]),
+                                _p(face_ptr), _p(face_nodes), _p(owner), _p(neighbour),
+                                _p(patches))
+    if rc != 0:
+        raise _lib.FcgError(rc, "fcg_hex_mesh_build")
+    neighbour = neighbour[:nin]
+    points = np.ascontiguousarray(pts.T)
+    g = compute_geometry(points, face_ptr, face_nodes, owner, neighbour, nc)
+    m = Mesh(nc, nf, nin, owner, neighbour, **g,
+             counts=dict(nsym=int(patches[0]), nwal=int(patches[2])),
+             starts=dict(iSymmetryFacesStart=int(patches[1]), iWallFacesStart=int(patches[3])))
+    if keep_topology:
+        m.points, m.face_ptr, m.face_nodes = points, face_ptr, face_nodes
+    return m
+
+
+def polymesh_mesh(points, face_ptr, face_nodes, owner, neighbour, numCells, patch_type,
+                  patch_nfaces, patch_start) -> Mesh:
+    """A polyMesh (1-based arrays) with the reference's boundary bookkeeping."""
+    counts = {k: 0 for k in ("ninl", "nout", "nsym", "nwal", "npru")}
+    starts = {}
+    key = {"inlet": ("ninl", "iInletFacesStart"), "outlet": ("nout", "iOutletFacesStart"),
+           "symmetry": ("nsym", "iSymmetryFacesStart"), "prOutlet": ("npru", "iPressOutletFacesStart")}
+    for t in _WALL_ALIASES:
+        key[t] = ("nwal", "iWallFacesStart")
+    for t, cnt, st in zip(patch_type, patch_nfaces, patch_start):
+        t = str(t)
+        if t not in key:
+            raise ValueError(f"boundary type {t!r} is not supported (O-C and cyclic faces)")
+        c, s = key[t]
+        if counts[c] == 0:
+            starts[s] = int(st)
+        counts[c] += int(cnt)
+    g = compute_geometry(points, face_ptr, face_nodes, owner, neighbour, int(numCells))
+    return Mesh(int(numCells), len(face_ptr) - 1, len(neighbour),
+                np.ascontiguousarray(owner, np.int32), np.ascontiguousarray(neighbour, np.int32),
+                **g, counts=counts, starts=starts, points=np.asarray(points),
+                face_ptr=np.asarray(face_ptr, np.int32), face_nodes=np.asarray(face_nodes, np.int32))
+
+
+def uniform(seed: int, stream: int, count: int, lo: float = -1.0, hi: float = 1.0) -> np.ndarray:
+    """Counter-based U(lo, hi) numbers keyed by (seed, stream)."""
+    out = np.zeros(count)
+    rc = _lib.load().fcg_uniform_fill(int(seed), int(stream), int(count), float(lo), float(hi), _p(out))
+    if rc != 0:
+        raise _lib.FcgError(rc, "fcg_uniform_fill")
+    return out

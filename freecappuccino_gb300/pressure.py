@@ -1,0 +1,221 @@
+"""Python face of the pressure-correction path, mirroring the reference's Fortran calls.
+
+The reference calls ``laplacian(mu,phi)``, ``facefluxmass(...)`` (inside ``calcp``),
+``fluxmc``, ``grad(phi,dPhidxi[,option])``, ``bpres(p,istage)`` and
+``dpcg/iccg/bicgstab(fi,ifi)`` on module-global arrays.  ``Context`` holds that state for
+one mesh on one GPU and exposes the same operations with the arrays passed explicitly.
+Arrays may be numpy arrays (host; copied in and out inside each call) or CUDA tensors
+(used in place).  Every call goes through libfcgpu.so; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from .mesh import Mesh
+
+_GRAD = {"gauss": _lib.FCG_GRAD_GAUSS, "gauss_corrected": _lib.FCG_GRAD_GAUSS_CORRECTED,
+         "lsq": _lib.FCG_GRAD_LSQ}
+
+
+def _is_torch(x) -> bool:
+    return hasattr(x, "data_ptr") and hasattr(x, "is_cuda")
+
+
+def _ptr(x):
+    if x is None:
+        return None
+    if _is_torch(x):
+        return x.data_ptr()
+    return x.ctypes.data
+
+
+def _like(ref, shape, dtype=np.float64):
+    """A zero array on the same side (host or device) as `ref`."""
+    if _is_torch(ref):
+        import torch
+
+        tdt = {np.float64: torch.float64, np.int32: torch.int32}[dtype]
+        return torch.zeros(shape, dtype=tdt, device=ref.device)
+    return np.zeros(shape, dtype=dtype)
+
+
+def _host(x, dtype=np.float64):
+    if _is_torch(x):
+        return x
+    return np.ascontiguousarray(x, dtype=dtype)
+
+
+@dataclass
+class SolveResult:
+    fi: object
+    res: object
+    res0: float
+    resl: float
+    iters: int
+    converged: bool
+    resor: float | None
+    l2_rel: float
+    seconds: float
+    trace: np.ndarray = field(default_factory=lambda: np.zeros((0, 2)))
+
+
+# Log-line names of the reference solvers (dpcg.f90:150, iccg.f90:328, bicgstab.f90:227).
+SOLVER_NAMES = {"dpcg": "PCG(Jacobi):  ", "iccg": "  PCG(IC0):  ", "bicgstab": "  BiCGStab(ILU(0)):  "}
+
+
+def solver_log(kind: str, var: str, r: SolveResult) -> str:
+    """The reference's one-line solver report, format '(3a,1PE10.3,a,1PE10.3,a,I0)'."""
+    return (f"{SOLVER_NAMES[kind]}Solving for {var}, Initial residual = {r.res0:10.3E}, "
+            f"Final residual = {r.resl:10.3E}, No Iterations {r.iters}")
+
+
+class Context:
+    """An fcg_context bound to one mesh."""
+
+    def __init__(self, mesh: Mesh, device: int = 0):
+        self.lib = _lib.load()
+        self.mesh = mesh
+        h = C.c_void_p()
+        rc = self.lib.fcg_create(C.byref(h), int(device))
+        if rc != 0:
+            raise _lib.FcgError(rc, "fcg_create", "no usable sm_103a CUDA device")
+        self.h = h
+        self._desc = mesh.desc()  # keeps the pointers alive for the call
+        self._check(self.lib.fcg_bind_mesh(self.h, C.byref(self._desc)), "fcg_bind_mesh")
+        self.n, self.nnz, self.ntot = mesh.numCells, mesh.nnz, mesh.numTotal
+
+    # -- plumbing -------------------------------------------------------------
+    def _check(self, rc, where):
+        if rc != 0:
+            raise _lib.FcgError(rc, where, self.lib.fcg_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fcg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle: int | None):
+        self._check(self.lib.fcg_set_stream(self.h, stream_handle), "fcg_set_stream")
+
+    def synchronize(self):
+        self._check(self.lib.fcg_synchronize(self.h), "fcg_synchronize")
+
+    # -- a1 -----------------------------------------------------------------------
+    def create_csr(self):
+        """(ioffset, ja, diag, slot_pn, slot_np), 1-based (sparse_matrix.f90:42-172)."""
+        n, nin = self.n, self.mesh.numInnerFaces
+        io, ja, dg = np.zeros(n + 1, np.int32), np.zeros(self.nnz, np.int32), np.zeros(n, np.int32)
+        spn, snp = np.zeros(max(nin, 1), np.int32), np.zeros(max(nin, 1), np.int32)
+        self._check(self.lib.fcg_create_csr(self.h, _ptr(io), _ptr(ja), _ptr(dg), _ptr(spn),
+                                            _ptr(snp)), "fcg_create_csr")
+        return io, ja, dg, spn[:nin], snp[:nin]
+
+    # -- a2-a4 ----------------------------------------------------------------------
+    def laplacian(self, mu, phi, su):
+        """fvm_laplacian.f90 laplacian(mu,phi): returns (a, su)."""
+        mu, phi = _host(mu), _host(phi)
+        su = su.clone() if _is_torch(su) else np.array(su, dtype=np.float64)
+        a = _like(mu, self.nnz)
+        self._check(self.lib.fcg_laplacian(self.h, _ptr(mu), _ptr(phi), _ptr(a), _ptr(su)),
+                    "fcg_laplacian")
+        return a, su
+
+    def facefluxmass(self, u, v, w, p, dUdxi, dVdxi, dWdxi, dPdxi, apu, apv, apw, den):
+        """calcp's assembly loop with facefluxmass: returns (a, su, flmass)."""
+        arrs = [_host(t) for t in (u, v, w, p, dUdxi, dVdxi, dWdxi, dPdxi, apu, apv, apw, den)]
+        ff = _lib.FlowFields(*[_ptr(t) for t in arrs])
+        a = _like(arrs[0], self.nnz)
+        su = _like(arrs[0], self.n)
+        fm = _like(arrs[0], max(self.mesh.numInnerFaces, 1))
+        self._check(self.lib.fcg_facefluxmass(self.h, C.byref(ff), _ptr(a), _ptr(su), _ptr(fm)),
+                    "fcg_facefluxmass")
+        return a, su, fm[: self.mesh.numInnerFaces]
+
+    def fluxmc(self, dPdxi, apu, den, flmass):
+        """calcp's non-orthogonal corrector with fluxmc: returns (su, flmass)."""
+        dPdxi, apu, den = _host(dPdxi), _host(apu), _host(den)
+        fm = flmass.clone() if _is_torch(flmass) else np.array(flmass, dtype=np.float64)
+        su = _like(apu, self.n)
+        self._check(self.lib.fcg_fluxmc(self.h, _ptr(dPdxi), _ptr(apu), _ptr(den), _ptr(su),
+                                        _ptr(fm)), "fcg_fluxmc")
+        return su, fm
+
+    # -- a5-a8 ----------------------------------------------------------------------
+    def grad(self, phi, option: str = "gauss", nigrad: int = 1, dphidxi=None):
+        """grad(phi,dPhidxi[,option]) without limiter: returns dPhidxi as (n, 3)."""
+        phi = _host(phi)
+        if option == "gauss_corrected" and dphidxi is not None:
+            g = dphidxi.clone() if _is_torch(dphidxi) else np.array(dphidxi, dtype=np.float64)
+        else:
+            g = _like(phi, (self.n, 3))
+        self._check(self.lib.fcg_grad(self.h, _ptr(phi), _ptr(g), _GRAD[option], int(nigrad)),
+                    "fcg_grad")
+        return g
+
+    def grad_lsq_matrix(self):
+        d = np.zeros((self.n, 9))
+        self._check(self.lib.fcg_grad_lsq_matrix(self.h, _ptr(d)), "fcg_grad_lsq_matrix")
+        return d
+
+    def bpres(self, p, dPdxi, istage: int):
+        """bpres(p,istage): returns the updated p(numTotal)."""
+        p = p.clone() if _is_torch(p) else np.array(p, dtype=np.float64)
+        g = _host(dPdxi) if dPdxi is not None else _like(p, (self.n, 3))
+        self._check(self.lib.fcg_bpres(self.h, _ptr(p), _ptr(g), int(istage)), "fcg_bpres")
+        return p
+
+    # -- a9-a11 ----------------------------------------------------------------------
+    def set_solver_options(self, small: float, early_exit: bool):
+        self._check(self.lib.fcg_set_solver_options(self.h, float(small), int(bool(early_exit))),
+                    "fcg_set_solver_options")
+
+    def trace(self, max_count: int = 1 << 20) -> np.ndarray:
+        cnt = C.c_int()
+        self._check(self.lib.fcg_get_solver_trace(self.h, None, 0, C.byref(cnt)), "trace")
+        m = min(cnt.value, max_count)
+        out = np.zeros((max(m, 1), 2))
+        self._check(self.lib.fcg_get_solver_trace(self.h, _ptr(out), m, C.byref(cnt)), "trace")
+        return out[: cnt.value]
+
+    def _solve(self, fn, name, a, su, fi, sor, nsw, want_res=True, want_trace=False):
+        a, su = _host(a), _host(su)
+        fi = fi.clone() if _is_torch(fi) else np.array(fi, dtype=np.float64)
+        res = _like(su, self.n) if want_res else None
+        resor = C.c_double(float("nan"))
+        rep = _lib.SolveReport()
+        self._check(fn(self.h, _ptr(a), _ptr(su), _ptr(fi), _ptr(res), float(sor), int(nsw),
+                       C.byref(resor), C.byref(rep)), name)
+        r = SolveResult(fi, res, rep.res0, rep.resl, rep.iters, bool(rep.converged),
+                        None if rep.iters == 0 else resor.value, rep.l2_rel, rep.seconds)
+        if want_trace:
+            r.trace = self.trace()
+        return r
+
+    def dpcg(self, a, su, fi, sor, nsw, **kw) -> SolveResult:
+        """dpcg(fi,ifi) (dpcg.f90:3-154)."""
+        return self._solve(self.lib.fcg_dpcg, "fcg_dpcg", a, su, fi, sor, nsw, **kw)
+
+    def iccg(self, a, su, fi, sor, nsw, **kw) -> SolveResult:
+        """iccg(fi,ifi) (iccg.f90:3-177)."""
+        return self._solve(self.lib.fcg_iccg, "fcg_iccg", a, su, fi, sor, nsw, **kw)
+
+    def bicgstab(self, a, su, fi, sor, nsw, **kw) -> SolveResult:
+        """bicgstab(fi,ifi) (bicgstab.f90:1-231)."""
+        return self._solve(self.lib.fcg_bicgstab, "fcg_bicgstab", a, su, fi, sor, nsw, **kw)
+
+    def spmv(self, a, x, y=None):
+        x = _host(x)
+        y = _like(x, self.n) if y is None else y
+        self._check(self.lib.fcg_spmv(self.h, _ptr(_host(a)) if a is not None else None, _ptr(x),
+                                      _ptr(y)), "fcg_spmv")
+        return y

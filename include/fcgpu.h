@@ -1,0 +1,201 @@
+/*
+ * fcgpu.h -- C ABI of libfcgpu.so, the GB300 (sm_103a) implementation of
+ * freeCappuccino's pressure-correction path.
+ *
+ * The reference exposes this path as Fortran subroutines working on module-global
+ * arrays (modules `geometry`, `sparse_matrix`, `variables`).  This library keeps the
+ * same arrays, index conventions and call sequence, but passes every array
+ * explicitly:
+ *   - index values are 1-based int32 exactly as the Fortran arrays hold them
+ *     (owner, neighbour, ioffset, ja, diag, slot maps);
+ *   - reals are IEEE binary64 (`real(dp)`); cell gradients are dPhidxi(3,numCells),
+ *     component fastest;
+ *   - a field of "numTotal" length holds the numCells cell values followed by one
+ *     value per boundary face, grouped by boundary type in the order inlet, outlet,
+ *     symmetry, wall, pressure outlet (mesh_geometry_and_topology.f90:593-605).
+ * Every pointer argument may point to host memory (pageable or pinned) or to device
+ * memory on the context's GPU; the library tells them apart and copies host arrays
+ * in and out inside the call.  Device arrays are used in place.
+ *
+ * Every function returns FCG_OK (0) or a negative status; fcg_last_error() gives a
+ * one-line description.  A context is not thread-safe (the reference is serial).
+ * The library has no CPU fallback: without a usable sm_103a device every compute
+ * entry point returns FCG_ERR_CUDA.
+ */
+#ifndef FCGPU_H
+#define FCGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FCG_ABI_VERSION 1
+
+/* Status codes. */
+#define FCG_OK 0
+#define FCG_ERR_ARG (-1)         /* bad argument: NULL pointer, size out of range */
+#define FCG_ERR_STATE (-2)       /* call order: e.g. a solve before fcg_bind_mesh */
+#define FCG_ERR_CUDA (-3)        /* CUDA runtime error or no usable device */
+#define FCG_ERR_INDEX (-4)       /* owner/neighbour/boundary index out of range or duplicate face */
+#define FCG_ERR_PIVOT (-5)       /* zero or non-finite pivot in a DIC/DILU factor */
+#define FCG_ERR_STALL (-6)       /* a preconditioned iteration stalled (learned FCG) */
+#define FCG_ERR_TIMEOUT (-7)     /* a bounded device-side wait gave up */
+#define FCG_ERR_UNSUPPORTED (-8) /* O-C grid cuts and cyclic faces are not supported */
+#define FCG_ERR_NOMEM (-9)       /* device allocation failed */
+#define FCG_ERR_NONFINITE (-10)  /* NaN/Inf reached a reduction */
+
+typedef struct fcg_context fcg_context;
+
+int fcg_abi_version(void);
+const char *fcg_status_string(int status);
+const char *fcg_last_error(const fcg_context *ctx);
+
+/* Creates a context on CUDA device `device` (the module-global state of the
+ * reference becomes per-context state). */
+int fcg_create(fcg_context **ctx, int device);
+int fcg_destroy(fcg_context *ctx);
+/* All work of the context is queued on this stream (cudaStream_t; NULL = the
+ * context's own stream). */
+int fcg_set_stream(fcg_context *ctx, void *cuda_stream);
+int fcg_synchronize(fcg_context *ctx);
+
+/* ---------------------------------------------------------------------------
+ * Mesh (module `geometry`, src/mesh_geometry_and_topology.f90:12-98).
+ * ------------------------------------------------------------------------- */
+typedef struct fcg_mesh_desc {
+  int numCells, numFaces, numInnerFaces;
+  /* Boundary faces per type and the 0-based start of each type's face range as the
+   * boundary file gives it (face index iface = start + i, i = 1..count). */
+  int ninl, nout, nsym, nwal, npru;
+  int iInletFacesStart, iOutletFacesStart, iSymmetryFacesStart, iWallFacesStart,
+      iPressOutletFacesStart;
+  int noc; /* O-C grid cut faces: must be 0 (FCG_ERR_UNSUPPORTED otherwise) */
+  const int *owner;                             /* [numFaces], 1-based */
+  const int *neighbour;                         /* [numInnerFaces], 1-based */
+  const double *arx, *ary, *arz, *xf, *yf, *zf; /* [numFaces] */
+  const double *xc, *yc, *zc, *vol;             /* [numCells] */
+  const double *facint;                         /* [numInnerFaces] */
+} fcg_mesh_desc;
+
+/* Uploads the mesh and builds, once, everything the kernels need: the CSR pattern
+ * of create_CSR_matrix_from_mesh_data (src/sparse_matrix.f90:42-172), the sliced
+ * ELL copy used by the solvers, the cell->face incidence lists that keep the
+ * reference's face-loop summation order, and the level schedules of the
+ * triangular sweeps.  Replaces: mesh_geometry (mesh_geometry_and_topology.f90:310)
+ * as a consumer of its arrays, and create_CSR_matrix_from_mesh_data. */
+int fcg_bind_mesh(fcg_context *ctx, const fcg_mesh_desc *mesh);
+int fcg_mesh_sizes(const fcg_context *ctx, int *numCells, int *numFaces, int *numInnerFaces,
+                   long long *nnz, int *numTotal);
+
+/* CSR arrays of create_CSR_matrix_from_mesh_data (sparse_matrix.f90:42-172),
+ * bit-exact, 1-based: ioffset[numCells+1], ja[nnz], diag[numCells], and the face
+ * slot maps icell_jcell_csr_value_index / jcell_icell_csr_value_index
+ * [numInnerFaces] (sparse_matrix.f90:153-167).  Any pointer may be NULL. */
+int fcg_create_csr(fcg_context *ctx, int *ioffset, int *ja, int *diag, int *slot_pn,
+                   int *slot_np);
+
+/* Host-only form of the same construction (no context, no GPU): the CSR arrays of
+ * create_CSR_matrix_from_mesh_data for an owner/neighbour list (sparse_matrix.f90:
+ * 42-172), 1-based, with nnz = numCells + 2*numInnerFaces. */
+int fcg_csr_build(int numCells, int numInnerFaces, const int *owner, const int *neighbour,
+                  int *ioffset, int *ja, int *diag, int *slot_pn, int *slot_np);
+
+/* ---------------------------------------------------------------------------
+ * Assembly (face loops into the CSR values a[nnz]).
+ * ------------------------------------------------------------------------- */
+
+/* laplacian(mu,phi), src/fvm_laplacian.f90:1-163: a = 0, then inner-face
+ * coefficients (mu[numCells], linear interpolation by facint), then wall faces,
+ * which also add a(diag)*phi(ijb) to su.  phi[numTotal] (only wall slots read),
+ * a[nnz] out, su[numCells] in/out. */
+int fcg_laplacian(fcg_context *ctx, const double *mu, const double *phi, double *a, double *su);
+
+/* Flow fields read by facefluxmass (module `variables`). */
+typedef struct fcg_flow_fields {
+  const double *u, *v, *w, *p;                 /* [numTotal] */
+  const double *dUdxi, *dVdxi, *dWdxi, *dPdxi; /* [3*numCells] */
+  const double *apu, *apv, *apw;               /* [numCells] */
+  const double *den;                           /* [numTotal] */
+} fcg_flow_fields;
+
+/* Pressure-correction assembly of calcp (calcp-multiple_correction_SIMPLE.f90:34-77)
+ * with facefluxmass (facefluxmass.f90:34-199): a = 0, su = 0, then per inner face
+ * the p' coefficients, the Rhie-Chow mass flux flmass[numInnerFaces] and its
+ * divergence into su. */
+int fcg_facefluxmass(fcg_context *ctx, const fcg_flow_fields *f, double *a, double *su,
+                     double *flmass);
+
+/* Non-orthogonal corrector source of calcp (calcp-multiple_correction_SIMPLE.f90:
+ * 193-206) with fluxmc (facefluxmass.f90:520-607): su = 0, then per inner face
+ * flmass += fmcor, su(P) -= fmcor, su(N) += fmcor. */
+int fcg_fluxmc(fcg_context *ctx, const double *dPdxi, const double *apu, const double *den,
+               double *su, double *flmass);
+
+/* ---------------------------------------------------------------------------
+ * Gradients and boundary values.
+ * ------------------------------------------------------------------------- */
+#define FCG_GRAD_GAUSS 1           /* grad_gauss.f90, nigrad passes */
+#define FCG_GRAD_GAUSS_CORRECTED 2 /* grad_gauss_corrected.f90, old gradient = dPhidxi on entry */
+#define FCG_GRAD_LSQ 3             /* grad_lsq.f90 stage 2 (needs fcg_grad_lsq_matrix first) */
+
+/* grad(phi,dPhidxi[,option]) (gradients.f90:95-151, :197-259) without limiter:
+ * phi[numTotal] in, dPhidxi[3*numCells] out (in/out for GAUSS_CORRECTED). */
+int fcg_grad(fcg_context *ctx, const double *phi, double *dPhidxi, int method, int nigrad);
+
+/* grad_lsq stage 1 (grad_lsq.f90:50-165): builds the per-cell inverse normal
+ * matrices on the device; dmat[9*numCells] may be NULL or receives a copy. */
+int fcg_grad_lsq_matrix(fcg_context *ctx, double *dmat);
+
+/* bpres(p,istage) (bpres.f90:3-152): istage 1 copies owner values into every
+ * boundary slot, istage >= 2 extrapolates wall and pressure-outlet slots with
+ * dPdxi[3*numCells].  p[numTotal] in/out. */
+int fcg_bpres(fcg_context *ctx, double *p, const double *dPdxi, int istage);
+
+/* ---------------------------------------------------------------------------
+ * Krylov solvers on the CSR matrix (a[nnz], su[numCells]).
+ * ------------------------------------------------------------------------- */
+typedef struct fcg_solve_report {
+  double res0;   /* initial L1 residual sum|su - A fi| */
+  double resl;   /* final L1 residual */
+  int iters;     /* sweeps done (itr_used) */
+  int converged; /* resl/(res0+small) < sor reached */
+  double l2_rel; /* FP64-recomputed ||su - A fi||_2 / ||su||_2 after the solve */
+  double seconds;
+} fcg_solve_report;
+
+/* dpcg(fi,ifi) (src/dpcg.f90:3-154): Jacobi-preconditioned CG, L1-relative stop
+ * resl/(res0+small) < sor, at most nsw sweeps, early return when res0 < 1e-13.
+ * fi[numCells] in/out (the reference's fi(numTotal); only cells are touched);
+ * res[numCells] (may be NULL) receives the final residual; *resor is set to res0
+ * when at least one sweep ran (dpcg.f90:139), as the reference's resor(ifi). */
+int fcg_dpcg(fcg_context *ctx, const double *a, const double *su, double *fi, double *res,
+             double sor, int nsw, double *resor, fcg_solve_report *rep);
+
+/* iccg(fi,ifi) (src/iccg.f90:3-177): CG preconditioned by the diagonal incomplete
+ * Cholesky M = (D+L) D^-1 (D+U); triangular sweeps run level by level. */
+int fcg_iccg(fcg_context *ctx, const double *a, const double *su, double *fi, double *res,
+             double sor, int nsw, double *resor, fcg_solve_report *rep);
+
+/* bicgstab(fi,ifi) (src/bicgstab.f90:1-231): right-preconditioned BiCGStab with the
+ * diagonal ILU factor. */
+int fcg_bicgstab(fcg_context *ctx, const double *a, const double *su, double *fi,
+                 double *res, double sor, int nsw, double *resor, fcg_solve_report *rep);
+
+/* Constants of the solvers: small (parameters::small, modules_allocatable.f90:27;
+ * default the REAL literal 1e-20) and whether a solve returns at once when
+ * res0 < 1e-13 (dpcg.f90:66-70; default 1).  The copies of the solvers in
+ * tests/test_sparse_solvers.f90 use small = 1e-30 and never return early. */
+int fcg_set_solver_options(fcg_context *ctx, double small, int early_exit);
+
+/* Per-sweep (resl, rsm) pairs of the last solve -- what the reference prints per
+ * sweep when ltest is set (dpcg.f90:141). */
+int fcg_get_solver_trace(fcg_context *ctx, double *resl_rsm, int max_count, int *count);
+
+/* y = A x (the matvec of dpcg.f90:105-110) with CSR values a[nnz]; a == NULL reuses
+ * the matrix of the previous solve or spmv call. */
+int fcg_spmv(fcg_context *ctx, const double *a, const double *x, double *y);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FCGPU_H */

@@ -1,0 +1,66 @@
+"""Mesh fixtures shared by the tests: jittered hex meshes from libfcgpu.so's generator
+and the reference's cavity and pitzDaily polyMeshes (tests/golden/*.npz)."""
+from __future__ import annotations
+
+import functools
+import os
+
+import numpy as np
+
+import freecappuccino_gb300 as fcg
+from oracle import oracle
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@functools.lru_cache(maxsize=None)
+def fixture_mesh(name: str) -> fcg.Mesh:
+    d = np.load(os.path.join(GOLDEN, f"{name}_mesh.npz"))
+    return fcg.polymesh_mesh(d["points"], d["face_ptr"], d["face_nodes"], d["owner"],
+                             d["neighbour"], int(d["numCells"]), d["patch_type"],
+                             d["patch_nfaces"], d["patch_start"])
+
+
+@functools.lru_cache(maxsize=None)
+def hex_mesh(N: int, jitter: float = 0.2, seed: int = 7) -> fcg.Mesh:
+    return fcg.hex_mesh(N, jitter=jitter, seed=seed, keep_topology=True)
+
+
+def mesh_by_name(name: str) -> fcg.Mesh:
+    if name.startswith("hex"):
+        # hexN or hexN_u (uniform)
+        body = name[3:]
+        uniform = body.endswith("_u")
+        N = int(body[:-2] if uniform else body)
+        return hex_mesh(N, 0.0 if uniform else 0.2)
+    return fixture_mesh(name)
+
+
+def oracle_mesh(m: fcg.Mesh) -> oracle.Mesh:
+    return oracle.Mesh(**m.oracle_kwargs())
+
+
+def oracle_csr(m: fcg.Mesh) -> oracle.CSR:
+    return oracle.create_csr(m.numCells, m.owner, m.neighbour)
+
+
+def seeded_fields(m: fcg.Mesh, seed: int = 3):
+    """Seeded flow fields for facefluxmass / fluxmc / gradient parity."""
+    n, nt = m.numCells, m.numTotal
+    u = fcg.uniform(seed, 1, nt)
+    v = fcg.uniform(seed, 2, nt)
+    w = fcg.uniform(seed, 3, nt)
+    p = fcg.uniform(seed, 4, nt)
+    g = [fcg.uniform(seed, 10 + k, 3 * n).reshape(n, 3) for k in range(4)]
+    ap = [1.0 / m.vol * (1.0 + 0.1 * fcg.uniform(seed, 20 + k, n)) for k in range(3)]
+    den = 1.0 + 0.2 * fcg.uniform(seed, 30, nt)
+    return dict(u=u, v=v, w=w, p=p, dUdxi=g[0], dVdxi=g[1], dWdxi=g[2], dPdxi=g[3],
+                apu=ap[0], apv=ap[1], apw=ap[2], den=den)
+
+
+def poisson_system(m: fcg.Mesh, seed: int = 11, mu_value: float = -1.0):
+    """The pressure Poisson system of the benchmark: mu = -1, su = U(-1,1)*vol, phi = 0."""
+    mu = np.full(m.numCells, mu_value)
+    phi = np.zeros(m.numTotal)
+    su = fcg.uniform(seed, 0, m.numCells) * m.vol
+    return mu, phi, su

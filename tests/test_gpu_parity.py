@@ -1,0 +1,235 @@
+"""GPU parity: every entry point of libfcgpu.so against the oracle on the same inputs.
+
+Assembly, gradients, boundary values and the CSR pattern must be bit-identical (the
+face-loop kernels keep the reference's summation order and round like it).  The
+solvers differ from the oracle only in the order of their global sums, so they are
+compared (a) after a fixed number of sweeps, within 1e-10 relative, and (b) at
+convergence, by the sweep count and the solution."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import freecappuccino_gb300 as fcg
+from oracle import oracle
+from tests.meshes import (GOLDEN, hex_mesh, mesh_by_name, oracle_csr, oracle_mesh,
+                          poisson_system, seeded_fields)
+
+pytestmark = pytest.mark.gpu
+
+MESHES = ["hex8", "hex12_u", "cavity", "pitzdaily"]
+_ctx_cache = {}
+
+
+def ctx_for(name):
+    if name not in _ctx_cache:
+        m = mesh_by_name(name)
+        _ctx_cache[name] = (m, fcg.Context(m))
+    return _ctx_cache[name]
+
+
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+@pytest.mark.parametrize("name", MESHES)
+def test_csr_from_context_bit_exact(name):
+    m, c = ctx_for(name)
+    ref = oracle_csr(m)
+    io, ja, dg, spn, snp = c.create_csr()
+    for got, exp in ((io, ref.ioffset), (ja, ref.ja), (dg, ref.diag), (spn, ref.slot_pn),
+                     (snp, ref.slot_np)):
+        assert np.array_equal(got, exp)
+
+
+@pytest.mark.parametrize("name", MESHES)
+def test_laplacian_bit_exact(name):
+    m, c = ctx_for(name)
+    mu = -(1.0 + 0.5 * fcg.uniform(1, 5, m.numCells))
+    phi = fcg.uniform(1, 6, m.numTotal)  # nonzero wall values exercise the su term
+    su = fcg.uniform(1, 7, m.numCells)
+    a, su_g = c.laplacian(mu, phi, su)
+    a_o, su_o = oracle.laplacian(oracle_mesh(m), oracle_csr(m), mu, phi, su)
+    assert np.array_equal(a, a_o)
+    assert np.array_equal(su_g, su_o)
+
+
+@pytest.mark.parametrize("name", MESHES)
+def test_facefluxmass_bit_exact(name):
+    m, c = ctx_for(name)
+    f = seeded_fields(m)
+    a, su, fm = c.facefluxmass(**f)
+    a_o, su_o, fm_o = oracle.facefluxmass(oracle_mesh(m), oracle_csr(m), *f.values())
+    assert np.array_equal(a, a_o)
+    assert np.array_equal(su, su_o)
+    assert np.array_equal(fm, fm_o)
+
+
+@pytest.mark.parametrize("name", MESHES)
+def test_fluxmc_bit_exact(name):
+    m, c = ctx_for(name)
+    f = seeded_fields(m)
+    flm = fcg.uniform(4, 8, m.numInnerFaces)
+    su, fm = c.fluxmc(f["dPdxi"], f["apu"], f["den"], flm)
+    su_o, fm_o = oracle.fluxmc(oracle_mesh(m), f["dPdxi"], f["apu"], f["den"], flm)
+    assert np.array_equal(su, su_o)
+    assert np.array_equal(fm, fm_o)
+
+
+@pytest.mark.parametrize("name", MESHES)
+@pytest.mark.parametrize("nigrad", [1, 3])
+def test_grad_gauss_bit_exact(name, nigrad):
+    m, c = ctx_for(name)
+    phi = fcg.uniform(2, 1, m.numTotal)
+    g = c.grad(phi, "gauss", nigrad=nigrad)
+    assert np.array_equal(g, oracle.grad_gauss(oracle_mesh(m), phi, nigrad=nigrad))
+
+
+@pytest.mark.parametrize("name", MESHES)
+def test_grad_gauss_corrected_and_lsq_bit_exact(name):
+    m, c = ctx_for(name)
+    om = oracle_mesh(m)
+    phi = fcg.uniform(2, 2, m.numTotal)
+    g0 = fcg.uniform(2, 3, 3 * m.numCells).reshape(-1, 3)
+    gc = c.grad(phi, "gauss_corrected", dphidxi=g0)
+    assert np.array_equal(gc, oracle.grad_gauss(om, phi, corrected=True, dphidxi_in=g0))
+    d = c.grad_lsq_matrix()
+    d_o = oracle.grad_lsq_matrix(om)
+    assert np.array_equal(d, d_o)
+    assert np.array_equal(c.grad(phi, "lsq"), oracle.grad_lsq(om, phi, d_o))
+
+
+@pytest.mark.parametrize("name", MESHES)
+def test_bpres_bit_exact(name):
+    m, c = ctx_for(name)
+    om = oracle_mesh(m)
+    p = fcg.uniform(3, 1, m.numTotal)
+    g = fcg.uniform(3, 2, 3 * m.numCells).reshape(-1, 3)
+    for stage in (1, 2):
+        assert np.array_equal(c.bpres(p, g, stage), oracle.bpres(om, p, g, stage))
+
+
+@pytest.mark.parametrize("name", MESHES)
+def test_spmv_matches_oracle(name):
+    m, c = ctx_for(name)
+    a, _ = c.laplacian(*poisson_system(m)[:2], np.zeros(m.numCells))
+    x = fcg.uniform(9, 9, m.numCells)
+    y = c.spmv(a, x)
+    y_o = oracle.spmv(oracle_csr(m), a, x)
+    assert rel(y, y_o) < 1e-14
+
+
+def _system(m, c):
+    mu, phi, su = poisson_system(m)
+    a, su = c.laplacian(mu, phi, su)
+    return a, su
+
+
+@pytest.mark.parametrize("name", ["hex8", "cavity", "pitzdaily"])
+@pytest.mark.parametrize("kind", ["dpcg", "iccg", "bicgstab"])
+def test_solver_fixed_sweeps_match_oracle(name, kind):
+    """Same number of sweeps (sor = 0 never stops early): only rounding differs."""
+    m, c = ctx_for(name)
+    a, su = _system(m, c)
+    K = 25
+    r = getattr(c, kind)(a, su, np.zeros(m.numCells), 0.0, K)
+    o = getattr(oracle, kind)(oracle_csr(m), a, su, np.zeros(m.numCells), 0.0, K)
+    assert r.iters == o.iters == K
+    assert abs(r.res0 - o.res0) <= 1e-13 * o.res0
+    assert rel(r.fi, o.fi) < 1e-10
+    assert rel(r.res, o.res) < 1e-8  # the residual itself is small: absolute drift shows
+    assert r.resor == pytest.approx(o.resor, rel=1e-13)
+
+
+@pytest.mark.parametrize("name", ["hex12_u", "cavity", "pitzdaily"])
+@pytest.mark.parametrize("kind", ["dpcg", "iccg", "bicgstab"])
+def test_solver_converged_matches_oracle(name, kind):
+    m, c = ctx_for(name)
+    a, su = _system(m, c)
+    r = getattr(c, kind)(a, su, np.zeros(m.numCells), 1e-8, 5000)
+    o = getattr(oracle, kind)(oracle_csr(m), a, su, np.zeros(m.numCells), 1e-8, 5000)
+    assert r.converged and o.iters < 5000
+    assert abs(r.iters - o.iters) <= 1
+    if r.iters == o.iters:
+        assert rel(r.fi, o.fi) < 1e-10
+    assert r.resl / r.res0 < 1e-8
+    assert r.l2_rel < 1e-6
+
+
+def test_reference_5x5_traces_on_gpu():
+    """tests/test_sparse_solvers.f90 replayed through the C ABI on a dense 5x5 'mesh'."""
+    g = json.load(open(os.path.join(GOLDEN, "sparse_solvers.json")))
+    n = 5
+    pairs = [(i, j) for i in range(1, n + 1) for j in range(i + 1, n + 1)]
+    owner = np.array([p[0] for p in pairs], np.int32)
+    nb = np.array([p[1] for p in pairs], np.int32)
+    nf = len(pairs)
+    ones = np.ones(nf)
+    m = fcg.Mesh(n, nf, nf, owner, nb, ones, ones * 0, ones * 0, ones * 0, ones * 0, ones * 0,
+                 np.arange(n, dtype=float), np.zeros(n), np.zeros(n), np.ones(n), ones * 0.5)
+    c = fcg.Context(m)
+    io, ja, dg, _, _ = c.create_csr()
+    assert list(io) == g["ioffset"] and list(ja) == g["ja"] and list(dg) == g["diag"]
+    c.set_solver_options(oracle.small_test(), early_exit=False)
+    f32 = lambda k, t: np.array([np.float32(v) for v in g[t][k]], np.float32).astype(np.float64)
+    expected = open(os.path.join(GOLDEN, "sparse_solvers_output.txt")).read()
+    blocks = expected.split("solver:")[1:]
+
+    def parse(block):
+        lines = [l for l in block.splitlines() if "iter =" in l]
+        return np.array([[float(l.split("resl =")[1].split()[0]), float(l.split("rsm =")[1])]
+                         for l in lines])
+
+    x = np.zeros(n)
+    for kind, t, blk in (("bicgstab", "test1", blocks[0]), ("iccg", "test2", blocks[1])):
+        r = getattr(c, kind)(f32("a", t), f32("b", t), x, oracle.tol(), 100, want_trace=True)
+        exp = parse(blk)
+        assert r.iters == len(exp)
+        big = exp[:, 0] > 1e-10  # rounding-dominated tails are not comparable digit by digit
+        assert np.allclose(r.trace[big], exp[big], rtol=6e-4)
+        x = r.fi
+    r = c.dpcg(f32("a", "test2"), f32("b", "test2"), x, oracle.tol(), 100, want_trace=True)
+    assert r.iters <= 6
+    assert np.allclose(np.round(r.fi, 2), [float(v) for v in g["test2"]["xa"]], atol=0.011)
+    c.close()
+
+
+def test_solver_edge_cases():
+    m, c = ctx_for("hex8")
+    a, su = _system(m, c)
+    # zero right-hand side from zero start: res0 = 0 < tol returns at once; resor untouched
+    r = c.dpcg(a, np.zeros(m.numCells), np.zeros(m.numCells), 1e-8, 100)
+    assert r.iters == 0 and r.resor is None and r.res0 == 0.0
+    # nsw caps the sweeps
+    r = c.iccg(a, su, np.zeros(m.numCells), 1e-30, 3)
+    assert r.iters == 3 and not r.converged
+    # nsw = 0: no sweep at all
+    r = c.bicgstab(a, su, np.zeros(m.numCells), 1e-8, 0)
+    assert r.iters == 0
+    # warm start from a converged solution converges in no more sweeps
+    r1 = c.dpcg(a, su, np.zeros(m.numCells), 1e-8, 2000)
+    r2 = c.dpcg(a, su, r1.fi, 1e-8, 2000)
+    assert r2.res0 < 1e-6 * r1.res0
+
+
+def test_device_arrays_in_place():
+    torch = pytest.importorskip("torch")
+    m, c = ctx_for("cavity")
+    a, su = _system(m, c)
+    r_host = c.dpcg(a, su, np.zeros(m.numCells), 1e-8, 2000)
+    ta, tsu = torch.from_numpy(a).cuda(), torch.from_numpy(su).cuda()
+    r_dev = c.dpcg(ta, tsu, torch.zeros(m.numCells, dtype=torch.float64, device="cuda"), 1e-8, 2000)
+    assert r_dev.iters == r_host.iters
+    assert np.array_equal(r_dev.fi.cpu().numpy(), r_host.fi)
+
+
+def test_errors_are_reported():
+    from freecappuccino_gb300 import _lib
+    m = hex_mesh(4)
+    bad = fcg.Mesh(**{**m.__dict__, "neighbour": m.neighbour.copy()})
+    bad.neighbour[3] = m.numCells + 7
+    with pytest.raises(_lib.FcgError) as e:
+        fcg.Context(bad)
+    assert e.value.status == _lib.FCG_ERR_INDEX
