@@ -822,9 +822,9 @@ extern "C" int fcg_set_solver_options(fcg_context *c, double small, int early_ex
 
 extern "C" int fcg_get_solver_trace(fcg_context *c, double *out, int max_count, int *count) {
   if (!c || !c->ks) return FCG_ERR_STATE;
-  int it = c->ks->hS->iter;
-  int m = std::min(std::min(it, max_count), c->ks->nsw_cap);
-  if (count) *count = m;
+  int avail = std::min(c->ks->hS->iter, c->ks->nsw_cap);
+  int m = std::min(avail, max_count);
+  if (count) *count = avail;
   if (out && m > 0)
     FCG_CUDA_TRY(c, cudaMemcpy(out, c->ks->trace.p, sizeof(double) * 2 * m, cudaMemcpyDeviceToHost));
   return FCG_OK;

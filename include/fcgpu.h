@@ -188,7 +188,8 @@ int fcg_bicgstab(fcg_context *ctx, const double *a, const double *su, double *fi
 int fcg_set_solver_options(fcg_context *ctx, double small, int early_exit);
 
 /* Per-sweep (resl, rsm) pairs of the last solve -- what the reference prints per
- * sweep when ltest is set (dpcg.f90:141). */
+ * sweep when ltest is set (dpcg.f90:141).  *count receives the number available;
+ * at most max_count pairs are copied to resl_rsm (which may be NULL). */
 int fcg_get_solver_trace(fcg_context *ctx, double *resl_rsm, int max_count, int *count);
 
 /* y = A x (the matvec of dpcg.f90:105-110) with CSR values a[nnz]; a == NULL reuses

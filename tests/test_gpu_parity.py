@@ -139,12 +139,20 @@ def test_solver_fixed_sweeps_match_oracle(name, kind):
     assert r.iters == o.iters == K
     assert abs(r.res0 - o.res0) <= 1e-13 * o.res0
     assert rel(r.fi, o.fi) < 1e-10
-    assert rel(r.res, o.res) < 1e-8  # the residual itself is small: absolute drift shows
+    # the residual may already sit at rounding level: compare on the scale of su
+    assert np.abs(r.res - o.res).max() < 1e-10 * np.abs(su).max()
     assert r.resor == pytest.approx(o.resor, rel=1e-13)
 
 
-@pytest.mark.parametrize("name", ["hex12_u", "cavity", "pitzdaily"])
-@pytest.mark.parametrize("kind", ["dpcg", "iccg", "bicgstab"])
+# The reference's BiCGStab(DILU) stagnates on the cavity and pitzDaily Poisson systems
+# (the oracle stops near 1e-5 and 2e-3 after 5000 sweeps), so its convergence is checked
+# on the hex meshes only; the fixed-sweep test above covers it on every mesh.
+CONVERGED_CASES = [(n, k) for n in ("hex12_u", "hex8", "cavity", "pitzdaily")
+                   for k in ("dpcg", "iccg", "bicgstab")
+                   if not (k == "bicgstab" and n in ("cavity", "pitzdaily"))]
+
+
+@pytest.mark.parametrize("name,kind", CONVERGED_CASES)
 def test_solver_converged_matches_oracle(name, kind):
     m, c = ctx_for(name)
     a, su = _system(m, c)
