@@ -83,6 +83,8 @@ _PROTOS = {
     "fcg_set_solver_options": (C.c_int, [_CTX, C.c_double, C.c_int]),
     "fcg_get_solver_trace": (C.c_int, [_CTX, _vp, C.c_int, _ip]),
     "fcg_spmv": (C.c_int, [_CTX, _vp, _vp, _vp]),
+    "fcg_dpcg_noalloc": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_double,
+                                   C.c_int, _dp, C.POINTER(SolveReport), _vp]),
     # synthetic inputs (include/fcgpu_meshgen.h)
     "fcg_hex_mesh_sizes": (C.c_int, [C.c_int, _ip, _ip, _ip, _ip]),
     "fcg_hex_mesh_build": (C.c_int, [C.c_int, C.c_double, C.c_ulonglong, _vp, _vp, _vp, _vp,

@@ -192,6 +192,23 @@ int fcg_set_solver_options(fcg_context *ctx, double small, int early_exit);
  * at most max_count pairs are copied to resl_rsm (which may be NULL). */
 int fcg_get_solver_trace(fcg_context *ctx, double *resl_rsm, int max_count, int *count);
 
+/* No counterpart in the reference.  dpcg for callers that cannot allocate device
+ * memory -- a host code whose GPU memory is all reserved by its own pool, or a loop
+ * whose rules forbid allocation after start-up.  It needs no context and allocates
+ * nothing: every array is the caller's DEVICE array (the reference's 1-based CSR
+ * ioffset[numCells+1], ja[nnz], diag[numCells], values a[nnz], su[numCells], fi
+ * in/out, res out), and the work vectors sit in one file-scope device array sized for
+ * at most FCG_NOALLOC_MAX_CELLS cells (about 6.4 MB, held by every GPU that loads the
+ * library until exit).  Larger systems and host arrays return FCG_ERR_ARG.  All calls
+ * share that array: calls that overlap on the GPU race.  The first call on a device
+ * looks up the array's address (cudaGetSymbolAddress) with that device current; make
+ * it before any stream capture.  Work runs on cuda_stream (NULL = legacy stream); the
+ * call returns when the solve is done. */
+#define FCG_NOALLOC_MAX_CELLS 262144
+int fcg_dpcg_noalloc(int numCells, const int *ioffset, const int *ja, const int *diag,
+                     const double *a, const double *su, double *fi, double *res, double sor,
+                     int nsw, double *resor, fcg_solve_report *rep, void *cuda_stream);
+
 /* y = A x (the matvec of dpcg.f90:105-110) with CSR values a[nnz]; a == NULL reuses
  * the matrix of the previous solve or spmv call. */
 int fcg_spmv(fcg_context *ctx, const double *a, const double *x, double *y);
