@@ -212,7 +212,13 @@ def main():
                     help="sweep count used by the reference arm when none is recorded")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--solver", default="dpcg", choices=["dpcg", "iccg", "bicgstab"])
+    ap.add_argument("--no-graph", action="store_true",
+                    help="host-driven sweep loop instead of the CUDA-graph WHILE loop")
     args = ap.parse_args()
+    if args.no_graph:
+        os.environ["FCG_NO_GRAPH"] = "1"
+
     ws, rank, local = dist_init()
     if args.impl == "reference":
         run_reference(args, ws, rank)
@@ -242,8 +248,10 @@ def main():
         fi0 = torch.zeros(n, dtype=torch.float64, device=dev)
     stream.synchronize()
 
+    solver = getattr(ctx, args.solver)
+
     def solve():
-        return ctx.dpcg(a_d, su_d, fi0, TOL, NSW, want_res=False)
+        return solver(a_d, su_d, fi0, TOL, NSW, want_res=False)
 
     for _ in range(args.warmup):
         r = solve()
@@ -271,14 +279,15 @@ def main():
     y = torch.empty_like(x)
     ctx.spmv(None, x, y)
     torch.cuda.synchronize()
-    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps = 20
-    s0.record(stream)
-    for _ in range(reps):
+    # one event pair per launch, so host-side gaps between launches are not counted
+    pairs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+             for _ in range(20)]
+    for s0, s1 in pairs:
+        s0.record(stream)
         ctx.spmv(None, x, y)
-    s1.record(stream)
+        s1.record(stream)
     torch.cuda.synchronize()
-    t_spmv = s0.elapsed_time(s1) * 1e-3 / reps
+    t_spmv = statistics.median(s0.elapsed_time(s1) for s0, s1 in pairs) * 1e-3
     peak, peak_kind = peaks()
     achieved = spmv_bytes(n, nnz) / t_spmv / 1e9
     traffic = None
@@ -326,7 +335,7 @@ def main():
                 "data": "synthetic: seeded jittered hex mesh and U(-1,1)*vol right-hand side",
                 "config": {"workload": f"pressure Poisson {N}^3 jittered hex ({n} cells, nnz {nnz}), "
                                        "solved to L1-relative 1e-8",
-                           "method": "dpcg_fp64", "N": N, "cells": n, "nnz": nnz,
+                           "method": f"{args.solver}_fp64", "N": N, "cells": n, "nnz": nnz,
                            "jitter": JITTER, "tolerance": TOL, "sweeps": iters,
                            "l2": "inputs larger than L2 (matrix 1.4 GB, vectors 134 MB each)",
                            "parallelism": f"replicas x{ws}"},

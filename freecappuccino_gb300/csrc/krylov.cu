@@ -46,8 +46,15 @@ struct Scal {
   unsigned int body_count;  // executions of the loop body, counted independently of iter
 };
 
+// Grid of each reduction kernel: one full wave of resident blocks on every SM (from the
+// occupancy calculator), so no kernel runs a partial second wave.
+struct Grids {
+  int init, p, spmv, update, dot, bdot, bp, bspmv1, bupd1, bspmv2, bupd2, fin, plain;
+};
+
 struct KrylovState {
   int n = 0, G = 0, nsw_cap = 0;
+  Grids gr{};
   unsigned bind_gen = 0;
   long long nnz = 0, sell_len = 0;
   DBuf vec;  // all vectors
@@ -206,7 +213,7 @@ __device__ __forceinline__ double sell_row(const SellView &s, const double *__re
   for (int slice = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);        \
        slice < (s).nslices; slice += (int)(((long long)gridDim.x * blockDim.x) >> 5))
 
-__global__ void k_spmv(SellView s, int n, const double *__restrict__ val,
+__global__ void __launch_bounds__(kTPB, 8) k_spmv(SellView s, int n, const double *__restrict__ val,
                        const double *__restrict__ x, double *__restrict__ y) {
   FCG_SLICE_LOOP(slice, lane, s) {
     int r = slice * 32 + lane;
@@ -219,7 +226,7 @@ __global__ void k_spmv(SellView s, int n, const double *__restrict__ val,
 // Solver kernels
 // ---------------------------------------------------------------------------
 // res = su - A x, res0 = sum|res| (dpcg.f90:51-64); DPCG also sk = sum res^2/a(diag).
-__global__ void k_init(SellView s, int n, const double *__restrict__ val,
+__global__ void __launch_bounds__(kTPB, 8) k_init(SellView s, int n, const double *__restrict__ val,
                        const double *__restrict__ su, const double *__restrict__ x,
                        double *__restrict__ res, const double *__restrict__ invd, Scal *S,
                        double *partials, int kind) {
@@ -255,7 +262,7 @@ __global__ void k_init(SellView s, int n, const double *__restrict__ val,
 }
 
 // Stop test shared by all solvers (dpcg.f90:130-142); thread 0 of the last block.
-__device__ void finish_sweep(Scal *S, double resl, double *trace, cudaGraphConditionalHandle h,
+__device__ __noinline__ void finish_sweep(Scal *S, double resl, double *trace, cudaGraphConditionalHandle h,
                              int use_cond) {
   int it = S->iter + 1;
   S->iter = it;
@@ -275,8 +282,25 @@ __device__ void finish_sweep(Scal *S, double resl, double *trace, cudaGraphCondi
   }
 }
 
+// Scalar tail of k_cg_update, run by one thread: s0, sk, beta and the stop test.
+__device__ __noinline__ void cg_close_sweep(Scal *S, double resl, double sk_new, double *trace,
+                                            cudaGraphConditionalHandle h, int use_cond,
+                                            int kind) {
+  S->s0 = S->sk;  // dpcg.f90:132
+  if (kind == SK_DPCG) {
+    S->sk = sk_new;
+    S->bet = sk_new / S->s0;  // next sweep's beta (dpcg.f90:95)
+  }
+  if (S->status) {
+    S->done = 1;
+    if (use_cond) cudaGraphSetConditional(h, 0);
+    return;
+  }
+  finish_sweep(S, resl, trace, h, use_cond);
+}
+
 // pk = M^-1 res + bet*pk: Jacobi (dpcg.f90:85-100) or z from the sweeps (iccg.f90:278).
-__global__ void k_cg_p(int n, const double *__restrict__ res, const double *__restrict__ invd,
+__global__ void __launch_bounds__(kTPB, 8) k_cg_p(int n, const double *__restrict__ res, const double *__restrict__ invd,
                        const double *__restrict__ z, double *__restrict__ pk, const Scal *S,
                        int kind) {
   if (solve_done(S)) return;
@@ -288,7 +312,7 @@ __global__ void k_cg_p(int n, const double *__restrict__ res, const double *__re
 }
 
 // qk = A pk, pkapk = sum pk*qk, alf = sk/pkapk (dpcg.f90:105-121).
-__global__ void k_cg_spmv(SellView s, int n, const double *__restrict__ val,
+__global__ void __launch_bounds__(kTPB, 8) k_cg_spmv(SellView s, int n, const double *__restrict__ val,
                           const double *__restrict__ pk, double *__restrict__ qk, Scal *S,
                           double *partials) {
   if (solve_done(S)) return;
@@ -310,7 +334,7 @@ __global__ void k_cg_spmv(SellView s, int n, const double *__restrict__ val,
 
 // fi += alf*pk, res -= alf*qk, resl = sum|res| (dpcg.f90:124-142); DPCG also forms
 // the next sk and beta in the same pass.
-__global__ void k_cg_update(int n, double *__restrict__ x, double *__restrict__ res,
+__global__ void __launch_bounds__(kTPB, 8) k_cg_update(int n, double *__restrict__ x, double *__restrict__ res,
                             const double *__restrict__ pk, const double *__restrict__ qk,
                             const double *__restrict__ invd, Scal *S, double *partials,
                             double *trace, cudaGraphConditionalHandle h, int use_cond, int kind) {
@@ -328,23 +352,12 @@ __global__ void k_cg_update(int n, double *__restrict__ x, double *__restrict__ 
     v[0] += fabs(r);
     if (kind == SK_DPCG) v[1] += r * (r * invd[i]);
   }
-  if (reduce_commit<2>(v, partials, &S->ticket[2]) && threadIdx.x == 0) {
-    S->s0 = S->sk;  // dpcg.f90:132
-    if (kind == SK_DPCG) {
-      S->sk = v[1];
-      S->bet = v[1] / S->s0;  // next sweep's beta (dpcg.f90:95)
-    }
-    if (S->status) {
-      S->done = 1;
-      if (use_cond) cudaGraphSetConditional(h, 0);
-      return;
-    }
-    finish_sweep(S, v[0], trace, h, use_cond);
-  }
+  if (reduce_commit<2>(v, partials, &S->ticket[2]) && threadIdx.x == 0)
+    cg_close_sweep(S, v[0], v[1], trace, h, use_cond, kind);
 }
 
 // ICCG: sk = sum res*z, bet = sk/s0 (iccg.f90:268-273).
-__global__ void k_cg_dot(int n, const double *__restrict__ res, const double *__restrict__ z,
+__global__ void __launch_bounds__(kTPB, 8) k_cg_dot(int n, const double *__restrict__ res, const double *__restrict__ z,
                          Scal *S, double *partials) {
   if (solve_done(S)) return;
   double v[1] = {0.0};
@@ -413,7 +426,7 @@ __global__ void k_factor_level(const int *__restrict__ rows, int count,
 
 // --- BiCGStab sweep (bicgstab.f90:99-224) -------------------------------------
 // bet = sum res*reso; om = bet*gam/(alf*beto+small); beto = bet
-__global__ void k_bi_dot1(int n, const double *__restrict__ res, const double *__restrict__ reso,
+__global__ void __launch_bounds__(kTPB, 8) k_bi_dot1(int n, const double *__restrict__ res, const double *__restrict__ reso,
                           Scal *S, double *partials) {
   if (solve_done(S)) return;
   double v[1] = {0.0};
@@ -427,7 +440,7 @@ __global__ void k_bi_dot1(int n, const double *__restrict__ res, const double *_
 }
 
 // pk = res + om*(pk - alf*uk)
-__global__ void k_bi_p(int n, const double *__restrict__ res, const double *__restrict__ uk,
+__global__ void __launch_bounds__(kTPB, 8) k_bi_p(int n, const double *__restrict__ res, const double *__restrict__ uk,
                        double *__restrict__ pk, const Scal *S) {
   if (solve_done(S)) return;
   const double om = __ldcg(&S->om), alf = __ldcg(&S->alf);
@@ -435,7 +448,7 @@ __global__ void k_bi_p(int n, const double *__restrict__ res, const double *__re
 }
 
 // uk = A zk; gam = bet / sum uk*reso
-__global__ void k_bi_spmv1(SellView s, int n, const double *__restrict__ val,
+__global__ void __launch_bounds__(kTPB, 8) k_bi_spmv1(SellView s, int n, const double *__restrict__ val,
                            const double *__restrict__ zk, const double *__restrict__ reso,
                            double *__restrict__ uk, Scal *S, double *partials) {
   if (solve_done(S)) return;
@@ -455,7 +468,7 @@ __global__ void k_bi_spmv1(SellView s, int n, const double *__restrict__ val,
 }
 
 // fi += gam*zk; res -= gam*uk
-__global__ void k_bi_upd1(int n, double *__restrict__ x, double *__restrict__ res,
+__global__ void __launch_bounds__(kTPB, 8) k_bi_upd1(int n, double *__restrict__ x, double *__restrict__ res,
                           const double *__restrict__ zk, const double *__restrict__ uk,
                           const Scal *S) {
   if (solve_done(S)) return;
@@ -467,7 +480,7 @@ __global__ void k_bi_upd1(int n, double *__restrict__ x, double *__restrict__ re
 }
 
 // vk = A zk; alf = sum vk*res / (sum vk*vk + small)
-__global__ void k_bi_spmv2(SellView s, int n, const double *__restrict__ val,
+__global__ void __launch_bounds__(kTPB, 8) k_bi_spmv2(SellView s, int n, const double *__restrict__ val,
                            const double *__restrict__ zk, const double *__restrict__ res,
                            double *__restrict__ vk, Scal *S, double *partials) {
   if (solve_done(S)) return;
@@ -487,8 +500,18 @@ __global__ void k_bi_spmv2(SellView s, int n, const double *__restrict__ val,
   }
 }
 
+__device__ __noinline__ void bi_close_sweep(Scal *S, double resl, double *trace,
+                                            cudaGraphConditionalHandle h, int use_cond) {
+  if (S->status) {
+    S->done = 1;
+    if (use_cond) cudaGraphSetConditional(h, 0);
+    return;
+  }
+  finish_sweep(S, resl, trace, h, use_cond);
+}
+
 // fi += alf*zk; res -= alf*vk; resl = sum|res|; stop test
-__global__ void k_bi_upd2(int n, double *__restrict__ x, double *__restrict__ res,
+__global__ void __launch_bounds__(kTPB, 8) k_bi_upd2(int n, double *__restrict__ x, double *__restrict__ res,
                           const double *__restrict__ zk, const double *__restrict__ vk, Scal *S,
                           double *partials, double *trace, cudaGraphConditionalHandle h,
                           int use_cond) {
@@ -505,18 +528,12 @@ __global__ void k_bi_upd2(int n, double *__restrict__ x, double *__restrict__ re
     res[i] = r;
     v[0] += fabs(r);
   }
-  if (reduce_commit<1>(v, partials, &S->ticket[6]) && threadIdx.x == 0) {
-    if (S->status) {
-      S->done = 1;
-      if (use_cond) cudaGraphSetConditional(h, 0);
-      return;
-    }
-    finish_sweep(S, v[0], trace, h, use_cond);
-  }
+  if (reduce_commit<1>(v, partials, &S->ticket[6]) && threadIdx.x == 0)
+    bi_close_sweep(S, v[0], trace, h, use_cond);
 }
 
 // Final FP64 check: ||su - A x||^2 and ||su||^2.
-__global__ void k_final(SellView s, int n, const double *__restrict__ val,
+__global__ void __launch_bounds__(kTPB, 8) k_final(SellView s, int n, const double *__restrict__ val,
                         const double *__restrict__ su, const double *__restrict__ x, Scal *S,
                         double *partials) {
   double v[2] = {0.0, 0.0};
@@ -581,6 +598,28 @@ static int ensure_state(fcg_context *c, int nsw) {
     k->nnz = c->nnz;
     k->sell_len = c->sell_len;
     k->G = G;
+    auto occ = [&](const void *fn) {
+      int b = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, kTPB, 0) != cudaSuccess) {
+        cudaGetLastError();
+        b = 1;
+      }
+      return c->num_sms * std::max(1, std::min(b, 8));
+    };
+    Grids &g = k->gr;
+    g.init = occ((const void *)k_init);
+    g.p = occ((const void *)k_cg_p);
+    g.spmv = occ((const void *)k_cg_spmv);
+    g.update = occ((const void *)k_cg_update);
+    g.dot = occ((const void *)k_cg_dot);
+    g.bdot = occ((const void *)k_bi_dot1);
+    g.bp = occ((const void *)k_bi_p);
+    g.bspmv1 = occ((const void *)k_bi_spmv1);
+    g.bupd1 = occ((const void *)k_bi_upd1);
+    g.bspmv2 = occ((const void *)k_bi_spmv2);
+    g.bupd2 = occ((const void *)k_bi_upd2);
+    g.fin = occ((const void *)k_final);
+    g.plain = occ((const void *)k_spmv);
     k->bind_gen = c->bind_gen;
     k->matrix_loaded = false;
   }
@@ -628,30 +667,30 @@ static void launch_sweeps(fcg_context *c, cudaStream_t st, const Level &lv, bool
 static void enqueue_sweep(fcg_context *c, cudaStream_t st, int kind, cudaGraphConditionalHandle h,
                           int use_cond) {
   KrylovState *k = c->ks;
-  const int n = c->n, G = k->G;
+  const int n = c->n;
   const SellView &s = c->sv;
   double *tr = k->trace.as<double>();
   if (kind == SK_DPCG || kind == SK_ICCG) {
     if (kind == SK_ICCG) {
       launch_sweeps(c, st, c->lf, true, k->res, k->zk);
       launch_sweeps(c, st, c->lb, false, nullptr, k->zk);
-      k_cg_dot<<<G, kTPB, 0, st>>>(n, k->res, k->zk, k->S, k->partials);
+      k_cg_dot<<<k->gr.dot, kTPB, 0, st>>>(n, k->res, k->zk, k->S, k->partials);
     }
-    k_cg_p<<<G, kTPB, 0, st>>>(n, k->res, k->invd, k->zk, k->pk, k->S, kind);
-    k_cg_spmv<<<G, kTPB, 0, st>>>(s, n, k->sval, k->pk, k->qk, k->S, k->partials);
-    k_cg_update<<<G, kTPB, 0, st>>>(n, k->x, k->res, k->pk, k->qk, k->invd, k->S, k->partials,
+    k_cg_p<<<k->gr.p, kTPB, 0, st>>>(n, k->res, k->invd, k->zk, k->pk, k->S, kind);
+    k_cg_spmv<<<k->gr.spmv, kTPB, 0, st>>>(s, n, k->sval, k->pk, k->qk, k->S, k->partials);
+    k_cg_update<<<k->gr.update, kTPB, 0, st>>>(n, k->x, k->res, k->pk, k->qk, k->invd, k->S, k->partials,
                                      tr, h, use_cond, kind);
   } else {
-    k_bi_dot1<<<G, kTPB, 0, st>>>(n, k->res, k->reso, k->S, k->partials);
-    k_bi_p<<<G, kTPB, 0, st>>>(n, k->res, k->uk, k->pk, k->S);
+    k_bi_dot1<<<k->gr.bdot, kTPB, 0, st>>>(n, k->res, k->reso, k->S, k->partials);
+    k_bi_p<<<k->gr.bp, kTPB, 0, st>>>(n, k->res, k->uk, k->pk, k->S);
     launch_sweeps(c, st, c->lf, true, k->pk, k->zk);
     launch_sweeps(c, st, c->lb, false, nullptr, k->zk);
-    k_bi_spmv1<<<G, kTPB, 0, st>>>(s, n, k->sval, k->zk, k->reso, k->uk, k->S, k->partials);
-    k_bi_upd1<<<G, kTPB, 0, st>>>(n, k->x, k->res, k->zk, k->uk, k->S);
+    k_bi_spmv1<<<k->gr.bspmv1, kTPB, 0, st>>>(s, n, k->sval, k->zk, k->reso, k->uk, k->S, k->partials);
+    k_bi_upd1<<<k->gr.bupd1, kTPB, 0, st>>>(n, k->x, k->res, k->zk, k->uk, k->S);
     launch_sweeps(c, st, c->lf, true, k->res, k->zk);
     launch_sweeps(c, st, c->lb, false, nullptr, k->zk);
-    k_bi_spmv2<<<G, kTPB, 0, st>>>(s, n, k->sval, k->zk, k->res, k->vk, k->S, k->partials);
-    k_bi_upd2<<<G, kTPB, 0, st>>>(n, k->x, k->res, k->zk, k->vk, k->S, k->partials, tr, h,
+    k_bi_spmv2<<<k->gr.bspmv2, kTPB, 0, st>>>(s, n, k->sval, k->zk, k->res, k->vk, k->S, k->partials);
+    k_bi_upd2<<<k->gr.bupd2, kTPB, 0, st>>>(n, k->x, k->res, k->zk, k->vk, k->S, k->partials, tr, h,
                                    use_cond);
   }
 }
@@ -727,8 +766,7 @@ static int run_solver(fcg_context *c, int kind, const double *a, const double *s
   init.trace_cap = k->nsw_cap;
   *k->hS = init;
   FCG_CUDA_TRY(c, cudaMemcpyAsync(k->S, k->hS, sizeof(Scal), cudaMemcpyHostToDevice, c->stream));
-  const int G = k->G;
-  k_init<<<G, kTPB, 0, c->stream>>>(c->sv, c->n, k->sval, k->su, k->x, k->res, k->invd, k->S,
+  k_init<<<k->gr.init, kTPB, 0, c->stream>>>(c->sv, c->n, k->sval, k->su, k->x, k->res, k->invd, k->S,
                                     k->partials, kind);
   FCG_CHECK_LAUNCH(c, "k_init");
   if (kind == SK_BICG)
@@ -755,7 +793,7 @@ static int run_solver(fcg_context *c, int kind, const double *a, const double *s
       done = k->hS->done;
     }
   }
-  k_final<<<G, kTPB, 0, c->stream>>>(c->sv, c->n, k->sval, k->su, k->x, k->S, k->partials);
+  k_final<<<k->gr.fin, kTPB, 0, c->stream>>>(c->sv, c->n, k->sval, k->su, k->x, k->S, k->partials);
   FCG_CHECK_LAUNCH(c, "k_final");
   FCG_CUDA_TRY(c, cudaEventRecord(k->ev1, c->stream));
   FCG_CUDA_TRY(c, cudaMemcpyAsync(dfi, k->x, n1, cudaMemcpyDeviceToDevice, c->stream));
@@ -850,7 +888,7 @@ extern "C" int fcg_spmv(fcg_context *c, const double *a, const double *x, double
   bool hx, hy;
   if ((rc = stage_in(c, x, n1, 1, true, &dx, &hx))) return rc;
   if ((rc = stage_in(c, y, n1, 2, false, &dy, &hy))) return rc;
-  k_spmv<<<k->G, kTPB, 0, c->stream>>>(c->sv, c->n, k->sval, (const double *)dx, (double *)dy);
+  k_spmv<<<k->gr.plain, kTPB, 0, c->stream>>>(c->sv, c->n, k->sval, (const double *)dx, (double *)dy);
   FCG_CHECK_LAUNCH(c, "k_spmv");
   if ((rc = stage_out(c, y, dy, n1, hy))) return rc;
   if (hy) FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
