@@ -212,7 +212,8 @@ def main():
                     help="sweep count used by the reference arm when none is recorded")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2)
-    ap.add_argument("--solver", default="dpcg", choices=["dpcg", "iccg", "bicgstab"])
+    ap.add_argument("--solver", default="dpcg_mixed",
+                    choices=["dpcg_mixed", "dpcg", "iccg", "bicgstab"])
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven sweep loop instead of the CUDA-graph WHILE loop")
     args = ap.parse_args()
@@ -248,13 +249,13 @@ def main():
         fi0 = torch.zeros(n, dtype=torch.float64, device=dev)
     stream.synchronize()
 
-    solver = getattr(ctx, args.solver)
+    method = args.solver
 
-    def solve():
-        return solver(a_d, su_d, fi0, TOL, NSW, want_res=False)
+    def run(name):
+        return getattr(ctx, name)(a_d, su_d, fi0, TOL, NSW, want_res=False)
 
     for _ in range(args.warmup):
-        r = solve()
+        run(method)
     sampler = ClockSampler(local)
     sampler.start()
     barrier(ws)
@@ -264,22 +265,63 @@ def main():
     reports = []
     for e0, e1 in evs:
         e0.record(stream)
-        reports.append(solve())
+        reports.append(run(method))
         e1.record(stream)
     torch.cuda.synchronize()
     barrier(ws)
     clocks = sampler.stop()
     step_s = [e0.elapsed_time(e1) * 1e-3 for e0, e1 in evs]
     t_solve = reduce_max(ws, statistics.mean(step_s))
-    iters = reports[-1].iters
-    launches = sum(3 + 3 * r.iters for r in reports)
+    last = reports[-1]
+    iters = last.iters
+    per_solve_launches = {"dpcg": lambda it: 3 + 3 * it, "dpcg_mixed": lambda it: 6 + 5 * it}
+    launches = sum(per_solve_launches.get(method, lambda it: 3 + 3 * it)(r.iters) for r in reports)
+    x_method = last.fi.clone()
 
-    # Dominant kernel: the sliced-ELL SpMV, timed alone on the same stream (20 launches).
+    # Per-kernel device time of the method's sweep, CUDA events around each launch.
+    prof = ctx.profile_sweeps(20)
+    peak, peak_kind = peaks()
+    if method == "dpcg_mixed":
+        dom = "k_mx_spmv"
+        dom_bytes = 8 * nnz + 4 * (n + 1) + 8 * n  # FP32 values + int32 columns, FP32 x/y
+        sweep_bytes = dom_bytes + 36 * n           # + FP32 vector passes of one sweep
+        dom_desc = "k_mx_spmv (FP32 sliced-ELL SpMV of the scaled matrix + p.Ap, 256^3)"
+    else:
+        dom = "k_cg_spmv"
+        dom_bytes = spmv_bytes(n, nnz)
+        sweep_bytes = dpcg_iter_bytes(n, nnz)
+        dom_desc = "k_cg_spmv (FP64 sliced-ELL SpMV + p.Ap, 256^3)"
+    t_dom = prof[dom] * 1e-3
+    achieved = dom_bytes / t_dom / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        traffic = json.load(open(tp)).get(dom, {}).get(f"bytes_per_launch_{N}")
+    roof = {"kernel": dom_desc, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+            "algorithmic_bytes_per_launch": dom_bytes, "launch_ms": t_dom * 1e3,
+            "sweep_kernels_ms": prof}
+    sweep_gbs = sweep_bytes / (t_solve / max(iters, 1)) / 1e9
+
+    # Plain FP64 DPCG on the same system: the method the headline is compared with.
+    fp64 = None
+    if method != "dpcg":
+        run("dpcg")
+        t0e, t1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0e.record(stream)
+        r64 = run("dpcg")
+        t1e.record(stream)
+        torch.cuda.synchronize()
+        t64 = reduce_max(ws, t0e.elapsed_time(t1e) * 1e-3)
+        err = float((x_method - r64.fi).abs().max() / r64.fi.abs().max())
+        fp64 = {"dpcg_fp64_s": t64, "dpcg_fp64_sweeps": r64.iters, "speedup_vs_fp64": t64 / t_solve,
+                "max_rel_diff_vs_fp64_solution": err,
+                "fp64_sweep_GBps": dpcg_iter_bytes(n, nnz) / (t64 / r64.iters) / 1e9}
+
+    # Standalone FP64 SpMV (one event pair per launch: host gaps are not counted).
     x = torch.rand(n, dtype=torch.float64, device=dev)
     y = torch.empty_like(x)
     ctx.spmv(None, x, y)
-    torch.cuda.synchronize()
-    # one event pair per launch, so host-side gaps between launches are not counted
     pairs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
              for _ in range(20)]
     for s0, s1 in pairs:
@@ -288,18 +330,9 @@ def main():
         s1.record(stream)
     torch.cuda.synchronize()
     t_spmv = statistics.median(s0.elapsed_time(s1) for s0, s1 in pairs) * 1e-3
-    peak, peak_kind = peaks()
-    achieved = spmv_bytes(n, nnz) / t_spmv / 1e9
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "spmv_traffic.json")
-    if os.path.exists(tp):
-        d = json.load(open(tp))
-        traffic = d.get("bytes_per_launch_256")
-    roof = {"kernel": "k_spmv (sliced-ELL FP64 SpMV, 256^3)", "bound": "hbm",
-            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "peak_kind": peak_kind, "traffic": traffic,
-            "algorithmic_bytes_per_launch": spmv_bytes(n, nnz), "launch_ms": t_spmv * 1e3}
-    iter_gbs = dpcg_iter_bytes(n, nnz) / (t_solve / max(iters, 1)) / 1e9
+    spmv64 = {"kernel": "k_spmv (FP64)", "launch_ms": t_spmv * 1e3,
+              "achieved_GBps": spmv_bytes(n, nnz) / t_spmv / 1e9,
+              "frac": spmv_bytes(n, nnz) / t_spmv / 1e9 / peak}
 
     # End to end through the C ABI with pinned host buffers: copies inside the timed region.
     e2e_s = []
@@ -313,8 +346,9 @@ def main():
         rep = _lib.SolveReport()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        rc = lib.fcg_dpcg(ctx.h, a_h.data_ptr(), su_h.data_ptr(), fi_h.data_ptr(), None, TOL, NSW,
-                          C.byref(resor), C.byref(rep))
+        entry = lib.fcg_dpcg_mixed if method == "dpcg_mixed" else lib.fcg_dpcg
+        rc = entry(ctx.h, a_h.data_ptr(), su_h.data_ptr(), fi_h.data_ptr(), None, TOL, NSW,
+                   C.byref(resor), C.byref(rep))
         e1.record(stream)
         torch.cuda.synchronize()
         assert rc == 0, rc
@@ -331,20 +365,20 @@ def main():
     if rank == 0:
         line = {"metric": METRIC, "value": t_solve, "unit": "s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_solve * 1e3, "higher_is_better": False,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32 sweeps, f64 residual/updates" if method == "dpcg_mixed" else "f64",
                 "data": "synthetic: seeded jittered hex mesh and U(-1,1)*vol right-hand side",
                 "config": {"workload": f"pressure Poisson {N}^3 jittered hex ({n} cells, nnz {nnz}), "
-                                       "solved to L1-relative 1e-8",
-                           "method": f"{args.solver}_fp64", "N": N, "cells": n, "nnz": nnz,
+                                       "solved to L1-relative 1e-8 (true FP64 residual)",
+                           "method": method, "N": N, "cells": n, "nnz": nnz,
                            "jitter": JITTER, "tolerance": TOL, "sweeps": iters,
                            "l2": "inputs larger than L2 (matrix 1.4 GB, vectors 134 MB each)",
                            "parallelism": f"replicas x{ws}"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
                 "gpu_launches": launches,
-                "extra": {"dpcg_fp64_s": t_solve, "dpcg_sweeps": iters,
-                          "dpcg_iteration_GBps": iter_gbs, "dpcg_iteration_frac": iter_gbs / peak,
-                          "l2_rel_final": reports[-1].l2_rel, "resl_over_res0":
-                              reports[-1].resl / reports[-1].res0,
+                "extra": {"fp64_comparison": fp64, "spmv_fp64": spmv64,
+                          "sweep_GBps_algorithmic": sweep_gbs, "sweep_frac": sweep_gbs / peak,
+                          "l2_rel_final": last.l2_rel, "resl_over_res0": last.resl / last.res0,
                           "mesh_setup_s": t_mesh, "bind_s": t_bind, "step_s": step_s}}
         print(json.dumps(line), flush=True)
     ctx.close()

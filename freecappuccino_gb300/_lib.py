@@ -80,9 +80,13 @@ _PROTOS = {
                            C.POINTER(SolveReport)]),
     "fcg_bicgstab": (C.c_int, [_CTX, _vp, _vp, _vp, _vp, C.c_double, C.c_int, _dp,
                                C.POINTER(SolveReport)]),
+    "fcg_dpcg_mixed": (C.c_int, [_CTX, _vp, _vp, _vp, _vp, C.c_double, C.c_int, _dp,
+                                 C.POINTER(SolveReport)]),
     "fcg_set_solver_options": (C.c_int, [_CTX, C.c_double, C.c_int]),
     "fcg_get_solver_trace": (C.c_int, [_CTX, _vp, C.c_int, _ip]),
     "fcg_spmv": (C.c_int, [_CTX, _vp, _vp, _vp]),
+    "fcg_profile_sweeps": (C.c_int, [_CTX, C.c_int, _dp, C.c_int, _ip]),
+    "fcg_profile_unit_name": (C.c_char_p, [_CTX, C.c_int]),
     "fcg_dpcg_noalloc": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_double,
                                    C.c_int, _dp, C.POINTER(SolveReport), _vp]),
     # synthetic inputs (include/fcgpu_meshgen.h)

@@ -279,10 +279,13 @@ extern "C" int fcg_bind_mesh(fcg_context *c, const fcg_mesh_desc *m) {
   s.nslices = (int)t.sell_width.size();
   UP(s.ptr, t.sell_ptr.data(), t.sell_ptr.size());
   UP(s.width, t.sell_width.data(), t.sell_width.size());
-  UP(s.col, t.sell_col.data(), t.sell_col.size());
+  UP(s.kind, t.sell_kind.data(), t.sell_kind.size());
+  UP(s.offp, t.sell_offp.data(), t.sell_offp.size());
+  UP(s.off, t.sell_off.data(), t.sell_off.size());
   UP(s.src, t.sell_src.data(), t.sell_src.size());
   c->sell_maxw = t.sell_maxw;
   c->sell_len = t.sell_ptr.back();
+  c->sell_nuniform = t.sell_nuniform;
 
   const int *rows;
   c->lf.ptr = t.lf_ptr;

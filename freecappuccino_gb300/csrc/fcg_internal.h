@@ -53,15 +53,20 @@ struct MeshView {
   const int *cbf_ptr, *cbf_face;
 };
 
-// Sliced-ELL copy of the CSR pattern used by the solvers: slices of 32 rows, each
-// slice as wide as its longest row, stored column-major inside the slice so that a
-// warp reads one entry of 32 consecutive rows per load.
+// Sliced-ELL copy of the CSR pattern used by the solvers: slices of 32 rows stored
+// column-major inside the slice, so that a warp reads one slot of 32 consecutive rows
+// per load.  A uniform slice (kind 0) keeps one column offset per slot (off[offp+j]):
+// slot j of row r reads column r + off[offp+j], clamped into range, with value 0 where
+// the row has no such entry.  An explicit slice (kind 1) keeps 32 columns per slot at
+// off[offp + 32*j + lane] (pads: the row itself, value 0).
 struct SellView {
   int nslices;
-  const long long *ptr; // [nslices+1] element offset of each slice
-  const int *width;     // [nslices]
-  const int *col;       // [len] 0-based column (pads: the row itself)
-  const int *src;       // [len] CSR position of the entry (pads: -1)
+  const long long *ptr; // [nslices+1] value offset of each slice
+  const int *width;     // [nslices] slots per row
+  const int *kind;      // [nslices] 0 uniform, 1 explicit
+  const int *offp;      // [nslices] start of the slice's offsets or column block in off
+  const int *off;       // offsets (uniform) and explicit column blocks
+  const int *src;       // [len] CSR position of each value slot (-1: no entry)
 };
 
 struct Level {
@@ -99,7 +104,7 @@ struct fcg_context {
   fcg::MeshView mv{};
   fcg::SellView sv{};
   int sell_maxw = 0;
-  long long sell_len = 0;
+  long long sell_len = 0, sell_nuniform = 0;
   fcg::Level lf, lb;  // forward (lower) and backward (upper) level schedules
   const int *tpos = nullptr;  // CSR position of the transpose entry of every entry
 
@@ -127,8 +132,9 @@ struct HostTopology {
   std::vector<int> cb_ptr, cb_face, cb_slot, cb_type;
   std::vector<int> cbf_ptr, cbf_face;
   std::vector<long long> sell_ptr;
-  std::vector<int> sell_width, sell_col, sell_src;
+  std::vector<int> sell_width, sell_kind, sell_offp, sell_off, sell_src;
   int sell_maxw = 0;
+  long long sell_nuniform = 0;
   std::vector<int> lf_ptr, lf_rows, lb_ptr, lb_rows;
   std::vector<int> tpos;
 };

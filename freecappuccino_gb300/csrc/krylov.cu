@@ -31,7 +31,7 @@
 
 namespace fcg {
 
-enum SolverKind { SK_DPCG = 0, SK_ICCG = 1, SK_BICG = 2, SK_N = 3 };
+enum SolverKind { SK_DPCG = 0, SK_ICCG = 1, SK_BICG = 2, SK_MIXED = 3, SK_N = 4 };
 
 // Device-resident solver scalars.  Written by the last block of a reduction kernel,
 // read by the following kernels (stream order makes the writes visible).
@@ -44,12 +44,16 @@ struct Scal {
   int iter, nsw, done, converged, status, early, trace_cap, pad;
   unsigned int ticket[8];
   unsigned int body_count;  // executions of the loop body, counted independently of iter
+  // mixed precision (reliable updates)
+  double rr, rr_old, maxr, l1ratio, delta;
+  int ru, nupdates;
 };
 
 // Grid of each reduction kernel: one full wave of resident blocks on every SM (from the
 // occupancy calculator), so no kernel runs a partial second wave.
 struct Grids {
   int init, p, spmv, update, dot, bdot, bp, bspmv1, bupd1, bspmv2, bupd2, fin, plain;
+  int mstart, mspmv, mupd, mru1, mru2, mp;
 };
 
 struct KrylovState {
@@ -62,13 +66,21 @@ struct KrylovState {
          *qk = nullptr, *invd = nullptr, *d = nullptr, *reso = nullptr, *uk = nullptr,
          *vk = nullptr, *a = nullptr, *sval = nullptr, *partials = nullptr, *rtmp = nullptr;
   DBuf trace;
+  // mixed precision: FP32 copy of D^-1/2 A D^-1/2 in the sliced layout, the scaling
+  // D^-1/2 in FP64 and the FP32 inner vectors (correction y, residual r, direction p, Ap)
+  DBuf mixed;
+  double *s64 = nullptr;
+  float *sval32 = nullptr, *y32 = nullptr, *r32 = nullptr, *p32 = nullptr, *q32 = nullptr;
+  bool mixed_ready = false;
+  double ru_delta = 0.1;  // reliable update when ||r32|| drops below delta * its last true value
   Scal *S = nullptr;  // device
   Scal *hS = nullptr; // pinned host copy
   cudaStream_t cap = nullptr;
-  cudaGraphExec_t exec[SK_N] = {nullptr, nullptr, nullptr};
-  cudaGraph_t graph[SK_N] = {nullptr, nullptr, nullptr};
+  cudaGraphExec_t exec[SK_N] = {};
+  cudaGraph_t graph[SK_N] = {};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool matrix_loaded = false;
+  int last_kind = -1;
   double small = (double)1e-20f;  // parameters::small (modules_allocatable.f90:27)
   int early_exit = 1;
 };
@@ -86,6 +98,7 @@ void destroy_krylov(KrylovState *k) {
   if (k->S) cudaFree(k->S);
   k->vec.release();
   k->trace.release();
+  k->mixed.release();
   delete k;
 }
 
@@ -194,16 +207,31 @@ __global__ void k_sell_fill(SellView s, int n, const int *__restrict__ diag,
   }
 }
 
-// y = A x for the rows of one warp's slice; returns the row's sum.
-__device__ __forceinline__ double sell_row(const SellView &s, const double *__restrict__ val,
-                                           const double *__restrict__ x, int slice, int lane) {
-  long long base = s.ptr[slice] + lane;
-  int w = s.width[slice];
-  double acc = 0.0;
+// Row sum of A x for lane `lane` of slice `slice` (one warp per slice).  Uniform
+// slices read one shared offset per slot (a broadcast load) instead of 32 columns.
+// V is the value type, X the vector type; the sum is accumulated in V*X's type.
+template <class V, class X>
+__device__ __forceinline__ decltype(V(0) * X(0)) sell_row(const SellView &s, int n,
+                                                         const V *__restrict__ val,
+                                                         const X *__restrict__ x, int slice,
+                                                         int lane) {
+  using A = decltype(V(0) * X(0));
+  const long long base = __ldg(&s.ptr[slice]) + lane;
+  const int w = __ldg(&s.width[slice]), op = __ldg(&s.offp[slice]);
+  A acc = 0;
+  if (__ldg(&s.kind[slice]) == 0) {
+    const int row = slice * 32 + lane;
+#pragma unroll 7
+    for (int j = 0; j < w; ++j) {
+      int c = row + __ldg(&s.off[op + j]);
+      c = c < 0 ? 0 : (c >= n ? n - 1 : c);
+      acc += (A)__ldg(&val[base + (long long)j * 32]) * (A)__ldg(&x[c]);
+    }
+  } else {
 #pragma unroll 4
-  for (int j = 0; j < w; ++j) {
-    long long p = base + (long long)j * 32;
-    acc += __ldg(&val[p]) * __ldg(&x[__ldg(&s.col[p])]);
+    for (int j = 0; j < w; ++j)
+      acc += (A)__ldg(&val[base + (long long)j * 32]) *
+             (A)__ldg(&x[__ldg(&s.off[op + 32 * j + lane])]);
   }
   return acc;
 }
@@ -217,7 +245,7 @@ __global__ void __launch_bounds__(kTPB, 8) k_spmv(SellView s, int n, const doubl
                        const double *__restrict__ x, double *__restrict__ y) {
   FCG_SLICE_LOOP(slice, lane, s) {
     int r = slice * 32 + lane;
-    double acc = sell_row(s, val, x, slice, lane);
+    double acc = sell_row(s, n, val, x, slice, lane);
     if (r < n) y[r] = acc;
   }
 }
@@ -233,7 +261,7 @@ __global__ void __launch_bounds__(kTPB, 8) k_init(SellView s, int n, const doubl
   double v[2] = {0.0, 0.0};
   FCG_SLICE_LOOP(slice, lane, s) {
     int r = slice * 32 + lane;
-    double ax = sell_row(s, val, x, slice, lane);
+    double ax = sell_row(s, n, val, x, slice, lane);
     if (r < n) {
       double rr = su[r] - ax;
       res[r] = rr;
@@ -319,7 +347,7 @@ __global__ void __launch_bounds__(kTPB, 8) k_cg_spmv(SellView s, int n, const do
   double v[1] = {0.0};
   FCG_SLICE_LOOP(slice, lane, s) {
     int r = slice * 32 + lane;
-    double q = sell_row(s, val, pk, slice, lane);
+    double q = sell_row(s, n, val, pk, slice, lane);
     if (r < n) {
       qk[r] = q;
       v[0] += pk[r] * q;
@@ -455,7 +483,7 @@ __global__ void __launch_bounds__(kTPB, 8) k_bi_spmv1(SellView s, int n, const d
   double v[1] = {0.0};
   FCG_SLICE_LOOP(slice, lane, s) {
     int r = slice * 32 + lane;
-    double u = sell_row(s, val, zk, slice, lane);
+    double u = sell_row(s, n, val, zk, slice, lane);
     if (r < n) {
       uk[r] = u;
       v[0] += u * reso[r];
@@ -487,7 +515,7 @@ __global__ void __launch_bounds__(kTPB, 8) k_bi_spmv2(SellView s, int n, const d
   double v[2] = {0.0, 0.0};
   FCG_SLICE_LOOP(slice, lane, s) {
     int r = slice * 32 + lane;
-    double q = sell_row(s, val, zk, slice, lane);
+    double q = sell_row(s, n, val, zk, slice, lane);
     if (r < n) {
       vk[r] = q;
       v[0] += q * res[r];
@@ -532,6 +560,191 @@ __global__ void __launch_bounds__(kTPB, 8) k_bi_upd2(int n, double *__restrict__
     bi_close_sweep(S, v[0], trace, h, use_cond);
 }
 
+// ---------------------------------------------------------------------------
+// Mixed precision: CG on D^-1/2 A D^-1/2 (Jacobi preconditioning folded into a
+// symmetric scaling) in FP32, with reliable updates (Clark et al. 2010, "Solving lattice
+// QCD systems of equations using mixed precision solvers on GPUs"): the FP32 recursion
+// keeps its direction p, and whenever ||r32|| has dropped by `delta` since the last true
+// residual, or the predicted L1 residual reaches the tolerance, the FP32 correction is
+// added to the FP64 solution and the residual is recomputed in FP64, su - A x.  The stop
+// test is the reference's L1-relative one, evaluated on that true residual only.
+// Dot products: FP32 products summed per thread in FP32 (a few dozen terms), then in
+// FP64 across threads, blocks and the grid.
+// ---------------------------------------------------------------------------
+__global__ void k_mx_scale(int n, const int *__restrict__ diag, const double *__restrict__ a,
+                           double *__restrict__ s64) {
+  FCG_GRID_STRIDE(i, n) s64[i] = 1.0 / sqrt(a[diag[i]]);
+}
+
+__global__ void k_mx_fill(SellView s, int n, const double *__restrict__ a,
+                          const double *__restrict__ s64, float *__restrict__ sv32) {
+  FCG_GRID_STRIDE(r, (long long)s.nslices * 32) {
+    int slice = (int)(r >> 5), lane = (int)(r & 31);
+    long long base = s.ptr[slice];
+    int w = s.width[slice], op = s.offp[slice];
+    double sr = r < n ? s64[r] : 0.0;
+    for (int j = 0; j < w; ++j) {
+      long long p = base + (long long)j * 32 + lane;
+      int src = s.src[p];
+      int c = s.kind[slice] == 0 ? (int)r + s.off[op + j] : s.off[op + 32 * j + lane];
+      c = c < 0 ? 0 : (c >= n ? n - 1 : c);
+      sv32[p] = src >= 0 ? (float)(a[src] * sr * s64[c]) : 0.0f;
+    }
+  }
+}
+
+// r32 = D^-1/2 res, y32 = 0, p32 = r32, rr = r32.r32
+__global__ void __launch_bounds__(kTPB, 8)
+    k_mx_start(int n, const double *__restrict__ res, const double *__restrict__ s64,
+               float *__restrict__ r32, float *__restrict__ y32, float *__restrict__ p32, Scal *S,
+               double *partials) {
+  float t = 0.f;
+  FCG_GRID_STRIDE(i, n) {
+    float r = (float)(s64[i] * res[i]);
+    r32[i] = r;
+    p32[i] = r;
+    y32[i] = 0.f;
+    t += r * r;
+  }
+  double v[1] = {(double)t};
+  if (reduce_commit<1>(v, partials, &S->ticket[3]) && threadIdx.x == 0) {
+    S->rr = v[0];
+    S->maxr = sqrt(v[0]);
+    S->l1ratio = v[0] > 0 ? S->res0 / sqrt(v[0]) : 0.0;
+    S->ru = 0;
+    S->nupdates = 0;
+  }
+}
+
+// q32 = Ahat p32, alf = rr / p.q
+__global__ void __launch_bounds__(kTPB, 8)
+    k_mx_spmv(SellView s, int n, const float *__restrict__ val, const float *__restrict__ p32,
+              float *__restrict__ q32, Scal *S, double *partials) {
+  if (solve_done(S)) return;
+  float t = 0.f;
+  FCG_SLICE_LOOP(slice, lane, s) {
+    int r = slice * 32 + lane;
+    float q = sell_row(s, n, val, p32, slice, lane);
+    if (r < n) {
+      q32[r] = q;
+      t += p32[r] * q;
+    }
+  }
+  double v[1] = {(double)t};
+  if (reduce_commit<1>(v, partials, &S->ticket[1]) && threadIdx.x == 0) {
+    S->alf = S->rr / v[0];
+    if (!isfinite(S->alf)) S->status = FCG_ERR_NONFINITE;
+  }
+}
+
+__device__ __noinline__ void mx_decide(Scal *S, double rrn) {
+  int it = S->iter + 1;
+  S->iter = it;
+  double nr = sqrt(rrn);
+  double pred = S->l1ratio * nr;  // predicted L1 of the unscaled residual
+  bool ru = nr < S->delta * S->maxr || pred < 0.9 * S->resmax * (S->res0 + S->small) ||
+            it >= S->nsw || !isfinite(rrn);
+  S->rr_old = S->rr;
+  if (ru) {
+    S->ru = 1;
+  } else {
+    S->bet = rrn / S->rr;
+    S->rr = rrn;
+  }
+}
+
+// y32 += alf p32, r32 -= alf q32, rr' = r32.r32; decides whether a reliable update follows
+__global__ void __launch_bounds__(kTPB, 8)
+    k_mx_update(int n, float *__restrict__ y32, float *__restrict__ r32,
+                const float *__restrict__ p32, const float *__restrict__ q32, Scal *S,
+                double *partials) {
+  if (solve_done(S)) return;
+  const float alf = (float)__ldcg(&S->alf);
+  float t = 0.f;
+  FCG_GRID_STRIDE(i, n) {
+    y32[i] = y32[i] + alf * p32[i];
+    float r = r32[i] - alf * q32[i];
+    r32[i] = r;
+    t += r * r;
+  }
+  double v[1] = {(double)t};
+  if (reduce_commit<1>(v, partials, &S->ticket[2]) && threadIdx.x == 0) mx_decide(S, v[0]);
+}
+
+// reliable update, part 1: x += D^-1/2 y32 in FP64, y32 = 0
+__global__ void k_mx_ru1(int n, double *__restrict__ x, float *__restrict__ y32,
+                         const double *__restrict__ s64, const Scal *S) {
+  if (solve_done(S) || !__ldcg(&S->ru)) return;
+  FCG_GRID_STRIDE(i, n) {
+    x[i] = x[i] + s64[i] * (double)y32[i];
+    y32[i] = 0.f;
+  }
+}
+
+__device__ __noinline__ void mx_after_update(Scal *S, double l1, double rrn, double *trace,
+                                             cudaGraphConditionalHandle h, int use_cond) {
+  S->resl = l1;
+  if (S->iter >= 1 && S->resor == 0.0) S->resor = S->res0;
+  double rsm = l1 / (S->res0 + S->small);
+  S->rsm = rsm;
+  S->nupdates++;
+  if (trace && S->nupdates <= S->trace_cap) {
+    trace[2 * (S->nupdates - 1)] = l1;
+    trace[2 * (S->nupdates - 1) + 1] = rsm;
+  }
+  if (rsm < S->resmax) S->converged = 1;
+  if (!isfinite(l1)) S->status = FCG_ERR_NONFINITE;
+  if (S->converged || S->iter >= S->nsw || S->status) {
+    S->done = 1;
+    if (use_cond) cudaGraphSetConditional(h, 0);
+    return;
+  }
+  S->bet = rrn / S->rr_old;  // continue the recursion with the true residual
+  S->rr = rrn;
+  S->maxr = sqrt(rrn);
+  S->l1ratio = rrn > 0 ? l1 / sqrt(rrn) : 0.0;
+  S->ru = 0;
+}
+
+// reliable update, part 2: res = su - A x (FP64), L1 of it, r32 = D^-1/2 res, rr
+__global__ void __launch_bounds__(kTPB, 8)
+    k_mx_ru2(SellView s, int n, const double *__restrict__ val, const double *__restrict__ su,
+             const double *__restrict__ x, double *__restrict__ res,
+             const double *__restrict__ s64, float *__restrict__ r32, Scal *S, double *partials,
+             double *trace, cudaGraphConditionalHandle h, int use_cond) {
+  if (solve_done(S) || !__ldcg(&S->ru)) return;
+  double l1 = 0.0;
+  float t = 0.f;
+  FCG_SLICE_LOOP(slice, lane, s) {
+    int r = slice * 32 + lane;
+    double ax = sell_row(s, n, val, x, slice, lane);
+    if (r < n) {
+      double rr = su[r] - ax;
+      res[r] = rr;
+      l1 += fabs(rr);
+      float r3 = (float)(s64[r] * rr);
+      r32[r] = r3;
+      t += r3 * r3;
+    }
+  }
+  double v[2] = {l1, (double)t};
+  if (reduce_commit<2>(v, partials, &S->ticket[4]) && threadIdx.x == 0)
+    mx_after_update(S, v[0], v[1], trace, h, use_cond);
+}
+
+// p32 = r32 + bet p32; closes the loop body
+__global__ void __launch_bounds__(kTPB, 8)
+    k_mx_p(int n, const float *__restrict__ r32, float *__restrict__ p32, Scal *S,
+           cudaGraphConditionalHandle h, int use_cond) {
+  if (solve_done(S)) {
+    stop_loop(h, use_cond);
+    return;
+  }
+  loop_guard(S, h, use_cond);
+  const float bet = (float)__ldcg(&S->bet);
+  FCG_GRID_STRIDE(i, n) p32[i] = r32[i] + bet * p32[i];
+}
+
 // Final FP64 check: ||su - A x||^2 and ||su||^2.
 __global__ void __launch_bounds__(kTPB, 8) k_final(SellView s, int n, const double *__restrict__ val,
                         const double *__restrict__ su, const double *__restrict__ x, Scal *S,
@@ -539,7 +752,7 @@ __global__ void __launch_bounds__(kTPB, 8) k_final(SellView s, int n, const doub
   double v[2] = {0.0, 0.0};
   FCG_SLICE_LOOP(slice, lane, s) {
     int r = slice * 32 + lane;
-    double ax = sell_row(s, val, x, slice, lane);
+    double ax = sell_row(s, n, val, x, slice, lane);
     if (r < n) {
       double rr = su[r] - ax;
       v[0] += rr * rr;
@@ -620,8 +833,15 @@ static int ensure_state(fcg_context *c, int nsw) {
     g.bupd2 = occ((const void *)k_bi_upd2);
     g.fin = occ((const void *)k_final);
     g.plain = occ((const void *)k_spmv);
+    g.mstart = occ((const void *)k_mx_start);
+    g.mspmv = occ((const void *)k_mx_spmv);
+    g.mupd = occ((const void *)k_mx_update);
+    g.mru1 = occ((const void *)k_mx_ru1);
+    g.mru2 = occ((const void *)k_mx_ru2);
+    g.mp = occ((const void *)k_mx_p);
     k->bind_gen = c->bind_gen;
     k->matrix_loaded = false;
+    k->mixed_ready = false;
   }
   if (nsw > k->nsw_cap) {
     FCG_CUDA_TRY(c, k->trace.ensure(sizeof(double) * 2 * (size_t)nsw));
@@ -663,36 +883,104 @@ static void launch_sweeps(fcg_context *c, cudaStream_t st, const Level &lv, bool
   }
 }
 
-// Enqueues one sweep of solver `kind` on stream st.
-static void enqueue_sweep(fcg_context *c, cudaStream_t st, int kind, cudaGraphConditionalHandle h,
-                          int use_cond) {
+// Kernels of one sweep, in order, as units (a unit of a DIC/DILU sweep is the whole
+// chain of level launches).  Unit names are listed in sweep_unit_names().
+static int sweep_units(int kind) {
+  switch (kind) {
+    case SK_DPCG: return 3;
+    case SK_ICCG: return 6;
+    case SK_BICG: return 10;
+    case SK_MIXED: return 5;
+  }
+  return 0;
+}
+
+static const char *sweep_unit_name(int kind, int u) {
+  static const char *dpcg[] = {"k_cg_p", "k_cg_spmv", "k_cg_update"};
+  static const char *iccg[] = {"fwd_levels", "bwd_levels", "k_cg_dot", "k_cg_p", "k_cg_spmv",
+                               "k_cg_update"};
+  static const char *bicg[] = {"k_bi_dot1", "k_bi_p", "fwd_levels", "bwd_levels", "k_bi_spmv1",
+                               "k_bi_upd1", "fwd_levels", "bwd_levels", "k_bi_spmv2", "k_bi_upd2"};
+  static const char *mixed[] = {"k_mx_spmv", "k_mx_update", "k_mx_ru1", "k_mx_ru2", "k_mx_p"};
+  if (u < 0 || u >= sweep_units(kind)) return "";
+  switch (kind) {
+    case SK_DPCG: return dpcg[u];
+    case SK_ICCG: return iccg[u];
+    case SK_BICG: return bicg[u];
+    default: return mixed[u];
+  }
+}
+
+// Enqueues unit u of one sweep of solver `kind` on stream st.
+static void enqueue_unit(fcg_context *c, cudaStream_t st, int kind, int u,
+                         cudaGraphConditionalHandle h, int use_cond) {
   KrylovState *k = c->ks;
   const int n = c->n;
   const SellView &s = c->sv;
   double *tr = k->trace.as<double>();
   if (kind == SK_DPCG || kind == SK_ICCG) {
-    if (kind == SK_ICCG) {
-      launch_sweeps(c, st, c->lf, true, k->res, k->zk);
-      launch_sweeps(c, st, c->lb, false, nullptr, k->zk);
-      k_cg_dot<<<k->gr.dot, kTPB, 0, st>>>(n, k->res, k->zk, k->S, k->partials);
+    int v = kind == SK_DPCG ? u + 3 : u;
+    switch (v) {
+      case 0: launch_sweeps(c, st, c->lf, true, k->res, k->zk); break;
+      case 1: launch_sweeps(c, st, c->lb, false, nullptr, k->zk); break;
+      case 2: k_cg_dot<<<k->gr.dot, kTPB, 0, st>>>(n, k->res, k->zk, k->S, k->partials); break;
+      case 3:
+        k_cg_p<<<k->gr.p, kTPB, 0, st>>>(n, k->res, k->invd, k->zk, k->pk, k->S, kind);
+        break;
+      case 4:
+        k_cg_spmv<<<k->gr.spmv, kTPB, 0, st>>>(s, n, k->sval, k->pk, k->qk, k->S, k->partials);
+        break;
+      case 5:
+        k_cg_update<<<k->gr.update, kTPB, 0, st>>>(n, k->x, k->res, k->pk, k->qk, k->invd, k->S,
+                                                   k->partials, tr, h, use_cond, kind);
+        break;
     }
-    k_cg_p<<<k->gr.p, kTPB, 0, st>>>(n, k->res, k->invd, k->zk, k->pk, k->S, kind);
-    k_cg_spmv<<<k->gr.spmv, kTPB, 0, st>>>(s, n, k->sval, k->pk, k->qk, k->S, k->partials);
-    k_cg_update<<<k->gr.update, kTPB, 0, st>>>(n, k->x, k->res, k->pk, k->qk, k->invd, k->S, k->partials,
-                                     tr, h, use_cond, kind);
+  } else if (kind == SK_MIXED) {
+    switch (u) {
+      case 0:
+        k_mx_spmv<<<k->gr.mspmv, kTPB, 0, st>>>(s, n, k->sval32, k->p32, k->q32, k->S,
+                                                 k->partials);
+        break;
+      case 1:
+        k_mx_update<<<k->gr.mupd, kTPB, 0, st>>>(n, k->y32, k->r32, k->p32, k->q32, k->S,
+                                                 k->partials);
+        break;
+      case 2: k_mx_ru1<<<k->gr.mru1, kTPB, 0, st>>>(n, k->x, k->y32, k->s64, k->S); break;
+      case 3:
+        k_mx_ru2<<<k->gr.mru2, kTPB, 0, st>>>(s, n, k->sval, k->su, k->x, k->res, k->s64, k->r32,
+                                              k->S, k->partials, tr, h, use_cond);
+        break;
+      case 4: k_mx_p<<<k->gr.mp, kTPB, 0, st>>>(n, k->r32, k->p32, k->S, h, use_cond); break;
+    }
   } else {
-    k_bi_dot1<<<k->gr.bdot, kTPB, 0, st>>>(n, k->res, k->reso, k->S, k->partials);
-    k_bi_p<<<k->gr.bp, kTPB, 0, st>>>(n, k->res, k->uk, k->pk, k->S);
-    launch_sweeps(c, st, c->lf, true, k->pk, k->zk);
-    launch_sweeps(c, st, c->lb, false, nullptr, k->zk);
-    k_bi_spmv1<<<k->gr.bspmv1, kTPB, 0, st>>>(s, n, k->sval, k->zk, k->reso, k->uk, k->S, k->partials);
-    k_bi_upd1<<<k->gr.bupd1, kTPB, 0, st>>>(n, k->x, k->res, k->zk, k->uk, k->S);
-    launch_sweeps(c, st, c->lf, true, k->res, k->zk);
-    launch_sweeps(c, st, c->lb, false, nullptr, k->zk);
-    k_bi_spmv2<<<k->gr.bspmv2, kTPB, 0, st>>>(s, n, k->sval, k->zk, k->res, k->vk, k->S, k->partials);
-    k_bi_upd2<<<k->gr.bupd2, kTPB, 0, st>>>(n, k->x, k->res, k->zk, k->vk, k->S, k->partials, tr, h,
-                                   use_cond);
+    switch (u) {
+      case 0: k_bi_dot1<<<k->gr.bdot, kTPB, 0, st>>>(n, k->res, k->reso, k->S, k->partials); break;
+      case 1: k_bi_p<<<k->gr.bp, kTPB, 0, st>>>(n, k->res, k->uk, k->pk, k->S); break;
+      case 2: launch_sweeps(c, st, c->lf, true, k->pk, k->zk); break;
+      case 3: launch_sweeps(c, st, c->lb, false, nullptr, k->zk); break;
+      case 4:
+        k_bi_spmv1<<<k->gr.bspmv1, kTPB, 0, st>>>(s, n, k->sval, k->zk, k->reso, k->uk, k->S,
+                                                   k->partials);
+        break;
+      case 5: k_bi_upd1<<<k->gr.bupd1, kTPB, 0, st>>>(n, k->x, k->res, k->zk, k->uk, k->S); break;
+      case 6: launch_sweeps(c, st, c->lf, true, k->res, k->zk); break;
+      case 7: launch_sweeps(c, st, c->lb, false, nullptr, k->zk); break;
+      case 8:
+        k_bi_spmv2<<<k->gr.bspmv2, kTPB, 0, st>>>(s, n, k->sval, k->zk, k->res, k->vk, k->S,
+                                                   k->partials);
+        break;
+      case 9:
+        k_bi_upd2<<<k->gr.bupd2, kTPB, 0, st>>>(n, k->x, k->res, k->zk, k->vk, k->S, k->partials,
+                                                tr, h, use_cond);
+        break;
+    }
   }
+}
+
+// Enqueues one sweep of solver `kind` on stream st.
+static void enqueue_sweep(fcg_context *c, cudaStream_t st, int kind, cudaGraphConditionalHandle h,
+                          int use_cond) {
+  for (int u = 0; u < sweep_units(kind); ++u) enqueue_unit(c, st, kind, u, h, use_cond);
 }
 
 static bool graphs_disabled() {
@@ -764,6 +1052,7 @@ static int run_solver(fcg_context *c, int kind, const double *a, const double *s
   init.resmax = sor;
   init.tol = (double)1e-13f;  // dpcg.f90:37
   init.trace_cap = k->nsw_cap;
+  init.delta = k->ru_delta;
   *k->hS = init;
   FCG_CUDA_TRY(c, cudaMemcpyAsync(k->S, k->hS, sizeof(Scal), cudaMemcpyHostToDevice, c->stream));
   k_init<<<k->gr.init, kTPB, 0, c->stream>>>(c->sv, c->n, k->sval, k->su, k->x, k->res, k->invd, k->S,
@@ -771,6 +1060,33 @@ static int run_solver(fcg_context *c, int kind, const double *a, const double *s
   FCG_CHECK_LAUNCH(c, "k_init");
   if (kind == SK_BICG)
     FCG_CUDA_TRY(c, cudaMemcpyAsync(k->reso, k->res, n1, cudaMemcpyDeviceToDevice, c->stream));
+  if (kind == SK_MIXED) {
+    if (!k->mixed_ready) {
+      size_t n4 = ((size_t)c->n + 63) & ~(size_t)63;
+      size_t bytes = sizeof(double) * n4 + sizeof(float) * (4 * n4 + (size_t)c->sell_len + 64);
+      FCG_CUDA_TRY(c, k->mixed.ensure(bytes));
+      k->s64 = k->mixed.as<double>();
+      float *f = (float *)(k->s64 + n4);
+      k->y32 = f;
+      k->r32 = f + n4;
+      k->p32 = f + 2 * n4;
+      k->q32 = f + 3 * n4;
+      k->sval32 = f + 4 * n4;
+      k->mixed_ready = true;
+      for (int i = SK_MIXED; i <= SK_MIXED; ++i) {  // buffers moved: recapture
+        if (k->exec[i]) cudaGraphExecDestroy(k->exec[i]);
+        if (k->graph[i]) cudaGraphDestroy(k->graph[i]);
+        k->exec[i] = nullptr;
+        k->graph[i] = nullptr;
+      }
+    }
+    k_mx_scale<<<grid_for(c->n, c->num_sms), kTPB, 0, c->stream>>>(c->n, c->mv.diag, k->a, k->s64);
+    k_mx_fill<<<grid_for((long long)c->sv.nslices * 32, c->num_sms), kTPB, 0, c->stream>>>(
+        c->sv, c->n, k->a, k->s64, k->sval32);
+    k_mx_start<<<k->gr.mstart, kTPB, 0, c->stream>>>(c->n, k->res, k->s64, k->r32, k->y32,
+                                                     k->p32, k->S, k->partials);
+    FCG_CHECK_LAUNCH(c, "mixed set-up");
+  }
   if (kind != SK_DPCG) {  // factor diagonal, level by level
     for (int l = 0; l < c->lf.count; ++l) {
       int start = c->lf.ptr[l], cnt = c->lf.ptr[l + 1] - c->lf.ptr[l];
@@ -808,6 +1124,7 @@ static int run_solver(fcg_context *c, int kind, const double *a, const double *s
   FCG_CUDA_TRY(c, cudaMemcpyAsync(k->hS, k->S, sizeof(Scal), cudaMemcpyDeviceToHost, c->stream));
   FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   const Scal &S = *k->hS;
+  k->last_kind = kind;
   if (resor && S.iter > 0) *resor = S.res0;  // dpcg.f90:139
   if (rep) {
     rep->res0 = S.res0;
@@ -848,6 +1165,12 @@ extern "C" int fcg_bicgstab(fcg_context *c, const double *a, const double *su, d
   return run_solver(c, SK_BICG, a, su, fi, res, sor, nsw, resor, rep);
 }
 
+extern "C" int fcg_dpcg_mixed(fcg_context *c, const double *a, const double *su, double *fi,
+                              double *res, double sor, int nsw, double *resor,
+                              fcg_solve_report *rep) {
+  return run_solver(c, SK_MIXED, a, su, fi, res, sor, nsw, resor, rep);
+}
+
 extern "C" int fcg_set_solver_options(fcg_context *c, double small, int early_exit) {
   if (!c) return FCG_ERR_ARG;
   FCG_CUDA_TRY(c, cudaSetDevice(c->device));
@@ -856,6 +1179,58 @@ extern "C" int fcg_set_solver_options(fcg_context *c, double small, int early_ex
   c->ks->small = small;
   c->ks->early_exit = early_exit ? 1 : 0;
   return FCG_OK;
+}
+
+// Re-opens the last solve for profiling: clears the stop flag, the reliable-update
+// flag and the sweep counters, and lifts the sweep cap.
+__global__ void k_prof_reopen(Scal *S) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    S->done = 0;
+    S->ru = 0;
+    S->status = 0;
+    S->converged = 0;
+    S->iter = 0;
+    S->body_count = 0;
+    S->nsw = 0x3fffffff;
+  }
+}
+
+extern "C" int fcg_profile_sweeps(fcg_context *c, int reps, double *ms, int max_units,
+                                  int *units) {
+  if (!c || reps < 1) return FCG_ERR_ARG;
+  if (!c->ks || c->ks->last_kind < 0)
+    return set_error(c, FCG_ERR_STATE, "fcg_profile_sweeps before any solve");
+  FCG_CUDA_TRY(c, cudaSetDevice(c->device));
+  KrylovState *k = c->ks;
+  const int kind = k->last_kind, nu = sweep_units(kind);
+  if (units) *units = nu;
+  std::vector<cudaEvent_t> ev(2 * nu);
+  for (auto &e : ev) FCG_CUDA_TRY(c, cudaEventCreate(&e));
+  std::vector<double> acc(nu, 0.0);
+  k_prof_reopen<<<1, 32, 0, c->stream>>>(k->S);
+  for (int r = 0; r < reps; ++r) {
+    for (int u = 0; u < nu; ++u) {
+      cudaEventRecord(ev[2 * u], c->stream);
+      enqueue_unit(c, c->stream, kind, u, 0, 0);
+      cudaEventRecord(ev[2 * u + 1], c->stream);
+    }
+    FCG_CHECK_LAUNCH(c, "profiled sweep");
+    FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    for (int u = 0; u < nu; ++u) {
+      float t = 0.f;
+      cudaEventElapsedTime(&t, ev[2 * u], ev[2 * u + 1]);
+      acc[u] += t;
+    }
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  for (int u = 0; u < nu && u < max_units; ++u)
+    if (ms) ms[u] = acc[u] / reps;
+  return FCG_OK;
+}
+
+extern "C" const char *fcg_profile_unit_name(const fcg_context *c, int unit) {
+  if (!c || !c->ks || c->ks->last_kind < 0) return "";
+  return sweep_unit_name(c->ks->last_kind, unit);
 }
 
 extern "C" int fcg_get_solver_trace(fcg_context *c, double *out, int max_count, int *count) {

@@ -155,39 +155,82 @@ int build_topology(const fcg_mesh_desc &m, const int cnt[B_NTYPES], const int fs
     for (int f = nin; f < nf; ++f) t.cbf_face[fill[m.owner[f] - 1]++] = f;
   }
 
-  // --- sliced ELL --------------------------------------------------------------
+  // --- sliced ELL with offset-uniform slices ------------------------------------
+  // A slice is "uniform" when it is cheaper to store, per slot j, one column offset
+  // shared by its 32 rows (slot j of row r reads column r + off[j]; a row without that
+  // offset gets the value 0) than 32 explicit columns.  Uniform slots follow the
+  // ascending offsets, so every row still meets its entries in CSR column order.  On a
+  // hex mesh numbered i-fastest every slice is uniform with the 7 offsets
+  // -N^2, -N, -1, 0, 1, N, N^2, and the SpMV reads no column indices at all.
   const int ns = (n + 31) / 32;
   t.sell_ptr.assign(ns + 1, 0);
   t.sell_width.assign(ns, 0);
+  t.sell_kind.assign(ns, 0);
+  t.sell_offp.assign(ns + 1, 0);
   t.sell_maxw = 0;
-  for (int s = 0; s < ns; ++s) {
-    int w = 0;
-    for (int r = 32 * s; r < std::min(n, 32 * s + 32); ++r)
-      w = std::max(w, t.ioffset[r + 1] - t.ioffset[r]);
-    t.sell_width[s] = w;
+  std::vector<std::vector<int>> uoffs(ns);
+  std::vector<int> ecols(ns, 0);  // explicit column block size per slice
+  parallel_for(ns, [&](long long sl) {
+    int wexp = 0;
+    std::vector<int> u;
+    for (long long r = 32 * sl; r < std::min<long long>(n, 32 * sl + 32); ++r) {
+      wexp = std::max(wexp, t.ioffset[r + 1] - t.ioffset[r]);
+      for (int k = t.ioffset[r] - 1; k < t.ioffset[r + 1] - 1; ++k) u.push_back(t.ja[k] - 1 - (int)r);
+    }
+    std::sort(u.begin(), u.end());
+    u.erase(std::unique(u.begin(), u.end()), u.end());
+    if (!u.empty() && 2 * (long long)u.size() < 3LL * wexp) {  // 8w_u < 12w_e bytes per row
+      t.sell_kind[sl] = 0;
+      t.sell_width[sl] = (int)u.size();
+      uoffs[sl] = std::move(u);
+    } else {
+      t.sell_kind[sl] = 1;
+      t.sell_width[sl] = wexp;
+      ecols[sl] = 32 * wexp;
+    }
+  });
+  for (int sl = 0; sl < ns; ++sl) {
+    int w = t.sell_width[sl];
     t.sell_maxw = std::max(t.sell_maxw, w);
-    t.sell_ptr[s + 1] = t.sell_ptr[s] + 32LL * w;
+    t.sell_ptr[sl + 1] = t.sell_ptr[sl] + 32LL * w;
+    t.sell_offp[sl + 1] = t.sell_offp[sl] + (t.sell_kind[sl] == 0 ? w : 0);
   }
-  t.sell_col.assign(t.sell_ptr[ns], 0);
+  // explicit column blocks are stored after the offset table, in one index array
+  std::vector<long long> colp(ns + 1, 0);
+  for (int sl = 0; sl < ns; ++sl) colp[sl + 1] = colp[sl] + ecols[sl];
+  t.sell_off.assign(t.sell_offp[ns] + colp[ns], 0);
   t.sell_src.assign(t.sell_ptr[ns], -1);
-  parallel_for(ns, [&](long long s) {
-    int w = t.sell_width[s];
+  parallel_for(ns, [&](long long sl) {
+    int w = t.sell_width[sl];
+    if (t.sell_kind[sl] == 0) {
+      const std::vector<int> &u = uoffs[sl];
+      for (int j = 0; j < w; ++j) t.sell_off[t.sell_offp[sl] + j] = u[j];
+    } else {
+      t.sell_offp[sl] = (int)(t.sell_offp[ns] + colp[sl]);  // explicit: start of the column block
+    }
     for (int lane = 0; lane < 32; ++lane) {
-      long long r = 32 * s + lane;
-      int len = r < n ? t.ioffset[r + 1] - t.ioffset[r] : 0;
+      long long r = 32 * sl + lane;
+      int b = r < n ? t.ioffset[r] - 1 : 0, e = r < n ? t.ioffset[r + 1] - 1 : 0;
       for (int j = 0; j < w; ++j) {
-        long long pos = t.sell_ptr[s] + (long long)j * 32 + lane;
-        if (j < len) {
-          int k = t.ioffset[r] - 1 + j;
-          t.sell_col[pos] = t.ja[k] - 1;
-          t.sell_src[pos] = k;
+        long long pos = t.sell_ptr[sl] + (long long)j * 32 + lane;
+        if (t.sell_kind[sl] == 0) {
+          int want = (int)r + uoffs[sl][j] + 1;  // 1-based column for this slot
+          for (int k = b; k < e; ++k)
+            if (t.ja[k] == want) t.sell_src[pos] = k;
         } else {
-          t.sell_col[pos] = (int)std::min<long long>(r, n - 1);
-          t.sell_src[pos] = -1;
+          long long cpos = t.sell_offp[sl] + (long long)j * 32 + lane;
+          if (j < e - b) {
+            t.sell_off[cpos] = t.ja[b + j] - 1;
+            t.sell_src[pos] = b + j;
+          } else {
+            t.sell_off[cpos] = (int)std::min<long long>(r, n - 1);
+          }
         }
       }
     }
   });
+  t.sell_nuniform = 0;
+  for (int sl = 0; sl < ns; ++sl) t.sell_nuniform += t.sell_kind[sl] == 0;
 
   // --- level schedules -----------------------------------------------------------
   std::vector<int> lev(n, 0);

@@ -64,7 +64,8 @@ class SolveResult:
 
 
 # Log-line names of the reference solvers (dpcg.f90:150, iccg.f90:328, bicgstab.f90:227).
-SOLVER_NAMES = {"dpcg": "PCG(Jacobi):  ", "iccg": "  PCG(IC0):  ", "bicgstab": "  BiCGStab(ILU(0)):  "}
+SOLVER_NAMES = {"dpcg": "PCG(Jacobi):  ", "iccg": "  PCG(IC0):  ", "bicgstab": "  BiCGStab(ILU(0)):  ",
+                "dpcg_mixed": "PCG(Jacobi, FP32 sweeps + FP64 updates):  "}
 
 
 def solver_log(kind: str, var: str, r: SolveResult) -> str:
@@ -205,6 +206,10 @@ class Context:
         """dpcg(fi,ifi) (dpcg.f90:3-154)."""
         return self._solve(self.lib.fcg_dpcg, "fcg_dpcg", a, su, fi, sor, nsw, **kw)
 
+    def dpcg_mixed(self, a, su, fi, sor, nsw, **kw) -> SolveResult:
+        """dpcg with FP32 sweeps under FP64 reliable updates (same stop test)."""
+        return self._solve(self.lib.fcg_dpcg_mixed, "fcg_dpcg_mixed", a, su, fi, sor, nsw, **kw)
+
     def iccg(self, a, su, fi, sor, nsw, **kw) -> SolveResult:
         """iccg(fi,ifi) (iccg.f90:3-177)."""
         return self._solve(self.lib.fcg_iccg, "fcg_iccg", a, su, fi, sor, nsw, **kw)
@@ -212,6 +217,21 @@ class Context:
     def bicgstab(self, a, su, fi, sor, nsw, **kw) -> SolveResult:
         """bicgstab(fi,ifi) (bicgstab.f90:1-231)."""
         return self._solve(self.lib.fcg_bicgstab, "fcg_bicgstab", a, su, fi, sor, nsw, **kw)
+
+    def profile_sweeps(self, reps: int = 10) -> dict:
+        """Mean milliseconds per kernel unit of the last solve's sweep (changes its state)."""
+        ms = (C.c_double * 32)()
+        nu = C.c_int()
+        self._check(self.lib.fcg_profile_sweeps(self.h, int(reps), ms, 32, C.byref(nu)),
+                    "fcg_profile_sweeps")
+        out = {}
+        for i in range(nu.value):
+            name = self.lib.fcg_profile_unit_name(self.h, i).decode()
+            key, j = name, 2
+            while key in out:
+                key, j = f"{name}#{j}", j + 1
+            out[key] = ms[i]
+        return out
 
     def spmv(self, a, x, y=None):
         x = _host(x)

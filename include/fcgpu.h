@@ -181,6 +181,17 @@ int fcg_iccg(fcg_context *ctx, const double *a, const double *su, double *fi, do
 int fcg_bicgstab(fcg_context *ctx, const double *a, const double *su, double *fi,
                  double *res, double sor, int nsw, double *resor, fcg_solve_report *rep);
 
+/* dpcg with FP32 inner sweeps under FP64 reliable updates (no reference counterpart;
+ * same arguments and stop test as fcg_dpcg).  The sweeps run CG on D^-1/2 A D^-1/2 in
+ * FP32 (the Jacobi preconditioner of dpcg.f90 folded into a symmetric scaling); FP64 is
+ * kept for the true residual su - A x, which replaces the FP32 one whenever the FP32
+ * residual has fallen 10x since the last replacement or predicts convergence, for the
+ * global sums that form alpha and beta, and for the solution.  The stop test
+ * resl/(res0+small) < sor is evaluated on the true FP64 residual only.  rep->iters
+ * counts FP32 sweeps; the trace holds one (resl, rsm) pair per FP64 replacement. */
+int fcg_dpcg_mixed(fcg_context *ctx, const double *a, const double *su, double *fi,
+                   double *res, double sor, int nsw, double *resor, fcg_solve_report *rep);
+
 /* Constants of the solvers: small (parameters::small, modules_allocatable.f90:27;
  * default the REAL literal 1e-20) and whether a solve returns at once when
  * res0 < 1e-13 (dpcg.f90:66-70; default 1).  The copies of the solvers in
@@ -208,6 +219,15 @@ int fcg_get_solver_trace(fcg_context *ctx, double *resl_rsm, int max_count, int 
 int fcg_dpcg_noalloc(int numCells, const int *ioffset, const int *ja, const int *diag,
                      const double *a, const double *su, double *fi, double *res, double sor,
                      int nsw, double *resor, fcg_solve_report *rep, void *cuda_stream);
+
+/* Diagnostics (no reference counterpart; the reference times whole outer iterations
+ * with cpu_time, main.f90:127-148).  Runs `reps` more sweeps of the last solve's method
+ * kernel by kernel, outside the CUDA graph, with CUDA events around every kernel (a
+ * triangular sweep counts as one unit), and writes the mean milliseconds of each unit
+ * to ms[0..*units-1].  It continues the last solve's iteration and so changes its
+ * state: solve again before using results.  fcg_profile_unit_name names unit i. */
+int fcg_profile_sweeps(fcg_context *ctx, int reps, double *ms, int max_units, int *units);
+const char *fcg_profile_unit_name(const fcg_context *ctx, int unit);
 
 /* y = A x (the matvec of dpcg.f90:105-110) with CSR values a[nnz]; a == NULL reuses
  * the matrix of the previous solve or spmv call. */

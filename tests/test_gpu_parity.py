@@ -241,3 +241,30 @@ def test_errors_are_reported():
     with pytest.raises(_lib.FcgError) as e:
         fcg.Context(bad)
     assert e.value.status == _lib.FCG_ERR_INDEX
+
+
+@pytest.mark.parametrize("name", ["hex12_u", "hex8", "cavity", "pitzdaily"])
+def test_mixed_dpcg_matches_fp64_solution(name):
+    """FP32 sweeps + FP64 reliable updates: same stop test on the true residual, about
+    the FP64 sweep count, solution within the tolerance-level distance of the oracle's."""
+    m, c = ctx_for(name)
+    a, su = _system(m, c)
+    o = oracle.dpcg(oracle_csr(m), a, su, np.zeros(m.numCells), 1e-8, 5000)
+    r = c.dpcg_mixed(a, su, np.zeros(m.numCells), 1e-8, 5000, want_trace=True)
+    assert r.converged
+    assert r.resl / r.res0 < 1e-8  # true FP64 residual
+    assert r.iters <= 1.15 * o.iters + 5
+    assert rel(r.fi, o.fi) < 1e-5
+    assert len(r.trace) >= 1 and r.trace[-1][1] < 1e-8
+    # the returned res is the true residual su - A fi
+    Ax = oracle.spmv(oracle_csr(m), a, r.fi)
+    assert np.abs((su - Ax) - r.res).max() < 1e-12 * np.abs(su).max()
+
+
+def test_mixed_dpcg_nsw_cap_and_zero_rhs():
+    m, c = ctx_for("hex8")
+    a, su = _system(m, c)
+    r = c.dpcg_mixed(a, su, np.zeros(m.numCells), 1e-30, 7)
+    assert r.iters == 7 and not r.converged
+    r = c.dpcg_mixed(a, np.zeros(m.numCells), np.zeros(m.numCells), 1e-8, 100)
+    assert r.iters == 0 and r.resor is None
