@@ -219,9 +219,26 @@ __device__ __forceinline__ decltype(V(0) * X(0)) sell_row(const SellView &s, int
   const long long base = __ldg(&s.ptr[slice]) + lane;
   const int w = __ldg(&s.width[slice]), op = __ldg(&s.offp[slice]);
   A acc = 0;
-  if (__ldg(&s.kind[slice]) == 0) {
+  const int kind = __ldg(&s.kind[slice]);
+  if (sizeof(V) == 4 && kind == 0 && w <= 8) {
+    // all loads of the row issue before the first multiply-add
     const int row = slice * 32 + lane;
-#pragma unroll 7
+    V v[8];
+    X xv[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      if (j < w) {
+        int c = row + __ldg(&s.off[op + j]);
+        c = c < 0 ? 0 : (c >= n ? n - 1 : c);
+        v[j] = __ldg(&val[base + (long long)j * 32]);
+        xv[j] = __ldg(&x[c]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      if (j < w) acc += (A)v[j] * (A)xv[j];
+  } else if (kind == 0) {
+    const int row = slice * 32 + lane;
     for (int j = 0; j < w; ++j) {
       int c = row + __ldg(&s.off[op + j]);
       c = c < 0 ? 0 : (c >= n ? n - 1 : c);
@@ -594,7 +611,7 @@ __global__ void k_mx_fill(SellView s, int n, const double *__restrict__ a,
 }
 
 // r32 = D^-1/2 res, y32 = 0, p32 = r32, rr = r32.r32
-__global__ void __launch_bounds__(kTPB, 8)
+__global__ void __launch_bounds__(kTPB, 6)
     k_mx_start(int n, const double *__restrict__ res, const double *__restrict__ s64,
                float *__restrict__ r32, float *__restrict__ y32, float *__restrict__ p32, Scal *S,
                double *partials) {
@@ -616,15 +633,21 @@ __global__ void __launch_bounds__(kTPB, 8)
   }
 }
 
-// q32 = Ahat p32, alf = rr / p.q
-__global__ void __launch_bounds__(kTPB, 8)
+// q32 = Ahat p32, alf = rr / p.q.  Each block walks a contiguous run of slices, eight
+// at a time (one per warp), so that the gathers of x at row, row+-1 and row+-N that one
+// step makes are L1 hits of the steps just before and after it; only the +-N^2
+// neighbours come from L2.
+__global__ void __launch_bounds__(kTPB, 6)
     k_mx_spmv(SellView s, int n, const float *__restrict__ val, const float *__restrict__ p32,
               float *__restrict__ q32, Scal *S, double *partials) {
   if (solve_done(S)) return;
   float t = 0.f;
-  FCG_SLICE_LOOP(slice, lane, s) {
-    int r = slice * 32 + lane;
-    float q = sell_row(s, n, val, p32, slice, lane);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int per = (s.nslices + gridDim.x - 1) / gridDim.x;
+  const int sbeg = blockIdx.x * per, send = min(s.nslices, sbeg + per);
+  for (int slice = sbeg + warp; slice < send; slice += kTPB / 32) {
+    const float q = sell_row(s, n, val, p32, slice, lane);
+    const int r = slice * 32 + lane;
     if (r < n) {
       q32[r] = q;
       t += p32[r] * q;
@@ -653,22 +676,38 @@ __device__ __noinline__ void mx_decide(Scal *S, double rrn) {
   }
 }
 
-// y32 += alf p32, r32 -= alf q32, rr' = r32.r32; decides whether a reliable update follows
-__global__ void __launch_bounds__(kTPB, 8)
+// y32 += alf p32, r32 -= alf q32, rr' = r32.r32; decides whether a reliable update
+// follows and, inside the graph, arms the IF node that runs it.  float4 accesses.
+__global__ void __launch_bounds__(kTPB, 6)
     k_mx_update(int n, float *__restrict__ y32, float *__restrict__ r32,
                 const float *__restrict__ p32, const float *__restrict__ q32, Scal *S,
-                double *partials) {
+                double *partials, cudaGraphConditionalHandle hif, int use_cond) {
   if (solve_done(S)) return;
   const float alf = (float)__ldcg(&S->alf);
   float t = 0.f;
-  FCG_GRID_STRIDE(i, n) {
+  const long long n4 = n >> 2;
+  FCG_GRID_STRIDE(i, n4) {
+    float4 y = reinterpret_cast<float4 *>(y32)[i], r = reinterpret_cast<float4 *>(r32)[i];
+    const float4 p = reinterpret_cast<const float4 *>(p32)[i];
+    const float4 q = reinterpret_cast<const float4 *>(q32)[i];
+    y.x += alf * p.x; y.y += alf * p.y; y.z += alf * p.z; y.w += alf * p.w;
+    r.x -= alf * q.x; r.y -= alf * q.y; r.z -= alf * q.z; r.w -= alf * q.w;
+    reinterpret_cast<float4 *>(y32)[i] = y;
+    reinterpret_cast<float4 *>(r32)[i] = r;
+    t += r.x * r.x + r.y * r.y + r.z * r.z + r.w * r.w;
+  }
+  FCG_GRID_STRIDE(j, n - 4 * n4) {
+    long long i = 4 * n4 + j;
     y32[i] = y32[i] + alf * p32[i];
     float r = r32[i] - alf * q32[i];
     r32[i] = r;
     t += r * r;
   }
   double v[1] = {(double)t};
-  if (reduce_commit<1>(v, partials, &S->ticket[2]) && threadIdx.x == 0) mx_decide(S, v[0]);
+  if (reduce_commit<1>(v, partials, &S->ticket[2]) && threadIdx.x == 0) {
+    mx_decide(S, v[0]);
+    if (use_cond) cudaGraphSetConditional(hif, S->ru ? 1u : 0u);
+  }
 }
 
 // reliable update, part 1: x += D^-1/2 y32 in FP64, y32 = 0
@@ -732,8 +771,8 @@ __global__ void __launch_bounds__(kTPB, 8)
     mx_after_update(S, v[0], v[1], trace, h, use_cond);
 }
 
-// p32 = r32 + bet p32; closes the loop body
-__global__ void __launch_bounds__(kTPB, 8)
+// p32 = r32 + bet p32; closes the loop body (float4 accesses)
+__global__ void __launch_bounds__(kTPB, 6)
     k_mx_p(int n, const float *__restrict__ r32, float *__restrict__ p32, Scal *S,
            cudaGraphConditionalHandle h, int use_cond) {
   if (solve_done(S)) {
@@ -742,7 +781,17 @@ __global__ void __launch_bounds__(kTPB, 8)
   }
   loop_guard(S, h, use_cond);
   const float bet = (float)__ldcg(&S->bet);
-  FCG_GRID_STRIDE(i, n) p32[i] = r32[i] + bet * p32[i];
+  const long long n4 = n >> 2;
+  FCG_GRID_STRIDE(i, n4) {
+    const float4 r = reinterpret_cast<const float4 *>(r32)[i];
+    float4 p = reinterpret_cast<float4 *>(p32)[i];
+    p.x = r.x + bet * p.x; p.y = r.y + bet * p.y; p.z = r.z + bet * p.z; p.w = r.w + bet * p.w;
+    reinterpret_cast<float4 *>(p32)[i] = p;
+  }
+  FCG_GRID_STRIDE(j, n - 4 * n4) {
+    long long i = 4 * n4 + j;
+    p32[i] = r32[i] + bet * p32[i];
+  }
 }
 
 // Final FP64 check: ||su - A x||^2 and ||su||^2.
@@ -913,7 +962,8 @@ static const char *sweep_unit_name(int kind, int u) {
 
 // Enqueues unit u of one sweep of solver `kind` on stream st.
 static void enqueue_unit(fcg_context *c, cudaStream_t st, int kind, int u,
-                         cudaGraphConditionalHandle h, int use_cond) {
+                         cudaGraphConditionalHandle h, int use_cond,
+                         cudaGraphConditionalHandle hif = 0) {
   KrylovState *k = c->ks;
   const int n = c->n;
   const SellView &s = c->sv;
@@ -943,12 +993,13 @@ static void enqueue_unit(fcg_context *c, cudaStream_t st, int kind, int u,
         break;
       case 1:
         k_mx_update<<<k->gr.mupd, kTPB, 0, st>>>(n, k->y32, k->r32, k->p32, k->q32, k->S,
-                                                 k->partials);
+                                                 k->partials, hif, use_cond);
         break;
       case 2: k_mx_ru1<<<k->gr.mru1, kTPB, 0, st>>>(n, k->x, k->y32, k->s64, k->S); break;
       case 3:
+        // sets only the stop flag: k_mx_p, after the IF node, ends the WHILE loop
         k_mx_ru2<<<k->gr.mru2, kTPB, 0, st>>>(s, n, k->sval, k->su, k->x, k->res, k->s64, k->r32,
-                                              k->S, k->partials, tr, h, use_cond);
+                                              k->S, k->partials, tr, h, 0);
         break;
       case 4: k_mx_p<<<k->gr.mp, kTPB, 0, st>>>(n, k->r32, k->p32, k->S, h, use_cond); break;
     }
@@ -1005,9 +1056,39 @@ static int build_graph(fcg_context *c, int kind) {
   cudaGraph_t body = np.conditional.phGraph_out[0];
   FCG_CUDA_TRY(c, cudaStreamBeginCaptureToGraph(k->cap, body, nullptr, nullptr, 0,
                                                 cudaStreamCaptureModeThreadLocal));
-  enqueue_sweep(c, k->cap, kind, h, 1);
   cudaGraph_t captured = nullptr;
-  cudaError_t e = cudaStreamEndCapture(k->cap, &captured);
+  cudaError_t e = cudaSuccess;
+  if (kind == SK_MIXED) {
+    // body: spmv -> update -> IF(reliable update){ ru1 -> ru2 } -> p
+    cudaGraphConditionalHandle hif;
+    FCG_CUDA_TRY(c, cudaGraphConditionalHandleCreate(&hif, body, 0, cudaGraphCondAssignDefault));
+    enqueue_unit(c, k->cap, kind, 0, h, 1);
+    enqueue_unit(c, k->cap, kind, 1, h, 1, hif);
+    cudaStreamCaptureStatus cs;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    FCG_CUDA_TRY(c, cudaStreamGetCaptureInfo(k->cap, &cs, nullptr, nullptr, &deps, nullptr, &nd));
+    cudaGraphNodeParams ip = {cudaGraphNodeTypeConditional};
+    ip.conditional.handle = hif;
+    ip.conditional.type = cudaGraphCondTypeIf;
+    ip.conditional.size = 1;
+    cudaGraphNode_t ifnode;
+    FCG_CUDA_TRY(c, cudaGraphAddNode(&ifnode, body, deps, nullptr, nd, &ip));
+    FCG_CUDA_TRY(c, cudaStreamUpdateCaptureDependencies(k->cap, &ifnode, nullptr, 1,
+                                                        cudaStreamSetCaptureDependencies));
+    enqueue_unit(c, k->cap, kind, 4, h, 1);
+    e = cudaStreamEndCapture(k->cap, &captured);
+    if (e == cudaSuccess) {
+      FCG_CUDA_TRY(c, cudaStreamBeginCaptureToGraph(k->cap, ip.conditional.phGraph_out[0], nullptr,
+                                                    nullptr, 0, cudaStreamCaptureModeThreadLocal));
+      enqueue_unit(c, k->cap, kind, 2, h, 1);
+      enqueue_unit(c, k->cap, kind, 3, h, 1);
+      e = cudaStreamEndCapture(k->cap, &captured);
+    }
+  } else {
+    enqueue_sweep(c, k->cap, kind, h, 1);
+    e = cudaStreamEndCapture(k->cap, &captured);
+  }
   if (e != cudaSuccess) {
     cudaGraphDestroy(g);
     return cuda_fail(c, e, "capture of the solver sweep");
