@@ -82,6 +82,8 @@ _PROTOS = {
                                C.POINTER(SolveReport)]),
     "fcg_dpcg_mixed": (C.c_int, [_CTX, _vp, _vp, _vp, _vp, C.c_double, C.c_int, _dp,
                                  C.POINTER(SolveReport)]),
+    "fcg_bicgstab_multi": (C.c_int, [_CTX, C.c_int, _vp, _vp, _vp, C.c_double, C.c_int, _dp,
+                                     C.POINTER(SolveReport)]),
     "fcg_set_solver_options": (C.c_int, [_CTX, C.c_double, C.c_int]),
     "fcg_get_solver_trace": (C.c_int, [_CTX, _vp, C.c_int, _ip]),
     "fcg_spmv": (C.c_int, [_CTX, _vp, _vp, _vp]),

@@ -11,6 +11,7 @@ fcg_context::~fcg_context() {
   dmat.release();
   scratch.release();
   fcg::destroy_krylov(ks);
+  fcg::destroy_multi(ms);
   if (own_stream) cudaStreamDestroy(own_stream);
 }
 

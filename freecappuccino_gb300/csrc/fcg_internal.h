@@ -80,6 +80,8 @@ struct Level {
 namespace fcg {
 struct KrylovState;
 void destroy_krylov(KrylovState *k);
+struct MultiState;
+void destroy_multi(MultiState *m);
 }  // namespace fcg
 
 struct fcg_context {
@@ -116,6 +118,7 @@ struct fcg_context {
   std::vector<fcg::DBuf> stage;
   fcg::DBuf scratch;
   fcg::KrylovState *ks = nullptr;  // solver workspaces and captured graphs (krylov.cu)
+  fcg::MultiState *ms = nullptr;   // multi-RHS BiCGStab workspaces (multi.cu)
 
   ~fcg_context();
 };

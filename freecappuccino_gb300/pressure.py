@@ -210,6 +210,21 @@ class Context:
         """dpcg with FP32 sweeps under FP64 reliable updates (same stop test)."""
         return self._solve(self.lib.fcg_dpcg_mixed, "fcg_dpcg_mixed", a, su, fi, sor, nsw, **kw)
 
+    def bicgstab_multi(self, a, su, fi, sor, nsw):
+        """Several systems on this pattern in one solve: a[nsys, nnz], su and fi[nsys, n].
+        Returns (fi, list of SolveResult)."""
+        a, su = _host(a), _host(su)
+        fi = fi.clone() if _is_torch(fi) else np.array(fi, dtype=np.float64)
+        ns = a.shape[0]
+        resor = (C.c_double * ns)(*([float("nan")] * ns))
+        reps = (_lib.SolveReport * ns)()
+        self._check(self.lib.fcg_bicgstab_multi(self.h, ns, _ptr(a), _ptr(su), _ptr(fi), float(sor),
+                                                int(nsw), resor, reps), "fcg_bicgstab_multi")
+        out = [SolveResult(fi[k], None, reps[k].res0, reps[k].resl, reps[k].iters,
+                           bool(reps[k].converged), None if reps[k].iters == 0 else resor[k],
+                           reps[k].l2_rel, reps[k].seconds) for k in range(ns)]
+        return fi, out
+
     def iccg(self, a, su, fi, sor, nsw, **kw) -> SolveResult:
         """iccg(fi,ifi) (iccg.f90:3-177)."""
         return self._solve(self.lib.fcg_iccg, "fcg_iccg", a, su, fi, sor, nsw, **kw)

@@ -192,6 +192,18 @@ int fcg_bicgstab(fcg_context *ctx, const double *a, const double *su, double *fi
 int fcg_dpcg_mixed(fcg_context *ctx, const double *a, const double *su, double *fi,
                    double *res, double sor, int nsw, double *resor, fcg_solve_report *rep);
 
+/* Several systems on the bound pattern solved together (no single reference call; it
+ * replaces the three bicgstab(u/v/w) calls of calcuvw.f90:441,498,556, which share one
+ * set of off-diagonals, and the bicgstab calls of the k and epsilon equations, e.g.
+ * k_epsilon_std.f90:528).  a[nsys*nnz], su[nsys*n], fi[nsys*n] (system k at offset
+ * k*nnz or k*n), 1 <= nsys <= 8.  DILU-BiCGStab sweeps (bicgstab.f90) in FP32 under an
+ * FP64 defect-correction loop: the FP64 residual su - A x decides convergence with the
+ * reference's test resl/(res0+small) < sor per system; the FP32 solve of each
+ * correction runs until its L1 residual has dropped 1e4-fold.  resor[nsys] and
+ * rep[nsys] (iters = FP32 sweeps of all systems together) may be NULL. */
+int fcg_bicgstab_multi(fcg_context *ctx, int nsys, const double *a, const double *su, double *fi,
+                       double sor, int nsw, double *resor, fcg_solve_report *rep);
+
 /* Constants of the solvers: small (parameters::small, modules_allocatable.f90:27;
  * default the REAL literal 1e-20) and whether a solve returns at once when
  * res0 < 1e-13 (dpcg.f90:66-70; default 1).  The copies of the solvers in

@@ -268,3 +268,34 @@ def test_mixed_dpcg_nsw_cap_and_zero_rhs():
     assert r.iters == 7 and not r.converged
     r = c.dpcg_mixed(a, np.zeros(m.numCells), np.zeros(m.numCells), 1e-8, 100)
     assert r.iters == 0 and r.resor is None
+
+
+# (on the cavity mesh the reference's BiCGStab itself stagnates near 1e-7 on these
+# systems, as it does on the cavity Poisson system; the hex meshes converge)
+@pytest.mark.parametrize("name", ["hex12_u", "hex8", "hex16"])
+def test_multi_rhs_bicgstab_matches_oracle(name):
+    """Five transport systems on one pattern in one solve vs the oracle's FP64 bicgstab
+    of each system: every system meets the reference's stop test on its FP64 residual."""
+    from freecappuccino_gb300.systems import transport_systems
+    m, c = ctx_for(name)
+    csr = oracle_csr(m)
+    a, su, dt = transport_systems(m, (csr.ioffset, csr.ja, csr.diag, csr.slot_pn, csr.slot_np))
+    x, reps = c.bicgstab_multi(a, su, np.zeros_like(su), 1e-10, 2000)
+    for k in range(a.shape[0]):
+        o = oracle.bicgstab(csr, a[k], su[k], np.zeros(m.numCells), 1e-10, 2000)
+        r_true = su[k] - oracle.spmv(csr, a[k], x[k])
+        assert reps[k].converged
+        assert np.abs(r_true).sum() / reps[k].res0 < 1e-10
+        assert reps[k].res0 == pytest.approx(o.res0, rel=1e-12)
+        assert rel(x[k], o.fi) < 1e-8
+
+
+def test_multi_rhs_single_system_equals_stacked():
+    """Systems do not interact: solving one alone gives the same solution as in a batch."""
+    from freecappuccino_gb300.systems import transport_systems
+    m, c = ctx_for("hex8")
+    csr = oracle_csr(m)
+    a, su, _ = transport_systems(m, (csr.ioffset, csr.ja, csr.diag, csr.slot_pn, csr.slot_np))
+    xs, _ = c.bicgstab_multi(a, su, np.zeros_like(su), 1e-10, 2000)
+    x1, _ = c.bicgstab_multi(a[3:4], su[3:4], np.zeros((1, m.numCells)), 1e-10, 2000)
+    assert rel(x1[0], xs[3]) < 1e-7
