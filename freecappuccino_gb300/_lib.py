@@ -54,6 +54,7 @@ class SolveReport(C.Structure):
 
 
 _CTX = C.c_void_p
+_LP = C.c_void_p
 
 # name -> (restype, argtypes)
 _PROTOS = {
@@ -91,6 +92,22 @@ _PROTOS = {
     "fcg_profile_unit_name": (C.c_char_p, [_CTX, C.c_int]),
     "fcg_dpcg_noalloc": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_double,
                                    C.c_int, _dp, C.POINTER(SolveReport), _vp]),
+    # learned preconditioner and flexible CG
+    "fcg_lp_create": (C.c_int, [C.c_int, C.c_ulonglong, C.POINTER(_LP)]),
+    "fcg_lp_destroy": (C.c_int, [_LP]),
+    "fcg_lp_last_error": (C.c_char_p, [_LP]),
+    "fcg_lp_get_weights": (C.c_int, [_LP, _vp, C.c_int]),
+    "fcg_lp_set_weights": (C.c_int, [_LP, _vp, C.c_int]),
+    "fcg_lp_save": (C.c_int, [_LP, C.c_char_p]),
+    "fcg_lp_load": (C.c_int, [_LP, C.c_char_p]),
+    "fcg_lp_set_matrix": (C.c_int, [_LP, _CTX, _vp]),
+    "fcg_lp_features": (C.c_int, [_LP, _CTX, _vp]),
+    "fcg_lp_apply": (C.c_int, [_LP, _CTX, _vp, _vp]),
+    "fcg_lp_loss_grad": (C.c_int, [_LP, _CTX, _vp, _vp, C.POINTER(C.c_float), _vp]),
+    "fcg_lp_train_step": (C.c_int, [_LP, _CTX, _vp, _vp, C.c_float, C.POINTER(C.c_float)]),
+    "fcg_lp_set_fcg_options": (C.c_int, [_LP, C.c_int, C.c_int, C.c_double]),
+    "fcg_fcg_learned": (C.c_int, [_CTX, _LP, _vp, _vp, _vp, _vp, C.c_double, C.c_int, _dp,
+                                  C.POINTER(SolveReport), _ip, _ip]),
     # synthetic inputs (include/fcgpu_meshgen.h)
     "fcg_hex_mesh_sizes": (C.c_int, [C.c_int, _ip, _ip, _ip, _ip]),
     "fcg_hex_mesh_build": (C.c_int, [C.c_int, C.c_double, C.c_ulonglong, _vp, _vp, _vp, _vp,

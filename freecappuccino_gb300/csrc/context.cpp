@@ -1,4 +1,5 @@
 // Context lifecycle, mesh binding, CSR export and host<->device staging of libfcgpu.so.
+#include <atomic>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -122,7 +123,9 @@ extern "C" int fcg_create(fcg_context **out, int device) {
   if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return FCG_ERR_CUDA;
   if (prop.major * 10 + prop.minor < 100) return FCG_ERR_CUDA;  // built for sm_103a only
   if (cudaSetDevice(device) != cudaSuccess) return FCG_ERR_CUDA;
+  static std::atomic<unsigned long long> next_uid{1};
   fcg_context *c = new fcg_context();
+  c->uid = next_uid++;
   c->device = device;
   c->num_sms = prop.multiProcessorCount;
   if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) {

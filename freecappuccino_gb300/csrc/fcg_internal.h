@@ -85,6 +85,7 @@ void destroy_multi(MultiState *m);
 }  // namespace fcg
 
 struct fcg_context {
+  unsigned long long uid = 0;  // unique per process: handles key cached state on it
   int device = 0;
   int num_sms = 0;
   cudaStream_t stream = nullptr;
@@ -152,6 +153,13 @@ int stage_in(fcg_context *c, const void *user, size_t bytes, int slot, bool copy
              bool *was_host);
 int stage_out(fcg_context *c, void *user, const void *dev, size_t bytes, bool was_host);
 bool is_device_pointer(const void *p);
+
+// Solver matrices shared with the learned preconditioner (krylov.cu): loads CSR values
+// a (device) and builds D^-1/2 (FP64) and D^-1/2 A D^-1/2 (FP32) in the sliced layout.
+int prepare_scaled32(fcg_context *c, const double *a_dev);
+const float *scaled32(const fcg_context *c);
+const double *scale64(const fcg_context *c);
+const double *sliced64(const fcg_context *c);
 
 }  // namespace fcg
 

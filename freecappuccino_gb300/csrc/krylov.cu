@@ -807,6 +807,45 @@ static int load_matrix(fcg_context *c, const double *da) {
   return FCG_OK;
 }
 
+// FP32 copy of D^-1/2 A D^-1/2 in the sliced layout and D^-1/2 in FP64, from the
+// matrix load_matrix() placed in the state (used by the mixed and learned solvers).
+int build_scaled32(fcg_context *c) {
+  KrylovState *k = c->ks;
+  if (!k->mixed_ready) {
+    size_t n4 = ((size_t)c->n + 63) & ~(size_t)63;
+    size_t bytes = sizeof(double) * n4 + sizeof(float) * (4 * n4 + (size_t)c->sell_len + 64);
+    FCG_CUDA_TRY(c, k->mixed.ensure(bytes));
+    k->s64 = k->mixed.as<double>();
+    float *f = (float *)(k->s64 + n4);
+    k->y32 = f;
+    k->r32 = f + n4;
+    k->p32 = f + 2 * n4;
+    k->q32 = f + 3 * n4;
+    k->sval32 = f + 4 * n4;
+    k->mixed_ready = true;
+    if (k->exec[SK_MIXED]) cudaGraphExecDestroy(k->exec[SK_MIXED]);  // buffers moved: recapture
+    if (k->graph[SK_MIXED]) cudaGraphDestroy(k->graph[SK_MIXED]);
+    k->exec[SK_MIXED] = nullptr;
+    k->graph[SK_MIXED] = nullptr;
+  }
+  k_mx_scale<<<grid_for(c->n, c->num_sms), kTPB, 0, c->stream>>>(c->n, c->mv.diag, k->a, k->s64);
+  k_mx_fill<<<grid_for((long long)c->sv.nslices * 32, c->num_sms), kTPB, 0, c->stream>>>(
+      c->sv, c->n, k->a, k->s64, k->sval32);
+  FCG_CHECK_LAUNCH(c, "scaled FP32 matrix");
+  return FCG_OK;
+}
+
+int prepare_scaled32(fcg_context *c, const double *a_dev) {
+  int rc = ensure_state(c, 1);
+  if (rc) return rc;
+  if ((rc = load_matrix(c, a_dev))) return rc;
+  return build_scaled32(c);
+}
+
+const float *scaled32(const fcg_context *c) { return c->ks ? c->ks->sval32 : nullptr; }
+const double *scale64(const fcg_context *c) { return c->ks ? c->ks->s64 : nullptr; }
+const double *sliced64(const fcg_context *c) { return c->ks ? c->ks->sval : nullptr; }
+
 static void launch_sweeps(fcg_context *c, cudaStream_t st, const Level &lv, bool forward,
                           const double *b, double *z) {
   KrylovState *k = c->ks;
@@ -1032,28 +1071,7 @@ static int run_solver(fcg_context *c, int kind, const double *a, const double *s
   if (kind == SK_BICG)
     FCG_CUDA_TRY(c, cudaMemcpyAsync(k->reso, k->res, n1, cudaMemcpyDeviceToDevice, c->stream));
   if (kind == SK_MIXED) {
-    if (!k->mixed_ready) {
-      size_t n4 = ((size_t)c->n + 63) & ~(size_t)63;
-      size_t bytes = sizeof(double) * n4 + sizeof(float) * (4 * n4 + (size_t)c->sell_len + 64);
-      FCG_CUDA_TRY(c, k->mixed.ensure(bytes));
-      k->s64 = k->mixed.as<double>();
-      float *f = (float *)(k->s64 + n4);
-      k->y32 = f;
-      k->r32 = f + n4;
-      k->p32 = f + 2 * n4;
-      k->q32 = f + 3 * n4;
-      k->sval32 = f + 4 * n4;
-      k->mixed_ready = true;
-      for (int i = SK_MIXED; i <= SK_MIXED; ++i) {  // buffers moved: recapture
-        if (k->exec[i]) cudaGraphExecDestroy(k->exec[i]);
-        if (k->graph[i]) cudaGraphDestroy(k->graph[i]);
-        k->exec[i] = nullptr;
-        k->graph[i] = nullptr;
-      }
-    }
-    k_mx_scale<<<grid_for(c->n, c->num_sms), kTPB, 0, c->stream>>>(c->n, c->mv.diag, k->a, k->s64);
-    k_mx_fill<<<grid_for((long long)c->sv.nslices * 32, c->num_sms), kTPB, 0, c->stream>>>(
-        c->sv, c->n, k->a, k->s64, k->sval32);
+    if ((rc = build_scaled32(c))) return rc;
     k_mx_start<<<k->gr.mstart, kTPB, 0, c->stream>>>(c->n, k->res, k->s64, k->r32, k->y32,
                                                      k->p32, k->S, k->partials);
     FCG_CHECK_LAUNCH(c, "mixed set-up");

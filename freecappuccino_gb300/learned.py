@@ -1,0 +1,278 @@
+"""Learned preconditioner for the pressure solve and the flexible CG that uses it.
+
+No reference counterpart: the reference solves the pressure equation with dpcg/iccg
+(dpcg.f90, iccg.f90).  Here a small message-passing network (libfcgpu.so, learned.cu)
+approximates the inverse of the Jacobi-scaled pressure matrix and serves as the
+preconditioner of a flexible CG; plain FP64 DPCG stays the fallback (taken when the
+FCG stalls) and the judge of the result (the stop test is dpcg.f90's L1 test on the
+FP64 residual).  Training data are (residual, error) pairs of DPCG iterates on seeded
+jittered meshes with a smoothed log-uniform diffusivity; training runs on the GPU
+through the library's own forward, backward and Adam kernels.
+
+Vectors of the network live in the scaled system: r = D^-1/2 (su - A x) and
+e = D^1/2 (x* - x), FP32, D = diag(A).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .mesh import Mesh, hex_mesh, uniform
+from .pressure import Context, SolveResult, _host, _is_torch, _ptr
+
+WIDTH, LAYERS, FEATURES, PARAMS = 32, 6, 6, 12737
+# default checkpoint shipped with the package (trained by train_default())
+DEFAULT_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights",
+                               "lp_c32_l6.fcglp")
+
+
+def _f32(x):
+    if _is_torch(x):
+        import torch
+
+        return x.to(torch.float32).contiguous()
+    return np.ascontiguousarray(x, dtype=np.float32)
+
+
+class LearnedPreconditioner:
+    """An fcg_learned handle: FP32 weights and Adam state on one device."""
+
+    def __init__(self, device: int = 0, seed: int = 0, path: str | None = None):
+        self.lib = _lib.load()
+        h = C.c_void_p()
+        rc = self.lib.fcg_lp_create(int(device), int(seed), C.byref(h))
+        if rc != 0:
+            raise _lib.FcgError(rc, "fcg_lp_create", "no usable sm_103a CUDA device")
+        self.h = h
+        if path is not None:
+            self.load(path)
+
+    def _check(self, rc, where):
+        if rc != 0:
+            raise _lib.FcgError(rc, where, self.lib.fcg_lp_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fcg_lp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- weights ------------------------------------------------------------------
+    @property
+    def weights(self) -> np.ndarray:
+        w = np.zeros(PARAMS, np.float32)
+        self._check(self.lib.fcg_lp_get_weights(self.h, _ptr(w), PARAMS), "fcg_lp_get_weights")
+        return w
+
+    @weights.setter
+    def weights(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        self._check(self.lib.fcg_lp_set_weights(self.h, _ptr(w), int(w.size)), "fcg_lp_set_weights")
+
+    def save(self, path: str):
+        self._check(self.lib.fcg_lp_save(self.h, os.fsencode(path)), "fcg_lp_save")
+
+    def load(self, path: str):
+        self._check(self.lib.fcg_lp_load(self.h, os.fsencode(path)), "fcg_lp_load")
+
+    # -- network ------------------------------------------------------------------
+    def set_matrix(self, ctx: Context, a):
+        self._check(self.lib.fcg_lp_set_matrix(self.h, ctx.h, _ptr(_host(a))), "fcg_lp_set_matrix")
+
+    def features(self, ctx: Context) -> np.ndarray:
+        out = np.zeros((ctx.n, FEATURES), np.float32)
+        self._check(self.lib.fcg_lp_features(self.h, ctx.h, _ptr(out)), "fcg_lp_features")
+        return out
+
+    def apply(self, ctx: Context, r):
+        r = _f32(r)
+        if _is_torch(r):
+            import torch
+
+            z = torch.empty_like(r)
+        else:
+            z = np.zeros_like(r)
+        self._check(self.lib.fcg_lp_apply(self.h, ctx.h, _ptr(r), _ptr(z)), "fcg_lp_apply")
+        return z
+
+    def loss_grad(self, ctx: Context, r, e):
+        r, e = _f32(r), _f32(e)
+        loss = C.c_float()
+        g = np.zeros(PARAMS, np.float32)
+        self._check(self.lib.fcg_lp_loss_grad(self.h, ctx.h, _ptr(r), _ptr(e), C.byref(loss),
+                                              _ptr(g)), "fcg_lp_loss_grad")
+        return float(loss.value), g
+
+    def train_step(self, ctx: Context, r, e, lr: float) -> float:
+        r, e = _f32(r), _f32(e)
+        loss = C.c_float()
+        self._check(self.lib.fcg_lp_train_step(self.h, ctx.h, _ptr(r), _ptr(e), float(lr),
+                                               C.byref(loss)), "fcg_lp_train_step")
+        return float(loss.value)
+
+    def set_fcg_options(self, ru_every: int = 50, stall_window: int = 400,
+                        stall_factor: float = 0.5):
+        self._check(self.lib.fcg_lp_set_fcg_options(self.h, int(ru_every), int(stall_window),
+                                                    float(stall_factor)), "fcg_lp_set_fcg_options")
+
+    # -- solver ---------------------------------------------------------------------
+    def solve(self, ctx: Context, a, su, fi, sor: float, nsw: int) -> "FcgResult":
+        """Learned-preconditioned flexible CG with the arguments of dpcg(fi,ifi)."""
+        a, su = _host(a), _host(su)
+        fi = fi.clone() if _is_torch(fi) else np.array(fi, dtype=np.float64)
+        if _is_torch(su):
+            import torch
+
+            res = torch.zeros_like(su)
+        else:
+            res = np.zeros(ctx.n)
+        resor = C.c_double(float("nan"))
+        rep = _lib.SolveReport()
+        it, fb = C.c_int(), C.c_int()
+        rc = self.lib.fcg_fcg_learned(ctx.h, self.h, _ptr(a), _ptr(su), _ptr(fi), _ptr(res),
+                                      float(sor), int(nsw), C.byref(resor), C.byref(rep),
+                                      C.byref(it), C.byref(fb))
+        ctx._check(rc, "fcg_fcg_learned")
+        return FcgResult(fi, res, rep.res0, rep.resl, rep.iters, bool(rep.converged),
+                         None if rep.iters == 0 else resor.value, rep.l2_rel, rep.seconds,
+                         fcg_iters=it.value, fallback=bool(fb.value))
+
+
+@dataclass
+class FcgResult(SolveResult):
+    fcg_iters: int = 0
+    fallback: bool = False
+
+
+# ---------------------------------------------------------------------------------
+# Training data
+# ---------------------------------------------------------------------------------
+def diffusivity_field(m: Mesh, seed: int, lo: float = 0.1, hi: float = 10.0,
+                      passes: int = 3) -> np.ndarray:
+    """Per-cell diffusivity: log-uniform on [lo, hi], then `passes` Jacobi smoothing
+    passes of log(diffusivity) over face neighbours (each cell becomes the mean of
+    itself and its neighbours)."""
+    g = np.log(lo) + (np.log(hi) - np.log(lo)) * uniform(seed, 9000, m.numCells, 0.0, 1.0)
+    nin = m.numInnerFaces
+    P, N = m.owner[:nin] - 1, m.neighbour[:nin] - 1
+    cnt = np.ones(m.numCells)
+    np.add.at(cnt, P, 1.0)
+    np.add.at(cnt, N, 1.0)
+    for _ in range(passes):
+        s = g.copy()
+        np.add.at(s, P, g[N])
+        np.add.at(s, N, g[P])
+        g = s / cnt
+    return np.exp(g)
+
+
+@dataclass
+class TrainingSystem:
+    mesh: Mesh
+    ctx: Context
+    a: np.ndarray
+    su: np.ndarray
+    scale: np.ndarray  # D^-1/2
+
+
+def pressure_system(N: int, jitter: float, seed: int, variable: bool = True,
+                    device: int = 0) -> TrainingSystem:
+    """A pressure Poisson system on the N^3 jittered hex mesh: the laplacian with
+    diffusivity `diffusivity_field` (or 1), RHS uniform[-1,1] * vol."""
+    m = hex_mesh(N, jitter=jitter, seed=seed)
+    ctx = Context(m, device)
+    gam = diffusivity_field(m, seed) if variable else np.ones(m.numCells)
+    su0 = uniform(seed, 0, m.numCells) * m.vol
+    a, su = ctx.laplacian(-gam, np.zeros(m.numTotal), su0)
+    io, ja, dg, _, _ = ctx.create_csr()
+    return TrainingSystem(m, ctx, a, su, 1.0 / np.sqrt(a[dg - 1]))
+
+
+def dpcg_pairs(sysm: TrainingSystem, ks, tight: float = 1e-13, nsw_max: int = 20000,
+               device=None):
+    """(r, e) pairs of the scaled system from DPCG iterates x_k (k sweeps from x = 0):
+    r = D^-1/2 (su - A x_k), e = D^1/2 (x* - x_k), x* solved to `tight`.  FP32 arrays,
+    or CUDA tensors when `device` is a torch device."""
+    ctx, a, su, s = sysm.ctx, sysm.a, sysm.su, sysm.scale
+    zero = np.zeros(ctx.n)
+    xs = ctx.dpcg(a, su, zero, tight, nsw_max).fi
+    out = []
+    for k in ks:
+        x = ctx.dpcg(a, su, zero, 0.0, int(k)).fi if k > 0 else zero
+        r = (su - ctx.spmv(a, x)) * s
+        e = (xs - x) / s
+        r, e = r.astype(np.float32), e.astype(np.float32)
+        if device is not None:
+            import torch
+
+            r, e = torch.from_numpy(r).to(device), torch.from_numpy(e).to(device)
+        out.append((r, e))
+    return out
+
+
+def train(lp: LearnedPreconditioner, systems, pairs, steps: int, lr: float = 1e-3, seed: int = 0,
+          log_every: int = 0, log=print):
+    """Adam on the pairs: `pairs[i]` is a list of (r, e) for `systems[i]`; each step
+    takes one pair drawn uniformly (seeded).  Returns the per-step losses."""
+    rng = np.random.default_rng(seed)
+    flat = [(i, j) for i, ps in enumerate(pairs) for j in range(len(ps))]
+    losses = np.zeros(steps)
+    try:  # device copies of the matrices: switching systems is then a device copy
+        import torch
+
+        mats = [torch.from_numpy(np.ascontiguousarray(s.a)).cuda() for s in systems]
+    except Exception:
+        mats = [s.a for s in systems]
+    cur = None
+    t0 = time.perf_counter()
+    for step in range(steps):
+        i, j = flat[rng.integers(len(flat))]
+        if cur != i:
+            lp.set_matrix(systems[i].ctx, mats[i])
+            cur = i
+        r, e = pairs[i][j]
+        losses[step] = lp.train_step(systems[i].ctx, r, e, lr)
+        if log_every and (step + 1) % log_every == 0:
+            log(f"step {step + 1}: mean loss {losses[step + 1 - log_every:step + 1].mean():.4f} "
+                f"({time.perf_counter() - t0:.1f} s)")
+    return losses
+
+
+def train_default(path: str = DEFAULT_WEIGHTS, steps: int = 20000, n_pairs: int = 2000,
+                  sizes=(64, 96), systems_per_size: int = 5, lr: float = 1e-3, seed: int = 7,
+                  log=print):
+    """The shipped checkpoint: `n_pairs` DPCG-iterate pairs from jittered meshes of the
+    given sizes (jitter uniform on [0, 0.25] per mesh, smoothed log-uniform diffusivity
+    on [0.1, 10]), Adam with rate `lr` for `steps` steps."""
+    import torch
+
+    dev = torch.device("cuda")
+    per = n_pairs // (len(sizes) * systems_per_size)
+    systems, pairs = [], []
+    t0 = time.perf_counter()
+    for si, N in enumerate(sizes):
+        for j in range(systems_per_size):
+            sd = seed * 1000 + si * 100 + j
+            jit = 0.25 * uniform(sd, 77, 1, 0.0, 1.0)[0]
+            sysm = pressure_system(N, jit, sd)
+            conv = sysm.ctx.dpcg(sysm.a, sysm.su, np.zeros(sysm.ctx.n), 1e-8, 20000).iters
+            ks = np.unique(np.round(np.linspace(0, conv, per)).astype(int))
+            systems.append(sysm)
+            pairs.append(dpcg_pairs(sysm, ks, device=dev))
+            log(f"N={N} jitter={jit:.3f}: DPCG {conv} sweeps, {len(ks)} pairs "
+                f"({time.perf_counter() - t0:.1f} s)")
+    lp = LearnedPreconditioner(seed=seed)
+    losses = train(lp, systems, pairs, steps, lr, seed, log_every=max(1, steps // 20), log=log)
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    lp.save(path)
+    return lp, losses

@@ -245,6 +245,74 @@ const char *fcg_profile_unit_name(const fcg_context *ctx, int unit);
  * the matrix of the previous solve or spmv call. */
 int fcg_spmv(fcg_context *ctx, const double *a, const double *x, double *y);
 
+/* ---------------------------------------------------------------------------------
+ * Learned preconditioner (no reference counterpart; it is used in place of the
+ * Jacobi preconditioner of dpcg.f90:85-100 inside flexible CG, with dpcg as fallback).
+ *
+ * A message-passing network of FCG_LP_LAYERS layers of width FCG_LP_WIDTH maps the
+ * residual of the scaled system Ahat = D^-1/2 A D^-1/2 (D = diag(A)) to an
+ * approximation of its error Ahat^-1 r.  Per-cell inputs (FCG_LP_FEATURES): the
+ * residual divided by its rms, log(a_PP / vol^1/3) - log 6, log(vol / mean vol) and
+ * the three face-area sums sum|S_x,y,z| / (2 vol^2/3) - 1.  Layer l:
+ * h_l = h_{l-1} + relu(W_l [h_{l-1}; Ahat h_{l-1}] + b_l), BF16 activations, tensor
+ * cores with FP32 accumulation.  Output: N(r) = r + rms(r) (w_out . h_L + b_out) -- the
+ * Jacobi preconditioner plus a learned correction (zero output weights at creation).  Weights are
+ * FP32 (FCG_LP_PARAMS values in the order W_in[32][6], b_in[32], then per layer
+ * W_l[32][64] (row = output channel, columns h then Ahat h), b_l[32], then w_out[32],
+ * b_out).  A handle holds weights and Adam state on one device and can serve several
+ * contexts on that device; its calls are ordered on the stream of the context they
+ * are given.  Vectors r, z, e are FP32 of numCells values in the scaled system
+ * (r = D^-1/2 (su - A x), e = D^1/2 (x* - x)), host or device memory.  Errors of the
+ * fcg_lp_* calls are described by fcg_lp_last_error. */
+#define FCG_LP_WIDTH 32
+#define FCG_LP_LAYERS 6
+#define FCG_LP_FEATURES 6
+#define FCG_LP_PARAMS 12737
+typedef struct fcg_learned fcg_learned;
+int fcg_lp_create(int device, unsigned long long seed, fcg_learned **out);
+int fcg_lp_destroy(fcg_learned *lp);
+const char *fcg_lp_last_error(const fcg_learned *lp);
+/* FP32 weights out / in (count must be FCG_LP_PARAMS); set clears the Adam state. */
+int fcg_lp_get_weights(fcg_learned *lp, float *out, int count);
+int fcg_lp_set_weights(fcg_learned *lp, const float *w, int count);
+/* Checkpoint of weights and Adam state: magic "FCGLP001", int32 width, layers,
+ * features, parameter count, int64 step, then weights, Adam m, Adam v (FP32). */
+int fcg_lp_save(fcg_learned *lp, const char *path);
+int fcg_lp_load(fcg_learned *lp, const char *path);
+/* Loads CSR values a[nnz] into the context, builds Ahat in FP32 and the features. */
+int fcg_lp_set_matrix(fcg_learned *lp, fcg_context *ctx, const double *a);
+/* Features of the last fcg_lp_set_matrix: out[numCells][FCG_LP_FEATURES] (column 0 is
+ * the residual input of the last forward pass). */
+int fcg_lp_features(fcg_learned *lp, fcg_context *ctx, float *out);
+/* z = N(r). */
+int fcg_lp_apply(fcg_learned *lp, fcg_context *ctx, const float *r, float *z);
+/* Energy-norm loss (N(r) - e).Ahat (N(r) - e) / e.Ahat e and d loss / d weights
+ * (grad[FCG_LP_PARAMS], may be NULL); BF16 roundings are treated as identities in the
+ * gradient. */
+int fcg_lp_loss_grad(fcg_learned *lp, fcg_context *ctx, const float *r, const float *e,
+                     float *loss, float *grad);
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on the pair (r, e) with rate lr;
+ * *loss (may be NULL) receives the loss before the step. */
+int fcg_lp_train_step(fcg_learned *lp, fcg_context *ctx, const float *r, const float *e,
+                      float lr, float *loss);
+/* Flexible-CG controls: FP64 residual replacement at least every ru_every iterations
+ * (default 50); the FCG is declared stalled when the true L1 residual has not fallen
+ * below stall_factor (default 0.5) times its value at the last such drop within
+ * stall_window iterations (default 400). */
+int fcg_lp_set_fcg_options(fcg_learned *lp, int ru_every, int stall_window, double stall_factor);
+
+/* Flexible CG (Notay 2000, one previous direction) preconditioned by the network, on
+ * the arguments of fcg_dpcg and with its stop test resl/(res0+small) < sor on the
+ * FP64 L1 residual.  The iteration runs in FP32 on Ahat with reliable updates: the
+ * true residual su - A x is recomputed in FP64 when the FP32 residual has fallen 10x,
+ * predicts convergence, or ru_every iterations have passed.  When the FCG stalls or a
+ * value turns non-finite, fcg_dpcg continues from the current solution with the
+ * remaining sweeps (rep->iters counts both; *fcg_iters the FCG iterations and
+ * *fallback 1 when fcg_dpcg ran; both may be NULL). */
+int fcg_fcg_learned(fcg_context *ctx, fcg_learned *lp, const double *a, const double *su,
+                    double *fi, double *res, double sor, int nsw, double *resor,
+                    fcg_solve_report *rep, int *fcg_iters, int *fallback);
+
 #ifdef __cplusplus
 }
 #endif
