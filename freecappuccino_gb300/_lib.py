@@ -55,6 +55,7 @@ class SolveReport(C.Structure):
 
 _CTX = C.c_void_p
 _LP = C.c_void_p
+_BATCH = C.c_void_p
 
 # name -> (restype, argtypes)
 _PROTOS = {
@@ -92,6 +93,15 @@ _PROTOS = {
     "fcg_profile_unit_name": (C.c_char_p, [_CTX, C.c_int]),
     "fcg_dpcg_noalloc": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_double,
                                    C.c_int, _dp, C.POINTER(SolveReport), _vp]),
+    # batched DPCG
+    "fcg_batch_create": (C.c_int, [_vp, C.c_int, C.POINTER(_BATCH)]),
+    "fcg_batch_destroy": (C.c_int, [_BATCH]),
+    "fcg_batch_last_error": (C.c_char_p, [_BATCH]),
+    "fcg_batch_set_params": (C.c_int, [_BATCH, C.c_int, C.c_int]),
+    "fcg_batch_get_params": (C.c_int, [_BATCH, _ip, _ip, _ip]),
+    "fcg_batch_dpcg": (C.c_int, [_BATCH, _vp, _vp, _vp, C.c_double, C.c_int, _dp,
+                                 C.POINTER(SolveReport)]),
+    "fcg_batch_autotune": (C.c_int, [_BATCH, _vp, _vp, C.c_int, _dp]),
     # learned preconditioner and flexible CG
     "fcg_lp_create": (C.c_int, [C.c_int, C.c_ulonglong, C.POINTER(_LP)]),
     "fcg_lp_destroy": (C.c_int, [_LP]),
@@ -105,7 +115,8 @@ _PROTOS = {
     "fcg_lp_apply": (C.c_int, [_LP, _CTX, _vp, _vp]),
     "fcg_lp_loss_grad": (C.c_int, [_LP, _CTX, _vp, _vp, C.POINTER(C.c_float), _vp]),
     "fcg_lp_train_step": (C.c_int, [_LP, _CTX, _vp, _vp, C.c_float, C.POINTER(C.c_float)]),
-    "fcg_lp_set_fcg_options": (C.c_int, [_LP, C.c_int, C.c_int, C.c_double]),
+    "fcg_lp_set_loss": (C.c_int, [_LP, C.c_int]),
+    "fcg_lp_set_fcg_options": (C.c_int, [_LP, C.c_int, C.c_int, C.c_int, C.c_double]),
     "fcg_fcg_learned": (C.c_int, [_CTX, _LP, _vp, _vp, _vp, _vp, C.c_double, C.c_int, _dp,
                                   C.POINTER(SolveReport), _ip, _ip]),
     # synthetic inputs (include/fcgpu_meshgen.h)

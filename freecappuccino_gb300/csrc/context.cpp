@@ -13,6 +13,7 @@ fcg_context::~fcg_context() {
   scratch.release();
   fcg::destroy_krylov(ks);
   fcg::destroy_multi(ms);
+  if (switch_ev) cudaEventDestroy(switch_ev);
   if (own_stream) cudaStreamDestroy(own_stream);
 }
 
@@ -145,9 +146,19 @@ extern "C" int fcg_destroy(fcg_context *c) {
   return FCG_OK;
 }
 
+// Work queued later on the new stream is ordered after work already queued on the old
+// one (an event, no host wait); the old stream must still exist.
 extern "C" int fcg_set_stream(fcg_context *c, void *s) {
   if (!c) return FCG_ERR_ARG;
-  c->stream = s ? (cudaStream_t)s : c->own_stream;
+  cudaStream_t ns = s ? (cudaStream_t)s : c->own_stream;
+  if (ns != c->stream) {
+    FCG_CUDA_TRY(c, cudaSetDevice(c->device));
+    if (!c->switch_ev)
+      FCG_CUDA_TRY(c, cudaEventCreateWithFlags(&c->switch_ev, cudaEventDisableTiming));
+    FCG_CUDA_TRY(c, cudaEventRecord(c->switch_ev, c->stream));
+    FCG_CUDA_TRY(c, cudaStreamWaitEvent(ns, c->switch_ev, 0));
+  }
+  c->stream = ns;
   return FCG_OK;
 }
 

@@ -90,6 +90,7 @@ struct fcg_context {
   int num_sms = 0;
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
+  cudaEvent_t switch_ev = nullptr;  // orders a new stream after the old (fcg_set_stream)
   std::string err;
   bool bound = false;
   unsigned bind_gen = 0;  // bumped by every fcg_bind_mesh; captured graphs depend on it
@@ -160,6 +161,16 @@ int prepare_scaled32(fcg_context *c, const double *a_dev);
 const float *scaled32(const fcg_context *c);
 const double *scale64(const fcg_context *c);
 const double *sliced64(const fcg_context *c);
+
+// Device vectors of one system of a batched solve (krylov.cu): loads CSR values a
+// (device; NULL reuses the loaded matrix), su and the initial guess into the context's
+// solver state and returns its FP64 sliced matrix, 1/a(diag) and vectors.
+struct BatchVecs {
+  const double *val, *invd, *su;
+  double *x, *res, *p, *q;
+};
+int batch_load(fcg_context *c, const double *a_dev, const double *su_dev, const double *fi_dev,
+               BatchVecs *out);
 
 }  // namespace fcg
 

@@ -842,6 +842,30 @@ int prepare_scaled32(fcg_context *c, const double *a_dev) {
   return build_scaled32(c);
 }
 
+int batch_load(fcg_context *c, const double *a_dev, const double *su_dev, const double *fi_dev,
+               BatchVecs *out) {
+  int rc = ensure_state(c, 1);
+  if (rc) return rc;
+  KrylovState *k = c->ks;
+  if (a_dev) {
+    if ((rc = load_matrix(c, a_dev))) return rc;
+  } else if (!k->matrix_loaded) {
+    return set_error(c, FCG_ERR_STATE, "batched solve with a == NULL before a matrix was loaded");
+  }
+  const size_t n1 = sizeof(double) * c->n;
+  FCG_CUDA_TRY(c, cudaMemcpyAsync(k->su, su_dev, n1, cudaMemcpyDeviceToDevice, c->stream));
+  FCG_CUDA_TRY(c, cudaMemcpyAsync(k->x, fi_dev, n1, cudaMemcpyDeviceToDevice, c->stream));
+  FCG_CUDA_TRY(c, cudaMemsetAsync(k->pk, 0, n1, c->stream));
+  out->val = k->sval;
+  out->invd = k->invd;
+  out->su = k->su;
+  out->x = k->x;
+  out->res = k->res;
+  out->p = k->pk;
+  out->q = k->qk;
+  return FCG_OK;
+}
+
 const float *scaled32(const fcg_context *c) { return c->ks ? c->ks->sval32 : nullptr; }
 const double *scale64(const fcg_context *c) { return c->ks ? c->ks->s64 : nullptr; }
 const double *sliced64(const fcg_context *c) { return c->ks ? c->ks->sval : nullptr; }

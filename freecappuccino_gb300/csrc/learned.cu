@@ -14,17 +14,23 @@
 // Activations are stored in BF16.  The 64 -> 32 products of the layers run on tensor
 // cores (mma.sync m16n8k16, BF16 operands, FP32 accumulation; weights staged in shared
 // memory); the aggregation Ahat h gathers BF16 neighbour activations through the FP32
-// scaled matrix of the sliced layout the solvers use.  Training minimises the energy
-// norm of the error of z, (z - e^).Ahat (z - e^) / e^.Ahat e^, the norm CG itself
-// minimises, on (residual, error) pairs.  It keeps FP32 master weights: the forward
-// pass saves its pre-activations, the backward pass runs in FP32
+// scaled matrix of the sliced layout the solvers use.  Training minimises, on
+// (residual, error) pairs, the error of z in the residual norm,
+// |Ahat z - r^|^2 / |r^|^2 = |Ahat (z - e^)|^2 / |Ahat e^|^2 (default), or in the energy
+// norm (z - e^).Ahat (z - e^) / e^.Ahat e^.  Measured on jittered 64^3 and 128^3
+// pressure systems, the energy-norm loss drives the network towards corrections of the
+// smooth error that six hops cannot represent and the flexible CG stalls, while the
+// residual-norm loss (the sparse-approximate-inverse criterion) gives 3.4-4.5x fewer
+// iterations than Jacobi.  It keeps FP32 master weights: the forward pass saves its
+// pre-activations, the backward pass runs in FP32
 // (the BF16 roundings pass gradients through unchanged), weight gradients are summed per
 // block and then over blocks in index order (deterministic), and Adam updates the
 // weights and refreshes their BF16 copies.
 //
-// Flexible CG (Notay, SIAM J. Sci. Comput. 22 (2000) 1444, truncated to one previous
-// direction): z = N(r), p = z - (z.q_old / p_old.q_old) p_old, q = Ahat p,
-// alpha = p.r / p.q.  It runs in FP32 on the scaled system with reliable updates in
+// Flexible CG (Notay, SIAM J. Sci. Comput. 22 (2000) 1444, truncated to the last m
+// directions, m <= 8): z = N(r), p = z - sum_j (z.q_j / p_j.q_j) p_j, q = Ahat p,
+// alpha = p.r / p.q.  Keeping several directions makes the iteration robust to the
+// network being a nonlinear preconditioner.  It runs in FP32 on the scaled system with reliable updates in
 // FP64 (true residual su - A x recomputed, correction folded into the FP64 solution,
 // also at least every `ru_every` iterations) and the reference's L1 stop test on the
 // true residual.  When the true residual has not fallen by `stall_factor` within
@@ -57,16 +63,20 @@ static_assert(P == FCG_LP_PARAMS, "parameter count must match the header");
 constexpr int kBwdTile = 64;            // cells per shared-memory tile of the layer backward
 constexpr int kTileStride = 2 * C + 8;  // padded BF16 row of the [h; m] tile and of W_l
 constexpr int kRed = 8;                 // reduction tickets
+constexpr int kMaxDir = 8;              // most previous directions the FCG keeps
 
 // Device scalars of one learned FCG solve.
 struct LScal {
   double res0, resl, small, resmax;
   double rr, maxr, l1ratio, delta;
-  double zq, pq, alf, bet;
+  double pqs[kMaxDir];  // p_j . Ahat p_j of the stored directions (ring slots)
+  double bets[kMaxDir]; // z . q_j / p_j . q_j of the current iteration
+  double alf;
   double chk_l1, stall_factor;
   double l2r, l2b;
   int iter, nsw, done, converged, status, ru, nupdates, last_ru;
-  int chk_iter, stall_window, ru_every, first;
+  int chk_iter, stall_window, ru_every;
+  int mdir, nwin, head;  // directions kept, directions stored, slot of the next one
   unsigned int ticket[kRed];
   unsigned int body_count;
 };
@@ -103,7 +113,8 @@ struct fcg_learned {
   std::vector<const void *> graph_key;
   cudaStream_t cap = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  int ru_every = 50, stall_window = 400;
+  int mdir = 8, ru_every = 50, stall_window = 400;
+  int loss_kind = 1;  // 0 energy norm, 1 residual norm
   double stall_factor = 0.5, delta = 0.1;
 };
 
@@ -216,12 +227,23 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4],
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-// One message-passing layer.  A warp owns 16 cells at a time.  Two lanes per cell sum
-// m = Ahat h over the cell's sliced row (16 channels each) and write the [h; m] row
-// (64 BF16) into the warp's shared tile; 4 k-steps x 4 n-blocks of mma.sync give the
-// 16 x 32 pre-activation; the epilogue adds the bias, applies the ReLU and the skip
-// connection and stores h' as BF16.  Rows of the tile and of W_l are padded to 72
-// elements so that the fragment loads of the 8 row groups fall in distinct banks.
+// acc[0..7] += v * (8 BF16 values packed in q)
+__device__ __forceinline__ void fma8(float (&acc)[8], float v, const uint4 &q) {
+  const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(&q);
+#pragma unroll
+  for (int c = 0; c < 8; ++c) acc[c] += v * bf(e[c]);
+}
+
+// One message-passing layer.  A warp owns 16 cells (one tile) at a time and takes them
+// in two rounds of 8: four lanes per cell, eight channels per lane, sum
+// m = Ahat h over the cell's sliced row -- for uniform slices the column offsets,
+// values and neighbour activations of four slots are loaded before any is used -- and
+// write the [h; m] row (64 BF16) into the warp's shared tile.  4 k-steps x 4 n-blocks of
+// mma.sync give the 16 x 32 pre-activation; the epilogue adds the bias, applies the ReLU
+// and the skip connection, puts h' back into the tile, and the tile leaves in 16-byte
+// stores (16 consecutive cells = 1 KB contiguous).  Rows of the tile and of W_l are
+// padded to 72 elements so that the fragment loads of the 8 row groups fall in distinct
+// banks.
 __global__ void __launch_bounds__(kTPB, 4)
     k_lp_layer(SellView s, int n, const float *__restrict__ aval,
                const __nv_bfloat16 *__restrict__ hin, __nv_bfloat16 *__restrict__ hout,
@@ -237,53 +259,64 @@ __global__ void __launch_bounds__(kTPB, 4)
   if (threadIdx.x < C) bsm[threadIdx.x] = bl[threadIdx.x];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int g = lane >> 2, tg = lane & 3;
+  const int g = lane >> 2, tg = lane & 3, qc = 8 * (lane & 3);
   __nv_bfloat16 *tw = tile[warp];
   const int ntiles = (n + 15) / 16;
   const int nwarps = (int)(((long long)gridDim.x * blockDim.x) >> 5);
   for (int tt = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5); tt < ntiles;
        tt += nwarps) {
-    const int r = tt * 16 + (lane >> 1), half = lane & 1;
-    float acc[16];
+#pragma unroll 1
+    for (int rd = 0; rd < 2; ++rd) {
+      const int rloc = rd * 8 + (lane >> 2);
+      const int r = tt * 16 + rloc;
+      float acc[8];
 #pragma unroll
-    for (int c = 0; c < 16; ++c) acc[c] = 0.f;
-    uint4 own0 = make_uint4(0, 0, 0, 0), own1 = make_uint4(0, 0, 0, 0);
-    if (r < n) {
-      const int slice = r >> 5, ln = r & 31;
-      const long long base = __ldg(&s.ptr[slice]) + ln;
-      const int w = __ldg(&s.width[slice]), op = __ldg(&s.offp[slice]);
-      const bool uni = __ldg(&s.kind[slice]) == 0;
-      for (int j = 0; j < w; ++j) {
-        int col = uni ? r + __ldg(&s.off[op + j]) : __ldg(&s.off[op + 32 * j + ln]);
-        col = col < 0 ? 0 : (col >= n ? n - 1 : col);
-        const float v = __ldg(&aval[base + (long long)j * 32]);
-        const uint4 *hp = reinterpret_cast<const uint4 *>(hin + (long long)col * C + 16 * half);
-        const uint4 q0 = __ldg(hp), q1 = __ldg(hp + 1);
-        const __nv_bfloat16 *e0 = reinterpret_cast<const __nv_bfloat16 *>(&q0);
-        const __nv_bfloat16 *e1 = reinterpret_cast<const __nv_bfloat16 *>(&q1);
+      for (int c = 0; c < 8; ++c) acc[c] = 0.f;
+      uint4 own = make_uint4(0, 0, 0, 0);
+      if (r < n) {
+        const int slice = r >> 5, ln = r & 31;
+        const long long base = __ldg(&s.ptr[slice]) + ln;
+        const int w = __ldg(&s.width[slice]), op = __ldg(&s.offp[slice]);
+        const __nv_bfloat16 *hq = hin + qc;
+        if (__ldg(&s.kind[slice]) == 0 && w <= 8) {
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-          acc[c] += v * bf(e0[c]);
-          acc[8 + c] += v * bf(e1[c]);
+          for (int j0 = 0; j0 < 8; j0 += 4) {
+            float v[4];
+            uint4 hv[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              if (j0 + j < w) {
+                int col = r + __ldg(&s.off[op + j0 + j]);
+                col = col < 0 ? 0 : (col >= n ? n - 1 : col);
+                v[j] = __ldg(&aval[base + (long long)(j0 + j) * 32]);
+                hv[j] = __ldg(reinterpret_cast<const uint4 *>(hq + (long long)col * C));
+              }
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              if (j0 + j < w) fma8(acc, v[j], hv[j]);
+          }
+        } else {
+          const bool uni = __ldg(&s.kind[slice]) == 0;
+          for (int j = 0; j < w; ++j) {
+            int col = uni ? r + __ldg(&s.off[op + j]) : __ldg(&s.off[op + 32 * j + ln]);
+            col = col < 0 ? 0 : (col >= n ? n - 1 : col);
+            fma8(acc, __ldg(&aval[base + (long long)j * 32]),
+                 __ldg(reinterpret_cast<const uint4 *>(hq + (long long)col * C)));
+          }
         }
+        own = __ldg(reinterpret_cast<const uint4 *>(hq + (long long)r * C));
       }
-      const uint4 *op4 = reinterpret_cast<const uint4 *>(hin + (long long)r * C + 16 * half);
-      own0 = __ldg(op4);
-      own1 = __ldg(op4 + 1);
-    }
-    {
-      __nv_bfloat16 *row = tw + (lane >> 1) * TS;
-      *reinterpret_cast<uint4 *>(row + 16 * half) = own0;
-      *reinterpret_cast<uint4 *>(row + 16 * half + 8) = own1;
-      __align__(16) __nv_bfloat16 mb[16];
+      __nv_bfloat16 *row = tw + rloc * TS;
+      *reinterpret_cast<uint4 *>(row + qc) = own;
+      __align__(16) __nv_bfloat16 mb[8];
 #pragma unroll
-      for (int c = 0; c < 16; ++c) mb[c] = __float2bfloat16(acc[c]);
-      *reinterpret_cast<uint4 *>(row + C + 16 * half) = *reinterpret_cast<const uint4 *>(&mb[0]);
-      *reinterpret_cast<uint4 *>(row + C + 16 * half + 8) =
-          *reinterpret_cast<const uint4 *>(&mb[8]);
+      for (int c = 0; c < 8; ++c) mb[c] = __float2bfloat16(acc[c]);
+      *reinterpret_cast<uint4 *>(row + C + qc) = *reinterpret_cast<const uint4 *>(mb);
       if (mout && r < n) {
-#pragma unroll
-        for (int c = 0; c < 16; ++c) mout[(long long)r * C + 16 * half + c] = bf(mb[c]);
+        float4 *mo = reinterpret_cast<float4 *>(mout + (long long)r * C + qc);
+        mo[0] = make_float4(bf(mb[0]), bf(mb[1]), bf(mb[2]), bf(mb[3]));
+        mo[1] = make_float4(bf(mb[4]), bf(mb[5]), bf(mb[6]), bf(mb[7]));
       }
     }
     __syncwarp();
@@ -309,25 +342,32 @@ __global__ void __launch_bounds__(kTPB, 4)
         mma_bf16(d[nt], a, b);
       }
     }
+    __syncwarp();  // every lane has its fragments: the h part of the tile may change
 #pragma unroll
     for (int nt = 0; nt < 4; ++nt) {
 #pragma unroll
       for (int hh = 0; hh < 2; ++hh) {
         const int rr = g + 8 * hh, cell = tt * 16 + rr;
         const int col = nt * 8 + tg * 2;
-        if (cell < n) {
-          const float z0 = d[nt][2 * hh] + bsm[col], z1 = d[nt][2 * hh + 1] + bsm[col + 1];
-          const float h0 = bf(tw[rr * TS + col]), h1 = bf(tw[rr * TS + col + 1]);
-          __nv_bfloat162 o;
-          o.x = __float2bfloat16(h0 + fmaxf(z0, 0.f));
-          o.y = __float2bfloat16(h1 + fmaxf(z1, 0.f));
-          *reinterpret_cast<__nv_bfloat162 *>(hout + (long long)cell * C + col) = o;
-          if (zout) {
-            zout[(long long)cell * C + col] = z0;
-            zout[(long long)cell * C + col + 1] = z1;
-          }
-        }
+        const float z0 = d[nt][2 * hh] + bsm[col], z1 = d[nt][2 * hh + 1] + bsm[col + 1];
+        __nv_bfloat162 *hp = reinterpret_cast<__nv_bfloat162 *>(tw + rr * TS + col);
+        const __nv_bfloat162 hold = *hp;
+        __nv_bfloat162 o;
+        o.x = __float2bfloat16(bf(hold.x) + fmaxf(z0, 0.f));
+        o.y = __float2bfloat16(bf(hold.y) + fmaxf(z1, 0.f));
+        *hp = o;
+        if (zout && cell < n)
+          *reinterpret_cast<float2 *>(zout + (long long)cell * C + col) = make_float2(z0, z1);
       }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int idx = lane + 32 * k, rr = idx >> 2, part = idx & 3;
+      const int cell = tt * 16 + rr;
+      if (cell < n)
+        *reinterpret_cast<uint4 *>(hout + (long long)cell * C + 8 * part) =
+            *reinterpret_cast<const uint4 *>(tw + rr * TS + 8 * part);
     }
     __syncwarp();
   }
@@ -370,24 +410,30 @@ __global__ void __launch_bounds__(kTPB)
 // ---------------------------------------------------------------------------
 // Loss, backward, Adam
 // ---------------------------------------------------------------------------
-// Energy-norm loss of the normalised output, d = y - e/rms:
-//   loss = d.Ahat d / t.Ahat t with t = e/rms;  sums[0] = d.Ahat d, sums[1] = t.Ahat t.
-// Ad = Ahat d is kept for the backward (d loss / dy = 2 Ahat d / t.Ahat t).
+// Loss of the normalised output, d = y - e/rms, t = e/rms (Ahat d = Ahat y - r/rms):
+//   kind 0 (energy norm):   loss = d.Ahat d / t.Ahat t,         d loss/dy = 2 Ahat d / t.Ahat t
+//   kind 1 (residual norm): loss = |Ahat d|^2 / |Ahat t|^2,      d loss/dy = 2 Ahat Ahat d / |Ahat t|^2
+// sums[0], sums[1] = numerator, denominator; ad = Ahat d.
 __global__ void __launch_bounds__(kTPB, 6)
     k_lp_aloss(SellView s, int n, const float *__restrict__ val, const float *__restrict__ d,
                const float *__restrict__ e, const float *__restrict__ rms,
                float *__restrict__ ad, double *partials, unsigned *ticket,
-               float *__restrict__ sums) {
+               float *__restrict__ sums, int kind) {
   const float inv = 1.0f / rms[0];
   float a = 0.f, b = 0.f;
   FCG_SLICE_LOOP(slice, lane, s) {
     const float adv = sell_row(s, n, val, d, slice, lane);
-    const float aev = sell_row(s, n, val, e, slice, lane);
+    const float atv = sell_row(s, n, val, e, slice, lane) * inv;
     const int row = slice * 32 + lane;
     if (row < n) {
       ad[row] = adv;
-      a += d[row] * adv;
-      b += (e[row] * inv) * (aev * inv);
+      if (kind == 0) {
+        a += d[row] * adv;
+        b += (e[row] * inv) * atv;
+      } else {
+        a += adv * adv;
+        b += atv * atv;
+      }
     }
   }
   double v[2] = {(double)a, (double)b};
@@ -397,7 +443,19 @@ __global__ void __launch_bounds__(kTPB, 6)
   }
 }
 
-// dy = 2 Ahat d / t.Ahat t; dh_L = dy w_out; per-block sums of dy h_L and dy.
+// y = Ahat x in FP32 (the second product of the residual-norm loss)
+__global__ void __launch_bounds__(kTPB, 6)
+    k_lp_spmv32(SellView s, int n, const float *__restrict__ val, const float *__restrict__ x,
+                float *__restrict__ y) {
+  FCG_SLICE_LOOP(slice, lane, s) {
+    const float v = sell_row(s, n, val, x, slice, lane);
+    const int row = slice * 32 + lane;
+    if (row < n) y[row] = v;
+  }
+}
+
+// dy = 2 g / sums[1] (g = Ahat d or Ahat Ahat d); dh_L = dy w_out; per-block sums of
+// dy h_L and dy.
 __global__ void __launch_bounds__(kTPB)
     k_lp_out_bwd(int n, const float *__restrict__ ad, const float *__restrict__ sums,
                  const __nv_bfloat16 *__restrict__ h, const float *__restrict__ prm,
@@ -598,54 +656,79 @@ __global__ void __launch_bounds__(kTPB, 8)
     S->maxr = sqrt(v[1]);
     S->l1ratio = v[1] > 0 ? v[0] / sqrt(v[1]) : 0.0;
     S->chk_l1 = v[0];
-    S->first = 1;
+    S->nwin = 0;
+    S->head = 0;
     if (!isfinite(v[0])) S->status = FCG_ERR_NONFINITE;
     if (S->nsw <= 0 || v[0] == 0.0 || S->status) S->done = 1;
     if (v[0] == 0.0) S->converged = 1;
   }
 }
 
-// z = r + rms (w_out . h_L + b_out); beta = z.q_old / p_old.q_old (0 on the first
-// iteration)
-__global__ void __launch_bounds__(kTPB, 8)
+// z = r + rms (w_out . h_L + b_out) and z . q_j for the stored directions j, which give
+// beta_j = z . q_j / p_j . q_j (truncated flexible CG, Notay 2000, eq. 2.7)
+__global__ void __launch_bounds__(kTPB, 4)
     k_f_out(int n, const __nv_bfloat16 *__restrict__ h, const float *__restrict__ prm,
             const float *__restrict__ rms, const float *__restrict__ r, float *__restrict__ z,
-            const float *__restrict__ q, LScal *S, double *partials) {
+            const float *__restrict__ qring, long long stride, LScal *S, double *partials) {
   if (fdone(S)) return;
   __shared__ float w[C + 1];
   if (threadIdx.x <= C) w[threadIdx.x] = prm[lp::oWout + threadIdx.x];
   __syncthreads();
   const float sc = rms[0];
-  float t = 0.f;
+  const int nwin = __ldcg(&S->nwin);
+  float t[lp::kMaxDir];
+#pragma unroll
+  for (int j = 0; j < lp::kMaxDir; ++j) t[j] = 0.f;
   FCG_GRID_STRIDE(i, n) {
     const float zi = r[i] + sc * out_dot(h, i, w);
     z[i] = zi;
-    t += zi * q[i];
+#pragma unroll
+    for (int j = 0; j < lp::kMaxDir; ++j)
+      if (j < nwin) t[j] += zi * qring[j * stride + i];
   }
-  double v[1] = {(double)t};
-  if (reduce_commit<1>(v, partials, &S->ticket[1]) && threadIdx.x == 0) {
-    S->zq = v[0];
-    S->bet = S->first ? 0.0 : v[0] / S->pq;
-    if (!isfinite(S->bet)) {
-      S->status = FCG_ERR_NONFINITE;
-      S->done = 1;
+  double v[lp::kMaxDir];
+#pragma unroll
+  for (int j = 0; j < lp::kMaxDir; ++j) v[j] = (double)t[j];
+  if (reduce_commit<lp::kMaxDir>(v, partials, &S->ticket[1]) && threadIdx.x == 0) {
+    for (int j = 0; j < lp::kMaxDir; ++j) {
+      S->bets[j] = j < nwin ? v[j] / S->pqs[j] : 0.0;
+      if (!isfinite(S->bets[j])) {
+        S->status = FCG_ERR_NONFINITE;
+        S->done = 1;
+      }
     }
   }
 }
 
-// p = z - beta p
+// p_head = z - sum_j beta_j p_j (the slot written may be the oldest one read: each
+// element reads all slots before it is written)
 __global__ void __launch_bounds__(kTPB, 8)
-    k_f_p(int n, const float *__restrict__ z, float *__restrict__ p, const LScal *S) {
+    k_f_p(int n, const float *__restrict__ z, float *__restrict__ pring, long long stride,
+          const LScal *S) {
   if (fdone(S)) return;
-  const float bet = (float)__ldcg(&S->bet);
-  FCG_GRID_STRIDE(i, n) p[i] = z[i] - bet * p[i];
+  const int nwin = __ldcg(&S->nwin), head = __ldcg(&S->head);
+  float b[lp::kMaxDir];
+#pragma unroll
+  for (int j = 0; j < lp::kMaxDir; ++j) b[j] = (float)__ldcg(&S->bets[j]);
+  float *ph = pring + head * stride;
+  FCG_GRID_STRIDE(i, n) {
+    float acc = z[i];
+#pragma unroll
+    for (int j = 0; j < lp::kMaxDir; ++j)
+      if (j < nwin) acc -= b[j] * pring[j * stride + i];
+    ph[i] = acc;
+  }
 }
 
-// q = Ahat p; alpha = p.r / p.q
+// q_head = Ahat p_head; alpha = p.r / p.q; the new direction joins the window
 __global__ void __launch_bounds__(kTPB, 6)
-    k_f_spmv(SellView s, int n, const float *__restrict__ val, const float *__restrict__ p,
-             float *__restrict__ q, const float *__restrict__ r, LScal *S, double *partials) {
+    k_f_spmv(SellView s, int n, const float *__restrict__ val, const float *__restrict__ pring,
+             float *__restrict__ qring, long long stride, const float *__restrict__ r, LScal *S,
+             double *partials) {
   if (fdone(S)) return;
+  const int head = __ldcg(&S->head);
+  const float *p = pring + head * stride;
+  float *q = qring + head * stride;
   float tq = 0.f, tr = 0.f;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int per = (s.nslices + gridDim.x - 1) / gridDim.x;
@@ -662,9 +745,10 @@ __global__ void __launch_bounds__(kTPB, 6)
   }
   double v[2] = {(double)tq, (double)tr};
   if (reduce_commit<2>(v, partials, &S->ticket[2]) && threadIdx.x == 0) {
-    S->pq = v[0];
+    S->pqs[head] = v[0];
     S->alf = v[1] / v[0];
-    S->first = 0;
+    S->head = (head + 1) % S->mdir;
+    S->nwin = min(S->nwin + 1, S->mdir);
     if (!isfinite(S->alf) || !(v[0] > 0.0)) {
       S->status = FCG_ERR_NONFINITE;
       S->done = 1;
@@ -683,15 +767,19 @@ __device__ __noinline__ void f_decide(LScal *S, double rrn) {
   S->ru = ru ? 1 : 0;
 }
 
-// y += alpha p, r -= alpha q; ||r||^2 decides on a reliable update (arms the IF node)
+// y += alpha p, r -= alpha q (the direction just added); ||r||^2 decides on a reliable
+// update (arms the IF node)
 __global__ void __launch_bounds__(kTPB, 8)
-    k_f_update(int n, float *__restrict__ y, float *__restrict__ r, const float *__restrict__ p,
-               const float *__restrict__ q, LScal *S, double *partials,
-               cudaGraphConditionalHandle hif, int use_cond) {
+    k_f_update(int n, float *__restrict__ y, float *__restrict__ r,
+               const float *__restrict__ pring, const float *__restrict__ qring,
+               long long stride, LScal *S, double *partials, cudaGraphConditionalHandle hif,
+               int use_cond) {
   if (fdone(S)) {
     if (use_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(hif, 0u);
     return;
   }
+  const int m = __ldcg(&S->mdir), slot = (__ldcg(&S->head) + m - 1) % m;
+  const float *p = pring + slot * stride, *q = qring + slot * stride;
   const float alf = (float)__ldcg(&S->alf);
   float t = 0.f;
   FCG_GRID_STRIDE(i, n) {
@@ -867,7 +955,7 @@ int ensure_workspace(fcg_learned *Lp, fcg_context *c, bool train) {
     LP_TRY(Lp, Lp->dh.ensure(sizeof(float) * nc));
     LP_TRY(Lp, Lp->dh2.ensure(sizeof(float) * nc));
     LP_TRY(Lp, Lp->dm.ensure(sizeof(float) * nc));
-    LP_TRY(Lp, Lp->dvec.ensure(sizeof(float) * 2 * Lp->ncap));
+    LP_TRY(Lp, Lp->dvec.ensure(sizeof(float) * 3 * Lp->ncap));
     Lp->train_cap = true;
   }
   return FCG_OK;
@@ -917,9 +1005,9 @@ int compute_features(fcg_learned *Lp, fcg_context *c) {
   const int G = reduction_grid(c);
   double *red = Lp->red.as<double>();
   k_lp_volsum<<<G, kTPB, 0, c->stream>>>(c->n, c->mv.vol, red, Lp->scal.as<unsigned>() + 16,
-                                         red + 2 * kMaxBlocks);
+                                         red + lp::kMaxDir * kMaxBlocks);
   k_lp_features<<<grid_for(c->n, c->num_sms), kTPB, 0, c->stream>>>(
-      c->mv, scale64(c), red + 2 * kMaxBlocks, Lp->feat.as<float>());
+      c->mv, scale64(c), red + lp::kMaxDir * kMaxBlocks, Lp->feat.as<float>());
   LP_TRY(Lp, cudaGetLastError());
   Lp->fuid = c->uid;
   Lp->fgen = c->bind_gen;
@@ -973,18 +1061,23 @@ int loss_grad(fcg_learned *Lp, fcg_context *c, const float *r, const float *e) {
   float *sums = rms + 2;
   const float *prm = Lp->params.as<float>();
   const int G = reduction_grid(c);
-  float *dvec = Lp->dvec.as<float>(), *advec = dvec + Lp->ncap;
+  float *dvec = Lp->dvec.as<float>(), *advec = dvec + Lp->ncap, *aadvec = advec + Lp->ncap;
   k_lp_out<<<grid_for(n, c->num_sms), kTPB, 0, st>>>(n, last_activation(Lp, c, true), prm, rms, r,
                                                      e, Lp->y.as<float>(), dvec, nullptr);
   k_lp_aloss<<<G, kTPB, 0, st>>>(c->sv, n, scaled32(c), dvec, e, rms, advec,
-                                 Lp->red.as<double>(), tk + 2, sums);
+                                 Lp->red.as<double>(), tk + 2, sums, Lp->loss_kind);
+  const float *gy = advec;
+  if (Lp->loss_kind == 1) {
+    k_lp_spmv32<<<G, kTPB, 0, st>>>(c->sv, n, scaled32(c), advec, aadvec);
+    gy = aadvec;
+  }
   const int GB = c->num_sms * 2;  // blocks of the weight-gradient kernels
   float *part = Lp->part.as<float>();
   float *grad = Lp->grad.as<float>();
   const size_t hs = (size_t)n * lp::C;
   const __nv_bfloat16 *H = Lp->hbuf.as<__nv_bfloat16>();
   float *dh = Lp->dh.as<float>(), *dh2 = Lp->dh2.as<float>();
-  k_lp_out_bwd<<<GB, kTPB, 0, st>>>(n, advec, sums, H + (size_t)lp::L * hs, prm, dh, part);
+  k_lp_out_bwd<<<GB, kTPB, 0, st>>>(n, gy, sums, H + (size_t)lp::L * hs, prm, dh, part);
   k_lp_sum_parts<<<1, kTPB, 0, st>>>(part, GB, lp::C + 1, grad + lp::oWout);
   for (int l = lp::L - 1; l >= 0; --l) {
     k_lp_layer_bwd<<<GB, kTPB, 0, st>>>(n, dh, Lp->zbuf.as<float>() + (l + 1) * hs, H + l * hs,
@@ -1057,7 +1150,7 @@ extern "C" int fcg_lp_create(int device, unsigned long long seed, fcg_learned **
   if (Lp->params.ensure(pb) || Lp->adam_m.ensure(pb) || Lp->adam_v.ensure(pb) ||
       Lp->grad.ensure(pb) || Lp->wbf.ensure(sizeof(__nv_bfloat16) * lp::L * 2 * lp::C * lp::C) ||
       Lp->part.ensure(sizeof(float) * (size_t)Lp->num_sms * 2 * lp::kLayerParams) ||
-      Lp->red.ensure(sizeof(double) * (2 * kMaxBlocks + 8)) ||
+      Lp->red.ensure(sizeof(double) * (lp::kMaxDir * kMaxBlocks + 8)) ||
       Lp->scal.ensure(sizeof(float) * 64) || cudaMalloc(&Lp->S, sizeof(lp::LScal)) ||
       cudaMallocHost(&Lp->hS, sizeof(lp::LScal)) ||
       cudaStreamCreateWithFlags(&Lp->cap, cudaStreamNonBlocking) ||
@@ -1266,10 +1359,18 @@ extern "C" int fcg_lp_train_step(fcg_learned *Lp, fcg_context *c, const float *r
   return read_loss(Lp, c, loss);
 }
 
-extern "C" int fcg_lp_set_fcg_options(fcg_learned *Lp, int ru_every, int stall_window,
-                                      double stall_factor) {
-  if (!Lp || ru_every < 1 || stall_window < 1 || !(stall_factor > 0.0) || !(stall_factor <= 1.0))
+extern "C" int fcg_lp_set_loss(fcg_learned *Lp, int kind) {
+  if (!Lp || kind < 0 || kind > 1) return FCG_ERR_ARG;
+  Lp->loss_kind = kind;
+  return FCG_OK;
+}
+
+extern "C" int fcg_lp_set_fcg_options(fcg_learned *Lp, int directions, int ru_every,
+                                      int stall_window, double stall_factor) {
+  if (!Lp || directions < 1 || directions > lp::kMaxDir || ru_every < 1 || stall_window < 1 ||
+      !(stall_factor > 0.0) || !(stall_factor <= 1.0))
     return FCG_ERR_ARG;
+  Lp->mdir = directions;
   Lp->ru_every = ru_every;
   Lp->stall_window = stall_window;
   Lp->stall_factor = stall_factor;
@@ -1280,14 +1381,21 @@ namespace {
 
 struct FcgVecs {
   double *x, *res, *su;
-  float *y, *r, *z, *p, *q;
+  float *y, *r, *z, *p, *q;  // p, q: rings of kMaxDir vectors, `stride` apart
+  long long stride;
 };
+
+size_t fcg_bytes(int n) {
+  const size_t n8 = ((size_t)n + 63) & ~(size_t)63;
+  return 3 * n8 * sizeof(double) + (3 + 2 * lp::kMaxDir) * n8 * sizeof(float);
+}
 
 FcgVecs fcg_vectors(fcg_learned *Lp, int n) {
   const size_t n8 = ((size_t)n + 63) & ~(size_t)63;
   double *d = Lp->fvec.as<double>();
   float *f = (float *)(d + 3 * n8);
-  return {d, d + n8, d + 2 * n8, f, f + n8, f + 2 * n8, f + 3 * n8, f + 4 * n8};
+  return {d,      d + n8,          d + 2 * n8, f, f + n8, f + 2 * n8, f + 3 * n8,
+          f + (3 + lp::kMaxDir) * n8, (long long)n8};
 }
 
 void enqueue_body_head(fcg_learned *Lp, fcg_context *c, cudaStream_t st, const FcgVecs &v,
@@ -1297,10 +1405,10 @@ void enqueue_body_head(fcg_learned *Lp, fcg_context *c, cudaStream_t st, const F
   double *red = Lp->red.as<double>();
   enqueue_forward(Lp, c, st, v.r, false, &Lp->S->done, &Lp->S->ticket[6]);
   k_f_out<<<G, kTPB, 0, st>>>(n, last_activation(Lp, c, false), Lp->params.as<float>(),
-                              Lp->scal.as<float>(), v.r, v.z, v.q, Lp->S, red);
-  k_f_p<<<grid_for(n, c->num_sms), kTPB, 0, st>>>(n, v.z, v.p, Lp->S);
-  k_f_spmv<<<G, kTPB, 0, st>>>(c->sv, n, scaled32(c), v.p, v.q, v.r, Lp->S, red);
-  k_f_update<<<G, kTPB, 0, st>>>(n, v.y, v.r, v.p, v.q, Lp->S, red, hif, use_cond);
+                              Lp->scal.as<float>(), v.r, v.z, v.q, v.stride, Lp->S, red);
+  k_f_p<<<grid_for(n, c->num_sms), kTPB, 0, st>>>(n, v.z, v.p, v.stride, Lp->S);
+  k_f_spmv<<<G, kTPB, 0, st>>>(c->sv, n, scaled32(c), v.p, v.q, v.stride, v.r, Lp->S, red);
+  k_f_update<<<G, kTPB, 0, st>>>(n, v.y, v.r, v.p, v.q, v.stride, Lp->S, red, hif, use_cond);
 }
 
 void enqueue_ru(fcg_learned *Lp, fcg_context *c, cudaStream_t st, const FcgVecs &v) {
@@ -1407,12 +1515,11 @@ extern "C" int fcg_fcg_learned(fcg_context *c, fcg_learned *Lp, const double *a,
   if ((rc = compute_features(Lp, c))) return set_error(c, rc, Lp->err);
   if ((rc = ensure_workspace(Lp, c, false))) return set_error(c, rc, Lp->err);
   const size_t n8 = ((size_t)n + 63) & ~(size_t)63;
-  FCG_CUDA_TRY(c, Lp->fvec.ensure(3 * n8 * sizeof(double) + 5 * n8 * sizeof(float)));
+  (void)n8;
+  FCG_CUDA_TRY(c, Lp->fvec.ensure(fcg_bytes(n)));
   const FcgVecs v = fcg_vectors(Lp, n);
   FCG_CUDA_TRY(c, cudaMemcpyAsync(v.su, dsu, n1, cudaMemcpyDeviceToDevice, c->stream));
   FCG_CUDA_TRY(c, cudaMemcpyAsync(v.x, dfi, n1, cudaMemcpyDeviceToDevice, c->stream));
-  FCG_CUDA_TRY(c, cudaMemsetAsync(v.p, 0, sizeof(float) * n, c->stream));
-  FCG_CUDA_TRY(c, cudaMemsetAsync(v.q, 0, sizeof(float) * n, c->stream));
   lp::LScal init;
   std::memset(&init, 0, sizeof init);
   init.small = (double)1e-20f;  // parameters::small (modules_allocatable.f90:27)
@@ -1422,6 +1529,7 @@ extern "C" int fcg_fcg_learned(fcg_context *c, fcg_learned *Lp, const double *a,
   init.ru_every = Lp->ru_every;
   init.stall_window = Lp->stall_window;
   init.stall_factor = Lp->stall_factor;
+  init.mdir = Lp->mdir;
   *Lp->hS = init;
   FCG_CUDA_TRY(c, cudaMemcpyAsync(Lp->S, Lp->hS, sizeof(lp::LScal), cudaMemcpyHostToDevice,
                                   c->stream));

@@ -87,6 +87,7 @@ class LearnedPreconditioner:
 
     # -- network ------------------------------------------------------------------
     def set_matrix(self, ctx: Context, a):
+        ctx._follow(a)
         self._check(self.lib.fcg_lp_set_matrix(self.h, ctx.h, _ptr(_host(a))), "fcg_lp_set_matrix")
 
     def features(self, ctx: Context) -> np.ndarray:
@@ -96,6 +97,7 @@ class LearnedPreconditioner:
 
     def apply(self, ctx: Context, r):
         r = _f32(r)
+        ctx._follow(r)
         if _is_torch(r):
             import torch
 
@@ -107,6 +109,7 @@ class LearnedPreconditioner:
 
     def loss_grad(self, ctx: Context, r, e):
         r, e = _f32(r), _f32(e)
+        ctx._follow(r, e)
         loss = C.c_float()
         g = np.zeros(PARAMS, np.float32)
         self._check(self.lib.fcg_lp_loss_grad(self.h, ctx.h, _ptr(r), _ptr(e), C.byref(loss),
@@ -115,19 +118,28 @@ class LearnedPreconditioner:
 
     def train_step(self, ctx: Context, r, e, lr: float) -> float:
         r, e = _f32(r), _f32(e)
+        ctx._follow(r, e)
         loss = C.c_float()
         self._check(self.lib.fcg_lp_train_step(self.h, ctx.h, _ptr(r), _ptr(e), float(lr),
                                                C.byref(loss)), "fcg_lp_train_step")
         return float(loss.value)
 
-    def set_fcg_options(self, ru_every: int = 50, stall_window: int = 400,
+    def set_loss(self, kind: str = "residual"):
+        """Training loss: "residual" (|Ahat N(r) - r|^2 / |r|^2, the default) or "energy"
+        ((N(r)-e).Ahat(N(r)-e) / e.Ahat e)."""
+        k = {"energy": 0, "residual": 1}[kind]
+        self._check(self.lib.fcg_lp_set_loss(self.h, k), "fcg_lp_set_loss")
+
+    def set_fcg_options(self, directions: int = 8, ru_every: int = 50, stall_window: int = 400,
                         stall_factor: float = 0.5):
-        self._check(self.lib.fcg_lp_set_fcg_options(self.h, int(ru_every), int(stall_window),
-                                                    float(stall_factor)), "fcg_lp_set_fcg_options")
+        self._check(self.lib.fcg_lp_set_fcg_options(self.h, int(directions), int(ru_every),
+                                                    int(stall_window), float(stall_factor)),
+                    "fcg_lp_set_fcg_options")
 
     # -- solver ---------------------------------------------------------------------
     def solve(self, ctx: Context, a, su, fi, sor: float, nsw: int) -> "FcgResult":
         """Learned-preconditioned flexible CG with the arguments of dpcg(fi,ifi)."""
+        ctx._follow(a, su, fi)
         a, su = _host(a), _host(su)
         fi = fi.clone() if _is_torch(fi) else np.array(fi, dtype=np.float64)
         if _is_torch(su):
@@ -276,3 +288,13 @@ def train_default(path: str = DEFAULT_WEIGHTS, steps: int = 20000, n_pairs: int 
     os.makedirs(os.path.dirname(path), exist_ok=True)
     lp.save(path)
     return lp, losses
+
+
+if __name__ == "__main__":  # python -m freecappuccino_gb300.learned [out_path] [steps]
+    import sys
+
+    out = sys.argv[1] if len(sys.argv) > 1 else DEFAULT_WEIGHTS
+    n_steps = int(sys.argv[2]) if len(sys.argv) > 2 else 20000
+    t_start = time.perf_counter()
+    train_default(out, steps=n_steps)
+    print(f"saved {out} ({time.perf_counter() - t_start:.1f} s)")

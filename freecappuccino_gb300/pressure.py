@@ -85,6 +85,7 @@ class Context:
         if rc != 0:
             raise _lib.FcgError(rc, "fcg_create", "no usable sm_103a CUDA device")
         self.h = h
+        self._stream, self._pinned = None, False
         self._desc = mesh.desc()  # keeps the pointers alive for the call
         self._check(self.lib.fcg_bind_mesh(self.h, C.byref(self._desc)), "fcg_bind_mesh")
         self.n, self.nnz, self.ntot = mesh.numCells, mesh.nnz, mesh.numTotal
@@ -106,7 +107,29 @@ class Context:
             pass
 
     def set_stream(self, stream_handle: int | None):
+        """Queue the context's work on this CUDA stream from now on (and stop following
+        torch's current stream)."""
         self._check(self.lib.fcg_set_stream(self.h, stream_handle), "fcg_set_stream")
+        self._stream, self._pinned = stream_handle, True
+
+    def _follow(self, *xs):
+        """With CUDA tensors among the arguments, queue the library's work on torch's
+        current stream (unless a stream was set explicitly): the work is then ordered
+        after the kernels that produced the tensors and before those that read the
+        results."""
+        if self._pinned:
+            return
+        for x in xs:
+            if _is_torch(x) and x.is_cuda:
+                import torch
+
+                # handle 0 is the legacy default stream, while the library reads NULL as
+                # the context's own stream: pass cudaStreamLegacy (1) for it
+                s = torch.cuda.current_stream(x.device).cuda_stream or 1
+                if s != self._stream:
+                    self._check(self.lib.fcg_set_stream(self.h, s), "fcg_set_stream")
+                    self._stream = s
+                return
 
     def synchronize(self):
         self._check(self.lib.fcg_synchronize(self.h), "fcg_synchronize")
@@ -124,6 +147,7 @@ class Context:
     # -- a2-a4 ----------------------------------------------------------------------
     def laplacian(self, mu, phi, su):
         """fvm_laplacian.f90 laplacian(mu,phi): returns (a, su)."""
+        self._follow(mu, phi, su)
         mu, phi = _host(mu), _host(phi)
         su = su.clone() if _is_torch(su) else np.array(su, dtype=np.float64)
         a = _like(mu, self.nnz)
@@ -133,6 +157,7 @@ class Context:
 
     def facefluxmass(self, u, v, w, p, dUdxi, dVdxi, dWdxi, dPdxi, apu, apv, apw, den):
         """calcp's assembly loop with facefluxmass: returns (a, su, flmass)."""
+        self._follow(u, v, w, p, dUdxi, dVdxi, dWdxi, dPdxi, apu, apv, apw, den)
         arrs = [_host(t) for t in (u, v, w, p, dUdxi, dVdxi, dWdxi, dPdxi, apu, apv, apw, den)]
         ff = _lib.FlowFields(*[_ptr(t) for t in arrs])
         a = _like(arrs[0], self.nnz)
@@ -144,6 +169,7 @@ class Context:
 
     def fluxmc(self, dPdxi, apu, den, flmass):
         """calcp's non-orthogonal corrector with fluxmc: returns (su, flmass)."""
+        self._follow(dPdxi, apu, den, flmass)
         dPdxi, apu, den = _host(dPdxi), _host(apu), _host(den)
         fm = flmass.clone() if _is_torch(flmass) else np.array(flmass, dtype=np.float64)
         su = _like(apu, self.n)
@@ -154,6 +180,7 @@ class Context:
     # -- a5-a8 ----------------------------------------------------------------------
     def grad(self, phi, option: str = "gauss", nigrad: int = 1, dphidxi=None):
         """grad(phi,dPhidxi[,option]) without limiter: returns dPhidxi as (n, 3)."""
+        self._follow(phi, dphidxi)
         phi = _host(phi)
         if option == "gauss_corrected" and dphidxi is not None:
             g = dphidxi.clone() if _is_torch(dphidxi) else np.array(dphidxi, dtype=np.float64)
@@ -170,6 +197,7 @@ class Context:
 
     def bpres(self, p, dPdxi, istage: int):
         """bpres(p,istage): returns the updated p(numTotal)."""
+        self._follow(p, dPdxi)
         p = p.clone() if _is_torch(p) else np.array(p, dtype=np.float64)
         g = _host(dPdxi) if dPdxi is not None else _like(p, (self.n, 3))
         self._check(self.lib.fcg_bpres(self.h, _ptr(p), _ptr(g), int(istage)), "fcg_bpres")
@@ -189,6 +217,7 @@ class Context:
         return out[: cnt.value]
 
     def _solve(self, fn, name, a, su, fi, sor, nsw, want_res=True, want_trace=False):
+        self._follow(a, su, fi)
         a, su = _host(a), _host(su)
         fi = fi.clone() if _is_torch(fi) else np.array(fi, dtype=np.float64)
         res = _like(su, self.n) if want_res else None
@@ -213,6 +242,7 @@ class Context:
     def bicgstab_multi(self, a, su, fi, sor, nsw):
         """Several systems on this pattern in one solve: a[nsys, nnz], su and fi[nsys, n].
         Returns (fi, list of SolveResult)."""
+        self._follow(a, su, fi)
         a, su = _host(a), _host(su)
         fi = fi.clone() if _is_torch(fi) else np.array(fi, dtype=np.float64)
         ns = a.shape[0]
@@ -249,8 +279,84 @@ class Context:
         return out
 
     def spmv(self, a, x, y=None):
+        self._follow(a, x, y)
         x = _host(x)
         y = _like(x, self.n) if y is None else y
         self._check(self.lib.fcg_spmv(self.h, _ptr(_host(a)) if a is not None else None, _ptr(x),
                                       _ptr(y)), "fcg_spmv")
         return y
+
+
+class Batch:
+    """An fcg_batch: independent DPCG solves on several contexts in one persistent
+    launch (fcg_batch_dpcg).  Arrays may be numpy arrays or CUDA tensors."""
+
+    def __init__(self, contexts):
+        self.lib = _lib.load()
+        self.contexts = list(contexts)
+        arr = (C.c_void_p * len(self.contexts))(*[c.h.value for c in self.contexts])
+        h = C.c_void_p()
+        rc = self.lib.fcg_batch_create(arr, len(self.contexts), C.byref(h))
+        if rc != 0:
+            raise _lib.FcgError(rc, "fcg_batch_create", "contexts must be bound, distinct, one device")
+        self.h = h
+
+    def _check(self, rc, where):
+        if rc != 0:
+            raise _lib.FcgError(rc, where, self.lib.fcg_batch_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fcg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _ptrs(xs):
+        if xs is None:
+            return None
+        return (C.c_void_p * len(xs))(*[_ptr(x) for x in xs])
+
+    @property
+    def params(self):
+        spi, bps, mx = C.c_int(), C.c_int(), C.c_int()
+        self._check(self.lib.fcg_batch_get_params(self.h, C.byref(spi), C.byref(bps), C.byref(mx)),
+                    "fcg_batch_get_params")
+        return {"slices_per_item": spi.value, "blocks_per_sm": bps.value,
+                "max_blocks_per_sm": mx.value}
+
+    def set_params(self, slices_per_item: int, blocks_per_sm: int):
+        self._check(self.lib.fcg_batch_set_params(self.h, int(slices_per_item), int(blocks_per_sm)),
+                    "fcg_batch_set_params")
+
+    def autotune(self, a, su, sweeps: int = 20) -> float:
+        for k, c in enumerate(self.contexts):
+            c._follow(None if a is None else a[k], su[k])
+        a = None if a is None else [_host(x) for x in a]
+        su = [_host(x) for x in su]
+        best = C.c_double()
+        self._check(self.lib.fcg_batch_autotune(self.h, self._ptrs(a), self._ptrs(su), int(sweeps),
+                                                C.byref(best)), "fcg_batch_autotune")
+        return best.value
+
+    def dpcg(self, a, su, fi, sor, nsw):
+        """Returns (fi list, list of SolveResult); `a` may be None (matrices loaded last)."""
+        for k, c in enumerate(self.contexts):
+            c._follow(None if a is None else a[k], su[k], fi[k])
+        a = None if a is None else [_host(x) for x in a]
+        su = [_host(x) for x in su]
+        fi = [x.clone() if _is_torch(x) else np.array(x, dtype=np.float64) for x in fi]
+        ns = len(fi)
+        resor = (C.c_double * ns)(*([float("nan")] * ns))
+        reps = (_lib.SolveReport * ns)()
+        self._check(self.lib.fcg_batch_dpcg(self.h, self._ptrs(a), self._ptrs(su), self._ptrs(fi),
+                                            float(sor), int(nsw), resor, reps), "fcg_batch_dpcg")
+        out = [SolveResult(fi[k], None, reps[k].res0, reps[k].resl, reps[k].iters,
+                           bool(reps[k].converged), None if reps[k].iters == 0 else resor[k],
+                           reps[k].l2_rel, reps[k].seconds) for k in range(ns)]
+        return fi, out

@@ -54,8 +54,10 @@ const char *fcg_last_error(const fcg_context *ctx);
  * reference becomes per-context state). */
 int fcg_create(fcg_context **ctx, int device);
 int fcg_destroy(fcg_context *ctx);
-/* All work of the context is queued on this stream (cudaStream_t; NULL = the
- * context's own stream). */
+/* All later work of the context is queued on this stream (cudaStream_t; NULL = the
+ * context's own stream), ordered after the work already queued on the previous one.
+ * Device arrays passed to the library must be ready on this stream: the library does
+ * not wait for other streams. */
 int fcg_set_stream(fcg_context *ctx, void *cuda_stream);
 int fcg_synchronize(fcg_context *ctx);
 
@@ -246,6 +248,33 @@ const char *fcg_profile_unit_name(const fcg_context *ctx, int unit);
 int fcg_spmv(fcg_context *ctx, const double *a, const double *x, double *y);
 
 /* ---------------------------------------------------------------------------------
+ * Batched DPCG (no single reference call: it replaces a sequence of dpcg(fi,ifi) calls,
+ * dpcg.f90:3-154, on independent pressure systems).  Each system lives on its own bound
+ * context (its own mesh); all contexts must be on one device and distinct.  One
+ * persistent cooperative kernel, captured in a CUDA graph, runs every system's DPCG
+ * (the recurrence, constants and L1 stop test of dpcg.f90, per system) in lockstep
+ * phases separated by grid-wide barriers whose waits are bounded (FCG_ERR_TIMEOUT when
+ * one gives up).  Work items are runs of `slices_per_item` 32-row slices;
+ * fcg_batch_autotune times the candidates on the caller's systems and keeps the
+ * fastest (item size and CTAs per SM).  The batch runs on the first context's stream.
+ * --------------------------------------------------------------------------------- */
+typedef struct fcg_batch fcg_batch;
+int fcg_batch_create(fcg_context *const *ctxs, int nsys, fcg_batch **out);
+int fcg_batch_destroy(fcg_batch *batch);
+const char *fcg_batch_last_error(const fcg_batch *batch);
+int fcg_batch_set_params(fcg_batch *batch, int slices_per_item, int blocks_per_sm);
+int fcg_batch_get_params(const fcg_batch *batch, int *slices_per_item, int *blocks_per_sm,
+                         int *max_blocks_per_sm);
+/* a[k] (nnz of system k; a == NULL or a[k] == NULL reuses the matrix loaded last),
+ * su[k], fi[k] (in/out) of numCells of system k, host or device.  resor[nsys] and
+ * rep[nsys] may be NULL; rep[k].seconds is the time of the whole batch. */
+int fcg_batch_dpcg(fcg_batch *batch, const double *const *a, const double *const *su,
+                   double *const *fi, double sor, int nsw, double *resor, fcg_solve_report *rep);
+/* Times `sweeps` fixed sweeps of every candidate (x = 0) and keeps the fastest. */
+int fcg_batch_autotune(fcg_batch *batch, const double *const *a, const double *const *su,
+                       int sweeps, double *best_ms);
+
+/* ---------------------------------------------------------------------------------
  * Learned preconditioner (no reference counterpart; it is used in place of the
  * Jacobi preconditioner of dpcg.f90:85-100 inside flexible CG, with dpcg as fallback).
  *
@@ -286,22 +315,31 @@ int fcg_lp_set_matrix(fcg_learned *lp, fcg_context *ctx, const double *a);
 int fcg_lp_features(fcg_learned *lp, fcg_context *ctx, float *out);
 /* z = N(r). */
 int fcg_lp_apply(fcg_learned *lp, fcg_context *ctx, const float *r, float *z);
-/* Energy-norm loss (N(r) - e).Ahat (N(r) - e) / e.Ahat e and d loss / d weights
- * (grad[FCG_LP_PARAMS], may be NULL); BF16 roundings are treated as identities in the
- * gradient. */
+/* The loss chosen by fcg_lp_set_loss (default: residual norm, |Ahat N(r) - r|^2 / |r|^2)
+ * and d loss / d weights (grad[FCG_LP_PARAMS], may be NULL); BF16 roundings are treated
+ * as identities in the gradient. */
 int fcg_lp_loss_grad(fcg_learned *lp, fcg_context *ctx, const float *r, const float *e,
                      float *loss, float *grad);
+/* Loss of fcg_lp_loss_grad and fcg_lp_train_step: FCG_LP_LOSS_RESIDUAL (default),
+ * |Ahat N(r) - r|^2 / |r|^2, or FCG_LP_LOSS_ENERGY, (N(r) - e).Ahat (N(r) - e) / e.Ahat e
+ * (the same error measured in the energy norm). */
+#define FCG_LP_LOSS_ENERGY 0
+#define FCG_LP_LOSS_RESIDUAL 1
+int fcg_lp_set_loss(fcg_learned *lp, int kind);
 /* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on the pair (r, e) with rate lr;
  * *loss (may be NULL) receives the loss before the step. */
 int fcg_lp_train_step(fcg_learned *lp, fcg_context *ctx, const float *r, const float *e,
                       float lr, float *loss);
-/* Flexible-CG controls: FP64 residual replacement at least every ru_every iterations
- * (default 50); the FCG is declared stalled when the true L1 residual has not fallen
- * below stall_factor (default 0.5) times its value at the last such drop within
+/* Flexible-CG controls: the number of previous directions each new one is made
+ * A-orthogonal to (1..8, default 8); FP64 residual replacement at least every ru_every
+ * iterations (default 50); the FCG is declared stalled when the true L1 residual has not
+ * fallen below stall_factor (default 0.5) times its value at the last such drop within
  * stall_window iterations (default 400). */
-int fcg_lp_set_fcg_options(fcg_learned *lp, int ru_every, int stall_window, double stall_factor);
+int fcg_lp_set_fcg_options(fcg_learned *lp, int directions, int ru_every, int stall_window,
+                           double stall_factor);
 
-/* Flexible CG (Notay 2000, one previous direction) preconditioned by the network, on
+/* Truncated flexible CG (Notay, SIAM J. Sci. Comput. 22 (2000) 1444) preconditioned by
+ * the network, on
  * the arguments of fcg_dpcg and with its stop test resl/(res0+small) < sor on the
  * FP64 L1 residual.  The iteration runs in FP32 on Ahat with reliable updates: the
  * true residual su - A x is recomputed in FP64 when the FP32 residual has fallen 10x,

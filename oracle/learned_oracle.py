@@ -126,17 +126,25 @@ def forward(A: ScaledMatrix, feat, r, w, emulate: bool = True):
     return rms * y, dict(rms=rms, f=f, z0=z0, hs=hs, xs=xs, zs=zs, y=y)
 
 
-def loss_grad(A: ScaledMatrix, feat, r, e, w, emulate: bool = True):
-    """Energy-norm loss (N(r) - e).Ahat (N(r) - e) / e.Ahat e and its gradient
-    (straight-through roundings; Ahat symmetric, d loss / dy = 2 Ahat d / t.Ahat t)."""
+def loss_grad(A: ScaledMatrix, feat, r, e, w, emulate: bool = True, kind: str = "energy"):
+    """Loss of the normalised output d = y - t, t = e/rms, and its gradient
+    (straight-through roundings, Ahat symmetric):
+      energy:   d.Ahat d / t.Ahat t,        d loss/dy = 2 Ahat d / t.Ahat t
+      residual: |Ahat d|^2 / |Ahat t|^2,    d loss/dy = 2 Ahat Ahat d / |Ahat t|^2"""
     W_in, b_in, layers, w_out, b_out = unpack(w)
     z, c = forward(A, feat, r, w, emulate)
     t = np.asarray(e, dtype=np.float64) / c["rms"]
     d = c["y"] - t
     Ad = A.matmul(d[:, None])[:, 0]
-    tAt = np.dot(t, A.matmul(t[:, None])[:, 0])
-    loss = np.dot(d, Ad) / tAt
-    dy = 2.0 * Ad / tAt
+    At = A.matmul(t[:, None])[:, 0]
+    if kind == "energy":
+        den = np.dot(t, At)
+        loss = np.dot(d, Ad) / den
+        dy = 2.0 * Ad / den
+    else:
+        den = np.dot(At, At)
+        loss = np.dot(Ad, Ad) / den
+        dy = 2.0 * A.matmul(Ad[:, None])[:, 0] / den
     g_wout = c["hs"][-1].T @ dy
     g_bout = dy.sum()
     dh = np.outer(dy, w_out)

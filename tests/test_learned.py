@@ -60,7 +60,8 @@ def test_bf16_rounding_matches_torch():
     assert np.array_equal(lo.bf16(x), ref)
 
 
-def test_oracle_gradient_matches_finite_differences():
+@pytest.mark.parametrize("kind", ["energy", "residual"])
+def test_oracle_gradient_matches_finite_differences(kind):
     m, csr, a, su = _oracle_system(4)
     A = lo.ScaledMatrix(csr.ioffset, csr.ja, csr.diag, a)
     feat = lo.features(m, A.s)
@@ -68,7 +69,7 @@ def test_oracle_gradient_matches_finite_differences():
     r = rng.standard_normal(m.numCells)
     e = rng.standard_normal(m.numCells)
     w = _random_weights(2, scale=3.0).astype(np.float64)
-    loss, g = lo.loss_grad(A, feat, r, e, w, emulate=False)
+    loss, g = lo.loss_grad(A, feat, r, e, w, emulate=False, kind=kind)
     idx = rng.choice(lo.P, 80, replace=False)
     idx = np.concatenate([idx, [lo.P - 1, 0, lo.C * lo.F]])  # b_out, W_in, b_in
     h = 1e-6
@@ -76,8 +77,8 @@ def test_oracle_gradient_matches_finite_differences():
         wp, wm = w.copy(), w.copy()
         wp[i] += h
         wm[i] -= h
-        fd = (lo.loss_grad(A, feat, r, e, wp, emulate=False)[0] -
-              lo.loss_grad(A, feat, r, e, wm, emulate=False)[0]) / (2 * h)
+        fd = (lo.loss_grad(A, feat, r, e, wp, emulate=False, kind=kind)[0] -
+              lo.loss_grad(A, feat, r, e, wm, emulate=False, kind=kind)[0]) / (2 * h)
         assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(g[i])) + 1e-7, (i, fd, g[i])
 
 
@@ -154,20 +155,22 @@ def test_forward_matches_oracle(N):
 
 
 @pytest.mark.gpu
-def test_loss_gradient_matches_oracle():
+@pytest.mark.parametrize("kind", ["energy", "residual"])
+def test_loss_gradient_matches_oracle(kind):
     from freecappuccino_gb300.learned import LearnedPreconditioner
 
     sysm = _gpu_system(14)
     io, ja, dg, _, _ = sysm.ctx.create_csr()
     A = lo.ScaledMatrix(io, ja, dg, sysm.a)
     lp = LearnedPreconditioner(seed=1)
+    lp.set_loss(kind)
     w = _random_weights(5, scale=2.0)
     lp.weights = w
     lp.set_matrix(sysm.ctx, sysm.a)
     r, e = _pair(sysm, 5)
     loss, g = lp.loss_grad(sysm.ctx, r, e)
     feat = lo.features(sysm.mesh, sysm.scale)
-    lr_, gr = lo.loss_grad(A, feat, r, e, w, emulate=True)
+    lr_, gr = lo.loss_grad(A, feat, r, e, w, emulate=True, kind=kind)
     assert loss == pytest.approx(lr_, rel=2e-3)
     # per parameter group: embedding, each layer, output
     bounds = [0, lo.C * lo.F + lo.C] + [lo.C * lo.F + lo.C + (l + 1) * lo.LAYER
@@ -233,7 +236,7 @@ def test_fcg_stall_falls_back_to_dpcg():
 
     sysm = _gpu_system(16)
     lp = LearnedPreconditioner(seed=1)
-    lp.set_fcg_options(ru_every=5, stall_window=10, stall_factor=1e-9)
+    lp.set_fcg_options(directions=2, ru_every=5, stall_window=10, stall_factor=1e-9)
     x0 = np.zeros(sysm.ctx.n)
     r = lp.solve(sysm.ctx, sysm.a, sysm.su, x0, 1e-8, 5000)
     assert r.fallback and r.converged
