@@ -6,9 +6,13 @@ vertices jittered U(-0.2h, 0.2h), unit diffusivity, Dirichlet p = 0 on the x = 0
 zero-gradient elsewhere, RHS U(-1,1) * cell volume from a fixed seed), assembled with
 the laplacian kernel and solved to the reference's stop test, L1-relative residual
 < 1e-8.  One step = one solve from a zero start through the C ABI (matrix load into the
-solver's sliced-ELL copy, the whole Krylov loop, the final FP64 residual check).
+solver's copies, the whole Krylov loop, the final FP64 residual check).
 
-Metric: time to 1e-8 relative residual (seconds, lower is better).
+Metric: time to 1e-8 relative residual (seconds, lower is better) of the learned
+preconditioner's flexible CG (FP32 iteration, FP64 residual replacements, BF16 network),
+next to plain FP64 DPCG and mixed-precision DPCG on the same system (extra.comparisons).
+The uneven batch of 24 pressure systems solved by the persistent batched DPCG is
+reported in extra.batched.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -199,10 +203,75 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def learned_launches(stats):
+    """Kernels one learned FCG solve launches: init 1 + per iteration 9 (network) + 4 (FCG)
+    + 1 (loop close) + 2 per FP64 residual replacement + final check 1; matrix set-up 4."""
+    return 4 + 1 + 14 * stats["iters"] + 2 * stats["updates"] + 1
+
+
+def batch_workload(seed, count=24, sizes=(32, 48, 64, 96, 128)):
+    """The uneven batch: `count` pressure systems, N drawn uniformly from `sizes`, each
+    with its own seeded jitter field (a = 0.2) and RHS."""
+    import freecappuccino_gb300 as fcg
+
+    pick = fcg.uniform(seed, 31, count, 0.0, 1.0)
+    return [(sizes[min(len(sizes) - 1, int(u * len(sizes)))], seed * 100 + k)
+            for k, u in enumerate(pick)]
+
+
+def run_batch(args, dev, peak):
+    """Batched persistent DPCG over the uneven batch (inputs resident); the same
+    systems solved one after another with fcg_dpcg for comparison."""
+    import torch
+
+    import freecappuccino_gb300 as fcg
+
+    t0 = time.perf_counter()
+    systems = []
+    for N, sd in batch_workload(args.batch_seed):
+        m = fcg.hex_mesh(N, jitter=JITTER, seed=sd)
+        ctx = fcg.Context(m, device=dev.index or 0)
+        su0 = torch.from_numpy(fcg.uniform(sd, 0, m.numCells) * m.vol).to(dev)
+        a, su = ctx.laplacian(torch.full((m.numCells,), -1.0, dtype=torch.float64, device=dev),
+                              torch.zeros(m.numTotal, dtype=torch.float64, device=dev), su0)
+        systems.append((N, m.numCells, m.nnz, ctx, a, su))
+    setup = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    ctxs = [s[3] for s in systems]
+    a = [s[4] for s in systems]
+    su = [s[5] for s in systems]
+    x0 = [torch.zeros(s[1], dtype=torch.float64, device=dev) for s in systems]
+    b = fcg.Batch(ctxs)
+    best = b.autotune(a, su, sweeps=20)
+    b.dpcg(a, su, x0, TOL, NSW)  # warm-up (graph capture)
+    _, reps = b.dpcg(None, su, x0, TOL, NSW)
+    t_batch = reps[0].seconds
+    seq = [c.dpcg(ak, sk, xk, TOL, NSW, want_res=False) for c, ak, sk, xk in zip(ctxs, a, su, x0)]
+    t_seq = sum(r.seconds for r in seq)
+    cells = sum(s[1] for s in systems)
+    cell_sweeps = sum(s[1] * r.iters for s, r in zip(systems, reps))
+    nbytes = sum(r.iters * dpcg_iter_bytes(s[1], s[2]) + 2 * spmv_bytes(s[1], s[2])
+                 for s, r in zip(systems, reps))
+    out = {"workload": "24 pressure Poisson systems, N^3 jittered hex with N drawn uniformly "
+                       "from {32,48,64,96,128}, own seeded jitter and RHS, FP64 DPCG to 1e-8",
+           "sizes": [s[0] for s in systems], "cells": cells, "seconds": t_batch,
+           "solves_per_s": len(systems) / t_batch, "cell_sweeps_per_s": cell_sweeps / t_batch,
+           "cells_per_s": cells / t_batch,
+           "hbm_GBps_algorithmic": nbytes / t_batch / 1e9, "hbm_frac": nbytes / t_batch / 1e9 / peak,
+           "sequential_fcg_dpcg_s": t_seq, "speedup_vs_sequential": t_seq / t_batch,
+           "iters": [r.iters for r in reps], "all_converged": all(r.converged for r in reps),
+           "max_l2_rel": max(r.l2_rel for r in reps), "autotune": b.params,
+           "autotune_best_ms_20_sweeps": best, "gpu_launches": 1, "setup_s": setup}
+    b.close()
+    for c in ctxs:
+        c.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="fcg", choices=["fcg", "reference"])
     ap.add_argument("--N", type=int, default=256)
@@ -211,9 +280,12 @@ def main():
     ap.add_argument("--ref-sweeps", type=int, default=1200,
                     help="sweep count used by the reference arm when none is recorded")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-seed", type=int, default=4242)
     ap.add_argument("--e2e-steps", type=int, default=2)
-    ap.add_argument("--solver", default="dpcg_mixed",
-                    choices=["dpcg_mixed", "dpcg", "iccg", "bicgstab"])
+    ap.add_argument("--solver", default="learned",
+                    choices=["learned", "dpcg_mixed", "dpcg", "iccg", "bicgstab"])
+    ap.add_argument("--weights", default=None, help="learned checkpoint (default: shipped)")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven sweep loop instead of the CUDA-graph WHILE loop")
     args = ap.parse_args()
@@ -229,6 +301,7 @@ def main():
 
     import freecappuccino_gb300 as fcg
     from freecappuccino_gb300 import _lib
+    from freecappuccino_gb300.learned import DEFAULT_WEIGHTS, LearnedPreconditioner
 
     torch.cuda.set_device(local)
     lib = _lib.load()
@@ -248,11 +321,22 @@ def main():
         a_d, su_d = ctx.laplacian(mu_d, phi_d, su_d)
         fi0 = torch.zeros(n, dtype=torch.float64, device=dev)
     stream.synchronize()
+    lp = LearnedPreconditioner(device=local, path=args.weights or DEFAULT_WEIGHTS)
 
     method = args.solver
 
     def run(name):
+        if name == "learned":
+            return lp.solve(ctx, a_d, su_d, fi0, TOL, NSW)
         return getattr(ctx, name)(a_d, su_d, fi0, TOL, NSW, want_res=False)
+
+    def timed(name):
+        t0e, t1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0e.record(stream)
+        r = run(name)
+        t1e.record(stream)
+        torch.cuda.synchronize()
+        return r, reduce_max(ws, t0e.elapsed_time(t1e) * 1e-3)
 
     for _ in range(args.warmup):
         run(method)
@@ -262,11 +346,13 @@ def main():
     torch.cuda.synchronize()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
            for _ in range(args.steps)]
-    reports = []
+    reports, launches = [], 0
     for e0, e1 in evs:
         e0.record(stream)
         reports.append(run(method))
         e1.record(stream)
+        if method == "learned":
+            launches += learned_launches(lp.last_solve_stats())
     torch.cuda.synchronize()
     barrier(ws)
     clocks = sampler.stop()
@@ -274,54 +360,61 @@ def main():
     t_solve = reduce_max(ws, statistics.mean(step_s))
     last = reports[-1]
     iters = last.iters
-    per_solve_launches = {"dpcg": lambda it: 3 + 3 * it, "dpcg_mixed": lambda it: 6 + 5 * it}
-    launches = sum(per_solve_launches.get(method, lambda it: 3 + 3 * it)(r.iters) for r in reports)
+    if method != "learned":
+        per_solve = {"dpcg": lambda it: 3 + 3 * it, "dpcg_mixed": lambda it: 6 + 5 * it}
+        launches = sum(per_solve.get(method, lambda it: 3 + 3 * it)(r.iters) for r in reports)
     x_method = last.fi.clone()
-
-    # Per-kernel device time of the method's sweep, CUDA events around each launch.
-    prof = ctx.profile_sweeps(20)
     peak, peak_kind = peaks()
-    if method == "dpcg_mixed":
-        dom = "k_mx_spmv"
-        dom_bytes = 8 * nnz + 4 * (n + 1) + 8 * n  # FP32 values + int32 columns, FP32 x/y
-        sweep_bytes = dom_bytes + 36 * n           # + FP32 vector passes of one sweep
-        dom_desc = "k_mx_spmv (FP32 sliced-ELL SpMV of the scaled matrix + p.Ap, 256^3)"
-    else:
-        dom = "k_cg_spmv"
-        dom_bytes = spmv_bytes(n, nnz)
-        sweep_bytes = dpcg_iter_bytes(n, nnz)
-        dom_desc = "k_cg_spmv (FP64 sliced-ELL SpMV + p.Ap, 256^3)"
-    t_dom = prof[dom] * 1e-3
-    achieved = dom_bytes / t_dom / 1e9
-    traffic = None
+
+    # Roofline of the dominant kernel, from CUDA events around each launch.
     tp = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tp):
-        traffic = json.load(open(tp)).get(dom, {}).get(f"bytes_per_launch_{N}")
+    traffic_db = json.load(open(tp)) if os.path.exists(tp) else {}
+    if method == "learned":
+        r32 = (su_d * (1.0 / torch.sqrt(a_d[torch.from_numpy(ctx.create_csr()[2] - 1).to(dev)])))
+        prof = lp.profile(ctx, r32.to(torch.float32), reps=10)
+        layers = [v for k, v in prof.items() if k.startswith("k_lp_layer")]
+        t_dom = statistics.mean(layers) * 1e-3
+        dom_bytes = 128 * n + 4 * nnz  # BF16 activations in and out, FP32 Ahat values
+        dom_desc = ("k_lp_layer (one message-passing layer: gather of BF16 neighbour rows "
+                    "through the FP32 scaled matrix, 16x64x32 mma.sync BF16 tiles, 256^3)")
+        dom = "k_lp_layer"
+        prof_extra = {"forward_kernels_ms": prof, "forward_ms": sum(prof.values()),
+                      "layer_tensor_TFLOPs": 4096.0 * n / t_dom / 1e12}
+    else:
+        prof = ctx.profile_sweeps(20)
+        if method == "dpcg_mixed":
+            dom = "k_mx_spmv"
+            dom_bytes = 8 * nnz + 4 * (n + 1) + 8 * n  # FP32 values + int32 columns, FP32 x/y
+            dom_desc = "k_mx_spmv (FP32 sliced-ELL SpMV of the scaled matrix + p.Ap, 256^3)"
+        else:
+            dom = "k_cg_spmv"
+            dom_bytes = spmv_bytes(n, nnz)
+            dom_desc = "k_cg_spmv (FP64 sliced-ELL SpMV + p.Ap, 256^3)"
+        t_dom = prof[dom] * 1e-3
+        prof_extra = {"sweep_kernels_ms": prof}
+    achieved = dom_bytes / t_dom / 1e9
+    traffic = traffic_db.get(dom, {}).get(f"bytes_per_launch_{N}")
     roof = {"kernel": dom_desc, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
-            "algorithmic_bytes_per_launch": dom_bytes, "launch_ms": t_dom * 1e3,
-            "sweep_kernels_ms": prof}
-    sweep_gbs = sweep_bytes / (t_solve / max(iters, 1)) / 1e9
+            "algorithmic_bytes_per_launch": dom_bytes, "launch_ms": t_dom * 1e3, **prof_extra}
 
-    # Plain FP64 DPCG on the same system: the method the headline is compared with.
-    fp64 = None
-    if method != "dpcg":
-        run("dpcg")
-        t0e, t1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        t0e.record(stream)
-        r64 = run("dpcg")
-        t1e.record(stream)
-        torch.cuda.synchronize()
-        t64 = reduce_max(ws, t0e.elapsed_time(t1e) * 1e-3)
-        err = float((x_method - r64.fi).abs().max() / r64.fi.abs().max())
-        fp64 = {"dpcg_fp64_s": t64, "dpcg_fp64_sweeps": r64.iters, "speedup_vs_fp64": t64 / t_solve,
-                "max_rel_diff_vs_fp64_solution": err,
-                "fp64_sweep_GBps": dpcg_iter_bytes(n, nnz) / (t64 / r64.iters) / 1e9}
+    # The methods the headline is compared with, on the same system.
+    comparisons = {}
+    for other in ("dpcg", "dpcg_mixed"):
+        if other == method:
+            continue
+        run(other)
+        r_o, t_o = timed(other)
+        err = float((x_method - r_o.fi).abs().max() / r_o.fi.abs().max())
+        comparisons[other] = {"seconds": t_o, "sweeps": r_o.iters, "l2_rel": r_o.l2_rel,
+                              "headline_speedup": t_o / t_solve,
+                              "max_rel_diff_of_headline_solution": err}
+    dpcg_sweeps = comparisons.get("dpcg", {}).get("sweeps", iters)
 
     # Standalone FP64 SpMV (one event pair per launch: host gaps are not counted).
     x = torch.rand(n, dtype=torch.float64, device=dev)
     y = torch.empty_like(x)
-    ctx.spmv(None, x, y)
+    ctx.spmv(a_d, x, y)
     pairs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
              for _ in range(20)]
     for s0, s1 in pairs:
@@ -346,9 +439,13 @@ def main():
         rep = _lib.SolveReport()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        entry = lib.fcg_dpcg_mixed if method == "dpcg_mixed" else lib.fcg_dpcg
-        rc = entry(ctx.h, a_h.data_ptr(), su_h.data_ptr(), fi_h.data_ptr(), None, TOL, NSW,
-                   C.byref(resor), C.byref(rep))
+        if method == "learned":
+            rc = lib.fcg_fcg_learned(ctx.h, lp.h, a_h.data_ptr(), su_h.data_ptr(), fi_h.data_ptr(),
+                                     None, TOL, NSW, C.byref(resor), C.byref(rep), None, None)
+        else:
+            entry = lib.fcg_dpcg_mixed if method == "dpcg_mixed" else lib.fcg_dpcg
+            rc = entry(ctx.h, a_h.data_ptr(), su_h.data_ptr(), fi_h.data_ptr(), None, TOL, NSW,
+                       C.byref(resor), C.byref(rep))
         e1.record(stream)
         torch.cuda.synchronize()
         assert rc == 0, rc
@@ -358,29 +455,38 @@ def main():
         e2e = {"value": reduce_max(ws, statistics.mean(e2e_s)), "unit": "s",
                "h2d_bytes_per_step": 8 * nnz + 16 * n, "d2h_bytes_per_step": 8 * n}
 
+    batch = None
+    if not args.no_batch:
+        batch = run_batch(args, dev, peak)
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        cpu = cpu_baseline(m, mu, phi, su, iters, args.cpu_sample)
+        cpu = cpu_baseline(m, mu, phi, su, dpcg_sweeps, args.cpu_sample)
 
     if rank == 0:
+        dtype = {"learned": "f32 FCG + bf16 network (fp32 accumulate), f64 residual/updates",
+                 "dpcg_mixed": "f32 sweeps, f64 residual/updates"}.get(method, "f64")
+        extra = {"comparisons": comparisons, "spmv_fp64": spmv64,
+                 "l2_rel_final": last.l2_rel, "resl_over_res0": last.resl / last.res0,
+                 "mesh_setup_s": t_mesh, "bind_s": t_bind, "step_s": step_s, "batched": batch}
+        if method == "learned":
+            extra["learned"] = {"fcg_iterations": last.fcg_iters, "fallback": last.fallback,
+                                "directions": 8, "weights": os.path.relpath(
+                                    args.weights or DEFAULT_WEIGHTS, ROOT)}
         line = {"metric": METRIC, "value": t_solve, "unit": "s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_solve * 1e3, "higher_is_better": False,
-                "scaling": "weak", "vs_baseline": None,
-                "dtype": "f32 sweeps, f64 residual/updates" if method == "dpcg_mixed" else "f64",
+                "scaling": "weak", "vs_baseline": None, "dtype": dtype,
                 "data": "synthetic: seeded jittered hex mesh and U(-1,1)*vol right-hand side",
                 "config": {"workload": f"pressure Poisson {N}^3 jittered hex ({n} cells, nnz {nnz}), "
                                        "solved to L1-relative 1e-8 (true FP64 residual)",
                            "method": method, "N": N, "cells": n, "nnz": nnz,
-                           "jitter": JITTER, "tolerance": TOL, "sweeps": iters,
-                           "l2": "inputs larger than L2 (matrix 1.4 GB, vectors 134 MB each)",
+                           "jitter": JITTER, "tolerance": TOL, "iterations": iters,
+                           "l2": "inputs larger than L2 (matrix 0.94 GB, vectors 134 MB each)",
                            "parallelism": f"replicas x{ws}"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
-                "gpu_launches": launches,
-                "extra": {"fp64_comparison": fp64, "spmv_fp64": spmv64,
-                          "sweep_GBps_algorithmic": sweep_gbs, "sweep_frac": sweep_gbs / peak,
-                          "l2_rel_final": last.l2_rel, "resl_over_res0": last.resl / last.res0,
-                          "mesh_setup_s": t_mesh, "bind_s": t_bind, "step_s": step_s}}
+                "gpu_launches": launches, "extra": extra}
         print(json.dumps(line), flush=True)
+    lp.close()
     ctx.close()
 
 

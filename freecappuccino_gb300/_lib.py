@@ -73,6 +73,9 @@ _PROTOS = {
     "fcg_laplacian": (C.c_int, [_CTX, _vp, _vp, _vp, _vp]),
     "fcg_facefluxmass": (C.c_int, [_CTX, C.POINTER(FlowFields), _vp, _vp, _vp]),
     "fcg_fluxmc": (C.c_int, [_CTX, _vp, _vp, _vp, _vp, _vp]),
+    "fcg_flux_correct": (C.c_int, [_CTX, _vp, _vp, _vp]),
+    "fcg_correct_fields": (C.c_int, [_CTX, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_int, _vp,
+                                     _vp, _vp, _vp]),
     "fcg_grad": (C.c_int, [_CTX, _vp, _vp, C.c_int, C.c_int]),
     "fcg_grad_lsq_matrix": (C.c_int, [_CTX, _vp]),
     "fcg_bpres": (C.c_int, [_CTX, _vp, _vp, C.c_int]),
@@ -116,6 +119,8 @@ _PROTOS = {
     "fcg_lp_loss_grad": (C.c_int, [_LP, _CTX, _vp, _vp, C.POINTER(C.c_float), _vp]),
     "fcg_lp_train_step": (C.c_int, [_LP, _CTX, _vp, _vp, C.c_float, C.POINTER(C.c_float)]),
     "fcg_lp_set_loss": (C.c_int, [_LP, C.c_int]),
+    "fcg_lp_last_solve_stats": (C.c_int, [_LP, _ip, _ip]),
+    "fcg_lp_profile": (C.c_int, [_LP, _CTX, _vp, C.c_int, _dp, C.c_int, _ip]),
     "fcg_lp_set_fcg_options": (C.c_int, [_LP, C.c_int, C.c_int, C.c_int, C.c_double]),
     "fcg_fcg_learned": (C.c_int, [_CTX, _LP, _vp, _vp, _vp, _vp, C.c_double, C.c_int, _dp,
                                   C.POINTER(SolveReport), _ip, _ip]),

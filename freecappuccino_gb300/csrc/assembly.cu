@@ -292,3 +292,99 @@ extern "C" int fcg_fluxmc(fcg_context *c, const double *dPdxi, const double *apu
   if (hsu || hfm) FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return FCG_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Corrections of calcp after the p' solve
+// ---------------------------------------------------------------------------
+namespace fcg {
+namespace corr {
+
+// flmass(f) += a(slot_pn(f)) * (pp(N) - pp(P)) (calcp-multiple_correction_SIMPLE.f90:159-171)
+__global__ void k_flux_correct(MeshView m, const double *__restrict__ a,
+                               const double *__restrict__ pp, double *__restrict__ flmass) {
+  FCG_GRID_STRIDE(f, m.nin) {
+    const int P = m.owner[f], N = m.neighbour[f];
+    flmass[f] = flmass[f] + a[m.slot_pn[f]] * (pp[N] - pp[P]);
+  }
+}
+
+// u -= dPdxi(1)*vol*apu, v -= dPdxi(2)*vol*apv, w -= dPdxi(3)*vol*apw,
+// p += urf*(pp - ppref) (calcp-multiple_correction_SIMPLE.f90:184-189)
+__global__ void k_correct_fields(MeshView m, const double *__restrict__ g,
+                                 const double *__restrict__ apu, const double *__restrict__ apv,
+                                 const double *__restrict__ apw, const double *__restrict__ pp,
+                                 double urf, int ref, double *__restrict__ u,
+                                 double *__restrict__ v, double *__restrict__ w,
+                                 double *__restrict__ p) {
+  const double ppref = pp[ref];
+  FCG_GRID_STRIDE(i, m.n) {
+    const double vol = m.vol[i];
+    u[i] = u[i] - g[3 * i] * vol * apu[i];
+    v[i] = v[i] - g[3 * i + 1] * vol * apv[i];
+    w[i] = w[i] - g[3 * i + 2] * vol * apw[i];
+    p[i] = p[i] + urf * (pp[i] - ppref);
+  }
+}
+
+}  // namespace corr
+}  // namespace fcg
+
+extern "C" int fcg_flux_correct(fcg_context *c, const double *a, const double *pp,
+                                double *flmass) {
+  if (!c) return FCG_ERR_ARG;
+  if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_flux_correct before fcg_bind_mesh");
+  if (!a || !pp || !flmass) return set_error(c, FCG_ERR_ARG, "NULL a, pp or flmass");
+  FCG_CUDA_TRY(c, cudaSetDevice(c->device));
+  void *da, *dpp, *dfm;
+  bool ha, hpp, hfm;
+  int rc;
+  const size_t nf = sizeof(double) * (c->nin > 0 ? c->nin : 1);
+  if ((rc = stage_in(c, a, sizeof(double) * c->nnz, 0, true, &da, &ha))) return rc;
+  if ((rc = stage_in(c, pp, sizeof(double) * c->ntot, 1, true, &dpp, &hpp))) return rc;
+  if ((rc = stage_in(c, flmass, nf, 2, true, &dfm, &hfm))) return rc;
+  if (c->nin > 0) {
+    fcg::corr::k_flux_correct<<<grid_for(c->nin, c->num_sms), kTPB, 0, c->stream>>>(
+        c->mv, (const double *)da, (const double *)dpp, (double *)dfm);
+    FCG_CHECK_LAUNCH(c, "k_flux_correct");
+  }
+  if ((rc = stage_out(c, flmass, dfm, sizeof(double) * c->nin, hfm))) return rc;
+  if (hfm) FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return FCG_OK;
+}
+
+extern "C" int fcg_correct_fields(fcg_context *c, const double *dPdxi, const double *apu,
+                                  const double *apv, const double *apw, const double *pp,
+                                  double urf, int pRefCell, double *u, double *v, double *w,
+                                  double *p) {
+  if (!c) return FCG_ERR_ARG;
+  if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_correct_fields before fcg_bind_mesh");
+  if (!dPdxi || !apu || !apv || !apw || !pp || !u || !v || !w || !p)
+    return set_error(c, FCG_ERR_ARG, "NULL array");
+  if (pRefCell < 1 || pRefCell > c->n) return set_error(c, FCG_ERR_INDEX, "pRefCell out of range");
+  FCG_CUDA_TRY(c, cudaSetDevice(c->device));
+  const size_t n1 = sizeof(double) * c->n, nt = sizeof(double) * c->ntot;
+  const void *in[6] = {dPdxi, apu, apv, apw, pp, nullptr};
+  const size_t inb[5] = {3 * n1, n1, n1, n1, nt};
+  void *din[5];
+  bool hin[5];
+  int rc;
+  for (int k = 0; k < 5; ++k)
+    if ((rc = stage_in(c, in[k], inb[k], k, true, &din[k], &hin[k]))) return rc;
+  double *out[4] = {u, v, w, p};
+  void *dout[4];
+  bool hout[4];
+  for (int k = 0; k < 4; ++k)
+    if ((rc = stage_in(c, out[k], nt, 5 + k, true, &dout[k], &hout[k]))) return rc;
+  fcg::corr::k_correct_fields<<<grid_for(c->n, c->num_sms), kTPB, 0, c->stream>>>(
+      c->mv, (const double *)din[0], (const double *)din[1], (const double *)din[2],
+      (const double *)din[3], (const double *)din[4], urf, pRefCell - 1, (double *)dout[0],
+      (double *)dout[1], (double *)dout[2], (double *)dout[3]);
+  FCG_CHECK_LAUNCH(c, "k_correct_fields");
+  bool any = false;
+  for (int k = 0; k < 4; ++k) {
+    if ((rc = stage_out(c, out[k], dout[k], nt, hout[k]))) return rc;
+    any = any || hout[k];
+  }
+  if (any) FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return FCG_OK;
+}

@@ -60,6 +60,7 @@ constexpr int oWin = 0, oBin = C * F, oLayer0 = C * F + C;
 constexpr int oWout = oLayer0 + L * kLayerParams, oBout = oWout + C;
 constexpr int P = oBout + 1;
 static_assert(P == FCG_LP_PARAMS, "parameter count must match the header");
+static_assert(oBin == oWin + C * F && oLayer0 == oBin + C, "parameter layout");
 constexpr int kBwdTile = 64;            // cells per shared-memory tile of the layer backward
 constexpr int kTileStride = 2 * C + 8;  // padded BF16 row of the [h; m] tile and of W_l
 constexpr int kRed = 8;                 // reduction tickets
@@ -96,6 +97,7 @@ struct fcg_learned {
   size_t ncap = 0;
   bool train_cap = false;
   DBuf feat, hbuf, mbuf, zbuf, dh, dh2, dm, y, dvec, part, red, scal;
+  DBuf chunks;  // per-128-row chunk descriptors of the layer kernel (pattern of the mesh)
   // which context, mesh and matrix the features belong to
   unsigned long long fuid = 0;
   unsigned fgen = 0;
@@ -227,6 +229,94 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4],
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
+
+// Chunks of the layer kernel: 128 rows = 4 slices = 8 tiles of 16 cells.  A chunk
+// whose four slices are uniform with the same <= 8 column offsets (one of them 0) and
+// lie inside the mesh takes the staged path: the rows r0 + off .. r0 + off + 127 of
+// every offset, merged into windows where offsets lie within kMergeGap of each other,
+// are copied into shared memory once (cp.async, 16 bytes per copy) together with the
+// chunk's matrix values, and all gathers then read shared memory.  Other chunks gather
+// from global memory row by row.
+constexpr int kChunkRows = 128;
+constexpr int kStageRows = 704;  // staged activation rows per chunk (44 KB of BF16)
+constexpr int kMergeGap = 32;
+
+struct ChunkDesc {
+  int fast, w, nwin, j0;            // staged path?, slots, windows, slot of offset 0
+  int win_first[8], win_len[8];     // window start (offset from r0) and length in rows
+  int win_smem[8];                  // first staged row of each window
+  int soff[8];                      // staged row of local row 0 for each slot
+};
+
+__global__ void k_lp_chunks(SellView s, int n, ChunkDesc *__restrict__ d, int nchunks) {
+  FCG_GRID_STRIDE(c, nchunks) {
+    ChunkDesc D;
+    memset(&D, 0, sizeof D);
+    const int s0 = (int)c * 4;
+    const long long r0 = c * kChunkRows;
+    bool ok = s0 + 3 < s.nslices && r0 + kChunkRows <= n;
+    int off[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int w = 0;
+    if (ok) {
+      w = s.width[s0];
+      ok = w >= 1 && w <= 8;
+      for (int k = 0; ok && k < 4; ++k) {
+        ok = s.kind[s0 + k] == 0 && s.width[s0 + k] == w;
+        for (int j = 0; ok && j < w; ++j) {
+          const int o = s.off[s.offp[s0 + k] + j];
+          if (k == 0) off[j] = o;
+          else ok = off[j] == o;
+        }
+      }
+    }
+    int j0 = -1;
+    for (int j = 0; ok && j < w; ++j)
+      if (off[j] == 0) j0 = j;
+    ok = ok && j0 >= 0;
+    if (ok) {
+      int order[8];
+      for (int j = 0; j < w; ++j) order[j] = j;
+      for (int a = 1; a < w; ++a)  // insertion sort of the slots by offset
+        for (int b = a; b > 0 && off[order[b - 1]] > off[order[b]]; --b) {
+          const int t = order[b];
+          order[b] = order[b - 1];
+          order[b - 1] = t;
+        }
+      int nwin = 0, rows = 0, first = 0, last = 0;
+      for (int k = 0; k < w; ++k) {
+        const int o = off[order[k]];
+        if (k == 0 || o - last > kMergeGap) {
+          if (k > 0) {
+            D.win_first[nwin] = first;
+            D.win_len[nwin] = last - first + kChunkRows;
+            D.win_smem[nwin] = rows;
+            rows += D.win_len[nwin];
+            ++nwin;
+          }
+          first = o;
+        }
+        last = o;
+        D.soff[order[k]] = nwin;  // window index for now
+      }
+      D.win_first[nwin] = first;
+      D.win_len[nwin] = last - first + kChunkRows;
+      D.win_smem[nwin] = rows;
+      rows += D.win_len[nwin];
+      ++nwin;
+      for (int j = 0; j < w; ++j) {
+        const int k = D.soff[j];
+        D.soff[j] = D.win_smem[k] + (off[j] - D.win_first[k]);
+      }
+      D.nwin = nwin;
+      ok = rows <= kStageRows;
+    }
+    D.fast = ok ? 1 : 0;
+    D.w = w;
+    D.j0 = j0;
+    d[c] = D;
+  }
+}
+
 // acc[0..7] += v * (8 BF16 values packed in q)
 __device__ __forceinline__ void fma8(float (&acc)[8], float v, const uint4 &q) {
   const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(&q);
@@ -234,26 +324,55 @@ __device__ __forceinline__ void fma8(float (&acc)[8], float v, const uint4 &q) {
   for (int c = 0; c < 8; ++c) acc[c] += v * bf(e[c]);
 }
 
-// One message-passing layer.  A warp owns 16 cells (one tile) at a time and takes them
-// in two rounds of 8: four lanes per cell, eight channels per lane, sum
-// m = Ahat h over the cell's sliced row -- for uniform slices the column offsets,
-// values and neighbour activations of four slots are loaded before any is used -- and
-// write the [h; m] row (64 BF16) into the warp's shared tile.  4 k-steps x 4 n-blocks of
-// mma.sync give the 16 x 32 pre-activation; the epilogue adds the bias, applies the ReLU
-// and the skip connection, puts h' back into the tile, and the tile leaves in 16-byte
-// stores (16 consecutive cells = 1 KB contiguous).  Rows of the tile and of W_l are
-// padded to 72 elements so that the fragment loads of the 8 row groups fall in distinct
-// banks.
-__global__ void __launch_bounds__(kTPB, 4)
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem));
+}
+
+// Writes row `rloc` of the warp's [h; m] tile: own h (8 channels) and m = Ahat h.
+__device__ __forceinline__ void put_row(__nv_bfloat16 *tw, int rloc, int qc, const uint4 &own,
+                                        const float (&acc)[8], float *mout, int r, int n) {
+  constexpr int TS = lp::kTileStride;
+  __nv_bfloat16 *row = tw + rloc * TS;
+  *reinterpret_cast<uint4 *>(row + qc) = own;
+  __align__(16) __nv_bfloat16 mb[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) mb[c] = __float2bfloat16(acc[c]);
+  *reinterpret_cast<uint4 *>(row + C + qc) = *reinterpret_cast<const uint4 *>(mb);
+  if (mout && r < n) {
+    float4 *mo = reinterpret_cast<float4 *>(mout + (long long)r * C + qc);
+    mo[0] = make_float4(bf(mb[0]), bf(mb[1]), bf(mb[2]), bf(mb[3]));
+    mo[1] = make_float4(bf(mb[4]), bf(mb[5]), bf(mb[6]), bf(mb[7]));
+  }
+}
+
+// One message-passing layer.  A block walks chunks of 128 cells; warp k owns tile k
+// (16 cells) of the chunk.  The aggregation m = Ahat h writes the [h; m] rows (64 BF16)
+// into the warp's shared tile -- four lanes per cell, eight channels per lane -- from
+// the staged rows (staged chunks) or straight from global memory (other chunks).  Then
+// 4 k-steps x 4 n-blocks of mma.sync give the 16 x 32 pre-activation; the epilogue adds
+// the bias, applies the ReLU and the skip connection, puts h' back into the tile, and
+// the tile leaves in 16-byte stores (16 consecutive cells = 1 KB contiguous).  Rows of
+// the tile and of W_l are padded to 72 elements so that the fragment loads of the 8 row
+// groups fall in distinct banks.  Dynamic shared memory: kStageRows x 64 B of staged
+// activations + the chunk's values (<= 4 slices x 8 slots x 32 floats).
+constexpr int kStageBytes = kStageRows * C * 2 + 4 * 8 * 32 * 4;
+
+__global__ void __launch_bounds__(kTPB, 3)
     k_lp_layer(SellView s, int n, const float *__restrict__ aval,
                const __nv_bfloat16 *__restrict__ hin, __nv_bfloat16 *__restrict__ hout,
                const __nv_bfloat16 *__restrict__ wl, const float *__restrict__ bl,
-               float *__restrict__ mout, float *__restrict__ zout, const int *done) {
+               float *__restrict__ mout, float *__restrict__ zout, const int *done,
+               const ChunkDesc *__restrict__ desc) {
   if (stopped(done)) return;
   constexpr int TS = lp::kTileStride;
   __shared__ __align__(16) __nv_bfloat16 wsm[C * TS];
   __shared__ float bsm[C];
   __shared__ __align__(16) __nv_bfloat16 tile[kTPB / 32][16 * TS];
+  __shared__ ChunkDesc dsm;
+  extern __shared__ __align__(16) unsigned char stage_raw[];
+  __nv_bfloat16 *sh = reinterpret_cast<__nv_bfloat16 *>(stage_raw);
+  float *sv = reinterpret_cast<float *>(stage_raw + kStageRows * C * 2);
   for (int t = threadIdx.x; t < C * 2 * C; t += blockDim.x)
     wsm[(t / (2 * C)) * TS + t % (2 * C)] = wl[t];
   if (threadIdx.x < C) bsm[threadIdx.x] = bl[threadIdx.x];
@@ -261,62 +380,86 @@ __global__ void __launch_bounds__(kTPB, 4)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g = lane >> 2, tg = lane & 3, qc = 8 * (lane & 3);
   __nv_bfloat16 *tw = tile[warp];
-  const int ntiles = (n + 15) / 16;
-  const int nwarps = (int)(((long long)gridDim.x * blockDim.x) >> 5);
-  for (int tt = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5); tt < ntiles;
-       tt += nwarps) {
-#pragma unroll 1
-    for (int rd = 0; rd < 2; ++rd) {
-      const int rloc = rd * 8 + (lane >> 2);
-      const int r = tt * 16 + rloc;
-      float acc[8];
-#pragma unroll
-      for (int c = 0; c < 8; ++c) acc[c] = 0.f;
-      uint4 own = make_uint4(0, 0, 0, 0);
-      if (r < n) {
-        const int slice = r >> 5, ln = r & 31;
-        const long long base = __ldg(&s.ptr[slice]) + ln;
-        const int w = __ldg(&s.width[slice]), op = __ldg(&s.offp[slice]);
-        const __nv_bfloat16 *hq = hin + qc;
-        if (__ldg(&s.kind[slice]) == 0 && w <= 8) {
-#pragma unroll
-          for (int j0 = 0; j0 < 8; j0 += 4) {
-            float v[4];
-            uint4 hv[4];
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-              if (j0 + j < w) {
-                int col = r + __ldg(&s.off[op + j0 + j]);
-                col = col < 0 ? 0 : (col >= n ? n - 1 : col);
-                v[j] = __ldg(&aval[base + (long long)(j0 + j) * 32]);
-                hv[j] = __ldg(reinterpret_cast<const uint4 *>(hq + (long long)col * C));
-              }
-            }
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-              if (j0 + j < w) fma8(acc, v[j], hv[j]);
+  const int nchunks = (n + kChunkRows - 1) / kChunkRows;
+  for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+    if (threadIdx.x < (int)(sizeof(ChunkDesc) / 4))
+      reinterpret_cast<int *>(&dsm)[threadIdx.x] =
+          __ldg(reinterpret_cast<const int *>(desc + ch) + threadIdx.x);
+    __syncthreads();
+    const long long r0 = (long long)ch * kChunkRows;
+    const int tt = ch * 8 + warp;  // this warp's tile
+    if (dsm.fast) {
+      // stage the windows (zero rows outside the mesh) and the chunk's values
+      const int w = dsm.w;
+      int units = 0;
+      for (int k = 0; k < dsm.nwin; ++k) units += dsm.win_len[k] * 4;
+      const int nval4 = w * 32;  // 4 slices x w slots x 32 rows / 4 floats per copy
+      for (int u = threadIdx.x; u < units + nval4; u += blockDim.x) {
+        if (u < units) {
+          int k = 0, uu = u;
+          while (uu >= dsm.win_len[k] * 4) {
+            uu -= dsm.win_len[k] * 4;
+            ++k;
           }
+          const int row = uu >> 2, part = uu & 3;
+          const long long grow = r0 + dsm.win_first[k] + row;
+          __nv_bfloat16 *dst = sh + (long long)(dsm.win_smem[k] + row) * C + 8 * part;
+          if (grow >= 0 && grow < n)
+            cp_async16(dst, hin + grow * C + 8 * part);
+          else
+            *reinterpret_cast<uint4 *>(dst) = make_uint4(0, 0, 0, 0);
         } else {
+          const int v = u - units;
+          cp_async16(sv + 4 * v, aval + __ldg(&s.ptr[ch * 4]) + 4 * v);
+        }
+      }
+      asm volatile("cp.async.commit_group;\n" ::);
+      asm volatile("cp.async.wait_group 0;\n" ::);
+      __syncthreads();
+#pragma unroll 1
+      for (int rd = 0; rd < 2; ++rd) {
+        const int i = warp * 16 + rd * 8 + (lane >> 2);  // row inside the chunk
+        const int sl = i >> 5, ln = i & 31;
+        float acc[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) acc[c] = 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          if (j < w) {
+            const float v = sv[sl * 32 * w + j * 32 + ln];
+            const uint4 hq =
+                *reinterpret_cast<const uint4 *>(sh + (long long)(dsm.soff[j] + i) * C + qc);
+            fma8(acc, v, hq);
+          }
+        }
+        const uint4 own =
+            *reinterpret_cast<const uint4 *>(sh + (long long)(dsm.soff[dsm.j0] + i) * C + qc);
+        put_row(tw, rd * 8 + (lane >> 2), qc, own, acc, mout, (int)(r0 + i), n);
+      }
+    } else {
+#pragma unroll 1
+      for (int rd = 0; rd < 2; ++rd) {
+        const int rloc = rd * 8 + (lane >> 2);
+        const int r = tt * 16 + rloc;
+        float acc[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) acc[c] = 0.f;
+        uint4 own = make_uint4(0, 0, 0, 0);
+        if (r < n) {
+          const int slice = r >> 5, ln = r & 31;
+          const long long base = __ldg(&s.ptr[slice]) + ln;
+          const int w = __ldg(&s.width[slice]), op = __ldg(&s.offp[slice]);
           const bool uni = __ldg(&s.kind[slice]) == 0;
+          const __nv_bfloat16 *hq = hin + qc;
           for (int j = 0; j < w; ++j) {
             int col = uni ? r + __ldg(&s.off[op + j]) : __ldg(&s.off[op + 32 * j + ln]);
             col = col < 0 ? 0 : (col >= n ? n - 1 : col);
             fma8(acc, __ldg(&aval[base + (long long)j * 32]),
                  __ldg(reinterpret_cast<const uint4 *>(hq + (long long)col * C)));
           }
+          own = __ldg(reinterpret_cast<const uint4 *>(hq + (long long)r * C));
         }
-        own = __ldg(reinterpret_cast<const uint4 *>(hq + (long long)r * C));
-      }
-      __nv_bfloat16 *row = tw + rloc * TS;
-      *reinterpret_cast<uint4 *>(row + qc) = own;
-      __align__(16) __nv_bfloat16 mb[8];
-#pragma unroll
-      for (int c = 0; c < 8; ++c) mb[c] = __float2bfloat16(acc[c]);
-      *reinterpret_cast<uint4 *>(row + C + qc) = *reinterpret_cast<const uint4 *>(mb);
-      if (mout && r < n) {
-        float4 *mo = reinterpret_cast<float4 *>(mout + (long long)r * C + qc);
-        mo[0] = make_float4(bf(mb[0]), bf(mb[1]), bf(mb[2]), bf(mb[3]));
-        mo[1] = make_float4(bf(mb[4]), bf(mb[5]), bf(mb[6]), bf(mb[7]));
+        put_row(tw, rloc, qc, own, acc, mout, r, n);
       }
     }
     __syncwarp();
@@ -369,7 +512,7 @@ __global__ void __launch_bounds__(kTPB, 4)
         *reinterpret_cast<uint4 *>(hout + (long long)cell * C + 8 * part) =
             *reinterpret_cast<const uint4 *>(tw + rr * TS + 8 * part);
     }
-    __syncwarp();
+    __syncthreads();  // the stage and the descriptor are reused by the next chunk
   }
 }
 
@@ -1008,6 +1151,11 @@ int compute_features(fcg_learned *Lp, fcg_context *c) {
                                          red + lp::kMaxDir * kMaxBlocks);
   k_lp_features<<<grid_for(c->n, c->num_sms), kTPB, 0, c->stream>>>(
       c->mv, scale64(c), red + lp::kMaxDir * kMaxBlocks, Lp->feat.as<float>());
+  const int nchunks = (c->n + kChunkRows - 1) / kChunkRows;
+  LP_TRY(Lp, Lp->chunks.ensure(sizeof(ChunkDesc) * nchunks));
+  k_lp_chunks<<<grid_for(nchunks, c->num_sms), kTPB, 0, c->stream>>>(c->sv, c->n,
+                                                                    Lp->chunks.as<ChunkDesc>(),
+                                                                    nchunks);
   LP_TRY(Lp, cudaGetLastError());
   Lp->fuid = c->uid;
   Lp->fgen = c->bind_gen;
@@ -1035,11 +1183,11 @@ void enqueue_forward(fcg_learned *Lp, fcg_context *c, cudaStream_t st, const flo
   for (int l = 0; l < lp::L; ++l) {
     const __nv_bfloat16 *hin = train ? H + l * hs : H + (l % 2) * hs;
     __nv_bfloat16 *hout = train ? H + (l + 1) * hs : H + ((l + 1) % 2) * hs;
-    k_lp_layer<<<lg, kTPB, 0, st>>>(c->sv, n, aval, hin, hout,
-                                    wbf + (size_t)l * 2 * lp::C * lp::C,
-                                    prm + lp::oLayer0 + l * lp::kLayerParams + 2 * lp::C * lp::C,
-                                    train ? Lp->mbuf.as<float>() + l * hs : nullptr,
-                                    train ? Lp->zbuf.as<float>() + (l + 1) * hs : nullptr, done);
+    k_lp_layer<<<lg, kTPB, kStageBytes, st>>>(
+        c->sv, n, aval, hin, hout, wbf + (size_t)l * 2 * lp::C * lp::C,
+        prm + lp::oLayer0 + l * lp::kLayerParams + 2 * lp::C * lp::C,
+        train ? Lp->mbuf.as<float>() + l * hs : nullptr,
+        train ? Lp->zbuf.as<float>() + (l + 1) * hs : nullptr, done, Lp->chunks.as<ChunkDesc>());
   }
 }
 
@@ -1162,6 +1310,9 @@ extern "C" int fcg_lp_create(int device, unsigned long long seed, fcg_learned **
       cudaMemset(Lp->adam_m.p, 0, pb) || cudaMemset(Lp->adam_v.p, 0, pb) ||
       cudaMemset(Lp->scal.p, 0, sizeof(float) * 64) || cudaMemset(Lp->S, 0, sizeof(lp::LScal)))
     return fail(FCG_ERR_CUDA);
+  if (cudaFuncSetAttribute(k_lp_layer, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kStageBytes) != cudaSuccess)
+    return fail(FCG_ERR_CUDA);
   k_lp_to_bf16<<<64, kTPB>>>(Lp->params.as<float>(), Lp->wbf.as<__nv_bfloat16>());
   if (cudaDeviceSynchronize() != cudaSuccess) return fail(FCG_ERR_CUDA);
   *out = Lp;
@@ -1182,7 +1333,8 @@ extern "C" int fcg_lp_destroy(fcg_learned *Lp) {
   if (Lp->hS) cudaFreeHost(Lp->hS);
   DBuf *bufs[] = {&Lp->params, &Lp->adam_m, &Lp->adam_v, &Lp->grad, &Lp->wbf, &Lp->feat,
                   &Lp->hbuf,   &Lp->mbuf,   &Lp->zbuf,   &Lp->dh,   &Lp->dh2, &Lp->dm,
-                  &Lp->y,      &Lp->dvec,   &Lp->part,   &Lp->red,  &Lp->scal, &Lp->fvec};
+                  &Lp->y,      &Lp->dvec,   &Lp->part,   &Lp->red,  &Lp->scal, &Lp->fvec,
+                  &Lp->chunks};
   for (DBuf *b : bufs) b->release();
   delete Lp;
   return FCG_OK;
@@ -1315,6 +1467,66 @@ extern "C" int fcg_lp_apply(fcg_learned *Lp, fcg_context *c, const float *r, flo
   return mark_done(Lp, c);
 }
 
+// Diagnostics: mean milliseconds of each kernel of one forward pass on r (host or
+// device), CUDA events around every launch: 0 k_lp_rms, 1 k_lp_embed, 2..7 k_lp_layer
+// (layers 1..6), 8 k_lp_out.
+extern "C" int fcg_lp_profile(fcg_learned *Lp, fcg_context *c, const float *r, int reps,
+                              double *ms, int max_units, int *units) {
+  int rc = check_ctx(Lp, c);
+  if (rc) return rc;
+  if (!r || reps < 1 || !ms) return lp_fail(Lp, FCG_ERR_ARG, "NULL r/ms or reps < 1");
+  if ((rc = matrix_ready(Lp, c)) || (rc = ensure_workspace(Lp, c, false))) return rc;
+  float *dr;
+  bool hr;
+  if ((rc = stage_f32(Lp, c, r, 4, true, &dr, &hr))) return rc;
+  constexpr int U = 3 + lp::L;
+  cudaEvent_t ev[U + 1];
+  for (auto &e : ev) LP_TRY(Lp, cudaEventCreate(&e));
+  double acc[U] = {0};
+  const int n = c->n;
+  cudaStream_t st = c->stream;
+  const size_t hs = (size_t)n * lp::C;
+  __nv_bfloat16 *H = Lp->hbuf.as<__nv_bfloat16>();
+  float *rms = Lp->scal.as<float>();
+  const float *prm = Lp->params.as<float>();
+  const int ntiles = (n + 15) / 16;
+  const int lg = std::max(1, std::min((ntiles + 7) / 8, c->num_sms * 4));
+  for (int it = 0; it <= reps; ++it) {  // the first pass warms up
+    LP_TRY(Lp, cudaEventRecord(ev[0], st));
+    k_lp_rms<<<reduction_grid(c), kTPB, 0, st>>>(n, dr, Lp->red.as<double>(),
+                                                 Lp->scal.as<unsigned>() + 17, rms, nullptr);
+    LP_TRY(Lp, cudaEventRecord(ev[1], st));
+    k_lp_embed<<<grid_for(4LL * n, c->num_sms, 4), kTPB, 0, st>>>(n, dr, rms, Lp->feat.as<float>(),
+                                                                 prm, H, nullptr, nullptr);
+    LP_TRY(Lp, cudaEventRecord(ev[2], st));
+    for (int l = 0; l < lp::L; ++l) {
+      k_lp_layer<<<lg, kTPB, kStageBytes, st>>>(
+          c->sv, n, scaled32(c), H + (l % 2) * hs, H + ((l + 1) % 2) * hs,
+          Lp->wbf.as<__nv_bfloat16>() + (size_t)l * 2 * lp::C * lp::C,
+          prm + lp::oLayer0 + l * lp::kLayerParams + 2 * lp::C * lp::C, nullptr, nullptr, nullptr,
+          Lp->chunks.as<ChunkDesc>());
+      LP_TRY(Lp, cudaEventRecord(ev[3 + l], st));
+    }
+    k_lp_out<<<grid_for(n, c->num_sms), kTPB, 0, st>>>(n, H + (lp::L % 2) * hs, prm, rms, dr,
+                                                       nullptr, Lp->y.as<float>(), nullptr,
+                                                       nullptr);
+    LP_TRY(Lp, cudaEventRecord(ev[U], st));
+    LP_TRY(Lp, cudaGetLastError());
+    LP_TRY(Lp, cudaEventSynchronize(ev[U]));
+    if (it == 0) continue;
+    for (int u = 0; u < U; ++u) {
+      float t = 0.f;
+      LP_TRY(Lp, cudaEventElapsedTime(&t, ev[u], ev[u + 1]));
+      acc[u] += t;
+    }
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  const int nu = std::min(U, max_units);
+  for (int u = 0; u < nu; ++u) ms[u] = acc[u] / reps;
+  if (units) *units = U;
+  return mark_done(Lp, c);
+}
+
 // loss = ||N(r) - e||^2 / ||e||^2 and its gradient with respect to the FP32 weights.
 extern "C" int fcg_lp_loss_grad(fcg_learned *Lp, fcg_context *c, const float *r, const float *e,
                                 float *loss, float *grad) {
@@ -1362,6 +1574,15 @@ extern "C" int fcg_lp_train_step(fcg_learned *Lp, fcg_context *c, const float *r
 extern "C" int fcg_lp_set_loss(fcg_learned *Lp, int kind) {
   if (!Lp || kind < 0 || kind > 1) return FCG_ERR_ARG;
   Lp->loss_kind = kind;
+  return FCG_OK;
+}
+
+// Iterations and FP64 residual replacements of the last fcg_fcg_learned call (the
+// reliable-update branch of the CUDA graph runs two kernels per replacement).
+extern "C" int fcg_lp_last_solve_stats(const fcg_learned *Lp, int *iters, int *updates) {
+  if (!Lp || !Lp->hS) return FCG_ERR_ARG;
+  if (iters) *iters = Lp->hS->iter;
+  if (updates) *updates = Lp->hS->nupdates;
   return FCG_OK;
 }
 

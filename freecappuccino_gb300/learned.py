@@ -124,6 +124,25 @@ class LearnedPreconditioner:
                                                C.byref(loss)), "fcg_lp_train_step")
         return float(loss.value)
 
+    def last_solve_stats(self) -> dict:
+        """FCG iterations and FP64 residual replacements of the last solve."""
+        it, up = C.c_int(), C.c_int()
+        self._check(self.lib.fcg_lp_last_solve_stats(self.h, C.byref(it), C.byref(up)),
+                    "fcg_lp_last_solve_stats")
+        return {"iters": it.value, "updates": up.value}
+
+    def profile(self, ctx: Context, r, reps: int = 10) -> dict:
+        """Mean milliseconds of each kernel of one forward pass on r."""
+        r = _f32(r)
+        ctx._follow(r)
+        ms = (C.c_double * 16)()
+        nu = C.c_int()
+        self._check(self.lib.fcg_lp_profile(self.h, ctx.h, _ptr(r), int(reps), ms, 16,
+                                            C.byref(nu)), "fcg_lp_profile")
+        names = ["k_lp_rms", "k_lp_embed"] + [f"k_lp_layer#{l + 1}" for l in range(LAYERS)]
+        names.append("k_lp_out")
+        return {names[i]: ms[i] for i in range(nu.value)}
+
     def set_loss(self, kind: str = "residual"):
         """Training loss: "residual" (|Ahat N(r) - r|^2 / |r|^2, the default) or "energy"
         ((N(r)-e).Ahat(N(r)-e) / e.Ahat e)."""

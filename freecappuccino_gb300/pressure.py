@@ -178,6 +178,25 @@ class Context:
         return su, fm
 
     # -- a5-a8 ----------------------------------------------------------------------
+    def flux_correct(self, a, pp, flmass):
+        """calcp :159-171: flmass += a(slot_PN) * (pp(N) - pp(P)); returns flmass."""
+        self._follow(a, pp, flmass)
+        a, pp = _host(a), _host(pp)
+        flmass = flmass.clone() if _is_torch(flmass) else np.array(flmass, dtype=np.float64)
+        self._check(self.lib.fcg_flux_correct(self.h, _ptr(a), _ptr(pp), _ptr(flmass)),
+                    "fcg_flux_correct")
+        return flmass
+
+    def correct_fields(self, dPdxi, apu, apv, apw, pp, urf, pRefCell, u, v, w, p):
+        """calcp :147,184-189: corrected (u, v, w, p); pRefCell is 1-based."""
+        self._follow(dPdxi, apu, apv, apw, pp, u, v, w, p)
+        ins = [_host(x) for x in (dPdxi, apu, apv, apw, pp)]
+        outs = [x.clone() if _is_torch(x) else np.array(x, dtype=np.float64) for x in (u, v, w, p)]
+        self._check(self.lib.fcg_correct_fields(self.h, *[_ptr(x) for x in ins], float(urf),
+                                                int(pRefCell), *[_ptr(x) for x in outs]),
+                    "fcg_correct_fields")
+        return tuple(outs)
+
     def grad(self, phi, option: str = "gauss", nigrad: int = 1, dphidxi=None):
         """grad(phi,dPhidxi[,option]) without limiter: returns dPhidxi as (n, 3)."""
         self._follow(phi, dphidxi)

@@ -133,6 +133,19 @@ int fcg_facefluxmass(fcg_context *ctx, const fcg_flow_fields *f, double *a, doub
 int fcg_fluxmc(fcg_context *ctx, const double *dPdxi, const double *apu, const double *den,
                double *su, double *flmass);
 
+/* Mass-flux correction by the pressure correction, calcp-multiple_correction_SIMPLE.f90:
+ * 159-171: flmass(f) += a(icell_jcell_csr_value_index(f)) * (pp(N) - pp(P)) over the
+ * inner faces.  a[nnz], pp[numTotal], flmass[numInnerFaces] in/out. */
+int fcg_flux_correct(fcg_context *ctx, const double *a, const double *pp, double *flmass);
+
+/* Velocity and pressure correction, calcp-multiple_correction_SIMPLE.f90:147,184-189:
+ * ppref = pp(pRefCell) (1-based); u -= dPdxi(1,:)*vol*apu, v -= dPdxi(2,:)*vol*apv,
+ * w -= dPdxi(3,:)*vol*apw, p += urf*(pp - ppref) over the cells.  u, v, w, p, pp of
+ * numTotal length (only the cell part is written), dPdxi(3,numCells), ap*[numCells]. */
+int fcg_correct_fields(fcg_context *ctx, const double *dPdxi, const double *apu,
+                       const double *apv, const double *apw, const double *pp, double urf,
+                       int pRefCell, double *u, double *v, double *w, double *p);
+
 /* ---------------------------------------------------------------------------
  * Gradients and boundary values.
  * ------------------------------------------------------------------------- */
@@ -337,6 +350,14 @@ int fcg_lp_train_step(fcg_learned *lp, fcg_context *ctx, const float *r, const f
  * stall_window iterations (default 400). */
 int fcg_lp_set_fcg_options(fcg_learned *lp, int directions, int ru_every, int stall_window,
                            double stall_factor);
+
+/* FCG iterations and FP64 residual replacements of the last fcg_fcg_learned call. */
+int fcg_lp_last_solve_stats(const fcg_learned *lp, int *iters, int *updates);
+/* Diagnostics: mean milliseconds of each kernel of one forward pass on r, over `reps`
+ * passes timed with CUDA events per launch: unit 0 rms, 1 embedding, 2..7 the six
+ * message-passing layers, 8 output (*units receives 9). */
+int fcg_lp_profile(fcg_learned *lp, fcg_context *ctx, const float *r, int reps, double *ms,
+                   int max_units, int *units);
 
 /* Truncated flexible CG (Notay, SIAM J. Sci. Comput. 22 (2000) 1444) preconditioned by
  * the network, on

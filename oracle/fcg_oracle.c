@@ -818,3 +818,30 @@ int orc_bicgstab(int n, const int *ioffset, const int *ja, const int *diag, cons
   free(reso), free(pk), free(uk), free(zk), free(vk), free(d);
   return 0;
 }
+
+/* --- calcp corrections after the p' solve --------------------------------------------- */
+/* calcp-multiple_correction_SIMPLE.f90:159-171: flmass(i) = flmass(i) + a(k)*(pp(ijn)-pp(ijp)),
+ * k = icell_jcell_csr_value_index(i). */
+int orc_flux_correct(const orc_mesh *m, const int *slot_pn, const double *a, const double *pp,
+                     double *flmass) {
+  for (int i = 0; i < m->numInnerFaces; ++i) {
+    const int ijp = m->owner[i] - 1, ijn = m->neighbour[i] - 1;
+    flmass[i] = flmass[i] + a[slot_pn[i] - 1] * (pp[ijn] - pp[ijp]);
+  }
+  return 0;
+}
+
+/* calcp-multiple_correction_SIMPLE.f90:184-189: velocity and pressure correction,
+ * ppref = pp(pRefCell) (:147). */
+int orc_correct_fields(const orc_mesh *m, const double *dPdxi, const double *apu,
+                       const double *apv, const double *apw, const double *pp, double urf,
+                       int pRefCell, double *u, double *v, double *w, double *p) {
+  const double ppref = pp[pRefCell - 1];
+  for (int inp = 0; inp < m->numCells; ++inp) {
+    u[inp] = u[inp] - dPdxi[3 * inp] * m->vol[inp] * apu[inp];
+    v[inp] = v[inp] - dPdxi[3 * inp + 1] * m->vol[inp] * apv[inp];
+    w[inp] = w[inp] - dPdxi[3 * inp + 2] * m->vol[inp] * apw[inp];
+    p[inp] = p[inp] + urf * (pp[inp] - ppref);
+  }
+  return 0;
+}

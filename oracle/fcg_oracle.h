@@ -88,6 +88,13 @@ int orc_grad_lsq(const orc_mesh *m, const double *phi, const double *dmat, doubl
 /* --- a8: bpres.f90:3-152 --- */
 int orc_bpres(const orc_mesh *m, double *p /*[numTotal]*/, const double *dPdxi, int istage);
 
+/* --- calcp corrections: calcp-multiple_correction_SIMPLE.f90:159-171 and :184-189 --- */
+int orc_flux_correct(const orc_mesh *m, const int *slot_pn, const double *a, const double *pp,
+                     double *flmass);
+int orc_correct_fields(const orc_mesh *m, const double *dPdxi, const double *apu,
+                       const double *apv, const double *apw, const double *pp, double urf,
+                       int pRefCell, double *u, double *v, double *w, double *p);
+
 /* --- a9-a11: dpcg.f90, iccg.f90, bicgstab.f90 --- */
 typedef struct orc_solver_opts {
   double resmax;   /* sor(ifi) */

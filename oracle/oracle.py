@@ -202,6 +202,23 @@ def fluxmc(m: Mesh, dPdxi, apu, den, flmass):
     return su, flmass
 
 
+def flux_correct(m: Mesh, csr: CSR, a, pp, flmass):
+    """calcp-multiple_correction_SIMPLE.f90:159-171 (mass-flux correction by p')."""
+    flmass = _f64(flmass).copy()
+    assert lib().orc_flux_correct(C.byref(m.struct), _i(_i32(csr.slot_pn)), _d(_f64(a)),
+                                  _d(_f64(pp)), _d(flmass)) == 0
+    return flmass
+
+
+def correct_fields(m: Mesh, dPdxi, apu, apv, apw, pp, urf, pRefCell, u, v, w, p):
+    """calcp-multiple_correction_SIMPLE.f90:184-189 (velocity and pressure correction)."""
+    u, v, w, p = (_f64(x).copy() for x in (u, v, w, p))
+    assert lib().orc_correct_fields(C.byref(m.struct), _d(_f64(dPdxi)), _d(_f64(apu)),
+                                    _d(_f64(apv)), _d(_f64(apw)), _d(_f64(pp)), C.c_double(urf),
+                                    int(pRefCell), _d(u), _d(v), _d(w), _d(p)) == 0
+    return u, v, w, p
+
+
 def grad_gauss(m: Mesh, phi, nigrad=1, corrected=False, dphidxi_in=None):
     """grad_gauss.f90 (nigrad passes) or grad_gauss_corrected.f90 (one pass, old = incoming)."""
     phi = _f64(phi)
