@@ -97,7 +97,6 @@ struct fcg_learned {
   size_t ncap = 0;
   bool train_cap = false;
   DBuf feat, hbuf, mbuf, zbuf, dh, dh2, dm, y, dvec, part, red, scal;
-  DBuf chunks;  // per-128-row chunk descriptors of the layer kernel (pattern of the mesh)
   // which context, mesh and matrix the features belong to
   unsigned long long fuid = 0;
   unsigned fgen = 0;
@@ -148,7 +147,7 @@ __global__ void k_lp_features(MeshView m, const double *__restrict__ s64,
   const double vmean = vsum[0] / m.n;
   FCG_GRID_STRIDE(i, m.n) {
     const double v = m.vol[i], d = 1.0 / (s64[i] * s64[i]);
-    const double h = cbrt(v);
+    const double h = (double)cbrtf((float)v);  // the features are FP32
     double ax = 0.0, ay = 0.0, az = 0.0;
     for (int e = m.cf_ptr[i]; e < m.cf_ptr[i + 1]; ++e) {
       const int ent = m.cf_ent[e], f = (ent > 0 ? ent : -ent) - 1;
@@ -163,13 +162,13 @@ __global__ void k_lp_features(MeshView m, const double *__restrict__ s64,
       az += fabs(m.arz[f]);
     }
     const double a2 = 2.0 * h * h;
-    float *o = feat + i * F;
-    o[0] = 0.f;
-    o[1] = (float)(log(d / h) - log(6.0));
-    o[2] = (float)log(v / vmean);
-    o[3] = (float)(ax / a2 - 1.0);
-    o[4] = (float)(ay / a2 - 1.0);
-    o[5] = (float)(az / a2 - 1.0);
+    const long long nn = m.n;  // feature-major: feature k of cell i at k * n + i
+    feat[i] = 0.f;
+    feat[nn + i] = logf((float)(d / h)) - 1.7917595f;  // log 6
+    feat[2 * nn + i] = logf((float)(v / vmean));
+    feat[3 * nn + i] = (float)(ax / a2 - 1.0);
+    feat[4 * nn + i] = (float)(ay / a2 - 1.0);
+    feat[5 * nn + i] = (float)(az / a2 - 1.0);
   }
 }
 
@@ -188,8 +187,9 @@ __global__ void __launch_bounds__(kTPB, 8)
     out[0] = v[0] > 0 ? (float)sqrt(v[0] / n) : 1.0f;
 }
 
-// f[i][0] = r[i] / rms; h0 = relu(W_in f + b_in) in BF16; z0 (pre-activation) when
-// training.  Four threads per cell, eight output channels each (one 16-byte store).
+// f0 = r / rms (stored as feature 0); h0 = relu(W_in f + b_in) in BF16; z0
+// (pre-activation) when training.  Features are feature-major (k * n + i).  Four threads
+// per cell, eight output channels each (one 16-byte store).
 __global__ void __launch_bounds__(kTPB)
     k_lp_embed(int n, const float *__restrict__ r, const float *__restrict__ rms,
                float *__restrict__ feat, const float *__restrict__ prm,
@@ -204,9 +204,9 @@ __global__ void __launch_bounds__(kTPB)
     const int o0 = (int)(t & 3) * 8;
     float f[F];
     f[0] = r[i] * inv;
-    if (o0 == 0) feat[i * F] = f[0];
+    if (o0 == 0) feat[i] = f[0];
 #pragma unroll
-    for (int k = 1; k < F; ++k) f[k] = feat[i * F + k];
+    for (int k = 1; k < F; ++k) f[k] = feat[k * (long long)n + i];
     __align__(16) __nv_bfloat16 hv[8];
 #pragma unroll
     for (int o = 0; o < 8; ++o) {
@@ -230,93 +230,6 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4],
 }
 
 
-// Chunks of the layer kernel: 128 rows = 4 slices = 8 tiles of 16 cells.  A chunk
-// whose four slices are uniform with the same <= 8 column offsets (one of them 0) and
-// lie inside the mesh takes the staged path: the rows r0 + off .. r0 + off + 127 of
-// every offset, merged into windows where offsets lie within kMergeGap of each other,
-// are copied into shared memory once (cp.async, 16 bytes per copy) together with the
-// chunk's matrix values, and all gathers then read shared memory.  Other chunks gather
-// from global memory row by row.
-constexpr int kChunkRows = 128;
-constexpr int kStageRows = 704;  // staged activation rows per chunk (44 KB of BF16)
-constexpr int kMergeGap = 32;
-
-struct ChunkDesc {
-  int fast, w, nwin, j0;            // staged path?, slots, windows, slot of offset 0
-  int win_first[8], win_len[8];     // window start (offset from r0) and length in rows
-  int win_smem[8];                  // first staged row of each window
-  int soff[8];                      // staged row of local row 0 for each slot
-};
-
-__global__ void k_lp_chunks(SellView s, int n, ChunkDesc *__restrict__ d, int nchunks) {
-  FCG_GRID_STRIDE(c, nchunks) {
-    ChunkDesc D;
-    memset(&D, 0, sizeof D);
-    const int s0 = (int)c * 4;
-    const long long r0 = c * kChunkRows;
-    bool ok = s0 + 3 < s.nslices && r0 + kChunkRows <= n;
-    int off[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    int w = 0;
-    if (ok) {
-      w = s.width[s0];
-      ok = w >= 1 && w <= 8;
-      for (int k = 0; ok && k < 4; ++k) {
-        ok = s.kind[s0 + k] == 0 && s.width[s0 + k] == w;
-        for (int j = 0; ok && j < w; ++j) {
-          const int o = s.off[s.offp[s0 + k] + j];
-          if (k == 0) off[j] = o;
-          else ok = off[j] == o;
-        }
-      }
-    }
-    int j0 = -1;
-    for (int j = 0; ok && j < w; ++j)
-      if (off[j] == 0) j0 = j;
-    ok = ok && j0 >= 0;
-    if (ok) {
-      int order[8];
-      for (int j = 0; j < w; ++j) order[j] = j;
-      for (int a = 1; a < w; ++a)  // insertion sort of the slots by offset
-        for (int b = a; b > 0 && off[order[b - 1]] > off[order[b]]; --b) {
-          const int t = order[b];
-          order[b] = order[b - 1];
-          order[b - 1] = t;
-        }
-      int nwin = 0, rows = 0, first = 0, last = 0;
-      for (int k = 0; k < w; ++k) {
-        const int o = off[order[k]];
-        if (k == 0 || o - last > kMergeGap) {
-          if (k > 0) {
-            D.win_first[nwin] = first;
-            D.win_len[nwin] = last - first + kChunkRows;
-            D.win_smem[nwin] = rows;
-            rows += D.win_len[nwin];
-            ++nwin;
-          }
-          first = o;
-        }
-        last = o;
-        D.soff[order[k]] = nwin;  // window index for now
-      }
-      D.win_first[nwin] = first;
-      D.win_len[nwin] = last - first + kChunkRows;
-      D.win_smem[nwin] = rows;
-      rows += D.win_len[nwin];
-      ++nwin;
-      for (int j = 0; j < w; ++j) {
-        const int k = D.soff[j];
-        D.soff[j] = D.win_smem[k] + (off[j] - D.win_first[k]);
-      }
-      D.nwin = nwin;
-      ok = rows <= kStageRows;
-    }
-    D.fast = ok ? 1 : 0;
-    D.w = w;
-    D.j0 = j0;
-    d[c] = D;
-  }
-}
-
 // acc[0..7] += v * (8 BF16 values packed in q)
 __device__ __forceinline__ void fma8(float (&acc)[8], float v, const uint4 &q) {
   const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(&q);
@@ -324,55 +237,29 @@ __device__ __forceinline__ void fma8(float (&acc)[8], float v, const uint4 &q) {
   for (int c = 0; c < 8; ++c) acc[c] += v * bf(e[c]);
 }
 
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem));
-}
-
-// Writes row `rloc` of the warp's [h; m] tile: own h (8 channels) and m = Ahat h.
-__device__ __forceinline__ void put_row(__nv_bfloat16 *tw, int rloc, int qc, const uint4 &own,
-                                        const float (&acc)[8], float *mout, int r, int n) {
-  constexpr int TS = lp::kTileStride;
-  __nv_bfloat16 *row = tw + rloc * TS;
-  *reinterpret_cast<uint4 *>(row + qc) = own;
-  __align__(16) __nv_bfloat16 mb[8];
-#pragma unroll
-  for (int c = 0; c < 8; ++c) mb[c] = __float2bfloat16(acc[c]);
-  *reinterpret_cast<uint4 *>(row + C + qc) = *reinterpret_cast<const uint4 *>(mb);
-  if (mout && r < n) {
-    float4 *mo = reinterpret_cast<float4 *>(mout + (long long)r * C + qc);
-    mo[0] = make_float4(bf(mb[0]), bf(mb[1]), bf(mb[2]), bf(mb[3]));
-    mo[1] = make_float4(bf(mb[4]), bf(mb[5]), bf(mb[6]), bf(mb[7]));
-  }
-}
-
-// One message-passing layer.  A block walks chunks of 128 cells; warp k owns tile k
-// (16 cells) of the chunk.  The aggregation m = Ahat h writes the [h; m] rows (64 BF16)
-// into the warp's shared tile -- four lanes per cell, eight channels per lane -- from
-// the staged rows (staged chunks) or straight from global memory (other chunks).  Then
-// 4 k-steps x 4 n-blocks of mma.sync give the 16 x 32 pre-activation; the epilogue adds
-// the bias, applies the ReLU and the skip connection, puts h' back into the tile, and
-// the tile leaves in 16-byte stores (16 consecutive cells = 1 KB contiguous).  Rows of
-// the tile and of W_l are padded to 72 elements so that the fragment loads of the 8 row
-// groups fall in distinct banks.  Dynamic shared memory: kStageRows x 64 B of staged
-// activations + the chunk's values (<= 4 slices x 8 slots x 32 floats).
-constexpr int kStageBytes = kStageRows * C * 2 + 4 * 8 * 32 * 4;
-
-__global__ void __launch_bounds__(kTPB, 3)
+// One message-passing layer.  Tiles are dealt to warps grid-stride, so all blocks work
+// on one narrow band of the mesh at a time and the rows at +-N^2 that a tile gathers were
+// loaded moments before by other blocks (L2 hits); a contiguous run of tiles per block
+// measured 14% slower at 256^3.  A warp owns 16 cells (one tile) at a time and takes them
+// in two rounds of 8: four lanes per cell, eight channels per lane, sum
+// m = Ahat h over the cell's sliced row -- for uniform slices the column offsets,
+// values and neighbour activations of four slots are loaded before any is used -- and
+// write the [h; m] row (64 BF16) into the warp's shared tile.  4 k-steps x 4 n-blocks of
+// mma.sync give the 16 x 32 pre-activation; the epilogue adds the bias, applies the ReLU
+// and the skip connection, puts h' back into the tile, and the tile leaves in 16-byte
+// stores (16 consecutive cells = 1 KB contiguous).  Rows of the tile and of W_l are
+// padded to 72 elements so that the fragment loads of the 8 row groups fall in distinct
+// banks.
+__global__ void __launch_bounds__(kTPB, 4)
     k_lp_layer(SellView s, int n, const float *__restrict__ aval,
                const __nv_bfloat16 *__restrict__ hin, __nv_bfloat16 *__restrict__ hout,
                const __nv_bfloat16 *__restrict__ wl, const float *__restrict__ bl,
-               float *__restrict__ mout, float *__restrict__ zout, const int *done,
-               const ChunkDesc *__restrict__ desc) {
+               float *__restrict__ mout, float *__restrict__ zout, const int *done) {
   if (stopped(done)) return;
   constexpr int TS = lp::kTileStride;
   __shared__ __align__(16) __nv_bfloat16 wsm[C * TS];
   __shared__ float bsm[C];
   __shared__ __align__(16) __nv_bfloat16 tile[kTPB / 32][16 * TS];
-  __shared__ ChunkDesc dsm;
-  extern __shared__ __align__(16) unsigned char stage_raw[];
-  __nv_bfloat16 *sh = reinterpret_cast<__nv_bfloat16 *>(stage_raw);
-  float *sv = reinterpret_cast<float *>(stage_raw + kStageRows * C * 2);
   for (int t = threadIdx.x; t < C * 2 * C; t += blockDim.x)
     wsm[(t / (2 * C)) * TS + t % (2 * C)] = wl[t];
   if (threadIdx.x < C) bsm[threadIdx.x] = bl[threadIdx.x];
@@ -380,86 +267,62 @@ __global__ void __launch_bounds__(kTPB, 3)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g = lane >> 2, tg = lane & 3, qc = 8 * (lane & 3);
   __nv_bfloat16 *tw = tile[warp];
-  const int nchunks = (n + kChunkRows - 1) / kChunkRows;
-  for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
-    if (threadIdx.x < (int)(sizeof(ChunkDesc) / 4))
-      reinterpret_cast<int *>(&dsm)[threadIdx.x] =
-          __ldg(reinterpret_cast<const int *>(desc + ch) + threadIdx.x);
-    __syncthreads();
-    const long long r0 = (long long)ch * kChunkRows;
-    const int tt = ch * 8 + warp;  // this warp's tile
-    if (dsm.fast) {
-      // stage the windows (zero rows outside the mesh) and the chunk's values
-      const int w = dsm.w;
-      int units = 0;
-      for (int k = 0; k < dsm.nwin; ++k) units += dsm.win_len[k] * 4;
-      const int nval4 = w * 32;  // 4 slices x w slots x 32 rows / 4 floats per copy
-      for (int u = threadIdx.x; u < units + nval4; u += blockDim.x) {
-        if (u < units) {
-          int k = 0, uu = u;
-          while (uu >= dsm.win_len[k] * 4) {
-            uu -= dsm.win_len[k] * 4;
-            ++k;
+  const int ntiles = (n + 15) / 16;
+  const int nwarps = (int)(((long long)gridDim.x * blockDim.x) >> 5);
+  for (int tt = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5); tt < ntiles;
+       tt += nwarps) {
+#pragma unroll 1
+    for (int rd = 0; rd < 2; ++rd) {
+      const int rloc = rd * 8 + (lane >> 2);
+      const int r = tt * 16 + rloc;
+      float acc[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) acc[c] = 0.f;
+      uint4 own = make_uint4(0, 0, 0, 0);
+      if (r < n) {
+        const int slice = r >> 5, ln = r & 31;
+        const long long base = __ldg(&s.ptr[slice]) + ln;
+        const int w = __ldg(&s.width[slice]), op = __ldg(&s.offp[slice]);
+        const __nv_bfloat16 *hq = hin + qc;
+        if (__ldg(&s.kind[slice]) == 0 && w <= 8) {
+#pragma unroll
+          for (int j0 = 0; j0 < 8; j0 += 4) {
+            float v[4];
+            uint4 hv[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              if (j0 + j < w) {
+                int col = r + __ldg(&s.off[op + j0 + j]);
+                col = col < 0 ? 0 : (col >= n ? n - 1 : col);
+                v[j] = __ldg(&aval[base + (long long)(j0 + j) * 32]);
+                hv[j] = __ldg(reinterpret_cast<const uint4 *>(hq + (long long)col * C));
+              }
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              if (j0 + j < w) fma8(acc, v[j], hv[j]);
           }
-          const int row = uu >> 2, part = uu & 3;
-          const long long grow = r0 + dsm.win_first[k] + row;
-          __nv_bfloat16 *dst = sh + (long long)(dsm.win_smem[k] + row) * C + 8 * part;
-          if (grow >= 0 && grow < n)
-            cp_async16(dst, hin + grow * C + 8 * part);
-          else
-            *reinterpret_cast<uint4 *>(dst) = make_uint4(0, 0, 0, 0);
         } else {
-          const int v = u - units;
-          cp_async16(sv + 4 * v, aval + __ldg(&s.ptr[ch * 4]) + 4 * v);
-        }
-      }
-      asm volatile("cp.async.commit_group;\n" ::);
-      asm volatile("cp.async.wait_group 0;\n" ::);
-      __syncthreads();
-#pragma unroll 1
-      for (int rd = 0; rd < 2; ++rd) {
-        const int i = warp * 16 + rd * 8 + (lane >> 2);  // row inside the chunk
-        const int sl = i >> 5, ln = i & 31;
-        float acc[8];
-#pragma unroll
-        for (int c = 0; c < 8; ++c) acc[c] = 0.f;
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          if (j < w) {
-            const float v = sv[sl * 32 * w + j * 32 + ln];
-            const uint4 hq =
-                *reinterpret_cast<const uint4 *>(sh + (long long)(dsm.soff[j] + i) * C + qc);
-            fma8(acc, v, hq);
-          }
-        }
-        const uint4 own =
-            *reinterpret_cast<const uint4 *>(sh + (long long)(dsm.soff[dsm.j0] + i) * C + qc);
-        put_row(tw, rd * 8 + (lane >> 2), qc, own, acc, mout, (int)(r0 + i), n);
-      }
-    } else {
-#pragma unroll 1
-      for (int rd = 0; rd < 2; ++rd) {
-        const int rloc = rd * 8 + (lane >> 2);
-        const int r = tt * 16 + rloc;
-        float acc[8];
-#pragma unroll
-        for (int c = 0; c < 8; ++c) acc[c] = 0.f;
-        uint4 own = make_uint4(0, 0, 0, 0);
-        if (r < n) {
-          const int slice = r >> 5, ln = r & 31;
-          const long long base = __ldg(&s.ptr[slice]) + ln;
-          const int w = __ldg(&s.width[slice]), op = __ldg(&s.offp[slice]);
           const bool uni = __ldg(&s.kind[slice]) == 0;
-          const __nv_bfloat16 *hq = hin + qc;
           for (int j = 0; j < w; ++j) {
             int col = uni ? r + __ldg(&s.off[op + j]) : __ldg(&s.off[op + 32 * j + ln]);
             col = col < 0 ? 0 : (col >= n ? n - 1 : col);
             fma8(acc, __ldg(&aval[base + (long long)j * 32]),
                  __ldg(reinterpret_cast<const uint4 *>(hq + (long long)col * C)));
           }
-          own = __ldg(reinterpret_cast<const uint4 *>(hq + (long long)r * C));
         }
-        put_row(tw, rloc, qc, own, acc, mout, r, n);
+        own = __ldg(reinterpret_cast<const uint4 *>(hq + (long long)r * C));
+      }
+      __nv_bfloat16 *row = tw + rloc * TS;
+      *reinterpret_cast<uint4 *>(row + qc) = own;
+      __align__(16) __nv_bfloat16 mb[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) mb[c] = __float2bfloat16(acc[c]);
+      *reinterpret_cast<uint4 *>(row + C + qc) = *reinterpret_cast<const uint4 *>(mb);
+      if (mout && r < n) {
+        float4 *mo = reinterpret_cast<float4 *>(mout + (long long)r * C + qc);
+        mo[0] = make_float4(bf(mb[0]), bf(mb[1]), bf(mb[2]), bf(mb[3]));
+        mo[1] = make_float4(bf(mb[4]), bf(mb[5]), bf(mb[6]), bf(mb[7]));
       }
     }
     __syncwarp();
@@ -512,7 +375,7 @@ __global__ void __launch_bounds__(kTPB, 3)
         *reinterpret_cast<uint4 *>(hout + (long long)cell * C + 8 * part) =
             *reinterpret_cast<const uint4 *>(tw + rr * TS + 8 * part);
     }
-    __syncthreads();  // the stage and the descriptor are reused by the next chunk
+    __syncwarp();
   }
 }
 
@@ -721,7 +584,7 @@ __global__ void __launch_bounds__(kTPB)
     const long long o = i * C + lane;
     const float dz = z0[o] > 0.f ? dh[o] : 0.f;
 #pragma unroll
-    for (int k = 0; k < F; ++k) g[k] += dz * feat[i * F + k];
+    for (int k = 0; k < F; ++k) g[k] += dz * feat[k * (long long)n + i];
     g[F] += dz;
   }
 #pragma unroll
@@ -1151,11 +1014,6 @@ int compute_features(fcg_learned *Lp, fcg_context *c) {
                                          red + lp::kMaxDir * kMaxBlocks);
   k_lp_features<<<grid_for(c->n, c->num_sms), kTPB, 0, c->stream>>>(
       c->mv, scale64(c), red + lp::kMaxDir * kMaxBlocks, Lp->feat.as<float>());
-  const int nchunks = (c->n + kChunkRows - 1) / kChunkRows;
-  LP_TRY(Lp, Lp->chunks.ensure(sizeof(ChunkDesc) * nchunks));
-  k_lp_chunks<<<grid_for(nchunks, c->num_sms), kTPB, 0, c->stream>>>(c->sv, c->n,
-                                                                    Lp->chunks.as<ChunkDesc>(),
-                                                                    nchunks);
   LP_TRY(Lp, cudaGetLastError());
   Lp->fuid = c->uid;
   Lp->fgen = c->bind_gen;
@@ -1183,11 +1041,11 @@ void enqueue_forward(fcg_learned *Lp, fcg_context *c, cudaStream_t st, const flo
   for (int l = 0; l < lp::L; ++l) {
     const __nv_bfloat16 *hin = train ? H + l * hs : H + (l % 2) * hs;
     __nv_bfloat16 *hout = train ? H + (l + 1) * hs : H + ((l + 1) % 2) * hs;
-    k_lp_layer<<<lg, kTPB, kStageBytes, st>>>(
-        c->sv, n, aval, hin, hout, wbf + (size_t)l * 2 * lp::C * lp::C,
-        prm + lp::oLayer0 + l * lp::kLayerParams + 2 * lp::C * lp::C,
-        train ? Lp->mbuf.as<float>() + l * hs : nullptr,
-        train ? Lp->zbuf.as<float>() + (l + 1) * hs : nullptr, done, Lp->chunks.as<ChunkDesc>());
+    k_lp_layer<<<lg, kTPB, 0, st>>>(c->sv, n, aval, hin, hout,
+                                    wbf + (size_t)l * 2 * lp::C * lp::C,
+                                    prm + lp::oLayer0 + l * lp::kLayerParams + 2 * lp::C * lp::C,
+                                    train ? Lp->mbuf.as<float>() + l * hs : nullptr,
+                                    train ? Lp->zbuf.as<float>() + (l + 1) * hs : nullptr, done);
   }
 }
 
@@ -1310,9 +1168,6 @@ extern "C" int fcg_lp_create(int device, unsigned long long seed, fcg_learned **
       cudaMemset(Lp->adam_m.p, 0, pb) || cudaMemset(Lp->adam_v.p, 0, pb) ||
       cudaMemset(Lp->scal.p, 0, sizeof(float) * 64) || cudaMemset(Lp->S, 0, sizeof(lp::LScal)))
     return fail(FCG_ERR_CUDA);
-  if (cudaFuncSetAttribute(k_lp_layer, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           kStageBytes) != cudaSuccess)
-    return fail(FCG_ERR_CUDA);
   k_lp_to_bf16<<<64, kTPB>>>(Lp->params.as<float>(), Lp->wbf.as<__nv_bfloat16>());
   if (cudaDeviceSynchronize() != cudaSuccess) return fail(FCG_ERR_CUDA);
   *out = Lp;
@@ -1333,8 +1188,7 @@ extern "C" int fcg_lp_destroy(fcg_learned *Lp) {
   if (Lp->hS) cudaFreeHost(Lp->hS);
   DBuf *bufs[] = {&Lp->params, &Lp->adam_m, &Lp->adam_v, &Lp->grad, &Lp->wbf, &Lp->feat,
                   &Lp->hbuf,   &Lp->mbuf,   &Lp->zbuf,   &Lp->dh,   &Lp->dh2, &Lp->dm,
-                  &Lp->y,      &Lp->dvec,   &Lp->part,   &Lp->red,  &Lp->scal, &Lp->fvec,
-                  &Lp->chunks};
+                  &Lp->y,      &Lp->dvec,   &Lp->part,   &Lp->red,  &Lp->scal, &Lp->fvec};
   for (DBuf *b : bufs) b->release();
   delete Lp;
   return FCG_OK;
@@ -1500,11 +1354,10 @@ extern "C" int fcg_lp_profile(fcg_learned *Lp, fcg_context *c, const float *r, i
                                                                  prm, H, nullptr, nullptr);
     LP_TRY(Lp, cudaEventRecord(ev[2], st));
     for (int l = 0; l < lp::L; ++l) {
-      k_lp_layer<<<lg, kTPB, kStageBytes, st>>>(
+      k_lp_layer<<<lg, kTPB, 0, st>>>(
           c->sv, n, scaled32(c), H + (l % 2) * hs, H + ((l + 1) % 2) * hs,
           Lp->wbf.as<__nv_bfloat16>() + (size_t)l * 2 * lp::C * lp::C,
-          prm + lp::oLayer0 + l * lp::kLayerParams + 2 * lp::C * lp::C, nullptr, nullptr, nullptr,
-          Lp->chunks.as<ChunkDesc>());
+          prm + lp::oLayer0 + l * lp::kLayerParams + 2 * lp::C * lp::C, nullptr, nullptr, nullptr);
       LP_TRY(Lp, cudaEventRecord(ev[3 + l], st));
     }
     k_lp_out<<<grid_for(n, c->num_sms), kTPB, 0, st>>>(n, H + (lp::L % 2) * hs, prm, rms, dr,

@@ -91,9 +91,10 @@ class LearnedPreconditioner:
         self._check(self.lib.fcg_lp_set_matrix(self.h, ctx.h, _ptr(_host(a))), "fcg_lp_set_matrix")
 
     def features(self, ctx: Context) -> np.ndarray:
-        out = np.zeros((ctx.n, FEATURES), np.float32)
+        """Per-cell inputs of the network as (numCells, FEATURES)."""
+        out = np.zeros((FEATURES, ctx.n), np.float32)
         self._check(self.lib.fcg_lp_features(self.h, ctx.h, _ptr(out)), "fcg_lp_features")
-        return out
+        return np.ascontiguousarray(out.T)
 
     def apply(self, ctx: Context, r):
         r = _f32(r)

@@ -323,8 +323,8 @@ int fcg_lp_save(fcg_learned *lp, const char *path);
 int fcg_lp_load(fcg_learned *lp, const char *path);
 /* Loads CSR values a[nnz] into the context, builds Ahat in FP32 and the features. */
 int fcg_lp_set_matrix(fcg_learned *lp, fcg_context *ctx, const double *a);
-/* Features of the last fcg_lp_set_matrix: out[numCells][FCG_LP_FEATURES] (column 0 is
- * the residual input of the last forward pass). */
+/* Features of the last fcg_lp_set_matrix, feature-major: out[FCG_LP_FEATURES][numCells]
+ * (feature 0 is the residual input of the last forward pass). */
 int fcg_lp_features(fcg_learned *lp, fcg_context *ctx, float *out);
 /* z = N(r). */
 int fcg_lp_apply(fcg_learned *lp, fcg_context *ctx, const float *r, float *z);
