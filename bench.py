@@ -361,7 +361,8 @@ def main():
     last = reports[-1]
     iters = last.iters
     if method != "learned":
-        per_solve = {"dpcg": lambda it: 3 + 3 * it, "dpcg_mixed": lambda it: 6 + 5 * it}
+        per_solve = {"dpcg": lambda it: 3 + 3 * it, "dpcg_mixed": lambda it: 6 + 5 * it,
+                     "iccg": lambda it: 4 + 5 * it, "bicgstab": lambda it: 4 + 8 * it}
         launches = sum(per_solve.get(method, lambda it: 3 + 3 * it)(r.iters) for r in reports)
     x_method = last.fi.clone()
     peak, peak_kind = peaks()

@@ -105,6 +105,7 @@ _PROTOS = {
     "fcg_batch_dpcg": (C.c_int, [_BATCH, _vp, _vp, _vp, C.c_double, C.c_int, _dp,
                                  C.POINTER(SolveReport)]),
     "fcg_batch_autotune": (C.c_int, [_BATCH, _vp, _vp, C.c_int, _dp]),
+    "fcg_batch_set_wait_test": (C.c_int, [_BATCH, C.c_longlong, C.c_int]),
     # learned preconditioner and flexible CG
     "fcg_lp_create": (C.c_int, [C.c_int, C.c_ulonglong, C.POINTER(_LP)]),
     "fcg_lp_destroy": (C.c_int, [_LP]),

@@ -188,9 +188,12 @@ __device__ __noinline__ void fin_update(BSys &S, BCtl *ctl, double resl, double 
 
 __global__ void __launch_bounds__(kTPB)
     k_batch_dpcg(BSys *sys, const BItem *__restrict__ items, int nitems, double *part,
-                 BCtl *ctl, int max_loops, long long spin_limit) {
+                 BCtl *ctl, int max_loops, long long spin_limit, int absent_block) {
   __shared__ double sh[2][kWarps];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // diagnostics only (fcg_batch_set_wait_test): one CTA never reaches a barrier, so the
+  // others' bounded waits run out and the solve ends with FCG_ERR_TIMEOUT
+  if ((int)blockIdx.x == absent_block) return;
   // initial residual res = su - A x, res0 = sum|res|, sk = sum res^2 / a_PP (dpcg.f90:51-90)
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const BItem I = items[it];
@@ -304,6 +307,8 @@ struct fcg_batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int graph_grid = 0, graph_loops = 0;
+  long long spin_limit = 1LL << 22;  // polls of 64 ns sleeps per barrier wait: over 0.25 s
+  int absent_block = -1;              // diagnostics: a CTA that skips the barriers
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
@@ -320,8 +325,6 @@ int bfail(fcg_batch *b, int status, const std::string &msg) {
     if (_e != cudaSuccess)                                                                \
       return bfail((b), FCG_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e)); \
   } while (0)
-
-constexpr long long kSpinLimit = 1LL << 22;  // polls of 64 ns sleeps: well over 0.25 s
 
 void drop_graph(fcg_batch *b) {
   if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -369,7 +372,8 @@ int enqueue(fcg_batch *b, cudaStream_t st, int grid, int max_loops) {
   cfg.numAttrs = 1;
   B_TRY(b, cudaLaunchKernelEx(&cfg, k_batch_dpcg, b->dsys.as<BSys>(),
                               (const BItem *)b->ditems.as<BItem>(), b->nitems,
-                              b->dpart.as<double>(), b->dctl.as<BCtl>(), max_loops, kSpinLimit));
+                              b->dpart.as<double>(), b->dctl.as<BCtl>(), max_loops,
+                              b->spin_limit, b->absent_block));
   return FCG_OK;
 }
 
@@ -541,6 +545,17 @@ extern "C" int fcg_batch_set_params(fcg_batch *b, int slices_per_item, int block
   b->blocks_per_sm = blocks_per_sm;
   B_TRY(b, cudaSetDevice(b->device));
   return build_items(b);
+}
+
+// Diagnostics for the timeout path: the poll limit of every grid-barrier wait and a CTA
+// (absent_block >= 0) that returns before the first barrier.  (polls, -1) restores
+// normal operation; polls <= 0 restores the default limit.
+extern "C" int fcg_batch_set_wait_test(fcg_batch *b, long long polls, int absent_block) {
+  if (!b || absent_block < -1) return FCG_ERR_ARG;
+  b->spin_limit = polls > 0 ? polls : (1LL << 22);
+  b->absent_block = absent_block;
+  drop_graph(b);
+  return FCG_OK;
 }
 
 extern "C" int fcg_batch_get_params(const fcg_batch *b, int *slices_per_item, int *blocks_per_sm,

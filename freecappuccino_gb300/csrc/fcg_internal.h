@@ -70,8 +70,9 @@ struct SellView {
 };
 
 struct Level {
-  std::vector<int> ptr;  // host: level offsets into rows
-  int *rows = nullptr;   // device: rows sorted by level, ascending inside a level
+  std::vector<int> ptr;        // host: level offsets into rows
+  int *rows = nullptr;         // device: rows sorted by level, ascending inside a level
+  const int *dptr = nullptr;   // device copy of ptr
   int count = 0;
 };
 

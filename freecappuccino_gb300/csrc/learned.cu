@@ -1032,7 +1032,7 @@ void enqueue_forward(fcg_learned *Lp, fcg_context *c, cudaStream_t st, const flo
   __nv_bfloat16 *H = Lp->hbuf.as<__nv_bfloat16>();
   const size_t hs = (size_t)n * lp::C;
   k_lp_rms<<<reduction_grid(c), kTPB, 0, st>>>(n, r, Lp->red.as<double>(), rms_ticket, rms, done);
-  k_lp_embed<<<grid_for(4LL * n, c->num_sms, 4), kTPB, 0, st>>>(
+  k_lp_embed<<<grid_for(4LL * n, c->num_sms, 16), kTPB, 0, st>>>(
       n, r, rms, Lp->feat.as<float>(), prm, H, train ? Lp->zbuf.as<float>() : nullptr, done);
   const float *aval = scaled32(c);
   const __nv_bfloat16 *wbf = Lp->wbf.as<__nv_bfloat16>();
@@ -1350,7 +1350,7 @@ extern "C" int fcg_lp_profile(fcg_learned *Lp, fcg_context *c, const float *r, i
     k_lp_rms<<<reduction_grid(c), kTPB, 0, st>>>(n, dr, Lp->red.as<double>(),
                                                  Lp->scal.as<unsigned>() + 17, rms, nullptr);
     LP_TRY(Lp, cudaEventRecord(ev[1], st));
-    k_lp_embed<<<grid_for(4LL * n, c->num_sms, 4), kTPB, 0, st>>>(n, dr, rms, Lp->feat.as<float>(),
+    k_lp_embed<<<grid_for(4LL * n, c->num_sms, 16), kTPB, 0, st>>>(n, dr, rms, Lp->feat.as<float>(),
                                                                  prm, H, nullptr, nullptr);
     LP_TRY(Lp, cudaEventRecord(ev[2], st));
     for (int l = 0; l < lp::L; ++l) {

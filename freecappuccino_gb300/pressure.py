@@ -353,6 +353,12 @@ class Batch:
         self._check(self.lib.fcg_batch_set_params(self.h, int(slices_per_item), int(blocks_per_sm)),
                     "fcg_batch_set_params")
 
+    def set_wait_test(self, polls: int = 0, absent_block: int = -1):
+        """Diagnostics: shorten the grid-barrier waits and keep one CTA away from them,
+        so that a solve ends with FCG_ERR_TIMEOUT; (0, -1) restores normal runs."""
+        self._check(self.lib.fcg_batch_set_wait_test(self.h, int(polls), int(absent_block)),
+                    "fcg_batch_set_wait_test")
+
     def autotune(self, a, su, sweeps: int = 20) -> float:
         for k, c in enumerate(self.contexts):
             c._follow(None if a is None else a[k], su[k])

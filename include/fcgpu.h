@@ -283,6 +283,11 @@ int fcg_batch_get_params(const fcg_batch *batch, int *slices_per_item, int *bloc
  * rep[nsys] may be NULL; rep[k].seconds is the time of the whole batch. */
 int fcg_batch_dpcg(fcg_batch *batch, const double *const *a, const double *const *su,
                    double *const *fi, double sor, int nsw, double *resor, fcg_solve_report *rep);
+/* Diagnostics for the timeout path of the grid barriers: every barrier wait gives up
+ * after `polls` polls (<= 0: the default, over 0.25 s), and CTA absent_block (>= 0)
+ * leaves before the first barrier, so the other CTAs' waits run out and fcg_batch_dpcg
+ * returns FCG_ERR_TIMEOUT with the device still usable.  (0, -1) restores normal runs. */
+int fcg_batch_set_wait_test(fcg_batch *batch, long long polls, int absent_block);
 /* Times `sweeps` fixed sweeps of every candidate (x = 0) and keeps the fastest. */
 int fcg_batch_autotune(fcg_batch *batch, const double *const *a, const double *const *su,
                        int sweeps, double *best_ms);

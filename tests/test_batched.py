@@ -104,3 +104,24 @@ def test_batch_argument_errors():
     with pytest.raises(fcg._lib.FcgError):
         b.set_params(16, b.params["max_blocks_per_sm"] + 1)
     b.close()
+
+
+def test_barrier_wait_runs_out_and_device_stays_usable():
+    """A CTA that never reaches the grid barrier: the others give up after the poll limit,
+    the call returns FCG_ERR_TIMEOUT, and the same batch then solves normally."""
+    systems = [_system(8, 1), _system(10, 2)]
+    ctxs = [c for c, _, _ in systems]
+    a = [x for _, x, _ in systems]
+    su = [x for _, _, x in systems]
+    x0 = [np.zeros(c.n) for c in ctxs]
+    b = fcg.Batch(ctxs)
+    b.set_wait_test(polls=4096, absent_block=0)
+    with pytest.raises(fcg._lib.FcgError) as ei:
+        b.dpcg(a, su, x0, 1e-8, 500)
+    assert ei.value.status == fcg._lib.FCG_ERR_TIMEOUT
+    b.set_wait_test(0, -1)
+    fi, reps = b.dpcg(a, su, x0, 1e-8, 500)
+    for k, (c, ak, sk) in enumerate(systems):
+        ref = c.dpcg(ak, sk, x0[k], 1e-8, 500)
+        assert reps[k].converged and _rel(fi[k], ref.fi) < 1e-7
+    b.close()
