@@ -268,6 +268,91 @@ def run_batch(args, dev, peak):
     return out
 
 
+def run_calcp(dev, N=128, npcor=3, seed=SEED + 1):
+    """One pressure step of calcp (calcp-multiple_correction_SIMPLE.f90:34-223) on the N^3
+    jittered mesh with seeded flow fields, all arrays on the device: facefluxmass, then
+    per correction ICCG to 1e-8, bpres + Gauss gradient (2 stages), Gauss-corrected
+    gradient, flux and field corrections, and fluxmc between corrections."""
+    import torch
+
+    import freecappuccino_gb300 as fcg
+    from freecappuccino_gb300.systems import flow_fields
+
+    m = fcg.hex_mesh(N, jitter=JITTER, seed=seed)
+    ctx = fcg.Context(m, device=dev.index or 0)
+    f = {k: torch.from_numpy(v).to(dev) for k, v in flow_fields(m, seed).items()}
+    n = m.numCells
+
+    def step():
+        a, su, flmass = ctx.facefluxmass(**f)
+        u, v, w, p, dPdxi = f["u"], f["v"], f["w"], f["p"], f["dPdxi"]
+        iters = []
+        for ipcorr in range(1, npcor + 1):
+            r = ctx.iccg(a, su, torch.zeros(n, dtype=torch.float64, device=dev), TOL, NSW,
+                         want_res=False)
+            iters.append(r.iters)
+            pp = torch.cat([r.fi, torch.zeros(m.numTotal - n, dtype=torch.float64, device=dev)])
+            for istage in (1, 2):
+                pp = ctx.bpres(pp, dPdxi, istage)
+                dPdxi = ctx.grad(pp, "gauss")
+            dPdxi = ctx.grad(pp, "gauss_corrected",
+                             dphidxi=torch.zeros((n, 3), dtype=torch.float64, device=dev))
+            flmass = ctx.flux_correct(a, pp, flmass)
+            u, v, w, p = ctx.correct_fields(dPdxi, f["apu"], f["apv"], f["apw"], pp, 0.3, 1,
+                                            u, v, w, p)
+            if ipcorr != npcor:
+                su, flmass = ctx.fluxmc(dPdxi, f["apu"], f["den"], flmass)
+        return iters
+
+    step()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    iters = step()
+    e1.record()
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) * 1e-3
+    ctx.close()
+    return {"workload": f"calcp pressure step, {N}^3 jittered hex, seeded flow fields, "
+                        f"{npcor} pressure corrections (ICCG to 1e-8) with non-orthogonal "
+                        "correctors, Gauss and Gauss-corrected gradients",
+            "seconds": t, "iccg_iterations": iters, "cells": n}
+
+
+def run_multi(dev, N=128, seed=SEED + 2):
+    """The five transport systems (u, v, w, k, eps) on one pattern solved in one
+    multi-RHS BiCGStab (FP32 DILU inner, FP64 correction to 1e-10) against five FP64
+    BiCGStab solves one after another."""
+    import torch
+
+    import freecappuccino_gb300 as fcg
+    from freecappuccino_gb300.systems import transport_systems
+
+    m = fcg.hex_mesh(N, jitter=JITTER, seed=seed)
+    ctx = fcg.Context(m, device=dev.index or 0)
+    a, su, dt = transport_systems(m, ctx.create_csr(), seed=seed)
+    a_d, su_d = torch.from_numpy(a).to(dev), torch.from_numpy(su).to(dev)
+    x0 = torch.zeros_like(su_d)
+    ctx.bicgstab_multi(a_d, su_d, x0, 1e-10, 2000)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    _, reps = ctx.bicgstab_multi(a_d, su_d, x0, 1e-10, 2000)
+    e1.record()
+    torch.cuda.synchronize()
+    t_multi = e0.elapsed_time(e1) * 1e-3
+    seq = [ctx.bicgstab(a_d[k], su_d[k], x0[k], 1e-10, 2000, want_res=False)
+           for k in range(a.shape[0])]
+    t_seq = sum(r.seconds for r in seq)
+    ctx.close()
+    return {"workload": f"5 transport systems (u, v, w, k, eps) on the {N}^3 jittered hex "
+                        "pattern, BiCGStab(DILU) to 1e-10", "seconds": t_multi,
+            "fp32_sweeps": [r.iters for r in reps], "all_converged": all(r.converged for r in reps),
+            "max_l2_rel": max(r.l2_rel for r in reps), "sequential_fp64_bicgstab_s": t_seq,
+            "sequential_iterations": [r.iters for r in seq],
+            "speedup_vs_sequential": t_seq / t_multi}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -281,6 +366,8 @@ def main():
                     help="sweep count used by the reference arm when none is recorded")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the calcp step (config 1) and the multi-RHS solve (config 2)")
     ap.add_argument("--batch-seed", type=int, default=4242)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--solver", default="learned",
@@ -459,6 +546,10 @@ def main():
     batch = None
     if not args.no_batch:
         batch = run_batch(args, dev, peak)
+    calcp = multi = None
+    if not args.no_configs:
+        calcp = run_calcp(dev)
+        multi = run_multi(dev)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -469,7 +560,8 @@ def main():
                  "dpcg_mixed": "f32 sweeps, f64 residual/updates"}.get(method, "f64")
         extra = {"comparisons": comparisons, "spmv_fp64": spmv64,
                  "l2_rel_final": last.l2_rel, "resl_over_res0": last.resl / last.res0,
-                 "mesh_setup_s": t_mesh, "bind_s": t_bind, "step_s": step_s, "batched": batch}
+                 "mesh_setup_s": t_mesh, "bind_s": t_bind, "step_s": step_s, "batched": batch,
+                 "calcp_step": calcp, "multi_rhs": multi}
         if method == "learned":
             extra["learned"] = {"fcg_iterations": last.fcg_iters, "fallback": last.fallback,
                                 "directions": 8, "weights": os.path.relpath(

@@ -379,6 +379,141 @@ __global__ void __launch_bounds__(kTPB, 4)
   }
 }
 
+// The same layer as two streaming kernels (k_lp_agg, k_lp_dense), bit-identical to
+// k_lp_layer: the aggregation writes m = Ahat h rounded to BF16, four threads per cell
+// and eight channels per thread with all neighbour loads of a row in flight at full
+// occupancy; the dense kernel streams the [h; m] rows of a 16-cell tile into the warp's
+// shared tile and runs the same mma.sync product and epilogue.
+__global__ void __launch_bounds__(kTPB)
+    k_lp_agg(SellView s, int n, const float *__restrict__ aval,
+             const __nv_bfloat16 *__restrict__ hin, __nv_bfloat16 *__restrict__ mout,
+             const int *done) {
+  if (stopped(done)) return;
+  FCG_GRID_STRIDE(t, 4LL * n) {
+    const int r = (int)(t >> 2), qc = 8 * (int)(t & 3);
+    const int slice = r >> 5, ln = r & 31;
+    const long long base = __ldg(&s.ptr[slice]) + ln;
+    const int w = __ldg(&s.width[slice]), op = __ldg(&s.offp[slice]);
+    const __nv_bfloat16 *hq = hin + qc;
+    float acc[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) acc[c] = 0.f;
+    if (__ldg(&s.kind[slice]) == 0 && w <= 8) {
+      float v[8];
+      uint4 hv[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        if (j < w) {
+          int col = r + __ldg(&s.off[op + j]);
+          col = col < 0 ? 0 : (col >= n ? n - 1 : col);
+          v[j] = __ldg(&aval[base + (long long)j * 32]);
+          hv[j] = __ldg(reinterpret_cast<const uint4 *>(hq + (long long)col * C));
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if (j < w) fma8(acc, v[j], hv[j]);
+    } else {
+      const bool uni = __ldg(&s.kind[slice]) == 0;
+      for (int j = 0; j < w; ++j) {
+        int col = uni ? r + __ldg(&s.off[op + j]) : __ldg(&s.off[op + 32 * j + ln]);
+        col = col < 0 ? 0 : (col >= n ? n - 1 : col);
+        fma8(acc, __ldg(&aval[base + (long long)j * 32]),
+             __ldg(reinterpret_cast<const uint4 *>(hq + (long long)col * C)));
+      }
+    }
+    __align__(16) __nv_bfloat16 mb[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) mb[c] = __float2bfloat16(acc[c]);
+    *reinterpret_cast<uint4 *>(mout + (long long)r * C + qc) = *reinterpret_cast<const uint4 *>(mb);
+  }
+}
+
+__global__ void __launch_bounds__(kTPB, 4)
+    k_lp_dense(int n, const __nv_bfloat16 *__restrict__ hin,
+               const __nv_bfloat16 *__restrict__ min_, __nv_bfloat16 *__restrict__ hout,
+               const __nv_bfloat16 *__restrict__ wl, const float *__restrict__ bl,
+               const int *done) {
+  if (stopped(done)) return;
+  constexpr int TS = lp::kTileStride;
+  __shared__ __align__(16) __nv_bfloat16 wsm[C * TS];
+  __shared__ float bsm[C];
+  __shared__ __align__(16) __nv_bfloat16 tile[kTPB / 32][16 * TS];
+  for (int t = threadIdx.x; t < C * 2 * C; t += blockDim.x)
+    wsm[(t / (2 * C)) * TS + t % (2 * C)] = wl[t];
+  if (threadIdx.x < C) bsm[threadIdx.x] = bl[threadIdx.x];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane >> 2, tg = lane & 3;
+  __nv_bfloat16 *tw = tile[warp];
+  const int ntiles = (n + 15) / 16;
+  const int nwarps = (int)(((long long)gridDim.x * blockDim.x) >> 5);
+  for (int tt = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5); tt < ntiles;
+       tt += nwarps) {
+    // 16 rows x (4 uint4 of h + 4 uint4 of m): 128 copies, 4 per lane
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int idx = lane + 32 * k, rr = idx >> 3, part = idx & 7;
+      const int cell = tt * 16 + rr;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (cell < n) {
+        const __nv_bfloat16 *src = part < 4 ? hin + (long long)cell * C + 8 * part
+                                            : min_ + (long long)cell * C + 8 * (part - 4);
+        v = __ldg(reinterpret_cast<const uint4 *>(src));
+      }
+      *reinterpret_cast<uint4 *>(tw + rr * TS + 8 * part) = v;
+    }
+    __syncwarp();
+    float d[4][4];
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) d[nt][q] = 0.f;
+#pragma unroll
+    for (int kb = 0; kb < 4; ++kb) {
+      const int k0 = kb * 16 + tg * 2;
+      unsigned a[4];
+      a[0] = *reinterpret_cast<const unsigned *>(tw + g * TS + k0);
+      a[1] = *reinterpret_cast<const unsigned *>(tw + (g + 8) * TS + k0);
+      a[2] = *reinterpret_cast<const unsigned *>(tw + g * TS + k0 + 8);
+      a[3] = *reinterpret_cast<const unsigned *>(tw + (g + 8) * TS + k0 + 8);
+#pragma unroll
+      for (int nt = 0; nt < 4; ++nt) {
+        const int oc = nt * 8 + g;
+        unsigned b[2];
+        b[0] = *reinterpret_cast<const unsigned *>(wsm + oc * TS + k0);
+        b[1] = *reinterpret_cast<const unsigned *>(wsm + oc * TS + k0 + 8);
+        mma_bf16(d[nt], a, b);
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh) {
+        const int rr = g + 8 * hh, col = nt * 8 + tg * 2;
+        const float z0 = d[nt][2 * hh] + bsm[col], z1 = d[nt][2 * hh + 1] + bsm[col + 1];
+        __nv_bfloat162 *hp = reinterpret_cast<__nv_bfloat162 *>(tw + rr * TS + col);
+        const __nv_bfloat162 hold = *hp;
+        __nv_bfloat162 o;
+        o.x = __float2bfloat16(bf(hold.x) + fmaxf(z0, 0.f));
+        o.y = __float2bfloat16(bf(hold.y) + fmaxf(z1, 0.f));
+        *hp = o;
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int idx = lane + 32 * k, rr = idx >> 2, part = idx & 3;
+      const int cell = tt * 16 + rr;
+      if (cell < n)
+        *reinterpret_cast<uint4 *>(hout + (long long)cell * C + 8 * part) =
+            *reinterpret_cast<const uint4 *>(tw + rr * TS + 8 * part);
+    }
+    __syncwarp();
+  }
+}
+
 __device__ __forceinline__ float out_dot(const __nv_bfloat16 *__restrict__ h, long long i,
                                          const float *w) {
   const uint4 *hp = reinterpret_cast<const uint4 *>(h + i * C);
@@ -950,7 +1085,7 @@ int ensure_workspace(fcg_learned *Lp, fcg_context *c, bool train) {
     Lp->train_cap = false;
     LP_TRY(Lp, Lp->feat.ensure(sizeof(float) * n * lp::F));
     LP_TRY(Lp, Lp->y.ensure(sizeof(float) * n));
-    LP_TRY(Lp, Lp->hbuf.ensure(sizeof(__nv_bfloat16) * 2 * n * lp::C));
+    LP_TRY(Lp, Lp->hbuf.ensure(sizeof(__nv_bfloat16) * 3 * n * lp::C));  // h ping-pong + m
     Lp->fuid = 0;  // features must be recomputed into the new buffer
   }
   if (train && !Lp->train_cap) {
@@ -1021,6 +1156,13 @@ int compute_features(fcg_learned *Lp, fcg_context *c) {
   return FCG_OK;
 }
 
+// Inference runs each layer as k_lp_agg + k_lp_dense unless FCG_LP_LAYER=fused selects
+// the one-kernel form (both give the same bits).
+bool layer_split() {
+  const char *e = std::getenv("FCG_LP_LAYER");
+  return !(e && std::strcmp(e, "fused") == 0);
+}
+
 // Forward pass on r (device, FP32) up to h_L.  Training keeps h_0..h_L, m_1..m_L and the
 // pre-activations; inference ping-pongs two activation buffers.  `done` (device flag or
 // NULL) turns the launches into no-ops.
@@ -1038,14 +1180,21 @@ void enqueue_forward(fcg_learned *Lp, fcg_context *c, cudaStream_t st, const flo
   const __nv_bfloat16 *wbf = Lp->wbf.as<__nv_bfloat16>();
   const int ntiles = (n + 15) / 16;
   const int lg = std::max(1, std::min((ntiles + 7) / 8, c->num_sms * 4));
+  const bool split = !train && layer_split();
   for (int l = 0; l < lp::L; ++l) {
     const __nv_bfloat16 *hin = train ? H + l * hs : H + (l % 2) * hs;
     __nv_bfloat16 *hout = train ? H + (l + 1) * hs : H + ((l + 1) % 2) * hs;
-    k_lp_layer<<<lg, kTPB, 0, st>>>(c->sv, n, aval, hin, hout,
-                                    wbf + (size_t)l * 2 * lp::C * lp::C,
-                                    prm + lp::oLayer0 + l * lp::kLayerParams + 2 * lp::C * lp::C,
-                                    train ? Lp->mbuf.as<float>() + l * hs : nullptr,
-                                    train ? Lp->zbuf.as<float>() + (l + 1) * hs : nullptr, done);
+    const __nv_bfloat16 *wl = wbf + (size_t)l * 2 * lp::C * lp::C;
+    const float *bl = prm + lp::oLayer0 + l * lp::kLayerParams + 2 * lp::C * lp::C;
+    if (split) {
+      k_lp_agg<<<grid_for(4LL * n, c->num_sms, 8), kTPB, 0, st>>>(c->sv, n, aval, hin, H + 2 * hs,
+                                                                 done);
+      k_lp_dense<<<lg, kTPB, 0, st>>>(n, hin, H + 2 * hs, hout, wl, bl, done);
+    } else {
+      k_lp_layer<<<lg, kTPB, 0, st>>>(c->sv, n, aval, hin, hout, wl, bl,
+                                      train ? Lp->mbuf.as<float>() + l * hs : nullptr,
+                                      train ? Lp->zbuf.as<float>() + (l + 1) * hs : nullptr, done);
+    }
   }
 }
 
@@ -1354,10 +1503,17 @@ extern "C" int fcg_lp_profile(fcg_learned *Lp, fcg_context *c, const float *r, i
                                                                  prm, H, nullptr, nullptr);
     LP_TRY(Lp, cudaEventRecord(ev[2], st));
     for (int l = 0; l < lp::L; ++l) {
-      k_lp_layer<<<lg, kTPB, 0, st>>>(
-          c->sv, n, scaled32(c), H + (l % 2) * hs, H + ((l + 1) % 2) * hs,
-          Lp->wbf.as<__nv_bfloat16>() + (size_t)l * 2 * lp::C * lp::C,
-          prm + lp::oLayer0 + l * lp::kLayerParams + 2 * lp::C * lp::C, nullptr, nullptr, nullptr);
+      const __nv_bfloat16 *wl = Lp->wbf.as<__nv_bfloat16>() + (size_t)l * 2 * lp::C * lp::C;
+      const float *bl = prm + lp::oLayer0 + l * lp::kLayerParams + 2 * lp::C * lp::C;
+      if (layer_split()) {
+        k_lp_agg<<<grid_for(4LL * n, c->num_sms, 8), kTPB, 0, st>>>(
+            c->sv, n, scaled32(c), H + (l % 2) * hs, H + 2 * hs, nullptr);
+        k_lp_dense<<<lg, kTPB, 0, st>>>(n, H + (l % 2) * hs, H + 2 * hs, H + ((l + 1) % 2) * hs,
+                                        wl, bl, nullptr);
+      } else {
+        k_lp_layer<<<lg, kTPB, 0, st>>>(c->sv, n, scaled32(c), H + (l % 2) * hs,
+                                        H + ((l + 1) % 2) * hs, wl, bl, nullptr, nullptr, nullptr);
+      }
       LP_TRY(Lp, cudaEventRecord(ev[3 + l], st));
     }
     k_lp_out<<<grid_for(n, c->num_sms), kTPB, 0, st>>>(n, H + (lp::L % 2) * hs, prm, rms, dr,

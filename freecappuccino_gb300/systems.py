@@ -1,4 +1,5 @@
-"""Synthetic linear systems of the benchmark configurations.
+"""Synthetic inputs of the benchmark configurations: flow fields of the pressure step
+and the linear systems of the multi-RHS configuration.
 
 ``transport_systems`` builds the five convection-diffusion systems of the multi-RHS
 configuration on a mesh: momentum u, v, w (one set of off-diagonals, as calcuvw.f90
@@ -15,6 +16,22 @@ from __future__ import annotations
 import numpy as np
 
 from .mesh import Mesh, uniform
+
+
+def flow_fields(m: Mesh, seed: int = 3):
+    """Seeded flow fields of the pressure step (calcp): u, v, w, p and den of numTotal
+    length (U(-1,1), den 1 +- 0.2), gradients (numCells, 3) U(-1,1), and
+    ap* = (1 +- 0.1) / vol."""
+    n, nt = m.numCells, m.numTotal
+    u = uniform(seed, 1, nt)
+    v = uniform(seed, 2, nt)
+    w = uniform(seed, 3, nt)
+    p = uniform(seed, 4, nt)
+    g = [uniform(seed, 10 + k, 3 * n).reshape(n, 3) for k in range(4)]
+    ap = [1.0 / m.vol * (1.0 + 0.1 * uniform(seed, 20 + k, n)) for k in range(3)]
+    den = 1.0 + 0.2 * uniform(seed, 30, nt)
+    return dict(u=u, v=v, w=w, p=p, dUdxi=g[0], dVdxi=g[1], dWdxi=g[2], dPdxi=g[3],
+                apu=ap[0], apv=ap[1], apw=ap[2], den=den)
 
 
 def fourier_velocity(x, y, z, seed: int, modes: int = 3):

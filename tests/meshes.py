@@ -46,16 +46,9 @@ def oracle_csr(m: fcg.Mesh) -> oracle.CSR:
 
 def seeded_fields(m: fcg.Mesh, seed: int = 3):
     """Seeded flow fields for facefluxmass / fluxmc / gradient parity."""
-    n, nt = m.numCells, m.numTotal
-    u = fcg.uniform(seed, 1, nt)
-    v = fcg.uniform(seed, 2, nt)
-    w = fcg.uniform(seed, 3, nt)
-    p = fcg.uniform(seed, 4, nt)
-    g = [fcg.uniform(seed, 10 + k, 3 * n).reshape(n, 3) for k in range(4)]
-    ap = [1.0 / m.vol * (1.0 + 0.1 * fcg.uniform(seed, 20 + k, n)) for k in range(3)]
-    den = 1.0 + 0.2 * fcg.uniform(seed, 30, nt)
-    return dict(u=u, v=v, w=w, p=p, dUdxi=g[0], dVdxi=g[1], dWdxi=g[2], dPdxi=g[3],
-                apu=ap[0], apv=ap[1], apw=ap[2], den=den)
+    from freecappuccino_gb300.systems import flow_fields
+
+    return flow_fields(m, seed)
 
 
 def poisson_system(m: fcg.Mesh, seed: int = 11, mu_value: float = -1.0):
