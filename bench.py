@@ -448,8 +448,10 @@ def main():
     last = reports[-1]
     iters = last.iters
     if method != "learned":
+        ctx_levels = 3 * N - 2  # levels of each triangular sweep on the N^3 hex mesh
         per_solve = {"dpcg": lambda it: 3 + 3 * it, "dpcg_mixed": lambda it: 6 + 5 * it,
-                     "iccg": lambda it: 4 + 5 * it, "bicgstab": lambda it: 4 + 8 * it}
+                     "iccg": lambda it: 3 + (2 * ctx_levels + 4) * it,
+                     "bicgstab": lambda it: 3 + (4 * ctx_levels + 6) * it}
         launches = sum(per_solve.get(method, lambda it: 3 + 3 * it)(r.iters) for r in reports)
     x_method = last.fi.clone()
     peak, peak_kind = peaks()
@@ -470,7 +472,11 @@ def main():
                       "layer_tensor_TFLOPs": 4096.0 * n / t_dom / 1e12}
     else:
         prof = ctx.profile_sweeps(20)
-        if method == "dpcg_mixed":
+        if method in ("iccg", "bicgstab"):
+            dom = "fwd_levels"  # the forward triangular sweep, level by level
+            dom_bytes = 6 * (nnz - n) + 20 * n
+            dom_desc = "fwd_levels (DIC/DILU forward sweep, one launch per level, 256^3)"
+        elif method == "dpcg_mixed":
             dom = "k_mx_spmv"
             dom_bytes = 8 * nnz + 4 * (n + 1) + 8 * n  # FP32 values + int32 columns, FP32 x/y
             dom_desc = "k_mx_spmv (FP32 sliced-ELL SpMV of the scaled matrix + p.Ap, 256^3)"

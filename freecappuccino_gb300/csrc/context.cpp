@@ -311,8 +311,6 @@ extern "C" int fcg_bind_mesh(fcg_context *c, const fcg_mesh_desc *m) {
   c->lb.count = (int)t.lb_ptr.size() - 1;
   UP(rows, t.lb_rows.data(), t.lb_rows.size());
   c->lb.rows = const_cast<int *>(rows);
-  UP(c->lf.dptr, t.lf_ptr.data(), t.lf_ptr.size());
-  UP(c->lb.dptr, t.lb_ptr.data(), t.lb_ptr.size());
 #undef UP
 
   c->h_ioffset.swap(t.ioffset);

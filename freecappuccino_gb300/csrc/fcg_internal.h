@@ -70,9 +70,8 @@ struct SellView {
 };
 
 struct Level {
-  std::vector<int> ptr;        // host: level offsets into rows
-  int *rows = nullptr;         // device: rows sorted by level, ascending inside a level
-  const int *dptr = nullptr;   // device copy of ptr
+  std::vector<int> ptr;  // host: level offsets into rows
+  int *rows = nullptr;   // device: rows sorted by level, ascending inside a level
   int count = 0;
 };
 

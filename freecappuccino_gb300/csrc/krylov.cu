@@ -80,8 +80,6 @@ struct KrylovState {
   cudaGraphExec_t exec[SK_N] = {};
   cudaGraph_t graph[SK_N] = {};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  void *sctl = nullptr;  // SweepCtl of the cooperative triangular sweeps (device)
-  int coop_grid = 0;     // CTAs of a cooperative sweep launch
   bool matrix_loaded = false;
   int last_kind = -1;
   double small = (double)1e-20f;  // parameters::small (modules_allocatable.f90:27)
@@ -99,7 +97,6 @@ void destroy_krylov(KrylovState *k) {
   if (k->ev1) cudaEventDestroy(k->ev1);
   if (k->hS) cudaFreeHost(k->hS);
   if (k->S) cudaFree(k->S);
-  if (k->sctl) cudaFree(k->sctl);
   k->vec.release();
   k->trace.release();
   k->mixed.release();
@@ -306,139 +303,60 @@ __global__ void __launch_bounds__(kTPB, 8) k_cg_dot(int n, const double *__restr
   }
 }
 
-// --- triangular sweeps and the factor, level by level, in one cooperative launch -----
-// The rows of a level depend only on rows of earlier levels.  All levels run in one
-// persistent launch, separated by a grid barrier whose wait is bounded: a CTA that gives
-// up marks the solve FCG_ERR_TIMEOUT and every CTA leaves at its next barrier.  Inside a
-// level the rows are dealt to the grid's threads in order.
-//   forward:  z_i = (b_i - sum_{k<diag} a_k z_{ja_k}) * d_i          (iccg.f90:248-254)
-//   backward: z_i = (z_i / (d_i + small) - sum_{k>diag} a_k z_{ja_k}) * d_i
-//             (iccg.f90:256-265, the rescale zk/(d+small) folded in)
-//   factor:   DIC  d_i = 1/(a_ii - sum a_ik^2 d_k)        (iccg.f90:231-237)
-//             DILU d_i = 1/(a_ii - sum a_ik d_k a_ki)      (bicgstab.f90:68-79)
-struct SweepCtl {
-  unsigned int count, gen;
-  int err, pad;
-};
-
-__device__ bool sweep_sync(SweepCtl *ctl, long long limit) {
-  __shared__ int ok_sh;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    volatile unsigned int *vgen = &ctl->gen;
-    volatile int *verr = &ctl->err;
-    if (*verr) {
-      ok = 0;
-    } else {
-      const unsigned int g = *vgen;
-      __threadfence();
-      if (atomicAdd(&ctl->count, 1u) == gridDim.x - 1) {
-        ctl->count = 0u;
-        __threadfence();
-        atomicAdd(&ctl->gen, 1u);
-      } else {
-        long long polls = 0;
-        while (*vgen == g) {
-          if (*verr) {
-            ok = 0;
-            break;
-          }
-          if (++polls > limit) {
-            atomicExch(&ctl->err, 1);
-            ok = 0;
-            break;
-          }
-          __nanosleep(32);
-        }
-      }
-    }
-    __threadfence();
-    ok_sh = ok;
-  }
-  __syncthreads();
-  __threadfence();
-  return ok_sh != 0;
-}
-
-__device__ __noinline__ void sweep_timeout(Scal *S) {
-  S->status = FCG_ERR_TIMEOUT;
-  S->done = 1;
-}
-
-// M^-1 b: the forward sweep over all levels of lf, then the backward sweep over lb
-// (iccg.f90:248-265; the DILU application of bicgstab.f90 has the same two sweeps).
-__global__ void __launch_bounds__(kTPB)
-    k_tri_apply(const int *__restrict__ lfr, const int *__restrict__ lfp, int nlf,
-                const int *__restrict__ lbr, const int *__restrict__ lbp, int nlb,
-                const int *__restrict__ ioffset, const int *__restrict__ ja,
-                const int *__restrict__ diag, const double *__restrict__ a,
-                const double *__restrict__ d, const double *b, double *z, Scal *S,
-                SweepCtl *ctl, long long limit) {
+// --- triangular sweeps, one launch per level -----------------------------------
+// forward: z_i = (b_i - sum_{k<diag} a_k z_{ja_k}) * d_i        (iccg.f90:248-254)
+__global__ void k_fwd_level(const int *__restrict__ rows, int count,
+                            const int *__restrict__ ioffset, const int *__restrict__ ja,
+                            const int *__restrict__ diag, const double *__restrict__ a,
+                            const double *__restrict__ d, const double *__restrict__ b,
+                            double *__restrict__ z, const Scal *S) {
   if (solve_done(S)) return;
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
-  for (int l = 0; l < nlf; ++l) {
-    const int s1 = __ldg(&lfp[l + 1]);
-    for (int t = __ldg(&lfp[l]) + tid; t < s1; t += nth) {
-      const int i = __ldg(&lfr[t]);
-      double zi = b[i];
-      for (int k = __ldg(&ioffset[i]); k < __ldg(&diag[i]); ++k)
-        zi = zi - __ldg(&a[k]) * z[__ldg(&ja[k])];
-      z[i] = zi * __ldg(&d[i]);
-    }
-    if (!sweep_sync(ctl, limit)) {
-      if (threadIdx.x == 0) sweep_timeout(S);
-      return;
-    }
-  }
-  const double small = S->small;
-  for (int l = 0; l < nlb; ++l) {
-    const int s1 = __ldg(&lbp[l + 1]);
-    for (int t = __ldg(&lbp[l]) + tid; t < s1; t += nth) {
-      const int i = __ldg(&lbr[t]);
-      const double di = __ldg(&d[i]);
-      double zi = z[i] / (di + small);
-      for (int k = __ldg(&diag[i]) + 1; k < __ldg(&ioffset[i + 1]); ++k)
-        zi = zi - __ldg(&a[k]) * z[__ldg(&ja[k])];
-      z[i] = zi * di;
-    }
-    if (l + 1 < nlb && !sweep_sync(ctl, limit)) {
-      if (threadIdx.x == 0) sweep_timeout(S);
-      return;
-    }
-  }
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  int i = rows[t];
+  double zi = b[i];
+  for (int k = ioffset[i]; k < diag[i]; ++k) zi = zi - a[k] * z[ja[k]];
+  z[i] = zi * d[i];
 }
 
-// The factor diagonal over all levels of lf in one launch.
-__global__ void __launch_bounds__(kTPB)
-    k_factor_coop(const int *__restrict__ lfr, const int *__restrict__ lfp, int nlf,
-                  const int *__restrict__ ioffset, const int *__restrict__ ja,
-                  const int *__restrict__ diag, const int *__restrict__ tpos,
-                  const double *__restrict__ a, double *d, Scal *S, int dilu, SweepCtl *ctl,
-                  long long limit) {
+// backward with the reference's rescale zk/(d+small) folded in (iccg.f90:256-265).
+__global__ void k_bwd_level(const int *__restrict__ rows, int count,
+                            const int *__restrict__ ioffset, const int *__restrict__ ja,
+                            const int *__restrict__ diag, const double *__restrict__ a,
+                            const double *__restrict__ d, double *__restrict__ z,
+                            const Scal *S) {
   if (solve_done(S)) return;
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
-  for (int l = 0; l < nlf; ++l) {
-    const int s1 = __ldg(&lfp[l + 1]);
-    for (int t = __ldg(&lfp[l]) + tid; t < s1; t += nth) {
-      const int i = __ldg(&lfr[t]);
-      double di = __ldg(&a[__ldg(&diag[i])]);
-      for (int k = __ldg(&ioffset[i]); k < __ldg(&diag[i]); ++k) {
-        const int j = __ldg(&ja[k]);
-        if (dilu)
-          di = di - __ldg(&a[k]) * d[j] * __ldg(&a[__ldg(&tpos[k])]);
-        else
-          di = di - __ldg(&a[k]) * __ldg(&a[k]) * d[j];
-      }
-      const double inv = 1.0 / di;
-      d[i] = inv;
-      if (!isfinite(inv) || di == 0.0) S->status = FCG_ERR_PIVOT;
-    }
-    if (!sweep_sync(ctl, limit)) {
-      if (threadIdx.x == 0) sweep_timeout(S);
-      return;
-    }
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  int i = rows[t];
+  double di = d[i];
+  double zi = z[i] / (di + S->small);
+  for (int k = diag[i] + 1; k < ioffset[i + 1]; ++k) zi = zi - a[k] * z[ja[k]];
+  z[i] = zi * di;
+}
+
+// Factor diagonals, level by level: DIC d_i = 1/(a_ii - sum a_ik^2 d_k) (iccg.f90:
+// 231-237); DILU d_i = 1/(a_ii - sum a_ik d_k a_ki) (bicgstab.f90:68-79).
+__global__ void k_factor_level(const int *__restrict__ rows, int count,
+                               const int *__restrict__ ioffset, const int *__restrict__ ja,
+                               const int *__restrict__ diag, const int *__restrict__ tpos,
+                               const double *__restrict__ a, double *__restrict__ d, Scal *S,
+                               int dilu) {
+  if (solve_done(S)) return;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  int i = rows[t];
+  double di = a[diag[i]];
+  for (int k = ioffset[i]; k < diag[i]; ++k) {
+    int j = ja[k];
+    if (dilu)
+      di = di - a[k] * d[j] * a[tpos[k]];
+    else
+      di = di - a[k] * a[k] * d[j];
   }
+  double inv = 1.0 / di;
+  d[i] = inv;
+  if (!isfinite(inv) || di == 0.0) S->status = FCG_ERR_PIVOT;
 }
 
 // --- BiCGStab sweep (bicgstab.f90:99-224) -------------------------------------
@@ -801,17 +719,6 @@ static int ensure_state(fcg_context *c, int nsw) {
     FCG_CUDA_TRY(c, cudaStreamCreateWithFlags(&k->cap, cudaStreamNonBlocking));
     FCG_CUDA_TRY(c, cudaEventCreate(&k->ev0));
     FCG_CUDA_TRY(c, cudaEventCreate(&k->ev1));
-    FCG_CUDA_TRY(c, cudaMalloc(&k->sctl, sizeof(SweepCtl)));
-    FCG_CUDA_TRY(c, cudaMemset(k->sctl, 0, sizeof(SweepCtl)));
-    // one CTA per SM: every level of a sweep is a few thousand rows at most per SM, and
-    // fewer CTAs make the level barrier cheaper
-    int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_tri_apply, kTPB, 0) != cudaSuccess ||
-        occ < 1) {
-      cudaGetLastError();
-      return set_error(c, FCG_ERR_CUDA, "k_tri_apply cannot be resident");
-    }
-    k->coop_grid = c->num_sms;
   }
   const int G = c->num_sms * 8;
   if (k->n != c->n || k->nnz != c->nnz || k->sell_len != c->sell_len || k->G != G ||
@@ -963,24 +870,19 @@ const float *scaled32(const fcg_context *c) { return c->ks ? c->ks->sval32 : nul
 const double *scale64(const fcg_context *c) { return c->ks ? c->ks->s64 : nullptr; }
 const double *sliced64(const fcg_context *c) { return c->ks ? c->ks->sval : nullptr; }
 
-constexpr long long kSweepSpin = 1LL << 22;  // polls of 32 ns sleeps per level barrier
-
-// M^-1 b -> z in one cooperative launch (both triangular sweeps).
-static void launch_tri_apply(fcg_context *c, cudaStream_t st, const double *b, double *z) {
+static void launch_sweeps(fcg_context *c, cudaStream_t st, const Level &lv, bool forward,
+                          const double *b, double *z) {
   KrylovState *k = c->ks;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(k->coop_grid);
-  cfg.blockDim = dim3(kTPB);
-  cfg.stream = st;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeCooperative;
-  attr[0].val.cooperative = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, k_tri_apply, (const int *)c->lf.rows, c->lf.dptr, c->lf.count,
-                     (const int *)c->lb.rows, c->lb.dptr, c->lb.count, c->mv.ioffset, c->mv.ja,
-                     c->mv.diag, (const double *)k->a, (const double *)k->d, b, z, k->S,
-                     (SweepCtl *)k->sctl, kSweepSpin);
+  for (int l = 0; l < lv.count; ++l) {
+    int start = lv.ptr[l], cnt = lv.ptr[l + 1] - lv.ptr[l];
+    int g = (cnt + kTPB - 1) / kTPB;
+    if (forward)
+      k_fwd_level<<<g, kTPB, 0, st>>>(lv.rows + start, cnt, c->mv.ioffset, c->mv.ja, c->mv.diag,
+                                      k->a, k->d, b, z, k->S);
+    else
+      k_bwd_level<<<g, kTPB, 0, st>>>(lv.rows + start, cnt, c->mv.ioffset, c->mv.ja, c->mv.diag,
+                                      k->a, k->d, z, k->S);
+  }
 }
 
 // Kernels of one sweep, in order, as units (a unit of a DIC/DILU sweep is the whole
@@ -988,8 +890,8 @@ static void launch_tri_apply(fcg_context *c, cudaStream_t st, const double *b, d
 static int sweep_units(int kind) {
   switch (kind) {
     case SK_DPCG: return 3;
-    case SK_ICCG: return 5;
-    case SK_BICG: return 8;
+    case SK_ICCG: return 6;
+    case SK_BICG: return 10;
     case SK_MIXED: return 5;
   }
   return 0;
@@ -997,9 +899,10 @@ static int sweep_units(int kind) {
 
 static const char *sweep_unit_name(int kind, int u) {
   static const char *dpcg[] = {"k_cg_p", "k_cg_spmv", "k_cg_update"};
-  static const char *iccg[] = {"k_tri_apply", "k_cg_dot", "k_cg_p", "k_cg_spmv", "k_cg_update"};
-  static const char *bicg[] = {"k_bi_dot1", "k_bi_p", "k_tri_apply", "k_bi_spmv1",
-                               "k_bi_upd1", "k_tri_apply", "k_bi_spmv2", "k_bi_upd2"};
+  static const char *iccg[] = {"fwd_levels", "bwd_levels", "k_cg_dot", "k_cg_p", "k_cg_spmv",
+                               "k_cg_update"};
+  static const char *bicg[] = {"k_bi_dot1", "k_bi_p", "fwd_levels", "bwd_levels", "k_bi_spmv1",
+                               "k_bi_upd1", "fwd_levels", "bwd_levels", "k_bi_spmv2", "k_bi_upd2"};
   static const char *mixed[] = {"k_mx_spmv", "k_mx_update", "k_mx_ru1", "k_mx_ru2", "k_mx_p"};
   if (u < 0 || u >= sweep_units(kind)) return "";
   switch (kind) {
@@ -1019,9 +922,10 @@ static void enqueue_unit(fcg_context *c, cudaStream_t st, int kind, int u,
   const SellView &s = c->sv;
   double *tr = k->trace.as<double>();
   if (kind == SK_DPCG || kind == SK_ICCG) {
-    int v = kind == SK_DPCG ? u + 3 : (u == 0 ? 0 : u + 1);
+    int v = kind == SK_DPCG ? u + 3 : u;
     switch (v) {
-      case 0: launch_tri_apply(c, st, k->res, k->zk); break;
+      case 0: launch_sweeps(c, st, c->lf, true, k->res, k->zk); break;
+      case 1: launch_sweeps(c, st, c->lb, false, nullptr, k->zk); break;
       case 2: k_cg_dot<<<k->gr.dot, kTPB, 0, st>>>(n, k->res, k->zk, k->S, k->partials); break;
       case 3:
         k_cg_p<<<k->gr.p, kTPB, 0, st>>>(n, k->res, k->invd, k->zk, k->pk, k->S, kind);
@@ -1056,18 +960,20 @@ static void enqueue_unit(fcg_context *c, cudaStream_t st, int kind, int u,
     switch (u) {
       case 0: k_bi_dot1<<<k->gr.bdot, kTPB, 0, st>>>(n, k->res, k->reso, k->S, k->partials); break;
       case 1: k_bi_p<<<k->gr.bp, kTPB, 0, st>>>(n, k->res, k->uk, k->pk, k->S); break;
-      case 2: launch_tri_apply(c, st, k->pk, k->zk); break;
-      case 3:
+      case 2: launch_sweeps(c, st, c->lf, true, k->pk, k->zk); break;
+      case 3: launch_sweeps(c, st, c->lb, false, nullptr, k->zk); break;
+      case 4:
         k_bi_spmv1<<<k->gr.bspmv1, kTPB, 0, st>>>(s, n, k->sval, k->zk, k->reso, k->uk, k->S,
                                                    k->partials);
         break;
-      case 4: k_bi_upd1<<<k->gr.bupd1, kTPB, 0, st>>>(n, k->x, k->res, k->zk, k->uk, k->S); break;
-      case 5: launch_tri_apply(c, st, k->res, k->zk); break;
-      case 6:
+      case 5: k_bi_upd1<<<k->gr.bupd1, kTPB, 0, st>>>(n, k->x, k->res, k->zk, k->uk, k->S); break;
+      case 6: launch_sweeps(c, st, c->lf, true, k->res, k->zk); break;
+      case 7: launch_sweeps(c, st, c->lb, false, nullptr, k->zk); break;
+      case 8:
         k_bi_spmv2<<<k->gr.bspmv2, kTPB, 0, st>>>(s, n, k->sval, k->zk, k->res, k->vk, k->S,
                                                    k->partials);
         break;
-      case 7:
+      case 9:
         k_bi_upd2<<<k->gr.bupd2, kTPB, 0, st>>>(n, k->x, k->res, k->zk, k->vk, k->S, k->partials,
                                                 tr, h, use_cond);
         break;
@@ -1194,21 +1100,14 @@ static int run_solver(fcg_context *c, int kind, const double *a, const double *s
                                                      k->p32, k->S, k->partials);
     FCG_CHECK_LAUNCH(c, "mixed set-up");
   }
-  if (kind != SK_DPCG) {  // factor diagonal, all levels in one cooperative launch
-    FCG_CUDA_TRY(c, cudaMemsetAsync(k->sctl, 0, sizeof(SweepCtl), c->stream));
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(k->coop_grid);
-    cfg.blockDim = dim3(kTPB);
-    cfg.stream = c->stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    FCG_CUDA_TRY(c, cudaLaunchKernelEx(&cfg, k_factor_coop, (const int *)c->lf.rows, c->lf.dptr,
-                                       c->lf.count, c->mv.ioffset, c->mv.ja, c->mv.diag, c->tpos,
-                                       (const double *)k->a, k->d, k->S, (int)(kind == SK_BICG),
-                                       (SweepCtl *)k->sctl, kSweepSpin));
+  if (kind != SK_DPCG) {  // factor diagonal, level by level
+    for (int l = 0; l < c->lf.count; ++l) {
+      int start = c->lf.ptr[l], cnt = c->lf.ptr[l + 1] - c->lf.ptr[l];
+      k_factor_level<<<(cnt + kTPB - 1) / kTPB, kTPB, 0, c->stream>>>(
+          c->lf.rows + start, cnt, c->mv.ioffset, c->mv.ja, c->mv.diag, c->tpos, k->a, k->d, k->S,
+          kind == SK_BICG);
+    }
+    FCG_CHECK_LAUNCH(c, "k_factor_level");
   }
   if (!graphs_disabled()) {
     if ((rc = build_graph(c, kind))) return rc;
@@ -1306,6 +1205,7 @@ __global__ void k_prof_reopen(Scal *S) {
     S->iter = 0;
     S->body_count = 0;
     S->nsw = 0x3fffffff;
+    S->resmax = 0.0;  // never converges: every profiled sweep does its full work
   }
 }
 

@@ -1156,11 +1156,11 @@ int compute_features(fcg_learned *Lp, fcg_context *c) {
   return FCG_OK;
 }
 
-// Inference runs each layer as k_lp_agg + k_lp_dense unless FCG_LP_LAYER=fused selects
-// the one-kernel form (both give the same bits).
+// Inference runs each layer as the one-kernel form k_lp_layer; FCG_LP_LAYER=split selects
+// k_lp_agg + k_lp_dense (same bits; measured 2.0 ms against 1.44 ms per layer at 256^3).
 bool layer_split() {
   const char *e = std::getenv("FCG_LP_LAYER");
-  return !(e && std::strcmp(e, "fused") == 0);
+  return e && std::strcmp(e, "split") == 0;
 }
 
 // Forward pass on r (device, FP32) up to h_L.  Training keeps h_0..h_L, m_1..m_L and the
