@@ -1,0 +1,143 @@
+"""polyMesh files of the reference's cases (points, faces, owner, neighbour, boundary).
+
+The reference reads an OpenFOAM-style polyMesh plus its own `boundary` file
+(mesh_geometry_and_topology.f90:310-560): ASCII lists with a FoamFile header, faces as
+`n(i j k ...)` with 0-based point labels, owner/neighbour as 0-based cell labels (the
+cell count in the owner header note `nCells:`), and one `type nFaces startFace` line per
+patch in the boundary file.  Indices are returned 1-based, as the reference holds them.
+"""
+from __future__ import annotations
+
+import os
+import re
+
+import numpy as np
+
+from .mesh import Mesh, polymesh_mesh
+
+
+def _body(text: str) -> str:
+    """The list part of a FOAM file: comments and the FoamFile header removed."""
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    text = re.sub(r"FoamFile\s*\{.*?\}", "", text, flags=re.S)
+    return text.strip()
+
+
+def parse_points(text: str) -> np.ndarray:
+    t = _body(text)
+    n = int(t.split("(", 1)[0])
+    xyz = np.array([[float(v) for v in p.split()]
+                    for p in re.findall(r"\(([^()]*)\)", t.split("(", 1)[1])], dtype=np.float64)
+    if xyz.shape != (n, 3):
+        raise ValueError(f"points: expected {n} x 3 values, found {xyz.shape}")
+    return xyz
+
+
+def parse_faces(text: str):
+    """(face_ptr, face_nodes), 1-based node labels."""
+    t = _body(text)
+    nf = int(t.split("(", 1)[0])
+    ptr, nodes = [0], []
+    for cnt, body in re.findall(r"(\d+)\(([^()]*)\)", t.split("(", 1)[1]):
+        ids = [int(v) + 1 for v in body.split()]
+        if len(ids) != int(cnt):
+            raise ValueError("faces: a face lists a wrong number of nodes")
+        nodes.extend(ids)
+        ptr.append(len(nodes))
+    if len(ptr) != nf + 1:
+        raise ValueError(f"faces: expected {nf} faces, found {len(ptr) - 1}")
+    return np.array(ptr, np.int32), np.array(nodes, np.int32)
+
+
+def parse_labels(text: str) -> np.ndarray:
+    """A label list as 1-based int32."""
+    t = _body(text)
+    cnt = int(t.split("(", 1)[0])
+    vals = np.array(t.split("(", 1)[1].rsplit(")", 1)[0].split(), dtype=np.int64) + 1
+    if len(vals) != cnt:
+        raise ValueError(f"labels: expected {cnt}, found {len(vals)}")
+    return vals.astype(np.int32)
+
+
+def parse_ncells(owner_text: str) -> int:
+    m = re.search(r"nCells:\s*(\d+)", owner_text)
+    if not m:
+        raise ValueError("owner: the header note carries no nCells")
+    return int(m.group(1))
+
+
+def parse_boundary(text: str):
+    """[(type, nFaces, startFace)] from the reference's boundary file."""
+    out = []
+    for line in text.splitlines():
+        line = line.strip()
+        if not line or line.startswith("#"):
+            continue
+        t, cnt, start = line.split()
+        out.append((t, int(cnt), int(start)))
+    return out
+
+
+def read_polymesh(path: str) -> Mesh:
+    """The mesh of a polyMesh directory, with the reference's geometry and boundary
+    bookkeeping (mesh.polymesh_mesh)."""
+    def get(name):
+        with open(os.path.join(path, name)) as f:
+            return f.read()
+
+    owner_text = get("owner")
+    face_ptr, face_nodes = parse_faces(get("faces"))
+    patches = parse_boundary(get("boundary"))
+    return polymesh_mesh(parse_points(get("points")), face_ptr, face_nodes,
+                         parse_labels(owner_text), parse_labels(get("neighbour")),
+                         parse_ncells(owner_text), np.array([p[0] for p in patches]),
+                         np.array([p[1] for p in patches], np.int32),
+                         np.array([p[2] for p in patches], np.int32))
+
+
+_HEADER = """FoamFile
+{{
+    version     2.0;
+    format      ascii;
+    class       {cls};
+    note        "{note}";
+    location    "constant/polyMesh";
+    object      {obj};
+}}
+"""
+
+
+def write_polymesh(m: Mesh, path: str):
+    """Writes points, faces, owner, neighbour and boundary of a mesh that keeps its
+    topology (hex_mesh(..., keep_topology=True) or read_polymesh)."""
+    if m.points is None or m.face_ptr is None:
+        raise ValueError("the mesh keeps no points/faces (build it with keep_topology=True)")
+    os.makedirs(path, exist_ok=True)
+    note = f"nPoints:{len(m.points)} nCells:{m.numCells} nFaces:{m.numFaces} " \
+           f"nInternalFaces:{m.numInnerFaces}"
+
+    def write(name, cls, lines):
+        with open(os.path.join(path, name), "w") as f:
+            f.write(_HEADER.format(cls=cls, note=note, obj=name))
+            f.write(f"\n{len(lines)}\n(\n")
+            f.write("\n".join(lines))
+            f.write("\n)\n")
+
+    write("points", "vectorField", ["(%r %r %r)" % tuple(map(float, p)) for p in m.points])
+    fp, fn = m.face_ptr, m.face_nodes
+    write("faces", "faceList",
+          [f"{fp[i + 1] - fp[i]}(" + " ".join(str(int(v) - 1) for v in fn[fp[i]:fp[i + 1]]) + ")"
+           for i in range(len(fp) - 1)])
+    write("owner", "labelList", [str(int(v) - 1) for v in m.owner])
+    write("neighbour", "labelList", [str(int(v) - 1) for v in m.neighbour])
+    names = {"nsym": "symmetry", "nwal": "wall", "ninl": "inlet", "nout": "outlet",
+             "npru": "prOutlet"}
+    start_key = {"nsym": "iSymmetryFacesStart", "nwal": "iWallFacesStart",
+                 "ninl": "iInletFacesStart", "nout": "iOutletFacesStart",
+                 "npru": "iPressOutletFacesStart"}
+    rows = sorted((m.starts[start_key[k]], names[k], c) for k, c in m.counts.items() if c)
+    with open(os.path.join(path, "boundary"), "w") as f:
+        f.write("# type nFaces startFace\n")
+        for st, t, c in rows:
+            f.write(f"{t} {c} {st}\n")
