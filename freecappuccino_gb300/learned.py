@@ -252,6 +252,31 @@ def dpcg_pairs(sysm: TrainingSystem, ks, tight: float = 1e-13, nsw_max: int = 20
     return out
 
 
+def save_pairs(path: str, pairs, meta: dict | None = None):
+    """One training-data shard: the (r, e) pairs of one system as FP32 arrays r[k], e[k]
+    in an .npz, with optional scalar metadata (mesh size, seed, jitter, ...)."""
+    def host(x):
+        return x.detach().cpu().numpy() if _is_torch(x) else np.asarray(x, np.float32)
+
+    r = np.stack([host(a) for a, _ in pairs]).astype(np.float32)
+    e = np.stack([host(b) for _, b in pairs]).astype(np.float32)
+    np.savez(path, r=r, e=e, **{f"meta_{k}": np.asarray(v) for k, v in (meta or {}).items()})
+
+
+def load_pairs(path: str, device=None):
+    """(pairs, meta) of a shard written by save_pairs; CUDA tensors when `device` is given."""
+    d = np.load(path)
+    pairs = []
+    for r, e in zip(d["r"], d["e"]):
+        if device is not None:
+            import torch
+
+            r, e = torch.from_numpy(r).to(device), torch.from_numpy(e).to(device)
+        pairs.append((r, e))
+    meta = {k[5:]: d[k].item() for k in d.files if k.startswith("meta_")}
+    return pairs, meta
+
+
 def train(lp: LearnedPreconditioner, systems, pairs, steps: int, lr: float = 1e-3, seed: int = 0,
           log_every: int = 0, log=print):
     """Adam on the pairs: `pairs[i]` is a list of (r, e) for `systems[i]`; each step

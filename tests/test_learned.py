@@ -98,6 +98,20 @@ def test_oracle_features_of_uniform_cube_are_zero():
     assert np.abs(f[nbf > 0, 1]).max() > 0.1
 
 
+def test_training_shard_round_trip(tmp_path):
+    from freecappuccino_gb300.learned import load_pairs, save_pairs
+
+    rng = np.random.default_rng(4)
+    pairs = [(rng.standard_normal(50).astype(np.float32), rng.standard_normal(50).astype(np.float32))
+             for _ in range(3)]
+    path = str(tmp_path / "shard.npz")
+    save_pairs(path, pairs, {"N": 64, "seed": 7, "jitter": 0.125})
+    back, meta = load_pairs(path)
+    assert meta == {"N": 64, "seed": 7, "jitter": 0.125}
+    for (r0, e0), (r1, e1) in zip(pairs, back):
+        assert np.array_equal(r0, r1) and np.array_equal(e0, e1)
+
+
 # ----------------------------------------------------------------------------- GPU
 def _gpu_system(N, seed=3, variable=True):
     from freecappuccino_gb300.learned import pressure_system
