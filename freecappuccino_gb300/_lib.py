@@ -74,6 +74,8 @@ _PROTOS = {
     "fcg_facefluxmass": (C.c_int, [_CTX, C.POINTER(FlowFields), _vp, _vp, _vp]),
     "fcg_fluxmc": (C.c_int, [_CTX, _vp, _vp, _vp, _vp, _vp]),
     "fcg_flux_correct": (C.c_int, [_CTX, _vp, _vp, _vp]),
+    "fcg_correct_bc_velocity": (C.c_int, [_CTX, _vp, C.c_double, _vp, _vp, _vp, _vp]),
+    "fcg_continuity_errors": (C.c_int, [_CTX, _vp, _vp, _vp, _vp, _dp, _dp]),
     "fcg_correct_fields": (C.c_int, [_CTX, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_int, _vp,
                                      _vp, _vp, _vp]),
     "fcg_grad": (C.c_int, [_CTX, _vp, _vp, C.c_int, C.c_int]),

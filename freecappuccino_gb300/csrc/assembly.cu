@@ -12,6 +12,8 @@
 // This file is compiled with --fmad=false: every a*b+c below is a rounded multiply
 // followed by a rounded add, as gfortran evaluates it, so the coefficients are
 // bit-identical to the reference's loop on the same inputs.
+#include <algorithm>
+
 #include "fcg_internal.h"
 #include "launch.h"
 
@@ -326,8 +328,198 @@ __global__ void k_correct_fields(MeshView m, const double *__restrict__ g,
   }
 }
 
+// correctBoundaryConditionsVelocity.f90:20-57, outlet part one: one thread walks the
+// outlet faces in order (flowo is summed in the reference's order), then fac.
+__global__ void k_cbv_outlet(MeshView m, int nout, int fst, int bst, const double *__restrict__ den,
+                             double flomas, double small, double *__restrict__ u,
+                             double *__restrict__ v, double *__restrict__ w,
+                             double *__restrict__ fmo, double *__restrict__ fac) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  double flowo = 0.0;
+  for (int i = 0; i < nout; ++i) {
+    const int f = fst + i, P = m.owner[f], b = bst + i;
+    u[b] = u[P];
+    v[b] = v[P];
+    w[b] = w[P];
+    fmo[i] = den[P] * (u[b] * m.arx[f] + v[b] * m.ary[f] + w[b] * m.arz[f]);
+    flowo = flowo + fmo[i];
+  }
+  fac[0] = flomas / (flowo + small);
+}
+
+// outlet part two (:45-57): fmo and the outlet velocities times fac
+__global__ void k_cbv_scale(int nout, int bst, const double *__restrict__ fac,
+                            double *__restrict__ u, double *__restrict__ v, double *__restrict__ w,
+                            double *__restrict__ fmo) {
+  const double f = fac[0];
+  FCG_GRID_STRIDE(i, nout) {
+    const int b = bst + (int)i;
+    fmo[i] = fmo[i] * f;
+    u[b] = u[b] * f;
+    v[b] = v[b] * f;
+    w[b] = w[b] * f;
+  }
+}
+
+// symmetry faces (:60-76): the cell velocity minus (u.S) S, S the area vector
+__global__ void k_cbv_sym(MeshView m, int nsym, int fst, int bst, double *__restrict__ u,
+                          double *__restrict__ v, double *__restrict__ w) {
+  FCG_GRID_STRIDE(i, nsym) {
+    const int f = fst + (int)i, P = m.owner[f], b = bst + (int)i;
+    const double un = u[P] * m.arx[f] + v[P] * m.ary[f] + w[P] * m.arz[f];
+    u[b] = u[P] - un * m.arx[f];
+    v[b] = v[P] - un * m.ary[f];
+    w[b] = w[P] - un * m.arz[f];
+  }
+}
+
+// continuityErrors.h:7-41 per cell, in the reference's order: the inner faces in face
+// order (res(ijp) -= flmass(ijp), res(ijn) += flmass(ijp) -- flmass indexed by the
+// owner cell, as the reference does), then the inlet and outlet faces.
+__global__ void k_contin_cells(MeshView m, const double *__restrict__ flmass,
+                               const double *__restrict__ fmi, const double *__restrict__ fmo,
+                               int bst_inl, int bst_out, double *__restrict__ res) {
+  FCG_GRID_STRIDE(c, m.n) {
+    double r = 0.0;
+    for (int e = m.cf_ptr[c]; e < m.cf_ptr[c + 1]; ++e) {
+      const int ent = m.cf_ent[e];
+      if (ent > 0)
+        r = r - flmass[c];
+      else
+        r = r + flmass[m.owner[-ent - 1]];
+    }
+    for (int e = m.cb_ptr[c]; e < m.cb_ptr[c + 1]; ++e) {
+      const int t = m.cb_type[e];
+      if (t == B_INLET) r = r - fmi[m.cb_slot[e] - bst_inl];
+      else if (t == B_OUTLET) r = r - fmo[m.cb_slot[e] - bst_out];
+    }
+    res[c] = r;
+  }
+}
+
+// sum|res| and sum res: per-block partials (fixed thread order), then one block adds
+// them in block order
+__global__ void k_contin_part(int n, const double *__restrict__ res, double *__restrict__ part) {
+  __shared__ double sh[2][kTPB];
+  double a = 0.0, b = 0.0;
+  FCG_GRID_STRIDE(i, n) {
+    a += fabs(res[i]);
+    b += res[i];
+  }
+  sh[0][threadIdx.x] = a;
+  sh[1][threadIdx.x] = b;
+  __syncthreads();
+  for (int s = kTPB / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + s];
+      sh[1][threadIdx.x] += sh[1][threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = sh[0][0];
+    part[2 * blockIdx.x + 1] = sh[1][0];
+  }
+}
+
+__global__ void k_contin_total(int nblocks, const double *__restrict__ part,
+                               double *__restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double a = 0.0, b = 0.0;
+  for (int k = 0; k < nblocks; ++k) {
+    a += part[2 * k];
+    b += part[2 * k + 1];
+  }
+  out[0] = a;
+  out[1] = b;
+}
+
 }  // namespace corr
 }  // namespace fcg
+
+extern "C" int fcg_correct_bc_velocity(fcg_context *c, const double *den, double flomas,
+                                       double *u, double *v, double *w, double *fmo) {
+  if (!c) return FCG_ERR_ARG;
+  if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_correct_bc_velocity before fcg_bind_mesh");
+  if (!den || !u || !v || !w || (!fmo && c->cnt[B_OUTLET] > 0))
+    return set_error(c, FCG_ERR_ARG, "NULL array");
+  FCG_CUDA_TRY(c, cudaSetDevice(c->device));
+  const size_t nt = sizeof(double) * c->ntot;
+  const int nout = c->cnt[B_OUTLET], nsym = c->cnt[B_SYMMETRY];
+  void *dden, *du, *dv, *dw, *dfmo = nullptr;
+  bool hden, hu, hv, hw, hfmo = false;
+  int rc;
+  if ((rc = stage_in(c, den, nt, 0, true, &dden, &hden))) return rc;
+  if ((rc = stage_in(c, u, nt, 1, true, &du, &hu))) return rc;
+  if ((rc = stage_in(c, v, nt, 2, true, &dv, &hv))) return rc;
+  if ((rc = stage_in(c, w, nt, 3, true, &dw, &hw))) return rc;
+  if (nout > 0 && (rc = stage_in(c, fmo, sizeof(double) * nout, 4, false, &dfmo, &hfmo))) return rc;
+  FCG_CUDA_TRY(c, c->scratch.ensure(sizeof(double) * 8));
+  if (nout > 0) {
+    fcg::corr::k_cbv_outlet<<<1, 32, 0, c->stream>>>(
+        c->mv, nout, c->fst[B_OUTLET], c->bst[B_OUTLET], (const double *)dden, flomas,
+        (double)1e-20f /* parameters::small, modules_allocatable.f90:27 */, (double *)du,
+        (double *)dv, (double *)dw, (double *)dfmo, c->scratch.as<double>());
+    fcg::corr::k_cbv_scale<<<grid_for(nout, c->num_sms), kTPB, 0, c->stream>>>(
+        nout, c->bst[B_OUTLET], c->scratch.as<double>(), (double *)du, (double *)dv,
+        (double *)dw, (double *)dfmo);
+  }
+  if (nsym > 0)
+    fcg::corr::k_cbv_sym<<<grid_for(nsym, c->num_sms), kTPB, 0, c->stream>>>(
+        c->mv, nsym, c->fst[B_SYMMETRY], c->bst[B_SYMMETRY], (double *)du, (double *)dv,
+        (double *)dw);
+  FCG_CHECK_LAUNCH(c, "correct_bc_velocity");
+  bool any = hu || hv || hw || hfmo;
+  if ((rc = stage_out(c, u, du, nt, hu)) || (rc = stage_out(c, v, dv, nt, hv)) ||
+      (rc = stage_out(c, w, dw, nt, hw)))
+    return rc;
+  if (nout > 0 && (rc = stage_out(c, fmo, dfmo, sizeof(double) * nout, hfmo))) return rc;
+  if (any) FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return FCG_OK;
+}
+
+extern "C" int fcg_continuity_errors(fcg_context *c, const double *flmass, const double *fmi,
+                                     const double *fmo, double *res, double *sum_local,
+                                     double *global) {
+  if (!c) return FCG_ERR_ARG;
+  if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_continuity_errors before fcg_bind_mesh");
+  if (!flmass || (!fmi && c->cnt[B_INLET] > 0) || (!fmo && c->cnt[B_OUTLET] > 0))
+    return set_error(c, FCG_ERR_ARG, "NULL array");
+  if (c->n > c->nin)
+    return set_error(c, FCG_ERR_INDEX,
+                     "continuityErrors.h:14 indexes flmass by cell: needs numCells <= numInnerFaces");
+  FCG_CUDA_TRY(c, cudaSetDevice(c->device));
+  const int nin_ = c->cnt[B_INLET], nout = c->cnt[B_OUTLET];
+  void *dfm, *dfmi = nullptr, *dfmo = nullptr, *dres;
+  bool h0, h1 = false, h2 = false, hres = false;
+  int rc;
+  if ((rc = stage_in(c, flmass, sizeof(double) * c->nin, 0, true, &dfm, &h0))) return rc;
+  if (nin_ > 0 && (rc = stage_in(c, fmi, sizeof(double) * nin_, 1, true, &dfmi, &h1))) return rc;
+  if (nout > 0 && (rc = stage_in(c, fmo, sizeof(double) * nout, 2, true, &dfmo, &h2))) return rc;
+  const size_t n1 = sizeof(double) * c->n;
+  const int G = std::min(grid_for(c->n, c->num_sms), 1024);
+  // scratch: block partials, the two totals and, without a caller array, res itself
+  FCG_CUDA_TRY(c, c->scratch.ensure(sizeof(double) * (2 * 1024 + 8 + (res ? 0 : c->n))));
+  double *part = c->scratch.as<double>(), *tot = part + 2 * 1024;
+  if (res) {
+    if ((rc = stage_in(c, res, n1, 3, false, &dres, &hres))) return rc;
+  } else {
+    dres = tot + 8;
+  }
+  fcg::corr::k_contin_cells<<<grid_for(c->n, c->num_sms), kTPB, 0, c->stream>>>(
+      c->mv, (const double *)dfm, (const double *)dfmi, (const double *)dfmo, c->bst[B_INLET],
+      c->bst[B_OUTLET], (double *)dres);
+  fcg::corr::k_contin_part<<<G, kTPB, 0, c->stream>>>(c->n, (const double *)dres, part);
+  fcg::corr::k_contin_total<<<1, 32, 0, c->stream>>>(G, part, tot);
+  FCG_CHECK_LAUNCH(c, "continuity_errors");
+  double h[2];
+  FCG_CUDA_TRY(c, cudaMemcpyAsync(h, tot, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+  if (res && (rc = stage_out(c, res, dres, n1, hres))) return rc;
+  FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (sum_local) *sum_local = h[0];
+  if (global) *global = h[1];
+  return FCG_OK;
+}
 
 extern "C" int fcg_flux_correct(fcg_context *c, const double *a, const double *pp,
                                 double *flmass) {

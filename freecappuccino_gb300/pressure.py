@@ -197,6 +197,31 @@ class Context:
                     "fcg_correct_fields")
         return tuple(outs)
 
+    def correct_bc_velocity(self, den, flomas, u, v, w):
+        """correctBoundaryConditionsVelocity: returns (u, v, w, fmo)."""
+        self._follow(den, u, v, w)
+        den = _host(den)
+        outs = [x.clone() if _is_torch(x) else np.array(x, dtype=np.float64) for x in (u, v, w)]
+        nout = self.mesh.counts.get("nout", 0)
+        fmo = _like(den, max(nout, 1))
+        self._check(self.lib.fcg_correct_bc_velocity(self.h, _ptr(den), float(flomas),
+                                                     *[_ptr(x) for x in outs], _ptr(fmo)),
+                    "fcg_correct_bc_velocity")
+        return (*outs, fmo[:nout])
+
+    def continuity_errors(self, flmass, fmi, fmo):
+        """continuityErrors.h: returns (res, sumLocalContErr, globalContErr)."""
+        self._follow(flmass, fmi, fmo)
+        flmass = _host(flmass)
+        fmi = _host(fmi) if len(fmi) else _like(flmass, 1)
+        fmo = _host(fmo) if len(fmo) else _like(flmass, 1)
+        res = _like(flmass, self.n)
+        sl, sg = C.c_double(), C.c_double()
+        self._check(self.lib.fcg_continuity_errors(self.h, _ptr(flmass), _ptr(fmi), _ptr(fmo),
+                                                   _ptr(res), C.byref(sl), C.byref(sg)),
+                    "fcg_continuity_errors")
+        return res, sl.value, sg.value
+
     def grad(self, phi, option: str = "gauss", nigrad: int = 1, dphidxi=None):
         """grad(phi,dPhidxi[,option]) without limiter: returns dPhidxi as (n, 3)."""
         self._follow(phi, dphidxi)

@@ -146,6 +146,22 @@ int fcg_correct_fields(fcg_context *ctx, const double *dPdxi, const double *apu,
                        const double *apv, const double *apw, const double *pp, double urf,
                        int pRefCell, double *u, double *v, double *w, double *p);
 
+/* correctBoundaryConditionsVelocity.f90:1-80: outlet slots of u, v, w take their cell's
+ * value, fmo(i) = den(ijp) (u,v,w)(ijb).S, the outflow is scaled to flomas
+ * (fac = flomas/(sum fmo + small), fmo and the outlet velocities times fac), symmetry
+ * slots take the cell velocity minus ((u,v,w)(ijp).S) S with S the area vector (as the
+ * reference does).  u, v, w, den [numTotal]; fmo[nout] out (may be NULL without outlets). */
+int fcg_correct_bc_velocity(fcg_context *ctx, const double *den, double flomas, double *u,
+                            double *v, double *w, double *fmo);
+
+/* continuityErrors.h:1-52: res(numCells) = the divergence of the mass fluxes -- per inner
+ * face res(ijp) -= flmass(ijp), res(ijn) += flmass(ijp), with flmass indexed by the owner
+ * cell as the reference does (so numCells <= numInnerFaces is required, FCG_ERR_INDEX
+ * otherwise) -- minus fmi over inlet and fmo over outlet faces; *sum_local = sum|res|,
+ * *global = sum res (deterministic order; res may be NULL). */
+int fcg_continuity_errors(fcg_context *ctx, const double *flmass, const double *fmi,
+                          const double *fmo, double *res, double *sum_local, double *global);
+
 /* ---------------------------------------------------------------------------
  * Gradients and boundary values.
  * ------------------------------------------------------------------------- */

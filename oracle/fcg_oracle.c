@@ -845,3 +845,72 @@ int orc_correct_fields(const orc_mesh *m, const double *dPdxi, const double *apu
   }
   return 0;
 }
+
+/* correctBoundaryConditionsVelocity.f90:1-80: outlet slots take their cell's velocity,
+ * fmo(i) = den(ijp) (u,v,w)(ijb).S, flowo = sum fmo, fac = flomas/(flowo+small), then
+ * fmo and the outlet velocities are scaled by fac; symmetry slots take the cell velocity
+ * minus Unmag S with Unmag = (u,v,w)(ijp).S (the area vector, as the reference does). */
+int orc_correct_bc_velocity(const orc_mesh *m, const double *den, double flomas, double *u,
+                            double *v, double *w, double *fmo) {
+  const double small = orc_const_small_src();
+  double flowo = 0.0;
+  for (int i = 1; i <= m->nout; ++i) {
+    const int iface = m->iOutletFacesStart + i, ijp = F(m->owner, iface);
+    const int ijb = iOutletStart(m) + i;
+    F(u, ijb) = F(u, ijp);
+    F(v, ijb) = F(v, ijp);
+    F(w, ijb) = F(w, ijp);
+    F(fmo, i) = F(den, ijp) * (F(u, ijb) * F(m->arx, iface) + F(v, ijb) * F(m->ary, iface) +
+                               F(w, ijb) * F(m->arz, iface));
+    flowo = flowo + F(fmo, i);
+  }
+  const double fac = flomas / (flowo + small);
+  for (int i = 1; i <= m->nout; ++i) {
+    const int ijb = iOutletStart(m) + i;
+    F(fmo, i) = F(fmo, i) * fac;
+    F(u, ijb) = F(u, ijb) * fac;
+    F(v, ijb) = F(v, ijb) * fac;
+    F(w, ijb) = F(w, ijb) * fac;
+  }
+  for (int i = 1; i <= m->nsym; ++i) {
+    const int iface = m->iSymmetryFacesStart + i, ijp = F(m->owner, iface);
+    const int ijb = iSymmetryStart(m) + i;
+    const double unmag = F(u, ijp) * F(m->arx, iface) + F(v, ijp) * F(m->ary, iface) +
+                         F(w, ijp) * F(m->arz, iface);
+    F(u, ijb) = F(u, ijp) - unmag * F(m->arx, iface);
+    F(v, ijb) = F(v, ijp) - unmag * F(m->ary, iface);
+    F(w, ijb) = F(w, ijp) - unmag * F(m->arz, iface);
+  }
+  return 0;
+}
+
+/* continuityErrors.h:1-52: res = 0; per inner face res(ijp) -= flmass(ijp),
+ * res(ijn) += flmass(ijp) -- the reference indexes flmass by the owner CELL here, which
+ * is kept; then res(owner) -= fmi(i) over inlet faces and -= fmo(i) over outlet faces;
+ * sumLocalContErr = sum|res|, globalContErr = sum res (in cell order). */
+int orc_continuity_errors(const orc_mesh *m, const double *flmass, const double *fmi,
+                          const double *fmo, double *res, double *sum_local, double *global) {
+  if (m->numCells > m->numInnerFaces) return -4;
+  for (int i = 1; i <= m->numCells; ++i) F(res, i) = 0.0;
+  for (int i = 1; i <= m->numInnerFaces; ++i) {
+    const int ijp = F(m->owner, i), ijn = F(m->neighbour, i);
+    F(res, ijp) = F(res, ijp) - F(flmass, ijp);
+    F(res, ijn) = F(res, ijn) + F(flmass, ijp);
+  }
+  for (int i = 1; i <= m->ninl; ++i) {
+    const int ijp = F(m->owner, m->iInletFacesStart + i);
+    F(res, ijp) = F(res, ijp) - F(fmi, i);
+  }
+  for (int i = 1; i <= m->nout; ++i) {
+    const int ijp = F(m->owner, m->iOutletFacesStart + i);
+    F(res, ijp) = F(res, ijp) - F(fmo, i);
+  }
+  double sl = 0.0, sg = 0.0;
+  for (int i = 1; i <= m->numCells; ++i) {
+    sl = sl + fabs(F(res, i));
+    sg = sg + F(res, i);
+  }
+  *sum_local = sl;
+  *global = sg;
+  return 0;
+}

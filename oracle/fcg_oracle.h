@@ -91,6 +91,10 @@ int orc_bpres(const orc_mesh *m, double *p /*[numTotal]*/, const double *dPdxi, 
 /* --- calcp corrections: calcp-multiple_correction_SIMPLE.f90:159-171 and :184-189 --- */
 int orc_flux_correct(const orc_mesh *m, const int *slot_pn, const double *a, const double *pp,
                      double *flmass);
+int orc_correct_bc_velocity(const orc_mesh *m, const double *den, double flomas, double *u,
+                            double *v, double *w, double *fmo);
+int orc_continuity_errors(const orc_mesh *m, const double *flmass, const double *fmi,
+                          const double *fmo, double *res, double *sum_local, double *global);
 int orc_correct_fields(const orc_mesh *m, const double *dPdxi, const double *apu,
                        const double *apv, const double *apw, const double *pp, double urf,
                        int pRefCell, double *u, double *v, double *w, double *p);

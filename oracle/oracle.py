@@ -219,6 +219,26 @@ def correct_fields(m: Mesh, dPdxi, apu, apv, apw, pp, urf, pRefCell, u, v, w, p)
     return u, v, w, p
 
 
+def correct_bc_velocity(m: Mesh, den, flomas, u, v, w):
+    """correctBoundaryConditionsVelocity.f90:1-80: returns (u, v, w, fmo)."""
+    u, v, w = (_f64(x).copy() for x in (u, v, w))
+    fmo = np.zeros(max(m.struct.nout, 1))
+    assert lib().orc_correct_bc_velocity(C.byref(m.struct), _d(_f64(den)), C.c_double(flomas),
+                                         _d(u), _d(v), _d(w), _d(fmo)) == 0
+    return u, v, w, fmo[:m.struct.nout]
+
+
+def continuity_errors(m: Mesh, flmass, fmi, fmo):
+    """continuityErrors.h:1-52: returns (res, sumLocalContErr, globalContErr)."""
+    res = np.zeros(m.struct.numCells)
+    sl, sg = C.c_double(), C.c_double()
+    fmi = _f64(fmi) if len(fmi) else np.zeros(1)
+    fmo = _f64(fmo) if len(fmo) else np.zeros(1)
+    assert lib().orc_continuity_errors(C.byref(m.struct), _d(_f64(flmass)), _d(fmi), _d(fmo),
+                                       _d(res), C.byref(sl), C.byref(sg)) == 0
+    return res, sl.value, sg.value
+
+
 def grad_gauss(m: Mesh, phi, nigrad=1, corrected=False, dphidxi_in=None):
     """grad_gauss.f90 (nigrad passes) or grad_gauss_corrected.f90 (one pass, old = incoming)."""
     phi = _f64(phi)

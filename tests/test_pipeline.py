@@ -84,8 +84,6 @@ def test_calcp_pressure_step_matches_oracle(N, npcor):
     dp_g = g["p"][:n] - f["p"][:n]
     dp_o = o["p"][:n] - f["p"][:n]
     assert _rel(dp_g, dp_o) < 1e-8
-    # continuity after the correction: the corrected fluxes leave a residual divergence
-    # no larger than the p' solve's tolerance allows
     c.close()
 
 
@@ -129,3 +127,26 @@ def test_oracle_corrections_restate_the_loops():
     assert np.array_equal(u[:n], uvwp[0][:n] - g[:, 0] * m.vol * ap[0])
     assert np.array_equal(w[:n], uvwp[2][:n] - g[:, 2] * m.vol * ap[2])
     assert np.array_equal(p[:n], uvwp[3][:n] + 0.3 * (pp[:n] - pp[1]))
+
+
+@pytest.mark.gpu
+def test_boundary_velocity_and_continuity_errors_bit_exact():
+    """correctBoundaryConditionsVelocity and continuityErrors.h on the pitzDaily mesh
+    (inlet, outlet and walls) and a hex mesh (symmetry patches)."""
+    from tests.meshes import fixture_mesh
+
+    for m in (fixture_mesh("pitzdaily"), hex_mesh(8, 0.2)):
+        c = fcg.Context(m)
+        om = oracle_mesh(m)
+        f = seeded_fields(m, seed=5)
+        got = c.correct_bc_velocity(f["den"], 0.75, f["u"], f["v"], f["w"])
+        ref = oracle.correct_bc_velocity(om, f["den"], 0.75, f["u"], f["v"], f["w"])
+        for x, y in zip(got, ref):
+            assert np.array_equal(x, y)
+        flm = fcg.uniform(9, 1, m.numInnerFaces)
+        fmi = fcg.uniform(9, 2, m.counts.get("ninl", 0))
+        res, sl, sg = c.continuity_errors(flm, fmi, got[3])
+        res_o, sl_o, sg_o = oracle.continuity_errors(om, flm, fmi, ref[3])
+        assert np.array_equal(res, res_o)
+        assert sl == pytest.approx(sl_o, rel=1e-13) and sg == pytest.approx(sg_o, rel=1e-9, abs=1e-12)
+        c.close()
