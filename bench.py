@@ -321,8 +321,11 @@ def run_calcp(dev, N=128, npcor=3, seed=SEED + 1):
 
 def run_multi(dev, N=128, seed=SEED + 2):
     """The five transport systems (u, v, w, k, eps) on one pattern solved in one
-    multi-RHS BiCGStab (FP32 DILU inner, FP64 correction to 1e-10) against five FP64
-    BiCGStab solves one after another."""
+    multi-RHS BiCGStab (FP32 DILU inner, FP64 correction to 1e-10) against the same
+    solver run on the systems one after another.  (The reference's FP64 BiCGStab does not
+    reach 1e-10 here: with right-hand sides of order vol ~ 5e-7 its absolute small = 1e-20
+    in alf = (v.r)/(v.v + small) dominates v.v once the residual is small; 200 of its
+    sweeps are timed for the record.)"""
     import torch
 
     import freecappuccino_gb300 as fcg
@@ -341,16 +344,23 @@ def run_multi(dev, N=128, seed=SEED + 2):
     e1.record()
     torch.cuda.synchronize()
     t_multi = e0.elapsed_time(e1) * 1e-3
-    seq = [ctx.bicgstab(a_d[k], su_d[k], x0[k], 1e-10, 2000, want_res=False)
-           for k in range(a.shape[0])]
-    t_seq = sum(r.seconds for r in seq)
+    t_one = 0.0
+    for k in range(a.shape[0]):  # the same solver, one system per call
+        e0.record()
+        ctx.bicgstab_multi(a_d[k:k + 1], su_d[k:k + 1], x0[k:k + 1], 1e-10, 2000)
+        e1.record()
+        torch.cuda.synchronize()
+        t_one += e0.elapsed_time(e1) * 1e-3
+    ref = [ctx.bicgstab(a_d[k], su_d[k], x0[k], 1e-10, 200, want_res=False) for k in range(2)]
     ctx.close()
     return {"workload": f"5 transport systems (u, v, w, k, eps) on the {N}^3 jittered hex "
                         "pattern, BiCGStab(DILU) to 1e-10", "seconds": t_multi,
             "fp32_sweeps": [r.iters for r in reps], "all_converged": all(r.converged for r in reps),
-            "max_l2_rel": max(r.l2_rel for r in reps), "sequential_fp64_bicgstab_s": t_seq,
-            "sequential_iterations": [r.iters for r in seq],
-            "speedup_vs_sequential": t_seq / t_multi}
+            "max_l2_rel": max(r.l2_rel for r in reps), "one_system_per_call_s": t_one,
+            "speedup_vs_one_per_call": t_one / t_multi,
+            "reference_fp64_bicgstab_200_sweeps": [{"seconds": r.seconds, "converged": r.converged,
+                                                    "resl_over_res0": r.resl / r.res0}
+                                                   for r in ref]}
 
 
 def main():

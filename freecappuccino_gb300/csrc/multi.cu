@@ -31,6 +31,7 @@ struct MScal {
   double r0in[kMaxSys], rl[kMaxSys];    // inner residual L1: at the inner start, current
   double res0[kMaxSys], resl[kMaxSys];  // FP64 residual L1: first, latest
   double scale[kMaxSys];  // the inner solve works on r / scale (entries of order one)
+  double l2r[kMaxSys], l2b[kMaxSys];    // final FP64 ||su - A x||^2 and ||su||^2
   double small, resmax, inner_tol;
   int active[kMaxSys], conv[kMaxSys];
   int iter, inner_iter, inner_max, nsw, idone, status, any_active, pad;
@@ -158,6 +159,35 @@ __global__ void __launch_bounds__(kTPB, 4)
 
 // r = rh = (FP64 residual) / scale, in FP32: the inner solve sees entries of order one,
 // so the reference's absolute `small` stays negligible however far the outer loop got.
+// Final FP64 check per system: ||su - A x||^2 and ||su||^2.
+template <int NS>
+__global__ void __launch_bounds__(kTPB, 4)
+    k_m_final(SellView s, int n, long long len, const double *__restrict__ sv64,
+              const double *__restrict__ su, const double *__restrict__ x, MScal *S,
+              double *partials) {
+  double v[2 * NS];
+#pragma unroll
+  for (int k = 0; k < 2 * NS; ++k) v[k] = 0.0;
+  FCG_SLICE_LOOP(slice, lane, s) {
+    const int row = slice * 32 + lane;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const double ax = sell_row(s, n, sv64 + k * len, x + (long long)k * n, slice, lane);
+      if (row < n) {
+        const long long o = (long long)k * n + row;
+        const double rr = su[o] - ax;
+        v[k] += rr * rr;
+        v[NS + k] += su[o] * su[o];
+      }
+    }
+  }
+  if (reduce_commit<2 * NS>(v, partials, &S->ticket[5]) && threadIdx.x == 0)
+    for (int k = 0; k < NS; ++k) {
+      S->l2r[k] = v[k];
+      S->l2b[k] = v[NS + k];
+    }
+}
+
 template <int NS>
 __global__ void k_m_normalise(int n, const double *__restrict__ x_res, float *__restrict__ r,
                               float *__restrict__ rh, const MScal *S) {
@@ -522,6 +552,9 @@ int solve_multi(fcg_context *c, const double *da, const double *dsu, double *dfi
     Launch<NS>::correct(c);
     FCG_CHECK_LAUNCH(c, "k_m_correct");
   }
+  k_m_final<NS><<<m->G, kTPB, 0, c->stream>>>(c->sv, m->n, m->len, m->sv64, m->su, m->x, m->S,
+                                             m->partials);
+  FCG_CHECK_LAUNCH(c, "k_m_final");
   FCG_CUDA_TRY(c, cudaMemcpyAsync(dfi, m->x, nb, cudaMemcpyDeviceToDevice, c->stream));
   FCG_CUDA_TRY(c, cudaMemcpyAsync(m->hS, m->S, sizeof(MScal), cudaMemcpyDeviceToHost, c->stream));
   FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
@@ -533,7 +566,7 @@ int solve_multi(fcg_context *c, const double *da, const double *dsu, double *dfi
       rep[k].resl = S.resl[k];
       rep[k].iters = S.iter;
       rep[k].converged = S.conv[k];
-      rep[k].l2_rel = -1.0;
+      rep[k].l2_rel = S.l2b[k] > 0 ? std::sqrt(S.l2r[k] / S.l2b[k]) : std::sqrt(S.l2r[k]);
       rep[k].seconds = 0.0;
     }
   }

@@ -286,6 +286,9 @@ def test_multi_rhs_bicgstab_matches_oracle(name):
         r_true = su[k] - oracle.spmv(csr, a[k], x[k])
         assert reps[k].converged
         assert np.abs(r_true).sum() / reps[k].res0 < 1e-10
+        # the reported FP64 norm is that of the returned solution
+        l2 = np.linalg.norm(r_true) / np.linalg.norm(su[k])
+        assert reps[k].l2_rel == pytest.approx(l2, rel=1e-6, abs=1e-15)
         assert reps[k].res0 == pytest.approx(o.res0, rel=1e-12)
         assert rel(x[k], o.fi) < 1e-8
 
