@@ -48,6 +48,19 @@ class FlowFields(C.Structure):
                                    "apu", "apv", "apw", "den")]
 
 
+class HbyaParams(C.Structure):
+    """fcg_hbya_params: the parameters get_rAU_x_UEqnH reads."""
+    _fields_ = [("timestep", C.c_double), ("btime", C.c_double), ("bdf", C.c_int),
+                ("cn", C.c_int), ("buoyancy", C.c_int), ("boussinesq", C.c_int),
+                ("beta", C.c_double), ("densit", C.c_double), ("tref", C.c_double),
+                ("gravx", C.c_double), ("gravy", C.c_double), ("gravz", C.c_double)]
+
+
+class HbyaFields(C.Structure):
+    _fields_ = [(k, _vp) for k in ("den", "t", "uo", "vo", "wo", "uoo", "voo", "woo",
+                                   "apu", "apv", "apw")]
+
+
 class SolveReport(C.Structure):
     _fields_ = [("res0", C.c_double), ("resl", C.c_double), ("iters", C.c_int),
                 ("converged", C.c_int), ("l2_rel", C.c_double), ("seconds", C.c_double)]
@@ -78,6 +91,12 @@ _PROTOS = {
     "fcg_continuity_errors": (C.c_int, [_CTX, _vp, _vp, _vp, _vp, _dp, _dp]),
     "fcg_correct_fields": (C.c_int, [_CTX, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_int, _vp,
                                      _vp, _vp, _vp]),
+    "fcg_piso_hbya": (C.c_int, [_CTX, C.POINTER(HbyaParams), C.POINTER(HbyaFields), _vp, _vp,
+                                _vp, _vp, _vp, _vp, _vp]),
+    "fcg_facefluxmass_piso": (C.c_int, [_CTX, C.POINTER(FlowFields), _vp, _vp, _vp]),
+    "fcg_adjust_mass_flow": (C.c_int, [_CTX, _vp, C.c_double, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "fcg_set_reference_pressure": (C.c_int, [_CTX, C.c_int, _vp, _vp, _vp]),
+    "fcg_correct_velocity_piso": (C.c_int, [_CTX, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "fcg_grad": (C.c_int, [_CTX, _vp, _vp, C.c_int, C.c_int]),
     "fcg_grad_lsq_matrix": (C.c_int, [_CTX, _vp]),
     "fcg_bpres": (C.c_int, [_CTX, _vp, _vp, C.c_int]),

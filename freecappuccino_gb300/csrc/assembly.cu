@@ -144,6 +144,33 @@ __global__ void k_ffm_cells(MeshView m, const double *__restrict__ flmass, doubl
 }
 
 // ---------------------------------------------------------------------------
+// facefluxmass_piso inside the PISO corrector (PISO_multiple_correction.f90:116-148)
+// ---------------------------------------------------------------------------
+__global__ void k_ffp_faces(MeshView m, FlowView fl, double *__restrict__ a,
+                            double *__restrict__ flmass) {
+  FCG_GRID_STRIDE(f, m.nin) {
+    int p = m.owner[f], q = m.neighbour[f];
+    double xf = m.xf[f], yf = m.yf[f], zf = m.zf[f];
+    double arx = m.arx[f], ary = m.ary[f], arz = m.arz[f];
+    double fxn = m.facint[f];  // facefluxmass.f90:325-326
+    double fxp = 1.0 - fxn;
+    double xpn = m.xc[q] - m.xc[p], ypn = m.yc[q] - m.yc[p], zpn = m.zc[q] - m.zc[p];
+    double dpn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);  // :334
+    double are = sqrt(arx * arx + ary * ary + arz * arz);  // :337
+    double dene = fl.den[p] * fxp + fl.den[q] * fxn;       // :340
+    // :343, cap = -dene*(...)*are/dpn; can = cap
+    double cap =
+        -(dene * (fxp * m.vol[p] * fl.apu[p] + fxn * m.vol[q] * fl.apu[q]) * are / dpn);
+    double ui = face_value_central(m, p, q, xf, yf, zf, fl.u, fl.dU);  // :349-351
+    double vi = face_value_central(m, p, q, xf, yf, zf, fl.v, fl.dV);
+    double wi = face_value_central(m, p, q, xf, yf, zf, fl.w, fl.dW);
+    flmass[f] = dene * (ui * arx + vi * ary + wi * arz);  // :356
+    a[m.slot_pn[f]] = cap;                                // PISO :126-131
+    a[m.slot_np[f]] = cap;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // fluxmc inside calcp :193-206
 // ---------------------------------------------------------------------------
 __global__ void k_fmc_faces(MeshView m, const double *__restrict__ dP,
@@ -253,6 +280,46 @@ extern "C" int fcg_facefluxmass(fcg_context *c, const fcg_flow_fields *f, double
                                                                         (double *)dfm);
     FCG_CHECK_LAUNCH(c, "k_ffm_faces");
   }
+  k_ffm_cells<<<grid_for(m.n, c->num_sms), kTPB, 0, c->stream>>>(m, (const double *)dfm,
+                                                                    (double *)da, (double *)dsu);
+  FCG_CHECK_LAUNCH(c, "k_ffm_cells");
+  if ((rc = stage_out(c, a, da, sizeof(double) * c->nnz, ha))) return rc;
+  if ((rc = stage_out(c, su, dsu, n1, hsu))) return rc;
+  if ((rc = stage_out(c, flmass, dfm, sizeof(double) * c->nin, hfm))) return rc;
+  if (ha || hsu || hfm) FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return FCG_OK;
+}
+
+extern "C" int fcg_facefluxmass_piso(fcg_context *c, const fcg_flow_fields *f, double *a,
+                                     double *su, double *flmass) {
+  if (!c || !f) return FCG_ERR_ARG;
+  if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_facefluxmass_piso before fcg_bind_mesh");
+  FCG_CUDA_TRY(c, cudaSetDevice(c->device));
+  const size_t nt = sizeof(double) * c->ntot, n1 = sizeof(double) * c->n, n3 = 3 * n1;
+  // the fields facefluxmass_piso reads (facefluxmass.f90:300-302)
+  const double *src[8] = {f->u, f->v, f->w, f->dUdxi, f->dVdxi, f->dWdxi, f->apu, f->den};
+  const size_t bytes[8] = {nt, nt, nt, n3, n3, n3, n1, nt};
+  void *dev[8];
+  bool host[8];
+  int rc;
+  for (int i = 0; i < 8; ++i)
+    if ((rc = stage_in(c, src[i], bytes[i], i, true, &dev[i], &host[i]))) return rc;
+  void *da, *dsu, *dfm;
+  bool ha, hsu, hfm;
+  if ((rc = stage_in(c, a, sizeof(double) * c->nnz, 12, false, &da, &ha))) return rc;
+  if ((rc = stage_in(c, su, n1, 13, false, &dsu, &hsu))) return rc;
+  if ((rc = stage_in(c, flmass, sizeof(double) * (c->nin > 0 ? c->nin : 1), 14, false, &dfm, &hfm)))
+    return rc;
+  FlowView fl{(const double *)dev[0], (const double *)dev[1], (const double *)dev[2], nullptr,
+              (const double *)dev[3], (const double *)dev[4], (const double *)dev[5], nullptr,
+              (const double *)dev[6], nullptr, nullptr, (const double *)dev[7]};
+  const MeshView &m = c->mv;
+  if (m.nin > 0) {
+    k_ffp_faces<<<grid_for(m.nin, c->num_sms), kTPB, 0, c->stream>>>(m, fl, (double *)da,
+                                                                        (double *)dfm);
+    FCG_CHECK_LAUNCH(c, "k_ffp_faces");
+  }
+  // a = 0, su = 0 (PISO :109-110), then the diagonal and su in face order (:133-146)
   k_ffm_cells<<<grid_for(m.n, c->num_sms), kTPB, 0, c->stream>>>(m, (const double *)dfm,
                                                                     (double *)da, (double *)dsu);
   FCG_CHECK_LAUNCH(c, "k_ffm_cells");
@@ -434,6 +501,24 @@ __global__ void k_contin_total(int nblocks, const double *__restrict__ part,
   out[1] = b;
 }
 
+// The outlet part shared by correctBoundaryConditionsVelocity (:20-57) and adjustMassFlow
+// (adjustMassFlow.f90:30-63): outlet slots take their cell's velocity, fmo, the sequential
+// outflow sum, fac, and fmo and the outlet velocities times fac.  fac lands in scratch[0].
+int outlet_flow(fcg_context *c, const double *den, double flomas, double *u, double *v,
+                double *w, double *fmo) {
+  const int nout = c->cnt[B_OUTLET];
+  if (nout <= 0) return FCG_OK;
+  FCG_CUDA_TRY(c, c->scratch.ensure(sizeof(double) * 8));
+  k_cbv_outlet<<<1, 32, 0, c->stream>>>(
+      c->mv, nout, c->fst[B_OUTLET], c->bst[B_OUTLET], den, flomas,
+      (double)1e-20f /* parameters::small, modules_allocatable.f90:27 */, u, v, w, fmo,
+      c->scratch.as<double>());
+  k_cbv_scale<<<grid_for(nout, c->num_sms), kTPB, 0, c->stream>>>(
+      nout, c->bst[B_OUTLET], c->scratch.as<double>(), u, v, w, fmo);
+  FCG_CHECK_LAUNCH(c, "outlet_flow");
+  return FCG_OK;
+}
+
 }  // namespace corr
 }  // namespace fcg
 
@@ -454,16 +539,9 @@ extern "C" int fcg_correct_bc_velocity(fcg_context *c, const double *den, double
   if ((rc = stage_in(c, v, nt, 2, true, &dv, &hv))) return rc;
   if ((rc = stage_in(c, w, nt, 3, true, &dw, &hw))) return rc;
   if (nout > 0 && (rc = stage_in(c, fmo, sizeof(double) * nout, 4, false, &dfmo, &hfmo))) return rc;
-  FCG_CUDA_TRY(c, c->scratch.ensure(sizeof(double) * 8));
-  if (nout > 0) {
-    fcg::corr::k_cbv_outlet<<<1, 32, 0, c->stream>>>(
-        c->mv, nout, c->fst[B_OUTLET], c->bst[B_OUTLET], (const double *)dden, flomas,
-        (double)1e-20f /* parameters::small, modules_allocatable.f90:27 */, (double *)du,
-        (double *)dv, (double *)dw, (double *)dfmo, c->scratch.as<double>());
-    fcg::corr::k_cbv_scale<<<grid_for(nout, c->num_sms), kTPB, 0, c->stream>>>(
-        nout, c->bst[B_OUTLET], c->scratch.as<double>(), (double *)du, (double *)dv,
-        (double *)dw, (double *)dfmo);
-  }
+  if ((rc = fcg::corr::outlet_flow(c, (const double *)dden, flomas, (double *)du, (double *)dv,
+                                   (double *)dw, (double *)dfmo)))
+    return rc;
   if (nsym > 0)
     fcg::corr::k_cbv_sym<<<grid_for(nsym, c->num_sms), kTPB, 0, c->stream>>>(
         c->mv, nsym, c->fst[B_SYMMETRY], c->bst[B_SYMMETRY], (double *)du, (double *)dv,

@@ -172,6 +172,13 @@ struct BatchVecs {
 int batch_load(fcg_context *c, const double *a_dev, const double *su_dev, const double *fi_dev,
                BatchVecs *out);
 
+namespace corr {
+// Outlet velocities, fmo and the flomas scaling (assembly.cu), device arrays; fac is
+// left in c->scratch[0].
+int outlet_flow(fcg_context *c, const double *den, double flomas, double *u, double *v,
+                double *w, double *fmo);
+}  // namespace corr
+
 }  // namespace fcg
 
 #define FCG_CUDA_TRY(ctx, expr)                                   \

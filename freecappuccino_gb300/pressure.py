@@ -222,6 +222,76 @@ class Context:
                     "fcg_continuity_errors")
         return res, sl.value, sg.value
 
+    # -- PISO pressure path (PISO_multiple_correction.f90:83-307) -----------------------
+    def piso_hbya(self, h, u, v, w, apu, apv, apw, den=None, *, timestep=1.0, btime=0.0,
+                  bdf=False, cn=False, buoyancy=False, boussinesq=False, beta=0.0, densit=1.0,
+                  tref=0.0, grav=(0.0, 0.0, 0.0), t=None, uo=None, vo=None, wo=None,
+                  uoo=None, voo=None, woo=None):
+        """get_rAU_x_UEqnH: returns (u, v, w, su, sv, sw) with the cell part of u, v, w
+        replaced by HbyA = apu*H(U) (and the volume and old-level sources)."""
+        opt = (den, t, uo, vo, wo, uoo, voo, woo)
+        self._follow(h, u, v, w, apu, apv, apw, *opt)
+        prm = _lib.HbyaParams(float(timestep), float(btime), int(bool(bdf)), int(bool(cn)),
+                              int(bool(buoyancy)), int(bool(boussinesq)), float(beta),
+                              float(densit), float(tref), *[float(g) for g in grav])
+        ins = [None if x is None else _host(x) for x in opt + (apu, apv, apw)]
+        fl = _lib.HbyaFields(*[_ptr(x) for x in ins])
+        h = _host(h)
+        outs = [x.clone() if _is_torch(x) else np.array(x, dtype=np.float64) for x in (u, v, w)]
+        srcs = [_like(outs[0], self.n) for _ in range(3)]
+        self._check(self.lib.fcg_piso_hbya(self.h, C.byref(prm), C.byref(fl), _ptr(h),
+                                           *[_ptr(x) for x in outs], *[_ptr(x) for x in srcs]),
+                    "fcg_piso_hbya")
+        return (*outs, *srcs)
+
+    def facefluxmass_piso(self, u, v, w, dUdxi, dVdxi, dWdxi, apu, den):
+        """The PISO corrector's assembly with facefluxmass_piso: returns (a, su, flmass)."""
+        self._follow(u, v, w, dUdxi, dVdxi, dWdxi, apu, den)
+        u, v, w, dU, dV, dW, apu, den = (_host(t) for t in (u, v, w, dUdxi, dVdxi, dWdxi, apu,
+                                                            den))
+        ff = _lib.FlowFields(_ptr(u), _ptr(v), _ptr(w), None, _ptr(dU), _ptr(dV), _ptr(dW), None,
+                             _ptr(apu), None, None, _ptr(den))
+        a = _like(u, self.nnz)
+        su = _like(u, self.n)
+        fm = _like(u, max(self.mesh.numInnerFaces, 1))
+        self._check(self.lib.fcg_facefluxmass_piso(self.h, C.byref(ff), _ptr(a), _ptr(su),
+                                                   _ptr(fm)), "fcg_facefluxmass_piso")
+        return a, su, fm[: self.mesh.numInnerFaces]
+
+    def adjust_mass_flow(self, den, flomas, fmi, u, v, w, su):
+        """adjustMassFlow: returns (u, v, w, fmo, su)."""
+        self._follow(den, u, v, w, su)
+        den = _host(den)
+        fmi = _host(fmi) if len(fmi) else _like(den, 1)
+        outs = [x.clone() if _is_torch(x) else np.array(x, dtype=np.float64)
+                for x in (u, v, w, su)]
+        nout = self.mesh.counts.get("nout", 0)
+        fmo = _like(den, max(nout, 1))
+        self._check(self.lib.fcg_adjust_mass_flow(self.h, _ptr(den), float(flomas), _ptr(fmi),
+                                                  *[_ptr(x) for x in outs[:3]], _ptr(fmo),
+                                                  _ptr(outs[3])), "fcg_adjust_mass_flow")
+        return (*outs[:3], fmo[:nout], outs[3])
+
+    def set_reference_pressure(self, pRefCell, p, a, su):
+        """PISO :188-192, row pRefCell (1-based) of a set to the identity row and
+        su(pRefCell) = p(pRefCell): returns (a, su)."""
+        self._follow(p, a, su)
+        p = _host(p)
+        a, su = (x.clone() if _is_torch(x) else np.array(x, dtype=np.float64) for x in (a, su))
+        self._check(self.lib.fcg_set_reference_pressure(self.h, int(pRefCell), _ptr(p), _ptr(a),
+                                                        _ptr(su)), "fcg_set_reference_pressure")
+        return a, su
+
+    def correct_velocity_piso(self, dPdxi, apu, apv, apw, u, v, w):
+        """PISO :300-304: returns the corrected (u, v, w)."""
+        self._follow(dPdxi, apu, apv, apw, u, v, w)
+        ins = [_host(x) for x in (dPdxi, apu, apv, apw)]
+        outs = [x.clone() if _is_torch(x) else np.array(x, dtype=np.float64) for x in (u, v, w)]
+        self._check(self.lib.fcg_correct_velocity_piso(self.h, *[_ptr(x) for x in ins],
+                                                       *[_ptr(x) for x in outs]),
+                    "fcg_correct_velocity_piso")
+        return tuple(outs)
+
     def grad(self, phi, option: str = "gauss", nigrad: int = 1, dphidxi=None):
         """grad(phi,dPhidxi[,option]) without limiter: returns dPhidxi as (n, 3)."""
         self._follow(phi, dphidxi)

@@ -163,6 +163,67 @@ int fcg_continuity_errors(fcg_context *ctx, const double *flmass, const double *
                           const double *fmo, double *res, double *sum_local, double *global);
 
 /* ---------------------------------------------------------------------------
+ * PISO pressure path (PISO_multiple_correction.f90:83-307).
+ * ------------------------------------------------------------------------- */
+
+/* Parameters read by get_rAU_x_UEqnH (module parameters, modules_allocatable.f90:40-106).
+ * buoyancy = lcal(ien) .and. lbuoy. */
+typedef struct fcg_hbya_params {
+  double timestep, btime;
+  int bdf, cn, buoyancy, boussinesq;
+  double beta, densit, tref, gravx, gravy, gravz;
+} fcg_hbya_params;
+
+/* Fields read by get_rAU_x_UEqnH; only the cell part [numCells] of each is read.  uo/vo/wo
+ * are needed with bdf or cn, uoo/voo/woo with bdf and btime > 0.99, t with buoyancy and
+ * boussinesq; the others may be NULL. */
+typedef struct fcg_hbya_fields {
+  const double *den, *t;
+  const double *uo, *vo, *wo, *uoo, *voo, *woo;
+  const double *apu, *apv, *apw;
+} fcg_hbya_fields;
+
+/* get_rAU_x_UEqnH.f90:3-208: su/sv/sw = the volume sources (buoyancy :37-56, BDF
+ * :62-83), the Crank-Nicolson terms of the old time level (:90-110), and
+ * H(U) = -sum_nb h(k) U_nb over the inner faces (:112-123), all summed in the
+ * reference's order; then u = apu*su, v = apv*sv, w = apw*sw on the cells (:204-206).
+ * h[nnz] is the momentum matrix saved before the corrector loop (PISO :84).  u, v, w
+ * [numTotal] in/out (only the cell part is read and written); su, sv, sw [numCells] out
+ * (each may be NULL). */
+int fcg_piso_hbya(fcg_context *ctx, const fcg_hbya_params *prm, const fcg_hbya_fields *f,
+                  const double *h, double *u, double *v, double *w, double *su, double *sv,
+                  double *sw);
+
+/* Pressure assembly of the PISO corrector (PISO_multiple_correction.f90:108-148) with
+ * facefluxmass_piso (facefluxmass.f90:294-358): a = 0, su = 0, per inner face
+ * cap = can = -dene (fxp vol_P apu_P + fxn vol_N apu_N) |S| / |d_PN|, the mass flux of the
+ * centrally interpolated velocity flmass = dene (u_f.S) (no Rhie-Chow term), the diagonal
+ * and su = -div(flmass) in face order.  Fields as fcg_facefluxmass (p, dPdxi, apv and
+ * apw are not read and may be NULL). */
+int fcg_facefluxmass_piso(fcg_context *ctx, const fcg_flow_fields *f, double *a, double *su,
+                          double *flmass);
+
+/* adjustMassFlow.f90:1-71: su(owner) -= fmi(i) over the inlet faces; the outlet slots of
+ * u, v, w take their cell's velocity, fmo(i) = den(ijp) (u,v,w)(ijb).S, the outflow is
+ * scaled to flomas (fac = flomas/(sum fmo + small)) and su(owner) -= fmo(i).  den, u, v, w
+ * [numTotal]; fmi[ninl] in, fmo[nout] out; su[numCells] in/out. */
+int fcg_adjust_mass_flow(fcg_context *ctx, const double *den, double flomas, const double *fmi,
+                         double *u, double *v, double *w, double *fmo, double *su);
+
+/* Reference pressure of the PISO pressure equation (PISO_multiple_correction.f90:188-192):
+ * row pRefCell (1-based) of a is zeroed, its diagonal set to 1 and su(pRefCell) =
+ * p(pRefCell).  a[nnz], su[numCells] in/out; p[numCells or numTotal]. */
+int fcg_set_reference_pressure(fcg_context *ctx, int pRefCell, const double *p, double *a,
+                               double *su);
+
+/* PISO velocity correction (PISO_multiple_correction.f90:300-304): u -= apu*dPdxi(1,:)*vol,
+ * v -= apv*dPdxi(2,:)*vol, w -= apw*dPdxi(3,:)*vol over the cells (the product in the
+ * reference's order, which differs from calcp's).  u, v, w [numTotal] in/out. */
+int fcg_correct_velocity_piso(fcg_context *ctx, const double *dPdxi, const double *apu,
+                              const double *apv, const double *apw, double *u, double *v,
+                              double *w);
+
+/* ---------------------------------------------------------------------------
  * Gradients and boundary values.
  * ------------------------------------------------------------------------- */
 #define FCG_GRAD_GAUSS 1           /* grad_gauss.f90, nigrad passes */

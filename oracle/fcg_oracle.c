@@ -831,6 +831,172 @@ int orc_flux_correct(const orc_mesh *m, const int *slot_pn, const double *a, con
   return 0;
 }
 
+/* ------------------------------------------------------------------------- */
+/* PISO pressure path                                                          */
+/* ------------------------------------------------------------------------- */
+
+/* get_rAU_x_UEqnH.f90:32-206, loop by loop: su = sv = sw = 0; the cell loop of volume
+ * sources (buoyancy :42-56, BDF :62-83, where `0.99` and `0.5` are default-real
+ * literals); per component the Crank-Nicolson face loop and cell loop (:90-110), then the
+ * H(U) face loop (:113-123); finally u = apu*su on the cells (:204-206). */
+int orc_piso_hbya(const orc_mesh *m, const int *ioffset, const int *diag, const int *slot_pn,
+                  const int *slot_np, const orc_hbya_params *prm, const double *h,
+                  const double *den, const double *t, const double *uo, const double *vo,
+                  const double *wo, const double *uoo, const double *voo, const double *woo,
+                  const double *apu, const double *apv, const double *apw, double *u, double *v,
+                  double *w, double *su, double *sv, double *sw) {
+  const int n = m->numCells;
+  for (int i = 1; i <= n; ++i) F(su, i) = F(sv, i) = F(sw, i) = 0.0;
+  for (int inp = 1; inp <= n; ++inp) {
+    if (prm->buoyancy) {
+      double heat = 0.0;
+      if (prm->boussinesq)
+        heat = prm->beta * prm->densit * (F(t, inp) - prm->tref) * F(m->vol, inp);
+      else
+        heat = (prm->densit - F(den, inp)) * F(m->vol, inp);
+      F(su, inp) = F(su, inp) - prm->gravx * heat;
+      F(sv, inp) = F(sv, inp) - prm->gravy * heat;
+      F(sw, inp) = F(sw, inp) - prm->gravz * heat;
+    }
+    if (prm->bdf) {
+      const double apotime = F(den, inp) * F(m->vol, inp) / prm->timestep;
+      double sut = apotime * ((1 + prm->btime) * F(uo, inp));
+      double svt = apotime * ((1 + prm->btime) * F(vo, inp));
+      double swt = apotime * ((1 + prm->btime) * F(wo, inp));
+      if (prm->btime > (double)0.99f) {
+        sut = sut - apotime * ((double)0.5f * prm->btime * F(uoo, inp));
+        svt = svt - apotime * ((double)0.5f * prm->btime * F(voo, inp));
+        swt = swt - apotime * ((double)0.5f * prm->btime * F(woo, inp));
+      }
+      F(su, inp) = F(su, inp) + sut;
+      F(sv, inp) = F(sv, inp) + svt;
+      F(sw, inp) = F(sw, inp) + swt;
+    }
+  }
+  double *s[3] = {su, sv, sw};
+  const double *cur[3] = {u, v, w}, *old[3] = {uo, vo, wo};
+  for (int comp = 0; comp < 3; ++comp) {
+    double *S = s[comp];
+    if (prm->cn) {
+      for (int i = 1; i <= m->numInnerFaces; ++i) {
+        const int ijp = F(m->owner, i), ijn = F(m->neighbour, i);
+        F(S, ijp) = F(S, ijp) - F(h, F(slot_pn, i)) * F(old[comp], ijn);
+        F(S, ijn) = F(S, ijn) - F(h, F(slot_np, i)) * F(old[comp], ijp);
+      }
+      for (int ijp = 1; ijp <= n; ++ijp) {
+        const double apotime = F(den, ijp) * F(m->vol, ijp) / prm->timestep;
+        double sum = 0.0; /* sum(h(ioffset(ijp):ioffset(ijp+1)-1)) */
+        for (int k = F(ioffset, ijp); k <= F(ioffset, ijp + 1) - 1; ++k) sum = sum + F(h, k);
+        const double off_diagonal_terms = sum - F(h, F(diag, ijp));
+        F(S, ijp) = F(S, ijp) + (apotime + off_diagonal_terms) * F(old[comp], ijp);
+      }
+    }
+    for (int i = 1; i <= m->numInnerFaces; ++i) {
+      const int ijp = F(m->owner, i), ijn = F(m->neighbour, i);
+      F(S, ijp) = F(S, ijp) - F(h, F(slot_pn, i)) * F(cur[comp], ijn);
+      F(S, ijn) = F(S, ijn) - F(h, F(slot_np, i)) * F(cur[comp], ijp);
+    }
+  }
+  for (int i = 1; i <= n; ++i) {
+    F(u, i) = F(apu, i) * F(su, i);
+    F(v, i) = F(apv, i) * F(sv, i);
+    F(w, i) = F(apw, i) * F(sw, i);
+  }
+  return 0;
+}
+
+/* PISO_multiple_correction.f90:109-148 with facefluxmass_piso (facefluxmass.f90:294-358). */
+int orc_facefluxmass_piso(const orc_mesh *m, const int *diag, const int *slot_pn,
+                          const int *slot_np, const double *u, const double *v, const double *w,
+                          const double *dUdxi, const double *dVdxi, const double *dWdxi,
+                          const double *apu, const double *den, int nnz, double *a, double *su,
+                          double *flmass) {
+  for (int k = 0; k < nnz; ++k) a[k] = 0.0;          /* :109 */
+  for (int i = 0; i < m->numCells; ++i) su[i] = 0.0; /* :110 */
+  for (int i = 1; i <= m->numInnerFaces; ++i) {
+    const int ijp = F(m->owner, i), ijn = F(m->neighbour, i);
+    const double xf = F(m->xf, i), yf = F(m->yf, i), zf = F(m->zf, i);
+    const double arx = F(m->arx, i), ary = F(m->ary, i), arz = F(m->arz, i);
+    const double fxn = F(m->facint, i);
+    const double fxp = 1.0 - fxn;
+    const double xpn = F(m->xc, ijn) - F(m->xc, ijp);
+    const double ypn = F(m->yc, ijn) - F(m->yc, ijp);
+    const double zpn = F(m->zc, ijn) - F(m->zc, ijp);
+    const double dpn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
+    const double are = sqrt(arx * arx + ary * ary + arz * arz);
+    const double dene = F(den, ijp) * fxp + F(den, ijn) * fxn;
+    const double cap = -(dene *
+                         (fxp * F(m->vol, ijp) * F(apu, ijp) + fxn * F(m->vol, ijn) * F(apu, ijn)) *
+                         are / dpn);
+    const double can = cap;
+    const double ui = face_value_central(m, ijp, ijn, xf, yf, zf, u, dUdxi);
+    const double vi = face_value_central(m, ijp, ijn, xf, yf, zf, v, dVdxi);
+    const double wi = face_value_central(m, ijp, ijn, xf, yf, zf, w, dWdxi);
+    const double fm = dene * (ui * arx + vi * ary + wi * arz);
+    F(flmass, i) = fm;
+    F(a, F(slot_pn, i)) = can;
+    F(a, F(slot_np, i)) = cap;
+    F(a, F(diag, ijp)) = F(a, F(diag, ijp)) - can;
+    F(a, F(diag, ijn)) = F(a, F(diag, ijn)) - cap;
+    F(su, ijp) = F(su, ijp) - fm;
+    F(su, ijn) = F(su, ijn) + fm;
+  }
+  return 0;
+}
+
+/* adjustMassFlow.f90:15-69. */
+int orc_adjust_mass_flow(const orc_mesh *m, const double *den, double flomas, const double *fmi,
+                         double *u, double *v, double *w, double *fmo, double *su) {
+  const double small = orc_const_small_src();
+  for (int i = 1; i <= m->ninl; ++i) {
+    const int ijp = F(m->owner, m->iInletFacesStart + i);
+    F(su, ijp) = F(su, ijp) - F(fmi, i);
+  }
+  double flowo = 0.0;
+  for (int i = 1; i <= m->nout; ++i) {
+    const int iface = m->iOutletFacesStart + i, ijp = F(m->owner, iface);
+    const int ijb = iOutletStart(m) + i;
+    F(u, ijb) = F(u, ijp);
+    F(v, ijb) = F(v, ijp);
+    F(w, ijb) = F(w, ijp);
+    F(fmo, i) = F(den, ijp) * (F(u, ijb) * F(m->arx, iface) + F(v, ijb) * F(m->ary, iface) +
+                               F(w, ijb) * F(m->arz, iface));
+    flowo = flowo + F(fmo, i);
+  }
+  const double fac = flomas / (flowo + small);
+  for (int i = 1; i <= m->nout; ++i) {
+    const int iface = m->iOutletFacesStart + i, ijp = F(m->owner, iface);
+    const int ijb = iOutletStart(m) + i;
+    F(fmo, i) = F(fmo, i) * fac;
+    F(u, ijb) = F(u, ijb) * fac;
+    F(v, ijb) = F(v, ijb) * fac;
+    F(w, ijb) = F(w, ijb) * fac;
+    F(su, ijp) = F(su, ijp) - F(fmo, i);
+  }
+  return 0;
+}
+
+/* PISO_multiple_correction.f90:188-192. */
+int orc_set_reference_pressure(const int *ioffset, const int *diag, int pRefCell,
+                               const double *p, double *a, double *su) {
+  for (int k = F(ioffset, pRefCell); k <= F(ioffset, pRefCell + 1) - 1; ++k) F(a, k) = 0.0;
+  F(a, F(diag, pRefCell)) = 1.0;
+  F(su, pRefCell) = F(p, pRefCell);
+  return 0;
+}
+
+/* PISO_multiple_correction.f90:300-304. */
+int orc_correct_velocity_piso(const orc_mesh *m, const double *dPdxi, const double *apu,
+                              const double *apv, const double *apw, double *u, double *v,
+                              double *w) {
+  for (int inp = 1; inp <= m->numCells; ++inp) {
+    F(u, inp) = F(u, inp) - F(apu, inp) * G3(dPdxi, 1, inp) * F(m->vol, inp);
+    F(v, inp) = F(v, inp) - F(apv, inp) * G3(dPdxi, 2, inp) * F(m->vol, inp);
+    F(w, inp) = F(w, inp) - F(apw, inp) * G3(dPdxi, 3, inp) * F(m->vol, inp);
+  }
+  return 0;
+}
+
 /* calcp-multiple_correction_SIMPLE.f90:184-189: velocity and pressure correction,
  * ppref = pp(pRefCell) (:147). */
 int orc_correct_fields(const orc_mesh *m, const double *dPdxi, const double *apu,

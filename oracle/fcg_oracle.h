@@ -99,6 +99,34 @@ int orc_correct_fields(const orc_mesh *m, const double *dPdxi, const double *apu
                        const double *apv, const double *apw, const double *pp, double urf,
                        int pRefCell, double *u, double *v, double *w, double *p);
 
+/* --- PISO pressure path: PISO_multiple_correction.f90, get_rAU_x_UEqnH.f90,
+ *     facefluxmass_piso (facefluxmass.f90:294-358), adjustMassFlow.f90 --- */
+typedef struct orc_hbya_params {
+  double timestep, btime;
+  int bdf, cn, buoyancy, boussinesq;
+  double beta, densit, tref, gravx, gravy, gravz;
+} orc_hbya_params;
+/* Cell arrays [numCells]; uo..woo, t may be NULL where the parameters do not read them.
+ * h[nnz]; u, v, w in/out [numCells+] (the cells are overwritten); su, sv, sw out. */
+int orc_piso_hbya(const orc_mesh *m, const int *ioffset, const int *diag, const int *slot_pn,
+                  const int *slot_np, const orc_hbya_params *prm, const double *h,
+                  const double *den, const double *t, const double *uo, const double *vo,
+                  const double *wo, const double *uoo, const double *voo, const double *woo,
+                  const double *apu, const double *apv, const double *apw, double *u, double *v,
+                  double *w, double *su, double *sv, double *sw);
+int orc_facefluxmass_piso(const orc_mesh *m, const int *diag, const int *slot_pn,
+                          const int *slot_np, const double *u, const double *v, const double *w,
+                          const double *dUdxi, const double *dVdxi, const double *dWdxi,
+                          const double *apu, const double *den, int nnz, double *a, double *su,
+                          double *flmass);
+int orc_adjust_mass_flow(const orc_mesh *m, const double *den, double flomas, const double *fmi,
+                         double *u, double *v, double *w, double *fmo, double *su);
+int orc_set_reference_pressure(const int *ioffset, const int *diag, int pRefCell,
+                               const double *p, double *a, double *su);
+int orc_correct_velocity_piso(const orc_mesh *m, const double *dPdxi, const double *apu,
+                              const double *apv, const double *apw, double *u, double *v,
+                              double *w);
+
 /* --- a9-a11: dpcg.f90, iccg.f90, bicgstab.f90 --- */
 typedef struct orc_solver_opts {
   double resmax;   /* sor(ifi) */

@@ -219,6 +219,72 @@ def correct_fields(m: Mesh, dPdxi, apu, apv, apw, pp, urf, pRefCell, u, v, w, p)
     return u, v, w, p
 
 
+class HbyaParams(C.Structure):
+    """Parameters read by get_rAU_x_UEqnH (modules_allocatable.f90:40-106)."""
+    _fields_ = [("timestep", C.c_double), ("btime", C.c_double), ("bdf", C.c_int),
+                ("cn", C.c_int), ("buoyancy", C.c_int), ("boussinesq", C.c_int),
+                ("beta", C.c_double), ("densit", C.c_double), ("tref", C.c_double),
+                ("gravx", C.c_double), ("gravy", C.c_double), ("gravz", C.c_double)]
+
+
+def _opt(a, n):
+    return _d(_f64(a)) if a is not None else _d(np.zeros(max(n, 1)))
+
+
+def piso_hbya(m: Mesh, csr: CSR, prm: HbyaParams, h, den, apu, apv, apw, u, v, w,
+              t=None, uo=None, vo=None, wo=None, uoo=None, voo=None, woo=None):
+    """get_rAU_x_UEqnH.f90:3-208. Returns (u, v, w, su, sv, sw); the cell part of u, v, w
+    is overwritten with apu*su etc."""
+    n = m.numCells
+    u, v, w = (_f64(x).copy() for x in (u, v, w))
+    su, sv, sw = np.zeros(n), np.zeros(n), np.zeros(n)
+    assert lib().orc_piso_hbya(
+        C.byref(m.struct), _i(csr.ioffset), _i(csr.diag), _i(csr.slot_pn), _i(csr.slot_np),
+        C.byref(prm), _d(_f64(h)), _opt(den, n), _opt(t, n), _opt(uo, n), _opt(vo, n),
+        _opt(wo, n), _opt(uoo, n), _opt(voo, n), _opt(woo, n), _d(_f64(apu)), _d(_f64(apv)),
+        _d(_f64(apw)), _d(u), _d(v), _d(w), _d(su), _d(sv), _d(sw)) == 0
+    return u, v, w, su, sv, sw
+
+
+def facefluxmass_piso(m: Mesh, csr: CSR, u, v, w, dUdxi, dVdxi, dWdxi, apu, den):
+    """PISO_multiple_correction.f90:109-148 with facefluxmass_piso (facefluxmass.f90:294-358).
+    Returns (a, su, flmass)."""
+    args = [_f64(t) for t in (u, v, w, dUdxi, dVdxi, dWdxi, apu, den)]
+    a = np.zeros(csr.nnz)
+    su = np.zeros(m.numCells)
+    flmass = np.zeros(max(m.numInnerFaces, 1))
+    assert lib().orc_facefluxmass_piso(C.byref(m.struct), _i(csr.diag), _i(csr.slot_pn),
+                                       _i(csr.slot_np), *[_d(t) for t in args], csr.nnz, _d(a),
+                                       _d(su), _d(flmass)) == 0
+    return a, su, flmass[:m.numInnerFaces]
+
+
+def adjust_mass_flow(m: Mesh, den, flomas, fmi, u, v, w, su):
+    """adjustMassFlow.f90:1-71. Returns (u, v, w, fmo, su)."""
+    u, v, w, su = (_f64(x).copy() for x in (u, v, w, su))
+    fmo = np.zeros(max(m.struct.nout, 1))
+    fmi = _f64(fmi) if len(fmi) else np.zeros(1)
+    assert lib().orc_adjust_mass_flow(C.byref(m.struct), _d(_f64(den)), C.c_double(flomas),
+                                      _d(fmi), _d(u), _d(v), _d(w), _d(fmo), _d(su)) == 0
+    return u, v, w, fmo[:m.struct.nout], su
+
+
+def set_reference_pressure(csr: CSR, pRefCell, p, a, su):
+    """PISO_multiple_correction.f90:188-192. Returns (a, su)."""
+    a, su = _f64(a).copy(), _f64(su).copy()
+    assert lib().orc_set_reference_pressure(_i(csr.ioffset), _i(csr.diag), int(pRefCell),
+                                            _d(_f64(p)), _d(a), _d(su)) == 0
+    return a, su
+
+
+def correct_velocity_piso(m: Mesh, dPdxi, apu, apv, apw, u, v, w):
+    """PISO_multiple_correction.f90:300-304. Returns (u, v, w)."""
+    u, v, w = (_f64(x).copy() for x in (u, v, w))
+    assert lib().orc_correct_velocity_piso(C.byref(m.struct), _d(_f64(dPdxi)), _d(_f64(apu)),
+                                           _d(_f64(apv)), _d(_f64(apw)), _d(u), _d(v), _d(w)) == 0
+    return u, v, w
+
+
 def correct_bc_velocity(m: Mesh, den, flomas, u, v, w):
     """correctBoundaryConditionsVelocity.f90:1-80: returns (u, v, w, fmo)."""
     u, v, w = (_f64(x).copy() for x in (u, v, w))
