@@ -113,8 +113,81 @@ def compute_geometry(points, face_ptr, face_nodes, owner, neighbour, numCells):
     return g
 
 
-def hex_mesh(N: int, jitter: float = 0.0, seed: int = 0, keep_topology: bool = False) -> Mesh:
-    """N^3 hex mesh of the unit cube: wall at x=0, symmetry on the other five faces."""
+class _Device:
+    """A libfcgpu context that is not bound to a mesh: the device and stream the setup
+    kernels (fcg_mesh_geometry_gpu, fcg_csr_build_gpu) run on."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        self.h = C.c_void_p()
+        rc = self.lib.fcg_create(C.byref(self.h), int(device))
+        if rc != 0:
+            raise _lib.FcgError(rc, "fcg_create", "no usable sm_103a CUDA device")
+
+    def check(self, rc, what):
+        if rc != 0:
+            raise _lib.FcgError(rc, what, self.lib.fcg_last_error(self.h).decode())
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.lib.fcg_destroy(self.h)
+        self.h = None
+
+
+def _ptr(x):
+    if hasattr(x, "data_ptr"):  # a CUDA tensor, used in place
+        return x.data_ptr()
+    return x.ctypes.data
+
+
+def compute_geometry_gpu(points, face_ptr, face_nodes, owner, neighbour, numCells,
+                         device: int = 0):
+    """mesh_geometry's geometric part (:859-1079) by the GPU kernels of
+    fcg_mesh_geometry_gpu; the same results as compute_geometry, bit for bit."""
+    x, y, z = (np.ascontiguousarray(points[:, i], dtype=np.float64) for i in range(3))
+    face_ptr = np.ascontiguousarray(face_ptr, dtype=np.int32)
+    face_nodes = np.ascontiguousarray(face_nodes, dtype=np.int32)
+    owner = np.ascontiguousarray(owner, dtype=np.int32)
+    neighbour = np.ascontiguousarray(neighbour, dtype=np.int32)
+    nf, nin = len(face_ptr) - 1, len(neighbour)
+    g = {k: np.zeros(nf) for k in ("arx", "ary", "arz", "xf", "yf", "zf")}
+    g.update({k: np.zeros(numCells) for k in ("xc", "yc", "zc", "vol")})
+    g["facint"] = np.zeros(max(nin, 1))
+    with _Device(device) as d:
+        d.check(d.lib.fcg_mesh_geometry_gpu(
+            d.h, len(x), _p(x), _p(y), _p(z), int(numCells), nf, nin, _p(face_ptr),
+            _p(face_nodes), _p(owner), _p(neighbour if nin else g["facint"]),
+            *[_p(g[k]) for k in ("arx", "ary", "arz", "xf", "yf", "zf", "xc", "yc", "zc", "vol",
+                                 "facint")]), "fcg_mesh_geometry_gpu")
+    g["facint"] = g["facint"][:nin]
+    return g
+
+
+def csr_build_gpu(numCells: int, owner, neighbour, device: int = 0):
+    """create_CSR_matrix_from_mesh_data (sparse_matrix.f90:42-172) by the GPU kernels of
+    fcg_csr_build_gpu: (ioffset, ja, diag, slot_pn, slot_np), 1-based int32.  owner and
+    neighbour may be numpy arrays or CUDA int32 tensors; the results come back as numpy."""
+    nin = len(neighbour)
+    if not hasattr(owner, "data_ptr"):
+        owner = np.ascontiguousarray(owner, dtype=np.int32)
+        neighbour = np.ascontiguousarray(neighbour, dtype=np.int32)
+    nnz = numCells + 2 * nin
+    io, ja = np.zeros(numCells + 1, np.int32), np.zeros(nnz, np.int32)
+    dg = np.zeros(numCells, np.int32)
+    spn, snp = np.zeros(max(nin, 1), np.int32), np.zeros(max(nin, 1), np.int32)
+    with _Device(device) as d:
+        d.check(d.lib.fcg_csr_build_gpu(d.h, int(numCells), nin, _ptr(owner), _ptr(neighbour),
+                                        _p(io), _p(ja), _p(dg), _p(spn), _p(snp)),
+                "fcg_csr_build_gpu")
+    return io, ja, dg, spn[:nin], snp[:nin]
+
+
+def hex_mesh(N: int, jitter: float = 0.0, seed: int = 0, keep_topology: bool = False,
+             device: int | None = None) -> Mesh:
+    """N^3 hex mesh of the unit cube: wall at x=0, symmetry on the other five faces.
+    With `device` set, the geometry is computed by the GPU kernels on that device."""
     lib = _lib.load()
     nn, nc, nf, nin = C.c_int(), C.c_int(), C.c_int(), C.c_int()
     rc = lib.fcg_hex_mesh_sizes(N, C.byref(nn), C.byref(nc), C.byref(nf), C.byref(nin))
@@ -134,7 +207,10 @@ def hex_mesh(N: int, jitter: float = 0.0, seed: int = 0, keep_topology: bool = F
         raise _lib.FcgError(rc, "fcg_hex_mesh_build")
     neighbour = neighbour[:nin]
     points = np.ascontiguousarray(pts.T)
-    g = compute_geometry(points, face_ptr, face_nodes, owner, neighbour, nc)
+    if device is None:
+        g = compute_geometry(points, face_ptr, face_nodes, owner, neighbour, nc)
+    else:
+        g = compute_geometry_gpu(points, face_ptr, face_nodes, owner, neighbour, nc, device)
     m = Mesh(nc, nf, nin, owner, neighbour, **g,
              counts=dict(nsym=int(patches[0]), nwal=int(patches[2])),
              starts=dict(iSymmetryFacesStart=int(patches[1]), iWallFacesStart=int(patches[3])))
@@ -144,8 +220,9 @@ def hex_mesh(N: int, jitter: float = 0.0, seed: int = 0, keep_topology: bool = F
 
 
 def polymesh_mesh(points, face_ptr, face_nodes, owner, neighbour, numCells, patch_type,
-                  patch_nfaces, patch_start) -> Mesh:
-    """A polyMesh (1-based arrays) with the reference's boundary bookkeeping."""
+                  patch_nfaces, patch_start, device: int | None = None) -> Mesh:
+    """A polyMesh (1-based arrays) with the reference's boundary bookkeeping; with
+    `device` set, the geometry is computed by the GPU kernels on that device."""
     counts = {k: 0 for k in ("ninl", "nout", "nsym", "nwal", "npru")}
     starts = {}
     key = {"inlet": ("ninl", "iInletFacesStart"), "outlet": ("nout", "iOutletFacesStart"),
@@ -160,7 +237,9 @@ def polymesh_mesh(points, face_ptr, face_nodes, owner, neighbour, numCells, patc
         if counts[c] == 0:
             starts[s] = int(st)
         counts[c] += int(cnt)
-    g = compute_geometry(points, face_ptr, face_nodes, owner, neighbour, int(numCells))
+    geo = compute_geometry if device is None else (
+        lambda *a: compute_geometry_gpu(*a, device=device))
+    g = geo(points, face_ptr, face_nodes, owner, neighbour, int(numCells))
     return Mesh(int(numCells), len(face_ptr) - 1, len(neighbour),
                 np.ascontiguousarray(owner, np.int32), np.ascontiguousarray(neighbour, np.int32),
                 **g, counts=counts, starts=starts, points=np.asarray(points),

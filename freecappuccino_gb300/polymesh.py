@@ -79,9 +79,10 @@ def parse_boundary(text: str):
     return out
 
 
-def read_polymesh(path: str) -> Mesh:
+def read_polymesh(path: str, device: int | None = None) -> Mesh:
     """The mesh of a polyMesh directory, with the reference's geometry and boundary
-    bookkeeping (mesh.polymesh_mesh)."""
+    bookkeeping (mesh.polymesh_mesh); with `device` set, the geometry is computed by the
+    GPU kernels on that device."""
     def get(name):
         with open(os.path.join(path, name)) as f:
             return f.read()
@@ -93,7 +94,7 @@ def read_polymesh(path: str) -> Mesh:
                          parse_labels(owner_text), parse_labels(get("neighbour")),
                          parse_ncells(owner_text), np.array([p[0] for p in patches]),
                          np.array([p[1] for p in patches], np.int32),
-                         np.array([p[2] for p in patches], np.int32))
+                         np.array([p[2] for p in patches], np.int32), device=device)
 
 
 _HEADER = """FoamFile

@@ -102,6 +102,28 @@ int fcg_create_csr(fcg_context *ctx, int *ioffset, int *ja, int *diag, int *slot
 int fcg_csr_build(int numCells, int numInnerFaces, const int *owner, const int *neighbour,
                   int *ioffset, int *ja, int *diag, int *slot_pn, int *slot_np);
 
+/* The same construction by kernels on ctx's device and stream (the context need not be
+ * bound to a mesh); arrays host or device, results identical to fcg_csr_build.  Bad
+ * indices and two faces on one cell pair give FCG_ERR_INDEX. */
+int fcg_csr_build_gpu(fcg_context *ctx, int numCells, int numInnerFaces, const int *owner,
+                      const int *neighbour, int *ioffset, int *ja, int *diag, int *slot_pn,
+                      int *slot_np);
+
+/* The geometry pass of mesh_geometry (mesh_geometry_and_topology.f90:859-1079) by kernels
+ * on ctx's device: face area vectors by triangle fans from the first node, arithmetic-mean
+ * face centres, divergence-theorem volumes, Nurnberg centroids and the interpolation
+ * factor through the plane of the first three face nodes, bit-identical to the host form
+ * fcg_mesh_geometry (fcgpu_meshgen.h).  x, y, z [numNodes]; face_ptr[numFaces+1]
+ * (0-based offsets); face_nodes (1-based); owner[numFaces], neighbour[numInnerFaces]
+ * 1-based; outputs arx..zf [numFaces], xc, yc, zc, vol [numCells], facint
+ * [numInnerFaces].  Arrays host or device. */
+int fcg_mesh_geometry_gpu(fcg_context *ctx, int numNodes, const double *x, const double *y,
+                          const double *z, int numCells, int numFaces, int numInnerFaces,
+                          const int *face_ptr, const int *face_nodes, const int *owner,
+                          const int *neighbour, double *arx, double *ary, double *arz,
+                          double *xf, double *yf, double *zf, double *xc, double *yc,
+                          double *zc, double *vol, double *facint);
+
 /* ---------------------------------------------------------------------------
  * Assembly (face loops into the CSR values a[nnz]).
  * ------------------------------------------------------------------------- */
