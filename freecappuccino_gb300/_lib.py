@@ -16,6 +16,10 @@ FCG_OK = 0
 FCG_ERR_ARG = -1
 FCG_ERR_STATE = -2
 FCG_ERR_CUDA = -3
+CONV_SCHEMES = {"cds": 0, "cds_corrected": 1, "central": 2, "second_upwind": 3, "muscl": 4,
+                "flux_limiter": 5}
+LIMITERS = {"smart": 0, "avl": 1, "muscl": 2, "umist": 3, "koren": 4, "charm": 5, "ospre": 6,
+            "uds": 7}
 FCG_ERR_INDEX = -4
 FCG_ERR_PIVOT = -5
 FCG_ERR_STALL = -6
@@ -61,6 +65,25 @@ class HbyaFields(C.Structure):
                                    "apu", "apv", "apw")]
 
 
+class UvwParams(C.Structure):
+    """fcg_uvw_params: the parameters calcuvw reads."""
+    _fields_ = [("scheme", C.c_int), ("limiter", C.c_int), ("gds", C.c_double),
+                ("viscos", C.c_double), ("urfr", C.c_double * 3), ("urfm", C.c_double * 3),
+                ("bdf", C.c_int), ("cn", C.c_int), ("timestep", C.c_double),
+                ("btime", C.c_double), ("const_mflux", C.c_int), ("gradPcmf", C.c_double),
+                ("buoyancy", C.c_int), ("boussinesq", C.c_int), ("beta", C.c_double),
+                ("densit", C.c_double), ("tref", C.c_double), ("gravx", C.c_double),
+                ("gravy", C.c_double), ("gravz", C.c_double)]
+
+
+UVW_FIELDS = ("u", "v", "w", "p", "vis", "den", "t", "uo", "vo", "wo", "uoo", "voo", "woo",
+              "dUdxi", "dVdxi", "dWdxi", "dPdxi", "flmass", "fmi", "fmo")
+
+
+class UvwFields(C.Structure):
+    _fields_ = [(k, _vp) for k in UVW_FIELDS]
+
+
 class SolveReport(C.Structure):
     _fields_ = [("res0", C.c_double), ("resl", C.c_double), ("iters", C.c_int),
                 ("converged", C.c_int), ("l2_rel", C.c_double), ("seconds", C.c_double)]
@@ -94,6 +117,8 @@ _PROTOS = {
     "fcg_continuity_errors": (C.c_int, [_CTX, _vp, _vp, _vp, _vp, _dp, _dp]),
     "fcg_correct_fields": (C.c_int, [_CTX, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_int, _vp,
                                      _vp, _vp, _vp]),
+    "fcg_calcuvw": (C.c_int, [_CTX, C.POINTER(UvwParams), C.POINTER(UvwFields), _vp, _vp, _vp,
+                              _vp]),
     "fcg_piso_hbya": (C.c_int, [_CTX, C.POINTER(HbyaParams), C.POINTER(HbyaFields), _vp, _vp,
                                 _vp, _vp, _vp, _vp, _vp]),
     "fcg_facefluxmass_piso": (C.c_int, [_CTX, C.POINTER(FlowFields), _vp, _vp, _vp]),

@@ -1,0 +1,470 @@
+// Momentum assembly of calcuvw (calcuvw.f90:48-438): the u, v and w systems that the
+// three bicgstab calls (or one multi-RHS solve) take.
+//
+// Two kernels and no atomics, like the pressure assembly:
+//   1. one thread per inner face computes facefluxuvw (faceflux_velocity.f90:35-184) and
+//      the pressure-divergence term of presFaceDivInner (fieldManipulation.f90:395-443),
+//      writes the face's two off-diagonal slots and keeps its six source terms;
+//   2. one thread per cell adds every source in the reference's order -- the pressure
+//      divergence, the volume sources, the face fluxes, the boundary loops,
+//      Crank-Nicolson -- and assembles the three diagonals from its own CSR row.
+// Compiled with --fmad=false: bit-identical to the reference's loops on the same inputs.
+//
+// MIN and MAX keep the first argument on ties (only the sign of a zero can differ).
+#include "fcg_internal.h"
+#include "launch.h"
+
+using namespace fcg;
+
+namespace {
+
+__device__ __forceinline__ double rmin(double a, double b) { return b < a ? b : a; }
+__device__ __forceinline__ double rmax(double a, double b) { return b > a ? b : a; }
+
+struct UvwView {
+  const double *u, *v, *w, *p, *vis, *den, *t, *uo, *vo, *wo, *uoo, *voo, *woo;
+  const double *dU, *dV, *dW, *dP, *flmass, *fmi, *fmo;
+};
+
+// face_value (interpolation.f90:20-60) with the first cell upwind: f is the first cell,
+// s the second, lam the weight of the second (the caller passes fxp or fxn as the
+// reference does).
+__device__ double face_value(const MeshView &m, int scheme, int limiter, int f, int s,
+                             double xf, double yf, double zf, double lam,
+                             const double *__restrict__ fi, const double *__restrict__ g) {
+  switch (scheme) {
+    case FCG_CONV_CDS: {  // :65-93
+      const double fxn = lam, fxp = 1.0 - lam;
+      return fi[f] * fxp + fi[s] * fxn;
+    }
+    case FCG_CONV_CDS_CORRECTED: {  // :99-139
+      const double fxn = lam, fxp = 1.0 - lam;
+      const double xi = m.xc[f] * fxp + m.xc[s] * fxn, yi = m.yc[f] * fxp + m.yc[s] * fxn,
+                   zi = m.zc[f] * fxp + m.zc[s] * fxn;
+      const double dx = g[3 * f] * fxp + g[3 * s] * fxn, dy = g[3 * f + 1] * fxp + g[3 * s + 1] * fxn,
+                   dz = g[3 * f + 2] * fxp + g[3 * s + 2] * fxn;
+      return fi[f] * fxp + fi[s] * fxn + (dx * (xf - xi) + dy * (yf - yi) + dz * (zf - zi));
+    }
+    case FCG_CONV_CENTRAL: {  // :145-199
+      const double r = g[3 * f] * (xf - m.xc[f]) + g[3 * f + 1] * (yf - m.yc[f]) +
+                       g[3 * f + 2] * (zf - m.zc[f]) + g[3 * s] * (xf - m.xc[s]) +
+                       g[3 * s + 1] * (yf - m.yc[s]) + g[3 * s + 2] * (zf - m.zc[s]);
+      return 0.5 * (fi[f] + fi[s] + r);
+    }
+    case FCG_CONV_SECOND_UPWIND: {  // :204-249
+      const double r = g[3 * f] * (xf - m.xc[f]) + g[3 * f + 1] * (yf - m.yc[f]) +
+                       g[3 * f + 2] * (zf - m.zc[f]);
+      return fi[f] + r;
+    }
+    case FCG_CONV_FLUX_LIMITER: {  // :325-393
+      const double fxp = 1.0 - lam;
+      const double xpn = m.xc[s] - m.xc[f], ypn = m.yc[s] - m.yc[f], zpn = m.zc[s] - m.zc[f];
+      const double r = (2.0 * g[3 * f] * xpn + 2.0 * g[3 * f + 1] * ypn + 2.0 * g[3 * f + 2] * zpn) /
+                           (fi[s] - fi[f]) -
+                       1.0;
+      double psi;
+      switch (limiter) {
+        case FCG_LIM_SMART:
+          psi = rmax(0.0, rmin(rmin(2.0 * r, 0.75 * r + 0.25), 4.0));
+          break;
+        case FCG_LIM_AVL:
+          psi = rmax(0.0, rmin(rmin(1.5 * r, 0.75 * r + 0.25), 2.5));
+          break;
+        case FCG_LIM_MUSCL:
+          psi = rmax(0.0, rmin(rmin(2.0 * r, 0.5 * r + 0.5), 2.0));
+          break;
+        case FCG_LIM_UMIST:
+          psi = rmax(0.0, rmin(rmin(rmin(2.0 * r, 0.75 * r + 0.25), 0.25 * r + 0.75), 2.0));
+          break;
+        case FCG_LIM_KOREN:
+          psi = rmax(0.0, rmin(rmin(2.0 * r, 2.0 / 3.0 * r + 1.0 / 3.0), 2.0));
+          break;
+        case FCG_LIM_CHARM:
+          psi = (r + fabs(r)) * (3.0 * r + 1.0) / (2.0 * ((r + 1.0) * (r + 1.0)));
+          break;
+        case FCG_LIM_OSPRE:
+          psi = 1.5 * r * (r + 1.0) / (r * r + r + 1.0);
+          break;
+        default:
+          psi = 1.0;
+      }
+      return fi[f] + fxp * psi * (fi[s] - fi[f]);
+    }
+    default: {  // FCG_CONV_MUSCL, :254-320
+      const double theta = 0.125;
+      const double g2 = g[3 * f] * (xf - m.xc[f]) + g[3 * f + 1] * (yf - m.yc[f]) +
+                        g[3 * f + 2] * (zf - m.zc[f]);
+      const double gc = g[3 * f] * (xf - m.xc[f]) + g[3 * f + 1] * (yf - m.yc[f]) +
+                        g[3 * f + 2] * (zf - m.zc[f]) + g[3 * s] * (xf - m.xc[s]) +
+                        g[3 * s + 1] * (yf - m.yc[s]) + g[3 * s + 2] * (zf - m.zc[s]);
+      const double fv2 = fi[f] + g2;
+      const double fvc = 0.5 * (fi[f] + fi[s] + gc);
+      return theta * fvc + (1.0 - theta) * fv2;
+    }
+  }
+}
+
+// sngrad with nrelax = 0 and the skewness approach (gradients.f90:597-668): the face
+// gradient interpolated (dxi..) and corrected (dxii..).
+struct SnGrad {
+  double xi, yi, zi, xii, yii, zii;
+};
+
+__device__ __forceinline__ SnGrad sngrad(int p, int q, double arx, double ary, double arz,
+                                         double fxp, double fxn, double xpn, double ypn,
+                                         double zpn, double vole,
+                                         const double *__restrict__ fi,
+                                         const double *__restrict__ g) {
+  SnGrad s;
+  s.xi = g[3 * p] * fxp + g[3 * q] * fxn;
+  s.yi = g[3 * p + 1] * fxp + g[3 * q + 1] * fxn;
+  s.zi = g[3 * p + 2] * fxp + g[3 * q + 2] * fxn;
+  const double costn = 1.0;
+  const double d2x = xpn * costn, d2y = ypn * costn, d2z = zpn * costn;
+  s.xii = s.xi * costn + arx / vole * (fi[q] - fi[p] - s.xi * d2x - s.yi * d2y - s.zi * d2z);
+  s.yii = s.yi * costn + ary / vole * (fi[q] - fi[p] - s.xi * d2x - s.yi * d2y - s.zi * d2z);
+  s.zii = s.zi * costn + arz / vole * (fi[q] - fi[p] - s.xi * d2x - s.yi * d2y - s.zi * d2z);
+  return s;
+}
+
+__global__ void k_uvw_faces(MeshView m, fcg_uvw_params prm, UvwView F, double *__restrict__ a,
+                            double *__restrict__ fsrc, double *__restrict__ fdiv) {
+  const long long nin = m.nin;
+  FCG_GRID_STRIDE(f, nin) {
+    const int p = m.owner[f], q = m.neighbour[f];
+    const double xf = m.xf[f], yf = m.yf[f], zf = m.zf[f];
+    const double arx = m.arx[f], ary = m.ary[f], arz = m.arz[f];
+    const double lambda = m.facint[f];
+    const double flomass = F.flmass[f];
+    // facefluxuvw (faceflux_velocity.f90:78-182)
+    const double fxn = lambda, fxp = 1.0 - lambda;
+    const double xpn = m.xc[q] - m.xc[p], ypn = m.yc[q] - m.yc[p], zpn = m.zc[q] - m.zc[p];
+    const double dpn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
+    const double are = sqrt(arx * arx + ary * ary + arz * arz);
+    const double game = F.vis[p] * fxp + F.vis[q] * fxn;
+    const double de = game * are / dpn;
+    double can = -de + rmin(flomass, 0.0);
+    double cap = -de - rmax(flomass, 0.0);
+    const double vole = xpn * arx + ypn * ary + zpn * arz;
+    const SnGrad du = sngrad(p, q, arx, ary, arz, fxp, fxn, xpn, ypn, zpn, vole, F.u, F.dU);
+    const SnGrad dv = sngrad(p, q, arx, ary, arz, fxp, fxn, xpn, ypn, zpn, vole, F.v, F.dV);
+    const SnGrad dw = sngrad(p, q, arx, ary, arz, fxp, fxn, xpn, ypn, zpn, vole, F.w, F.dW);
+    const double fdue = game * ((du.xii + du.xii) * arx + (du.yii + dv.xii) * ary + (du.zii + dw.xii) * arz);
+    const double fdve = game * ((du.yii + dv.xii) * arx + (dv.yii + dv.yii) * ary + (dv.zii + dw.yii) * arz);
+    const double fdwe = game * ((du.zii + dw.xii) * arx + (dw.yii + dv.zii) * ary + (dw.zii + dw.zii) * arz);
+    const double fdui = game * are / dpn * (du.xi * xpn + du.yi * ypn + du.zi * zpn);
+    const double fdvi = game * are / dpn * (dv.xi * xpn + dv.yi * ypn + dv.zi * zpn);
+    const double fdwi = game * are / dpn * (dw.xi * xpn + dw.yi * ypn + dw.zi * zpn);
+    const double fpos = rmax(flomass, 0.0), fneg = rmin(flomass, 0.0);
+    const double fuuds = fpos * F.u[p] + fneg * F.u[q];
+    const double fvuds = fpos * F.v[p] + fneg * F.v[q];
+    const double fwuds = fpos * F.w[p] + fneg * F.w[q];
+    double ue, ve, we;
+    if (flomass >= 0.0) {
+      ue = face_value(m, prm.scheme, prm.limiter, p, q, xf, yf, zf, fxp, F.u, F.dU);
+      ve = face_value(m, prm.scheme, prm.limiter, p, q, xf, yf, zf, fxp, F.v, F.dV);
+      we = face_value(m, prm.scheme, prm.limiter, p, q, xf, yf, zf, fxp, F.w, F.dW);
+    } else {
+      ue = face_value(m, prm.scheme, prm.limiter, q, p, xf, yf, zf, fxn, F.u, F.dU);
+      ve = face_value(m, prm.scheme, prm.limiter, q, p, xf, yf, zf, fxn, F.v, F.dV);
+      we = face_value(m, prm.scheme, prm.limiter, q, p, xf, yf, zf, fxn, F.w, F.dW);
+    }
+    const double gam = prm.gds;
+    fsrc[3 * f] = -gam * (flomass * ue - fuuds) + fdue - fdui;
+    fsrc[3 * f + 1] = -gam * (flomass * ve - fvuds) + fdve - fdvi;
+    fsrc[3 * f + 2] = -gam * (flomass * we - fwuds) + fdwe - fdwi;
+    if (prm.cn) {  // a = 0.5*a (calcuvw.f90:382-384)
+      can = 0.5 * can;
+      cap = 0.5 * cap;
+    }
+    a[m.slot_pn[f]] = can;  // :168-173
+    a[m.slot_np[f]] = cap;
+    // presFaceDivInner (fieldManipulation.f90:426-442).  The reference indexes its
+    // (3,numCells) gradient argument as df(ijp,k): element ijp + 3(k-1) of the flat array.
+    const double *dP = F.dP;
+    const double xi = m.xc[p] * fxp + m.xc[q] * fxn, yi = m.yc[p] * fxp + m.yc[q] * fxn,
+                 zi = m.zc[p] * fxp + m.zc[q] * fxn;
+    const double dfxi = dP[p] * fxp + dP[q] * fxn;
+    const double dfyi = dP[p + 3] * fxp + dP[q + 3] * fxn;
+    const double dfzi = dP[p + 6] * fxp + dP[q + 6] * fxn;
+    const double fie =
+        F.p[p] * fxp + F.p[q] * fxn + dfxi * (xf - xi) + dfyi * (yf - yi) + dfzi * (zf - zi);
+    fdiv[3 * f] = fie * arx;
+    fdiv[3 * f + 1] = fie * ary;
+    fdiv[3 * f + 2] = fie * arz;
+  }
+}
+
+// Sum of the row's values in row order with `dv` in place of the diagonal (Fortran SUM).
+__device__ __forceinline__ double row_sum(const MeshView &m, const double *__restrict__ a,
+                                          int c, double dv) {
+  const int dg = m.diag[c];
+  double s = 0.0;
+  for (int k = m.ioffset[c]; k < m.ioffset[c + 1]; ++k) s = s + (k == dg ? dv : a[k]);
+  return s;
+}
+
+__global__ void k_uvw_cells(MeshView m, fcg_uvw_params prm, UvwView F, int bst_inl,
+                            int bst_out, int bst_sym, int bst_wal, double *__restrict__ a,
+                            const double *__restrict__ fsrc, const double *__restrict__ fdiv,
+                            double *__restrict__ diag_vw, double *__restrict__ rhs,
+                            double *__restrict__ ap) {
+  const double small = (double)1e-20f;  // parameters::small, modules_allocatable.f90:27
+  FCG_GRID_STRIDE(c, m.n) {
+    const int e0 = m.cf_ptr[c], e1 = m.cf_ptr[c + 1];
+    const int b0 = m.cb_ptr[c], b1 = m.cb_ptr[c + 1];
+    const double vol = m.vol[c];
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;     // su, sv, sw (:49-51)
+    double sp0 = 0.0, sp1 = 0.0, sp2 = 0.0;  // spu, spv, sp (:54-56)
+    // calcPressDiv: inner faces (fieldManipulation.f90:92-108), then every boundary face
+    // in the loop order inlet, outlet, symmetry, wall, pressure outlet (:129-160)
+    for (int e = e0; e < e1; ++e) {
+      const int ent = m.cf_ent[e];
+      const int f = (ent > 0 ? ent : -ent) - 1;
+      if (ent > 0) {
+        s0 = s0 - fdiv[3 * f];
+        s1 = s1 - fdiv[3 * f + 1];
+        s2 = s2 - fdiv[3 * f + 2];
+      } else {
+        s0 = s0 + fdiv[3 * f];
+        s1 = s1 + fdiv[3 * f + 1];
+        s2 = s2 + fdiv[3 * f + 2];
+      }
+    }
+    for (int e = b0; e < b1; ++e) {
+      const int f = m.cb_face[e];
+      const double pb = F.p[m.cb_slot[e]];
+      s0 = s0 - pb * m.arx[f];
+      s1 = s1 - pb * m.ary[f];
+      s2 = s2 - pb * m.arz[f];
+    }
+    // volume sources (:76-139)
+    if (prm.const_mflux) s0 = s0 + prm.gradPcmf * vol;
+    if (prm.buoyancy) {
+      double heat;
+      if (prm.boussinesq)
+        heat = prm.beta * prm.densit * (F.t[c] - prm.tref) * vol;
+      else
+        heat = (prm.densit - F.den[c]) * vol;
+      s0 = s0 - prm.gravx * heat;
+      s1 = s1 - prm.gravy * heat;
+      s2 = s2 - prm.gravz * heat;
+    }
+    if (prm.bdf) {
+      const double apotime = F.den[c] * vol / prm.timestep;
+      double sut = apotime * ((1.0 + prm.btime) * F.uo[c]);
+      double svt = apotime * ((1.0 + prm.btime) * F.vo[c]);
+      double swt = apotime * ((1.0 + prm.btime) * F.wo[c]);
+      if (prm.btime > (double)0.99f) {
+        sut = sut - apotime * (0.5 * prm.btime * F.uoo[c]);
+        svt = svt - apotime * (0.5 * prm.btime * F.voo[c]);
+        swt = swt - apotime * (0.5 * prm.btime * F.woo[c]);
+      }
+      s0 = s0 + sut;
+      s1 = s1 + svt;
+      s2 = s2 + swt;
+      const double add = apotime * (1.0 + 0.5 * prm.btime);
+      sp0 = sp0 + add;
+      sp1 = sp1 + add;
+      sp2 = sp2 + add;
+    }
+    // inner faces (:157-185)
+    for (int e = e0; e < e1; ++e) {
+      const int ent = m.cf_ent[e];
+      const int f = (ent > 0 ? ent : -ent) - 1;
+      if (ent > 0) {
+        s0 = s0 + fsrc[3 * f];
+        s1 = s1 + fsrc[3 * f + 1];
+        s2 = s2 + fsrc[3 * f + 2];
+      } else {
+        s0 = s0 - fsrc[3 * f];
+        s1 = s1 - fsrc[3 * f + 1];
+        s2 = s2 - fsrc[3 * f + 2];
+      }
+    }
+    // boundary loops (:223-378): inlet, outlet, symmetry, wall
+    for (int e = b0; e < b1; ++e) {
+      const int t = m.cb_type[e];
+      if (t == B_PRESSOUT) continue;
+      const int f = m.cb_face[e], b = m.cb_slot[e];
+      const double arx = m.arx[f], ary = m.ary[f], arz = m.arz[f];
+      if (t == B_INLET || t == B_OUTLET) {
+        // facefluxuvw_boundary (faceflux_velocity.f90:403-468): only cb is used
+        const double flomass = t == B_INLET ? F.fmi[b - bst_inl] : F.fmo[b - bst_out];
+        const double xpn = m.xf[f] - m.xc[c], ypn = m.yf[f] - m.yc[c], zpn = m.zf[f] - m.zc[c];
+        const double dpn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
+        const double are = sqrt(arx * arx + ary * ary + arz * arz);
+        const double de = F.vis[b] * are / dpn;
+        const double cb = -de + rmin(flomass, 0.0);
+        sp0 = sp0 - cb;
+        sp1 = sp1 - cb;
+        sp2 = sp2 - cb;
+        s0 = s0 - cb * F.u[b];
+        s1 = s1 - cb * F.v[b];
+        s2 = s2 - cb * F.w[b];
+      } else {
+        const double are = sqrt(arx * arx + ary * ary + arz * arz);
+        const double nxf = arx / are, nyf = ary / are, nzf = arz / are;
+        // dns / dnw and srds / srdw (init.f90:1002-1027)
+        const double dn = (m.xf[f] - m.xc[c]) * nxf + (m.yf[f] - m.yc[c]) * nyf +
+                          (m.zf[f] - m.zc[c]) * nzf;
+        const double srd = are / dn;
+        const double dx = m.xc[c] - m.xf[f], dy = m.yc[c] - m.yf[f], dz = m.zc[c] - m.zf[f];
+        const double dpb = sqrt(dx * dx + dy * dy + dz * dz);
+        const double upb = F.u[c] - F.u[b], vpb = F.v[c] - F.v[b], wpb = F.w[c] - F.w[b];
+        if (t == B_SYMMETRY) {  // :268-306
+          const double vsi = F.vis[b];
+          const double cf = vsi * srd;
+          const double vsol = vsi * are / dpb;
+          const double fdne = 2.0 * cf * (upb * nxf + vpb * nyf + wpb * nzf);
+          sp0 = sp0 + vsol;
+          sp1 = sp1 + vsol;
+          sp2 = sp2 + vsol;
+          s0 = s0 + vsol * F.u[c] - fdne * nxf;
+          s1 = s1 + vsol * F.v[c] - fdne * nyf;
+          s2 = s2 + vsol * F.w[c] - fdne * nzf;
+        } else {  // wall, :309-378 (laminar: viss = viscos)
+          const double viss = prm.viscos;
+          const double cf = viss * srd;
+          const double vsol = viss * are / dpb;
+          const double vnp = upb * nxf + vpb * nyf + wpb * nzf;
+          const double utp = upb - vnp * nxf, vtp = vpb - vnp * nyf, wtp = wpb - vnp * nzf;
+          sp0 = sp0 + vsol;
+          sp1 = sp1 + vsol;
+          sp2 = sp2 + vsol;
+          s0 = s0 + vsol * F.u[c] - cf * utp;
+          s1 = s1 + vsol * F.v[c] - cf * vtp;
+          s2 = s2 + vsol * F.w[c] - cf * wtp;
+        }
+      }
+    }
+    // the diagonal the reference finds in a: halved with the rest of a under CN (:383)
+    double d_in = a[m.diag[c]];
+    if (prm.cn) d_in = 0.5 * d_in;
+    const double apotime = prm.cn ? F.den[c] * vol / prm.timestep : 0.0;
+    // u (:392-438)
+    if (prm.cn) {
+      for (int e = e0; e < e1; ++e) {
+        const int ent = m.cf_ent[e];
+        const int f = (ent > 0 ? ent : -ent) - 1;
+        const int o = ent > 0 ? m.neighbour[f] : m.owner[f];
+        s0 = s0 - a[m.cf_slot[e]] * F.uo[o];
+      }
+      s0 = s0 + (apotime + (row_sum(m, a, c, d_in) - d_in)) * F.uo[c];
+      sp0 = sp0 + apotime;
+    }
+    double du = (sp0 - (row_sum(m, a, c, d_in) - d_in)) * prm.urfr[0];
+    rhs[c] = s0 + prm.urfm[0] * du * F.u[c];
+    ap[c] = 1.0 / (du + small);
+    // v (:447-495): its CN term sees the u diagonal; its diagonal assembly a zero one
+    if (prm.cn) {
+      for (int e = e0; e < e1; ++e) {
+        const int ent = m.cf_ent[e];
+        const int f = (ent > 0 ? ent : -ent) - 1;
+        const int o = ent > 0 ? m.neighbour[f] : m.owner[f];
+        s1 = s1 - a[m.cf_slot[e]] * F.vo[o];
+      }
+      s1 = s1 + (apotime + (row_sum(m, a, c, du) - du)) * F.vo[c];
+      sp1 = sp1 + apotime;
+    }
+    const double dv = (sp1 - (row_sum(m, a, c, 0.0) - 0.0)) * prm.urfr[1];
+    rhs[m.n + c] = s1 + prm.urfm[1] * dv * F.v[c];
+    ap[m.n + c] = 1.0 / (dv + small);
+    // w (:504-553): its CN term sees the v diagonal
+    if (prm.cn) {
+      for (int e = e0; e < e1; ++e) {
+        const int ent = m.cf_ent[e];
+        const int f = (ent > 0 ? ent : -ent) - 1;
+        const int o = ent > 0 ? m.neighbour[f] : m.owner[f];
+        s2 = s2 - a[m.cf_slot[e]] * F.wo[o];
+      }
+      s2 = s2 + (apotime + (row_sum(m, a, c, dv) - dv)) * F.wo[c];
+      sp2 = sp2 + apotime;
+    }
+    const double dw = (sp2 - (row_sum(m, a, c, 0.0) - 0.0)) * prm.urfr[2];
+    rhs[2 * m.n + c] = s2 + prm.urfm[2] * dw * F.w[c];
+    ap[2 * m.n + c] = 1.0 / (dw + small);
+    a[m.diag[c]] = du;
+    diag_vw[c] = dv;
+    diag_vw[m.n + c] = dw;
+  }
+}
+
+}  // namespace
+
+extern "C" int fcg_calcuvw(fcg_context *c, const fcg_uvw_params *prm, const fcg_uvw_fields *f,
+                           double *a, double *diag_vw, double *rhs, double *ap) {
+  if (!c || !prm || !f) return FCG_ERR_ARG;
+  if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_calcuvw before fcg_bind_mesh");
+  const bool need_old = prm->bdf || prm->cn;
+  const bool need_oo = prm->bdf && prm->btime > (double)0.99f;
+  const bool need_t = prm->buoyancy && prm->boussinesq;
+  const int ninl = c->cnt[B_INLET], nout = c->cnt[B_OUTLET];
+  if (!f->u || !f->v || !f->w || !f->p || !f->vis || !f->den || !f->dUdxi || !f->dVdxi ||
+      !f->dWdxi || !f->dPdxi || (c->nin > 0 && !f->flmass) || (need_t && !f->t) ||
+      (need_old && (!f->uo || !f->vo || !f->wo)) || (need_oo && (!f->uoo || !f->voo || !f->woo)) ||
+      (ninl > 0 && !f->fmi) || (nout > 0 && !f->fmo) || !a || !diag_vw || !rhs || !ap)
+    return set_error(c, FCG_ERR_ARG, "fcg_calcuvw: NULL array the parameters need");
+  if (prm->scheme < FCG_CONV_CDS || prm->scheme > FCG_CONV_FLUX_LIMITER || prm->limiter < 0 ||
+      prm->limiter > FCG_LIM_UDS)
+    return set_error(c, FCG_ERR_ARG, "fcg_calcuvw: unknown scheme or limiter");
+  if ((prm->bdf || prm->cn) && !(prm->timestep != 0.0))
+    return set_error(c, FCG_ERR_ARG, "fcg_calcuvw: timestep must be nonzero");
+  if (c->n < 3)
+    return set_error(c, FCG_ERR_ARG,
+                     "fcg_calcuvw: presFaceDivInner's df(ijp,3) index needs numCells >= 3");
+  FCG_CUDA_TRY(c, cudaSetDevice(c->device));
+  const size_t nt = sizeof(double) * c->ntot, n1 = sizeof(double) * c->n, n3 = 3 * n1;
+  const size_t fb = sizeof(double) * (c->nin > 0 ? c->nin : 1);
+  struct In {
+    const double *src;
+    size_t bytes;
+    bool need;
+  } ins[] = {{f->u, nt, true},      {f->v, nt, true},        {f->w, nt, true},
+             {f->p, nt, true},      {f->vis, nt, true},      {f->den, n1, true},
+             {f->t, n1, need_t},    {f->uo, n1, need_old},   {f->vo, n1, need_old},
+             {f->wo, n1, need_old}, {f->uoo, n1, need_oo},   {f->voo, n1, need_oo},
+             {f->woo, n1, need_oo}, {f->dUdxi, n3, true},    {f->dVdxi, n3, true},
+             {f->dWdxi, n3, true},  {f->dPdxi, n3, true},    {f->flmass, fb, c->nin > 0},
+             {f->fmi, sizeof(double) * (ninl > 0 ? ninl : 1), ninl > 0},
+             {f->fmo, sizeof(double) * (nout > 0 ? nout : 1), nout > 0}};
+  const int NI = (int)(sizeof(ins) / sizeof(ins[0]));
+  const double *dev[20] = {};
+  int rc;
+  for (int k = 0; k < NI; ++k) {
+    if (!ins[k].need) continue;
+    void *d;
+    bool h;
+    if ((rc = stage_in(c, ins[k].src, ins[k].bytes, k, true, &d, &h))) return rc;
+    dev[k] = (const double *)d;
+  }
+  UvwView V{dev[0],  dev[1],  dev[2],  dev[3],  dev[4],  dev[5],  dev[6],
+            dev[7],  dev[8],  dev[9],  dev[10], dev[11], dev[12], dev[13],
+            dev[14], dev[15], dev[16], dev[17], dev[18], dev[19]};
+  void *da, *ddv, *drhs, *dap;
+  bool ha, hdv, hrhs, hap;
+  if ((rc = stage_in(c, a, sizeof(double) * c->nnz, NI, true, &da, &ha)) ||
+      (rc = stage_in(c, diag_vw, 2 * n1, NI + 1, false, &ddv, &hdv)) ||
+      (rc = stage_in(c, rhs, n3, NI + 2, false, &drhs, &hrhs)) ||
+      (rc = stage_in(c, ap, n3, NI + 3, false, &dap, &hap)))
+    return rc;
+  // face terms: 3 sources + 3 pressure-divergence terms per inner face
+  FCG_CUDA_TRY(c, c->scratch.ensure(6 * fb));
+  double *fsrc = c->scratch.as<double>(), *fdiv = fsrc + 3 * (c->nin > 0 ? c->nin : 1);
+  const MeshView &m = c->mv;
+  if (m.nin > 0) {
+    k_uvw_faces<<<grid_for(m.nin, c->num_sms), kTPB, 0, c->stream>>>(m, *prm, V, (double *)da,
+                                                                        fsrc, fdiv);
+    FCG_CHECK_LAUNCH(c, "k_uvw_faces");
+  }
+  k_uvw_cells<<<grid_for(m.n, c->num_sms), kTPB, 0, c->stream>>>(
+      m, *prm, V, c->bst[B_INLET], c->bst[B_OUTLET], c->bst[B_SYMMETRY], c->bst[B_WALL],
+      (double *)da, fsrc, fdiv, (double *)ddv, (double *)drhs, (double *)dap);
+  FCG_CHECK_LAUNCH(c, "k_uvw_cells");
+  if ((rc = stage_out(c, a, da, sizeof(double) * c->nnz, ha)) ||
+      (rc = stage_out(c, diag_vw, ddv, 2 * n1, hdv)) ||
+      (rc = stage_out(c, rhs, drhs, n3, hrhs)) || (rc = stage_out(c, ap, dap, n3, hap)))
+    return rc;
+  if (ha || hdv || hrhs || hap) FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return FCG_OK;
+}

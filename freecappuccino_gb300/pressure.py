@@ -222,6 +222,58 @@ class Context:
                     "fcg_continuity_errors")
         return res, sl.value, sg.value
 
+    # -- momentum assembly (calcuvw.f90:48-438) ------------------------------------------
+    def calcuvw(self, u, v, w, p, vis, den, dUdxi, dVdxi, dWdxi, dPdxi, flmass, a,
+                fmi=None, fmo=None, *, scheme="muscl", limiter="uds", gds=1.0, viscos=1e-3,
+                urf=(0.7, 0.7, 0.7), urfr=None, urfm=None, bdf=False, cn=False, timestep=1.0,
+                btime=0.0, const_mflux=False, gradPcmf=0.0, buoyancy=False, boussinesq=False,
+                beta=0.0, densit=1.0, tref=0.0, grav=(0.0, 0.0, 0.0), t=None, uo=None,
+                vo=None, wo=None, uoo=None, voo=None, woo=None):
+        """calcuvw without its solves.  `a` carries the diagonal the reference finds in
+        its module array (it is subtracted from the row sums).  Returns a dict: `a` (the
+        off-diagonals and the u diagonal), `diag_vw` (2, n), `rhs` (3, n), `ap` (3, n).
+        urfr/urfm default to 1/urf and 1-urf."""
+        urfr = [1.0 / x for x in urf] if urfr is None else list(urfr)
+        urfm = [1.0 - x for x in urf] if urfm is None else list(urfm)
+        prm = _lib.UvwParams(_lib.CONV_SCHEMES[scheme], _lib.LIMITERS[limiter], float(gds),
+                             float(viscos), (C.c_double * 3)(*urfr), (C.c_double * 3)(*urfm),
+                             int(bool(bdf)), int(bool(cn)), float(timestep), float(btime),
+                             int(bool(const_mflux)), float(gradPcmf), int(bool(buoyancy)),
+                             int(bool(boussinesq)), float(beta), float(densit), float(tref),
+                             *[float(g) for g in grav])
+        vals = dict(u=u, v=v, w=w, p=p, vis=vis, den=den, t=t, uo=uo, vo=vo, wo=wo, uoo=uoo,
+                    voo=voo, woo=woo, dUdxi=dUdxi, dVdxi=dVdxi, dWdxi=dWdxi, dPdxi=dPdxi,
+                    flmass=flmass, fmi=fmi, fmo=fmo)
+        self._follow(*[x for x in vals.values() if x is not None], a)
+        ins = {k: (None if x is None or (k in ("fmi", "fmo") and len(x) == 0) else _host(x))
+               for k, x in vals.items()}
+        fl = _lib.UvwFields(*[_ptr(ins[k]) for k in _lib.UVW_FIELDS])
+        a = a.clone() if _is_torch(a) else np.array(a, dtype=np.float64)
+        dvw = _like(a, (2, self.n))
+        rhs = _like(a, (3, self.n))
+        ap = _like(a, (3, self.n))
+        self._check(self.lib.fcg_calcuvw(self.h, C.byref(prm), C.byref(fl), _ptr(a), _ptr(dvw),
+                                         _ptr(rhs), _ptr(ap)), "fcg_calcuvw")
+        return dict(a=a, diag_vw=dvw, rhs=rhs, ap=ap)
+
+    def uvw_systems(self, asm):
+        """The three systems of a calcuvw result as the planar values (3, nnz) and
+        right-hand sides (3, n) that bicgstab_multi takes: the off-diagonals shared, each
+        with its own diagonal."""
+        a = asm["a"]
+        lib = a if _is_torch(a) else np
+        a3 = lib.stack([a, a.clone() if _is_torch(a) else a.copy(),
+                        a.clone() if _is_torch(a) else a.copy()])
+        d = self._diag0()
+        a3[1, d] = asm["diag_vw"][0]
+        a3[2, d] = asm["diag_vw"][1]
+        return a3, asm["rhs"]
+
+    def _diag0(self):
+        if getattr(self, "_diag_cache", None) is None:
+            self._diag_cache = self.create_csr()[2].astype(np.int64) - 1
+        return self._diag_cache
+
     # -- PISO pressure path (PISO_multiple_correction.f90:83-307) -----------------------
     def piso_hbya(self, h, u, v, w, apu, apv, apw, den=None, *, timestep=1.0, btime=0.0,
                   bdf=False, cn=False, buoyancy=False, boussinesq=False, beta=0.0, densit=1.0,

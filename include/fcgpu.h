@@ -185,6 +185,67 @@ int fcg_continuity_errors(fcg_context *ctx, const double *flmass, const double *
                           const double *fmo, double *res, double *sum_local, double *global);
 
 /* ---------------------------------------------------------------------------
+ * Momentum assembly (calcuvw.f90:48-438): the producer of the u, v, w systems.
+ * ------------------------------------------------------------------------- */
+
+/* Face-value schemes of face_value (interpolation.f90:20-60), in the order of its flags
+ * lcds, lcdsc, lcds_flnt, l2nd_flnt, lmuscl_flnt, flux_limiter; MUSCL is also its default. */
+#define FCG_CONV_CDS 0
+#define FCG_CONV_CDS_CORRECTED 1
+#define FCG_CONV_CENTRAL 2
+#define FCG_CONV_SECOND_UPWIND 3
+#define FCG_CONV_MUSCL 4
+#define FCG_CONV_FLUX_LIMITER 5
+/* Limiters of face_value_2nd_upwind_flux_limiter (interpolation.f90:364-389); UDS is its
+ * psi = 1 branch. */
+#define FCG_LIM_SMART 0
+#define FCG_LIM_AVL 1
+#define FCG_LIM_MUSCL 2
+#define FCG_LIM_UMIST 3
+#define FCG_LIM_KOREN 4
+#define FCG_LIM_CHARM 5
+#define FCG_LIM_OSPRE 6
+#define FCG_LIM_UDS 7
+
+/* Parameters calcuvw reads (modules_allocatable.f90:40-135).  urfr = 1/urf and urfm =
+ * 1 - urf per component (u, v, w) as the reference stores them; gds = gds(iu). */
+typedef struct fcg_uvw_params {
+  int scheme, limiter;
+  double gds, viscos;
+  double urfr[3], urfm[3];
+  int bdf, cn;
+  double timestep, btime;
+  int const_mflux;
+  double gradPcmf;
+  int buoyancy, boussinesq;
+  double beta, densit, tref, gravx, gravy, gravz;
+} fcg_uvw_params;
+
+/* Fields calcuvw reads.  u, v, w, p, vis [numTotal]; den, t, uo..woo [numCells] (t, uo..woo
+ * may be NULL where the parameters do not read them); dUdxi..dPdxi (3,numCells);
+ * flmass[numInnerFaces]; fmi[ninl], fmo[nout]. */
+typedef struct fcg_uvw_fields {
+  const double *u, *v, *w, *p, *vis, *den, *t;
+  const double *uo, *vo, *wo, *uoo, *voo, *woo;
+  const double *dUdxi, *dVdxi, *dWdxi, *dPdxi;
+  const double *flmass, *fmi, *fmo;
+} fcg_uvw_fields;
+
+/* calcuvw.f90:48-438 without its solves: the sources of calcPressDiv
+ * (fieldManipulation.f90:89-160), the volume sources (:76-139), facefluxuvw on the inner
+ * faces (faceflux_velocity.f90:35-184, sngrad gradients.f90:547-721 with nrelax 0 and the
+ * skewness approach), the inlet, outlet, symmetry and wall terms (:223-378),
+ * Crank-Nicolson (:381-412 and its v, w twins), the under-relaxed diagonals and ap*.
+ * a[nnz] in/out: its incoming diagonal is read (the reference subtracts it from the
+ * row sum) and the result holds the off-diagonals and the u system's diagonal.  Out:
+ * diag_vw[2*numCells] the v and w diagonals (the reference writes them into a(diag)
+ * before bicgstab(v) and bicgstab(w)), rhs[3*numCells] the right-hand side of each
+ * solve, ap[3*numCells] = apu, apv, apw.  Turbulence stresses (lturb) are not part of
+ * the path. */
+int fcg_calcuvw(fcg_context *ctx, const fcg_uvw_params *prm, const fcg_uvw_fields *f,
+                double *a, double *diag_vw, double *rhs, double *ap);
+
+/* ---------------------------------------------------------------------------
  * PISO pressure path (PISO_multiple_correction.f90:83-307).
  * ------------------------------------------------------------------------- */
 

@@ -832,6 +832,408 @@ int orc_flux_correct(const orc_mesh *m, const int *slot_pn, const double *a, con
 }
 
 /* ------------------------------------------------------------------------- */
+/* Momentum assembly: calcuvw.f90:48-438                                       */
+/* ------------------------------------------------------------------------- */
+
+/* MIN / MAX keeping the first argument on ties. */
+static double rmin(double a, double b) { return b < a ? b : a; }
+static double rmax(double a, double b) { return b > a ? b : a; }
+
+/* interpolation.f90:65-93 */
+static double fv_cds(int ijp, int ijn, double lambda, const double *fi) {
+  const double fxn = lambda, fxp = 1.0 - lambda;
+  return F(fi, ijp) * fxp + F(fi, ijn) * fxn;
+}
+
+/* interpolation.f90:99-139 */
+static double fv_cdsc(const orc_mesh *m, int ijp, int ijn, double xf, double yf, double zf,
+                      double lambda, const double *fi, const double *g) {
+  const double fxn = lambda, fxp = 1.0 - lambda;
+  const double xi = F(m->xc, ijp) * fxp + F(m->xc, ijn) * fxn;
+  const double yi = F(m->yc, ijp) * fxp + F(m->yc, ijn) * fxn;
+  const double zi = F(m->zc, ijp) * fxp + F(m->zc, ijn) * fxn;
+  const double dfixi = G3(g, 1, ijp) * fxp + G3(g, 1, ijn) * fxn;
+  const double dfiyi = G3(g, 2, ijp) * fxp + G3(g, 2, ijn) * fxn;
+  const double dfizi = G3(g, 3, ijp) * fxp + G3(g, 3, ijn) * fxn;
+  return F(fi, ijp) * fxp + F(fi, ijn) * fxn +
+         (dfixi * (xf - xi) + dfiyi * (yf - yi) + dfizi * (zf - zi));
+}
+
+/* interpolation.f90:204-249 */
+static double fv_2nd_upwind(const orc_mesh *m, int inp, double xf, double yf, double zf,
+                            const double *fi, const double *g) {
+  const double gradfidr = G3(g, 1, inp) * (xf - F(m->xc, inp)) + G3(g, 2, inp) * (yf - F(m->yc, inp)) +
+                          G3(g, 3, inp) * (zf - F(m->zc, inp));
+  return F(fi, inp) + gradfidr;
+}
+
+/* interpolation.f90:254-320 */
+static double fv_muscl(const orc_mesh *m, int inp, int inn, double xf, double yf, double zf,
+                       const double *fi, const double *g) {
+  const double theta = 0.125;
+  const double phi_p = F(fi, inp), phi_n = F(fi, inn);
+  const double xcp = F(m->xc, inp), ycp = F(m->yc, inp), zcp = F(m->zc, inp);
+  const double xcn = F(m->xc, inn), ycn = F(m->yc, inn), zcn = F(m->zc, inn);
+  const double gpx = G3(g, 1, inp), gpy = G3(g, 2, inp), gpz = G3(g, 3, inp);
+  const double gnx = G3(g, 1, inn), gny = G3(g, 2, inn), gnz = G3(g, 3, inn);
+  const double gr2 = gpx * (xf - xcp) + gpy * (yf - ycp) + gpz * (zf - zcp);
+  const double grc = gpx * (xf - xcp) + gpy * (yf - ycp) + gpz * (zf - zcp) + gnx * (xf - xcn) +
+                     gny * (yf - ycn) + gnz * (zf - zcn);
+  const double fv2 = (phi_p + gr2);
+  const double fvc = 0.5 * (phi_p + phi_n + grc);
+  return theta * fvc + (1.0 - theta) * fv2;
+}
+
+/* interpolation.f90:325-393 */
+static double fv_limiter(const orc_mesh *m, int limiter, int ijp, int ijn, double lambda,
+                         const double *u, const double *g) {
+  const double fxp = 1.0 - lambda;
+  const double xpn = F(m->xc, ijn) - F(m->xc, ijp);
+  const double ypn = F(m->yc, ijn) - F(m->yc, ijp);
+  const double zpn = F(m->zc, ijn) - F(m->zc, ijp);
+  const double r = (2 * G3(g, 1, ijp) * xpn + 2 * G3(g, 2, ijp) * ypn + 2 * G3(g, 3, ijp) * zpn) /
+                       (F(u, ijn) - F(u, ijp)) -
+                   1.0;
+  double psi;
+  if (limiter == 0)
+    psi = rmax(0., rmin(rmin(2. * r, 0.75 * r + 0.25), 4.));
+  else if (limiter == 1)
+    psi = rmax(0., rmin(rmin(1.5 * r, 0.75 * r + 0.25), 2.5));
+  else if (limiter == 2)
+    psi = rmax(0., rmin(rmin(2. * r, 0.5 * r + 0.5), 2.));
+  else if (limiter == 3)
+    psi = rmax(0., rmin(rmin(rmin(2. * r, 0.75 * r + 0.25), 0.25 * r + 0.75), 2.));
+  else if (limiter == 4)
+    psi = rmax(0., rmin(rmin(2. * r, 2. / 3. * r + 1. / 3.), 2.));
+  else if (limiter == 5)
+    psi = (r + fabs(r)) * (3 * r + 1.) / (2 * ((r + 1.) * (r + 1.)));
+  else if (limiter == 6)
+    psi = 1.5 * r * (r + 1.) / (r * r + r + 1.);
+  else
+    psi = 1.0;
+  return F(u, ijp) + fxp * psi * (F(u, ijn) - F(u, ijp));
+}
+
+/* face_value (interpolation.f90:20-60) */
+static double face_value(const orc_mesh *m, const orc_uvw_params *prm, int ijp, int ijn,
+                         double xf, double yf, double zf, double lambda, const double *u,
+                         const double *g) {
+  switch (prm->scheme) {
+    case 0: return fv_cds(ijp, ijn, lambda, u);
+    case 1: return fv_cdsc(m, ijp, ijn, xf, yf, zf, lambda, u, g);
+    case 2: return face_value_central(m, ijp, ijn, xf, yf, zf, u, g);
+    case 3: return fv_2nd_upwind(m, ijp, xf, yf, zf, u, g);
+    case 5: return fv_limiter(m, prm->limiter, ijp, ijn, lambda, u, g);
+    default: return fv_muscl(m, ijp, ijn, xf, yf, zf, u, g);
+  }
+}
+
+/* sngrad_scalar_field with nrelax = 0, approach 'skewness' (gradients.f90:547-721). */
+static void sngrad(const orc_mesh *m, int ijp, int ijn, double arx, double ary, double arz,
+                   double lambda, const double *fi, const double *g, double *dfixi,
+                   double *dfiyi, double *dfizi, double *dfixii, double *dfiyii, double *dfizii) {
+  const double fxn = lambda, fxp = 1.0 - lambda;
+  const double xpn = F(m->xc, ijn) - F(m->xc, ijp);
+  const double ypn = F(m->yc, ijn) - F(m->yc, ijp);
+  const double zpn = F(m->zc, ijn) - F(m->zc, ijp);
+  const double costn = 1.0;
+  const double vole = xpn * arx + ypn * ary + zpn * arz;
+  *dfixi = G3(g, 1, ijp) * fxp + G3(g, 1, ijn) * fxn;
+  *dfiyi = G3(g, 2, ijp) * fxp + G3(g, 2, ijn) * fxn;
+  *dfizi = G3(g, 3, ijp) * fxp + G3(g, 3, ijn) * fxn;
+  const double d1x = costn, d1y = costn, d1z = costn;
+  const double d2x = xpn * costn, d2y = ypn * costn, d2z = zpn * costn;
+  *dfixii = *dfixi * d1x + arx / vole * (F(fi, ijn) - F(fi, ijp) - *dfixi * d2x - *dfiyi * d2y - *dfizi * d2z);
+  *dfiyii = *dfiyi * d1y + ary / vole * (F(fi, ijn) - F(fi, ijp) - *dfixi * d2x - *dfiyi * d2y - *dfizi * d2z);
+  *dfizii = *dfizi * d1z + arz / vole * (F(fi, ijn) - F(fi, ijp) - *dfixi * d2x - *dfiyi * d2y - *dfizi * d2z);
+}
+
+/* facefluxuvw for inner faces (faceflux_velocity.f90:35-184). */
+static void facefluxuvw(const orc_mesh *m, const orc_uvw_params *prm, int ijp, int ijn,
+                        double xf, double yf, double zf, double arx, double ary, double arz,
+                        double flomass, double lambda, double gam, const double *u,
+                        const double *v, const double *w, const double *vis,
+                        const double *dUdxi, const double *dVdxi, const double *dWdxi,
+                        double *cap, double *can, double *sup, double *svp, double *swp) {
+  const double fxn = lambda, fxp = 1.0 - lambda;
+  const double xpn = F(m->xc, ijn) - F(m->xc, ijp);
+  const double ypn = F(m->yc, ijn) - F(m->yc, ijp);
+  const double zpn = F(m->zc, ijn) - F(m->zc, ijp);
+  const double dpn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
+  const double are = sqrt(arx * arx + ary * ary + arz * arz);
+  const double game = F(vis, ijp) * fxp + F(vis, ijn) * fxn;
+  const double de = game * are / dpn;
+  *can = -de + rmin(flomass, 0.0);
+  *cap = -de - rmax(flomass, 0.0);
+  double duxi, duyi, duzi, duxii, duyii, duzii, dvxi, dvyi, dvzi, dvxii, dvyii, dvzii;
+  double dwxi, dwyi, dwzi, dwxii, dwyii, dwzii;
+  sngrad(m, ijp, ijn, arx, ary, arz, lambda, u, dUdxi, &duxi, &duyi, &duzi, &duxii, &duyii, &duzii);
+  sngrad(m, ijp, ijn, arx, ary, arz, lambda, v, dVdxi, &dvxi, &dvyi, &dvzi, &dvxii, &dvyii, &dvzii);
+  sngrad(m, ijp, ijn, arx, ary, arz, lambda, w, dWdxi, &dwxi, &dwyi, &dwzi, &dwxii, &dwyii, &dwzii);
+  const double fdue = game * ((duxii + duxii) * arx + (duyii + dvxii) * ary + (duzii + dwxii) * arz);
+  const double fdve = game * ((duyii + dvxii) * arx + (dvyii + dvyii) * ary + (dvzii + dwyii) * arz);
+  const double fdwe = game * ((duzii + dwxii) * arx + (dwyii + dvzii) * ary + (dwzii + dwzii) * arz);
+  const double fdui = game * are / dpn * (duxi * xpn + duyi * ypn + duzi * zpn);
+  const double fdvi = game * are / dpn * (dvxi * xpn + dvyi * ypn + dvzi * zpn);
+  const double fdwi = game * are / dpn * (dwxi * xpn + dwyi * ypn + dwzi * zpn);
+  const double fuuds = rmax(flomass, 0.0) * F(u, ijp) + rmin(flomass, 0.0) * F(u, ijn);
+  const double fvuds = rmax(flomass, 0.0) * F(v, ijp) + rmin(flomass, 0.0) * F(v, ijn);
+  const double fwuds = rmax(flomass, 0.0) * F(w, ijp) + rmin(flomass, 0.0) * F(w, ijn);
+  double ue, ve, we;
+  if (flomass >= 0.0) {
+    ue = face_value(m, prm, ijp, ijn, xf, yf, zf, fxp, u, dUdxi);
+    ve = face_value(m, prm, ijp, ijn, xf, yf, zf, fxp, v, dVdxi);
+    we = face_value(m, prm, ijp, ijn, xf, yf, zf, fxp, w, dWdxi);
+  } else {
+    ue = face_value(m, prm, ijn, ijp, xf, yf, zf, fxn, u, dUdxi);
+    ve = face_value(m, prm, ijn, ijp, xf, yf, zf, fxn, v, dVdxi);
+    we = face_value(m, prm, ijn, ijp, xf, yf, zf, fxn, w, dWdxi);
+  }
+  const double fuhigh = flomass * ue, fvhigh = flomass * ve, fwhigh = flomass * we;
+  *sup = -gam * (fuhigh - fuuds) + fdue - fdui;
+  *svp = -gam * (fvhigh - fvuds) + fdve - fdvi;
+  *swp = -gam * (fwhigh - fwuds) + fdwe - fdwi;
+}
+
+/* The cb coefficient of facefluxuvw_boundary (faceflux_velocity.f90:403-468): the only
+ * result calcuvw's inlet and outlet loops use. */
+static double boundary_cb(const orc_mesh *m, int ijp, int ijb, int iface, double flomass,
+                          const double *vis) {
+  const double xpn = F(m->xf, iface) - F(m->xc, ijp);
+  const double ypn = F(m->yf, iface) - F(m->yc, ijp);
+  const double zpn = F(m->zf, iface) - F(m->zc, ijp);
+  const double dpn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
+  const double arx = F(m->arx, iface), ary = F(m->ary, iface), arz = F(m->arz, iface);
+  const double are = sqrt(arx * arx + ary * ary + arz * arz);
+  const double game = F(vis, ijb);
+  const double de = game * are / dpn;
+  return -de + rmin(flomass, 0.0);
+}
+
+/* Fortran SUM over a(ioffset(i):ioffset(i+1)-1). */
+static double row_sum(const int *ioffset, const double *a, int i) {
+  double s = 0.0;
+  for (int k = F(ioffset, i); k <= F(ioffset, i + 1) - 1; ++k) s = s + F(a, k);
+  return s;
+}
+
+int orc_calcuvw(const orc_mesh *m, const int *ioffset, const int *diag, const int *slot_pn,
+                const int *slot_np, const orc_uvw_params *prm, const double *u, const double *v,
+                const double *w, const double *p, const double *vis, const double *den,
+                const double *t, const double *uo, const double *vo, const double *wo,
+                const double *uoo, const double *voo, const double *woo, const double *dUdxi,
+                const double *dVdxi, const double *dWdxi, const double *dPdxi,
+                const double *flmass, const double *fmi, const double *fmo, double *a,
+                double *diag_vw, double *rhs, double *ap) {
+  const int n = m->numCells, nnz = F(ioffset, n + 1) - 1;
+  const double small = orc_const_small_src();
+  if (n < 3) return -1;
+  double *su = calloc(n, sizeof(double)), *sv = calloc(n, sizeof(double)),
+         *sw = calloc(n, sizeof(double)), *spu = calloc(n, sizeof(double)),
+         *spv = calloc(n, sizeof(double)), *sp = calloc(n, sizeof(double)),
+         *du = calloc(n, sizeof(double));
+  if (!su || !sv || !sw || !spu || !spv || !sp || !du) return -9;
+
+  /* calcPressDiv (fieldManipulation.f90:57-160), the pressure gradient given */
+  for (int i = 1; i <= m->numInnerFaces; ++i) {
+    const int ijp = F(m->owner, i), ijn = F(m->neighbour, i);
+    const double fxn = F(m->facint, i), fxp = 1.0 - fxn;
+    const double xi = F(m->xc, ijp) * fxp + F(m->xc, ijn) * fxn;
+    const double yi = F(m->yc, ijp) * fxp + F(m->yc, ijn) * fxn;
+    const double zi = F(m->zc, ijp) * fxp + F(m->zc, ijn) * fxn;
+    /* df(ijp,k) on the (3,numCells) array dPdxi: flat element ijp + 3(k-1) */
+    const double dfxi = dPdxi[ijp - 1] * fxp + dPdxi[ijn - 1] * fxn;
+    const double dfyi = dPdxi[ijp - 1 + 3] * fxp + dPdxi[ijn - 1 + 3] * fxn;
+    const double dfzi = dPdxi[ijp - 1 + 6] * fxp + dPdxi[ijn - 1 + 6] * fxn;
+    const double fie = F(p, ijp) * fxp + F(p, ijn) * fxn + dfxi * (F(m->xf, i) - xi) +
+                       dfyi * (F(m->yf, i) - yi) + dfzi * (F(m->zf, i) - zi);
+    const double dfxe = fie * F(m->arx, i), dfye = fie * F(m->ary, i), dfze = fie * F(m->arz, i);
+    F(su, ijp) = F(su, ijp) - dfxe;
+    F(sv, ijp) = F(sv, ijp) - dfye;
+    F(sw, ijp) = F(sw, ijp) - dfze;
+    F(su, ijn) = F(su, ijn) + dfxe;
+    F(sv, ijn) = F(sv, ijn) + dfye;
+    F(sw, ijn) = F(sw, ijn) + dfze;
+  }
+  {
+    const int cnt[5] = {m->ninl, m->nout, m->nsym, m->nwal, m->npru};
+    const int fst[5] = {m->iInletFacesStart, m->iOutletFacesStart, m->iSymmetryFacesStart,
+                        m->iWallFacesStart, m->iPressOutletFacesStart};
+    const int bst[5] = {iInletStart(m), iOutletStart(m), iSymmetryStart(m), iWallStart(m),
+                        iPressOutletStart(m)};
+    for (int ty = 0; ty < 5; ++ty)
+      for (int i = 1; i <= cnt[ty]; ++i) {
+        const int iface = fst[ty] + i, ijp = F(m->owner, iface), ijb = bst[ty] + i;
+        F(su, ijp) = F(su, ijp) - F(p, ijb) * F(m->arx, iface);
+        F(sv, ijp) = F(sv, ijp) - F(p, ijb) * F(m->ary, iface);
+        F(sw, ijp) = F(sw, ijp) - F(p, ijb) * F(m->arz, iface);
+      }
+  }
+  /* volume sources (:76-139) */
+  for (int inp = 1; inp <= n; ++inp) {
+    if (prm->const_mflux) F(su, inp) = F(su, inp) + prm->gradPcmf * F(m->vol, inp);
+    if (prm->buoyancy) {
+      double heat;
+      if (prm->boussinesq)
+        heat = prm->beta * prm->densit * (F(t, inp) - prm->tref) * F(m->vol, inp);
+      else
+        heat = (prm->densit - F(den, inp)) * F(m->vol, inp);
+      F(su, inp) = F(su, inp) - prm->gravx * heat;
+      F(sv, inp) = F(sv, inp) - prm->gravy * heat;
+      F(sw, inp) = F(sw, inp) - prm->gravz * heat;
+    }
+    if (prm->bdf) {
+      const double apotime = F(den, inp) * F(m->vol, inp) / prm->timestep;
+      double sut = apotime * ((1 + prm->btime) * F(uo, inp));
+      double svt = apotime * ((1 + prm->btime) * F(vo, inp));
+      double swt = apotime * ((1 + prm->btime) * F(wo, inp));
+      if (prm->btime > (double)0.99f) {
+        sut = sut - apotime * ((double)0.5f * prm->btime * F(uoo, inp));
+        svt = svt - apotime * ((double)0.5f * prm->btime * F(voo, inp));
+        swt = swt - apotime * ((double)0.5f * prm->btime * F(woo, inp));
+      }
+      F(su, inp) = F(su, inp) + sut;
+      F(sv, inp) = F(sv, inp) + svt;
+      F(sw, inp) = F(sw, inp) + swt;
+      F(spu, inp) = F(spu, inp) + apotime * (1 + (double)0.5f * prm->btime);
+      F(spv, inp) = F(spv, inp) + apotime * (1 + (double)0.5f * prm->btime);
+      F(sp, inp) = F(sp, inp) + apotime * (1 + (double)0.5f * prm->btime);
+    }
+  }
+  /* inner faces (:157-185) */
+  for (int i = 1; i <= m->numInnerFaces; ++i) {
+    const int ijp = F(m->owner, i), ijn = F(m->neighbour, i);
+    double cap, can, sup, svp, swp;
+    facefluxuvw(m, prm, ijp, ijn, F(m->xf, i), F(m->yf, i), F(m->zf, i), F(m->arx, i),
+                F(m->ary, i), F(m->arz, i), F(flmass, i), F(m->facint, i), prm->gds, u, v, w,
+                vis, dUdxi, dVdxi, dWdxi, &cap, &can, &sup, &svp, &swp);
+    F(a, F(slot_pn, i)) = can;
+    F(a, F(slot_np, i)) = cap;
+    F(su, ijp) = F(su, ijp) + sup;
+    F(sv, ijp) = F(sv, ijp) + svp;
+    F(sw, ijp) = F(sw, ijp) + swp;
+    F(su, ijn) = F(su, ijn) - sup;
+    F(sv, ijn) = F(sv, ijn) - svp;
+    F(sw, ijn) = F(sw, ijn) - swp;
+  }
+  /* inlet and outlet (:223-264) */
+  for (int pass = 0; pass < 2; ++pass) {
+    const int cnt = pass == 0 ? m->ninl : m->nout;
+    const int fst = pass == 0 ? m->iInletFacesStart : m->iOutletFacesStart;
+    const int bst = pass == 0 ? iInletStart(m) : iOutletStart(m);
+    const double *fm = pass == 0 ? fmi : fmo;
+    for (int i = 1; i <= cnt; ++i) {
+      const int iface = fst + i, ijp = F(m->owner, iface), ijb = bst + i;
+      const double cb = boundary_cb(m, ijp, ijb, iface, F(fm, i), vis);
+      F(spu, ijp) = F(spu, ijp) - cb;
+      F(spv, ijp) = F(spv, ijp) - cb;
+      F(sp, ijp) = F(sp, ijp) - cb;
+      F(su, ijp) = F(su, ijp) - cb * F(u, ijb);
+      F(sv, ijp) = F(sv, ijp) - cb * F(v, ijb);
+      F(sw, ijp) = F(sw, ijp) - cb * F(w, ijb);
+    }
+  }
+  /* symmetry (:268-306) and wall (:309-378), srds / srdw as init.f90:1002-1027 */
+  for (int pass = 0; pass < 2; ++pass) {
+    const int cnt = pass == 0 ? m->nsym : m->nwal;
+    const int fst = pass == 0 ? m->iSymmetryFacesStart : m->iWallFacesStart;
+    const int bst = pass == 0 ? iSymmetryStart(m) : iWallStart(m);
+    for (int i = 1; i <= cnt; ++i) {
+      const int iface = fst + i, ijp = F(m->owner, iface), ijb = bst + i;
+      const double arx = F(m->arx, iface), ary = F(m->ary, iface), arz = F(m->arz, iface);
+      const double are = sqrt(arx * arx + ary * ary + arz * arz);
+      const double nxf = arx / are, nyf = ary / are, nzf = arz / are;
+      const double dn = (F(m->xf, iface) - F(m->xc, ijp)) * nxf +
+                        (F(m->yf, iface) - F(m->yc, ijp)) * nyf +
+                        (F(m->zf, iface) - F(m->zc, ijp)) * nzf;
+      const double srd = are / dn;
+      const double dx = F(m->xc, ijp) - F(m->xf, iface), dy = F(m->yc, ijp) - F(m->yf, iface),
+                   dz = F(m->zc, ijp) - F(m->zf, iface);
+      const double dpb = sqrt(dx * dx + dy * dy + dz * dz);
+      const double upb = F(u, ijp) - F(u, ijb), vpb = F(v, ijp) - F(v, ijb),
+                   wpb = F(w, ijp) - F(w, ijb);
+      if (pass == 0) {
+        const double vsi = F(vis, ijb);
+        const double cf = vsi * srd;
+        const double vsol = vsi * are / dpb;
+        const double fdne = 2 * cf * (upb * nxf + vpb * nyf + wpb * nzf);
+        F(spu, ijp) = F(spu, ijp) + vsol;
+        F(spv, ijp) = F(spv, ijp) + vsol;
+        F(sp, ijp) = F(sp, ijp) + vsol;
+        F(su, ijp) = F(su, ijp) + vsol * F(u, ijp) - fdne * nxf;
+        F(sv, ijp) = F(sv, ijp) + vsol * F(v, ijp) - fdne * nyf;
+        F(sw, ijp) = F(sw, ijp) + vsol * F(w, ijp) - fdne * nzf;
+      } else {
+        const double viss = prm->viscos;
+        const double cf = viss * srd;
+        const double vsol = viss * are / dpb;
+        const double vnp = upb * nxf + vpb * nyf + wpb * nzf;
+        const double utp = upb - vnp * nxf, vtp = vpb - vnp * nyf, wtp = wpb - vnp * nzf;
+        F(spu, ijp) = F(spu, ijp) + vsol;
+        F(spv, ijp) = F(spv, ijp) + vsol;
+        F(sp, ijp) = F(sp, ijp) + vsol;
+        F(su, ijp) = F(su, ijp) + vsol * F(u, ijp) - cf * utp;
+        F(sv, ijp) = F(sv, ijp) + vsol * F(v, ijp) - cf * vtp;
+        F(sw, ijp) = F(sw, ijp) + vsol * F(w, ijp) - cf * wtp;
+      }
+    }
+  }
+  if (prm->cn)
+    for (int k = 1; k <= nnz; ++k) F(a, k) = 0.5 * F(a, k); /* :382-384 */
+
+  /* the three components (:391-553) */
+  double *S[3] = {su, sv, sw}, *SP[3] = {spu, spv, sp};
+  const double *old[3] = {uo, vo, wo}, *cur[3] = {u, v, w};
+  for (int comp = 0; comp < 3; ++comp) {
+    double *s = S[comp];
+    if (prm->cn) {
+      for (int i = 1; i <= m->numInnerFaces; ++i) {
+        const int ijp = F(m->owner, i), ijn = F(m->neighbour, i);
+        F(s, ijp) = F(s, ijp) - F(a, F(slot_pn, i)) * F(old[comp], ijn);
+        F(s, ijn) = F(s, ijn) - F(a, F(slot_np, i)) * F(old[comp], ijp);
+      }
+      for (int ijp = 1; ijp <= n; ++ijp) {
+        const double apotime = F(den, ijp) * F(m->vol, ijp) / prm->timestep;
+        const double sum_off = row_sum(ioffset, a, ijp) - F(a, F(diag, ijp));
+        F(s, ijp) = F(s, ijp) + (apotime + sum_off) * F(old[comp], ijp);
+        F(SP[comp], ijp) = F(SP[comp], ijp) + apotime;
+      }
+    }
+    if (comp > 0)
+      for (int inp = 1; inp <= n; ++inp) {
+        F(a, F(diag, inp)) = 0.0;
+        F(su, inp) = 0.0; /* :473-476: su is the right-hand side of the v and w solves */
+      }
+    for (int inp = 1; inp <= n; ++inp) {
+      const double sum_off = row_sum(ioffset, a, inp) - F(a, F(diag, inp));
+      F(a, F(diag, inp)) = F(SP[comp], inp) - sum_off;
+      F(a, F(diag, inp)) = F(a, F(diag, inp)) * prm->urfr[comp];
+      if (comp == 0)
+        F(su, inp) = F(su, inp) + prm->urfm[0] * F(a, F(diag, inp)) * F(u, inp);
+      else
+        F(su, inp) = F(S[comp], inp) + prm->urfm[comp] * F(a, F(diag, inp)) * F(cur[comp], inp);
+      ap[(size_t)comp * n + inp - 1] = (double)1.0f / (F(a, F(diag, inp)) + small);
+    }
+    for (int inp = 1; inp <= n; ++inp) {
+      rhs[(size_t)comp * n + inp - 1] = F(su, inp);
+      if (comp == 0)
+        du[inp - 1] = F(a, F(diag, inp));
+      else
+        diag_vw[(size_t)(comp - 1) * n + inp - 1] = F(a, F(diag, inp));
+    }
+  }
+  for (int inp = 1; inp <= n; ++inp) F(a, F(diag, inp)) = du[inp - 1];
+  free(su);
+  free(sv);
+  free(sw);
+  free(spu);
+  free(spv);
+  free(sp);
+  free(du);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------- */
 /* PISO pressure path                                                          */
 /* ------------------------------------------------------------------------- */
 

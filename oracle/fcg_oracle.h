@@ -99,6 +99,31 @@ int orc_correct_fields(const orc_mesh *m, const double *dPdxi, const double *apu
                        const double *apv, const double *apw, const double *pp, double urf,
                        int pRefCell, double *u, double *v, double *w, double *p);
 
+/* --- momentum assembly: calcuvw.f90:48-438 with facefluxuvw, sngrad, face_value and
+ *     calcPressDiv --- */
+typedef struct orc_uvw_params {
+  int scheme, limiter; /* FCG_CONV_* / FCG_LIM_* numbering of include/fcgpu.h */
+  double gds, viscos;
+  double urfr[3], urfm[3];
+  int bdf, cn;
+  double timestep, btime;
+  int const_mflux;
+  double gradPcmf;
+  int buoyancy, boussinesq;
+  double beta, densit, tref, gravx, gravy, gravz;
+} orc_uvw_params;
+/* u, v, w, p, vis [numTotal]; den, t, uo..woo [numCells]; gradients (3,numCells);
+ * a[nnz] in/out (diagonal read; out: off-diagonals and the u diagonal); diag_vw[2n],
+ * rhs[3n], ap[3n] out. */
+int orc_calcuvw(const orc_mesh *m, const int *ioffset, const int *diag, const int *slot_pn,
+                const int *slot_np, const orc_uvw_params *prm, const double *u, const double *v,
+                const double *w, const double *p, const double *vis, const double *den,
+                const double *t, const double *uo, const double *vo, const double *wo,
+                const double *uoo, const double *voo, const double *woo, const double *dUdxi,
+                const double *dVdxi, const double *dWdxi, const double *dPdxi,
+                const double *flmass, const double *fmi, const double *fmo, double *a,
+                double *diag_vw, double *rhs, double *ap);
+
 /* --- PISO pressure path: PISO_multiple_correction.f90, get_rAU_x_UEqnH.f90,
  *     facefluxmass_piso (facefluxmass.f90:294-358), adjustMassFlow.f90 --- */
 typedef struct orc_hbya_params {

@@ -219,6 +219,36 @@ def correct_fields(m: Mesh, dPdxi, apu, apv, apw, pp, urf, pRefCell, u, v, w, p)
     return u, v, w, p
 
 
+class UvwParams(C.Structure):
+    """orc_uvw_params (calcuvw's parameters)."""
+    _fields_ = [("scheme", C.c_int), ("limiter", C.c_int), ("gds", C.c_double),
+                ("viscos", C.c_double), ("urfr", C.c_double * 3), ("urfm", C.c_double * 3),
+                ("bdf", C.c_int), ("cn", C.c_int), ("timestep", C.c_double),
+                ("btime", C.c_double), ("const_mflux", C.c_int), ("gradPcmf", C.c_double),
+                ("buoyancy", C.c_int), ("boussinesq", C.c_int), ("beta", C.c_double),
+                ("densit", C.c_double), ("tref", C.c_double), ("gravx", C.c_double),
+                ("gravy", C.c_double), ("gravz", C.c_double)]
+
+
+def calcuvw(m: Mesh, csr: CSR, prm: UvwParams, a, u, v, w, p, vis, den, dUdxi, dVdxi, dWdxi,
+            dPdxi, flmass, fmi=None, fmo=None, t=None, uo=None, vo=None, wo=None, uoo=None,
+            voo=None, woo=None):
+    """calcuvw.f90:48-438 without its solves: returns (a, diag_vw (2,n), rhs (3,n), ap (3,n))."""
+    n = m.numCells
+    a = _f64(a).copy()
+    dvw, rhs, ap = np.zeros((2, n)), np.zeros((3, n)), np.zeros((3, n))
+    fmi = _f64(fmi) if fmi is not None and len(fmi) else np.zeros(1)
+    fmo = _f64(fmo) if fmo is not None and len(fmo) else np.zeros(1)
+    rc = lib().orc_calcuvw(
+        C.byref(m.struct), _i(csr.ioffset), _i(csr.diag), _i(csr.slot_pn), _i(csr.slot_np),
+        C.byref(prm), *[_d(_f64(x)) for x in (u, v, w, p, vis, den)], _opt(t, n), _opt(uo, n),
+        _opt(vo, n), _opt(wo, n), _opt(uoo, n), _opt(voo, n), _opt(woo, n),
+        *[_d(_f64(x)) for x in (dUdxi, dVdxi, dWdxi, dPdxi, flmass)], _d(fmi), _d(fmo), _d(a),
+        _d(dvw), _d(rhs), _d(ap))
+    assert rc == 0
+    return a, dvw, rhs, ap
+
+
 class HbyaParams(C.Structure):
     """Parameters read by get_rAU_x_UEqnH (modules_allocatable.f90:40-106)."""
     _fields_ = [("timestep", C.c_double), ("btime", C.c_double), ("bdf", C.c_int),
