@@ -311,6 +311,24 @@ extern "C" int fcg_bind_mesh(fcg_context *c, const fcg_mesh_desc *m) {
   c->lb.count = (int)t.lb_ptr.size() - 1;
   UP(rows, t.lb_rows.data(), t.lb_rows.size());
   c->lb.rows = const_cast<int *>(rows);
+  {
+    auto padded = [](const std::vector<int> &ptr, const std::vector<int> &rs) {
+      std::vector<int> out;
+      out.reserve(rs.size() + 32 * ptr.size());
+      for (size_t l = 0; l + 1 < ptr.size(); ++l) {
+        out.insert(out.end(), rs.begin() + ptr[l], rs.begin() + ptr[l + 1]);
+        while (out.size() % 32) out.push_back(-1);
+      }
+      return out;
+    };
+    std::vector<int> pf = padded(t.lf_ptr, t.lf_rows), pb = padded(t.lb_ptr, t.lb_rows);
+    UP(rows, pf.data(), pf.size());
+    c->lf.pad = const_cast<int *>(rows);
+    c->lf.pad_len = (int)pf.size();
+    UP(rows, pb.data(), pb.size());
+    c->lb.pad = const_cast<int *>(rows);
+    c->lb.pad_len = (int)pb.size();
+  }
 #undef UP
 
   c->h_ioffset.swap(t.ioffset);

@@ -73,6 +73,10 @@ struct Level {
   std::vector<int> ptr;  // host: level offsets into rows
   int *rows = nullptr;   // device: rows sorted by level, ascending inside a level
   int count = 0;
+  // device: the same list with every level padded with -1 to a multiple of 32 entries,
+  // so a warp's 32 consecutive entries never span two levels (sync-free sweeps)
+  int *pad = nullptr;
+  int pad_len = 0;
 };
 
 }  // namespace fcg

@@ -42,7 +42,7 @@ struct Scal {
   double gam, om, beto, bbet;      // BiCGStab
   double l2r, l2b;                 // final recomputed ||su - A x||^2 and ||su||^2
   double small, resmax, tol;
-  int iter, nsw, done, converged, status, early, trace_cap, pad;
+  int iter, nsw, done, converged, status, early, trace_cap, wait_fail;
   unsigned int ticket[8];
   unsigned int body_count;  // executions of the loop body, counted independently of iter
   // mixed precision (reliable updates)
@@ -84,6 +84,15 @@ struct KrylovState {
   int last_kind = -1;
   double small = (double)1e-20f;  // parameters::small (modules_allocatable.f90:27)
   int early_exit = 1;
+  // sync-free triangular sweeps: the forward result and the control words
+  // {forward claim counter, backward claim counter, -, error}
+  DBuf sfb;
+  double *sf_y = nullptr;
+  int *sf_ctl = nullptr;
+  int sf_grid = 0;
+  bool sf_on = true;
+  int sf_spin = 1 << 20;     // polls before a dependency wait gives up
+  int sf_absent_row = -1;    // test hook: this row never publishes its flag
 };
 
 void destroy_krylov(KrylovState *k) {
@@ -100,12 +109,19 @@ void destroy_krylov(KrylovState *k) {
   k->vec.release();
   k->trace.release();
   k->mixed.release();
+  k->sfb.release();
   delete k;
 }
 
 namespace {
 
 __device__ __forceinline__ bool solve_done(const Scal *S) { return __ldcg(&S->done) != 0; }
+
+// Records an error status unless one is already recorded: the first cause is reported
+// (a failed wait, say, rather than the non-finite values it leads to).
+__device__ __forceinline__ void fail_status(Scal *S, int code) {
+  atomicCAS(&S->status, 0, code);
+}
 
 __device__ __forceinline__ void stop_loop(cudaGraphConditionalHandle h, int use_cond) {
   if (use_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(h, 0);
@@ -118,7 +134,7 @@ __device__ __forceinline__ void loop_guard(Scal *S, cudaGraphConditionalHandle h
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     unsigned int c = atomicAdd(&S->body_count, 1u) + 1u;
     if (c > (unsigned int)S->nsw + 2u) {
-      S->status = FCG_ERR_TIMEOUT;
+      fail_status(S, FCG_ERR_TIMEOUT);
       S->done = 1;
       if (use_cond) cudaGraphSetConditional(h, 0);
     }
@@ -190,7 +206,7 @@ __global__ void __launch_bounds__(kTPB, 8) k_init(SellView s, int n, const doubl
     S->gam = 1.0;
     S->done = (S->nsw <= 0 || (S->early && v[0] < S->tol)) ? 1 : 0;  // dpcg.f90:66-70
     if (!isfinite(v[0])) {
-      S->status = FCG_ERR_NONFINITE;
+      fail_status(S, FCG_ERR_NONFINITE);
       S->done = 1;
     }
   }
@@ -210,7 +226,7 @@ __device__ __noinline__ void finish_sweep(Scal *S, double resl, double *trace, c
     trace[2 * (it - 1) + 1] = rsm;
   }
   if (rsm < S->resmax) S->converged = 1;
-  if (!isfinite(resl)) S->status = FCG_ERR_NONFINITE;
+  if (!isfinite(resl)) fail_status(S, FCG_ERR_NONFINITE);
   if (S->converged || it >= S->nsw || S->status) {
     S->done = 1;
     if (use_cond) cudaGraphSetConditional(h, 0);
@@ -263,7 +279,7 @@ __global__ void __launch_bounds__(kTPB, 8) k_cg_spmv(SellView s, int n, const do
   if (reduce_commit<1>(v, partials, &S->ticket[1]) && threadIdx.x == 0) {
     S->pkapk = v[0];
     S->alf = S->sk / v[0];
-    if (!isfinite(S->alf)) S->status = FCG_ERR_NONFINITE;
+    if (!isfinite(S->alf)) fail_status(S, FCG_ERR_NONFINITE);
   }
 }
 
@@ -304,6 +320,9 @@ __global__ void __launch_bounds__(kTPB, 8) k_cg_dot(int n, const double *__restr
 }
 
 // --- triangular sweeps, one launch per level -----------------------------------
+// The row arithmetic of the sweeps and factors is written with __dmul_rn / __dsub_rn: a
+// multiply and a subtract each rounded, as the reference's loops evaluate them, and the
+// same bits whichever kernel form (per level or one launch) runs it.
 // forward: z_i = (b_i - sum_{k<diag} a_k z_{ja_k}) * d_i        (iccg.f90:248-254)
 __global__ void k_fwd_level(const int *__restrict__ rows, int count,
                             const int *__restrict__ ioffset, const int *__restrict__ ja,
@@ -315,7 +334,7 @@ __global__ void k_fwd_level(const int *__restrict__ rows, int count,
   if (t >= count) return;
   int i = rows[t];
   double zi = b[i];
-  for (int k = ioffset[i]; k < diag[i]; ++k) zi = zi - a[k] * z[ja[k]];
+  for (int k = ioffset[i]; k < diag[i]; ++k) zi = __dsub_rn(zi, __dmul_rn(a[k], z[ja[k]]));
   z[i] = zi * d[i];
 }
 
@@ -331,8 +350,177 @@ __global__ void k_bwd_level(const int *__restrict__ rows, int count,
   int i = rows[t];
   double di = d[i];
   double zi = z[i] / (di + S->small);
-  for (int k = diag[i] + 1; k < ioffset[i + 1]; ++k) zi = zi - a[k] * z[ja[k]];
+  for (int k = diag[i] + 1; k < ioffset[i + 1]; ++k) zi = __dsub_rn(zi, __dmul_rn(a[k], z[ja[k]]));
   z[i] = zi * di;
+}
+
+// --- sync-free triangular sweeps ---------------------------------------------------
+// The same row arithmetic as the level kernels, in one launch: warps claim 32 entries of
+// the level-ordered row list (levels padded to multiples of 32, so a warp's rows are
+// independent) through an atomic counter, and each row waits for the values it reads.
+// The output vector is filled with a sentinel before the sweep, a signalling-NaN bit
+// pattern that arithmetic never produces; a row polls the 64-bit word it needs until the
+// sentinel is gone and uses the value it read, so the value is its own ready flag (an
+// aligned 64-bit access is single-copy atomic) and no fence is needed.  Claims are
+// monotone and a row only reads rows of earlier levels, so every awaited row was claimed
+// earlier by a warp that is running: the waits end.  Each wait is bounded; one that gives
+// up records FCG_ERR_TIMEOUT, and every row still writes its result so no other wait is
+// held up by it.  The backward sweep writes a second vector, so a forward result is
+// never mistaken for a backward one.
+constexpr unsigned long long kSentinel = 0x7ff0dead0badf00dULL;
+
+__device__ __forceinline__ double ld_relaxed64(const double *p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return __longlong_as_double((long long)v);
+}
+
+__device__ __forceinline__ void st_relaxed64(double *p, double x) {
+  asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p),
+               "l"((unsigned long long)__double_as_longlong(x))
+               : "memory");
+}
+
+__device__ __forceinline__ bool is_sentinel(double v) {
+  return (unsigned long long)__double_as_longlong(v) == kSentinel;
+}
+
+// The value at p once it is not the sentinel; gives up after `spin` polls (or when
+// another wait has given up) and returns what it last read.
+__device__ __forceinline__ double sf_value(const double *p, const int *err, int spin, bool *ok) {
+  double v = ld_relaxed64(p);
+  if (!is_sentinel(v)) return v;
+  for (int it = 0; it < spin; ++it) {
+    if (it >= 16) __nanosleep(32);
+    v = ld_relaxed64(p);
+    if (!is_sentinel(v)) return v;
+    if ((it & 63) == 63 && *(volatile const int *)err) break;
+  }
+  *ok = false;
+  return v;
+}
+
+__device__ __forceinline__ void sf_fail(int *err, Scal *S) {
+  if (atomicExch(err, 1) == 0) {
+    S->wait_fail = 1;
+    fail_status(S, FCG_ERR_TIMEOUT);
+  }
+}
+
+constexpr int kSfBatch = 8;  // dependencies of a row loaded and awaited together
+
+// Sentinel into the sweep outputs; ctl = {forward counter, backward counter, -, error}.
+__global__ void k_sf_fill(int n, double *__restrict__ o1, double *__restrict__ o2, int *ctl) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctl[0] = 0;
+    ctl[1] = 0;
+    ctl[3] = 0;
+  }
+  const double s = __longlong_as_double((long long)kSentinel);
+  FCG_GRID_STRIDE(i, n) {
+    o1[i] = s;
+    if (o2) o2[i] = s;
+  }
+}
+
+// One row: acc - sum a_k v_{ja_k} over k in [k0, hi), the values awaited in batches.
+__device__ __forceinline__ double sf_row(double acc, int k0, int hi, const int *__restrict__ ja,
+                                         const double *__restrict__ a, const double *v, int *ctl,
+                                         Scal *S, int spin) {
+  for (; k0 < hi; k0 += kSfBatch) {
+    int jj[kSfBatch];
+    double aa[kSfBatch], vv[kSfBatch];
+#pragma unroll
+    for (int t = 0; t < kSfBatch; ++t)
+      if (k0 + t < hi) {
+        jj[t] = ja[k0 + t];
+        aa[t] = a[k0 + t];
+      }
+    bool ok = true;
+#pragma unroll
+    for (int t = 0; t < kSfBatch; ++t)  // all first reads in flight together
+      if (k0 + t < hi) vv[t] = ld_relaxed64(&v[jj[t]]);
+#pragma unroll
+    for (int t = 0; t < kSfBatch; ++t)
+      if (k0 + t < hi && is_sentinel(vv[t])) vv[t] = sf_value(&v[jj[t]], &ctl[3], spin, &ok);
+    if (!ok) sf_fail(&ctl[3], S);
+#pragma unroll
+    for (int t = 0; t < kSfBatch; ++t)
+      if (k0 + t < hi) acc = __dsub_rn(acc, __dmul_rn(aa[t], vv[t]));
+  }
+  return acc;
+}
+
+// forward: y_i = (b_i - sum_{k<diag} a_k y_{ja_k}) * d_i        (iccg.f90:248-254)
+__global__ void k_fwd_sf(const int *__restrict__ rows, int len, const int *__restrict__ ioffset,
+                         const int *__restrict__ ja, const int *__restrict__ diag,
+                         const double *__restrict__ a, const double *__restrict__ d,
+                         const double *__restrict__ b, double *y, int *ctl, Scal *S, int spin,
+                         int absent) {
+  if (solve_done(S)) return;
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&ctl[0], 32);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= len) break;
+    const int i = rows[base + lane];
+    if (i < 0 || i == absent) continue;
+    const double zi = sf_row(b[i], ioffset[i], diag[i], ja, a, y, ctl, S, spin);
+    st_relaxed64(&y[i], zi * d[i]);
+  }
+}
+
+// backward from the forward result y with the reference's rescale zk/(d+small) folded
+// in (iccg.f90:256-265): z_i = (y_i/(d_i+small) - sum_{k>diag} a_k z_{ja_k}) * d_i
+__global__ void k_bwd_sf(const int *__restrict__ rows, int len, const int *__restrict__ ioffset,
+                         const int *__restrict__ ja, const int *__restrict__ diag,
+                         const double *__restrict__ a, const double *__restrict__ d,
+                         const double *__restrict__ y, double *z, int *ctl, Scal *S, int spin) {
+  if (solve_done(S)) return;
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&ctl[1], 32);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= len) break;
+    const int i = rows[base + lane];
+    if (i < 0) continue;
+    const double di = d[i];
+    const double zi = sf_row(y[i] / (di + S->small), diag[i] + 1, ioffset[i + 1], ja, a, z, ctl, S,
+                             spin);
+    st_relaxed64(&z[i], zi * di);
+  }
+}
+
+// DIC / DILU factor in one launch (iccg.f90:231-237, bicgstab.f90:68-79); d holds the
+// sentinel on entry.
+__global__ void k_factor_sf(const int *__restrict__ rows, int len, const int *__restrict__ ioffset,
+                            const int *__restrict__ ja, const int *__restrict__ diag,
+                            const int *__restrict__ tpos, const double *__restrict__ a, double *d,
+                            int *ctl, Scal *S, int spin, int dilu) {
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&ctl[0], 32);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= len) break;
+    const int i = rows[base + lane];
+    if (i < 0) continue;
+    double di = a[diag[i]];
+    bool ok = true;
+    for (int k = ioffset[i]; k < diag[i]; ++k) {
+      const double dj = sf_value(&d[ja[k]], &ctl[3], spin, &ok);
+      if (dilu)
+        di = __dsub_rn(di, __dmul_rn(__dmul_rn(a[k], dj), a[tpos[k]]));
+      else
+        di = __dsub_rn(di, __dmul_rn(__dmul_rn(a[k], a[k]), dj));
+    }
+    if (!ok) sf_fail(&ctl[3], S);
+    const double inv = 1.0 / di;
+    st_relaxed64(&d[i], inv);
+    if (!isfinite(inv) || di == 0.0) fail_status(S, FCG_ERR_PIVOT);
+  }
 }
 
 // Factor diagonals, level by level: DIC d_i = 1/(a_ii - sum a_ik^2 d_k) (iccg.f90:
@@ -350,13 +538,13 @@ __global__ void k_factor_level(const int *__restrict__ rows, int count,
   for (int k = ioffset[i]; k < diag[i]; ++k) {
     int j = ja[k];
     if (dilu)
-      di = di - a[k] * d[j] * a[tpos[k]];
+      di = __dsub_rn(di, __dmul_rn(__dmul_rn(a[k], d[j]), a[tpos[k]]));
     else
-      di = di - a[k] * a[k] * d[j];
+      di = __dsub_rn(di, __dmul_rn(__dmul_rn(a[k], a[k]), d[j]));
   }
   double inv = 1.0 / di;
   d[i] = inv;
-  if (!isfinite(inv) || di == 0.0) S->status = FCG_ERR_PIVOT;
+  if (!isfinite(inv) || di == 0.0) fail_status(S, FCG_ERR_PIVOT);
 }
 
 // --- BiCGStab sweep (bicgstab.f90:99-224) -------------------------------------
@@ -398,7 +586,7 @@ __global__ void __launch_bounds__(kTPB, 8) k_bi_spmv1(SellView s, int n, const d
   }
   if (reduce_commit<1>(v, partials, &S->ticket[4]) && threadIdx.x == 0) {
     S->gam = S->bbet / v[0];
-    if (!isfinite(S->gam)) S->status = FCG_ERR_NONFINITE;
+    if (!isfinite(S->gam)) fail_status(S, FCG_ERR_NONFINITE);
   }
 }
 
@@ -431,7 +619,7 @@ __global__ void __launch_bounds__(kTPB, 8) k_bi_spmv2(SellView s, int n, const d
   }
   if (reduce_commit<2>(v, partials, &S->ticket[5]) && threadIdx.x == 0) {
     S->alf = v[0] / (v[1] + S->small);
-    if (!isfinite(S->alf)) S->status = FCG_ERR_NONFINITE;
+    if (!isfinite(S->alf)) fail_status(S, FCG_ERR_NONFINITE);
   }
 }
 
@@ -546,7 +734,7 @@ __global__ void __launch_bounds__(kTPB, 6)
   double v[1] = {(double)t};
   if (reduce_commit<1>(v, partials, &S->ticket[1]) && threadIdx.x == 0) {
     S->alf = S->rr / v[0];
-    if (!isfinite(S->alf)) S->status = FCG_ERR_NONFINITE;
+    if (!isfinite(S->alf)) fail_status(S, FCG_ERR_NONFINITE);
   }
 }
 
@@ -622,7 +810,7 @@ __device__ __noinline__ void mx_after_update(Scal *S, double l1, double rrn, dou
     trace[2 * (S->nupdates - 1) + 1] = rsm;
   }
   if (rsm < S->resmax) S->converged = 1;
-  if (!isfinite(l1)) S->status = FCG_ERR_NONFINITE;
+  if (!isfinite(l1)) fail_status(S, FCG_ERR_NONFINITE);
   if (S->converged || S->iter >= S->nsw || S->status) {
     S->done = 1;
     if (use_cond) cudaGraphSetConditional(h, 0);
@@ -778,6 +966,18 @@ static int ensure_state(fcg_context *c, int nsw) {
     g.mru1 = occ((const void *)k_mx_ru1);
     g.mru2 = occ((const void *)k_mx_ru2);
     g.mp = occ((const void *)k_mx_p);
+    // sync-free sweeps: the forward result vector and the control words
+    FCG_CUDA_TRY(c, k->sfb.ensure(sizeof(double) * (n + 4)));
+    FCG_CUDA_TRY(c, cudaMemset(k->sfb.p, 0, sizeof(double) * (n + 4)));
+    k->sf_y = k->sfb.as<double>();
+    k->sf_ctl = (int *)(k->sf_y + n);
+    k->sf_grid = std::min(occ((const void *)k_fwd_sf), occ((const void *)k_bwd_sf));
+    {
+      const char *e = std::getenv("FCG_SWEEP");
+      k->sf_on = !(e && std::string(e) == "levels");
+      // two blocks per SM: more resident warps only poll further ahead (measured)
+      k->sf_grid = std::min(k->sf_grid, c->num_sms * 2);
+    }
     k->bind_gen = c->bind_gen;
     k->matrix_loaded = false;
     k->mixed_ready = false;
@@ -873,6 +1073,19 @@ const double *sliced64(const fcg_context *c) { return c->ks ? c->ks->sval : null
 static void launch_sweeps(fcg_context *c, cudaStream_t st, const Level &lv, bool forward,
                           const double *b, double *z) {
   KrylovState *k = c->ks;
+  if (k->sf_on) {
+    if (forward) {  // b -> sf_y, after the sentinel fill of sf_y and z
+      k_sf_fill<<<grid_for(c->n, c->num_sms), kTPB, 0, st>>>(c->n, k->sf_y, z, k->sf_ctl);
+      k_fwd_sf<<<k->sf_grid, kTPB, 0, st>>>(lv.pad, lv.pad_len, c->mv.ioffset, c->mv.ja,
+                                            c->mv.diag, k->a, k->d, b, k->sf_y, k->sf_ctl, k->S,
+                                            k->sf_spin, k->sf_absent_row);
+    } else {  // sf_y -> z
+      k_bwd_sf<<<k->sf_grid, kTPB, 0, st>>>(lv.pad, lv.pad_len, c->mv.ioffset, c->mv.ja,
+                                            c->mv.diag, k->a, k->d, k->sf_y, z, k->sf_ctl, k->S,
+                                            k->sf_spin);
+    }
+    return;
+  }
   for (int l = 0; l < lv.count; ++l) {
     int start = lv.ptr[l], cnt = lv.ptr[l + 1] - lv.ptr[l];
     int g = (cnt + kTPB - 1) / kTPB;
@@ -1100,7 +1313,14 @@ static int run_solver(fcg_context *c, int kind, const double *a, const double *s
                                                      k->p32, k->S, k->partials);
     FCG_CHECK_LAUNCH(c, "mixed set-up");
   }
-  if (kind != SK_DPCG) {  // factor diagonal, level by level
+  if (kind != SK_DPCG && k->sf_on) {  // factor diagonal in one sync-free launch
+    k_sf_fill<<<grid_for(c->n, c->num_sms), kTPB, 0, c->stream>>>(c->n, k->d, nullptr,
+                                                                    k->sf_ctl);
+    k_factor_sf<<<k->sf_grid, kTPB, 0, c->stream>>>(
+        c->lf.pad, c->lf.pad_len, c->mv.ioffset, c->mv.ja, c->mv.diag, c->tpos, k->a, k->d,
+        k->sf_ctl, k->S, k->sf_spin, kind == SK_BICG);
+    FCG_CHECK_LAUNCH(c, "k_factor_sf");
+  } else if (kind != SK_DPCG) {  // factor diagonal, level by level
     for (int l = 0; l < c->lf.count; ++l) {
       int start = c->lf.ptr[l], cnt = c->lf.ptr[l + 1] - c->lf.ptr[l];
       k_factor_level<<<(cnt + kTPB - 1) / kTPB, kTPB, 0, c->stream>>>(
@@ -1151,7 +1371,9 @@ static int run_solver(fcg_context *c, int kind, const double *a, const double *s
   }
   if (S.status) {
     const char *what = S.status == FCG_ERR_PIVOT     ? "zero or non-finite pivot in the factor"
-                       : S.status == FCG_ERR_TIMEOUT ? "solver loop exceeded nsw + 2 sweeps"
+                       : S.status == FCG_ERR_TIMEOUT
+                           ? (S.wait_fail ? "a triangular-sweep dependency wait gave up"
+                                          : "solver loop exceeded nsw + 2 sweeps")
                                                      : "non-finite value in a reduction";
     return set_error(c, S.status, what);
   }
@@ -1194,6 +1416,25 @@ extern "C" int fcg_set_solver_options(fcg_context *c, double small, int early_ex
   return FCG_OK;
 }
 
+extern "C" int fcg_set_sweep_wait_test(fcg_context *c, int polls, int absent_row) {
+  if (!c) return FCG_ERR_ARG;
+  if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_set_sweep_wait_test before fcg_bind_mesh");
+  if (absent_row < 0 || absent_row > c->n) return set_error(c, FCG_ERR_INDEX, "absent_row out of range");
+  FCG_CUDA_TRY(c, cudaSetDevice(c->device));
+  int rc = ensure_state(c, 1);
+  if (rc) return rc;
+  KrylovState *k = c->ks;
+  k->sf_spin = polls > 0 ? polls : (1 << 20);
+  k->sf_absent_row = absent_row - 1;
+  for (int i = 0; i < SK_N; ++i) {  // both values are kernel arguments of the graphs
+    if (k->exec[i]) cudaGraphExecDestroy(k->exec[i]);
+    if (k->graph[i]) cudaGraphDestroy(k->graph[i]);
+    k->exec[i] = nullptr;
+    k->graph[i] = nullptr;
+  }
+  return FCG_OK;
+}
+
 // Re-opens the last solve for profiling: clears the stop flag, the reliable-update
 // flag and the sweep counters, and lifts the sweep cap.
 __global__ void k_prof_reopen(Scal *S) {
@@ -1201,6 +1442,7 @@ __global__ void k_prof_reopen(Scal *S) {
     S->done = 0;
     S->ru = 0;
     S->status = 0;
+    S->wait_fail = 0;
     S->converged = 0;
     S->iter = 0;
     S->body_count = 0;

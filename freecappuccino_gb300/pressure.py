@@ -429,6 +429,13 @@ class Context:
         """bicgstab(fi,ifi) (bicgstab.f90:1-231)."""
         return self._solve(self.lib.fcg_bicgstab, "fcg_bicgstab", a, su, fi, sor, nsw, **kw)
 
+    def set_sweep_wait_test(self, polls: int = 0, absent_row: int = 0):
+        """Timeout diagnostics of the one-launch DIC/DILU sweeps: every dependency wait
+        gives up after `polls` polls and row `absent_row` (1-based) never announces its
+        forward result.  (0, 0) restores normal runs."""
+        self._check(self.lib.fcg_set_sweep_wait_test(self.h, int(polls), int(absent_row)),
+                    "fcg_set_sweep_wait_test")
+
     def profile_sweeps(self, reps: int = 10) -> dict:
         """Mean milliseconds per kernel unit of the last solve's sweep (changes its state)."""
         ms = (C.c_double * 32)()

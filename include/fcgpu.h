@@ -385,6 +385,13 @@ int fcg_bicgstab_multi(fcg_context *ctx, int nsys, const double *a, const double
  * tests/test_sparse_solvers.f90 use small = 1e-30 and never return early. */
 int fcg_set_solver_options(fcg_context *ctx, double small, int early_exit);
 
+/* Diagnostics for the timeout path of the DIC/DILU sweeps, which run in one launch with
+ * each row waiting on the rows it reads: every wait gives up after `polls` polls (<= 0:
+ * the default, about 0.4 s), and row absent_row (1-based; 0: none) never announces its
+ * result in forward sweeps, so the waits of the rows that read it run out and the solve
+ * returns FCG_ERR_TIMEOUT with the device still usable.  (0, 0) restores normal runs. */
+int fcg_set_sweep_wait_test(fcg_context *ctx, int polls, int absent_row);
+
 /* Per-sweep (resl, rsm) pairs of the last solve -- what the reference prints per
  * sweep when ltest is set (dpcg.f90:141).  *count receives the number available;
  * at most max_count pairs are copied to resl_rsm (which may be NULL). */

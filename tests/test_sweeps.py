@@ -1,0 +1,70 @@
+"""DIC / DILU triangular sweeps in one launch (rows waiting on the rows they read)
+against the level-by-level launches: the same row arithmetic, so the same bits.  And the
+timeout path of the dependency waits: a row that never announces its result makes the
+solve return FCG_ERR_TIMEOUT, and the context then solves normally."""
+import os
+
+import numpy as np
+import pytest
+
+import freecappuccino_gb300 as fcg
+from freecappuccino_gb300 import _lib
+from oracle import oracle
+from tests.meshes import fixture_mesh, hex_mesh, oracle_csr, poisson_system
+
+pytestmark = pytest.mark.gpu
+
+
+def _context(m, levels: bool):
+    """A context whose solver state (created at its first solve) uses the level
+    launches or the one-launch sweeps."""
+    old = os.environ.get("FCG_SWEEP")
+    if levels:
+        os.environ["FCG_SWEEP"] = "levels"
+    else:
+        os.environ.pop("FCG_SWEEP", None)
+    try:
+        c = fcg.Context(m)
+        c.set_solver_options(float(np.float32(1e-20)), True)  # creates the solver state
+    finally:
+        if old is None:
+            os.environ.pop("FCG_SWEEP", None)
+        else:
+            os.environ["FCG_SWEEP"] = old
+    return c
+
+
+@pytest.mark.parametrize("name", ["hex12", "pitzdaily"])
+def test_one_launch_sweeps_equal_level_sweeps(name):
+    m = hex_mesh(12, 0.2) if name == "hex12" else fixture_mesh("pitzdaily")
+    a_ctx, b_ctx = _context(m, False), _context(m, True)
+    mu, phi, su0 = poisson_system(m)
+    a, su = a_ctx.laplacian(mu, phi, su0)
+    x0 = np.zeros(m.numCells)
+    for solver in ("iccg", "bicgstab"):
+        for sor, nsw in ((0.0, 30), (1e-8, 3000)):
+            r1 = getattr(a_ctx, solver)(a, su, x0, sor, nsw)
+            r2 = getattr(b_ctx, solver)(a, su, x0, sor, nsw)
+            assert r1.iters == r2.iters and np.array_equal(r1.fi, r2.fi), (solver, sor)
+            assert r1.resl == r2.resl
+    a_ctx.close()
+    b_ctx.close()
+
+
+def test_sweep_wait_runs_out_and_device_stays_usable():
+    m = hex_mesh(10, 0.2)
+    c = fcg.Context(m)
+    mu, phi, su0 = poisson_system(m)
+    a, su = c.laplacian(mu, phi, su0)
+    x0 = np.zeros(m.numCells)
+    c.set_sweep_wait_test(polls=2048, absent_row=m.numCells // 2)
+    with pytest.raises(_lib.FcgError) as ei:
+        c.iccg(a, su, x0, 1e-8, 50)
+    assert ei.value.status == _lib.FCG_ERR_TIMEOUT
+    assert "dependency wait" in str(ei.value)
+    c.set_sweep_wait_test(0, 0)
+    r = c.iccg(a, su, x0, 1e-8, 3000)
+    o = oracle.iccg(oracle_csr(m), a, su, x0.copy(), 1e-8, 3000)
+    assert r.converged and abs(r.iters - o.iters) <= 1
+    assert np.abs(r.fi - o.fi).max() / np.abs(o.fi).max() < 1e-8
+    c.close()
