@@ -15,6 +15,7 @@
 // (a handful of iterations).
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -53,6 +54,13 @@ struct MultiState {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int G = 0;
+  // one-launch DILU sweeps (as krylov.cu): forward results and the control words
+  // {forward claim counter, backward claim counter, -, error}
+  DBuf sfb;
+  float *y32 = nullptr;
+  int *ctl = nullptr;
+  int sf_grid = 0;
+  bool sf_on = true;
 };
 
 void destroy_multi(MultiState *m) {
@@ -63,6 +71,7 @@ void destroy_multi(MultiState *m) {
   if (m->S) cudaFree(m->S);
   if (m->hS) cudaFreeHost(m->hS);
   m->buf.release();
+  m->sfb.release();
   delete m;
 }
 
@@ -101,10 +110,11 @@ __global__ void k_m_factor(const int *__restrict__ rows, int count, long long nn
     const float *a = a32 + k * nnz;
     float *d = d32 + (long long)k * n;
     float di = a[dg[i]];
-    for (int q = io[i]; q < dg[i]; ++q) di = di - a[q] * d[ja[q]] * a[tpos[q]];
+    for (int q = io[i]; q < dg[i]; ++q)
+      di = __fsub_rn(di, __fmul_rn(__fmul_rn(a[q], d[ja[q]]), a[tpos[q]]));
     const float inv = 1.0f / di;
     d[i] = inv;
-    if (!isfinite(inv)) S->status = FCG_ERR_PIVOT;
+    if (!isfinite(inv)) atomicCAS(&S->status, 0, FCG_ERR_PIVOT);
   }
 }
 
@@ -149,7 +159,7 @@ __global__ void __launch_bounds__(kTPB, 4)
       S->alf[k] = 1.0;  // bicgstab.f90:90-92
       S->beto[k] = 1.0;
       S->gam[k] = 1.0;
-      if (!isfinite(l1[k])) S->status = FCG_ERR_NONFINITE;
+      if (!isfinite(l1[k])) atomicCAS(&S->status, 0, FCG_ERR_NONFINITE);
     }
     S->any_active = any;
     S->inner_iter = 0;
@@ -267,7 +277,7 @@ __global__ void k_m_fwd(const int *__restrict__ rows, int count, long long nnz, 
     const float *a = a32 + k * nnz;
     const float *zk = z + (long long)k * n;
     float zi = b[(long long)k * n + i];
-    for (int q = io[i]; q < dg[i]; ++q) zi = zi - a[q] * zk[ja[q]];
+    for (int q = io[i]; q < dg[i]; ++q) zi = __fsub_rn(zi, __fmul_rn(a[q], zk[ja[q]]));
     z[(long long)k * n + i] = zi * d32[(long long)k * n + i];
   }
 }
@@ -289,8 +299,169 @@ __global__ void k_m_bwd(const int *__restrict__ rows, int count, long long nnz, 
     float *zk = z + (long long)k * n;
     const float di = d32[(long long)k * n + i];
     float zi = zk[i] / (di + small);
-    for (int q = dg[i] + 1; q < io[i + 1]; ++q) zi = zi - a[q] * zk[ja[q]];
+    for (int q = dg[i] + 1; q < io[i + 1]; ++q) zi = __fsub_rn(zi, __fmul_rn(a[q], zk[ja[q]]));
     zk[i] = zi * di;
+  }
+}
+
+// --- DILU sweeps in one launch (the scheme of krylov.cu's k_fwd_sf): rows claimed in
+// level order by warps, each waiting on the FP32 values it reads, which are filled with
+// a signalling-NaN sentinel before the sweep.  The same row arithmetic as the level
+// kernels above.
+constexpr unsigned kSent32 = 0x7f80deadu;
+constexpr int kSfSpin = 1 << 20;
+
+__device__ __forceinline__ float ld_relaxed32(const float *p) {
+  unsigned v;
+  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return __uint_as_float(v);
+}
+
+__device__ __forceinline__ void st_relaxed32(float *p, float x) {
+  asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(__float_as_uint(x)) : "memory");
+}
+
+__device__ __forceinline__ bool sent32(float v) { return __float_as_uint(v) == kSent32; }
+
+__device__ __forceinline__ float sf_value32(const float *p, const int *err, bool *ok) {
+  float v = ld_relaxed32(p);
+  if (!sent32(v)) return v;
+  for (int it = 0; it < kSfSpin; ++it) {
+    if (it >= 16) __nanosleep(32);
+    v = ld_relaxed32(p);
+    if (!sent32(v)) return v;
+    if ((it & 63) == 63 && *(volatile const int *)err) break;
+  }
+  *ok = false;
+  return v;
+}
+
+__device__ __forceinline__ void sf_fail32(int *err, MScal *S) {
+  if (atomicExch(err, 1) == 0) atomicCAS(&S->status, 0, FCG_ERR_TIMEOUT);
+}
+
+__global__ void k_m_sf_fill(long long count, float *__restrict__ o1, float *__restrict__ o2,
+                            int *ctl) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctl[0] = 0;
+    ctl[1] = 0;
+    ctl[3] = 0;
+  }
+  const float s = __uint_as_float(kSent32);
+  FCG_GRID_STRIDE(i, count) {
+    o1[i] = s;
+    if (o2) o2[i] = s;
+  }
+}
+
+// Claims the next 32 entries of the level list for the calling warp (-1: none left).
+__device__ __forceinline__ int sf_claim(int *ctr) {
+  int base = 0;
+  if ((threadIdx.x & 31) == 0) base = atomicAdd(ctr, 32);
+  return __shfl_sync(0xffffffffu, base, 0);
+}
+
+template <int NS>
+__global__ void k_m_fwd_sf(const int *__restrict__ rows, int len, long long nnz, int n,
+                           const int *__restrict__ io, const int *__restrict__ ja,
+                           const int *__restrict__ dg, const float *__restrict__ a32,
+                           const float *__restrict__ d32, const float *__restrict__ b, float *y,
+                           int *ctl, MScal *S) {
+  if (inner_done(S)) return;
+  for (;;) {
+    const int base = sf_claim(&ctl[0]);
+    if (base >= len) break;
+    const int i = rows[base + (threadIdx.x & 31)];
+    if (i < 0) continue;
+    float zi[NS];
+#pragma unroll
+    for (int k = 0; k < NS; ++k) zi[k] = b[(long long)k * n + i];
+    bool ok = true;
+    for (int q = io[i]; q < dg[i]; ++q) {
+      const int j = ja[q];
+      float v[NS];
+#pragma unroll
+      for (int k = 0; k < NS; ++k) v[k] = ld_relaxed32(&y[(long long)k * n + j]);
+#pragma unroll
+      for (int k = 0; k < NS; ++k) {
+        if (sent32(v[k])) v[k] = sf_value32(&y[(long long)k * n + j], &ctl[3], &ok);
+        zi[k] = __fsub_rn(zi[k], __fmul_rn(a32[k * nnz + q], v[k]));
+      }
+    }
+    if (!ok) sf_fail32(&ctl[3], S);
+#pragma unroll
+    for (int k = 0; k < NS; ++k)
+      st_relaxed32(&y[(long long)k * n + i], zi[k] * d32[(long long)k * n + i]);
+  }
+}
+
+template <int NS>
+__global__ void k_m_bwd_sf(const int *__restrict__ rows, int len, long long nnz, int n,
+                           const int *__restrict__ io, const int *__restrict__ ja,
+                           const int *__restrict__ dg, const float *__restrict__ a32,
+                           const float *__restrict__ d32, const float *__restrict__ y, float *z,
+                           int *ctl, MScal *S) {
+  if (inner_done(S)) return;
+  const float small = (float)S->small;
+  for (;;) {
+    const int base = sf_claim(&ctl[1]);
+    if (base >= len) break;
+    const int i = rows[base + (threadIdx.x & 31)];
+    if (i < 0) continue;
+    float zi[NS], di[NS];
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      di[k] = d32[(long long)k * n + i];
+      zi[k] = y[(long long)k * n + i] / (di[k] + small);
+    }
+    bool ok = true;
+    for (int q = dg[i] + 1; q < io[i + 1]; ++q) {
+      const int j = ja[q];
+      float v[NS];
+#pragma unroll
+      for (int k = 0; k < NS; ++k) v[k] = ld_relaxed32(&z[(long long)k * n + j]);
+#pragma unroll
+      for (int k = 0; k < NS; ++k) {
+        if (sent32(v[k])) v[k] = sf_value32(&z[(long long)k * n + j], &ctl[3], &ok);
+        zi[k] = __fsub_rn(zi[k], __fmul_rn(a32[k * nnz + q], v[k]));
+      }
+    }
+    if (!ok) sf_fail32(&ctl[3], S);
+#pragma unroll
+    for (int k = 0; k < NS; ++k) st_relaxed32(&z[(long long)k * n + i], zi[k] * di[k]);
+  }
+}
+
+template <int NS>
+__global__ void k_m_factor_sf(const int *__restrict__ rows, int len, long long nnz, int n,
+                              const int *__restrict__ io, const int *__restrict__ ja,
+                              const int *__restrict__ dg, const int *__restrict__ tpos,
+                              const float *__restrict__ a32, float *d32, int *ctl, MScal *S) {
+  for (;;) {
+    const int base = sf_claim(&ctl[0]);
+    if (base >= len) break;
+    const int i = rows[base + (threadIdx.x & 31)];
+    if (i < 0) continue;
+    float di[NS];
+#pragma unroll
+    for (int k = 0; k < NS; ++k) di[k] = a32[k * nnz + dg[i]];
+    bool ok = true;
+    for (int q = io[i]; q < dg[i]; ++q) {
+      const int j = ja[q];
+#pragma unroll
+      for (int k = 0; k < NS; ++k) {
+        const float *a = a32 + k * nnz;
+        const float dj = sf_value32(&d32[(long long)k * n + j], &ctl[3], &ok);
+        di[k] = __fsub_rn(di[k], __fmul_rn(__fmul_rn(a[q], dj), a[tpos[q]]));
+      }
+    }
+    if (!ok) sf_fail32(&ctl[3], S);
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+      const float inv = 1.0f / di[k];
+      st_relaxed32(&d32[(long long)k * n + i], inv);
+      if (!isfinite(inv)) atomicCAS(&S->status, 0, FCG_ERR_PIVOT);
+    }
   }
 }
 
@@ -328,10 +499,10 @@ __global__ void __launch_bounds__(kTPB, 4)
     for (int k = 0; k < NS; ++k) {
       if (which == 0) {  // gam = bet / (u.rh)   (bicgstab.f90:153-154)
         S->gam[k] = S->active[k] ? S->bet[k] / v[k] : 0.0;
-        if (S->active[k] && !isfinite(S->gam[k])) S->status = FCG_ERR_NONFINITE;
+        if (S->active[k] && !isfinite(S->gam[k])) atomicCAS(&S->status, 0, FCG_ERR_NONFINITE);
       } else {  // alf = (v.r) / (v.v + small)   (bicgstab.f90:200)
         S->alf[k] = S->active[k] ? v[k] / (v[NS + k] + S->small) : 0.0;
-        if (S->active[k] && !isfinite(S->alf[k])) S->status = FCG_ERR_NONFINITE;
+        if (S->active[k] && !isfinite(S->alf[k])) atomicCAS(&S->status, 0, FCG_ERR_NONFINITE);
       }
     }
   }
@@ -364,7 +535,7 @@ __device__ __noinline__ void m_close(MScal *S, const double *l1, int ns,
   for (int k = 0; k < ns; ++k) {
     if (!S->active[k]) continue;
     S->rl[k] = l1[k];
-    if (!isfinite(l1[k])) S->status = FCG_ERR_NONFINITE;
+    if (!isfinite(l1[k])) atomicCAS(&S->status, 0, FCG_ERR_NONFINITE);
     if (l1[k] < S->inner_tol * S->r0in[k]) S->active[k] = 0;
     any |= S->active[k];
   }
@@ -388,7 +559,7 @@ __global__ void __launch_bounds__(kTPB, 6)
   if (blockIdx.x == 0 && threadIdx.x == 0) {  // bound on the loop, independent of the sums
     unsigned int c = atomicAdd(&S->body_count, 1u) + 1u;
     if (c > (unsigned int)S->inner_max + 2u) {
-      S->status = FCG_ERR_TIMEOUT;
+      atomicCAS(&S->status, 0, FCG_ERR_TIMEOUT);
       S->idone = 1;
       if (use_cond) cudaGraphSetConditional(h, 0);
     }
@@ -434,6 +605,20 @@ struct Launch {
   static void sweeps(fcg_context *c, cudaStream_t st, const Level &lv, bool fwd, const float *b,
                      float *z) {
     MultiState *m = c->ms;
+    if (m->sf_on) {
+      if (fwd) {  // b -> y32, after the sentinel fill of y32 and z
+        k_m_sf_fill<<<grid_for((long long)NS * m->n, c->num_sms), kTPB, 0, st>>>(
+            (long long)NS * m->n, m->y32, z, m->ctl);
+        k_m_fwd_sf<NS><<<m->sf_grid, kTPB, 0, st>>>(lv.pad, lv.pad_len, m->nnz, m->n,
+                                                    c->mv.ioffset, c->mv.ja, c->mv.diag, m->a32,
+                                                    m->d32, b, m->y32, m->ctl, m->S);
+      } else {  // y32 -> z
+        k_m_bwd_sf<NS><<<m->sf_grid, kTPB, 0, st>>>(lv.pad, lv.pad_len, m->nnz, m->n,
+                                                    c->mv.ioffset, c->mv.ja, c->mv.diag, m->a32,
+                                                    m->d32, m->y32, z, m->ctl, m->S);
+      }
+      return;
+    }
     for (int l = 0; l < lv.count; ++l) {
       const int start = lv.ptr[l], cnt = lv.ptr[l + 1] - lv.ptr[l];
       const int g = (cnt + kTPB - 1) / kTPB;
@@ -465,6 +650,14 @@ struct Launch {
 
   static void factor(fcg_context *c) {
     MultiState *m = c->ms;
+    if (m->sf_on) {
+      k_m_sf_fill<<<grid_for((long long)NS * m->n, c->num_sms), kTPB, 0, c->stream>>>(
+          (long long)NS * m->n, m->d32, nullptr, m->ctl);
+      k_m_factor_sf<NS><<<m->sf_grid, kTPB, 0, c->stream>>>(
+          c->lf.pad, c->lf.pad_len, m->nnz, m->n, c->mv.ioffset, c->mv.ja, c->mv.diag, c->tpos,
+          m->a32, m->d32, m->ctl, m->S);
+      return;
+    }
     for (int l = 0; l < c->lf.count; ++l) {
       const int start = c->lf.ptr[l], cnt = c->lf.ptr[l + 1] - c->lf.ptr[l];
       k_m_factor<NS><<<(cnt + kTPB - 1) / kTPB, kTPB, 0, c->stream>>>(
@@ -614,6 +807,15 @@ int ensure_multi(fcg_context *c, int ns) {
   for (float **v : vecs) {
     *v = f;
     f += nn;
+  }
+  FCG_CUDA_TRY(c, m->sfb.ensure(nn * sizeof(float) + 16 * sizeof(int)));
+  FCG_CUDA_TRY(c, cudaMemset(m->sfb.p, 0, nn * sizeof(float) + 16 * sizeof(int)));
+  m->y32 = m->sfb.as<float>();
+  m->ctl = (int *)(m->y32 + nn);
+  m->sf_grid = c->num_sms * 2;
+  {
+    const char *e = std::getenv("FCG_SWEEP");
+    m->sf_on = !(e && std::string(e) == "levels");
   }
   m->n = c->n;
   m->ns = ns;

@@ -68,3 +68,31 @@ def test_sweep_wait_runs_out_and_device_stays_usable():
     assert r.converged and abs(r.iters - o.iters) <= 1
     assert np.abs(r.fi - o.fi).max() / np.abs(o.fi).max() < 1e-8
     c.close()
+
+
+@pytest.mark.parametrize("name", ["hex16", "pitzdaily"])
+def test_multi_rhs_one_launch_sweeps_equal_level_sweeps(name):
+    """The FP32 DILU sweeps of the multi-RHS BiCGStab in both kernel forms."""
+    from freecappuccino_gb300.systems import transport_systems
+
+    m = hex_mesh(16, 0.2) if name == "hex16" else fixture_mesh("pitzdaily")
+    csr = oracle_csr(m)
+    a, su, _ = transport_systems(m, (csr.ioffset, csr.ja, csr.diag, csr.slot_pn, csr.slot_np))
+    out = []
+    for levels in (False, True):
+        c = _context(m, levels)
+        old = os.environ.get("FCG_SWEEP")
+        if levels:
+            os.environ["FCG_SWEEP"] = "levels"  # read when the multi-RHS state is made
+        try:
+            out.append(c.bicgstab_multi(a, su, np.zeros_like(su), 1e-10, 2000))
+        finally:
+            if old is None:
+                os.environ.pop("FCG_SWEEP", None)
+            else:
+                os.environ["FCG_SWEEP"] = old
+        c.close()
+    (x1, r1), (x2, r2) = out
+    assert np.array_equal(x1, x2)
+    assert [r.iters for r in r1] == [r.iters for r in r2]
+    assert all(r.converged for r in r1)
