@@ -319,6 +319,98 @@ def run_calcp(dev, N=128, npcor=3, seed=SEED + 1):
             "seconds": t, "iccg_iterations": iters, "cells": n}
 
 
+def run_assembly(ctx, m, dev, stream, peak, reps=5, seed=SEED + 3):
+    """The face-loop entry points on the benchmark mesh through the C ABI with every array
+    on the device and preallocated (no copies inside the timed calls), each timed with
+    CUDA events on the library's stream: the mean of `reps` calls after one warm-up.
+    Algorithmic bytes are those of the arrays the reference routine reads and writes,
+    each counted once: mesh arrays (owner/neighbour 8 B, area vector 24 B, face centre
+    24 B, facint 8 B, slot maps 8 B per inner face; cell centre 24 B, volume 8 B, diag
+    4 B per cell), fields and results; the incidence lists the kernels gather through are
+    not counted."""
+    import torch
+
+    from freecappuccino_gb300 import _lib
+    from freecappuccino_gb300.systems import flow_fields
+
+    lib, h = ctx.lib, ctx.h
+    n, F, nnz = m.numCells, m.numInnerFaces, m.nnz
+    nb = m.numTotal - n
+    f64 = dict(dtype=torch.float64, device=dev)
+    with torch.cuda.stream(stream):
+        f = {k: torch.from_numpy(v).to(dev) for k, v in flow_fields(m, seed).items()}
+        g = torch.Generator(device="cpu").manual_seed(seed)
+        vis = (1e-3 * (1.0 + torch.rand(m.numTotal, generator=g, dtype=torch.float64))).to(dev)
+        flm = (0.05 * (2 * torch.rand(F, generator=g, dtype=torch.float64) - 1)).to(dev)
+        mu = -torch.ones(n, **f64)
+        phi = torch.zeros(m.numTotal, **f64)
+        a, su, sv, sw = torch.zeros(nnz, **f64), torch.zeros(n, **f64), torch.zeros(n, **f64), \
+            torch.zeros(n, **f64)
+        grad = torch.zeros((n, 3), **f64)
+        dvw, rhs, ap = torch.zeros((2, n), **f64), torch.zeros((3, n), **f64), \
+            torch.zeros((3, n), **f64)
+        uu, vv, ww = (f[k].clone() for k in ("u", "v", "w"))
+        den_c = f["den"][:n].contiguous()
+        hmat = torch.zeros(nnz, **f64)
+        assert lib.fcg_laplacian(h, mu.data_ptr(), phi.data_ptr(), hmat.data_ptr(),
+                                 su.data_ptr()) == 0
+    stream.synchronize()
+    P = lambda t: t.data_ptr()  # noqa: E731
+    ff = _lib.FlowFields(*[P(f[k]) for k in ("u", "v", "w", "p", "dUdxi", "dVdxi", "dWdxi",
+                                              "dPdxi", "apu", "apv", "apw", "den")])
+    uvp = _lib.UvwParams(_lib.CONV_SCHEMES["muscl"], 0, 1.0, 1e-3, (C.c_double * 3)(*[1 / 0.7] * 3),
+                         (C.c_double * 3)(*[0.3] * 3), 0, 0, 1.0, 0.0, 0, 0.0, 0, 0, 0.0, 1.0,
+                         0.0, 0.0, 0.0, 0.0)
+    uvf = _lib.UvwFields(P(f["u"]), P(f["v"]), P(f["w"]), P(f["p"]), P(vis), P(den_c), None,
+                         None, None, None, None, None, None, P(f["dUdxi"]), P(f["dVdxi"]),
+                         P(f["dWdxi"]), P(f["dPdxi"]), P(flm), None, None)
+    hp = _lib.HbyaParams(1.0, 0.0, 0, 0, 0, 0, 0.0, 1.0, 0.0, 0.0, 0.0, 0.0)
+    hf = _lib.HbyaFields(P(den_c), None, None, None, None, None, None, None, P(f["apu"]),
+                         P(f["apv"]), P(f["apw"]))
+    ops = {
+        "laplacian": (lambda: lib.fcg_laplacian(h, P(mu), P(phi), P(a), P(su)),
+                      48 * F + 52 * n + 8 * nnz),
+        "facefluxmass": (lambda: lib.fcg_facefluxmass(h, C.byref(ff), P(a), P(su), P(flm)),
+                         80 * F + 204 * n + 8 * nnz),
+        "fluxmc": (lambda: lib.fcg_fluxmc(h, P(f["dPdxi"]), P(f["apu"]), P(f["den"]), P(su),
+                                          P(flm)), 80 * F + 80 * n),
+        "grad_gauss": (lambda: lib.fcg_grad(h, P(f["p"]), P(grad), _lib.FCG_GRAD_GAUSS, 1),
+                       64 * F + 36 * nb + 64 * n),
+        "calcuvw": (lambda: lib.fcg_calcuvw(h, C.byref(uvp), C.byref(uvf), P(a), P(dvw), P(rhs),
+                                            P(ap)), 80 * F + 256 * n + 8 * nnz + 92 * nb),
+        "piso_hbya": (lambda: lib.fcg_piso_hbya(h, C.byref(hp), C.byref(hf), P(hmat), P(uu),
+                                                P(vv), P(ww), P(su), P(sv), P(sw)),
+                      32 * F + 96 * n),
+        "facefluxmass_piso": (lambda: lib.fcg_facefluxmass_piso(h, C.byref(ff), P(a), P(su),
+                                                                P(flm)),
+                              80 * F + 156 * n + 8 * nnz),
+        "flux_correct": (lambda: lib.fcg_flux_correct(h, P(hmat), P(f["p"]), P(flm)),
+                         36 * F + 8 * n),
+        "correct_velocity_piso": (lambda: lib.fcg_correct_velocity_piso(
+            h, P(f["dPdxi"]), P(f["apu"]), P(f["apv"]), P(f["apw"]), P(uu), P(vv), P(ww)),
+            104 * n),
+    }
+    out = {}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for name, (fn, nbytes) in ops.items():
+        assert fn() == 0, name
+        stream.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        out[name] = {"ms": ms, "algorithmic_bytes": nbytes, "achieved_GBps": gbs,
+                     "frac": gbs / peak}
+    return {"workload": f"face-loop assembly entry points, {n} cells ({F} inner faces), "
+                        "device arrays, seeded fields",
+            "bound": "fp64 pipe: bit-exact FP64 face arithmetic keeps it 77-87% busy "
+                     "(ncu, profiles/assembly_kernels_128.md); frac is of the HBM peak",
+            "kernels": out}
+
+
 def run_multi(dev, N=128, seed=SEED + 2):
     """The five transport systems (u, v, w, k, eps) on one pattern solved in one
     multi-RHS BiCGStab (FP32 DILU inner, FP64 correction to 1e-10) against the same
@@ -385,6 +477,8 @@ def main():
     ap.add_argument("--weights", default=None, help="learned checkpoint (default: shipped)")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven sweep loop instead of the CUDA-graph WHILE loop")
+    ap.add_argument("--only", choices=["assembly"], default=None,
+                    help="run one section alone on the --N mesh and print it (profiling)")
     args = ap.parse_args()
     if args.no_graph:
         os.environ["FCG_NO_GRAPH"] = "1"
@@ -409,6 +503,12 @@ def main():
     t_bind = time.perf_counter() - t0
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
+    if args.only == "assembly":
+        out = run_assembly(ctx, m, torch.device("cuda", local), stream, peaks()[0])
+        if rank == 0:
+            print(json.dumps({"section": "assembly", "N": N, **out}), flush=True)
+        ctx.close()
+        return
     n, nnz = m.numCells, m.nnz
     dev = torch.device("cuda", local)
     with torch.cuda.stream(stream):
@@ -562,10 +662,11 @@ def main():
     batch = None
     if not args.no_batch:
         batch = run_batch(args, dev, peak)
-    calcp = multi = None
+    calcp = multi = assembly = None
     if not args.no_configs:
         calcp = run_calcp(dev)
         multi = run_multi(dev)
+        assembly = run_assembly(ctx, m, dev, stream, peak)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -577,7 +678,7 @@ def main():
         extra = {"comparisons": comparisons, "spmv_fp64": spmv64,
                  "l2_rel_final": last.l2_rel, "resl_over_res0": last.resl / last.res0,
                  "mesh_setup_s": t_mesh, "bind_s": t_bind, "step_s": step_s, "batched": batch,
-                 "calcp_step": calcp, "multi_rhs": multi}
+                 "calcp_step": calcp, "multi_rhs": multi, "assembly": assembly}
         if method == "learned":
             extra["learned"] = {"fcg_iterations": last.fcg_iters, "fallback": last.fallback,
                                 "directions": 8, "weights": os.path.relpath(
