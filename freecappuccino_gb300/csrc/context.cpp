@@ -222,7 +222,22 @@ extern "C" int fcg_bind_mesh(fcg_context *c, const fcg_mesh_desc *m) {
   hm.neighbour = nei.data();
   HostTopology t;
   std::string err;
-  rc = build_topology(hm, cnt, fst, bst, t, err);
+  if ((rc = validate_topology(hm, cnt, fst, err))) return set_error(c, rc, err);
+  // The CSR and slot maps by the GPU kernels of fcg_csr_build_gpu (identical to the host
+  // construction, which is a sequential scatter over the faces), the rest on the host.
+  if ((long long)n + 2LL * nin <= 0x7fffffffLL) {
+    t.ioffset.resize(n + 1);
+    t.ja.resize((size_t)n + 2 * (size_t)nin);
+    t.diag.resize(n);
+    t.slot_pn.resize(nin);
+    t.slot_np.resize(nin);
+    if ((rc = fcg_csr_build_gpu(c, n, nin, own.data(), nei.data(), t.ioffset.data(), t.ja.data(),
+                                t.diag.data(), t.slot_pn.data(), t.slot_np.data())))
+      return rc;
+    rc = build_topology(hm, cnt, fst, bst, t, err, true);
+  } else {
+    rc = build_topology(hm, cnt, fst, bst, t, err);
+  }
   if (rc) return set_error(c, rc, err);
 
   c->n = n;

@@ -148,8 +148,16 @@ struct HostTopology {
   std::vector<int> tpos;
 };
 
+// csr_given: t already holds the 1-based CSR and slot maps (built on the GPU by
+// fcg_csr_build_gpu, which also refuses duplicate cell pairs).
 int build_topology(const fcg_mesh_desc &m, const int cnt[B_NTYPES], const int fst[B_NTYPES],
-                   const int bst[B_NTYPES], HostTopology &t, std::string &err);
+                   const int bst[B_NTYPES], HostTopology &t, std::string &err,
+                   bool csr_given = false);
+int validate_topology(const fcg_mesh_desc &m, const int cnt[B_NTYPES], const int fst[B_NTYPES],
+                      std::string &err);
+int build_csr(const fcg_mesh_desc &m, HostTopology &t, std::string &err);
+int build_rest(const fcg_mesh_desc &m, const int cnt[B_NTYPES], const int fst[B_NTYPES],
+               const int bst[B_NTYPES], HostTopology &t);
 
 // Pointer staging: returns a device pointer for a user array of `bytes` bytes.  A
 // device pointer is returned as is; a host array is copied into staging slot `slot`

@@ -12,6 +12,7 @@
 // * Level schedules of the lower and upper triangles (row i waits for the rows its
 //   lower/upper entries name) for the DIC/DILU sweeps of iccg.f90 / bicgstab.f90.
 #include <algorithm>
+#include <cstdlib>
 #include <string>
 
 #include "fcg_internal.h"
@@ -19,10 +20,9 @@
 
 namespace fcg {
 
-int build_topology(const fcg_mesh_desc &m, const int cnt[B_NTYPES], const int fst[B_NTYPES],
-                   const int bst[B_NTYPES], HostTopology &t, std::string &err) {
+int validate_topology(const fcg_mesh_desc &m, const int cnt[B_NTYPES], const int fst[B_NTYPES],
+                      std::string &err) {
   const int n = m.numCells, nf = m.numFaces, nin = m.numInnerFaces;
-  // --- validation ----------------------------------------------------------
   for (int f = 0; f < nf; ++f) {
     int o = m.owner[f];
     if (o < 1 || o > n) {
@@ -44,7 +44,25 @@ int build_topology(const fcg_mesh_desc &m, const int cnt[B_NTYPES], const int fs
       return FCG_ERR_INDEX;
     }
   }
-  // --- CSR -------------------------------------------------------------------
+  return FCG_OK;
+}
+
+int build_topology(const fcg_mesh_desc &m, const int cnt[B_NTYPES], const int fst[B_NTYPES],
+                   const int bst[B_NTYPES], HostTopology &t, std::string &err, bool csr_given) {
+  const int n = m.numCells, nf = m.numFaces, nin = m.numInnerFaces;
+  int vrc = validate_topology(m, cnt, fst, err);
+  if (vrc) return vrc;
+  if (!csr_given) {
+    int crc = build_csr(m, t, err);
+    if (crc) return crc;
+  }
+  return build_rest(m, cnt, fst, bst, t);
+}
+
+// CSR of create_CSR_matrix_from_mesh_data (sparse_matrix.f90:42-172), 1-based, with the
+// face slot maps.
+int build_csr(const fcg_mesh_desc &m, HostTopology &t, std::string &err) {
+  const int n = m.numCells, nin = m.numInnerFaces;
   t.ioffset.assign(n + 1, 0);
   std::vector<int> rowcnt(n, 1);
   for (int f = 0; f < nin; ++f) {
@@ -101,6 +119,20 @@ int build_topology(const fcg_mesh_desc &m, const int cnt[B_NTYPES], const int fs
     t.slot_pn[f] = find(m.owner[f], m.neighbour[f]);
     t.slot_np[f] = find(m.neighbour[f], m.owner[f]);
   });
+  return FCG_OK;
+}
+
+// Everything built from the CSR and the face lists: transpose positions, incidence lists,
+// the sliced ELL copy and the level schedules.
+int build_rest(const fcg_mesh_desc &m, const int cnt[B_NTYPES], const int fst[B_NTYPES],
+               const int bst[B_NTYPES], HostTopology &t) {
+  const int n = m.numCells, nf = m.numFaces, nin = m.numInnerFaces;
+  const long long nnz = (long long)t.ioffset[n] - 1;
+  auto find = [&](int row1, int col1) {  // 1-based position of (row, col), 0 if absent
+    int b = t.ioffset[row1 - 1] - 1, e = t.ioffset[row1] - 1;
+    auto it = std::lower_bound(t.ja.begin() + b, t.ja.begin() + e, col1);
+    return (it != t.ja.begin() + e && *it == col1) ? (int)(it - t.ja.begin()) + 1 : 0;
+  };
   t.tpos.assign(nnz, 0);
   parallel_for(n, [&](long long i) {
     for (int k = t.ioffset[i] - 1; k < t.ioffset[i + 1] - 1; ++k)
@@ -108,25 +140,35 @@ int build_topology(const fcg_mesh_desc &m, const int cnt[B_NTYPES], const int fs
   });
 
   // --- incidence lists ---------------------------------------------------------
+  // The inner faces of cell i are its off-diagonal CSR entries (one per face), so the
+  // list is built per row from the CSR: each entry's face (the inverse of the slot
+  // maps), sorted by face index -- the order of a face loop over the cell.
   t.cf_ptr.assign(n + 1, 0);
-  for (int f = 0; f < nin; ++f) {
-    t.cf_ptr[m.owner[f]]++;
-    t.cf_ptr[m.neighbour[f]]++;
-  }
-  for (int i = 0; i < n; ++i) t.cf_ptr[i + 1] += t.cf_ptr[i];
+  for (int i = 0; i <= n; ++i) t.cf_ptr[i] = (t.ioffset[i] - 1) - i;
   t.cf_ent.assign(t.cf_ptr[n], 0);
   t.cf_slot.assign(t.cf_ptr[n], 0);
   {
-    std::vector<int> fill(t.cf_ptr.begin(), t.cf_ptr.end() - 1);
-    for (int f = 0; f < nin; ++f) {
-      int o = m.owner[f] - 1, nb = m.neighbour[f] - 1;
-      int e = fill[o]++;
-      t.cf_ent[e] = f + 1;
-      t.cf_slot[e] = t.slot_pn[f] - 1;
-      e = fill[nb]++;
-      t.cf_ent[e] = -(f + 1);
-      t.cf_slot[e] = t.slot_np[f] - 1;
-    }
+    std::vector<int> face_at(nnz, -1);
+    parallel_for(nin, [&](long long f) {
+      face_at[t.slot_pn[f] - 1] = (int)f;
+      face_at[t.slot_np[f] - 1] = (int)f;
+    });
+    parallel_for(n, [&](long long i) {
+      int e = t.cf_ptr[i];
+      for (int k = t.ioffset[i] - 1; k < t.ioffset[i + 1] - 1; ++k) {
+        if (k == t.diag[i] - 1) continue;
+        const int f = face_at[k];
+        int j = e++;
+        // insertion into the row's list, ascending face index
+        while (j > t.cf_ptr[i] && std::abs(t.cf_ent[j - 1]) > f + 1) {
+          t.cf_ent[j] = t.cf_ent[j - 1];
+          t.cf_slot[j] = t.cf_slot[j - 1];
+          --j;
+        }
+        t.cf_ent[j] = m.owner[f] == (int)i + 1 ? f + 1 : -(f + 1);
+        t.cf_slot[j] = k;
+      }
+    });
   }
   t.cb_ptr.assign(n + 1, 0);
   for (int ty = 0; ty < B_NTYPES; ++ty)
@@ -172,7 +214,8 @@ int build_topology(const fcg_mesh_desc &m, const int cnt[B_NTYPES], const int fs
   std::vector<int> ecols(ns, 0);  // explicit column block size per slice
   parallel_for(ns, [&](long long sl) {
     int wexp = 0;
-    std::vector<int> u;
+    thread_local std::vector<int> u;
+    u.clear();
     for (long long r = 32 * sl; r < std::min<long long>(n, 32 * sl + 32); ++r) {
       wexp = std::max(wexp, t.ioffset[r + 1] - t.ioffset[r]);
       for (int k = t.ioffset[r] - 1; k < t.ioffset[r + 1] - 1; ++k) u.push_back(t.ja[k] - 1 - (int)r);
@@ -182,7 +225,7 @@ int build_topology(const fcg_mesh_desc &m, const int cnt[B_NTYPES], const int fs
     if (!u.empty() && 2 * (long long)u.size() < 3LL * wexp) {  // 8w_u < 12w_e bytes per row
       t.sell_kind[sl] = 0;
       t.sell_width[sl] = (int)u.size();
-      uoffs[sl] = std::move(u);
+      uoffs[sl] = u;
     } else {
       t.sell_kind[sl] = 1;
       t.sell_width[sl] = wexp;
