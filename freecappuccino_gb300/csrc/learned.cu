@@ -188,35 +188,61 @@ __global__ void __launch_bounds__(kTPB, 8)
 }
 
 // f0 = r / rms (stored as feature 0); h0 = relu(W_in f + b_in) in BF16; z0
-// (pre-activation) when training.  Features are feature-major (k * n + i).  Four threads
-// per cell, eight output channels each (one 16-byte store).
+// (pre-activation) when training.  Features are feature-major (k * n + i).  One thread
+// per cell, the weights broadcast from shared memory; each warp stages its 32 x 32 BF16
+// output tile in shared memory (rows padded to 80 bytes, so the 16-byte writes of eight
+// lanes fall in distinct banks) and stores it as 2 KB of contiguous 16-byte writes.
+constexpr int kEmbRow = 40;  // BF16 elements per staged row (32 + 8 padding)
+
 __global__ void __launch_bounds__(kTPB)
     k_lp_embed(int n, const float *__restrict__ r, const float *__restrict__ rms,
                float *__restrict__ feat, const float *__restrict__ prm,
                __nv_bfloat16 *__restrict__ h0, float *__restrict__ z0, const int *done) {
   if (stopped(done)) return;
   __shared__ float w[C * F + C];
+  __shared__ __align__(16) __nv_bfloat16 tile[kTPB / 32][32 * kEmbRow];
   for (int t = threadIdx.x; t < C * F + C; t += blockDim.x) w[t] = prm[lp::oWin + t];
   __syncthreads();
   const float inv = 1.0f / rms[0];
-  FCG_GRID_STRIDE(t, 4LL * n) {
-    const long long i = t >> 2;
-    const int o0 = (int)(t & 3) * 8;
-    float f[F];
-    f[0] = r[i] * inv;
-    if (o0 == 0) feat[i] = f[0];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __nv_bfloat16 *my = tile[warp];
+  const long long nwarps = (long long)gridDim.x * (kTPB / 32);
+  for (long long base = ((long long)blockIdx.x * (kTPB / 32) + warp) * 32; base < n;
+       base += nwarps * 32) {
+    const long long i = base + lane;
+    if (i < n) {
+      float f[F];
+      f[0] = r[i] * inv;
+      feat[i] = f[0];
 #pragma unroll
-    for (int k = 1; k < F; ++k) f[k] = feat[k * (long long)n + i];
-    __align__(16) __nv_bfloat16 hv[8];
+      for (int k = 1; k < F; ++k) f[k] = feat[k * (long long)n + i];
 #pragma unroll
-    for (int o = 0; o < 8; ++o) {
-      float z = w[C * F + o0 + o];
+      for (int g = 0; g < C / 8; ++g) {
+        __align__(16) __nv_bfloat16 hv[8];
 #pragma unroll
-      for (int k = 0; k < F; ++k) z += w[(o0 + o) * F + k] * f[k];
-      if (z0) z0[i * C + o0 + o] = z;
-      hv[o] = __float2bfloat16(fmaxf(z, 0.f));
+        for (int o = 0; o < 8; ++o) {
+          const int oc = g * 8 + o;
+          float z = w[C * F + oc];
+#pragma unroll
+          for (int k = 0; k < F; ++k) z += w[oc * F + k] * f[k];
+          if (z0) z0[i * C + oc] = z;
+          hv[o] = __float2bfloat16(fmaxf(z, 0.f));
+        }
+        *reinterpret_cast<uint4 *>(my + lane * kEmbRow + g * 8) =
+            *reinterpret_cast<const uint4 *>(hv);
+      }
     }
-    *reinterpret_cast<uint4 *>(h0 + i * C + o0) = *reinterpret_cast<const uint4 *>(hv);
+    __syncwarp();
+    // 32 rows x 64 bytes = 128 chunks of 16 bytes, four per lane
+    const long long rows = n - base < 32 ? n - base : 32;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int c = lane + 32 * j, row = c >> 2, part = c & 3;
+      if (row < rows)
+        *reinterpret_cast<uint4 *>(h0 + (base + row) * C + part * 8) =
+            *reinterpret_cast<const uint4 *>(my + row * kEmbRow + part * 8);
+    }
+    __syncwarp();
   }
 }
 
@@ -1174,7 +1200,7 @@ void enqueue_forward(fcg_learned *Lp, fcg_context *c, cudaStream_t st, const flo
   __nv_bfloat16 *H = Lp->hbuf.as<__nv_bfloat16>();
   const size_t hs = (size_t)n * lp::C;
   k_lp_rms<<<reduction_grid(c), kTPB, 0, st>>>(n, r, Lp->red.as<double>(), rms_ticket, rms, done);
-  k_lp_embed<<<grid_for(4LL * n, c->num_sms, 16), kTPB, 0, st>>>(
+  k_lp_embed<<<grid_for(n, c->num_sms, 8), kTPB, 0, st>>>(
       n, r, rms, Lp->feat.as<float>(), prm, H, train ? Lp->zbuf.as<float>() : nullptr, done);
   const float *aval = scaled32(c);
   const __nv_bfloat16 *wbf = Lp->wbf.as<__nv_bfloat16>();
@@ -1499,7 +1525,7 @@ extern "C" int fcg_lp_profile(fcg_learned *Lp, fcg_context *c, const float *r, i
     k_lp_rms<<<reduction_grid(c), kTPB, 0, st>>>(n, dr, Lp->red.as<double>(),
                                                  Lp->scal.as<unsigned>() + 17, rms, nullptr);
     LP_TRY(Lp, cudaEventRecord(ev[1], st));
-    k_lp_embed<<<grid_for(4LL * n, c->num_sms, 16), kTPB, 0, st>>>(n, dr, rms, Lp->feat.as<float>(),
+    k_lp_embed<<<grid_for(n, c->num_sms, 8), kTPB, 0, st>>>(n, dr, rms, Lp->feat.as<float>(),
                                                                  prm, H, nullptr, nullptr);
     LP_TRY(Lp, cudaEventRecord(ev[2], st));
     for (int l = 0; l < lp::L; ++l) {
