@@ -1491,7 +1491,9 @@ extern "C" const char *fcg_profile_unit_name(const fcg_context *c, int unit) {
 
 extern "C" int fcg_get_solver_trace(fcg_context *c, double *out, int max_count, int *count) {
   if (!c || !c->ks) return FCG_ERR_STATE;
-  int avail = std::min(c->ks->hS->iter, c->ks->nsw_cap);
+  // the mixed solver records one entry per FP64 reliable update, the others one per sweep
+  const int written = c->ks->last_kind == SK_MIXED ? c->ks->hS->nupdates : c->ks->hS->iter;
+  int avail = std::min(written, c->ks->nsw_cap);
   int m = std::min(avail, max_count);
   if (count) *count = avail;
   if (out && m > 0)

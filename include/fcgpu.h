@@ -393,8 +393,9 @@ int fcg_set_solver_options(fcg_context *ctx, double small, int early_exit);
 int fcg_set_sweep_wait_test(fcg_context *ctx, int polls, int absent_row);
 
 /* Per-sweep (resl, rsm) pairs of the last solve -- what the reference prints per
- * sweep when ltest is set (dpcg.f90:141).  *count receives the number available;
- * at most max_count pairs are copied to resl_rsm (which may be NULL). */
+ * sweep when ltest is set (dpcg.f90:141); for fcg_dpcg_mixed one pair per FP64 residual
+ * replacement (the true residual).  *count receives the number available; at most
+ * max_count pairs are copied to resl_rsm (which may be NULL). */
 int fcg_get_solver_trace(fcg_context *ctx, double *resl_rsm, int max_count, int *count);
 
 /* No counterpart in the reference.  dpcg for callers that cannot allocate device

@@ -26,7 +26,24 @@ def hex_mesh(N: int, jitter: float = 0.2, seed: int = 7) -> fcg.Mesh:
     return fcg.hex_mesh(N, jitter=jitter, seed=seed, keep_topology=True)
 
 
+@functools.lru_cache(maxsize=None)
+def mixed_patch_mesh(N: int = 8) -> fcg.Mesh:
+    """A jittered N^3 hex mesh whose boundary faces carry all five boundary types: the
+    symmetry faces relabelled in four runs as inlet, outlet, pressure outlet and symmetry,
+    the x = 0 faces kept as wall."""
+    m = hex_mesh(N, 0.2)
+    ns, ss = m.counts["nsym"], m.starts["iSymmetryFacesStart"]
+    q = ns // 4
+    types = ["inlet", "outlet", "prOutlet", "symmetry", "wall"]
+    nfaces = [q, q, q, ns - 3 * q, m.counts["nwal"]]
+    starts = [ss, ss + q, ss + 2 * q, ss + 3 * q, m.starts["iWallFacesStart"]]
+    return fcg.polymesh_mesh(m.points, m.face_ptr, m.face_nodes, m.owner, m.neighbour,
+                             m.numCells, types, nfaces, starts)
+
+
 def mesh_by_name(name: str) -> fcg.Mesh:
+    if name.startswith("hexmix"):
+        return mixed_patch_mesh(int(name[6:]))
     if name.startswith("hex"):
         # hexN or hexN_u (uniform)
         body = name[3:]

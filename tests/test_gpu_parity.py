@@ -18,7 +18,7 @@ from tests.meshes import (GOLDEN, hex_mesh, mesh_by_name, oracle_csr, oracle_mes
 
 pytestmark = pytest.mark.gpu
 
-MESHES = ["hex8", "hex12_u", "cavity", "pitzdaily"]
+MESHES = ["hex8", "hex12_u", "cavity", "pitzdaily", "hexmix8"]
 _ctx_cache = {}
 
 

@@ -307,7 +307,9 @@ def _calcuvw_numpy(m, csr, kw, f, a_in):
 @pytest.mark.parametrize("k", [0, 4, 5, 9, 13, 14, 15, 16])
 def test_oracle_calcuvw_restates_the_loops(k):
     kw = OPTS[k]
-    for m in (hex_mesh(5, 0.2), fixture_mesh("pitzdaily")):
+    from tests.meshes import mixed_patch_mesh
+
+    for m in (hex_mesh(5, 0.2), fixture_mesh("pitzdaily"), mixed_patch_mesh(6)):
         csr = oracle_csr(m)
         f, a = _fields(m, 3), _a_in(m, 3)
         got = _oracle(m, csr, kw, f, a)
@@ -317,9 +319,11 @@ def test_oracle_calcuvw_restates_the_loops(k):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["pitzdaily", "hex8"])
+@pytest.mark.parametrize("name", ["pitzdaily", "hex8", "hexmix8"])
 def test_calcuvw_bit_exact(name):
-    m = fixture_mesh(name) if name == "pitzdaily" else hex_mesh(8, 0.2)
+    from tests.meshes import mesh_by_name
+
+    m = mesh_by_name(name)
     c = fcg.Context(m)
     csr = oracle_csr(m)
     f, a = _fields(m, 5), _a_in(m, 5)

@@ -135,7 +135,9 @@ def test_boundary_velocity_and_continuity_errors_bit_exact():
     (inlet, outlet and walls) and a hex mesh (symmetry patches)."""
     from tests.meshes import fixture_mesh
 
-    for m in (fixture_mesh("pitzdaily"), hex_mesh(8, 0.2)):
+    from tests.meshes import mixed_patch_mesh
+
+    for m in (fixture_mesh("pitzdaily"), hex_mesh(8, 0.2), mixed_patch_mesh(8)):
         c = fcg.Context(m)
         om = oracle_mesh(m)
         f = seeded_fields(m, seed=5)

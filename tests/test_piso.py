@@ -195,11 +195,13 @@ def test_oracle_piso_assembly_and_mass_flow_restate_the_loops():
     assert np.array_equal(wc[:n], f["w"][:n] - f["apw"] * f["dPdxi"][:, 2] * m.vol)
 
 
-MESHES = ["pitzdaily", "hex8"]
+MESHES = ["pitzdaily", "hex8", "hexmix8"]
 
 
 def _mesh(name):
-    return fixture_mesh(name) if name == "pitzdaily" else hex_mesh(8, 0.2)
+    from tests.meshes import mesh_by_name
+
+    return mesh_by_name(name)
 
 
 @pytest.mark.gpu
