@@ -106,6 +106,7 @@ _PROTOS = {
     "fcg_mesh_sizes": (C.c_int, [_CTX, _ip, _ip, _ip, C.POINTER(C.c_longlong), _ip]),
     "fcg_create_csr": (C.c_int, [_CTX, _vp, _vp, _vp, _vp, _vp]),
     "fcg_csr_build": (C.c_int, [C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "fcg_topology_digest": (C.c_int, [_CTX, C.POINTER(C.c_ulonglong)]),
     "fcg_csr_build_gpu": (C.c_int, [_CTX, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "fcg_mesh_geometry_gpu": (C.c_int, [_CTX, C.c_int, _vp, _vp, _vp, C.c_int, C.c_int, C.c_int,
                                         _vp, _vp, _vp, _vp] + [_vp] * 11),

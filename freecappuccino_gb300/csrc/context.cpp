@@ -1,5 +1,6 @@
 // Context lifecycle, mesh binding, CSR export and host<->device staging of libfcgpu.so.
 #include <atomic>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -83,6 +84,21 @@ static int host_copy(fcg_context *c, const T *user, size_t count, std::vector<T>
   } else {
     std::memcpy(out.data(), user, count * sizeof(T));
   }
+  return FCG_OK;
+}
+
+// A bound device copy of a caller array that may be host or device memory, copied in
+// one transfer (no host staging).
+template <class T>
+static int upload_any(fcg_context *c, const T *user, size_t count, const T **out) {
+  c->bound_allocs.emplace_back();
+  DBuf &b = c->bound_allocs.back();
+  FCG_CUDA_TRY(c, b.ensure(count * sizeof(T)));
+  if (count)
+    FCG_CUDA_TRY(c, cudaMemcpy(b.p, user, count * sizeof(T),
+                               is_device_pointer(user) ? cudaMemcpyDeviceToDevice
+                                                       : cudaMemcpyHostToDevice));
+  *out = (const T *)b.p;
   return FCG_OK;
 }
 
@@ -223,29 +239,19 @@ extern "C" int fcg_bind_mesh(fcg_context *c, const fcg_mesh_desc *m) {
   HostTopology t;
   std::string err;
   if ((rc = validate_topology(hm, cnt, fst, err))) return set_error(c, rc, err);
-  // The CSR and slot maps by the GPU kernels of fcg_csr_build_gpu (identical to the host
-  // construction, which is a sequential scatter over the faces), the rest on the host.
-  if ((long long)n + 2LL * nin <= 0x7fffffffLL) {
-    t.ioffset.resize(n + 1);
-    t.ja.resize((size_t)n + 2 * (size_t)nin);
-    t.diag.resize(n);
-    t.slot_pn.resize(nin);
-    t.slot_np.resize(nin);
-    if ((rc = fcg_csr_build_gpu(c, n, nin, own.data(), nei.data(), t.ioffset.data(), t.ja.data(),
-                                t.diag.data(), t.slot_pn.data(), t.slot_np.data())))
-      return rc;
-    rc = build_topology(hm, cnt, fst, bst, t, err, true);
-  } else {
-    rc = build_topology(hm, cnt, fst, bst, t, err);
-  }
-  if (rc) return set_error(c, rc, err);
+  // The topology is built on the device (bind_topology_device), identical to the host
+  // construction, which FCG_TOPOLOGY=host selects instead.
+  const char *te = std::getenv("FCG_TOPOLOGY");
+  const bool host_topo =
+      (te && std::string(te) == "host") || (long long)n + 2LL * nin > 0x7fffffffLL;
+  if (host_topo && (rc = build_topology(hm, cnt, fst, bst, t, err))) return set_error(c, rc, err);
 
   c->n = n;
   c->nf = nf;
   c->nin = nin;
   c->nb = nb;
   c->ntot = n + nb;
-  c->nnz = (long long)t.ja.size();
+  c->nnz = host_topo ? (long long)t.ja.size() : (long long)n + 2LL * nin;
   std::memcpy(c->cnt, cnt, sizeof cnt);
   std::memcpy(c->fst, fst, sizeof fst);
   std::memcpy(c->bst, bst, sizeof bst);
@@ -257,102 +263,156 @@ extern "C" int fcg_bind_mesh(fcg_context *c, const fcg_mesh_desc *m) {
   v.nin = nin;
   v.ntot = c->ntot;
   v.nnz = c->nnz;
-  std::vector<int> own0(own), nei0(nei);
-  for (auto &x : own0) x -= 1;
-  for (auto &x : nei0) x -= 1;
 #define UP(dst, src, count)                                  \
   do {                                                       \
     if ((rc = upload(c, (src), (size_t)(count), &(dst)))) return rc; \
   } while (0)
-  UP(v.owner, own0.data(), nf);
-  UP(v.neighbour, nei0.data(), nin);
-  // Geometry may be host or device; stage it through host vectors.
-  std::vector<double> tmp;
+  // owner / neighbour: the 1-based host copies, made 0-based on the device
+  if ((rc = upload_any(c, own.data(), (size_t)nf, &v.owner)) ||
+      (rc = upload_any(c, nei.data(), (size_t)nin, &v.neighbour)))
+    return rc;
+  if ((rc = to_zero_based(c, const_cast<int *>(v.owner), nf)) ||
+      (rc = to_zero_based(c, const_cast<int *>(v.neighbour), nin)))
+    return rc;
+  // geometry, host or device, copied as it is
   const double *src_f[] = {m->arx, m->ary, m->arz, m->xf, m->yf, m->zf};
   const double **dst_f[] = {&v.arx, &v.ary, &v.arz, &v.xf, &v.yf, &v.zf};
-  for (int i = 0; i < 6; ++i) {
-    if ((rc = host_copy(c, src_f[i], nf, tmp))) return rc;
-    UP(*dst_f[i], tmp.data(), nf);
-  }
+  for (int i = 0; i < 6; ++i)
+    if ((rc = upload_any(c, src_f[i], (size_t)nf, dst_f[i]))) return rc;
   const double *src_c[] = {m->xc, m->yc, m->zc, m->vol};
   const double **dst_c[] = {&v.xc, &v.yc, &v.zc, &v.vol};
-  for (int i = 0; i < 4; ++i) {
-    if ((rc = host_copy(c, src_c[i], n, tmp))) return rc;
-    UP(*dst_c[i], tmp.data(), n);
-  }
-  if ((rc = host_copy(c, m->facint, nin, tmp))) return rc;
-  UP(v.facint, tmp.data(), nin);
+  for (int i = 0; i < 4; ++i)
+    if ((rc = upload_any(c, src_c[i], (size_t)n, dst_c[i]))) return rc;
+  if ((rc = upload_any(c, m->facint, (size_t)nin, &v.facint))) return rc;
+  FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
 
-  std::vector<int> io0(t.ioffset), ja0(t.ja), dg0(t.diag), spn0(t.slot_pn), snp0(t.slot_np);
-  for (auto &x : io0) x -= 1;
-  for (auto &x : ja0) x -= 1;
-  for (auto &x : dg0) x -= 1;
-  for (auto &x : spn0) x -= 1;
-  for (auto &x : snp0) x -= 1;
-  UP(v.ioffset, io0.data(), n + 1);
-  UP(v.ja, ja0.data(), ja0.size());
-  UP(v.diag, dg0.data(), n);
-  UP(v.slot_pn, spn0.data(), nin);
-  UP(v.slot_np, snp0.data(), nin);
-  UP(c->tpos, t.tpos.data(), t.tpos.size());
-  UP(v.cf_ptr, t.cf_ptr.data(), t.cf_ptr.size());
-  UP(v.cf_ent, t.cf_ent.data(), t.cf_ent.size());
-  UP(v.cf_slot, t.cf_slot.data(), t.cf_slot.size());
-  UP(v.cb_ptr, t.cb_ptr.data(), t.cb_ptr.size());
-  UP(v.cb_face, t.cb_face.data(), t.cb_face.size());
-  UP(v.cb_slot, t.cb_slot.data(), t.cb_slot.size());
-  UP(v.cb_type, t.cb_type.data(), t.cb_type.size());
-  UP(v.cbf_ptr, t.cbf_ptr.data(), t.cbf_ptr.size());
-  UP(v.cbf_face, t.cbf_face.data(), t.cbf_face.size());
+  if (!host_topo) {
+    if ((rc = bind_topology_device(c, v.owner, v.neighbour, own, cnt, fst, bst, err)))
+      return err.empty() ? rc : set_error(c, rc, err);
+  } else {
+    std::vector<int> io0(t.ioffset), ja0(t.ja), dg0(t.diag), spn0(t.slot_pn), snp0(t.slot_np);
+    for (auto &x : io0) x -= 1;
+    for (auto &x : ja0) x -= 1;
+    for (auto &x : dg0) x -= 1;
+    for (auto &x : spn0) x -= 1;
+    for (auto &x : snp0) x -= 1;
+    UP(v.ioffset, io0.data(), n + 1);
+    UP(v.ja, ja0.data(), ja0.size());
+    UP(v.diag, dg0.data(), n);
+    UP(v.slot_pn, spn0.data(), nin);
+    UP(v.slot_np, snp0.data(), nin);
+    UP(c->tpos, t.tpos.data(), t.tpos.size());
+    UP(v.cf_ptr, t.cf_ptr.data(), t.cf_ptr.size());
+    UP(v.cf_ent, t.cf_ent.data(), t.cf_ent.size());
+    UP(v.cf_slot, t.cf_slot.data(), t.cf_slot.size());
+    UP(v.cb_ptr, t.cb_ptr.data(), t.cb_ptr.size());
+    UP(v.cb_face, t.cb_face.data(), t.cb_face.size());
+    UP(v.cb_slot, t.cb_slot.data(), t.cb_slot.size());
+    UP(v.cb_type, t.cb_type.data(), t.cb_type.size());
+    UP(v.cbf_ptr, t.cbf_ptr.data(), t.cbf_ptr.size());
+    UP(v.cbf_face, t.cbf_face.data(), t.cbf_face.size());
 
-  SellView &s = c->sv;
-  s.nslices = (int)t.sell_width.size();
-  UP(s.ptr, t.sell_ptr.data(), t.sell_ptr.size());
-  UP(s.width, t.sell_width.data(), t.sell_width.size());
-  UP(s.kind, t.sell_kind.data(), t.sell_kind.size());
-  UP(s.offp, t.sell_offp.data(), t.sell_offp.size());
-  UP(s.off, t.sell_off.data(), t.sell_off.size());
-  UP(s.src, t.sell_src.data(), t.sell_src.size());
-  c->sell_maxw = t.sell_maxw;
-  c->sell_len = t.sell_ptr.back();
-  c->sell_nuniform = t.sell_nuniform;
+    SellView &s = c->sv;
+    s.nslices = (int)t.sell_width.size();
+    UP(s.ptr, t.sell_ptr.data(), t.sell_ptr.size());
+    UP(s.width, t.sell_width.data(), t.sell_width.size());
+    UP(s.kind, t.sell_kind.data(), t.sell_kind.size());
+    UP(s.offp, t.sell_offp.data(), t.sell_offp.size());
+    UP(s.off, t.sell_off.data(), t.sell_off.size());
+    UP(s.src, t.sell_src.data(), t.sell_src.size());
+    c->sell_maxw = t.sell_maxw;
+    c->sell_len = t.sell_ptr.back();
+    c->sell_nuniform = t.sell_nuniform;
 
-  const int *rows;
-  c->lf.ptr = t.lf_ptr;
-  c->lf.count = (int)t.lf_ptr.size() - 1;
-  UP(rows, t.lf_rows.data(), t.lf_rows.size());
-  c->lf.rows = const_cast<int *>(rows);
-  c->lb.ptr = t.lb_ptr;
-  c->lb.count = (int)t.lb_ptr.size() - 1;
-  UP(rows, t.lb_rows.data(), t.lb_rows.size());
-  c->lb.rows = const_cast<int *>(rows);
-  {
-    auto padded = [](const std::vector<int> &ptr, const std::vector<int> &rs) {
-      std::vector<int> out;
-      out.reserve(rs.size() + 32 * ptr.size());
-      for (size_t l = 0; l + 1 < ptr.size(); ++l) {
-        out.insert(out.end(), rs.begin() + ptr[l], rs.begin() + ptr[l + 1]);
-        while (out.size() % 32) out.push_back(-1);
-      }
-      return out;
-    };
-    std::vector<int> pf = padded(t.lf_ptr, t.lf_rows), pb = padded(t.lb_ptr, t.lb_rows);
-    UP(rows, pf.data(), pf.size());
-    c->lf.pad = const_cast<int *>(rows);
-    c->lf.pad_len = (int)pf.size();
-    UP(rows, pb.data(), pb.size());
-    c->lb.pad = const_cast<int *>(rows);
-    c->lb.pad_len = (int)pb.size();
+    const int *rows;
+    c->lf.ptr = t.lf_ptr;
+    c->lf.count = (int)t.lf_ptr.size() - 1;
+    UP(rows, t.lf_rows.data(), t.lf_rows.size());
+    c->lf.rows = const_cast<int *>(rows);
+    c->lb.ptr = t.lb_ptr;
+    c->lb.count = (int)t.lb_ptr.size() - 1;
+    UP(rows, t.lb_rows.data(), t.lb_rows.size());
+    c->lb.rows = const_cast<int *>(rows);
+    {
+      auto padded = [](const std::vector<int> &ptr, const std::vector<int> &rs) {
+        std::vector<int> out;
+        out.reserve(rs.size() + 32 * ptr.size());
+        for (size_t l = 0; l + 1 < ptr.size(); ++l) {
+          out.insert(out.end(), rs.begin() + ptr[l], rs.begin() + ptr[l + 1]);
+          while (out.size() % 32) out.push_back(-1);
+        }
+        return out;
+      };
+      std::vector<int> pf = padded(t.lf_ptr, t.lf_rows), pb = padded(t.lb_ptr, t.lb_rows);
+      UP(rows, pf.data(), pf.size());
+      c->lf.pad = const_cast<int *>(rows);
+      c->lf.pad_len = (int)pf.size();
+      UP(rows, pb.data(), pb.size());
+      c->lb.pad = const_cast<int *>(rows);
+      c->lb.pad_len = (int)pb.size();
+    }
   }
 #undef UP
 
-  c->h_ioffset.swap(t.ioffset);
-  c->h_ja.swap(t.ja);
-  c->h_diag.swap(t.diag);
-  c->h_slot_pn.swap(t.slot_pn);
-  c->h_slot_np.swap(t.slot_np);
+  if (host_topo) {
+    c->topo.clear();
+    {
+      auto rec = [&](const void *p, size_t bytes) { c->topo.emplace_back(p, bytes); };
+      rec(v.ioffset, sizeof(int) * (n + 1));
+      rec(v.ja, sizeof(int) * t.ja.size());
+      rec(v.diag, sizeof(int) * n);
+      rec(v.slot_pn, sizeof(int) * nin);
+      rec(v.slot_np, sizeof(int) * nin);
+      rec(c->tpos, sizeof(int) * t.tpos.size());
+      rec(v.cf_ptr, sizeof(int) * t.cf_ptr.size());
+      rec(v.cf_ent, sizeof(int) * t.cf_ent.size());
+      rec(v.cf_slot, sizeof(int) * t.cf_slot.size());
+      rec(v.cb_ptr, sizeof(int) * t.cb_ptr.size());
+      rec(v.cb_face, sizeof(int) * t.cb_face.size());
+      rec(v.cb_slot, sizeof(int) * t.cb_slot.size());
+      rec(v.cb_type, sizeof(int) * t.cb_type.size());
+      rec(v.cbf_ptr, sizeof(int) * t.cbf_ptr.size());
+      rec(v.cbf_face, sizeof(int) * t.cbf_face.size());
+      rec(c->sv.ptr, sizeof(long long) * t.sell_ptr.size());
+      rec(c->sv.width, sizeof(int) * t.sell_width.size());
+      rec(c->sv.kind, sizeof(int) * t.sell_kind.size());
+      rec(c->sv.offp, sizeof(int) * t.sell_offp.size());
+      rec(c->sv.off, sizeof(int) * t.sell_off.size());
+      rec(c->sv.src, sizeof(int) * t.sell_src.size());
+      rec(c->lf.rows, sizeof(int) * t.lf_rows.size());
+      rec(c->lb.rows, sizeof(int) * t.lb_rows.size());
+      rec(c->lf.pad, sizeof(int) * c->lf.pad_len);
+      rec(c->lb.pad, sizeof(int) * c->lb.pad_len);
+    }
+  }
   c->bound = true;
   c->bind_gen++;
+  return FCG_OK;
+}
+
+extern "C" int fcg_topology_digest(fcg_context *c, unsigned long long *digest) {
+  if (!c || !digest) return FCG_ERR_ARG;
+  if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_topology_digest before fcg_bind_mesh");
+  FCG_CUDA_TRY(c, cudaSetDevice(c->device));
+  FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  unsigned long long h = 1469598103934665603ULL;  // FNV-1a, 64 bit
+  auto mix = [&](const unsigned char *b, size_t nb) {
+    for (size_t i = 0; i < nb; ++i) {
+      h ^= b[i];
+      h *= 1099511628211ULL;
+    }
+  };
+  std::vector<unsigned char> buf;
+  for (const auto &a : c->topo) {
+    buf.resize(a.second);
+    if (a.second) FCG_CUDA_TRY(c, cudaMemcpy(buf.data(), a.first, a.second, cudaMemcpyDeviceToHost));
+    const unsigned long long len = a.second;
+    mix(reinterpret_cast<const unsigned char *>(&len), sizeof len);
+    mix(buf.data(), buf.size());
+  }
+  for (const auto *lv : {&c->lf, &c->lb})
+    mix(reinterpret_cast<const unsigned char *>(lv->ptr.data()), sizeof(int) * lv->ptr.size());
+  *digest = h;
   return FCG_OK;
 }
 
@@ -360,18 +420,26 @@ extern "C" int fcg_create_csr(fcg_context *c, int *ioffset, int *ja, int *diag, 
                               int *slot_np) {
   if (!c) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_create_csr before fcg_bind_mesh");
+  FCG_CUDA_TRY(c, cudaSetDevice(c->device));
+  FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  // the bound CSR is 0-based on the device; the reference's arrays are 1-based
   struct {
     int *dst;
-    const std::vector<int> *src;
-  } outs[] = {{ioffset, &c->h_ioffset}, {ja, &c->h_ja}, {diag, &c->h_diag},
-              {slot_pn, &c->h_slot_pn}, {slot_np, &c->h_slot_np}};
+    const int *src;
+    size_t count;
+  } outs[] = {{ioffset, c->mv.ioffset, (size_t)c->n + 1}, {ja, c->mv.ja, (size_t)c->nnz},
+              {diag, c->mv.diag, (size_t)c->n}, {slot_pn, c->mv.slot_pn, (size_t)c->nin},
+              {slot_np, c->mv.slot_np, (size_t)c->nin}};
+  std::vector<int> tmp;
   for (auto &o : outs) {
-    if (!o.dst || o.src->empty()) continue;
-    size_t bytes = o.src->size() * sizeof(int);
+    if (!o.dst || !o.count) continue;
+    tmp.resize(o.count);
+    FCG_CUDA_TRY(c, cudaMemcpy(tmp.data(), o.src, o.count * sizeof(int), cudaMemcpyDeviceToHost));
+    for (auto &x : tmp) x += 1;
     if (is_device_pointer(o.dst)) {
-      FCG_CUDA_TRY(c, cudaMemcpy(o.dst, o.src->data(), bytes, cudaMemcpyHostToDevice));
+      FCG_CUDA_TRY(c, cudaMemcpy(o.dst, tmp.data(), o.count * sizeof(int), cudaMemcpyHostToDevice));
     } else {
-      std::memcpy(o.dst, o.src->data(), bytes);
+      std::memcpy(o.dst, tmp.data(), o.count * sizeof(int));
     }
   }
   return FCG_OK;

@@ -5,6 +5,7 @@
 
 #include <cstdint>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/fcgpu.h"
@@ -104,8 +105,6 @@ struct fcg_context {
   long long nnz = 0;
   int cnt[fcg::B_NTYPES] = {0}, fst[fcg::B_NTYPES] = {0}, bst[fcg::B_NTYPES] = {0};
 
-  // host copies of the 1-based CSR (fcg_create_csr hands them back)
-  std::vector<int> h_ioffset, h_ja, h_diag, h_slot_pn, h_slot_np;
 
   // device allocations made by fcg_bind_mesh (mesh arrays and topology)
   std::vector<fcg::DBuf> bound_allocs;
@@ -115,6 +114,8 @@ struct fcg_context {
   long long sell_len = 0, sell_nuniform = 0;
   fcg::Level lf, lb;  // forward (lower) and backward (upper) level schedules
   const int *tpos = nullptr;  // CSR position of the transpose entry of every entry
+  // every topology array bound to the device (pointer, bytes), for fcg_topology_digest
+  std::vector<std::pair<const void *, size_t>> topo;
 
   // lazily built lsq matrices dmat(9,n)
   fcg::DBuf dmat;
@@ -158,6 +159,15 @@ int validate_topology(const fcg_mesh_desc &m, const int cnt[B_NTYPES], const int
 int build_csr(const fcg_mesh_desc &m, HostTopology &t, std::string &err);
 int build_rest(const fcg_mesh_desc &m, const int cnt[B_NTYPES], const int fst[B_NTYPES],
                const int bst[B_NTYPES], HostTopology &t);
+// The whole topology built on c's device (setup.cu), 0-based and owned by the bound
+// mesh, element for element the host construction: fills c->mv's CSR, slot maps and
+// incidence lists, c->tpos, c->sv, c->lf / c->lb, c->nnz and c->topo.  own0 / nei0 are
+// the device copies (0-based) of owner / neighbour, own_host the 1-based host owner.
+// a[i] -= 1 on the device (1-based index arrays to 0-based), on c's stream.
+int to_zero_based(fcg_context *c, int *a, long long n);
+int bind_topology_device(fcg_context *c, const int *own0, const int *nei0,
+                         const std::vector<int> &own_host, const int cnt[B_NTYPES],
+                         const int fst[B_NTYPES], const int bst[B_NTYPES], std::string &err);
 
 // Pointer staging: returns a device pointer for a user array of `bytes` bytes.  A
 // device pointer is returned as is; a host array is copied into staging slot `slot`

@@ -8,7 +8,10 @@
 // the atomics land.  The floating-point passes evaluate the host form's expressions in
 // the same order; this file is compiled with --fmad=false.  Every input index is checked
 // by a validation kernel before any kernel gathers through it.
+#include <algorithm>
 #include <climits>
+#include <string>
+#include <vector>
 
 #include "fcg_internal.h"
 #include "launch.h"
@@ -157,11 +160,13 @@ __global__ void k_csr_check(int n, int nin, const int *__restrict__ owner,
 }
 
 // row counts: 1 (the diagonal) + one per inner face the row's cell is on
+// (owner and neighbour indices are `base`-based: 1 for the reference's arrays, 0 for the
+// bound copies)
 __global__ void k_csr_count(int nin, const int *__restrict__ owner,
-                            const int *__restrict__ neighbour, int *__restrict__ cnt) {
+                            const int *__restrict__ neighbour, int base, int *__restrict__ cnt) {
   FCG_GRID_STRIDE(f, nin) {
-    atomicAdd(&cnt[owner[f] - 1], 1);
-    atomicAdd(&cnt[neighbour[f] - 1], 1);
+    atomicAdd(&cnt[owner[f] - base], 1);
+    atomicAdd(&cnt[neighbour[f] - base], 1);
   }
 }
 
@@ -175,10 +180,11 @@ __global__ void k_csr_fill_diag(int n, const int *__restrict__ off, int *__restr
 
 // (owner, neighbour) and (neighbour, owner) of every inner face (sparse_matrix.f90:60-71)
 __global__ void k_csr_fill_faces(int nin, const int *__restrict__ owner,
-                                 const int *__restrict__ neighbour, const int *__restrict__ off,
-                                 int *__restrict__ cursor, int *__restrict__ ja) {
+                                 const int *__restrict__ neighbour, int base,
+                                 const int *__restrict__ off, int *__restrict__ cursor,
+                                 int *__restrict__ ja) {
   FCG_GRID_STRIDE(f, nin) {
-    const int o = owner[f] - 1, q = neighbour[f] - 1;
+    const int o = owner[f] - base, q = neighbour[f] - base;
     ja[off[o] + atomicAdd(&cursor[o], 1)] = q + 1;
     ja[off[q] + atomicAdd(&cursor[q], 1)] = o + 1;
   }
@@ -213,11 +219,11 @@ __device__ __forceinline__ int find_col(const int *__restrict__ ja, int lo, int 
 
 // icell_jcell / jcell_icell slot maps (sparse_matrix.f90:153-167), 1-based
 __global__ void k_csr_slots(int nin, const int *__restrict__ owner,
-                            const int *__restrict__ neighbour, const int *__restrict__ off,
-                            const int *__restrict__ ja, int *__restrict__ slot_pn,
-                            int *__restrict__ slot_np) {
+                            const int *__restrict__ neighbour, int base,
+                            const int *__restrict__ off, const int *__restrict__ ja,
+                            int *__restrict__ slot_pn, int *__restrict__ slot_np) {
   FCG_GRID_STRIDE(f, nin) {
-    const int o = owner[f] - 1, q = neighbour[f] - 1;
+    const int o = owner[f] - base, q = neighbour[f] - base;
     slot_pn[f] = find_col(ja, off[o], off[o + 1], q + 1) + 1;
     slot_np[f] = find_col(ja, off[q], off[q + 1], o + 1) + 1;
   }
@@ -509,17 +515,17 @@ extern "C" int fcg_csr_build_gpu(fcg_context *c, int numCells, int numInnerFaces
   }
   k_fill_int<<<grid_for(n, c->num_sms), kTPB, 0, c->stream>>>(cnt, n, 1);
   if (nin > 0)
-    k_csr_count<<<grid_for(nin, c->num_sms), kTPB, 0, c->stream>>>(nin, ow, nb, cnt);
+    k_csr_count<<<grid_for(nin, c->num_sms), kTPB, 0, c->stream>>>(nin, ow, nb, 1, cnt);
   FCG_CHECK_LAUNCH(c, "k_csr_count");
   if ((rc = scan_exclusive(c, cnt, off, n, scan))) return rc;
   int *dj = (int *)dja;
   k_csr_fill_diag<<<grid_for(n, c->num_sms), kTPB, 0, c->stream>>>(n, off, dj, cursor);
   if (nin > 0)
-    k_csr_fill_faces<<<grid_for(nin, c->num_sms), kTPB, 0, c->stream>>>(nin, ow, nb, off, cursor,
+    k_csr_fill_faces<<<grid_for(nin, c->num_sms), kTPB, 0, c->stream>>>(nin, ow, nb, 1, off, cursor,
                                                                          dj);
   k_csr_sort<<<grid_for(n, c->num_sms), kTPB, 0, c->stream>>>(n, off, dj, (int *)ddg, flag);
   if (nin > 0)
-    k_csr_slots<<<grid_for(nin, c->num_sms), kTPB, 0, c->stream>>>(nin, ow, nb, off, dj,
+    k_csr_slots<<<grid_for(nin, c->num_sms), kTPB, 0, c->stream>>>(nin, ow, nb, 1, off, dj,
                                                                     (int *)dpn, (int *)dnp);
   k_csr_ioffset<<<grid_for(n + 1, c->num_sms), kTPB, 0, c->stream>>>(n + 1, off, (int *)dio);
   FCG_CHECK_LAUNCH(c, "fcg_csr_build_gpu");
@@ -632,3 +638,477 @@ extern "C" int fcg_mesh_geometry_gpu(fcg_context *c, int numNodes, const double 
   FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return FCG_OK;
 }
+
+// ---------------------------------------------------------------------------
+// The topology of fcg_bind_mesh on the device, 0-based, element for element the host
+// construction (topology.cpp): the CSR and slot maps (the kernels above), transpose
+// positions, inner-face incidence lists, the sliced ELL copy and the level values of the
+// sweeps.  The boundary lists (a pass over the boundary faces), the prefix sums over
+// slices and the grouping of rows by level run on the host.
+// ---------------------------------------------------------------------------
+namespace {
+
+__global__ void k_minus1(long long n, int *__restrict__ a) {
+  FCG_GRID_STRIDE(i, n) a[i] -= 1;
+}
+
+// 0-based position of column col in row `row`, -1 when absent (rows sorted)
+__device__ __forceinline__ int find0(const int *__restrict__ io, const int *__restrict__ ja,
+                                     int row, int col) {
+  int lo = io[row], hi = io[row + 1];
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (ja[mid] < col)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return (lo < io[row + 1] && ja[lo] == col) ? lo : -1;
+}
+
+__global__ void k_tpos0(int n, const int *__restrict__ io, const int *__restrict__ ja,
+                        int *__restrict__ tpos) {
+  FCG_GRID_STRIDE(i, n) {
+    for (int k = io[i]; k < io[i + 1]; ++k) tpos[k] = find0(io, ja, ja[k], (int)i);
+  }
+}
+
+__global__ void k_cf_ptr0(int n, const int *__restrict__ io, int *__restrict__ cf_ptr) {
+  FCG_GRID_STRIDE(i, n + 1) cf_ptr[i] = io[i] - (int)i;
+}
+
+__global__ void k_face_at0(int nin, const int *__restrict__ spn, const int *__restrict__ snp,
+                           int *__restrict__ face_at) {
+  FCG_GRID_STRIDE(f, nin) {
+    face_at[spn[f]] = (int)f;
+    face_at[snp[f]] = (int)f;
+  }
+}
+
+// inner faces of cell i in ascending face order: ent = f+1 (owner) / -(f+1), slot = the
+// CSR position of the entry in row i (the inverse of the slot maps, sorted by face)
+__global__ void k_cf_lists0(int n, const int *__restrict__ io, const int *__restrict__ dg,
+                            const int *__restrict__ owner0, const int *__restrict__ face_at,
+                            int *__restrict__ ent, int *__restrict__ slot) {
+  FCG_GRID_STRIDE(i, n) {
+    const int p0 = io[i] - (int)i;
+    int e = p0;
+    for (int k = io[i]; k < io[i + 1]; ++k) {
+      if (k == dg[i]) continue;
+      const int f = face_at[k];
+      int j = e++;
+      while (j > p0 && abs(ent[j - 1]) > f + 1) {
+        ent[j] = ent[j - 1];
+        slot[j] = slot[j - 1];
+        --j;
+      }
+      ent[j] = owner0[f] == (int)i ? f + 1 : -(f + 1);
+      slot[j] = k;
+    }
+  }
+}
+
+__global__ void k_maxrow(int n, const int *__restrict__ io, int *out) {
+  int m = 0;
+  FCG_GRID_STRIDE(i, n) m = max(m, io[i + 1] - io[i]);
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+// One warp per slice of 32 rows: the longest row, and the sorted distinct column offsets
+// (column - row) as long as a uniform slice stays cheaper than an explicit one
+// (2*|u| < 3*wexp); kind 0 with the offsets in u, or kind 1.
+__global__ void k_sell_shape0(int n, int ns, const int *__restrict__ io, const int *__restrict__ ja,
+                              int ucap, int *__restrict__ width, int *__restrict__ kind,
+                              int *__restrict__ u) {
+  const int lane = threadIdx.x & 31;
+  const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long sl = warp0; sl < ns; sl += nwarps) {
+    const long long r = 32 * sl + lane;
+    const int b = r < n ? io[r] : 0, e = r < n ? io[r + 1] : 0;
+    int wexp = e - b;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) wexp = max(wexp, __shfl_xor_sync(0xffffffffu, wexp, o));
+    int k = b, cnt = 0;
+    bool uniform = wexp > 0;
+    while (true) {
+      const int mine = k < e ? ja[k] - (int)r : INT_MAX;
+      const int m = __reduce_min_sync(0xffffffffu, mine);
+      if (m == INT_MAX) break;
+      if (2 * (cnt + 1) >= 3 * wexp) {  // one more distinct offset makes uniform dearer
+        uniform = false;
+        break;
+      }
+      if (lane == 0) u[sl * (long long)ucap + cnt] = m;
+      ++cnt;
+      if (mine == m) ++k;
+    }
+    if (lane == 0) {
+      kind[sl] = uniform ? 0 : 1;
+      width[sl] = uniform ? cnt : wexp;
+    }
+  }
+}
+
+// Offset table (uniform) or column block (explicit) of every slice and src = CSR
+// position of each value slot (-1: none).
+__global__ void k_sell_fill0(int n, int ns, const int *__restrict__ io, const int *__restrict__ ja,
+                             int ucap, const int *__restrict__ u, const int *__restrict__ width,
+                             const int *__restrict__ kind, const long long *__restrict__ ptr,
+                             const int *__restrict__ offp, int *__restrict__ off,
+                             int *__restrict__ src) {
+  const int lane = threadIdx.x & 31;
+  const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long sl = warp0; sl < ns; sl += nwarps) {
+    const long long r = 32 * sl + lane;
+    const int b = r < n ? io[r] : 0, e = r < n ? io[r + 1] : 0;
+    const int w = width[sl];
+    if (kind[sl] == 0) {
+      const int *us = u + sl * (long long)ucap;
+      for (int j = lane; j < w; j += 32) off[offp[sl] + j] = us[j];
+      for (int j = 0; j < w; ++j) {
+        int sidx = -1;
+        const int want = (int)r + us[j];
+        for (int k = b; k < e; ++k)
+          if (ja[k] == want) sidx = k;
+        src[ptr[sl] + (long long)j * 32 + lane] = sidx;
+      }
+    } else {
+      for (int j = 0; j < w; ++j) {
+        const long long pos = ptr[sl] + (long long)j * 32 + lane;
+        const long long cpos = offp[sl] + (long long)j * 32 + lane;
+        if (j < e - b) {
+          off[cpos] = ja[b + j];
+          src[pos] = b + j;
+        } else {
+          off[cpos] = (int)(r < n - 1 ? r : n - 1);
+          src[pos] = -1;
+        }
+      }
+    }
+  }
+}
+
+// Level of every row in one launch, rows taken in sweep order: lane 0 of a warp claims
+// 32 consecutive rows through a counter and does them in order; level = 1 + the largest
+// level of the rows it reads, 0 without any.  lev holds -1 until a row's level is
+// written; a row only reads rows earlier in the sweep order -- earlier in its own chunk
+// (done by this thread) or in a chunk claimed earlier by a running warp -- so every wait
+// ends; each is bounded, and one that gives up sets err.
+__global__ void k_levels0(int n, const int *__restrict__ io, const int *__restrict__ ja,
+                          const int *__restrict__ dg, int upper, int *lev, int *ctr, int *err,
+                          int spin) {
+  if ((threadIdx.x & 31) != 0) return;
+  for (;;) {
+    const int t0 = atomicAdd(ctr, 32);
+    if (t0 >= n) break;
+    const int t1 = min(n, t0 + 32);
+    for (int t = t0; t < t1; ++t) {
+      const int i = upper ? n - 1 - t : t;
+      const int k0 = upper ? dg[i] + 1 : io[i];
+      const int k1 = upper ? io[i + 1] : dg[i];
+      int l = 0;
+      for (int k = k0; k < k1; ++k) {
+        const int j = ja[k];
+        int v;
+        int it = 0;
+        while (true) {
+          asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(lev + j) : "memory");
+          if (v >= 0) break;
+          if (++it > spin || *(volatile int *)err) {
+            atomicExch(err, 1);
+            v = 0;
+            break;
+          }
+          if (it > 16) __nanosleep(64);
+        }
+        l = max(l, v + 1);
+      }
+      asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(lev + i), "r"(l) : "memory");
+    }
+  }
+}
+
+// A device array owned by the bound mesh.
+template <class T>
+T *bound_alloc(fcg_context *c, size_t count) {
+  c->bound_allocs.emplace_back();
+  DBuf &b = c->bound_allocs.back();
+  if (b.ensure(count * sizeof(T)) != cudaSuccess) return nullptr;
+  return (T *)b.p;
+}
+
+template <class T>
+int bound_upload(fcg_context *c, const std::vector<T> &h, const T **out) {
+  T *d = bound_alloc<T>(c, h.size());
+  if (!d) return set_error(c, FCG_ERR_NOMEM, "device allocation for the mesh topology failed");
+  if (!h.empty())
+    FCG_CUDA_TRY(c, cudaMemcpyAsync(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice,
+                                    c->stream));
+  *out = d;
+  return FCG_OK;
+}
+
+// rows grouped by level, ascending inside a level (a counting sort)
+void group_levels(const std::vector<int> &lev, std::vector<int> &ptr, std::vector<int> &rows) {
+  int nlev = 0;
+  for (int l : lev) nlev = std::max(nlev, l + 1);
+  ptr.assign(nlev + 1, 0);
+  for (int l : lev) ptr[l + 1]++;
+  for (int l = 0; l < nlev; ++l) ptr[l + 1] += ptr[l];
+  rows.assign(lev.size(), 0);
+  std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+  for (size_t i = 0; i < lev.size(); ++i) rows[fill[lev[i]]++] = (int)i;
+}
+
+std::vector<int> padded_levels(const std::vector<int> &ptr, const std::vector<int> &rows) {
+  std::vector<int> out;
+  out.reserve(rows.size() + 32 * ptr.size());
+  for (size_t l = 0; l + 1 < ptr.size(); ++l) {
+    out.insert(out.end(), rows.begin() + ptr[l], rows.begin() + ptr[l + 1]);
+    while (out.size() % 32) out.push_back(-1);
+  }
+  return out;
+}
+
+}  // namespace
+
+namespace fcg {
+
+int to_zero_based(fcg_context *c, int *a, long long n) {
+  if (n <= 0) return FCG_OK;
+  k_minus1<<<grid_for(n, c->num_sms), kTPB, 0, c->stream>>>(n, a);
+  FCG_CHECK_LAUNCH(c, "to_zero_based");
+  return FCG_OK;
+}
+
+int bind_topology_device(fcg_context *c, const int *own0, const int *nei0,
+                         const std::vector<int> &own_host, const int cnt[B_NTYPES],
+                         const int fst[B_NTYPES], const int bst[B_NTYPES], std::string &err) {
+  const int n = c->n, nf = c->nf, nin = c->nin;
+  const long long nnz = (long long)n + 2LL * nin;
+  MeshView &v = c->mv;
+  SellView &sv = c->sv;
+  int rc;
+  // --- CSR, 0-based, owned by the mesh -----------------------------------------------
+  int *io = bound_alloc<int>(c, (size_t)n + 1), *ja = bound_alloc<int>(c, (size_t)nnz),
+      *dg = bound_alloc<int>(c, n), *spn = bound_alloc<int>(c, std::max(nin, 1)),
+      *snp = bound_alloc<int>(c, std::max(nin, 1));
+  if (!io || !ja || !dg || !spn || !snp)
+    return set_error(c, FCG_ERR_NOMEM, "device allocation for the mesh topology failed");
+  Tmp work, scan;
+  FCG_CUDA_TRY(c, work.b.ensure(sizeof(int) * (4 + 2 * (size_t)n)));
+  int *flag = work.b.as<int>(), *cntr = flag + 4, *cursor = cntr + n;
+  FCG_CUDA_TRY(c, cudaMemsetAsync(flag, 0, sizeof(int), c->stream));
+  const int G = grid_for(n, c->num_sms);
+  k_fill_int<<<G, kTPB, 0, c->stream>>>(cntr, n, 1);
+  if (nin > 0)
+    k_csr_count<<<grid_for(nin, c->num_sms), kTPB, 0, c->stream>>>(nin, own0, nei0, 0, cntr);
+  if ((rc = scan_exclusive(c, cntr, io, n, scan))) return rc;
+  k_csr_fill_diag<<<G, kTPB, 0, c->stream>>>(n, io, ja, cursor);
+  if (nin > 0)
+    k_csr_fill_faces<<<grid_for(nin, c->num_sms), kTPB, 0, c->stream>>>(nin, own0, nei0, 0, io,
+                                                                         cursor, ja);
+  k_csr_sort<<<G, kTPB, 0, c->stream>>>(n, io, ja, dg, flag);
+  if (nin > 0)
+    k_csr_slots<<<grid_for(nin, c->num_sms), kTPB, 0, c->stream>>>(nin, own0, nei0, 0, io, ja,
+                                                                    spn, snp);
+  k_minus1<<<grid_for(nnz, c->num_sms), kTPB, 0, c->stream>>>(nnz, ja);
+  k_minus1<<<G, kTPB, 0, c->stream>>>(n, dg);
+  if (nin > 0) {
+    k_minus1<<<grid_for(nin, c->num_sms), kTPB, 0, c->stream>>>(nin, spn);
+    k_minus1<<<grid_for(nin, c->num_sms), kTPB, 0, c->stream>>>(nin, snp);
+  }
+  FCG_CHECK_LAUNCH(c, "device CSR");
+  int hflag = 0;
+  if ((rc = read_flag(c, flag, &hflag))) return rc;
+  if (hflag) {
+    err = flag_text(hflag);
+    return FCG_ERR_INDEX;
+  }
+  c->nnz = nnz;
+  v.ioffset = io;
+  v.ja = ja;
+  v.diag = dg;
+  v.slot_pn = spn;
+  v.slot_np = snp;
+
+  // --- transpose positions and incidence lists ---------------------------------------
+  const long long ncf = nnz - n;
+  int *tpos = bound_alloc<int>(c, (size_t)nnz), *cfp = bound_alloc<int>(c, (size_t)n + 1),
+      *cfe = bound_alloc<int>(c, std::max<long long>(ncf, 1)),
+      *cfs = bound_alloc<int>(c, std::max<long long>(ncf, 1));
+  if (!tpos || !cfp || !cfe || !cfs)
+    return set_error(c, FCG_ERR_NOMEM, "device allocation for the mesh topology failed");
+  {
+    Tmp fa;
+    FCG_CUDA_TRY(c, fa.b.ensure(sizeof(int) * (size_t)nnz));
+    k_tpos0<<<G, kTPB, 0, c->stream>>>(n, io, ja, tpos);
+    k_cf_ptr0<<<grid_for(n + 1, c->num_sms), kTPB, 0, c->stream>>>(n, io, cfp);
+    if (nin > 0)
+      k_face_at0<<<grid_for(nin, c->num_sms), kTPB, 0, c->stream>>>(nin, spn, snp,
+                                                                    fa.b.as<int>());
+    k_cf_lists0<<<G, kTPB, 0, c->stream>>>(n, io, dg, own0, fa.b.as<int>(), cfe, cfs);
+    FCG_CHECK_LAUNCH(c, "incidence lists");
+    FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  }
+  c->tpos = tpos;
+  v.cf_ptr = cfp;
+  v.cf_ent = cfe;
+  v.cf_slot = cfs;
+
+  // --- boundary lists (host) ------------------------------------------------------------
+  {
+    std::vector<int> cb_ptr(n + 1, 0);
+    for (int ty = 0; ty < B_NTYPES; ++ty)
+      for (int i = 0; i < cnt[ty]; ++i) cb_ptr[own_host[fst[ty] + i]]++;
+    for (int i = 0; i < n; ++i) cb_ptr[i + 1] += cb_ptr[i];
+    std::vector<int> cb_face(cb_ptr[n]), cb_slot(cb_ptr[n]), cb_type(cb_ptr[n]);
+    std::vector<int> fill(cb_ptr.begin(), cb_ptr.end() - 1);
+    for (int ty = 0; ty < B_NTYPES; ++ty)
+      for (int i = 0; i < cnt[ty]; ++i) {
+        const int face = fst[ty] + i, e = fill[own_host[face] - 1]++;
+        cb_face[e] = face;
+        cb_slot[e] = bst[ty] + i;
+        cb_type[e] = ty;
+      }
+    std::vector<int> cbf_ptr(n + 1, 0);
+    for (int f = nin; f < nf; ++f) cbf_ptr[own_host[f]]++;
+    for (int i = 0; i < n; ++i) cbf_ptr[i + 1] += cbf_ptr[i];
+    std::vector<int> cbf_face(cbf_ptr[n]);
+    std::vector<int> fill2(cbf_ptr.begin(), cbf_ptr.end() - 1);
+    for (int f = nin; f < nf; ++f) cbf_face[fill2[own_host[f] - 1]++] = f;
+    if ((rc = bound_upload(c, cb_ptr, &v.cb_ptr)) || (rc = bound_upload(c, cb_face, &v.cb_face)) ||
+        (rc = bound_upload(c, cb_slot, &v.cb_slot)) || (rc = bound_upload(c, cb_type, &v.cb_type)) ||
+        (rc = bound_upload(c, cbf_ptr, &v.cbf_ptr)) || (rc = bound_upload(c, cbf_face, &v.cbf_face)))
+      return rc;
+    c->topo.clear();
+    auto rec = [&](const void *p, size_t bytes) { c->topo.emplace_back(p, bytes); };
+    rec(io, sizeof(int) * (n + 1));
+    rec(ja, sizeof(int) * nnz);
+    rec(dg, sizeof(int) * n);
+    rec(spn, sizeof(int) * nin);
+    rec(snp, sizeof(int) * nin);
+    rec(tpos, sizeof(int) * nnz);
+    rec(cfp, sizeof(int) * (n + 1));
+    rec(cfe, sizeof(int) * ncf);
+    rec(cfs, sizeof(int) * ncf);
+    rec(v.cb_ptr, sizeof(int) * cb_ptr.size());
+    rec(v.cb_face, sizeof(int) * cb_face.size());
+    rec(v.cb_slot, sizeof(int) * cb_slot.size());
+    rec(v.cb_type, sizeof(int) * cb_type.size());
+    rec(v.cbf_ptr, sizeof(int) * cbf_ptr.size());
+    rec(v.cbf_face, sizeof(int) * cbf_face.size());
+  }
+
+  // --- sliced ELL ---------------------------------------------------------------------
+  const int ns = (n + 31) / 32;
+  int maxrow = 0;
+  {
+    Tmp mr;
+    FCG_CUDA_TRY(c, mr.b.ensure(sizeof(int)));
+    FCG_CUDA_TRY(c, cudaMemsetAsync(mr.b.p, 0, sizeof(int), c->stream));
+    k_maxrow<<<G, kTPB, 0, c->stream>>>(n, io, mr.b.as<int>());
+    FCG_CUDA_TRY(c, cudaMemcpyAsync(&maxrow, mr.b.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  }
+  const int ucap = std::max(1, (3 * maxrow + 1) / 2);
+  Tmp shape;
+  FCG_CUDA_TRY(c, shape.b.ensure(sizeof(int) * (2 * (size_t)ns + (size_t)ns * ucap)));
+  int *dw = shape.b.as<int>(), *dk = dw + ns, *du = dk + ns;
+  k_sell_shape0<<<grid_for(32LL * ns, c->num_sms), kTPB, 0, c->stream>>>(n, ns, io, ja, ucap, dw, dk,
+                                                                         du);
+  FCG_CHECK_LAUNCH(c, "k_sell_shape0");
+  std::vector<int> width(ns), kind(ns);
+  FCG_CUDA_TRY(c, cudaMemcpyAsync(width.data(), dw, sizeof(int) * ns, cudaMemcpyDeviceToHost, c->stream));
+  FCG_CUDA_TRY(c, cudaMemcpyAsync(kind.data(), dk, sizeof(int) * ns, cudaMemcpyDeviceToHost, c->stream));
+  FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  std::vector<long long> ptr(ns + 1, 0), colp(ns + 1, 0);
+  std::vector<int> offp(ns + 1, 0);
+  int maxw = 0;
+  long long nuni = 0;
+  for (int sl = 0; sl < ns; ++sl) {
+    const int w = width[sl];
+    maxw = std::max(maxw, w);
+    ptr[sl + 1] = ptr[sl] + 32LL * w;
+    offp[sl + 1] = offp[sl] + (kind[sl] == 0 ? w : 0);
+    colp[sl + 1] = colp[sl] + (kind[sl] == 1 ? 32LL * w : 0);
+    nuni += kind[sl] == 0;
+  }
+  const long long noff = (long long)offp[ns] + colp[ns];
+  if (noff > INT_MAX) {
+    err = "the sliced ELL column blocks do not fit 32-bit offsets";
+    return FCG_ERR_ARG;
+  }
+  for (int sl = 0; sl < ns; ++sl)
+    if (kind[sl] == 1) offp[sl] = (int)(offp[ns] + colp[sl]);
+  const long long len = ptr[ns];
+  if ((rc = bound_upload(c, ptr, &sv.ptr)) || (rc = bound_upload(c, width, &sv.width)) ||
+      (rc = bound_upload(c, kind, &sv.kind)) || (rc = bound_upload(c, offp, &sv.offp)))
+    return rc;
+  int *off = bound_alloc<int>(c, std::max<long long>(noff, 1)),
+      *src = bound_alloc<int>(c, std::max<long long>(len, 1));
+  if (!off || !src) return set_error(c, FCG_ERR_NOMEM, "device allocation for the sliced ELL failed");
+  k_sell_fill0<<<grid_for(32LL * ns, c->num_sms), kTPB, 0, c->stream>>>(
+      n, ns, io, ja, ucap, du, sv.width, sv.kind, sv.ptr, sv.offp, off, src);
+  FCG_CHECK_LAUNCH(c, "k_sell_fill0");
+  sv.nslices = ns;
+  sv.off = off;
+  sv.src = src;
+  c->sell_maxw = maxw;
+  c->sell_len = len;
+  c->sell_nuniform = nuni;
+  auto rec = [&](const void *p, size_t bytes) { c->topo.emplace_back(p, bytes); };
+  rec(sv.ptr, sizeof(long long) * (ns + 1));
+  rec(sv.width, sizeof(int) * ns);
+  rec(sv.kind, sizeof(int) * ns);
+  rec(sv.offp, sizeof(int) * (ns + 1));
+  rec(off, sizeof(int) * noff);
+  rec(src, sizeof(int) * len);
+
+  // --- level schedules ------------------------------------------------------------------
+  {
+    Tmp lw;
+    FCG_CUDA_TRY(c, lw.b.ensure(sizeof(int) * ((size_t)n + 4)));
+    int *lev = lw.b.as<int>(), *ctl = lev + n;
+    std::vector<int> hlev(n);
+    Level *lvs[2] = {&c->lf, &c->lb};
+    std::vector<int> rows[2], pads[2];
+    for (int upper = 0; upper < 2; ++upper) {
+      k_fill_int<<<G, kTPB, 0, c->stream>>>(lev, n, -1);
+      FCG_CUDA_TRY(c, cudaMemsetAsync(ctl, 0, 4 * sizeof(int), c->stream));
+      k_levels0<<<std::min(G, c->num_sms * 8), kTPB, 0, c->stream>>>(n, io, ja, dg, upper, lev, ctl,
+                                                                      ctl + 1, 1 << 22);
+      FCG_CHECK_LAUNCH(c, "k_levels0");
+      int herr = 0;
+      FCG_CUDA_TRY(c, cudaMemcpyAsync(hlev.data(), lev, sizeof(int) * n, cudaMemcpyDeviceToHost,
+                                      c->stream));
+      FCG_CUDA_TRY(c, cudaMemcpyAsync(&herr, ctl + 1, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+      FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+      if (herr) {
+        err = "a level wait gave up";
+        return FCG_ERR_TIMEOUT;
+      }
+      Level &L = *lvs[upper];
+      group_levels(hlev, L.ptr, rows[upper]);
+      L.count = (int)L.ptr.size() - 1;
+      pads[upper] = padded_levels(L.ptr, rows[upper]);
+      const int *d;
+      if ((rc = bound_upload(c, rows[upper], &d))) return rc;
+      L.rows = const_cast<int *>(d);
+      if ((rc = bound_upload(c, pads[upper], &d))) return rc;
+      L.pad = const_cast<int *>(d);
+      L.pad_len = (int)pads[upper].size();
+    }
+    rec(c->lf.rows, sizeof(int) * n);
+    rec(c->lb.rows, sizeof(int) * n);
+    rec(c->lf.pad, sizeof(int) * c->lf.pad_len);
+    rec(c->lb.pad, sizeof(int) * c->lb.pad_len);
+    FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  }
+  return FCG_OK;
+}
+
+}  // namespace fcg

@@ -131,6 +131,12 @@ class Context:
                     self._stream = s
                 return
 
+    def topology_digest(self) -> int:
+        """64-bit digest of every topology array bound to the device."""
+        d = C.c_ulonglong()
+        self._check(self.lib.fcg_topology_digest(self.h, C.byref(d)), "fcg_topology_digest")
+        return d.value
+
     def synchronize(self):
         self._check(self.lib.fcg_synchronize(self.h), "fcg_synchronize")
 

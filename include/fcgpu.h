@@ -96,6 +96,12 @@ int fcg_mesh_sizes(const fcg_context *ctx, int *numCells, int *numFaces, int *nu
 int fcg_create_csr(fcg_context *ctx, int *ioffset, int *ja, int *diag, int *slot_pn,
                    int *slot_np);
 
+/* A 64-bit FNV-1a digest over every topology array fcg_bind_mesh bound to the device
+ * (CSR, slot maps, transpose positions, incidence lists, sliced ELL copy, level
+ * schedules).  Two contexts on the same mesh agree exactly when their topologies do:
+ * the GPU construction (the default) against FCG_TOPOLOGY=host. */
+int fcg_topology_digest(fcg_context *ctx, unsigned long long *digest);
+
 /* Host-only form of the same construction (no context, no GPU): the CSR arrays of
  * create_CSR_matrix_from_mesh_data for an owner/neighbour list (sparse_matrix.f90:
  * 42-172), 1-based, with nnz = numCells + 2*numInnerFaces. */
