@@ -243,6 +243,57 @@ def test_errors_are_reported():
     assert e.value.status == _lib.FCG_ERR_INDEX
 
 
+def test_argument_errors_of_the_step_routines():
+    """The PISO, momentum and correction entry points refuse what the reference would
+    index out of range or read without a value, with the status and nothing written."""
+    import ctypes as C
+
+    from freecappuccino_gb300 import _lib
+    from tests.meshes import fixture_mesh
+
+    m = fixture_mesh("pitzdaily")
+    c = fcg.Context(m)
+    f = seeded_fields(m, seed=2)
+    n = m.numCells
+    a = np.zeros(m.nnz)
+    su = np.zeros(n)
+    for ref in (0, n + 1):
+        with pytest.raises(_lib.FcgError) as e:
+            c.set_reference_pressure(ref, f["p"], a, su)
+        assert e.value.status == _lib.FCG_ERR_INDEX
+    with pytest.raises(_lib.FcgError) as e:  # BDF reads the old velocities
+        c.piso_hbya(a, f["u"], f["v"], f["w"], f["apu"], f["apv"], f["apw"], f["den"],
+                    bdf=True, timestep=0.1)
+    assert e.value.status == _lib.FCG_ERR_ARG
+    # pitzDaily has inlet faces, so fmi is read
+    rc = c.lib.fcg_adjust_mass_flow(c.h, f["den"].ctypes.data, 1.0, None, f["u"].ctypes.data,
+                                    f["v"].ctypes.data, f["w"].ctypes.data,
+                                    np.zeros(m.counts["nout"]).ctypes.data, su.ctypes.data)
+    assert rc == _lib.FCG_ERR_ARG
+    keys = ("u", "v", "w", "p")
+    vis = np.full(m.numTotal, 1e-3)
+    flm = np.zeros(m.numInnerFaces)
+    prm = _lib.UvwParams(9, 0, 1.0, 1e-3, (C.c_double * 3)(1, 1, 1), (C.c_double * 3)(0, 0, 0),
+                         0, 0, 1.0, 0.0, 0, 0.0, 0, 0, 0.0, 1.0, 0.0, 0.0, 0.0, 0.0)
+    fl = _lib.UvwFields(*[f[k].ctypes.data for k in keys], vis.ctypes.data,
+                        f["den"].ctypes.data, None, None, None, None, None, None, None,
+                        f["dUdxi"].ctypes.data, f["dVdxi"].ctypes.data, f["dWdxi"].ctypes.data,
+                        f["dPdxi"].ctypes.data, flm.ctypes.data,
+                        np.zeros(m.counts["ninl"]).ctypes.data,
+                        np.zeros(m.counts["nout"]).ctypes.data)
+    out = [np.zeros(2 * n), np.zeros(3 * n), np.zeros(3 * n)]
+    rc = c.lib.fcg_calcuvw(c.h, C.byref(prm), C.byref(fl), a.ctypes.data,
+                           *[o.ctypes.data for o in out])
+    assert rc == _lib.FCG_ERR_ARG and "scheme" in c.lib.fcg_last_error(c.h).decode()
+    assert not any(o.any() for o in out)
+    # a context that has no mesh yet
+    h = C.c_void_p()
+    assert c.lib.fcg_create(C.byref(h), 0) == 0
+    assert c.lib.fcg_correct_velocity_piso(h, *([None] * 7)) == _lib.FCG_ERR_STATE
+    c.lib.fcg_destroy(h)
+    c.close()
+
+
 @pytest.mark.parametrize("name", ["hex12_u", "hex8", "cavity", "pitzdaily"])
 def test_mixed_dpcg_matches_fp64_solution(name):
     """FP32 sweeps + FP64 reliable updates: same stop test on the true residual, about
