@@ -9,8 +9,10 @@ the laplacian kernel and solved to the reference's stop test, L1-relative residu
 solver's copies, the whole Krylov loop, the final FP64 residual check).
 
 Metric: time to 1e-8 relative residual (seconds, lower is better) of the learned
-preconditioner's flexible CG (FP32 iteration, FP64 residual replacements, BF16 network),
-next to plain FP64 DPCG and mixed-precision DPCG on the same system (extra.comparisons).
+preconditioner's flexible CG (FP32 iteration, FP64 residual replacements, BF16 network
+followed by an aggregation coarse-grid correction), next to plain FP64 DPCG,
+mixed-precision DPCG, the same FCG with Jacobi sweeps in place of the network and the
+network without the correction, on the same system (extra.comparisons).
 The uneven batch of 24 pressure systems solved by the persistent batched DPCG is
 reported in extra.batched.
 
@@ -203,10 +205,22 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
-def learned_launches(stats):
+def learned_launches(stats, ml=None):
     """Kernels one learned FCG solve launches: init 1 + per iteration 9 (network) + 4 (FCG)
-    + 1 (loop close) + 2 per FP64 residual replacement + final check 1; matrix set-up 4."""
-    return 4 + 1 + 14 * stats["iters"] + 2 * stats["updates"] + 1
+    + 1 (loop close) + 2 per FP64 residual replacement + final check 1; matrix set-up 4.
+    With the coarse-grid correction (ml: levels counting the fine one, sweeps, dense
+    coarsest): per solve one Galerkin launch per coarse level and the dense inverse; per
+    iteration the fine residual, restriction and prolongation, per inner level the
+    pre-sweeps, residual, restriction, prolongation and post-sweeps, the coarsest solve,
+    and the dot products the network's output kernel no longer does."""
+    base = 4 + 1 + 14 * stats["iters"] + 2 * stats["updates"] + 1
+    if not ml or len(ml["cells"]) < 2:
+        return base
+    L, nu = len(ml["cells"]), ml["sweeps"]
+    coarse = L - 1
+    last = 1 if ml["dense"] else 2 * nu + 2
+    per_it = 3 + (2 * nu + 3) * (coarse - 1) + last + 1
+    return base + coarse + (1 if ml["dense"] else 0) + per_it * stats["iters"]
 
 
 def batch_workload(seed, count=24, sizes=(32, 48, 64, 96, 128)):
@@ -544,12 +558,19 @@ def main():
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
            for _ in range(args.steps)]
     reports, launches = [], 0
+    ml = None
+    if method == "learned" and lp.multilevel["enabled"]:
+        opts = lp.multilevel
+        h = lp.hierarchy(ctx)
+        ml = {"cells": h["cells"], "entries": h["entries"], "sweeps": opts["sweeps"],
+              "dense": h["cells"][-1] <= opts["dense_max"], "options": opts,
+              "host_setup_s": h["setup_seconds"]}
     for e0, e1 in evs:
         e0.record(stream)
         reports.append(run(method))
         e1.record(stream)
         if method == "learned":
-            launches += learned_launches(lp.last_solve_stats())
+            launches += learned_launches(lp.last_solve_stats(), ml)
     torch.cuda.synchronize()
     barrier(ws)
     clocks = sampler.stop()
@@ -613,6 +634,21 @@ def main():
         comparisons[other] = {"seconds": t_o, "sweeps": r_o.iters, "l2_rel": r_o.l2_rel,
                               "headline_speedup": t_o / t_solve,
                               "max_rel_diff_of_headline_solution": err}
+    if method == "learned" and ml:
+        # the same flexible CG without the network (Jacobi sweeps in its place) and the
+        # network without the coarse-grid correction; one timed solve each
+        for name, opt in (("fcg_coarse_jacobi_no_network", {"smoother": "jacobi"}),
+                          ("fcg_network_no_coarse", {"enabled": False})):
+            lp.set_multilevel(**opt)
+            if name == "fcg_coarse_jacobi_no_network":
+                run("learned")
+            r_o, t_o = timed("learned")
+            err = float((x_method - r_o.fi).abs().max() / r_o.fi.abs().max())
+            comparisons[name] = {"seconds": t_o, "fcg_iterations": r_o.fcg_iters,
+                                 "fallback": r_o.fallback, "l2_rel": r_o.l2_rel,
+                                 "headline_speedup": t_o / t_solve,
+                                 "max_rel_diff_of_headline_solution": err}
+            lp.set_multilevel(**ml["options"])
     dpcg_sweeps = comparisons.get("dpcg", {}).get("sweeps", iters)
 
     # Standalone FP64 SpMV (one event pair per launch: host gaps are not counted).
@@ -682,7 +718,8 @@ def main():
         if method == "learned":
             extra["learned"] = {"fcg_iterations": last.fcg_iters, "fallback": last.fallback,
                                 "directions": 8, "weights": os.path.relpath(
-                                    args.weights or DEFAULT_WEIGHTS, ROOT)}
+                                    args.weights or DEFAULT_WEIGHTS, ROOT),
+                                "coarse_correction": ml}
         line = {"metric": METRIC, "value": t_solve, "unit": "s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_solve * 1e3, "higher_is_better": False,
                 "scaling": "weak", "vs_baseline": None, "dtype": dtype,

@@ -84,6 +84,16 @@ class UvwFields(C.Structure):
     _fields_ = [(k, _vp) for k in UVW_FIELDS]
 
 
+class Multilevel(C.Structure):
+    """fcg_lp_multilevel: options of the learned FCG's coarse-grid correction."""
+    _fields_ = [("enabled", C.c_int), ("smoother", C.c_int), ("sweeps", C.c_int),
+                ("max_levels", C.c_int), ("dense_max", C.c_int), ("alpha", C.c_double),
+                ("omega", C.c_double)]
+
+
+SMOOTH_NETWORK, SMOOTH_JACOBI, MAX_LEVELS = 0, 1, 16
+
+
 class SolveReport(C.Structure):
     _fields_ = [("res0", C.c_double), ("resl", C.c_double), ("iters", C.c_int),
                 ("converged", C.c_int), ("l2_rel", C.c_double), ("seconds", C.c_double)]
@@ -174,6 +184,13 @@ _PROTOS = {
     "fcg_lp_last_solve_stats": (C.c_int, [_LP, _ip, _ip]),
     "fcg_lp_profile": (C.c_int, [_LP, _CTX, _vp, C.c_int, _dp, C.c_int, _ip]),
     "fcg_lp_set_fcg_options": (C.c_int, [_LP, C.c_int, C.c_int, C.c_int, C.c_double]),
+    "fcg_lp_set_multilevel": (C.c_int, [_LP, C.POINTER(Multilevel)]),
+    "fcg_lp_get_multilevel": (C.c_int, [_LP, C.POINTER(Multilevel)]),
+    "fcg_lp_hierarchy_info": (C.c_int, [_LP, _CTX, _ip, _ip, C.POINTER(C.c_longlong), _dp]),
+    "fcg_lp_hierarchy_level": (C.c_int, [_LP, _CTX, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "fcg_lp_precondition": (C.c_int, [_LP, _CTX, _vp, _vp]),
+    "fcg_lp_coarse_correct": (C.c_int, [_LP, _CTX, _vp, _vp, _vp]),
+    "fcg_aggregate": (C.c_int, [C.c_int, _vp, _vp, _vp, C.c_int, C.c_int, _vp, _ip]),
     "fcg_fcg_learned": (C.c_int, [_CTX, _LP, _vp, _vp, _vp, _vp, C.c_double, C.c_int, _dp,
                                   C.POINTER(SolveReport), _ip, _ip]),
     # synthetic inputs (include/fcgpu_meshgen.h)

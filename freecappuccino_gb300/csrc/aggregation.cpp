@@ -1,0 +1,196 @@
+// Aggregation hierarchy of the learned FCG's coarse-grid correction, built on the host
+// once per mesh from the first scaled matrix it is asked to solve.
+//
+// A level is formed by three passes of pairwise matching: each row, in ascending order,
+// pairs with its unmatched neighbour of most negative coupling (ties go to the lowest
+// column); a row left without one then joins the matched pair it is most negatively
+// coupled to, if any.  A coarse row so aggregates about eight rows of the level above.  Between passes the matrix is the Galerkin product P^T A P of the
+// piecewise-constant prolongation P, summed in a fixed order: member rows ascending,
+// and inside each member row the entries in column order, each added to the slot of its
+// coarse column in the order met.  Rows of the result are then sorted by column.  These
+// host values only steer the matching; the device recomputes every level's values from
+// the current matrix on each solve (coarse.cu).
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "coarse.h"
+
+namespace fcg {
+namespace ml {
+
+int pair_match(int n, const int *ptr, const int *col, const double *val, std::vector<int> &agg) {
+  agg.assign(n, -1);
+  std::vector<char> paired;
+  paired.reserve(n);
+  int nc = 0;
+  for (int i = 0; i < n; ++i) {
+    if (agg[i] >= 0) continue;
+    int best = -1;
+    double bv = 0.0;
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+      const int j = col[k];
+      if (j == i || agg[j] >= 0) continue;
+      if (val[k] < bv) {
+        bv = val[k];
+        best = j;
+      }
+    }
+    agg[i] = nc;
+    if (best >= 0) agg[best] = nc;
+    paired.push_back(best >= 0);
+    ++nc;
+  }
+  // a row left single joins the pair it is most strongly coupled to (pairs as matched,
+  // so joins do not chain); the aggregates are then renumbered in their order
+  bool moved = false;
+  for (int i = 0; i < n; ++i) {
+    if (paired[agg[i]]) continue;
+    int best = -1;
+    double bv = 0.0;
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+      const int j = col[k];
+      if (j == i || !paired[agg[j]]) continue;
+      if (val[k] < bv) {
+        bv = val[k];
+        best = j;
+      }
+    }
+    if (best >= 0) {
+      agg[i] = agg[best];
+      moved = true;
+    }
+  }
+  if (!moved) return nc;
+  std::vector<int> used(nc, 0);
+  for (int i = 0; i < n; ++i) used[agg[i]] = 1;
+  std::vector<int> id(nc, -1);
+  int m = 0;
+  for (int I = 0; I < nc; ++I)
+    if (used[I]) id[I] = m++;
+  for (int i = 0; i < n; ++i) agg[i] = id[agg[i]];
+  return m;
+}
+
+void members(int n, int nc, const std::vector<int> &agg, std::vector<int> &mptr,
+             std::vector<int> &mem) {
+  mptr.assign(nc + 1, 0);
+  for (int i = 0; i < n; ++i) ++mptr[agg[i] + 1];
+  for (int I = 0; I < nc; ++I) mptr[I + 1] += mptr[I];
+  mem.assign(n, 0);
+  std::vector<int> fill(mptr.begin(), mptr.end() - 1);
+  for (int i = 0; i < n; ++i) mem[fill[agg[i]]++] = i;
+}
+
+void galerkin(const HostCsr &A, const std::vector<int> &agg, int nc, const std::vector<int> &mptr,
+              const std::vector<int> &mem, HostCsr &out) {
+  out.n = nc;
+  out.ptr.assign(nc + 1, 0);
+  out.col.clear();
+  out.val.clear();
+  out.col.reserve(A.col.size() / 2 + nc);
+  out.val.reserve(A.col.size() / 2 + nc);
+  std::vector<int> marker(nc, -1);
+  std::vector<std::pair<int, double>> row;
+  for (int I = 0; I < nc; ++I) {
+    const int start = (int)out.col.size();
+    for (int m = mptr[I]; m < mptr[I + 1]; ++m) {
+      const int i = mem[m];
+      for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
+        const int J = agg[A.col[k]];
+        const int p = marker[J];
+        if (p >= start) {
+          out.val[p] += A.val[k];
+        } else {
+          marker[J] = (int)out.col.size();
+          out.col.push_back(J);
+          out.val.push_back(A.val[k]);
+        }
+      }
+    }
+    const int end = (int)out.col.size();
+    row.clear();
+    for (int p = start; p < end; ++p) row.emplace_back(out.col[p], out.val[p]);
+    std::sort(row.begin(), row.end(),
+              [](const std::pair<int, double> &a, const std::pair<int, double> &b) {
+                return a.first < b.first;
+              });
+    for (int p = start; p < end; ++p) {
+      out.col[p] = row[p - start].first;
+      out.val[p] = row[p - start].second;
+    }
+    out.ptr[I + 1] = end;
+  }
+}
+
+int build_levels(const HostCsr &fine, int max_levels, int dense_max, int passes,
+                 std::vector<HostLevel> &levels) {
+  levels.clear();
+  levels.reserve(max_levels);
+  const HostCsr *cur = &fine;
+  HostCsr work[2];
+  int wi = 0;
+  while ((int)levels.size() + 1 < max_levels) {
+    const int n0 = cur->n;
+    if (n0 < 2) break;
+    HostLevel lv;
+    std::vector<int> comp(n0);
+    for (int i = 0; i < n0; ++i) comp[i] = i;
+    const HostCsr *a = cur;
+    int nc = n0;
+    for (int p = 0; p < passes; ++p) {
+      std::vector<int> agg, mptr, mem;
+      const int m = pair_match(a->n, a->ptr.data(), a->col.data(), a->val.data(), agg);
+      if (m == a->n) break;  // no pair formed: this matrix does not coarsen
+      members(a->n, m, agg, mptr, mem);
+      HostCsr &dst = work[wi];
+      wi ^= 1;
+      galerkin(*a, agg, m, mptr, mem, dst);
+      for (int i = 0; i < n0; ++i) comp[i] = agg[comp[i]];
+      a = &dst;
+      nc = m;
+      if (nc <= dense_max) break;
+    }
+    if (nc == n0 || 10LL * nc > 9LL * n0) break;  // less than 10% fewer rows: stop
+    lv.n = nc;
+    lv.agg = std::move(comp);
+    members(n0, nc, lv.agg, lv.mptr, lv.mem);
+    lv.A = *a;  // pattern (and host values) of the level
+    levels.push_back(std::move(lv));
+    cur = &levels.back().A;
+    if (nc <= dense_max) break;
+  }
+  return (int)levels.size();
+}
+
+}  // namespace ml
+}  // namespace fcg
+
+// Host utility: the aggregation of one level (`passes` matching passes on a 0-based CSR
+// with ascending columns, stopping once at most dense_max aggregates remain).
+extern "C" int fcg_aggregate(int n, const int *ptr, const int *col, const double *val,
+                             int passes, int dense_max, int *agg, int *nc) {
+  if (n < 0 || !ptr || !agg || !nc || passes < 1 || (n > 0 && (!col || !val)))
+    return FCG_ERR_ARG;
+  if (ptr[0] != 0) return FCG_ERR_INDEX;
+  for (int i = 0; i < n; ++i) {
+    if (ptr[i + 1] < ptr[i]) return FCG_ERR_INDEX;
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k)
+      if (col[k] < 0 || col[k] >= n || (k > ptr[i] && col[k] <= col[k - 1])) return FCG_ERR_INDEX;
+  }
+  fcg::ml::HostCsr a;
+  a.n = n;
+  a.ptr.assign(ptr, ptr + n + 1);
+  a.col.assign(col, col + ptr[n]);
+  a.val.assign(val, val + ptr[n]);
+  std::vector<fcg::ml::HostLevel> lv;
+  fcg::ml::build_levels(a, 2, dense_max, passes, lv);
+  if (lv.empty()) {
+    for (int i = 0; i < n; ++i) agg[i] = i;
+    *nc = n;
+  } else {
+    for (int i = 0; i < n; ++i) agg[i] = lv[0].agg[i];
+    *nc = lv[0].n;
+  }
+  return FCG_OK;
+}

@@ -1,0 +1,561 @@
+// Coarse-grid correction of the learned FCG (a two-level-and-below V-cycle over the
+// aggregation hierarchy of aggregation.cpp), device side.
+//
+// The flexible CG of learned.cu preconditions with z = N(r), the network, and then
+//   z += alpha P V(P^T (r - Ahat z)),
+// where P is the piecewise-constant prolongation of the first aggregation level and V
+// a V-cycle on the levels below: `sweeps` damped Jacobi sweeps before and after each
+// level's own correction, over-corrected by alpha, and a dense inverse at the coarsest
+// level.  Everything runs in FP32 on the Jacobi-scaled matrix Ahat = D^-1/2 A D^-1/2.
+// The level matrices are Galerkin products P^T A P recomputed from the current matrix on
+// every solve: one warp per coarse row, one lane per coarse entry, adding the member
+// rows' entries in a fixed order (members ascending, entries in column order), in FP32
+// (the cycle's precision; FP64 adds would run at GB300's low FP64 rate).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <vector>
+
+#include "coarse.h"
+#include "krylov_common.cuh"
+#include "launch.h"
+
+namespace fcg {
+namespace ml {
+namespace {
+
+constexpr int kDenseThreads = 1024;
+constexpr int kDenseMaxRows = 160;  // 2 n^2 floats fit the shared memory of a block
+
+__device__ __forceinline__ bool stopped(const int *done) { return done && __ldcg(done); }
+
+// Values a of the coarse rows from the parent matrix (pptr, pcol, pval), summed in FP32
+// in the fixed order; dinv = 1 / diagonal (0 if not positive).
+__global__ void __launch_bounds__(kTPB)
+    k_ml_galerkin(int nc, const int *__restrict__ cptr, const int *__restrict__ ccol,
+                  const int *__restrict__ mptr, const int *__restrict__ mem,
+                  const int *__restrict__ pptr, const int *__restrict__ pcol,
+                  const float *__restrict__ pval, const int *__restrict__ agg,
+                  float *__restrict__ a, float *__restrict__ dinv) {
+  const int lane = threadIdx.x & 31;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long I = warp; I < nc; I += nwarps) {
+    const int cb = cptr[I], ce = cptr[I + 1];
+    const int mb = mptr[I], me = mptr[I + 1];
+    for (int sb = cb; sb < ce; sb += 32) {
+      const int my = sb + lane;
+      const int mycol = my < ce ? ccol[my] : -1;
+      float acc = 0.f;
+      for (int m = mb; m < me; ++m) {
+        const int i = mem[m];
+        const int kb0 = pptr[i], ke = pptr[i + 1];
+        for (int kb = kb0; kb < ke; kb += 32) {
+          const int k = kb + lane;
+          int J = -1;
+          float v = 0.f;
+          if (k < ke) {
+            v = pval[k];
+            J = agg[pcol[k]];
+          }
+          const int cnt = min(32, ke - kb);
+          for (int e = 0; e < cnt; ++e) {
+            const int Je = __shfl_sync(0xffffffffu, J, e);
+            const float ve = __shfl_sync(0xffffffffu, v, e);
+            if (Je == mycol) acc = __fadd_rn(acc, ve);
+          }
+        }
+      }
+      if (my < ce) {
+        a[my] = acc;
+        if (mycol == (int)I) dinv[I] = acc > 0.f ? 1.f / acc : 0.f;
+      }
+    }
+  }
+}
+
+// Level 1 from the fine matrix in the context's sliced layout (the FP32 scaled values
+// Ahat `val`, slot -> CSR position `src`, pads skipped).  A row's slots hold its entries
+// in column order, so the sums run in the order of k_ml_galerkin.
+// When every member row has at most 8 slots, four member rows are loaded per round
+// (lanes 8g..8g+7 hold member g's slots) and the lanes of the coarse entries then scan
+// the 32 loaded entries in lane order -- member by member, slot by slot: the same order.
+__device__ __forceinline__ void g0_entry(const SellView &sv, int n, const float *val,
+                                         const int *agg, int i, int j, int &J, float &v) {
+  J = -1;
+  v = 0.f;
+  const int slice = i >> 5, rl = i & 31;
+  const int w = sv.width[slice];
+  if (j >= w) return;
+  const long long pos = sv.ptr[slice] + rl + 32LL * j;
+  if (sv.src[pos] < 0) return;
+  const int op = sv.offp[slice];
+  int c = sv.kind[slice] == 0 ? i + sv.off[op + j] : sv.off[op + 32 * j + rl];
+  c = c < 0 ? 0 : (c >= n ? n - 1 : c);
+  v = val[pos];
+  J = agg[c];
+}
+
+__global__ void __launch_bounds__(kTPB)
+    k_ml_galerkin0(int nc, const int *__restrict__ cptr, const int *__restrict__ ccol,
+                   const int *__restrict__ mptr, const int *__restrict__ mem, SellView sv, int n,
+                   const float *__restrict__ val, const int *__restrict__ agg,
+                   float *__restrict__ a, float *__restrict__ dinv) {
+  const int lane = threadIdx.x & 31;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long I = warp; I < nc; I += nwarps) {
+    const int cb = cptr[I], ce = cptr[I + 1];
+    const int mb = mptr[I], me = mptr[I + 1];
+    int wide = 0;  // a member row wider than 8 slots
+    for (int m = mb + lane; m < me; m += 32) wide |= sv.width[mem[m] >> 5] > 8;
+    const bool grouped = !__any_sync(0xffffffffu, wide);
+    for (int sb = cb; sb < ce; sb += 32) {
+      const int my = sb + lane;
+      const int mycol = my < ce ? ccol[my] : -1;
+      float acc = 0.f;
+      if (grouped) {
+        const int g = lane >> 3, j = lane & 7;
+        for (int m0 = mb; m0 < me; m0 += 4) {
+          int J = -1;
+          float v = 0.f;
+          if (m0 + g < me) g0_entry(sv, n, val, agg, mem[m0 + g], j, J, v);
+          const int cnt = min(4, me - m0) * 8;
+          for (int e = 0; e < cnt; ++e) {
+            const int Je = __shfl_sync(0xffffffffu, J, e);
+            const float ve = __shfl_sync(0xffffffffu, v, e);
+            if (Je == mycol) acc = __fadd_rn(acc, ve);
+          }
+        }
+      } else {
+        for (int m = mb; m < me; ++m) {
+          const int i = mem[m];
+          const int w = sv.width[i >> 5];
+          for (int jb = 0; jb < w; jb += 32) {
+            int J;
+            float v;
+            g0_entry(sv, n, val, agg, i, jb + lane, J, v);
+            const int cnt = min(32, w - jb);
+            for (int e = 0; e < cnt; ++e) {
+              const int Je = __shfl_sync(0xffffffffu, J, e);
+              const float ve = __shfl_sync(0xffffffffu, v, e);
+              if (Je == mycol) acc = __fadd_rn(acc, ve);
+            }
+          }
+        }
+      }
+      if (my < ce) {
+        a[my] = acc;
+        if (mycol == (int)I) dinv[I] = acc > 0.f ? 1.f / acc : 0.f;
+      }
+    }
+  }
+}
+
+// Gauss-Jordan inverse of the (small, symmetric positive definite) coarsest matrix in
+// FP32, one block, the matrix and its inverse in shared memory (2 n^2 floats).  M
+// receives the inverse, row-major.  A pivot below 1e-5 of the largest diagonal entry
+// drops its row (a zero row and column of M), which keeps a singular coarsest matrix (no
+// Dirichlet boundary) from producing infinities.
+__global__ void __launch_bounds__(kDenseThreads)
+    k_ml_dense_inv(int n, const int *__restrict__ ptr, const int *__restrict__ col,
+                   const float *__restrict__ a, float *__restrict__ M) {
+  extern __shared__ float dsm[];
+  float *W = dsm, *V = dsm + n * n;
+  __shared__ float fcol[kDenseMaxRows];
+  __shared__ float pinv, tiny;
+  const int tid = threadIdx.x, bs = blockDim.x;
+  const int nn = n * n;
+  for (int i = tid; i < nn; i += bs) {
+    W[i] = 0.f;
+    V[i] = (i / n == i % n) ? 1.f : 0.f;
+  }
+  __syncthreads();
+  for (int r = tid; r < n; r += bs)
+    for (int k = ptr[r]; k < ptr[r + 1]; ++k) W[r * n + col[k]] = a[k];
+  __syncthreads();
+  if (tid == 0) {
+    float dmax = 0.f;
+    for (int r = 0; r < n; ++r) dmax = fmaxf(dmax, W[r * n + r]);
+    tiny = 1e-5f * dmax;
+  }
+  __syncthreads();
+  for (int p = 0; p < n; ++p) {
+    if (tid == 0) {
+      const float piv = W[p * n + p];
+      pinv = piv > tiny ? 1.f / piv : 0.f;
+    }
+    __syncthreads();
+    for (int c = tid; c < n; c += bs) {
+      W[p * n + c] *= pinv;
+      V[p * n + c] *= pinv;
+    }
+    for (int r = tid; r < n; r += bs) fcol[r] = (r == p) ? 0.f : W[r * n + p];
+    __syncthreads();
+    for (int i = tid; i < nn; i += bs) {
+      const int r = i / n, c = i - r * n;
+      const float f = fcol[r];
+      if (f != 0.f) {
+        W[i] -= f * W[p * n + c];
+        V[i] -= f * V[p * n + c];
+      }
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < nn; i += bs) M[i] = V[i];
+}
+
+// x = M b, one warp per row
+__global__ void __launch_bounds__(kTPB)
+    k_ml_dense_apply(int n, const float *__restrict__ M, const float *__restrict__ b,
+                     float *__restrict__ x, const int *done) {
+  if (stopped(done)) return;
+  const int lane = threadIdx.x & 31;
+  const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (r >= n) return;
+  float acc = 0.f;
+  for (int c = lane; c < n; c += 32) acc += M[(long long)r * n + c] * b[c];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) x[r] = acc;
+}
+
+// Row products of the coarse levels: four lanes per row (eight rows per warp), each
+// lane summing every fourth entry, then a shuffle sum.  Loops are warp-uniform.
+__device__ __forceinline__ float row4(const int *ptr, const int *col, const float *a,
+                                     const float *x, int row, int n, int q) {
+  float acc = 0.f;
+  if (row < n)
+    for (int k = ptr[row] + q; k < ptr[row + 1]; k += 4) acc += a[k] * x[col[k]];
+  acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+  acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+  return acc;
+}
+
+// y = x + omega dinv (b - A x); x == NULL stands for x = 0
+__global__ void __launch_bounds__(kTPB)
+    k_ml_jacobi(int n, const int *__restrict__ ptr, const int *__restrict__ col,
+                const float *__restrict__ a, const float *__restrict__ dinv,
+                const float *__restrict__ b, const float *__restrict__ x, float *__restrict__ y,
+                float omega, const int *done) {
+  if (stopped(done)) return;
+  const int lane = threadIdx.x & 31, q = lane & 3;
+  const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long base = w0 * 8; base < n; base += nw * 8) {
+    const int row = (int)base + (lane >> 2);
+    if (!x) {
+      if (q == 0 && row < n) y[row] = omega * dinv[row] * b[row];
+      continue;
+    }
+    const float ax = row4(ptr, col, a, x, row, n, q);
+    if (q == 0 && row < n) y[row] = x[row] + omega * dinv[row] * (b[row] - ax);
+  }
+}
+
+// t = b - A x
+__global__ void __launch_bounds__(kTPB)
+    k_ml_resid(int n, const int *__restrict__ ptr, const int *__restrict__ col,
+               const float *__restrict__ a, const float *__restrict__ b,
+               const float *__restrict__ x, float *__restrict__ t, const int *done) {
+  if (stopped(done)) return;
+  const int lane = threadIdx.x & 31, q = lane & 3;
+  const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long base = w0 * 8; base < n; base += nw * 8) {
+    const int row = (int)base + (lane >> 2);
+    const float ax = row4(ptr, col, a, x, row, n, q);
+    if (q == 0 && row < n) t[row] = b[row] - ax;
+  }
+}
+
+// bc[I] = sum over the member rows i of I of t_i
+__global__ void __launch_bounds__(kTPB)
+    k_ml_restrict(int nc, const int *__restrict__ mptr, const int *__restrict__ mem,
+                  const float *__restrict__ t, float *__restrict__ bc, const int *done) {
+  if (stopped(done)) return;
+  FCG_GRID_STRIDE(I, nc) {
+    float acc = 0.f;
+    for (int m = mptr[I]; m < mptr[I + 1]; ++m) acc += t[mem[m]];
+    bc[I] = acc;
+  }
+}
+
+// x_i += alpha xc[agg_i]
+__global__ void __launch_bounds__(kTPB)
+    k_ml_prolong(int n, const int *__restrict__ agg, const float *__restrict__ xc,
+                 float *__restrict__ x, float alpha, const int *done) {
+  if (stopped(done)) return;
+  FCG_GRID_STRIDE(i, n) x[i] += alpha * xc[agg[i]];
+}
+
+// fine level (sliced matrix, unit diagonal): t = r - Ahat z
+__global__ void __launch_bounds__(kTPB, 6)
+    k_ml_resid0(SellView s, int n, const float *__restrict__ val, const float *__restrict__ r,
+                const float *__restrict__ z, float *__restrict__ t, const int *done) {
+  if (stopped(done)) return;
+  FCG_SLICE_LOOP(slice, lane, s) {
+    const float az = sell_row(s, n, val, z, slice, lane);
+    const int row = slice * 32 + lane;
+    if (row < n) t[row] = r[row] - az;
+  }
+}
+
+// fine level Jacobi sweep: zout = zin + omega (r - Ahat zin); zin == NULL: zout = omega r
+__global__ void __launch_bounds__(kTPB, 6)
+    k_ml_jac0(SellView s, int n, const float *__restrict__ val, const float *__restrict__ r,
+              const float *__restrict__ zin, float *__restrict__ zout, float omega,
+              const int *done) {
+  if (stopped(done)) return;
+  FCG_SLICE_LOOP(slice, lane, s) {
+    const int row = slice * 32 + lane;
+    if (!zin) {
+      if (row < n) zout[row] = omega * r[row];
+      continue;
+    }
+    const float az = sell_row(s, n, val, zin, slice, lane);
+    if (row < n) zout[row] = zin[row] + omega * (r[row] - az);
+  }
+}
+
+__global__ void __launch_bounds__(kTPB)
+    k_ml_copy(int n, const float *__restrict__ a, float *__restrict__ b, const int *done) {
+  if (stopped(done)) return;
+  FCG_GRID_STRIDE(i, n) b[i] = a[i];
+}
+
+// One V-cycle on level k of H.lv for right-hand side lv[k].b; returns the vector holding
+// the result (lv[k].x or lv[k].y).
+float *enqueue_vcycle(Hierarchy &H, int num_sms, const Options &o, cudaStream_t st, int k,
+                      const int *done) {
+  DevLevel &L = H.lv[k];
+  const float om = (float)o.omega, al = (float)o.alpha;
+  const int g = grid_for(L.n, num_sms, 8);
+  const int g4 = grid_for(4LL * L.n, num_sms, 8);  // four lanes per row
+  const bool last = k + 1 == (int)H.lv.size();
+  if (last && H.has_dense) {
+    const int blocks = (L.n * 32 + kTPB - 1) / kTPB;
+    k_ml_dense_apply<<<blocks, kTPB, 0, st>>>(L.n, H.dense.as<float>(), L.b, L.x, done);
+    return L.x;
+  }
+  float *cur = L.x, *oth = L.y;
+  k_ml_jacobi<<<g4, kTPB, 0, st>>>(L.n, L.ptr, L.col, L.a32, L.dinv, L.b, nullptr, cur, om, done);
+  const int pre = last ? 2 * o.sweeps + 2 : o.sweeps;  // coarsest without a dense inverse
+  for (int s = 1; s < pre; ++s) {
+    k_ml_jacobi<<<g4, kTPB, 0, st>>>(L.n, L.ptr, L.col, L.a32, L.dinv, L.b, cur, oth, om, done);
+    std::swap(cur, oth);
+  }
+  if (last) return cur;
+  DevLevel &Lc = H.lv[k + 1];
+  k_ml_resid<<<g4, kTPB, 0, st>>>(L.n, L.ptr, L.col, L.a32, L.b, cur, oth, done);
+  k_ml_restrict<<<grid_for(Lc.n, num_sms, 8), kTPB, 0, st>>>(Lc.n, Lc.mptr, Lc.mem, oth, Lc.b,
+                                                            done);
+  const float *e = enqueue_vcycle(H, num_sms, o, st, k + 1, done);
+  k_ml_prolong<<<g, kTPB, 0, st>>>(L.n, Lc.agg, e, cur, al, done);
+  for (int s = 0; s < o.sweeps; ++s) {
+    k_ml_jacobi<<<g4, kTPB, 0, st>>>(L.n, L.ptr, L.col, L.a32, L.dinv, L.b, cur, oth, om, done);
+    std::swap(cur, oth);
+  }
+  return cur;
+}
+
+template <class T>
+T *carve(char *&p, size_t count) {
+  T *r = (T *)p;
+  p += ((count * sizeof(T) + 255) / 256) * 256;
+  return r;
+}
+
+size_t pad256(size_t b) { return ((b + 255) / 256) * 256; }
+
+}  // namespace
+
+void Hierarchy::release() {
+  for (auto &L : lv) {
+    L.ints.release();
+    L.vals.release();
+    L.vecs.release();
+  }
+  lv.clear();
+  dense.release();
+  fine_tmp.release();
+  has_dense = false;
+  uid = 0;
+}
+
+int build(Hierarchy &H, fcg_context *c, const Options &o, std::string &err) {
+  const auto t0 = std::chrono::steady_clock::now();
+  H.release();
+  const int n = c->n;
+  const long long nnz = c->nnz, len = c->sell_len;
+  HostCsr fine;
+  fine.n = n;
+  fine.ptr.resize(n + 1);
+  fine.col.resize(nnz);
+  fine.val.resize(nnz);
+  std::vector<double> s(n), sval(len);
+  std::vector<int> src(len);
+  cudaError_t e;
+  if ((e = cudaMemcpyAsync(fine.ptr.data(), c->mv.ioffset, sizeof(int) * (n + 1),
+                           cudaMemcpyDeviceToHost, c->stream)) ||
+      (e = cudaMemcpyAsync(fine.col.data(), c->mv.ja, sizeof(int) * nnz, cudaMemcpyDeviceToHost,
+                           c->stream)) ||
+      (e = cudaMemcpyAsync(sval.data(), sliced64(c), sizeof(double) * len, cudaMemcpyDeviceToHost,
+                           c->stream)) ||
+      (e = cudaMemcpyAsync(src.data(), c->sv.src, sizeof(int) * len, cudaMemcpyDeviceToHost,
+                           c->stream)) ||
+      (e = cudaMemcpyAsync(s.data(), scale64(c), sizeof(double) * n, cudaMemcpyDeviceToHost,
+                           c->stream)) ||
+      (e = cudaStreamSynchronize(c->stream))) {
+    err = std::string("hierarchy download: ") + cudaGetErrorString(e);
+    return FCG_ERR_CUDA;
+  }
+  for (long long p = 0; p < len; ++p)
+    if (src[p] >= 0) fine.val[src[p]] = sval[p];
+  sval = std::vector<double>();
+  src = std::vector<int>();
+  for (int i = 0; i < n; ++i)
+    for (int k = fine.ptr[i]; k < fine.ptr[i + 1]; ++k)
+      fine.val[k] = (fine.val[k] * s[i]) * s[fine.col[k]];
+  std::vector<HostLevel> hl;
+  const int dmax = std::min(std::max(o.dense_max, 1), kDenseMaxRows);
+  build_levels(fine, std::max(2, o.max_levels), dmax, H.passes, hl);
+  fine = HostCsr();
+  H.lv.resize(hl.size());
+  int np = n;  // rows of the parent level
+  for (size_t l = 0; l < hl.size(); ++l) {
+    const HostLevel &h = hl[l];
+    DevLevel &L = H.lv[l];
+    L.n = h.n;
+    L.nnz = (long long)h.A.col.size();
+    const size_t ib = pad256(sizeof(int) * (h.n + 1)) * 2 + pad256(sizeof(int) * L.nnz) +
+                      pad256(sizeof(int) * np) * 2;
+    const size_t vb = pad256(sizeof(float) * L.nnz) + pad256(sizeof(float) * h.n);
+    const size_t xb = 3 * pad256(sizeof(float) * h.n);
+    if ((e = L.ints.ensure(ib)) || (e = L.vals.ensure(vb)) || (e = L.vecs.ensure(xb))) {
+      err = std::string("hierarchy allocation: ") + cudaGetErrorString(e);
+      H.release();
+      return FCG_ERR_CUDA;
+    }
+    char *p = (char *)L.ints.p;
+    L.ptr = carve<int>(p, h.n + 1);
+    L.mptr = carve<int>(p, h.n + 1);
+    L.col = carve<int>(p, L.nnz);
+    L.agg = carve<int>(p, np);
+    L.mem = carve<int>(p, np);
+    p = (char *)L.vals.p;
+    L.a32 = carve<float>(p, L.nnz);
+    L.dinv = carve<float>(p, h.n);
+    p = (char *)L.vecs.p;
+    L.b = carve<float>(p, h.n);
+    L.x = carve<float>(p, h.n);
+    L.y = carve<float>(p, h.n);
+    if ((e = cudaMemcpy(L.ptr, h.A.ptr.data(), sizeof(int) * (h.n + 1), cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(L.mptr, h.mptr.data(), sizeof(int) * (h.n + 1), cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(L.col, h.A.col.data(), sizeof(int) * L.nnz, cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(L.agg, h.agg.data(), sizeof(int) * np, cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(L.mem, h.mem.data(), sizeof(int) * np, cudaMemcpyHostToDevice))) {
+      err = std::string("hierarchy upload: ") + cudaGetErrorString(e);
+      H.release();
+      return FCG_ERR_CUDA;
+    }
+    np = h.n;
+  }
+  if (!H.lv.empty()) {
+    const int nl = H.lv.back().n;
+    H.has_dense = nl <= dmax;
+    if (H.has_dense) {
+      if ((e = H.dense.ensure(sizeof(float) * nl * nl))) {
+        err = std::string("hierarchy allocation: ") + cudaGetErrorString(e);
+        H.release();
+        return FCG_ERR_CUDA;
+      }
+    }
+  }
+  if ((e = H.fine_tmp.ensure(2 * pad256(sizeof(float) * n)))) {
+    err = std::string("hierarchy allocation: ") + cudaGetErrorString(e);
+    H.release();
+    return FCG_ERR_CUDA;
+  }
+  H.uid = c->uid;
+  H.gen = c->bind_gen;
+  H.n0 = n;
+  H.max_levels = o.max_levels;
+  H.dense_max = o.dense_max;
+  H.build_id++;
+  H.setup_seconds =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return FCG_OK;
+}
+
+int values(Hierarchy &H, fcg_context *c, cudaStream_t st) {
+  const int ns = c->num_sms;
+  for (size_t l = 0; l < H.lv.size(); ++l) {
+    DevLevel &L = H.lv[l];
+    const int g = grid_for(32LL * L.n, ns, 8);
+    if (l == 0) {
+      k_ml_galerkin0<<<g, kTPB, 0, st>>>(L.n, L.ptr, L.col, L.mptr, L.mem, c->sv, c->n,
+                                         scaled32(c), L.agg, L.a32, L.dinv);
+    } else {
+      const DevLevel &P = H.lv[l - 1];
+      k_ml_galerkin<<<g, kTPB, 0, st>>>(L.n, L.ptr, L.col, L.mptr, L.mem, P.ptr, P.col, P.a32,
+                                        L.agg, L.a32, L.dinv);
+    }
+  }
+  if (H.has_dense) {
+    const DevLevel &L = H.lv.back();
+    const size_t smem = sizeof(float) * 2 * L.n * L.n;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(k_ml_dense_inv, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess)
+      return FCG_ERR_CUDA;
+    k_ml_dense_inv<<<1, kDenseThreads, smem, st>>>(L.n, L.ptr, L.col, L.a32,
+                                                   H.dense.as<float>());
+  }
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? FCG_OK : FCG_ERR_CUDA;
+}
+
+void enqueue_correction(Hierarchy &H, fcg_context *c, const Options &o, cudaStream_t st,
+                        const float *r, float *z, const int *done) {
+  if (H.lv.empty()) return;
+  const int n = c->n, ns = c->num_sms;
+  float *t = H.fine_tmp.as<float>();
+  DevLevel &L1 = H.lv[0];
+  k_ml_resid0<<<grid_for(n, ns, 6), kTPB, 0, st>>>(c->sv, n, scaled32(c), r, z, t, done);
+  k_ml_restrict<<<grid_for(L1.n, ns, 8), kTPB, 0, st>>>(L1.n, L1.mptr, L1.mem, t, L1.b, done);
+  const float *e = enqueue_vcycle(H, ns, o, st, 0, done);
+  k_ml_prolong<<<grid_for(n, ns, 8), kTPB, 0, st>>>(n, L1.agg, e, z, (float)o.alpha, done);
+}
+
+void enqueue_jacobi_cycle(Hierarchy &H, fcg_context *c, const Options &o, cudaStream_t st,
+                          const float *r, float *z, const int *done) {
+  const int n = c->n, ns = c->num_sms;
+  const float om = (float)o.omega;
+  float *t = H.fine_tmp.as<float>();
+  float *u = t + pad256(sizeof(float) * n) / sizeof(float);
+  const int gs = grid_for(n, ns, 6);
+  float *cur = z, *oth = u;
+  k_ml_jac0<<<gs, kTPB, 0, st>>>(c->sv, n, scaled32(c), r, nullptr, cur, om, done);
+  for (int s = 1; s < o.sweeps; ++s) {
+    k_ml_jac0<<<gs, kTPB, 0, st>>>(c->sv, n, scaled32(c), r, cur, oth, om, done);
+    std::swap(cur, oth);
+  }
+  if (!H.lv.empty()) {
+    DevLevel &L1 = H.lv[0];
+    k_ml_resid0<<<gs, kTPB, 0, st>>>(c->sv, n, scaled32(c), r, cur, t, done);
+    k_ml_restrict<<<grid_for(L1.n, ns, 8), kTPB, 0, st>>>(L1.n, L1.mptr, L1.mem, t, L1.b, done);
+    const float *e = enqueue_vcycle(H, ns, o, st, 0, done);
+    k_ml_prolong<<<grid_for(n, ns, 8), kTPB, 0, st>>>(n, L1.agg, e, cur, (float)o.alpha, done);
+  }
+  for (int s = 0; s < o.sweeps; ++s) {
+    k_ml_jac0<<<gs, kTPB, 0, st>>>(c->sv, n, scaled32(c), r, cur, oth, om, done);
+    std::swap(cur, oth);
+  }
+  if (cur != z) k_ml_copy<<<grid_for(n, ns, 8), kTPB, 0, st>>>(n, cur, z, done);
+}
+
+}  // namespace ml
+}  // namespace fcg

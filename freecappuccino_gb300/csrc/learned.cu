@@ -47,6 +47,7 @@
 #include <string>
 #include <vector>
 
+#include "coarse.h"
 #include "fcg_internal.h"
 #include "krylov_common.cuh"
 #include "launch.h"
@@ -117,6 +118,9 @@ struct fcg_learned {
   int mdir = 8, ru_every = 50, stall_window = 400;
   int loss_kind = 1;  // 0 energy norm, 1 residual norm
   double stall_factor = 0.5, delta = 0.1;
+  // coarse-grid correction of the flexible CG (coarse.cu, aggregation.cpp)
+  fcg::ml::Options mlo;
+  fcg::ml::Hierarchy *mlh = nullptr;
 };
 
 namespace fcg {
@@ -836,12 +840,17 @@ __global__ void __launch_bounds__(kTPB, 8)
 __global__ void __launch_bounds__(kTPB, 4)
     k_f_out(int n, const __nv_bfloat16 *__restrict__ h, const float *__restrict__ prm,
             const float *__restrict__ rms, const float *__restrict__ r, float *__restrict__ z,
-            const float *__restrict__ qring, long long stride, LScal *S, double *partials) {
+            const float *__restrict__ qring, long long stride, LScal *S, double *partials,
+            int dots) {
   if (fdone(S)) return;
   __shared__ float w[C + 1];
   if (threadIdx.x <= C) w[threadIdx.x] = prm[lp::oWout + threadIdx.x];
   __syncthreads();
   const float sc = rms[0];
+  if (!dots) {  // z only: a coarse-grid correction follows, then k_f_zdots
+    FCG_GRID_STRIDE(i, n) z[i] = r[i] + sc * out_dot(h, i, w);
+    return;
+  }
   const int nwin = __ldcg(&S->nwin);
   float t[lp::kMaxDir];
 #pragma unroll
@@ -849,6 +858,35 @@ __global__ void __launch_bounds__(kTPB, 4)
   FCG_GRID_STRIDE(i, n) {
     const float zi = r[i] + sc * out_dot(h, i, w);
     z[i] = zi;
+#pragma unroll
+    for (int j = 0; j < lp::kMaxDir; ++j)
+      if (j < nwin) t[j] += zi * qring[j * stride + i];
+  }
+  double v[lp::kMaxDir];
+#pragma unroll
+  for (int j = 0; j < lp::kMaxDir; ++j) v[j] = (double)t[j];
+  if (reduce_commit<lp::kMaxDir>(v, partials, &S->ticket[1]) && threadIdx.x == 0) {
+    for (int j = 0; j < lp::kMaxDir; ++j) {
+      S->bets[j] = j < nwin ? v[j] / S->pqs[j] : 0.0;
+      if (!isfinite(S->bets[j])) {
+        S->status = FCG_ERR_NONFINITE;
+        S->done = 1;
+      }
+    }
+  }
+}
+
+// beta_j = z . q_j / p_j . q_j of the stored directions (after a coarse-grid correction)
+__global__ void __launch_bounds__(kTPB, 4)
+    k_f_zdots(int n, const float *__restrict__ z, const float *__restrict__ qring,
+              long long stride, LScal *S, double *partials) {
+  if (fdone(S)) return;
+  const int nwin = __ldcg(&S->nwin);
+  float t[lp::kMaxDir];
+#pragma unroll
+  for (int j = 0; j < lp::kMaxDir; ++j) t[j] = 0.f;
+  FCG_GRID_STRIDE(i, n) {
+    const float zi = z[i];
 #pragma unroll
     for (int j = 0; j < lp::kMaxDir; ++j)
       if (j < nwin) t[j] += zi * qring[j * stride + i];
@@ -1365,6 +1403,10 @@ extern "C" int fcg_lp_destroy(fcg_learned *Lp) {
                   &Lp->hbuf,   &Lp->mbuf,   &Lp->zbuf,   &Lp->dh,   &Lp->dh2, &Lp->dm,
                   &Lp->y,      &Lp->dvec,   &Lp->part,   &Lp->red,  &Lp->scal, &Lp->fvec};
   for (DBuf *b : bufs) b->release();
+  if (Lp->mlh) {
+    Lp->mlh->release();
+    delete Lp->mlh;
+  }
   delete Lp;
   return FCG_OK;
 }
@@ -1654,14 +1696,64 @@ FcgVecs fcg_vectors(fcg_learned *Lp, int n) {
           f + (3 + lp::kMaxDir) * n8, (long long)n8};
 }
 
+// The coarse-grid correction is active for this context (options on, hierarchy built).
+bool ml_on(const fcg_learned *Lp, const fcg_context *c) {
+  return Lp->mlo.enabled && Lp->mlh && Lp->mlh->built_for(c, Lp->mlo);
+}
+
+// Builds the aggregation hierarchy for c's mesh from the loaded matrix when the handle
+// has none for it (once per mesh and options), then recomputes the level matrices from
+// the loaded matrix (every call).
+int ml_prepare(fcg_learned *Lp, fcg_context *c) {
+  if (!Lp->mlo.enabled) return FCG_OK;
+  if (!Lp->mlh) Lp->mlh = new fcg::ml::Hierarchy();
+  if (!Lp->mlh->built_for(c, Lp->mlo)) {
+    std::string err;
+    int rc = fcg::ml::build(*Lp->mlh, c, Lp->mlo, err);
+    if (rc) return lp_fail(Lp, rc, err);
+  }
+  if (fcg::ml::values(*Lp->mlh, c, c->stream))
+    return lp_cuda(Lp, cudaGetLastError(), "coarse level values");
+  return FCG_OK;
+}
+
+// z = M(r): the network (or Jacobi sweeps) followed by the coarse-grid correction.  In
+// the flexible CG (S given) the output kernel honours S->done and leaves the dot
+// products to k_f_zdots.
+void enqueue_preconditioner(fcg_learned *Lp, fcg_context *c, cudaStream_t st, const float *r,
+                            float *z, const int *done, unsigned *rms_ticket, lp::LScal *S) {
+  const int n = c->n;
+  if (Lp->mlo.smoother == FCG_LP_SMOOTH_JACOBI) {
+    fcg::ml::enqueue_jacobi_cycle(*Lp->mlh, c, Lp->mlo, st, r, z, done);
+    return;
+  }
+  enqueue_forward(Lp, c, st, r, false, done, rms_ticket);
+  if (S)
+    k_f_out<<<reduction_grid(c), kTPB, 0, st>>>(n, last_activation(Lp, c, false),
+                                                Lp->params.as<float>(), Lp->scal.as<float>(), r,
+                                                z, nullptr, 0, S, nullptr, 0);
+  else
+    k_lp_out<<<grid_for(n, c->num_sms), kTPB, 0, st>>>(n, last_activation(Lp, c, false),
+                                                       Lp->params.as<float>(),
+                                                       Lp->scal.as<float>(), r, nullptr, nullptr,
+                                                       nullptr, z);
+  fcg::ml::enqueue_correction(*Lp->mlh, c, Lp->mlo, st, r, z, done);
+}
+
 void enqueue_body_head(fcg_learned *Lp, fcg_context *c, cudaStream_t st, const FcgVecs &v,
                        cudaGraphConditionalHandle hif, int use_cond) {
   const int n = c->n;
   const int G = reduction_grid(c);
   double *red = Lp->red.as<double>();
-  enqueue_forward(Lp, c, st, v.r, false, &Lp->S->done, &Lp->S->ticket[6]);
-  k_f_out<<<G, kTPB, 0, st>>>(n, last_activation(Lp, c, false), Lp->params.as<float>(),
-                              Lp->scal.as<float>(), v.r, v.z, v.q, v.stride, Lp->S, red);
+  const int *done = &Lp->S->done;
+  if (!ml_on(Lp, c)) {
+    enqueue_forward(Lp, c, st, v.r, false, done, &Lp->S->ticket[6]);
+    k_f_out<<<G, kTPB, 0, st>>>(n, last_activation(Lp, c, false), Lp->params.as<float>(),
+                                Lp->scal.as<float>(), v.r, v.z, v.q, v.stride, Lp->S, red, 1);
+  } else {
+    enqueue_preconditioner(Lp, c, st, v.r, v.z, done, &Lp->S->ticket[6], Lp->S);
+    k_f_zdots<<<G, kTPB, 0, st>>>(n, v.z, v.q, v.stride, Lp->S, red);
+  }
   k_f_p<<<grid_for(n, c->num_sms), kTPB, 0, st>>>(n, v.z, v.p, v.stride, Lp->S);
   k_f_spmv<<<G, kTPB, 0, st>>>(c->sv, n, scaled32(c), v.p, v.q, v.stride, v.r, Lp->S, red);
   k_f_update<<<G, kTPB, 0, st>>>(n, v.y, v.r, v.p, v.q, v.stride, Lp->S, red, hif, use_cond);
@@ -1680,7 +1772,13 @@ int build_fcg_graph(fcg_learned *Lp, fcg_context *c, const FcgVecs &v) {
                                    scaled32(c), scale64(c),
                                    sliced64(c), Lp->fvec.p,
                                    Lp->hbuf.p,  Lp->feat.p,
-                                   c->stream,   (const void *)(uintptr_t)c->n};
+                                   c->stream,   (const void *)(uintptr_t)c->n,
+                                   (const void *)(uintptr_t)ml_on(Lp, c),
+                                   (const void *)(uintptr_t)(Lp->mlh ? Lp->mlh->build_id : 0),
+                                   (const void *)(uintptr_t)Lp->mlo.smoother,
+                                   (const void *)(uintptr_t)Lp->mlo.sweeps,
+                                   (const void *)(uintptr_t)(Lp->mlo.alpha * 1e6),
+                                   (const void *)(uintptr_t)(Lp->mlo.omega * 1e6)};
   if (Lp->exec && key == Lp->graph_key) return FCG_OK;
   if (Lp->exec) cudaGraphExecDestroy(Lp->exec);
   if (Lp->graph) cudaGraphDestroy(Lp->graph);
@@ -1770,6 +1868,7 @@ extern "C" int fcg_fcg_learned(fcg_context *c, fcg_learned *Lp, const double *a,
   if ((rc = prepare_scaled32(c, (const double *)da))) return rc;
   if ((rc = compute_features(Lp, c))) return set_error(c, rc, Lp->err);
   if ((rc = ensure_workspace(Lp, c, false))) return set_error(c, rc, Lp->err);
+  if ((rc = ml_prepare(Lp, c))) return set_error(c, rc, Lp->err);
   const size_t n8 = ((size_t)n + 63) & ~(size_t)63;
   (void)n8;
   FCG_CUDA_TRY(c, Lp->fvec.ensure(fcg_bytes(n)));
@@ -1868,4 +1967,123 @@ extern "C" int fcg_fcg_learned(fcg_context *c, fcg_learned *Lp, const double *a,
     return set_error(c, status, status == FCG_ERR_TIMEOUT ? "FCG loop exceeded nsw + 2 bodies"
                                                           : "non-finite value in the FCG");
   return FCG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Coarse-grid correction: options, hierarchy, standalone application
+// ---------------------------------------------------------------------------
+extern "C" int fcg_lp_set_multilevel(fcg_learned *Lp, const fcg_lp_multilevel *o) {
+  if (!Lp || !o) return FCG_ERR_ARG;
+  if ((o->enabled != 0 && o->enabled != 1) ||
+      (o->smoother != FCG_LP_SMOOTH_NETWORK && o->smoother != FCG_LP_SMOOTH_JACOBI) ||
+      o->sweeps < 1 || o->sweeps > 8 || o->max_levels < 2 || o->max_levels > FCG_LP_MAX_LEVELS ||
+      o->dense_max < 1 || o->dense_max > 160 || !(o->alpha > 0.0 && o->alpha < 4.0) ||
+      !(o->omega > 0.0 && o->omega < 2.0))
+    return lp_fail(Lp, FCG_ERR_ARG, "multilevel option out of range");
+  Lp->mlo.enabled = o->enabled;
+  Lp->mlo.smoother = o->smoother;
+  Lp->mlo.sweeps = o->sweeps;
+  Lp->mlo.max_levels = o->max_levels;
+  Lp->mlo.dense_max = o->dense_max;
+  Lp->mlo.alpha = o->alpha;
+  Lp->mlo.omega = o->omega;
+  return FCG_OK;
+}
+
+extern "C" int fcg_lp_get_multilevel(const fcg_learned *Lp, fcg_lp_multilevel *o) {
+  if (!Lp || !o) return FCG_ERR_ARG;
+  o->enabled = Lp->mlo.enabled;
+  o->smoother = Lp->mlo.smoother;
+  o->sweeps = Lp->mlo.sweeps;
+  o->max_levels = Lp->mlo.max_levels;
+  o->dense_max = Lp->mlo.dense_max;
+  o->alpha = Lp->mlo.alpha;
+  o->omega = Lp->mlo.omega;
+  return FCG_OK;
+}
+
+namespace {
+int ml_ready(fcg_learned *Lp, fcg_context *c) {
+  int rc = check_ctx(Lp, c);
+  if (rc) return rc;
+  if ((rc = matrix_ready(Lp, c))) return rc;
+  if (!Lp->mlo.enabled) return lp_fail(Lp, FCG_ERR_STATE, "the coarse-grid correction is off");
+  return ml_prepare(Lp, c);
+}
+}  // namespace
+
+extern "C" int fcg_lp_hierarchy_info(fcg_learned *Lp, fcg_context *c, int *levels, int *cells,
+                                     long long *entries, double *setup_seconds) {
+  int rc = ml_ready(Lp, c);
+  if (rc) return rc;
+  LP_TRY(Lp, cudaStreamSynchronize(c->stream));
+  const fcg::ml::Hierarchy &H = *Lp->mlh;
+  const int nl = (int)H.lv.size() + 1;
+  if (levels) *levels = nl;
+  for (int l = 0; l < nl; ++l) {
+    if (cells) cells[l] = l == 0 ? c->n : H.lv[l - 1].n;
+    if (entries) entries[l] = l == 0 ? c->nnz : H.lv[l - 1].nnz;
+  }
+  if (setup_seconds) *setup_seconds = H.setup_seconds;
+  return mark_done(Lp, c);
+}
+
+extern "C" int fcg_lp_hierarchy_level(fcg_learned *Lp, fcg_context *c, int level, int *agg,
+                                      int *mptr, int *mem, int *ptr, int *col, float *val) {
+  int rc = ml_ready(Lp, c);
+  if (rc) return rc;
+  const fcg::ml::Hierarchy &H = *Lp->mlh;
+  if (level < 1 || level > (int)H.lv.size())
+    return lp_fail(Lp, FCG_ERR_ARG, "no such coarse level");
+  const fcg::ml::DevLevel &L = H.lv[level - 1];
+  const int np = level == 1 ? c->n : H.lv[level - 2].n;
+  auto get = [&](void *dst, const void *src, size_t b) {
+    return dst ? cudaMemcpyAsync(dst, src, b, cudaMemcpyDefault, c->stream) : cudaSuccess;
+  };
+  LP_TRY(Lp, get(agg, L.agg, sizeof(int) * np));
+  LP_TRY(Lp, get(mptr, L.mptr, sizeof(int) * (L.n + 1)));
+  LP_TRY(Lp, get(mem, L.mem, sizeof(int) * np));
+  LP_TRY(Lp, get(ptr, L.ptr, sizeof(int) * (L.n + 1)));
+  LP_TRY(Lp, get(col, L.col, sizeof(int) * L.nnz));
+  LP_TRY(Lp, get(val, L.a32, sizeof(float) * L.nnz));
+  LP_TRY(Lp, cudaStreamSynchronize(c->stream));
+  return mark_done(Lp, c);
+}
+
+// z = M(r), the preconditioner of fcg_fcg_learned (FP32 vectors, host or device).
+extern "C" int fcg_lp_precondition(fcg_learned *Lp, fcg_context *c, const float *r, float *z) {
+  int rc = ml_ready(Lp, c);
+  if (rc) return rc;
+  if (!r || !z) return lp_fail(Lp, FCG_ERR_ARG, "NULL r or z");
+  if ((rc = ensure_workspace(Lp, c, false))) return rc;
+  float *dr, *dz;
+  bool hr, hz;
+  if ((rc = stage_f32(Lp, c, r, 4, true, &dr, &hr))) return rc;
+  if ((rc = stage_f32(Lp, c, z, 5, false, &dz, &hz))) return rc;
+  enqueue_preconditioner(Lp, c, c->stream, dr, dz, nullptr, Lp->scal.as<unsigned>() + 17, nullptr);
+  LP_TRY(Lp, cudaGetLastError());
+  if ((rc = stage_out(c, z, dz, sizeof(float) * c->n, hz)))
+    return lp_fail(Lp, rc, fcg_last_error(c));
+  LP_TRY(Lp, cudaStreamSynchronize(c->stream));
+  return mark_done(Lp, c);
+}
+
+// out = z + alpha P V(P^T (r - Ahat z)), the coarse-grid correction alone.
+extern "C" int fcg_lp_coarse_correct(fcg_learned *Lp, fcg_context *c, const float *r,
+                                     const float *z, float *out) {
+  int rc = ml_ready(Lp, c);
+  if (rc) return rc;
+  if (!r || !z || !out) return lp_fail(Lp, FCG_ERR_ARG, "NULL r, z or out");
+  float *dr, *dz, *dout;
+  bool hr, hz, ho;
+  if ((rc = stage_f32(Lp, c, r, 4, true, &dr, &hr))) return rc;
+  if ((rc = stage_f32(Lp, c, z, 5, true, &dz, &hz))) return rc;
+  if ((rc = stage_f32(Lp, c, out, 6, false, &dout, &ho))) return rc;
+  LP_TRY(Lp, cudaMemcpyAsync(dout, dz, sizeof(float) * c->n, cudaMemcpyDeviceToDevice, c->stream));
+  fcg::ml::enqueue_correction(*Lp->mlh, c, Lp->mlo, c->stream, dr, dout, nullptr);
+  LP_TRY(Lp, cudaGetLastError());
+  if ((rc = stage_out(c, out, dout, sizeof(float) * c->n, ho)))
+    return lp_fail(Lp, rc, fcg_last_error(c));
+  LP_TRY(Lp, cudaStreamSynchronize(c->stream));
+  return mark_done(Lp, c);
 }

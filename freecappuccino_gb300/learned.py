@@ -39,6 +39,14 @@ def _f32(x):
     return np.ascontiguousarray(x, dtype=np.float32)
 
 
+def _like(x):
+    if _is_torch(x):
+        import torch
+
+        return torch.empty_like(x)
+    return np.zeros_like(x)
+
+
 class LearnedPreconditioner:
     """An fcg_learned handle: FP32 weights and Adam state on one device."""
 
@@ -155,6 +163,77 @@ class LearnedPreconditioner:
         self._check(self.lib.fcg_lp_set_fcg_options(self.h, int(directions), int(ru_every),
                                                     int(stall_window), float(stall_factor)),
                     "fcg_lp_set_fcg_options")
+
+    # -- coarse-grid correction ---------------------------------------------------
+    @property
+    def multilevel(self) -> dict:
+        """Options of the coarse-grid correction (fcg_lp_multilevel) as a dict."""
+        o = _lib.Multilevel()
+        self._check(self.lib.fcg_lp_get_multilevel(self.h, C.byref(o)), "fcg_lp_get_multilevel")
+        d = {k: getattr(o, k) for k, _ in _lib.Multilevel._fields_}
+        d["smoother"] = "jacobi" if o.smoother == _lib.SMOOTH_JACOBI else "network"
+        return d
+
+    def set_multilevel(self, enabled: bool | None = None, smoother: str | None = None,
+                       sweeps: int | None = None, max_levels: int | None = None,
+                       dense_max: int | None = None, alpha: float | None = None,
+                       omega: float | None = None):
+        """Changes the given options of the coarse-grid correction; smoother is "network"
+        (the default) or "jacobi" (the same cycle without the network)."""
+        cur = self.multilevel
+        new = dict(enabled=enabled, smoother=smoother, sweeps=sweeps, max_levels=max_levels,
+                   dense_max=dense_max, alpha=alpha, omega=omega)
+        for k, v in new.items():
+            if v is not None:
+                cur[k] = v
+        o = _lib.Multilevel(int(bool(cur["enabled"])),
+                            {"network": _lib.SMOOTH_NETWORK, "jacobi": _lib.SMOOTH_JACOBI}[cur["smoother"]],
+                            int(cur["sweeps"]), int(cur["max_levels"]), int(cur["dense_max"]),
+                            float(cur["alpha"]), float(cur["omega"]))
+        self._check(self.lib.fcg_lp_set_multilevel(self.h, C.byref(o)), "fcg_lp_set_multilevel")
+
+    def hierarchy(self, ctx: Context) -> dict:
+        """Levels (the fine one first): cells and entries of each, and the seconds the
+        host construction took."""
+        nl = C.c_int()
+        cells = (C.c_int * _lib.MAX_LEVELS)()
+        ent = (C.c_longlong * _lib.MAX_LEVELS)()
+        sec = C.c_double()
+        self._check(self.lib.fcg_lp_hierarchy_info(self.h, ctx.h, C.byref(nl), cells, ent,
+                                                   C.byref(sec)), "fcg_lp_hierarchy_info")
+        return {"cells": list(cells[:nl.value]), "entries": list(ent[:nl.value]),
+                "setup_seconds": sec.value}
+
+    def hierarchy_level(self, ctx: Context, level: int) -> dict:
+        """Arrays of coarse level `level` (1-based below the fine one), 0-based."""
+        info = self.hierarchy(ctx)
+        n_above, n, nnz = info["cells"][level - 1], info["cells"][level], info["entries"][level]
+        out = dict(agg=np.zeros(n_above, np.int32), mptr=np.zeros(n + 1, np.int32),
+                   mem=np.zeros(n_above, np.int32), ptr=np.zeros(n + 1, np.int32),
+                   col=np.zeros(nnz, np.int32), val=np.zeros(nnz, np.float32))
+        self._check(self.lib.fcg_lp_hierarchy_level(self.h, ctx.h, int(level),
+                                                    *[_ptr(out[k]) for k in ("agg", "mptr", "mem",
+                                                                             "ptr", "col", "val")]),
+                    "fcg_lp_hierarchy_level")
+        return out
+
+    def precondition(self, ctx: Context, r):
+        """z = M(r): the network and the coarse-grid correction, as the solver applies it."""
+        r = _f32(r)
+        ctx._follow(r)
+        z = _like(r)
+        self._check(self.lib.fcg_lp_precondition(self.h, ctx.h, _ptr(r), _ptr(z)),
+                    "fcg_lp_precondition")
+        return z
+
+    def coarse_correct(self, ctx: Context, r, z):
+        """z + alpha P V(P^T (r - Ahat z)), the coarse-grid correction alone."""
+        r, z = _f32(r), _f32(z)
+        ctx._follow(r, z)
+        out = _like(r)
+        self._check(self.lib.fcg_lp_coarse_correct(self.h, ctx.h, _ptr(r), _ptr(z), _ptr(out)),
+                    "fcg_lp_coarse_correct")
+        return out
 
     # -- solver ---------------------------------------------------------------------
     def solve(self, ctx: Context, a, su, fi, sor: float, nsw: int) -> "FcgResult":

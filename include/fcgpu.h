@@ -538,8 +538,59 @@ int fcg_lp_last_solve_stats(const fcg_learned *lp, int *iters, int *updates);
 int fcg_lp_profile(fcg_learned *lp, fcg_context *ctx, const float *r, int reps, double *ms,
                    int max_units, int *units);
 
+/* Coarse-grid correction of the flexible CG (on by default).  The preconditioner is
+ *   M(r) = z + alpha P V(P^T (r - Ahat z)),  z = N(r),
+ * where P is the piecewise-constant prolongation from an aggregation of the cells and
+ * V a V-cycle below it: `sweeps` damped Jacobi sweeps (omega) before and after each
+ * level's own correction (also scaled by alpha) and a dense inverse at the coarsest
+ * level when it has at most dense_max rows.  A level aggregates the level above by
+ * three passes of pairwise matching: each row, in ascending order, pairs with its
+ * unmatched neighbour of most negative coupling in Ahat (ties: lowest column).  The
+ * aggregation is built on the host once per mesh, from the first matrix solved (or set)
+ * on it; the level matrices P^T Ahat P are recomputed on the device at every call.
+ * smoother FCG_LP_SMOOTH_JACOBI replaces N by `sweeps` Jacobi sweeps before and after
+ * the correction (the same cycle without the network).  FP32 throughout. */
+#define FCG_LP_SMOOTH_NETWORK 0
+#define FCG_LP_SMOOTH_JACOBI 1
+#define FCG_LP_MAX_LEVELS 16
+typedef struct fcg_lp_multilevel {
+  int enabled;    /* 1 (default) or 0: M(r) = N(r) */
+  int smoother;   /* FCG_LP_SMOOTH_NETWORK (default) or FCG_LP_SMOOTH_JACOBI */
+  int sweeps;     /* 1..8, default 2 */
+  int max_levels; /* 2..FCG_LP_MAX_LEVELS levels counting the fine one, default 10 */
+  int dense_max;  /* 1..160, default 128 */
+  double alpha;   /* (0, 4), default 1.8 */
+  double omega;   /* (0, 2), default 0.67 */
+} fcg_lp_multilevel;
+int fcg_lp_set_multilevel(fcg_learned *lp, const fcg_lp_multilevel *opt);
+int fcg_lp_get_multilevel(const fcg_learned *lp, fcg_lp_multilevel *opt);
+/* The hierarchy for ctx's mesh and the matrix last set (built if needed): *levels
+ * counting the fine one, cells[l] and entries[l] of every level (arrays of
+ * FCG_LP_MAX_LEVELS, may be NULL), and the seconds its host construction took. */
+int fcg_lp_hierarchy_info(fcg_learned *lp, fcg_context *ctx, int *levels, int *cells,
+                          long long *entries, double *setup_seconds);
+/* Arrays of coarse level `level` (1..levels-1), 0-based, each may be NULL: agg[n_above]
+ * (row of the level above -> row of this level), mptr[n+1] and mem[n_above] (rows above
+ * of every row, ascending), ptr[n+1] and col[entries] (pattern, columns ascending) and
+ * val[entries] (P^T Ahat P, summed in FP32 from the FP32 Ahat in a fixed order: member
+ * rows ascending, each row's entries in column order). */
+int fcg_lp_hierarchy_level(fcg_learned *lp, fcg_context *ctx, int level, int *agg, int *mptr,
+                           int *mem, int *ptr, int *col, float *val);
+/* z = M(r), the preconditioner fcg_fcg_learned applies, for the matrix last set. */
+int fcg_lp_precondition(fcg_learned *lp, fcg_context *ctx, const float *r, float *z);
+/* out = z + alpha P V(P^T (r - Ahat z)), the coarse-grid correction alone. */
+int fcg_lp_coarse_correct(fcg_learned *lp, fcg_context *ctx, const float *r, const float *z,
+                          float *out);
+/* Host utility (no device): the aggregation of one level as above, on a 0-based CSR
+ * (ptr[n+1], col and val[ptr[n]], columns strictly ascending in each row) -- `passes`
+ * matching passes, stopping once at most dense_max aggregates remain.  agg[n] receives
+ * the aggregate of every row and *nc their number (agg[i] = i, *nc = n when the matrix
+ * does not coarsen by 10%).  FCG_ERR_INDEX for a malformed CSR. */
+int fcg_aggregate(int n, const int *ptr, const int *col, const double *val, int passes,
+                  int dense_max, int *agg, int *nc);
+
 /* Truncated flexible CG (Notay, SIAM J. Sci. Comput. 22 (2000) 1444) preconditioned by
- * the network, on
+ * M (the network and the coarse-grid correction above), on
  * the arguments of fcg_dpcg and with its stop test resl/(res0+small) < sor on the
  * FP64 L1 residual.  The iteration runs in FP32 on Ahat with reliable updates: the
  * true residual su - A x is recomputed in FP64 when the FP32 residual has fallen 10x,

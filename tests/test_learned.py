@@ -250,6 +250,7 @@ def test_fcg_stall_falls_back_to_dpcg():
 
     sysm = _gpu_system(16)
     lp = LearnedPreconditioner(seed=1)
+    lp.set_multilevel(enabled=False)  # the network alone
     lp.set_fcg_options(directions=2, ru_every=5, stall_window=10, stall_factor=1e-9)
     x0 = np.zeros(sysm.ctx.n)
     r = lp.solve(sysm.ctx, sysm.a, sysm.su, x0, 1e-8, 5000)
@@ -274,6 +275,7 @@ def test_training_reduces_loss_and_fcg_iterations():
         conv = s.ctx.dpcg(s.a, s.su, np.zeros(s.ctx.n), 1e-8, 5000).iters
         pairs.append(dpcg_pairs(s, np.linspace(0, conv, 24).astype(int)))
     lp = LearnedPreconditioner(seed=5)
+    lp.set_multilevel(enabled=False)  # the network alone
     test = _gpu_system(16, seed=13)
     x0 = np.zeros(test.ctx.n)
     before = lp.solve(test.ctx, test.a, test.su, x0, 1e-8, 5000)
@@ -296,6 +298,7 @@ def test_shipped_weights_beat_jacobi_in_iterations():
         pytest.skip("no shipped checkpoint")
     sysm = _gpu_system(32, seed=21, variable=False)
     lp = LearnedPreconditioner(path=DEFAULT_WEIGHTS)
+    lp.set_multilevel(enabled=False)  # the network alone
     x0 = np.zeros(sysm.ctx.n)
     r = lp.solve(sysm.ctx, sysm.a, sysm.su, x0, 1e-8, 20000)
     d = sysm.ctx.dpcg(sysm.a, sysm.su, x0, 1e-8, 20000)
