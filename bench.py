@@ -484,6 +484,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the calcp step (config 1) and the multi-RHS solve (config 2)")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip the comparison solves (extra.comparisons)")
     ap.add_argument("--batch-seed", type=int, default=4242)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--solver", default="learned",
@@ -626,7 +628,7 @@ def main():
     # The methods the headline is compared with, on the same system.
     comparisons = {}
     for other in ("dpcg", "dpcg_mixed"):
-        if other == method:
+        if other == method or args.no_compare:
             continue
         run(other)
         r_o, t_o = timed(other)
@@ -634,7 +636,7 @@ def main():
         comparisons[other] = {"seconds": t_o, "sweeps": r_o.iters, "l2_rel": r_o.l2_rel,
                               "headline_speedup": t_o / t_solve,
                               "max_rel_diff_of_headline_solution": err}
-    if method == "learned" and ml:
+    if method == "learned" and ml and not args.no_compare:
         # the same flexible CG without the network (Jacobi sweeps in its place) and the
         # network without the coarse-grid correction; one timed solve each
         for name, opt in (("fcg_coarse_jacobi_no_network", {"smoother": "jacobi"}),
