@@ -120,7 +120,7 @@ struct fcg_learned {
   double stall_factor = 0.5, delta = 0.1;
   // coarse-grid correction of the flexible CG (coarse.cu, aggregation.cpp)
   fcg::ml::Options mlo;
-  fcg::ml::Hierarchy *mlh = nullptr;
+  std::vector<fcg::ml::Hierarchy *> mlc;  // one per context, least recently used first
 };
 
 namespace fcg {
@@ -623,6 +623,20 @@ __global__ void __launch_bounds__(kTPB, 6)
     const int row = slice * 32 + lane;
     if (row < n) y[row] = v;
   }
+}
+
+// d = y_c - e/rms (the cycle loss's output error)
+__global__ void __launch_bounds__(kTPB)
+    k_lp_cycle_d(int n, const float *__restrict__ yc, const float *__restrict__ e,
+                 const float *__restrict__ rms, float *__restrict__ d) {
+  const float inv = 1.0f / rms[0];
+  FCG_GRID_STRIDE(i, n) d[i] = yc[i] - e[i] * inv;
+}
+
+// g = u - g (the cycle loss's gradient, in place)
+__global__ void __launch_bounds__(kTPB)
+    k_lp_cycle_g(int n, const float *__restrict__ u, float *__restrict__ g) {
+  FCG_GRID_STRIDE(i, n) g[i] = u[i] - g[i];
 }
 
 // dy = 2 g / sums[1] (g = Ahat d or Ahat Ahat d); dh_L = dy w_out; per-block sums of
@@ -1160,7 +1174,7 @@ int ensure_workspace(fcg_learned *Lp, fcg_context *c, bool train) {
     LP_TRY(Lp, Lp->dh.ensure(sizeof(float) * nc));
     LP_TRY(Lp, Lp->dh2.ensure(sizeof(float) * nc));
     LP_TRY(Lp, Lp->dm.ensure(sizeof(float) * nc));
-    LP_TRY(Lp, Lp->dvec.ensure(sizeof(float) * 3 * Lp->ncap));
+    LP_TRY(Lp, Lp->dvec.ensure(sizeof(float) * 6 * Lp->ncap));
     Lp->train_cap = true;
   }
   return FCG_OK;
@@ -1268,10 +1282,56 @@ const __nv_bfloat16 *last_activation(fcg_learned *Lp, fcg_context *c, bool train
   return train ? H + (size_t)lp::L * hs : H + (lp::L % 2) * hs;
 }
 
+// Hierarchies of the coarse-grid correction, one per context (the handle may train on
+// several), at most kMlCache (16), least recently used first.
+constexpr size_t kMlCache = 16;
+
+fcg::ml::Hierarchy *ml_for(const fcg_learned *Lp, const fcg_context *c) {
+  for (fcg::ml::Hierarchy *h : Lp->mlc)
+    if (h->built_for(c, Lp->mlo)) return h;
+  return nullptr;
+}
+
+// The correction is active for this context (options on, hierarchy built).
+bool ml_on(const fcg_learned *Lp, const fcg_context *c) {
+  return Lp->mlo.enabled && ml_for(Lp, c) != nullptr;
+}
+
+// Builds the aggregation hierarchy for c's mesh from the loaded matrix when the handle
+// has none for it (once per mesh and options), then recomputes the level matrices from
+// the loaded matrix (every call).
+int ml_prepare(fcg_learned *Lp, fcg_context *c) {
+  if (!Lp->mlo.enabled) return FCG_OK;
+  fcg::ml::Hierarchy *H = ml_for(Lp, c);
+  if (!H) {
+    for (fcg::ml::Hierarchy *h : Lp->mlc)
+      if (h->uid == c->uid) H = h;  // same context, rebound or other options: rebuild
+    if (!H && Lp->mlc.size() >= kMlCache) H = Lp->mlc.front();
+    if (!H) {
+      H = new fcg::ml::Hierarchy();
+      Lp->mlc.push_back(H);
+    }
+    std::string err;
+    int rc = fcg::ml::build(*H, c, Lp->mlo, err);
+    if (rc) return lp_fail(Lp, rc, err);
+  }
+  auto it = std::find(Lp->mlc.begin(), Lp->mlc.end(), H);
+  Lp->mlc.erase(it);
+  Lp->mlc.push_back(H);
+  if (fcg::ml::values(*H, c, c->stream))
+    return lp_cuda(Lp, cudaGetLastError(), "coarse level values");
+  return FCG_OK;
+}
+
 // Loss and gradient of one (r, e) pair (device, FP32) into Lp->grad; sums at scal[2..3].
 int loss_grad(fcg_learned *Lp, fcg_context *c, const float *r, const float *e) {
   int rc = ensure_workspace(Lp, c, true);
   if (rc) return rc;
+  if (Lp->loss_kind == FCG_LP_LOSS_CYCLE) {
+    if (!Lp->mlo.enabled)
+      return lp_fail(Lp, FCG_ERR_STATE, "the cycle loss needs the coarse-grid correction on");
+    if ((rc = ml_prepare(Lp, c))) return rc;
+  }
   const int n = c->n;
   cudaStream_t st = c->stream;
   unsigned *tk = Lp->scal.as<unsigned>() + 16;
@@ -1283,12 +1343,31 @@ int loss_grad(fcg_learned *Lp, fcg_context *c, const float *r, const float *e) {
   float *dvec = Lp->dvec.as<float>(), *advec = dvec + Lp->ncap, *aadvec = advec + Lp->ncap;
   k_lp_out<<<grid_for(n, c->num_sms), kTPB, 0, st>>>(n, last_activation(Lp, c, true), prm, rms, r,
                                                      e, Lp->y.as<float>(), dvec, nullptr);
-  k_lp_aloss<<<G, kTPB, 0, st>>>(c->sv, n, scaled32(c), dvec, e, rms, advec,
-                                 Lp->red.as<double>(), tk + 2, sums, Lp->loss_kind);
   const float *gy = advec;
-  if (Lp->loss_kind == 1) {
-    k_lp_spmv32<<<G, kTPB, 0, st>>>(c->sv, n, scaled32(c), advec, aadvec);
-    gy = aadvec;
+  if (Lp->loss_kind == FCG_LP_LOSS_CYCLE) {
+    // y_c = y + alpha P V P^T (r/rms - Ahat y), d = y_c - e/rms; loss d.Ahat d / t.Ahat t
+    // (energy norm, t = e/rms); d loss / dy = E^T (2 Ahat d / t.Ahat t) with
+    // E = I - alpha P V P^T Ahat: for the symmetric V that is u - Ahat (alpha P V P^T u),
+    // u = Ahat d (the factor 2 / t.Ahat t is applied by k_lp_out_bwd)
+    fcg::ml::Hierarchy *H = ml_for(Lp, c);
+    float *yc = aadvec + Lp->ncap, *w = yc + Lp->ncap, *tmp = w + Lp->ncap;
+    LP_TRY(Lp, cudaMemcpyAsync(yc, Lp->y.p, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+    fcg::ml::enqueue_correction(*H, c, Lp->mlo, st, Lp->feat.as<float>(), yc, nullptr);
+    k_lp_cycle_d<<<grid_for(n, c->num_sms), kTPB, 0, st>>>(n, yc, e, rms, dvec);
+    k_lp_aloss<<<G, kTPB, 0, st>>>(c->sv, n, scaled32(c), dvec, e, rms, advec,
+                                   Lp->red.as<double>(), tk + 2, sums, 0);
+    LP_TRY(Lp, cudaMemsetAsync(w, 0, sizeof(float) * n, st));
+    fcg::ml::enqueue_correction(*H, c, Lp->mlo, st, advec, w, nullptr);
+    k_lp_spmv32<<<G, kTPB, 0, st>>>(c->sv, n, scaled32(c), w, tmp);
+    k_lp_cycle_g<<<grid_for(n, c->num_sms), kTPB, 0, st>>>(n, advec, tmp);
+    gy = tmp;
+  } else {
+    k_lp_aloss<<<G, kTPB, 0, st>>>(c->sv, n, scaled32(c), dvec, e, rms, advec,
+                                   Lp->red.as<double>(), tk + 2, sums, Lp->loss_kind);
+    if (Lp->loss_kind == FCG_LP_LOSS_RESIDUAL) {
+      k_lp_spmv32<<<G, kTPB, 0, st>>>(c->sv, n, scaled32(c), advec, aadvec);
+      gy = aadvec;
+    }
   }
   const int GB = c->num_sms * 2;  // blocks of the weight-gradient kernels
   float *part = Lp->part.as<float>();
@@ -1403,9 +1482,9 @@ extern "C" int fcg_lp_destroy(fcg_learned *Lp) {
                   &Lp->hbuf,   &Lp->mbuf,   &Lp->zbuf,   &Lp->dh,   &Lp->dh2, &Lp->dm,
                   &Lp->y,      &Lp->dvec,   &Lp->part,   &Lp->red,  &Lp->scal, &Lp->fvec};
   for (DBuf *b : bufs) b->release();
-  if (Lp->mlh) {
-    Lp->mlh->release();
-    delete Lp->mlh;
+  for (fcg::ml::Hierarchy *h : Lp->mlc) {
+    h->release();
+    delete h;
   }
   delete Lp;
   return FCG_OK;
@@ -1649,7 +1728,7 @@ extern "C" int fcg_lp_train_step(fcg_learned *Lp, fcg_context *c, const float *r
 }
 
 extern "C" int fcg_lp_set_loss(fcg_learned *Lp, int kind) {
-  if (!Lp || kind < 0 || kind > 1) return FCG_ERR_ARG;
+  if (!Lp || kind < FCG_LP_LOSS_ENERGY || kind > FCG_LP_LOSS_CYCLE) return FCG_ERR_ARG;
   Lp->loss_kind = kind;
   return FCG_OK;
 }
@@ -1696,27 +1775,6 @@ FcgVecs fcg_vectors(fcg_learned *Lp, int n) {
           f + (3 + lp::kMaxDir) * n8, (long long)n8};
 }
 
-// The coarse-grid correction is active for this context (options on, hierarchy built).
-bool ml_on(const fcg_learned *Lp, const fcg_context *c) {
-  return Lp->mlo.enabled && Lp->mlh && Lp->mlh->built_for(c, Lp->mlo);
-}
-
-// Builds the aggregation hierarchy for c's mesh from the loaded matrix when the handle
-// has none for it (once per mesh and options), then recomputes the level matrices from
-// the loaded matrix (every call).
-int ml_prepare(fcg_learned *Lp, fcg_context *c) {
-  if (!Lp->mlo.enabled) return FCG_OK;
-  if (!Lp->mlh) Lp->mlh = new fcg::ml::Hierarchy();
-  if (!Lp->mlh->built_for(c, Lp->mlo)) {
-    std::string err;
-    int rc = fcg::ml::build(*Lp->mlh, c, Lp->mlo, err);
-    if (rc) return lp_fail(Lp, rc, err);
-  }
-  if (fcg::ml::values(*Lp->mlh, c, c->stream))
-    return lp_cuda(Lp, cudaGetLastError(), "coarse level values");
-  return FCG_OK;
-}
-
 // z = M(r): the network (or Jacobi sweeps) followed by the coarse-grid correction.  In
 // the flexible CG (S given) the output kernel honours S->done and leaves the dot
 // products to k_f_zdots.
@@ -1724,7 +1782,7 @@ void enqueue_preconditioner(fcg_learned *Lp, fcg_context *c, cudaStream_t st, co
                             float *z, const int *done, unsigned *rms_ticket, lp::LScal *S) {
   const int n = c->n;
   if (Lp->mlo.smoother == FCG_LP_SMOOTH_JACOBI) {
-    fcg::ml::enqueue_jacobi_cycle(*Lp->mlh, c, Lp->mlo, st, r, z, done);
+    fcg::ml::enqueue_jacobi_cycle(*ml_for(Lp, c), c, Lp->mlo, st, r, z, done);
     return;
   }
   enqueue_forward(Lp, c, st, r, false, done, rms_ticket);
@@ -1737,7 +1795,7 @@ void enqueue_preconditioner(fcg_learned *Lp, fcg_context *c, cudaStream_t st, co
                                                        Lp->params.as<float>(),
                                                        Lp->scal.as<float>(), r, nullptr, nullptr,
                                                        nullptr, z);
-  fcg::ml::enqueue_correction(*Lp->mlh, c, Lp->mlo, st, r, z, done);
+  fcg::ml::enqueue_correction(*ml_for(Lp, c), c, Lp->mlo, st, r, z, done);
 }
 
 void enqueue_body_head(fcg_learned *Lp, fcg_context *c, cudaStream_t st, const FcgVecs &v,
@@ -1774,7 +1832,8 @@ int build_fcg_graph(fcg_learned *Lp, fcg_context *c, const FcgVecs &v) {
                                    Lp->hbuf.p,  Lp->feat.p,
                                    c->stream,   (const void *)(uintptr_t)c->n,
                                    (const void *)(uintptr_t)ml_on(Lp, c),
-                                   (const void *)(uintptr_t)(Lp->mlh ? Lp->mlh->build_id : 0),
+                                   (const void *)ml_for(Lp, c),
+                                   (const void *)(uintptr_t)(ml_for(Lp, c) ? ml_for(Lp, c)->build_id : 0),
                                    (const void *)(uintptr_t)Lp->mlo.smoother,
                                    (const void *)(uintptr_t)Lp->mlo.sweeps,
                                    (const void *)(uintptr_t)(Lp->mlo.alpha * 1e6),
@@ -2017,7 +2076,7 @@ extern "C" int fcg_lp_hierarchy_info(fcg_learned *Lp, fcg_context *c, int *level
   int rc = ml_ready(Lp, c);
   if (rc) return rc;
   LP_TRY(Lp, cudaStreamSynchronize(c->stream));
-  const fcg::ml::Hierarchy &H = *Lp->mlh;
+  const fcg::ml::Hierarchy &H = *ml_for(Lp, c);
   const int nl = (int)H.lv.size() + 1;
   if (levels) *levels = nl;
   for (int l = 0; l < nl; ++l) {
@@ -2032,7 +2091,7 @@ extern "C" int fcg_lp_hierarchy_level(fcg_learned *Lp, fcg_context *c, int level
                                       int *mptr, int *mem, int *ptr, int *col, float *val) {
   int rc = ml_ready(Lp, c);
   if (rc) return rc;
-  const fcg::ml::Hierarchy &H = *Lp->mlh;
+  const fcg::ml::Hierarchy &H = *ml_for(Lp, c);
   if (level < 1 || level > (int)H.lv.size())
     return lp_fail(Lp, FCG_ERR_ARG, "no such coarse level");
   const fcg::ml::DevLevel &L = H.lv[level - 1];
@@ -2080,7 +2139,7 @@ extern "C" int fcg_lp_coarse_correct(fcg_learned *Lp, fcg_context *c, const floa
   if ((rc = stage_f32(Lp, c, z, 5, true, &dz, &hz))) return rc;
   if ((rc = stage_f32(Lp, c, out, 6, false, &dout, &ho))) return rc;
   LP_TRY(Lp, cudaMemcpyAsync(dout, dz, sizeof(float) * c->n, cudaMemcpyDeviceToDevice, c->stream));
-  fcg::ml::enqueue_correction(*Lp->mlh, c, Lp->mlo, c->stream, dr, dout, nullptr);
+  fcg::ml::enqueue_correction(*ml_for(Lp, c), c, Lp->mlo, c->stream, dr, dout, nullptr);
   LP_TRY(Lp, cudaGetLastError());
   if ((rc = stage_out(c, out, dout, sizeof(float) * c->n, ho)))
     return lp_fail(Lp, rc, fcg_last_error(c));

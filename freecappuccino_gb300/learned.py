@@ -153,9 +153,10 @@ class LearnedPreconditioner:
         return {names[i]: ms[i] for i in range(nu.value)}
 
     def set_loss(self, kind: str = "residual"):
-        """Training loss: "residual" (|Ahat N(r) - r|^2 / |r|^2, the default) or "energy"
-        ((N(r)-e).Ahat(N(r)-e) / e.Ahat e)."""
-        k = {"energy": 0, "residual": 1}[kind]
+        """Training loss: "residual" (|Ahat N(r) - r|^2 / |r|^2, the default), "energy"
+        ((N(r)-e).Ahat(N(r)-e) / e.Ahat e) or "cycle" ((M(r)-e).Ahat(M(r)-e) / e.Ahat e
+        with M the network followed by the coarse-grid correction)."""
+        k = {"energy": 0, "residual": 1, "cycle": 2}[kind]
         self._check(self.lib.fcg_lp_set_loss(self.h, k), "fcg_lp_set_loss")
 
     def set_fcg_options(self, directions: int = 8, ru_every: int = 50, stall_window: int = 400,

@@ -514,9 +514,14 @@ int fcg_lp_loss_grad(fcg_learned *lp, fcg_context *ctx, const float *r, const fl
                      float *loss, float *grad);
 /* Loss of fcg_lp_loss_grad and fcg_lp_train_step: FCG_LP_LOSS_RESIDUAL (default),
  * |Ahat N(r) - r|^2 / |r|^2, or FCG_LP_LOSS_ENERGY, (N(r) - e).Ahat (N(r) - e) / e.Ahat e
- * (the same error measured in the energy norm). */
+ * (the same error measured in the energy norm), or FCG_LP_LOSS_CYCLE, the energy norm of
+ * the error of the whole preconditioner M (the network followed by the coarse-grid
+ * correction below), (M(r) - e).Ahat (M(r) - e) / e.Ahat e (the correction must be on;
+ * its hierarchy for the context is built on first use).  In every form r stands for
+ * Ahat e. */
 #define FCG_LP_LOSS_ENERGY 0
 #define FCG_LP_LOSS_RESIDUAL 1
+#define FCG_LP_LOSS_CYCLE 2
 int fcg_lp_set_loss(fcg_learned *lp, int kind);
 /* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on the pair (r, e) with rate lr;
  * *loss (may be NULL) receives the loss before the step. */

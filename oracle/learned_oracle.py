@@ -126,21 +126,31 @@ def forward(A: ScaledMatrix, feat, r, w, emulate: bool = True):
     return rms * y, dict(rms=rms, f=f, z0=z0, hs=hs, xs=xs, zs=zs, y=y)
 
 
-def loss_grad(A: ScaledMatrix, feat, r, e, w, emulate: bool = True, kind: str = "energy"):
+def loss_grad(A: ScaledMatrix, feat, r, e, w, emulate: bool = True, kind: str = "energy",
+              correct=None):
     """Loss of the normalised output d = y - t, t = e/rms, and its gradient
     (straight-through roundings, Ahat symmetric):
       energy:   d.Ahat d / t.Ahat t,        d loss/dy = 2 Ahat d / t.Ahat t
-      residual: |Ahat d|^2 / |Ahat t|^2,    d loss/dy = 2 Ahat Ahat d / |Ahat t|^2"""
+      residual: |Ahat d|^2 / |Ahat t|^2,    d loss/dy = 2 Ahat Ahat d / |Ahat t|^2
+      cycle:    the energy form of y_c = correct(r/rms, y) = y + alpha P V P^T (r/rms -
+                Ahat y), the coarse-grid correction after the network (a callable, e.g.
+                multilevel_oracle.Cycle.correct): d = y_c - t and, V being symmetric,
+                d loss/dy = u - Ahat correct(u, 0), u = 2 Ahat d / t.Ahat t"""
     W_in, b_in, layers, w_out, b_out = unpack(w)
     z, c = forward(A, feat, r, w, emulate)
     t = np.asarray(e, dtype=np.float64) / c["rms"]
-    d = c["y"] - t
+    y = c["y"]
+    if kind == "cycle":
+        y = correct(c["f"][:, 0], y)
+    d = y - t
     Ad = A.matmul(d[:, None])[:, 0]
     At = A.matmul(t[:, None])[:, 0]
-    if kind == "energy":
+    if kind in ("energy", "cycle"):
         den = np.dot(t, At)
         loss = np.dot(d, Ad) / den
         dy = 2.0 * Ad / den
+        if kind == "cycle":
+            dy = dy - A.matmul(correct(dy, np.zeros_like(dy))[:, None])[:, 0]
     else:
         den = np.dot(At, At)
         loss = np.dot(Ad, Ad) / den

@@ -152,13 +152,14 @@ def build_levels(ptr, col, val, max_levels=10, dense_max=128, passes=3):
     return levels
 
 
-def level_values(levels, fine):
-    """FP32 values of every level as the device computes them: level 1 from the fine
-    scaled matrix rounded to FP32, each level from the one above, FP32 sums in order."""
+def level_values(levels, fine, f32=True):
+    """Values of every level as the device computes them: level 1 from the fine scaled
+    matrix rounded to FP32, each level from the one above, FP32 sums in order (f32=False:
+    the same products in FP64 from the fine values as given)."""
     out = []
-    above = (fine[0], fine[1], np.asarray(fine[2], np.float32))
+    above = (fine[0], fine[1], np.asarray(fine[2], np.float32 if f32 else np.float64))
     for lv in levels:
-        _, _, v = galerkin(*above, lv["agg"], lv["n"], lv["mptr"], lv["mem"], f32=True)
+        _, _, v = galerkin(*above, lv["agg"], lv["n"], lv["mptr"], lv["mem"], f32=f32)
         out.append(v)
         above = (lv["ptr"], lv["col"], v)
     return out

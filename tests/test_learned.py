@@ -60,7 +60,7 @@ def test_bf16_rounding_matches_torch():
     assert np.array_equal(lo.bf16(x), ref)
 
 
-@pytest.mark.parametrize("kind", ["energy", "residual"])
+@pytest.mark.parametrize("kind", ["energy", "residual", "cycle"])
 def test_oracle_gradient_matches_finite_differences(kind):
     m, csr, a, su = _oracle_system(4)
     A = lo.ScaledMatrix(csr.ioffset, csr.ja, csr.diag, a)
@@ -69,7 +69,15 @@ def test_oracle_gradient_matches_finite_differences(kind):
     r = rng.standard_normal(m.numCells)
     e = rng.standard_normal(m.numCells)
     w = _random_weights(2, scale=3.0).astype(np.float64)
-    loss, g = lo.loss_grad(A, feat, r, e, w, emulate=False, kind=kind)
+    correct = None
+    if kind == "cycle":  # the coarse-grid correction on the same Ahat, in FP64
+        from oracle import multilevel_oracle as mo
+
+        fine = (np.asarray(csr.ioffset) - 1, np.asarray(csr.ja) - 1, A.val)
+        levels = mo.build_levels(*fine)
+        assert levels
+        correct = mo.Cycle(fine, levels, mo.level_values(levels, fine, f32=False)).correct
+    loss, g = lo.loss_grad(A, feat, r, e, w, emulate=False, kind=kind, correct=correct)
     idx = rng.choice(lo.P, 80, replace=False)
     idx = np.concatenate([idx, [lo.P - 1, 0, lo.C * lo.F]])  # b_out, W_in, b_in
     h = 1e-6
@@ -77,8 +85,8 @@ def test_oracle_gradient_matches_finite_differences(kind):
         wp, wm = w.copy(), w.copy()
         wp[i] += h
         wm[i] -= h
-        fd = (lo.loss_grad(A, feat, r, e, wp, emulate=False, kind=kind)[0] -
-              lo.loss_grad(A, feat, r, e, wm, emulate=False, kind=kind)[0]) / (2 * h)
+        fd = (lo.loss_grad(A, feat, r, e, wp, emulate=False, kind=kind, correct=correct)[0] -
+              lo.loss_grad(A, feat, r, e, wm, emulate=False, kind=kind, correct=correct)[0]) / (2 * h)
         assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(g[i])) + 1e-7, (i, fd, g[i])
 
 

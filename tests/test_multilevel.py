@@ -289,3 +289,43 @@ def test_multilevel_options():
     ctx.close()
     lp2.close()
     lp.close()
+
+
+@pytest.mark.gpu
+def test_cycle_loss_gradient_matches_oracle():
+    """The loss through the whole preconditioner (network, then the correction) and its
+    gradient against the oracle's network and cycle."""
+    from oracle import learned_oracle as lo
+
+    from freecappuccino_gb300.learned import LearnedPreconditioner, dpcg_pairs, pressure_system
+
+    sysm = pressure_system(14, 0.2, 3, variable=True)
+    io, ja, dg, _, _ = sysm.ctx.create_csr()
+    A = lo.ScaledMatrix(io, ja, dg, sysm.a)
+    _, _, _, cyc = mo.hierarchy(io, ja, dg, sysm.a)
+    lp = LearnedPreconditioner(seed=1)
+    rng = np.random.default_rng(5)
+    w = lo.pack(rng.uniform(-1, 1, (lo.C, lo.F)) / np.sqrt(lo.F), rng.uniform(-0.2, 0.2, lo.C),
+                [(rng.uniform(-1, 1, (lo.C, 2 * lo.C)) * 2.0 / np.sqrt(2 * lo.C),
+                  rng.uniform(-0.2, 0.2, lo.C)) for _ in range(lo.L)],
+                rng.uniform(-1, 1, lo.C) / np.sqrt(lo.C), 0.05).astype(np.float32)
+    lp.weights = w
+    lp.set_loss("cycle")
+    lp.set_matrix(sysm.ctx, sysm.a)
+    r, e = dpcg_pairs(sysm, [5])[0]
+    loss, g = lp.loss_grad(sysm.ctx, r, e)
+    feat = lo.features(sysm.mesh, sysm.scale)
+    lr_, gr = lo.loss_grad(A, feat, r, e, w, emulate=True, kind="cycle", correct=cyc.correct)
+    assert loss == pytest.approx(lr_, rel=5e-3)
+    bounds = [0, lo.C * lo.F + lo.C] + [lo.C * lo.F + lo.C + (l + 1) * lo.LAYER
+                                         for l in range(lo.L)] + [lo.P]
+    for b0, b1 in zip(bounds[:-1], bounds[1:]):
+        assert np.linalg.norm(g[b0:b1] - gr[b0:b1]) < 3e-2 * np.linalg.norm(gr[b0:b1]), (b0, b1)
+    # the correction off: the cycle loss is refused
+    lp.set_multilevel(enabled=False)
+    with pytest.raises(fcg._lib.FcgError) as ei:
+        lp.loss_grad(sysm.ctx, r, e)
+    assert ei.value.status == fcg._lib.FCG_ERR_STATE
+    lp.close()
+    sysm.ctx.close()
+
