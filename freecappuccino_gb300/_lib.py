@@ -88,7 +88,7 @@ class Multilevel(C.Structure):
     """fcg_lp_multilevel: options of the learned FCG's coarse-grid correction."""
     _fields_ = [("enabled", C.c_int), ("smoother", C.c_int), ("sweeps", C.c_int),
                 ("max_levels", C.c_int), ("dense_max", C.c_int), ("alpha", C.c_double),
-                ("omega", C.c_double)]
+                ("omega", C.c_double), ("smoothed", C.c_int)]
 
 
 SMOOTH_NETWORK, SMOOTH_JACOBI, MAX_LEVELS = 0, 1, 16

@@ -123,8 +123,124 @@ void galerkin(const HostCsr &A, const std::vector<int> &agg, int nc, const std::
   }
 }
 
+// P = (I - omega D^-1 A) P_tent of the level's aggregation, A P and P^T A P, patterns
+// sorted by column and FP64 values in the device's order (P: 1 at the own aggregate,
+// then minus (omega / a_ii) a_ik for the row's entries in column order; A P: for the
+// row's entries in column order, a_ik P_k in P_k's order; P^T A P: for the rows holding
+// the aggregate in ascending order, P_iI (A P)_i in column order).
+void smoothed_level(const HostCsr &A, double omega, HostLevel &lv) {
+  const int n = A.n, nc = lv.n;
+  const std::vector<int> &agg = lv.agg;
+  std::vector<int> marker(std::max(n, nc), -1);
+  // P pattern and values
+  lv.p_ptr.assign(n + 1, 0);
+  lv.p_col.clear();
+  std::vector<double> pv;
+  std::vector<int> row;
+  for (int i = 0; i < n; ++i) {
+    row.clear();
+    row.push_back(agg[i]);
+    for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) row.push_back(agg[A.col[k]]);
+    std::sort(row.begin(), row.end());
+    row.erase(std::unique(row.begin(), row.end()), row.end());
+    const int b = (int)lv.p_col.size();
+    double d = 0.0;
+    for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k)
+      if (A.col[k] == i) d = A.val[k];
+    const double w = d > 0.0 ? omega / d : 0.0;
+    for (int J : row) {
+      lv.p_col.push_back(J);
+      pv.push_back(J == agg[i] ? 1.0 : 0.0);
+    }
+    for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
+      const int J = agg[A.col[k]];
+      const int p = b + (int)(std::lower_bound(row.begin(), row.end(), J) - row.begin());
+      pv[p] -= w * A.val[k];
+    }
+    lv.p_ptr[i + 1] = (int)lv.p_col.size();
+  }
+  // transpose lists
+  lv.t_ptr.assign(nc + 1, 0);
+  for (int J : lv.p_col) ++lv.t_ptr[J + 1];
+  for (int I = 0; I < nc; ++I) lv.t_ptr[I + 1] += lv.t_ptr[I];
+  lv.t_row.assign(lv.p_col.size(), 0);
+  lv.t_pos.assign(lv.p_col.size(), 0);
+  {
+    std::vector<int> fill(lv.t_ptr.begin(), lv.t_ptr.end() - 1);
+    for (int i = 0; i < n; ++i)
+      for (int p = lv.p_ptr[i]; p < lv.p_ptr[i + 1]; ++p) {
+        const int f = fill[lv.p_col[p]]++;
+        lv.t_row[f] = i;
+        lv.t_pos[f] = p;
+      }
+  }
+  // A P
+  lv.ap_ptr.assign(n + 1, 0);
+  lv.ap_col.clear();
+  std::vector<double> apv;
+  for (int i = 0; i < n; ++i) {
+    row.clear();
+    for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
+      const int j = A.col[k];
+      for (int p = lv.p_ptr[j]; p < lv.p_ptr[j + 1]; ++p) row.push_back(lv.p_col[p]);
+    }
+    std::sort(row.begin(), row.end());
+    row.erase(std::unique(row.begin(), row.end()), row.end());
+    const int b = (int)lv.ap_col.size();
+    for (int J : row) {
+      lv.ap_col.push_back(J);
+      apv.push_back(0.0);
+    }
+    for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
+      const int j = A.col[k];
+      for (int p = lv.p_ptr[j]; p < lv.p_ptr[j + 1]; ++p) {
+        const int q = b + (int)(std::lower_bound(row.begin(), row.end(), lv.p_col[p]) - row.begin());
+        apv[q] += A.val[k] * pv[p];
+      }
+    }
+    lv.ap_ptr[i + 1] = (int)lv.ap_col.size();
+  }
+  // P^T A P
+  HostCsr &C = lv.A;
+  C.n = nc;
+  C.ptr.assign(nc + 1, 0);
+  C.col.clear();
+  C.val.clear();
+  std::fill(marker.begin(), marker.end(), -1);
+  std::vector<std::pair<int, double>> sr;
+  for (int I = 0; I < nc; ++I) {
+    const int start = (int)C.col.size();
+    for (int m = lv.t_ptr[I]; m < lv.t_ptr[I + 1]; ++m) {
+      const int i = lv.t_row[m];
+      const double p = pv[lv.t_pos[m]];
+      for (int q = lv.ap_ptr[i]; q < lv.ap_ptr[i + 1]; ++q) {
+        const int J = lv.ap_col[q];
+        if (marker[J] >= start) {
+          C.val[marker[J]] += p * apv[q];
+        } else {
+          marker[J] = (int)C.col.size();
+          C.col.push_back(J);
+          C.val.push_back(p * apv[q]);
+        }
+      }
+    }
+    const int end = (int)C.col.size();
+    sr.clear();
+    for (int q = start; q < end; ++q) sr.emplace_back(C.col[q], C.val[q]);
+    std::sort(sr.begin(), sr.end(),
+              [](const std::pair<int, double> &a, const std::pair<int, double> &b) {
+                return a.first < b.first;
+              });
+    for (int q = start; q < end; ++q) {
+      C.col[q] = sr[q - start].first;
+      C.val[q] = sr[q - start].second;
+    }
+    C.ptr[I + 1] = end;
+  }
+}
+
 int build_levels(const HostCsr &fine, int max_levels, int dense_max, int passes,
-                 std::vector<HostLevel> &levels) {
+                 std::vector<HostLevel> &levels, double sa_omega) {
   levels.clear();
   levels.reserve(max_levels);
   const HostCsr *cur = &fine;
@@ -155,7 +271,10 @@ int build_levels(const HostCsr &fine, int max_levels, int dense_max, int passes,
     lv.n = nc;
     lv.agg = std::move(comp);
     members(n0, nc, lv.agg, lv.mptr, lv.mem);
-    lv.A = *a;  // pattern (and host values) of the level
+    if (levels.empty() && sa_omega > 0.0)
+      smoothed_level(*cur, sa_omega, lv);  // P^T A P with the smoothed prolongation
+    else
+      lv.A = *a;  // pattern (and host values) of the level
     levels.push_back(std::move(lv));
     cur = &levels.back().A;
     if (nc <= dense_max) break;

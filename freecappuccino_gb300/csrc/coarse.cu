@@ -326,6 +326,149 @@ __global__ void __launch_bounds__(kTPB)
   FCG_GRID_STRIDE(i, n) b[i] = a[i];
 }
 
+// ---- smoothed first level: P = (I - omega D^-1 Ahat) P_tent, A P, P^T A P -----------
+// Column and value of slot j of fine row i in the sliced layout (c = -1 for a pad).
+__device__ __forceinline__ void sell_entry(const SellView &sv, int n, const float *val, int i,
+                                           int j, int &c, float &v) {
+  const int slice = i >> 5, rl = i & 31;
+  const long long pos = sv.ptr[slice] + rl + 32LL * j;
+  c = -1;
+  v = 0.f;
+  if (sv.src[pos] < 0) return;
+  const int op = sv.offp[slice];
+  int cc = sv.kind[slice] == 0 ? i + sv.off[op + j] : sv.off[op + 32 * j + rl];
+  c = cc < 0 ? 0 : (cc >= n ? n - 1 : cc);
+  v = val[pos];
+}
+
+// P row i: 1 at the own aggregate, then minus (omega / a_ii) a_ik for the row's entries
+// in column order, each product and difference rounded to FP32 on its own
+__global__ void __launch_bounds__(kTPB)
+    k_sa_p(SellView sv, int n, const float *__restrict__ val, const int *__restrict__ agg,
+           const int *__restrict__ p_ptr, const int *__restrict__ p_col, float omega,
+           float *__restrict__ p_val) {
+  FCG_GRID_STRIDE(i, n) {
+    const int w = sv.width[i >> 5];
+    float d = 0.f;
+    for (int j = 0; j < w; ++j) {
+      int c;
+      float v;
+      sell_entry(sv, n, val, (int)i, j, c, v);
+      if (c == i) d = v;
+    }
+    const float wgt = d > 0.f ? __fdiv_rn(omega, d) : 0.f;
+    const int pb = p_ptr[i], pe = p_ptr[i + 1], own = agg[i];
+    for (int p = pb; p < pe; ++p) p_val[p] = p_col[p] == own ? 1.f : 0.f;
+    for (int j = 0; j < w; ++j) {
+      int c;
+      float v;
+      sell_entry(sv, n, val, (int)i, j, c, v);
+      if (c < 0) continue;
+      const int J = agg[c];
+      int p = pb;
+      while (p < pe - 1 && p_col[p] != J) ++p;
+      p_val[p] = __fsub_rn(p_val[p], __fmul_rn(wgt, v));
+    }
+  }
+}
+
+// (A P) row i: for the row's entries in column order, a_ik P_k in P_k's column order
+__global__ void __launch_bounds__(kTPB)
+    k_sa_ap(SellView sv, int n, const float *__restrict__ val, const int *__restrict__ p_ptr,
+            const int *__restrict__ p_col, const float *__restrict__ p_val,
+            const int *__restrict__ ap_ptr, const int *__restrict__ ap_col,
+            float *__restrict__ ap_val) {
+  FCG_GRID_STRIDE(i, n) {
+    const int w = sv.width[i >> 5];
+    const int qb = ap_ptr[i], qe = ap_ptr[i + 1];
+    for (int q = qb; q < qe; ++q) ap_val[q] = 0.f;
+    for (int j = 0; j < w; ++j) {
+      int c;
+      float v;
+      sell_entry(sv, n, val, (int)i, j, c, v);
+      if (c < 0) continue;
+      for (int p = p_ptr[c]; p < p_ptr[c + 1]; ++p) {
+        const int J = p_col[p];
+        int q = qb;
+        while (q < qe - 1 && ap_col[q] != J) ++q;
+        ap_val[q] = __fadd_rn(ap_val[q], __fmul_rn(v, p_val[p]));
+      }
+    }
+  }
+}
+
+// P^T (A P): one warp per coarse row, one lane per coarse entry; the rows holding the
+// aggregate in ascending order, each row's (A P) entries in column order
+__global__ void __launch_bounds__(kTPB)
+    k_sa_a1(int nc, const int *__restrict__ cptr, const int *__restrict__ ccol,
+            const int *__restrict__ t_ptr, const int *__restrict__ t_row,
+            const int *__restrict__ t_pos, const float *__restrict__ p_val,
+            const int *__restrict__ ap_ptr, const int *__restrict__ ap_col,
+            const float *__restrict__ ap_val, float *__restrict__ a, float *__restrict__ dinv) {
+  const int lane = threadIdx.x & 31;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long I = warp; I < nc; I += nwarps) {
+    const int cb = cptr[I], ce = cptr[I + 1];
+    const int mb = t_ptr[I], me = t_ptr[I + 1];
+    for (int sb = cb; sb < ce; sb += 32) {
+      const int my = sb + lane;
+      const int mycol = my < ce ? ccol[my] : -1;
+      float acc = 0.f;
+      for (int m = mb; m < me; ++m) {
+        const int i = t_row[m];
+        const float p = p_val[t_pos[m]];
+        const int qb0 = ap_ptr[i], qe = ap_ptr[i + 1];
+        for (int qb = qb0; qb < qe; qb += 32) {
+          const int q = qb + lane;
+          int J = -1;
+          float v = 0.f;
+          if (q < qe) {
+            J = ap_col[q];
+            v = __fmul_rn(p, ap_val[q]);
+          }
+          const int cnt = min(32, qe - qb);
+          for (int e = 0; e < cnt; ++e) {
+            const int Je = __shfl_sync(0xffffffffu, J, e);
+            const float ve = __shfl_sync(0xffffffffu, v, e);
+            if (Je == mycol) acc = __fadd_rn(acc, ve);
+          }
+        }
+      }
+      if (my < ce) {
+        a[my] = acc;
+        if (mycol == (int)I) dinv[I] = acc > 0.f ? 1.f / acc : 0.f;
+      }
+    }
+  }
+}
+
+// b1 = P^T t
+__global__ void __launch_bounds__(kTPB)
+    k_sa_restrict(int nc, const int *__restrict__ t_ptr, const int *__restrict__ t_row,
+                  const int *__restrict__ t_pos, const float *__restrict__ p_val,
+                  const float *__restrict__ t, float *__restrict__ bc, const int *done) {
+  if (stopped(done)) return;
+  FCG_GRID_STRIDE(I, nc) {
+    float acc = 0.f;
+    for (int m = t_ptr[I]; m < t_ptr[I + 1]; ++m) acc += p_val[t_pos[m]] * t[t_row[m]];
+    bc[I] = acc;
+  }
+}
+
+// z += alpha P e
+__global__ void __launch_bounds__(kTPB)
+    k_sa_prolong(int n, const int *__restrict__ p_ptr, const int *__restrict__ p_col,
+                 const float *__restrict__ p_val, const float *__restrict__ e,
+                 float *__restrict__ z, float alpha, const int *done) {
+  if (stopped(done)) return;
+  FCG_GRID_STRIDE(i, n) {
+    float s = 0.f;
+    for (int p = p_ptr[i]; p < p_ptr[i + 1]; ++p) s += p_val[p] * e[p_col[p]];
+    z[i] += alpha * s;
+  }
+}
+
 // One V-cycle on level k of H.lv for right-hand side lv[k].b; returns the vector holding
 // the result (lv[k].x or lv[k].y).
 float *enqueue_vcycle(Hierarchy &H, int num_sms, const Options &o, cudaStream_t st, int k,
@@ -361,6 +504,28 @@ float *enqueue_vcycle(Hierarchy &H, int num_sms, const Options &o, cudaStream_t 
   return cur;
 }
 
+// Restriction of the fine residual t to level 1 and prolongation of its correction e:
+// the smoothed P (correction not scaled) or the aggregation (scaled by alpha).
+void fine_restrict(Hierarchy &H, int num_sms, cudaStream_t st, const float *t, const int *done) {
+  DevLevel &L1 = H.lv[0];
+  if (H.smoothed)
+    k_sa_restrict<<<grid_for(L1.n, num_sms, 8), kTPB, 0, st>>>(L1.n, H.t_ptr, H.t_row, H.t_pos,
+                                                              H.p_val, t, L1.b, done);
+  else
+    k_ml_restrict<<<grid_for(L1.n, num_sms, 8), kTPB, 0, st>>>(L1.n, L1.mptr, L1.mem, t, L1.b,
+                                                              done);
+}
+
+void fine_prolong(Hierarchy &H, int n, int num_sms, const Options &o, cudaStream_t st,
+                  const float *e, float *z, const int *done) {
+  if (H.smoothed)
+    k_sa_prolong<<<grid_for(n, num_sms, 8), kTPB, 0, st>>>(n, H.p_ptr, H.p_col, H.p_val, e, z,
+                                                          1.f, done);
+  else
+    k_ml_prolong<<<grid_for(n, num_sms, 8), kTPB, 0, st>>>(n, H.lv[0].agg, e, z, (float)o.alpha,
+                                                          done);
+}
+
 template <class T>
 T *carve(char *&p, size_t count) {
   T *r = (T *)p;
@@ -381,6 +546,9 @@ void Hierarchy::release() {
   lv.clear();
   dense.release();
   fine_tmp.release();
+  sa_ints.release();
+  sa_vals.release();
+  p_nnz = ap_nnz = 0;
   has_dense = false;
   uid = 0;
 }
@@ -421,7 +589,7 @@ int build(Hierarchy &H, fcg_context *c, const Options &o, std::string &err) {
       fine.val[k] = (fine.val[k] * s[i]) * s[fine.col[k]];
   std::vector<HostLevel> hl;
   const int dmax = std::min(std::max(o.dense_max, 1), kDenseMaxRows);
-  build_levels(fine, std::max(2, o.max_levels), dmax, H.passes, hl);
+  build_levels(fine, std::max(2, o.max_levels), dmax, H.passes, hl, o.smoothed ? o.omega : 0.0);
   fine = HostCsr();
   H.lv.resize(hl.size());
   int np = n;  // rows of the parent level
@@ -463,6 +631,44 @@ int build(Hierarchy &H, fcg_context *c, const Options &o, std::string &err) {
     }
     np = h.n;
   }
+  if (!hl.empty() && o.smoothed) {
+    const HostLevel &h = hl[0];
+    H.p_nnz = (long long)h.p_col.size();
+    H.ap_nnz = (long long)h.ap_col.size();
+    const int n1 = h.n;
+    const size_t ib = pad256(sizeof(int) * (n + 1)) * 2 + pad256(sizeof(int) * H.p_nnz) * 3 +
+                      pad256(sizeof(int) * (n1 + 1)) + pad256(sizeof(int) * H.ap_nnz);
+    const size_t vb = pad256(sizeof(float) * H.p_nnz) + pad256(sizeof(float) * H.ap_nnz);
+    if ((e = H.sa_ints.ensure(ib)) || (e = H.sa_vals.ensure(vb))) {
+      err = std::string("hierarchy allocation: ") + cudaGetErrorString(e);
+      H.release();
+      return FCG_ERR_CUDA;
+    }
+    char *p = (char *)H.sa_ints.p;
+    H.p_ptr = carve<int>(p, n + 1);
+    H.ap_ptr = carve<int>(p, n + 1);
+    H.p_col = carve<int>(p, H.p_nnz);
+    H.t_row = carve<int>(p, H.p_nnz);
+    H.t_pos = carve<int>(p, H.p_nnz);
+    H.t_ptr = carve<int>(p, n1 + 1);
+    H.ap_col = carve<int>(p, H.ap_nnz);
+    p = (char *)H.sa_vals.p;
+    H.p_val = carve<float>(p, H.p_nnz);
+    H.ap_val = carve<float>(p, H.ap_nnz);
+    if ((e = cudaMemcpy(H.p_ptr, h.p_ptr.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(H.ap_ptr, h.ap_ptr.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(H.p_col, h.p_col.data(), sizeof(int) * H.p_nnz, cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(H.t_row, h.t_row.data(), sizeof(int) * H.p_nnz, cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(H.t_pos, h.t_pos.data(), sizeof(int) * H.p_nnz, cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(H.t_ptr, h.t_ptr.data(), sizeof(int) * (n1 + 1), cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(H.ap_col, h.ap_col.data(), sizeof(int) * H.ap_nnz, cudaMemcpyHostToDevice))) {
+      err = std::string("hierarchy upload: ") + cudaGetErrorString(e);
+      H.release();
+      return FCG_ERR_CUDA;
+    }
+  }
+  H.smoothed = o.smoothed;
+  H.sa_omega = o.omega;
   if (!H.lv.empty()) {
     const int nl = H.lv.back().n;
     H.has_dense = nl <= dmax;
@@ -495,7 +701,15 @@ int values(Hierarchy &H, fcg_context *c, cudaStream_t st) {
   for (size_t l = 0; l < H.lv.size(); ++l) {
     DevLevel &L = H.lv[l];
     const int g = grid_for(32LL * L.n, ns, 8);
-    if (l == 0) {
+    if (l == 0 && H.smoothed) {
+      const int gn = grid_for(c->n, ns, 8);
+      k_sa_p<<<gn, kTPB, 0, st>>>(c->sv, c->n, scaled32(c), L.agg, H.p_ptr, H.p_col,
+                                  (float)H.sa_omega, H.p_val);
+      k_sa_ap<<<gn, kTPB, 0, st>>>(c->sv, c->n, scaled32(c), H.p_ptr, H.p_col, H.p_val, H.ap_ptr,
+                                   H.ap_col, H.ap_val);
+      k_sa_a1<<<g, kTPB, 0, st>>>(L.n, L.ptr, L.col, H.t_ptr, H.t_row, H.t_pos, H.p_val,
+                                  H.ap_ptr, H.ap_col, H.ap_val, L.a32, L.dinv);
+    } else if (l == 0) {
       k_ml_galerkin0<<<g, kTPB, 0, st>>>(L.n, L.ptr, L.col, L.mptr, L.mem, c->sv, c->n,
                                          scaled32(c), L.agg, L.a32, L.dinv);
     } else {
@@ -523,11 +737,10 @@ void enqueue_correction(Hierarchy &H, fcg_context *c, const Options &o, cudaStre
   if (H.lv.empty()) return;
   const int n = c->n, ns = c->num_sms;
   float *t = H.fine_tmp.as<float>();
-  DevLevel &L1 = H.lv[0];
   k_ml_resid0<<<grid_for(n, ns, 6), kTPB, 0, st>>>(c->sv, n, scaled32(c), r, z, t, done);
-  k_ml_restrict<<<grid_for(L1.n, ns, 8), kTPB, 0, st>>>(L1.n, L1.mptr, L1.mem, t, L1.b, done);
+  fine_restrict(H, ns, st, t, done);
   const float *e = enqueue_vcycle(H, ns, o, st, 0, done);
-  k_ml_prolong<<<grid_for(n, ns, 8), kTPB, 0, st>>>(n, L1.agg, e, z, (float)o.alpha, done);
+  fine_prolong(H, n, ns, o, st, e, z, done);
 }
 
 void enqueue_jacobi_cycle(Hierarchy &H, fcg_context *c, const Options &o, cudaStream_t st,
@@ -544,11 +757,10 @@ void enqueue_jacobi_cycle(Hierarchy &H, fcg_context *c, const Options &o, cudaSt
     std::swap(cur, oth);
   }
   if (!H.lv.empty()) {
-    DevLevel &L1 = H.lv[0];
     k_ml_resid0<<<gs, kTPB, 0, st>>>(c->sv, n, scaled32(c), r, cur, t, done);
-    k_ml_restrict<<<grid_for(L1.n, ns, 8), kTPB, 0, st>>>(L1.n, L1.mptr, L1.mem, t, L1.b, done);
+    fine_restrict(H, ns, st, t, done);
     const float *e = enqueue_vcycle(H, ns, o, st, 0, done);
-    k_ml_prolong<<<grid_for(n, ns, 8), kTPB, 0, st>>>(n, L1.agg, e, cur, (float)o.alpha, done);
+    fine_prolong(H, n, ns, o, st, e, cur, done);
   }
   for (int s = 0; s < o.sweeps; ++s) {
     k_ml_jac0<<<gs, kTPB, 0, st>>>(c->sv, n, scaled32(c), r, cur, oth, om, done);

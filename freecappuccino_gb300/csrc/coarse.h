@@ -26,6 +26,12 @@ struct HostLevel {
   int n = 0;
   std::vector<int> agg, mptr, mem;
   HostCsr A;
+  // first level with a smoothed prolongation P = (I - omega D^-1 A) P_tent: the pattern
+  // of P (p_ptr, p_col: the row's own aggregate and its neighbours' aggregates,
+  // ascending), its transpose (t_ptr, t_row, t_pos: for every aggregate the rows whose P
+  // row holds it, ascending, and the position in p_col), and the pattern of A P
+  // (ap_ptr, ap_col); A is then P^T A P
+  std::vector<int> p_ptr, p_col, t_ptr, t_row, t_pos, ap_ptr, ap_col;
 };
 
 // One pass of pairwise matching on (ptr, col, val); returns the number of aggregates.
@@ -39,7 +45,9 @@ void galerkin(const HostCsr &A, const std::vector<int> &agg, int nc, const std::
 // Levels below `fine`: `passes` matching passes per level, until a level has at most
 // dense_max rows, stops coarsening, or max_levels levels (the fine one included) exist.
 int build_levels(const HostCsr &fine, int max_levels, int dense_max, int passes,
-                 std::vector<HostLevel> &levels);
+                 std::vector<HostLevel> &levels, double sa_omega = 0.0);
+// The smoothed first level (sa_omega > 0 in build_levels): patterns and FP64 values.
+void smoothed_level(const HostCsr &A, double omega, HostLevel &lv);
 
 // Options of the correction (fcg_lp_set_multilevel).
 struct Options {
@@ -48,8 +56,9 @@ struct Options {
   int sweeps = 2;    // Jacobi sweeps before and after each coarse level's correction
   int max_levels = 10;
   int dense_max = 128;
-  double alpha = 1.8;  // scaling of every prolongated correction
-  double omega = 0.67; // Jacobi damping
+  double alpha = 1.8;  // scaling of every unsmoothed prolongated correction
+  double omega = 0.67; // Jacobi damping, and the prolongation smoothing of the first level
+  int smoothed = 1;    // first level: smoothed prolongation (correction not scaled)
 };
 
 // Device arrays of one coarse level.
@@ -66,7 +75,14 @@ struct Hierarchy {
   unsigned long long uid = 0;  // context and bind the hierarchy belongs to
   unsigned gen = 0;
   int n0 = 0;
-  int passes = 3, max_levels = 10, dense_max = 128;
+  int passes = 3, max_levels = 10, dense_max = 128, smoothed = 1;
+  double sa_omega = 0.0;
+  // smoothed first level: P (p_ptr, p_col, p_val), its transpose lists, A P
+  DBuf sa_ints, sa_vals;
+  int *p_ptr = nullptr, *p_col = nullptr, *t_ptr = nullptr, *t_row = nullptr, *t_pos = nullptr;
+  int *ap_ptr = nullptr, *ap_col = nullptr;
+  float *p_val = nullptr, *ap_val = nullptr;
+  long long p_nnz = 0, ap_nnz = 0;
   std::vector<DevLevel> lv;     // levels 1..L (lv[0] is level 1)
   DBuf dense;                   // inverse of the coarsest matrix (row-major)
   bool has_dense = false;
@@ -75,7 +91,8 @@ struct Hierarchy {
   unsigned long long build_id = 0;  // bumped at every build (keys captured graphs)
   bool built_for(const fcg_context *c, const struct Options &o) const {
     return uid == c->uid && gen == c->bind_gen && max_levels == o.max_levels &&
-           dense_max == o.dense_max;
+           dense_max == o.dense_max && smoothed == o.smoothed &&
+           (!smoothed || sa_omega == o.omega);
   }
   void release();
 };

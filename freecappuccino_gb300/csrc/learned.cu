@@ -1837,7 +1837,8 @@ int build_fcg_graph(fcg_learned *Lp, fcg_context *c, const FcgVecs &v) {
                                    (const void *)(uintptr_t)Lp->mlo.smoother,
                                    (const void *)(uintptr_t)Lp->mlo.sweeps,
                                    (const void *)(uintptr_t)(Lp->mlo.alpha * 1e6),
-                                   (const void *)(uintptr_t)(Lp->mlo.omega * 1e6)};
+                                   (const void *)(uintptr_t)(Lp->mlo.omega * 1e6),
+                                   (const void *)(uintptr_t)Lp->mlo.smoothed};
   if (Lp->exec && key == Lp->graph_key) return FCG_OK;
   if (Lp->exec) cudaGraphExecDestroy(Lp->exec);
   if (Lp->graph) cudaGraphDestroy(Lp->graph);
@@ -2037,7 +2038,7 @@ extern "C" int fcg_lp_set_multilevel(fcg_learned *Lp, const fcg_lp_multilevel *o
       (o->smoother != FCG_LP_SMOOTH_NETWORK && o->smoother != FCG_LP_SMOOTH_JACOBI) ||
       o->sweeps < 1 || o->sweeps > 8 || o->max_levels < 2 || o->max_levels > FCG_LP_MAX_LEVELS ||
       o->dense_max < 1 || o->dense_max > 160 || !(o->alpha > 0.0 && o->alpha < 4.0) ||
-      !(o->omega > 0.0 && o->omega < 2.0))
+      !(o->omega > 0.0 && o->omega < 2.0) || (o->smoothed != 0 && o->smoothed != 1))
     return lp_fail(Lp, FCG_ERR_ARG, "multilevel option out of range");
   Lp->mlo.enabled = o->enabled;
   Lp->mlo.smoother = o->smoother;
@@ -2046,6 +2047,7 @@ extern "C" int fcg_lp_set_multilevel(fcg_learned *Lp, const fcg_lp_multilevel *o
   Lp->mlo.dense_max = o->dense_max;
   Lp->mlo.alpha = o->alpha;
   Lp->mlo.omega = o->omega;
+  Lp->mlo.smoothed = o->smoothed;
   return FCG_OK;
 }
 
@@ -2058,6 +2060,7 @@ extern "C" int fcg_lp_get_multilevel(const fcg_learned *Lp, fcg_lp_multilevel *o
   o->dense_max = Lp->mlo.dense_max;
   o->alpha = Lp->mlo.alpha;
   o->omega = Lp->mlo.omega;
+  o->smoothed = Lp->mlo.smoothed;
   return FCG_OK;
 }
 

@@ -178,19 +178,19 @@ class LearnedPreconditioner:
     def set_multilevel(self, enabled: bool | None = None, smoother: str | None = None,
                        sweeps: int | None = None, max_levels: int | None = None,
                        dense_max: int | None = None, alpha: float | None = None,
-                       omega: float | None = None):
+                       omega: float | None = None, smoothed: bool | None = None):
         """Changes the given options of the coarse-grid correction; smoother is "network"
         (the default) or "jacobi" (the same cycle without the network)."""
         cur = self.multilevel
         new = dict(enabled=enabled, smoother=smoother, sweeps=sweeps, max_levels=max_levels,
-                   dense_max=dense_max, alpha=alpha, omega=omega)
+                   dense_max=dense_max, alpha=alpha, omega=omega, smoothed=smoothed)
         for k, v in new.items():
             if v is not None:
                 cur[k] = v
         o = _lib.Multilevel(int(bool(cur["enabled"])),
                             {"network": _lib.SMOOTH_NETWORK, "jacobi": _lib.SMOOTH_JACOBI}[cur["smoother"]],
                             int(cur["sweeps"]), int(cur["max_levels"]), int(cur["dense_max"]),
-                            float(cur["alpha"]), float(cur["omega"]))
+                            float(cur["alpha"]), float(cur["omega"]), int(bool(cur["smoothed"])))
         self._check(self.lib.fcg_lp_set_multilevel(self.h, C.byref(o)), "fcg_lp_set_multilevel")
 
     def hierarchy(self, ctx: Context) -> dict:

@@ -554,7 +554,10 @@ int fcg_lp_profile(fcg_learned *lp, fcg_context *ctx, const float *r, int reps, 
  * aggregation is built on the host once per mesh, from the first matrix solved (or set)
  * on it; the level matrices P^T Ahat P are recomputed on the device at every call.
  * smoother FCG_LP_SMOOTH_JACOBI replaces N by `sweeps` Jacobi sweeps before and after
- * the correction (the same cycle without the network).  FP32 throughout. */
+ * the correction (the same cycle without the network).  With `smoothed` (default) the
+ * first level uses the smoothed prolongation P = (I - omega D^-1 Ahat) P_tent of the
+ * piecewise-constant P_tent, its level matrix is P^T Ahat P, and its correction is not
+ * scaled by alpha (smoothed aggregation).  FP32 throughout. */
 #define FCG_LP_SMOOTH_NETWORK 0
 #define FCG_LP_SMOOTH_JACOBI 1
 #define FCG_LP_MAX_LEVELS 16
@@ -564,8 +567,9 @@ typedef struct fcg_lp_multilevel {
   int sweeps;     /* 1..8, default 2 */
   int max_levels; /* 2..FCG_LP_MAX_LEVELS levels counting the fine one, default 10 */
   int dense_max;  /* 1..160, default 128 */
-  double alpha;   /* (0, 4), default 1.8 */
+  double alpha;   /* (0, 4), default 1.8: scaling of every unsmoothed prolongation */
   double omega;   /* (0, 2), default 0.67 */
+  int smoothed;   /* 1 (default) or 0: the first level's prolongation P_tent */
 } fcg_lp_multilevel;
 int fcg_lp_set_multilevel(fcg_learned *lp, const fcg_lp_multilevel *opt);
 int fcg_lp_get_multilevel(const fcg_learned *lp, fcg_lp_multilevel *opt);

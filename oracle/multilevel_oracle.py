@@ -22,7 +22,11 @@ the restatement itself against scipy's sparse products and a CG it preconditions
   (FP32((a_ij s_i) s_j), s = 1/sqrt(a_ii)), level l + 1 of level l's device values,
   all with the composite aggregation of the level and the summation order above, every
   sum rounded to FP32 (bit-exact with the GPU).
-* Correction: out = z + alpha P V(P^T (r - Ahat z)), V as in coarse.cu.
+* Smoothed first level (the default): P = (I - omega D^-1 Ahat) P_tent, its pattern the
+  row's own and its neighbours' aggregates; A P and P^T A P summed in the documented
+  orders (host FP64, device FP32 with every product and sum rounded).
+* Correction: out = z + alpha P V(P^T (r - Ahat z)), V as in coarse.cu (alpha = 1 for
+  the smoothed P).
 """
 from __future__ import annotations
 
@@ -121,8 +125,120 @@ def galerkin(ptr, col, val, agg, nc, mptr, mem, f32=False):
             np.array(oval, np.float32 if f32 else np.float64))
 
 
-def build_levels(ptr, col, val, max_levels=10, dense_max=128, passes=3):
-    """Levels below (ptr, col, val): dicts with n, agg, mptr, mem, ptr, col, hval."""
+def smoothed_level(ptr, col, val, agg, nc, omega):
+    """P = (I - omega D^-1 A) P_tent, A P and P^T A P of the first level in FP64, in the
+    host's order; returns the pattern dict (p_ptr, p_col, t_ptr, t_row, t_pos, ap_ptr,
+    ap_col) and (ptr, col, val) of P^T A P."""
+    n = len(ptr) - 1
+    ptr_l, col_l, val_l, agg_l = ptr.tolist(), col.tolist(), val.tolist(), list(agg)
+    p_ptr, p_col, pv = [0], [], []
+    for i in range(n):
+        ks = range(ptr_l[i], ptr_l[i + 1])
+        row = sorted({agg_l[i]} | {agg_l[col_l[k]] for k in ks})
+        b = len(p_col)
+        d = 0.0
+        for k in ks:
+            if col_l[k] == i:
+                d = val_l[k]
+        w = omega / d if d > 0.0 else 0.0
+        p_col += row
+        pv += [1.0 if J == agg_l[i] else 0.0 for J in row]
+        for k in ks:
+            q = b + row.index(agg_l[col_l[k]])
+            pv[q] = pv[q] - w * val_l[k]
+        p_ptr.append(len(p_col))
+    t_lists = [[] for _ in range(nc)]
+    for i in range(n):
+        for q in range(p_ptr[i], p_ptr[i + 1]):
+            t_lists[p_col[q]].append((i, q))
+    t_ptr = np.cumsum([0] + [len(t) for t in t_lists])
+    t_row = [i for t in t_lists for i, _ in t]
+    t_pos = [q for t in t_lists for _, q in t]
+    ap_ptr, ap_col, apv = [0], [], []
+    for i in range(n):
+        ks = range(ptr_l[i], ptr_l[i + 1])
+        row = sorted({p_col[q] for k in ks for q in range(p_ptr[col_l[k]], p_ptr[col_l[k] + 1])})
+        b = len(ap_col)
+        ap_col += row
+        apv += [0.0] * len(row)
+        for k in ks:
+            j = col_l[k]
+            for q in range(p_ptr[j], p_ptr[j + 1]):
+                x = b + row.index(p_col[q])
+                apv[x] = apv[x] + val_l[k] * pv[q]
+        ap_ptr.append(len(ap_col))
+    optr, ocol, oval = [0], [], []
+    for I in range(nc):
+        slot, cols, vals = {}, [], []
+        for m in range(t_ptr[I], t_ptr[I + 1]):
+            i, p = t_row[m], pv[t_pos[m]]
+            for q in range(ap_ptr[i], ap_ptr[i + 1]):
+                J = ap_col[q]
+                if J in slot:
+                    vals[slot[J]] += p * apv[q]
+                else:
+                    slot[J] = len(cols)
+                    cols.append(J)
+                    vals.append(p * apv[q])
+        order = sorted(range(len(cols)), key=lambda q: cols[q])
+        ocol += [cols[q] for q in order]
+        oval += [vals[q] for q in order]
+        optr.append(len(ocol))
+    pat = dict(p_ptr=np.array(p_ptr), p_col=np.array(p_col), t_ptr=np.asarray(t_ptr),
+               t_row=np.array(t_row), t_pos=np.array(t_pos), ap_ptr=np.array(ap_ptr),
+               ap_col=np.array(ap_col), p_val64=np.array(pv))
+    return pat, (np.array(optr, np.int64), np.array(ocol, np.int64), np.array(oval))
+
+
+def smoothed_values32(pat, fine32, agg, level, omega):
+    """The device's FP32 values of the smoothed first level: P, A P and P^T A P, every
+    product and sum rounded to FP32 in the host's order; returns (p_val, a1)."""
+    f = np.float32
+    ptr, col, val = fine32
+    ptr_l, col_l = ptr.tolist(), col.tolist()
+    val_l = list(np.asarray(val, np.float32))
+    n = len(ptr) - 1
+    om = f(omega)
+    p_ptr, p_col = pat["p_ptr"].tolist(), pat["p_col"].tolist()
+    pv = [f(0)] * len(p_col)
+    for i in range(n):
+        ks = range(ptr_l[i], ptr_l[i + 1])
+        d = f(0)
+        for k in ks:
+            if col_l[k] == i:
+                d = val_l[k]
+        w = om / d if d > f(0) else f(0)
+        row = p_col[p_ptr[i]:p_ptr[i + 1]]
+        for q in range(p_ptr[i], p_ptr[i + 1]):
+            pv[q] = f(1) if p_col[q] == agg[i] else f(0)
+        for k in ks:
+            q = p_ptr[i] + row.index(agg[col_l[k]])
+            pv[q] = pv[q] - w * val_l[k]
+    ap_ptr, ap_col = pat["ap_ptr"].tolist(), pat["ap_col"].tolist()
+    apv = [f(0)] * len(ap_col)
+    for i in range(n):
+        row = ap_col[ap_ptr[i]:ap_ptr[i + 1]]
+        for k in range(ptr_l[i], ptr_l[i + 1]):
+            j = col_l[k]
+            for q in range(p_ptr[j], p_ptr[j + 1]):
+                x = ap_ptr[i] + row.index(p_col[q])
+                apv[x] = apv[x] + val_l[k] * pv[q]
+    t_ptr, t_row, t_pos = pat["t_ptr"].tolist(), pat["t_row"].tolist(), pat["t_pos"].tolist()
+    cptr, ccol = level["ptr"].tolist(), level["col"].tolist()
+    a1 = [f(0)] * len(ccol)
+    for I in range(len(cptr) - 1):
+        pos = {J: q for q, J in enumerate(ccol[cptr[I]:cptr[I + 1]], start=cptr[I])}
+        for m in range(t_ptr[I], t_ptr[I + 1]):
+            i, p = t_row[m], pv[t_pos[m]]
+            for q in range(ap_ptr[i], ap_ptr[i + 1]):
+                x = pos[ap_col[q]]
+                a1[x] = a1[x] + p * apv[q]
+    return np.array(pv, np.float32), np.array(a1, np.float32)
+
+
+def build_levels(ptr, col, val, max_levels=10, dense_max=128, passes=3, sa_omega=0.67):
+    """Levels below (ptr, col, val): dicts with n, agg, mptr, mem, ptr, col, hval, and for
+    a smoothed first level (sa_omega > 0) the pattern dict "sa"."""
     levels = []
     cur = (ptr, col, val)
     while len(levels) + 1 < max_levels:
@@ -145,20 +261,33 @@ def build_levels(ptr, col, val, max_levels=10, dense_max=128, passes=3):
         if nc == n0 or 10 * nc > 9 * n0:
             break
         mp, me = members(comp, nc)
-        levels.append(dict(n=nc, agg=comp, mptr=mp, mem=me, ptr=a[0], col=a[1], hval=a[2]))
+        lv = dict(n=nc, agg=comp, mptr=mp, mem=me, ptr=a[0], col=a[1], hval=a[2])
+        if not levels and sa_omega > 0:
+            lv["sa"], a = smoothed_level(*cur, comp, nc, sa_omega)
+            lv["ptr"], lv["col"], lv["hval"] = a
+        levels.append(lv)
         cur = a
         if nc <= dense_max:
             break
     return levels
 
 
-def level_values(levels, fine, f32=True):
+def level_values(levels, fine, f32=True, omega=0.67):
     """Values of every level as the device computes them: level 1 from the fine scaled
     matrix rounded to FP32, each level from the one above, FP32 sums in order (f32=False:
-    the same products in FP64 from the fine values as given)."""
+    the same products in FP64 from the fine values as given).  A smoothed first level
+    also gets its FP32 (or FP64) prolongation values in levels[0]["p_val"]."""
     out = []
     above = (fine[0], fine[1], np.asarray(fine[2], np.float32 if f32 else np.float64))
     for lv in levels:
+        if "sa" in lv:
+            if f32:
+                lv["p_val"], v = smoothed_values32(lv["sa"], above, lv["agg"], lv, omega)
+            else:
+                lv["p_val"], v = lv["sa"]["p_val64"], lv["hval"]
+            out.append(v)
+            above = (lv["ptr"], lv["col"], v)
+            continue
         _, _, v = galerkin(*above, lv["agg"], lv["n"], lv["mptr"], lv["mem"], f32=f32)
         out.append(v)
         above = (lv["ptr"], lv["col"], v)
@@ -197,8 +326,24 @@ class Cycle:
     def _restrict(self, k, t):
         lv = self.levels[k]
         bc = np.zeros(lv["n"])
-        np.add.at(bc, lv["agg"], t)
+        if "sa" in lv:
+            sa = lv["sa"]
+            rows = np.repeat(np.arange(len(t)), np.diff(sa["p_ptr"]))
+            np.add.at(bc, sa["p_col"], np.asarray(lv["p_val"], np.float64) * t[rows])
+        else:
+            np.add.at(bc, lv["agg"], t)
         return bc
+
+    def _prolong(self, k, e):
+        """(P e, scale): the smoothed P (not scaled) or the aggregation (alpha)."""
+        lv = self.levels[k]
+        if "sa" in lv:
+            sa = lv["sa"]
+            rows = np.repeat(np.arange(len(lv["agg"])), np.diff(sa["p_ptr"]))
+            out = np.zeros(len(lv["agg"]))
+            np.add.at(out, rows, np.asarray(lv["p_val"], np.float64) * e[sa["p_col"]])
+            return out, 1.0
+        return e[lv["agg"]], self.alpha
 
     def vcycle(self, k, b):
         A, dinv = self.mats[k], self.dinv[k]
@@ -226,7 +371,8 @@ class Cycle:
             return z.copy()
         t = r - _spmv(*self.fine, z)
         e = self.vcycle(0, self._restrict(0, t))
-        return z + self.alpha * e[self.levels[0]["agg"]]
+        pe, a = self._prolong(0, e)
+        return z + a * pe
 
     def jacobi_cycle(self, r):
         """The same cycle with Jacobi sweeps (unit diagonal) in place of the network."""
@@ -241,9 +387,11 @@ class Cycle:
         return z
 
 
-def hierarchy(ioffset, ja, diag, a, max_levels=10, dense_max=128, passes=3, **cycle):
+def hierarchy(ioffset, ja, diag, a, max_levels=10, dense_max=128, passes=3, sa_omega=0.67,
+              **cycle):
     """Everything for one scaled matrix: (fine csr, levels, device values, Cycle)."""
     fine = scaled_csr(ioffset, ja, diag, a)
-    levels = build_levels(*fine, max_levels=max_levels, dense_max=dense_max, passes=passes)
-    values = level_values(levels, fine)
+    levels = build_levels(*fine, max_levels=max_levels, dense_max=dense_max, passes=passes,
+                          sa_omega=sa_omega)
+    values = level_values(levels, fine, omega=sa_omega)
     return fine, levels, values, Cycle(fine, levels, values, dense_max=dense_max, **cycle)

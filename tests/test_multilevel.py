@@ -47,13 +47,24 @@ def test_oracle_galerkin_is_ptap(name):
     above = _scipy(*fine)
     for lv, v in zip(levels, vals):
         n0 = above.shape[0]
-        P = sp.csr_matrix((np.ones(n0), (np.arange(n0), lv["agg"])), shape=(n0, lv["n"]))
+        if "sa" in lv:  # the smoothed first level: P = (I - omega D^-1 A) P_tent
+            Pt = sp.csr_matrix((np.ones(n0), (np.arange(n0), lv["agg"])), shape=(n0, lv["n"]))
+            P = (Pt - 0.67 * sp.diags(1.0 / above.diagonal()) @ (above @ Pt)).tocsr()
+            P.sort_indices()
+            sa = lv["sa"]
+            Pg = sp.csr_matrix((sa["p_val64"], sa["p_col"], sa["p_ptr"]), shape=P.shape)
+            assert abs(Pg - P).max() <= 1e-15 * abs(P).max()
+            assert np.abs(lv["p_val"] - sa["p_val64"]).max() <= 1e-6
+            tol32 = 2e-5  # FP32 P, A P and P^T A P
+        else:
+            P = sp.csr_matrix((np.ones(n0), (np.arange(n0), lv["agg"])), shape=(n0, lv["n"]))
+            tol32 = 2e-6
         ref = (P.T @ above @ P).tocsr()
         ref.sort_indices()
         got = _scipy(lv["ptr"], lv["col"], v.astype(np.float64))
         assert np.array_equal(ref.indptr, got.indptr) and np.array_equal(ref.indices, got.indices)
         # device values: FP32 sums of the FP32-rounded fine matrix
-        assert np.abs(ref.data - got.data).max() <= 2e-6 * np.abs(ref.data).max()
+        assert np.abs(ref.data - got.data).max() <= tol32 * np.abs(ref.data).max()
         # the host values that steered the matching: the same product in FP64
         assert np.abs(lv["hval"] - ref.data).max() <= 1e-14 * np.abs(ref.data).max()
         above = _scipy(lv["ptr"], lv["col"], lv["hval"])
@@ -268,7 +279,7 @@ def test_multilevel_options():
     lp = LearnedPreconditioner()
     d = lp.multilevel
     assert d == dict(enabled=1, smoother="network", sweeps=2, max_levels=10, dense_max=128,
-                     alpha=1.8, omega=0.67)
+                     alpha=1.8, omega=0.67, smoothed=1)
     for bad in (dict(sweeps=0), dict(sweeps=9), dict(max_levels=1), dict(max_levels=17),
                 dict(dense_max=0), dict(dense_max=161), dict(alpha=0.0), dict(alpha=4.0),
                 dict(omega=0.0), dict(omega=2.0)):
