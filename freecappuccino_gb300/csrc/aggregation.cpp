@@ -15,9 +15,72 @@
 #include <vector>
 
 #include "coarse.h"
+#include "host_util.h"
 
 namespace fcg {
 namespace ml {
+
+namespace {
+// Builds a CSR row by row on all host threads: row(i, cols, vals) appends row i to the
+// thread's vectors (its own contiguous block of rows); the blocks are joined in order,
+// so the result does not depend on the thread count.
+template <class RowFn>
+void chunked_csr(int n, std::vector<int> &ptr, std::vector<int> &col, std::vector<double> *val,
+                 RowFn &&row) {
+  const unsigned nt = n < (1 << 14) ? 1u : std::max(1u, std::thread::hardware_concurrency());
+  const long long chunk = ((long long)n + nt - 1) / nt;
+  std::vector<std::vector<int>> cols(nt), lens(nt);
+  std::vector<std::vector<double>> vals(nt);
+  parallel_for(
+      nt,
+      [&](long long t) {
+        const long long b = t * chunk, e = std::min<long long>(n, b + chunk);
+        for (long long i = b; i < e; ++i) {
+          const size_t before = cols[t].size();
+          row((int)i, cols[t], vals[t]);
+          lens[t].push_back((int)(cols[t].size() - before));
+        }
+      },
+      1);
+  ptr.assign(n + 1, 0);
+  std::vector<long long> off(nt + 1, 0);
+  for (unsigned t = 0; t < nt; ++t) off[t + 1] = off[t] + (long long)cols[t].size();
+  col.resize(off[nt]);
+  if (val) val->resize(off[nt]);
+  long long r = 0;
+  for (unsigned t = 0; t < nt; ++t)
+    for (int L : lens[t]) {
+      ptr[r + 1] = ptr[r] + L;
+      ++r;
+    }
+  parallel_for(
+      nt,
+      [&](long long t) {
+        std::copy(cols[t].begin(), cols[t].end(), col.begin() + off[t]);
+        if (val) std::copy(vals[t].begin(), vals[t].end(), val->begin() + off[t]);
+      },
+      1);
+}
+
+// Sums (column, value) pairs met in order into one entry per column, columns ascending;
+// each column's values are added in the order met.
+void merge_row(std::vector<std::pair<int, double>> &ent, std::vector<int> &cols,
+               std::vector<double> &vals) {
+  std::stable_sort(ent.begin(), ent.end(),
+                   [](const std::pair<int, double> &a, const std::pair<int, double> &b) {
+                     return a.first < b.first;
+                   });
+  for (size_t q = 0; q < ent.size();) {
+    const int J = ent[q].first;
+    double acc = ent[q].second;
+    size_t r = q + 1;
+    for (; r < ent.size() && ent[r].first == J; ++r) acc += ent[r].second;
+    cols.push_back(J);
+    vals.push_back(acc);
+    q = r;
+  }
+}
+}  // namespace
 
 int pair_match(int n, const int *ptr, const int *col, const double *val, std::vector<int> &agg) {
   agg.assign(n, -1);
@@ -85,42 +148,17 @@ void members(int n, int nc, const std::vector<int> &agg, std::vector<int> &mptr,
 void galerkin(const HostCsr &A, const std::vector<int> &agg, int nc, const std::vector<int> &mptr,
               const std::vector<int> &mem, HostCsr &out) {
   out.n = nc;
-  out.ptr.assign(nc + 1, 0);
-  out.col.clear();
-  out.val.clear();
-  out.col.reserve(A.col.size() / 2 + nc);
-  out.val.reserve(A.col.size() / 2 + nc);
-  std::vector<int> marker(nc, -1);
-  std::vector<std::pair<int, double>> row;
-  for (int I = 0; I < nc; ++I) {
-    const int start = (int)out.col.size();
-    for (int m = mptr[I]; m < mptr[I + 1]; ++m) {
-      const int i = mem[m];
-      for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
-        const int J = agg[A.col[k]];
-        const int p = marker[J];
-        if (p >= start) {
-          out.val[p] += A.val[k];
-        } else {
-          marker[J] = (int)out.col.size();
-          out.col.push_back(J);
-          out.val.push_back(A.val[k]);
-        }
-      }
-    }
-    const int end = (int)out.col.size();
-    row.clear();
-    for (int p = start; p < end; ++p) row.emplace_back(out.col[p], out.val[p]);
-    std::sort(row.begin(), row.end(),
-              [](const std::pair<int, double> &a, const std::pair<int, double> &b) {
-                return a.first < b.first;
+  chunked_csr(nc, out.ptr, out.col, &out.val,
+              [&](int I, std::vector<int> &cols, std::vector<double> &vals) {
+                thread_local std::vector<std::pair<int, double>> ent;
+                ent.clear();
+                for (int m = mptr[I]; m < mptr[I + 1]; ++m) {
+                  const int i = mem[m];
+                  for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k)
+                    ent.emplace_back(agg[A.col[k]], A.val[k]);
+                }
+                merge_row(ent, cols, vals);
               });
-    for (int p = start; p < end; ++p) {
-      out.col[p] = row[p - start].first;
-      out.val[p] = row[p - start].second;
-    }
-    out.ptr[I + 1] = end;
-  }
 }
 
 // P = (I - omega D^-1 A) P_tent of the level's aggregation, A P and P^T A P, patterns
@@ -131,35 +169,30 @@ void galerkin(const HostCsr &A, const std::vector<int> &agg, int nc, const std::
 void smoothed_level(const HostCsr &A, double omega, HostLevel &lv) {
   const int n = A.n, nc = lv.n;
   const std::vector<int> &agg = lv.agg;
-  std::vector<int> marker(std::max(n, nc), -1);
-  // P pattern and values
-  lv.p_ptr.assign(n + 1, 0);
-  lv.p_col.clear();
+  // P: pattern and values
   std::vector<double> pv;
-  std::vector<int> row;
-  for (int i = 0; i < n; ++i) {
+  chunked_csr(n, lv.p_ptr, lv.p_col, &pv, [&](int i, std::vector<int> &cols, std::vector<double> &vals) {
+    thread_local std::vector<int> row;
     row.clear();
     row.push_back(agg[i]);
     for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) row.push_back(agg[A.col[k]]);
     std::sort(row.begin(), row.end());
     row.erase(std::unique(row.begin(), row.end()), row.end());
-    const int b = (int)lv.p_col.size();
+    const size_t b = cols.size();
     double d = 0.0;
     for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k)
       if (A.col[k] == i) d = A.val[k];
     const double w = d > 0.0 ? omega / d : 0.0;
     for (int J : row) {
-      lv.p_col.push_back(J);
-      pv.push_back(J == agg[i] ? 1.0 : 0.0);
+      cols.push_back(J);
+      vals.push_back(J == agg[i] ? 1.0 : 0.0);
     }
     for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
-      const int J = agg[A.col[k]];
-      const int p = b + (int)(std::lower_bound(row.begin(), row.end(), J) - row.begin());
-      pv[p] -= w * A.val[k];
+      const size_t p = b + (std::lower_bound(row.begin(), row.end(), agg[A.col[k]]) - row.begin());
+      vals[p] -= w * A.val[k];
     }
-    lv.p_ptr[i + 1] = (int)lv.p_col.size();
-  }
-  // transpose lists
+  });
+  // transpose lists: rows ascending within every aggregate
   lv.t_ptr.assign(nc + 1, 0);
   for (int J : lv.p_col) ++lv.t_ptr[J + 1];
   for (int I = 0; I < nc; ++I) lv.t_ptr[I + 1] += lv.t_ptr[I];
@@ -174,69 +207,31 @@ void smoothed_level(const HostCsr &A, double omega, HostLevel &lv) {
         lv.t_pos[f] = p;
       }
   }
-  // A P
-  lv.ap_ptr.assign(n + 1, 0);
-  lv.ap_col.clear();
+  // A P: for the row's entries in column order, a_ik P_k in P_k's order
   std::vector<double> apv;
-  for (int i = 0; i < n; ++i) {
-    row.clear();
+  chunked_csr(n, lv.ap_ptr, lv.ap_col, &apv, [&](int i, std::vector<int> &cols, std::vector<double> &vals) {
+    thread_local std::vector<std::pair<int, double>> ent;
+    ent.clear();
     for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
       const int j = A.col[k];
-      for (int p = lv.p_ptr[j]; p < lv.p_ptr[j + 1]; ++p) row.push_back(lv.p_col[p]);
+      for (int p = lv.p_ptr[j]; p < lv.p_ptr[j + 1]; ++p)
+        ent.emplace_back(lv.p_col[p], A.val[k] * pv[p]);
     }
-    std::sort(row.begin(), row.end());
-    row.erase(std::unique(row.begin(), row.end()), row.end());
-    const int b = (int)lv.ap_col.size();
-    for (int J : row) {
-      lv.ap_col.push_back(J);
-      apv.push_back(0.0);
-    }
-    for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
-      const int j = A.col[k];
-      for (int p = lv.p_ptr[j]; p < lv.p_ptr[j + 1]; ++p) {
-        const int q = b + (int)(std::lower_bound(row.begin(), row.end(), lv.p_col[p]) - row.begin());
-        apv[q] += A.val[k] * pv[p];
-      }
-    }
-    lv.ap_ptr[i + 1] = (int)lv.ap_col.size();
-  }
-  // P^T A P
+    merge_row(ent, cols, vals);
+  });
+  // P^T A P: for the rows holding the aggregate in ascending order, P_iI (A P)_i
   HostCsr &C = lv.A;
   C.n = nc;
-  C.ptr.assign(nc + 1, 0);
-  C.col.clear();
-  C.val.clear();
-  std::fill(marker.begin(), marker.end(), -1);
-  std::vector<std::pair<int, double>> sr;
-  for (int I = 0; I < nc; ++I) {
-    const int start = (int)C.col.size();
+  chunked_csr(nc, C.ptr, C.col, &C.val, [&](int I, std::vector<int> &cols, std::vector<double> &vals) {
+    thread_local std::vector<std::pair<int, double>> ent;
+    ent.clear();
     for (int m = lv.t_ptr[I]; m < lv.t_ptr[I + 1]; ++m) {
       const int i = lv.t_row[m];
       const double p = pv[lv.t_pos[m]];
-      for (int q = lv.ap_ptr[i]; q < lv.ap_ptr[i + 1]; ++q) {
-        const int J = lv.ap_col[q];
-        if (marker[J] >= start) {
-          C.val[marker[J]] += p * apv[q];
-        } else {
-          marker[J] = (int)C.col.size();
-          C.col.push_back(J);
-          C.val.push_back(p * apv[q]);
-        }
-      }
+      for (int q = lv.ap_ptr[i]; q < lv.ap_ptr[i + 1]; ++q) ent.emplace_back(lv.ap_col[q], p * apv[q]);
     }
-    const int end = (int)C.col.size();
-    sr.clear();
-    for (int q = start; q < end; ++q) sr.emplace_back(C.col[q], C.val[q]);
-    std::sort(sr.begin(), sr.end(),
-              [](const std::pair<int, double> &a, const std::pair<int, double> &b) {
-                return a.first < b.first;
-              });
-    for (int q = start; q < end; ++q) {
-      C.col[q] = sr[q - start].first;
-      C.val[q] = sr[q - start].second;
-    }
-    C.ptr[I + 1] = end;
-  }
+    merge_row(ent, cols, vals);
+  });
 }
 
 int build_levels(const HostCsr &fine, int max_levels, int dense_max, int passes,

@@ -389,9 +389,13 @@ __global__ void __launch_bounds__(kTPB)
       if (c < 0) continue;
       for (int p = p_ptr[c]; p < p_ptr[c + 1]; ++p) {
         const int J = p_col[p];
-        int q = qb;
-        while (q < qe - 1 && ap_col[q] != J) ++q;
-        ap_val[q] = __fadd_rn(ap_val[q], __fmul_rn(v, p_val[p]));
+        int lo = qb, hi = qe - 1;  // the row's columns ascend; J is among them
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (ap_col[mid] < J) lo = mid + 1;
+          else hi = mid;
+        }
+        ap_val[lo] = __fadd_rn(ap_val[lo], __fmul_rn(v, p_val[p]));
       }
     }
   }
@@ -411,10 +415,10 @@ __global__ void __launch_bounds__(kTPB)
   for (long long I = warp; I < nc; I += nwarps) {
     const int cb = cptr[I], ce = cptr[I + 1];
     const int mb = t_ptr[I], me = t_ptr[I + 1];
-    for (int sb = cb; sb < ce; sb += 32) {
-      const int my = sb + lane;
-      const int mycol = my < ce ? ccol[my] : -1;
-      float acc = 0.f;
+    for (int sb = cb; sb < ce; sb += 64) {  // two coarse entries per lane
+      const int my0 = sb + lane, my1 = sb + 32 + lane;
+      const int c0 = my0 < ce ? ccol[my0] : -1, c1 = my1 < ce ? ccol[my1] : -1;
+      float acc0 = 0.f, acc1 = 0.f;
       for (int m = mb; m < me; ++m) {
         const int i = t_row[m];
         const float p = p_val[t_pos[m]];
@@ -431,13 +435,18 @@ __global__ void __launch_bounds__(kTPB)
           for (int e = 0; e < cnt; ++e) {
             const int Je = __shfl_sync(0xffffffffu, J, e);
             const float ve = __shfl_sync(0xffffffffu, v, e);
-            if (Je == mycol) acc = __fadd_rn(acc, ve);
+            if (Je == c0) acc0 = __fadd_rn(acc0, ve);
+            else if (Je == c1) acc1 = __fadd_rn(acc1, ve);
           }
         }
       }
-      if (my < ce) {
-        a[my] = acc;
-        if (mycol == (int)I) dinv[I] = acc > 0.f ? 1.f / acc : 0.f;
+      if (my0 < ce) {
+        a[my0] = acc0;
+        if (c0 == (int)I) dinv[I] = acc0 > 0.f ? 1.f / acc0 : 0.f;
+      }
+      if (my1 < ce) {
+        a[my1] = acc1;
+        if (c1 == (int)I) dinv[I] = acc1 > 0.f ? 1.f / acc1 : 0.f;
       }
     }
   }
