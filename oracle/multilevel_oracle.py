@@ -16,8 +16,9 @@ the restatement itself against scipy's sparse products and a CG it preconditions
   and the aggregates are renumbered in their order.  Between passes the matrix is
   P^T A P summed in a fixed order: member rows ascending, each member row's entries in
   column order, each entry added to the slot of its coarse column in the order the
-  slots are first met; rows then sorted by column.  A pass that pairs nothing ends the level; a level with more than 90% of the
-  rows above it is dropped; a level with at most dense_max rows is the coarsest.
+  slots are first met; rows then sorted by column.  A pass that pairs nothing ends the
+  level; a level with more than 90% of the rows above it is dropped; a level with at
+  most dense_max rows is the coarsest.
 * Device values: level 1 is P^T Ahat P of the fine scaled matrix in FP32
   (FP32((a_ij s_i) s_j), s = 1/sqrt(a_ii)), level l + 1 of level l's device values,
   all with the composite aggregation of the level and the summation order above, every
