@@ -209,7 +209,8 @@ def learned_launches(stats, ml=None):
     """Kernels one learned FCG solve launches: init 1 + per iteration 9 (network) + 4 (FCG)
     + 1 (loop close) + 2 per FP64 residual replacement + final check 1; matrix set-up 4.
     With the coarse-grid correction (ml: levels counting the fine one, sweeps, dense
-    coarsest): per solve one Galerkin launch per coarse level and the dense inverse; per
+    coarsest): per solve one Galerkin launch per coarse level, the dense inverse and, for
+    the smoothed first level, the P and A P kernels; per
     iteration the fine residual, restriction and prolongation, per inner level the
     pre-sweeps, residual, restriction, prolongation and post-sweeps, the coarsest solve,
     and the dot products the network's output kernel no longer does."""
@@ -220,7 +221,8 @@ def learned_launches(stats, ml=None):
     coarse = L - 1
     last = 1 if ml["dense"] else 2 * nu + 2
     per_it = 3 + (2 * nu + 3) * (coarse - 1) + last + 1
-    return base + coarse + (1 if ml["dense"] else 0) + per_it * stats["iters"]
+    setup = coarse + (1 if ml["dense"] else 0) + (2 if ml["options"]["smoothed"] else 0)
+    return base + setup + per_it * stats["iters"]
 
 
 def batch_workload(seed, count=24, sizes=(32, 48, 64, 96, 128)):
