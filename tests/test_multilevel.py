@@ -192,12 +192,14 @@ def _gpu(name, variable=True):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["cavity", "pitzdaily", "hexmix8", "hex12"])
-def test_hierarchy_matches_oracle(name):
+@pytest.mark.parametrize("name,smoothed", [("cavity", 1), ("pitzdaily", 1), ("hexmix8", 1),
+                                           ("hex12", 1), ("pitzdaily", 0), ("hex12", 0)])
+def test_hierarchy_matches_oracle(name, smoothed):
     m, csr, a, su, ctx, lp = _gpu(name)
+    lp.set_multilevel(smoothed=bool(smoothed))
     info = lp.hierarchy(ctx)
     fine = mo.scaled_csr(csr.ioffset, csr.ja, csr.diag, a)
-    levels = mo.build_levels(*fine)
+    levels = mo.build_levels(*fine, sa_omega=0.67 if smoothed else 0.0)
     values = mo.level_values(levels, fine)
     assert info["cells"] == [m.numCells] + [lv["n"] for lv in levels]
     for l, (lv, v) in enumerate(zip(levels, values), start=1):
@@ -210,10 +212,12 @@ def test_hierarchy_matches_oracle(name):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["pitzdaily", "hex16"])
-def test_correction_matches_oracle(name):
+@pytest.mark.parametrize("name,smoothed", [("pitzdaily", 1), ("hex16", 1), ("hex16", 0)])
+def test_correction_matches_oracle(name, smoothed):
     m, csr, a, su, ctx, lp = _gpu(name)
-    _, _, _, cyc = mo.hierarchy(csr.ioffset, csr.ja, csr.diag, a)
+    lp.set_multilevel(smoothed=bool(smoothed))
+    _, _, _, cyc = mo.hierarchy(csr.ioffset, csr.ja, csr.diag, a,
+                                sa_omega=0.67 if smoothed else 0.0)
     rng = np.random.default_rng(1)
     r = rng.standard_normal(m.numCells).astype(np.float32)
     z = (0.5 * rng.standard_normal(m.numCells)).astype(np.float32)
