@@ -401,7 +401,7 @@ __global__ void __launch_bounds__(kTPB)
   }
 }
 
-// P^T (A P): one warp per coarse row, one lane per coarse entry; the rows holding the
+// P^T (A P): one warp per coarse row, two coarse entries per lane; the rows holding the
 // aggregate in ascending order, each row's (A P) entries in column order
 __global__ void __launch_bounds__(kTPB)
     k_sa_a1(int nc, const int *__restrict__ cptr, const int *__restrict__ ccol,
@@ -419,19 +419,48 @@ __global__ void __launch_bounds__(kTPB)
       const int my0 = sb + lane, my1 = sb + 32 + lane;
       const int c0 = my0 < ce ? ccol[my0] : -1, c1 = my1 < ce ? ccol[my1] : -1;
       float acc0 = 0.f, acc1 = 0.f;
-      for (int m = mb; m < me; ++m) {
-        const int i = t_row[m];
-        const float p = p_val[t_pos[m]];
-        const int qb0 = ap_ptr[i], qe = ap_ptr[i + 1];
-        for (int qb = qb0; qb < qe; qb += 32) {
-          const int q = qb + lane;
+      // up to 32 supporting rows at a time, one per lane; their (A P) entries are
+      // numbered consecutively (row by row, entries in column order) and taken in full
+      // chunks of 32, each lane finding its row by a binary search over the lanes'
+      // inclusive prefix sums
+      for (int gb = mb; gb < me; gb += 32) {
+        const int m = gb + lane;
+        int st = 0, len = 0;
+        float p = 0.f;
+        if (m < me) {
+          const int i = t_row[m];
+          p = p_val[t_pos[m]];
+          st = ap_ptr[i];
+          len = ap_ptr[i + 1] - st;
+        }
+        int inc = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(0xffffffffu, inc, o);
+          if (lane >= o) inc += t;
+        }
+        const int total = __shfl_sync(0xffffffffu, inc, 31);
+        for (int fb = 0; fb < total; fb += 32) {
+          const int f = fb + lane;
+          int lo = 0;  // lanes whose rows end at or before entry f
+#pragma unroll
+          for (int step = 16; step > 0; step >>= 1) {
+            const int iv = __shfl_sync(0xffffffffu, inc, lo + step - 1);
+            if (iv <= f) lo += step;
+          }
+          const int src = lo & 31;
+          const int ost = __shfl_sync(0xffffffffu, st, src);
+          const int oinc = __shfl_sync(0xffffffffu, inc, src);
+          const int olen = __shfl_sync(0xffffffffu, len, src);
+          const float op = __shfl_sync(0xffffffffu, p, src);
           int J = -1;
           float v = 0.f;
-          if (q < qe) {
+          if (f < total) {
+            const int q = ost + (f - (oinc - olen));
             J = ap_col[q];
-            v = __fmul_rn(p, ap_val[q]);
+            v = __fmul_rn(op, ap_val[q]);
           }
-          const int cnt = min(32, qe - qb);
+          const int cnt = min(32, total - fb);
           for (int e = 0; e < cnt; ++e) {
             const int Je = __shfl_sync(0xffffffffu, J, e);
             const float ve = __shfl_sync(0xffffffffu, v, e);
