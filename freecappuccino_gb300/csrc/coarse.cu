@@ -1,16 +1,18 @@
-// Coarse-grid correction of the learned FCG (a two-level-and-below V-cycle over the
-// aggregation hierarchy of aggregation.cpp), device side.
+// Coarse-grid correction of the learned FCG (a V-cycle over the aggregation hierarchy
+// of aggregation.cpp), device side.
 //
 // The flexible CG of learned.cu preconditions with z = N(r), the network, and then
-//   z += alpha P V(P^T (r - Ahat z)),
-// where P is the piecewise-constant prolongation of the first aggregation level and V
-// a V-cycle on the levels below: `sweeps` damped Jacobi sweeps before and after each
-// level's own correction, over-corrected by alpha, and a dense inverse at the coarsest
-// level.  Everything runs in FP32 on the Jacobi-scaled matrix Ahat = D^-1/2 A D^-1/2.
-// The level matrices are Galerkin products P^T A P recomputed from the current matrix on
-// every solve: one warp per coarse row, one lane per coarse entry, adding the member
-// rows' entries in a fixed order (members ascending, entries in column order), in FP32
-// (the cycle's precision; FP64 adds would run at GB300's low FP64 rate).
+//   z += P V(P^T (r - Ahat z)),
+// where P is the first level's prolongation and V a V-cycle on the levels below:
+// `sweeps` damped Jacobi sweeps before and after each level's own correction and a dense
+// inverse at the coarsest level.  By default the first P is smoothed,
+// P = (I - omega D^-1 Ahat) P_tent (smoothed aggregation); the deeper levels, and the
+// first one with `smoothed` off, use the piecewise-constant P_tent with every correction
+// scaled by alpha.  Everything runs in FP32 on the Jacobi-scaled matrix
+// Ahat = D^-1/2 A D^-1/2.  The level matrices P^T A P are recomputed from the current
+// matrix on every solve, summed in FP32 in a fixed order: one warp per coarse row, its
+// lanes holding the coarse entries and scanning the contributions in order (FP64 sums
+// would run at GB300's low FP64 rate).
 #include <cuda_runtime.h>
 
 #include <algorithm>

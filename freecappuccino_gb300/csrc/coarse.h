@@ -102,7 +102,8 @@ struct Hierarchy {
 int build(Hierarchy &H, fcg_context *c, const Options &o, std::string &err);
 // Galerkin values of every level from the loaded matrix, and the coarsest inverse.
 int values(Hierarchy &H, fcg_context *c, cudaStream_t st);
-// z += alpha P V(P^T (r - Ahat z)): the correction after the network (fine level).
+// z += P V(P^T (r - Ahat z)) (alpha P_tent for an unsmoothed first level): the
+// correction after the network (fine level).
 void enqueue_correction(Hierarchy &H, fcg_context *c, const Options &o, cudaStream_t st,
                         const float *r, float *z, const int *done);
 // z = V(r) with Jacobi sweeps at the fine level too (the cycle without the network).
