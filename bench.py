@@ -493,6 +493,8 @@ def main():
     ap.add_argument("--solver", default="learned",
                     choices=["learned", "dpcg_mixed", "dpcg", "iccg", "bicgstab"])
     ap.add_argument("--weights", default=None, help="learned checkpoint (default: shipped)")
+    ap.add_argument("--ml-sweeps", type=int, default=3,
+                    help="Jacobi sweeps per level of the coarse-grid correction (library default 2)")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven sweep loop instead of the CUDA-graph WHILE loop")
     ap.add_argument("--only", choices=["assembly"], default=None,
@@ -537,6 +539,7 @@ def main():
         fi0 = torch.zeros(n, dtype=torch.float64, device=dev)
     stream.synchronize()
     lp = LearnedPreconditioner(device=local, path=args.weights or DEFAULT_WEIGHTS)
+    lp.set_multilevel(sweeps=args.ml_sweeps)
 
     method = args.solver
 
@@ -731,6 +734,7 @@ def main():
                 "config": {"workload": f"pressure Poisson {N}^3 jittered hex ({n} cells, nnz {nnz}), "
                                        "solved to L1-relative 1e-8 (true FP64 residual)",
                            "method": method, "N": N, "cells": n, "nnz": nnz,
+                           "coarse_sweeps": args.ml_sweeps if method == "learned" else None,
                            "jitter": JITTER, "tolerance": TOL, "iterations": iters,
                            "l2": "inputs larger than L2 (matrix 0.94 GB, vectors 134 MB each)",
                            "parallelism": f"replicas x{ws}"},
