@@ -191,6 +191,8 @@ _PROTOS = {
     "fcg_lp_precondition": (C.c_int, [_LP, _CTX, _vp, _vp]),
     "fcg_lp_coarse_correct": (C.c_int, [_LP, _CTX, _vp, _vp, _vp]),
     "fcg_aggregate": (C.c_int, [C.c_int, _vp, _vp, _vp, C.c_int, C.c_int, _vp, _ip]),
+    "fcg_smoothed_level": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, C.c_int, C.c_double,
+                                     C.POINTER(C.c_longlong), _vp, _vp, _vp]),
     "fcg_fcg_learned": (C.c_int, [_CTX, _LP, _vp, _vp, _vp, _vp, C.c_double, C.c_int, _dp,
                                   C.POINTER(SolveReport), _ip, _ip]),
     # synthetic inputs (include/fcgpu_meshgen.h)

@@ -308,3 +308,41 @@ extern "C" int fcg_aggregate(int n, const int *ptr, const int *col, const double
   }
   return FCG_OK;
 }
+
+// Host utility: P^T A P of the smoothed prolongation P = (I - omega D^-1 A) P_tent of the
+// aggregation agg[n] (nc aggregates) of a 0-based CSR with ascending columns, in FP64 in
+// the order the hierarchy uses.  With cptr NULL only *nnz is returned; otherwise cptr[nc+1],
+// ccol[*nnz] and cval[*nnz] are filled (*nnz must hold their capacity).
+extern "C" int fcg_smoothed_level(int n, const int *ptr, const int *col, const double *val,
+                                  const int *agg, int nc, double omega, long long *nnz,
+                                  int *cptr, int *ccol, double *cval) {
+  if (n < 1 || nc < 1 || !ptr || !col || !val || !agg || !nnz || !(omega > 0.0))
+    return FCG_ERR_ARG;
+  if (ptr[0] != 0) return FCG_ERR_INDEX;
+  for (int i = 0; i < n; ++i) {
+    if (ptr[i + 1] < ptr[i] || agg[i] < 0 || agg[i] >= nc) return FCG_ERR_INDEX;
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k)
+      if (col[k] < 0 || col[k] >= n || (k > ptr[i] && col[k] <= col[k - 1])) return FCG_ERR_INDEX;
+  }
+  fcg::ml::HostCsr a;
+  a.n = n;
+  a.ptr.assign(ptr, ptr + n + 1);
+  a.col.assign(col, col + ptr[n]);
+  a.val.assign(val, val + ptr[n]);
+  fcg::ml::HostLevel lv;
+  lv.n = nc;
+  lv.agg.assign(agg, agg + n);
+  fcg::ml::smoothed_level(a, omega, lv);
+  const long long m = (long long)lv.A.col.size();
+  if (!cptr) {
+    *nnz = m;
+    return FCG_OK;
+  }
+  if (!ccol || !cval || *nnz < m) return FCG_ERR_ARG;
+  std::copy(lv.A.ptr.begin(), lv.A.ptr.end(), cptr);
+  std::copy(lv.A.col.begin(), lv.A.col.end(), ccol);
+  std::copy(lv.A.val.begin(), lv.A.val.end(), cval);
+  *nnz = m;
+  return FCG_OK;
+}
+

@@ -597,6 +597,14 @@ int fcg_lp_coarse_correct(fcg_learned *lp, fcg_context *ctx, const float *r, con
  * does not coarsen by 10%).  FCG_ERR_INDEX for a malformed CSR. */
 int fcg_aggregate(int n, const int *ptr, const int *col, const double *val, int passes,
                   int dense_max, int *agg, int *nc);
+/* Host utility (no device): P^T A P for the smoothed prolongation P = (I - omega D^-1 A)
+ * P_tent of the aggregation agg[n] (nc aggregates, as fcg_aggregate returns it) of a
+ * 0-based CSR with strictly ascending columns, in FP64 and in the order the hierarchy's
+ * host construction uses.  With cptr NULL only *nnz is set; otherwise cptr[nc+1],
+ * ccol[*nnz] and cval[*nnz] receive the matrix (*nnz in: their capacity, out: the count). */
+int fcg_smoothed_level(int n, const int *ptr, const int *col, const double *val,
+                       const int *agg, int nc, double omega, long long *nnz, int *cptr,
+                       int *ccol, double *cval);
 
 /* Truncated flexible CG (Notay, SIAM J. Sci. Comput. 22 (2000) 1444) preconditioned by
  * M (the network and the coarse-grid correction above), on

@@ -168,6 +168,53 @@ def test_host_aggregation_matches_oracle(name):
         above = (lv["ptr"], lv["col"], lv["hval"])
 
 
+def _host_smoothed(ptr, col, val, agg, nc, omega=0.67):
+    import ctypes as C
+
+    from freecappuccino_gb300 import _lib
+
+    lib = _lib.load()
+    ptr, col = np.ascontiguousarray(ptr, np.int32), np.ascontiguousarray(col, np.int32)
+    val, agg = np.ascontiguousarray(val, np.float64), np.ascontiguousarray(agg, np.int32)
+    n = len(ptr) - 1
+    nnz = C.c_longlong(0)
+    rc = lib.fcg_smoothed_level(n, ptr.ctypes.data, col.ctypes.data, val.ctypes.data,
+                                agg.ctypes.data, nc, omega, C.byref(nnz), None, None, None)
+    if rc:
+        return rc, None
+    out = (np.zeros(nc + 1, np.int32), np.zeros(nnz.value, np.int32), np.zeros(nnz.value))
+    rc = lib.fcg_smoothed_level(n, ptr.ctypes.data, col.ctypes.data, val.ctypes.data,
+                                agg.ctypes.data, nc, omega, C.byref(nnz),
+                                *[o.ctypes.data for o in out])
+    return rc, out
+
+
+@pytest.mark.parametrize("name", ["cavity", "pitzdaily", "hexmix8", "hex16"])
+def test_host_smoothed_level_matches_oracle(name):
+    """The library's host construction of the smoothed first level (P, A P, P^T A P on
+    all host threads, joined in order) against the oracle's, element for element."""
+    m = mesh_by_name(name)
+    csr, a, _ = _system(m)
+    fine = mo.scaled_csr(csr.ioffset, csr.ja, csr.diag, a)
+    lv = mo.build_levels(*fine)[0]
+    assert "sa" in lv
+    rc, (cptr, ccol, cval) = _host_smoothed(*fine, lv["agg"], lv["n"])
+    assert rc == 0
+    assert np.array_equal(cptr, lv["ptr"]) and np.array_equal(ccol, lv["col"])
+    assert np.array_equal(cval, lv["hval"])
+
+
+def test_host_smoothed_level_rejects_bad_input():
+    from freecappuccino_gb300 import _lib
+
+    ptr, col, val = np.array([0, 2, 4]), np.array([0, 1, 0, 1]), np.array([2.0, -1, -1, 2])
+    assert _host_smoothed(ptr, col, val, np.array([0, 0]), 1)[0] == 0
+    assert _host_smoothed(ptr, col, val, np.array([0, 2]), 1)[0] == _lib.FCG_ERR_INDEX
+    assert _host_smoothed(ptr, np.array([0, 1, 1, 0]), val, np.array([0, 0]), 1)[0] == \
+        _lib.FCG_ERR_INDEX
+    assert _host_smoothed(ptr, col, val, np.array([0, 0]), 1, omega=0.0)[0] == _lib.FCG_ERR_ARG
+
+
 def test_host_aggregation_rejects_malformed_csr():
     from freecappuccino_gb300 import _lib
 
