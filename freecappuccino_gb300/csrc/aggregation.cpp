@@ -62,24 +62,38 @@ void chunked_csr(int n, std::vector<int> &ptr, std::vector<int> &col, std::vecto
       1);
 }
 
-// Sums (column, value) pairs met in order into one entry per column, columns ascending;
-// each column's values are added in the order met.
-void merge_row(std::vector<std::pair<int, double>> &ent, std::vector<int> &cols,
-               std::vector<double> &vals) {
-  std::stable_sort(ent.begin(), ent.end(),
-                   [](const std::pair<int, double> &a, const std::pair<int, double> &b) {
-                     return a.first < b.first;
-                   });
-  for (size_t q = 0; q < ent.size();) {
-    const int J = ent[q].first;
-    double acc = ent[q].second;
-    size_t r = q + 1;
-    for (; r < ent.size() && ent[r].first == J; ++r) acc += ent[r].second;
-    cols.push_back(J);
-    vals.push_back(acc);
-    q = r;
+// Sums (column, value) pairs met in order into one entry per column, each column's values
+// added in the order met, and appends the row sorted by column.  One per thread: the
+// marker array (position of each column in the row, -1 when absent) is reset after every
+// row, so a row costs its pair count plus a sort of its distinct columns.
+struct RowSum {
+  std::vector<int> mk;
+  std::vector<std::pair<int, double>> row;
+  void begin(int ncols) {
+    if ((int)mk.size() < ncols) mk.assign(ncols, -1);
+    row.clear();
   }
-}
+  void add(int J, double v) {
+    const int p = mk[J];
+    if (p < 0) {
+      mk[J] = (int)row.size();
+      row.emplace_back(J, v);
+    } else {
+      row[p].second += v;
+    }
+  }
+  void end(std::vector<int> &cols, std::vector<double> &vals) {
+    for (const auto &e : row) mk[e.first] = -1;
+    std::sort(row.begin(), row.end(),
+              [](const std::pair<int, double> &a, const std::pair<int, double> &b) {
+                return a.first < b.first;
+              });
+    for (const auto &e : row) {
+      cols.push_back(e.first);
+      vals.push_back(e.second);
+    }
+  }
+};
 }  // namespace
 
 int pair_match(int n, const int *ptr, const int *col, const double *val, std::vector<int> &agg) {
@@ -150,14 +164,13 @@ void galerkin(const HostCsr &A, const std::vector<int> &agg, int nc, const std::
   out.n = nc;
   chunked_csr(nc, out.ptr, out.col, &out.val,
               [&](int I, std::vector<int> &cols, std::vector<double> &vals) {
-                thread_local std::vector<std::pair<int, double>> ent;
-                ent.clear();
+                thread_local RowSum rs;
+                rs.begin(nc);
                 for (int m = mptr[I]; m < mptr[I + 1]; ++m) {
                   const int i = mem[m];
-                  for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k)
-                    ent.emplace_back(agg[A.col[k]], A.val[k]);
+                  for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) rs.add(agg[A.col[k]], A.val[k]);
                 }
-                merge_row(ent, cols, vals);
+                rs.end(cols, vals);
               });
 }
 
@@ -210,27 +223,26 @@ void smoothed_level(const HostCsr &A, double omega, HostLevel &lv) {
   // A P: for the row's entries in column order, a_ik P_k in P_k's order
   std::vector<double> apv;
   chunked_csr(n, lv.ap_ptr, lv.ap_col, &apv, [&](int i, std::vector<int> &cols, std::vector<double> &vals) {
-    thread_local std::vector<std::pair<int, double>> ent;
-    ent.clear();
+    thread_local RowSum rs;
+    rs.begin(nc);
     for (int k = A.ptr[i]; k < A.ptr[i + 1]; ++k) {
       const int j = A.col[k];
-      for (int p = lv.p_ptr[j]; p < lv.p_ptr[j + 1]; ++p)
-        ent.emplace_back(lv.p_col[p], A.val[k] * pv[p]);
+      for (int p = lv.p_ptr[j]; p < lv.p_ptr[j + 1]; ++p) rs.add(lv.p_col[p], A.val[k] * pv[p]);
     }
-    merge_row(ent, cols, vals);
+    rs.end(cols, vals);
   });
   // P^T A P: for the rows holding the aggregate in ascending order, P_iI (A P)_i
   HostCsr &C = lv.A;
   C.n = nc;
   chunked_csr(nc, C.ptr, C.col, &C.val, [&](int I, std::vector<int> &cols, std::vector<double> &vals) {
-    thread_local std::vector<std::pair<int, double>> ent;
-    ent.clear();
+    thread_local RowSum rs;
+    rs.begin(nc);
     for (int m = lv.t_ptr[I]; m < lv.t_ptr[I + 1]; ++m) {
       const int i = lv.t_row[m];
       const double p = pv[lv.t_pos[m]];
-      for (int q = lv.ap_ptr[i]; q < lv.ap_ptr[i + 1]; ++q) ent.emplace_back(lv.ap_col[q], p * apv[q]);
+      for (int q = lv.ap_ptr[i]; q < lv.ap_ptr[i + 1]; ++q) rs.add(lv.ap_col[q], p * apv[q]);
     }
-    merge_row(ent, cols, vals);
+    rs.end(cols, vals);
   });
 }
 
