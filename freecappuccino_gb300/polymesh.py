@@ -167,13 +167,23 @@ def write_polymesh(m: Mesh, path: str):
             f.write("\n".join(lines))
             f.write("\n)\n")
 
-    write("points", "vectorField", ["(%r %r %r)" % tuple(map(float, p)) for p in m.points])
-    fp, fn = m.face_ptr, m.face_nodes
-    write("faces", "faceList",
-          [f"{fp[i + 1] - fp[i]}(" + " ".join(str(int(v) - 1) for v in fn[fp[i]:fp[i + 1]]) + ")"
-           for i in range(len(fp) - 1)])
-    write("owner", "labelList", [str(int(v) - 1) for v in m.owner])
-    write("neighbour", "labelList", [str(int(v) - 1) for v in m.neighbour])
+    write("points", "vectorField",
+          ["(%r %r %r)" % (x, y, z) for x, y, z in np.asarray(m.points, np.float64).tolist()])
+    fp = np.asarray(m.face_ptr, np.int64)
+    fn = (np.asarray(m.face_nodes, np.int64) - 1).tolist()
+    cnt = np.diff(fp)
+    if len(cnt) and np.all(cnt == cnt[0]):  # one node count: fixed-width rows
+        c = int(cnt[0])
+        fmt = f"{c}(" + " ".join(["%d"] * c) + ")"
+        rows = [fmt % tuple(fn[b:b + c]) for b in range(0, len(fn), c)]
+    else:
+        fpl = fp.tolist()
+        rows = [f"{fpl[i + 1] - fpl[i]}(" + " ".join(map(str, fn[fpl[i]:fpl[i + 1]])) + ")"
+                for i in range(len(fpl) - 1)]
+    write("faces", "faceList", rows)
+    write("owner", "labelList", list(map(str, (np.asarray(m.owner, np.int64) - 1).tolist())))
+    write("neighbour", "labelList",
+          list(map(str, (np.asarray(m.neighbour, np.int64) - 1).tolist())))
     names = {"nsym": "symmetry", "nwal": "wall", "ninl": "inlet", "nout": "outlet",
              "npru": "prOutlet"}
     start_key = {"nsym": "iSymmetryFacesStart", "nwal": "iWallFacesStart",
