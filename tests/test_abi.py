@@ -56,3 +56,24 @@ def test_null_context_is_rejected():
     lib = _lib.load()
     assert lib.fcg_dpcg(None, None, None, None, None, 1e-8, 10, None, None) == _lib.FCG_ERR_ARG
     assert lib.fcg_laplacian(None, None, None, None, None) == _lib.FCG_ERR_ARG
+
+
+def test_ctypes_structs_match_the_header():
+    """Member order and types of the ctypes mirrors of the header's option structs."""
+    import ctypes as C
+    import os
+    import re
+
+    from freecappuccino_gb300 import _lib
+
+    txt = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                            "include", "fcgpu.h")).read()
+    body = re.search(r"typedef struct fcg_lp_multilevel \{(.*?)\} fcg_lp_multilevel;", txt, re.S)
+    assert body
+    fields = []
+    for line in body.group(1).splitlines():
+        m = re.match(r"\s*(int|double)\s+(\w+);", line)
+        if m:
+            fields.append((m.group(2), C.c_int if m.group(1) == "int" else C.c_double))
+    assert [(n, t) for n, t in _lib.Multilevel._fields_] == fields
+
