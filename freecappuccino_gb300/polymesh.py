@@ -49,9 +49,10 @@ def _tokens_per_group(rest: str, ngroups: int) -> np.ndarray:
             ngroups and (np.any(op >= cl[:ngroups]) or np.any(cl[:ngroups - 1] >= op[1:]))):
         raise ValueError("faces: the parentheses of the face list do not pair up")
     dig = (b >= 48) & (b <= 57)
-    start = dig & ~np.concatenate(([False], dig[:-1]))
-    cs = np.concatenate(([0], np.cumsum(start)))
-    return cs[cl[:ngroups]] - cs[op]
+    starts = np.flatnonzero(dig[1:] & ~dig[:-1]) + 1  # first digit of every number
+    if len(dig) and dig[0]:
+        starts = np.concatenate(([0], starts))
+    return np.searchsorted(starts, cl[:ngroups]) - np.searchsorted(starts, op)
 
 
 def parse_points(text: str) -> np.ndarray:
