@@ -140,9 +140,15 @@ def build_system(N):
     return m, mu, phi, su, t_mesh
 
 
-def cpu_baseline(m, mu, phi, su, sweeps_needed, sample_sweeps):
+def cpu_baseline(m, mu, phi, su, sweeps_needed, sample_sweeps, gpu=None):
     """The oracle (serial restatement of dpcg.f90) on this host: a bounded sample of
-    sweeps on the full-size system, scaled to the sweep count of a full solve."""
+    sweeps on the full-size system, scaled to the sweep count of a full solve.
+
+    With `gpu` = (ctx, a, su, x_headline) the same oracle run also checks the GPU path on
+    the full-size system, outside every timed region: the CSR pattern and slot maps and
+    the assembled matrix bit for bit, FP64 DPCG after the same number of sweeps (within
+    1e-10 relative), and the FP64 residual of the headline solution recomputed by the
+    oracle's own product.  Returns (cpu_baseline, parity)."""
     from oracle import oracle
 
     om = oracle.Mesh(**m.oracle_kwargs())
@@ -152,10 +158,31 @@ def cpu_baseline(m, mu, phi, su, sweeps_needed, sample_sweeps):
     r = oracle.dpcg(csr, a, su2, np.zeros(m.numCells), 0.0, sample_sweeps)
     dt = time.perf_counter() - t0
     per_sweep = dt / max(r.iters, 1)
-    return {"value": per_sweep * sweeps_needed, "unit": "s", "cores": 1, "kind": "port",
-            "sample": f"{r.iters} DPCG sweeps of the full {m.numCells}-cell system on 1 host "
-                      f"thread ({dt:.2f} s, {per_sweep * 1e3:.1f} ms/sweep, {platform.machine()}), "
-                      f"scaled to {sweeps_needed} sweeps to 1e-8"}
+    cpu = {"value": per_sweep * sweeps_needed, "unit": "s", "cores": 1, "kind": "port",
+           "sample": f"{r.iters} DPCG sweeps of the full {m.numCells}-cell system on 1 host "
+                     f"thread ({dt:.2f} s, {per_sweep * 1e3:.1f} ms/sweep, {platform.machine()}), "
+                     f"scaled to {sweeps_needed} sweeps to 1e-8"}
+    if gpu is None:
+        return cpu, None
+    ctx, a_gpu, su_gpu, x_head = gpu
+    io, ja, dg, spn, snp = ctx.create_csr()
+    csr_ok = all(np.array_equal(g, e) for g, e in ((io, csr.ioffset), (ja, csr.ja),
+                                                     (dg, csr.diag), (spn, csr.slot_pn),
+                                                     (snp, csr.slot_np)))
+    a_g = a_gpu.cpu().numpy()
+    su_g = su_gpu.cpu().numpy()
+    g = ctx.dpcg(a_gpu, su_gpu, np.zeros(m.numCells), 0.0, r.iters)
+    fi_g = g.fi.cpu().numpy() if hasattr(g.fi, "cpu") else g.fi
+    x = x_head.cpu().numpy()
+    res = su2 - oracle.spmv(csr, a, x)
+    parity = {"oracle": "serial C restatement of the reference routines",
+              "csr_and_slot_maps_bit_exact": bool(csr_ok),
+              "laplacian_bit_exact": bool(np.array_equal(a_g, a) and np.array_equal(su_g, su2)),
+              f"dpcg_{r.iters}_sweeps_max_rel_diff": float(np.abs(fi_g - r.fi).max() /
+                                                           np.abs(r.fi).max()),
+              "headline_l1_rel_by_oracle": float(np.abs(res).sum() / np.abs(su2).sum()),
+              "headline_l2_rel_by_oracle": float(np.linalg.norm(res) / np.linalg.norm(su2))}
+    return cpu, parity
 
 
 def run_reference(args, ws, rank):
@@ -542,11 +569,27 @@ def main():
     lp.set_multilevel(sweeps=args.ml_sweeps)
 
     method = args.solver
+    # L1 tolerance per method: the reference's L1 test at 1e-8, tightened where the FP64
+    # L2 residual ||b - Ax||/||b|| is still above 1e-8, so that every method is timed to
+    # both criteria
+    l1_tol = {}
 
     def run(name):
+        tol = l1_tol.get(name, TOL)
         if name == "learned":
-            return lp.solve(ctx, a_d, su_d, fi0, TOL, NSW)
-        return getattr(ctx, name)(a_d, su_d, fi0, TOL, NSW, want_res=False)
+            return lp.solve(ctx, a_d, su_d, fi0, tol, NSW)
+        return getattr(ctx, name)(a_d, su_d, fi0, tol, NSW, want_res=False)
+
+    def calibrate(name):
+        """Solves once at the current tolerance and halves it (at most 6 times) until the
+        FP64 L2 residual meets 1e-8 too; returns the last report."""
+        r = run(name)
+        for _ in range(6):
+            if r.l2_rel <= TOL:
+                break
+            l1_tol[name] = l1_tol.get(name, TOL) * 0.5
+            r = run(name)
+        return r
 
     def timed(name):
         t0e, t1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -556,7 +599,14 @@ def main():
         torch.cuda.synchronize()
         return r, reduce_max(ws, t0e.elapsed_time(t1e) * 1e-3)
 
-    for _ in range(args.warmup):
+    # the first solve on this mesh includes the per-mesh set-up (for the learned
+    # preconditioner: the aggregation hierarchy, built on the host once per mesh)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    calibrate(method)
+    torch.cuda.synchronize()
+    first_solve_s = time.perf_counter() - t0
+    for _ in range(args.warmup - 1):
         run(method)
     sampler = ClockSampler(local)
     sampler.start()
@@ -635,11 +685,11 @@ def main():
     for other in ("dpcg", "dpcg_mixed"):
         if other == method or args.no_compare:
             continue
-        run(other)
+        calibrate(other)
         r_o, t_o = timed(other)
         err = float((x_method - r_o.fi).abs().max() / r_o.fi.abs().max())
         comparisons[other] = {"seconds": t_o, "sweeps": r_o.iters, "l2_rel": r_o.l2_rel,
-                              "headline_speedup": t_o / t_solve,
+                              "l1_tol": l1_tol.get(other, TOL), "headline_speedup": t_o / t_solve,
                               "max_rel_diff_of_headline_solution": err}
     if method == "learned" and ml and not args.no_compare:
         # the same flexible CG without the network (Jacobi sweeps in its place) and the
@@ -711,9 +761,10 @@ def main():
         multi = run_multi(dev)
         assembly = run_assembly(ctx, m, dev, stream, peak)
 
-    cpu = None
+    cpu = parity = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        cpu = cpu_baseline(m, mu, phi, su, dpcg_sweeps, args.cpu_sample)
+        cpu, parity = cpu_baseline(m, mu, phi, su, dpcg_sweeps, args.cpu_sample,
+                                   gpu=(ctx, a_d, su_d, x_method))
 
     if rank == 0:
         dtype = {"learned": "f32 FCG + bf16 network (fp32 accumulate), f64 residual/updates",
@@ -727,6 +778,14 @@ def main():
                                 "directions": 8, "weights": os.path.relpath(
                                     args.weights or DEFAULT_WEIGHTS, ROOT),
                                 "coarse_correction": ml}
+        head = {"method": method, "seconds": t_solve, "iterations": iters,
+                "l1_tol": l1_tol.get(method, TOL), "l2_rel": last.l2_rel,
+                "first_solve_s": first_solve_s}
+        for k, v in comparisons.items():
+            head[k + "_s"] = v["seconds"]
+            head["speedup_vs_" + k] = v["headline_speedup"]
+            if "l2_rel" in v:
+                head[k + "_l2_rel"] = v["l2_rel"]
         line = {"metric": METRIC, "value": t_solve, "unit": "s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_solve * 1e3, "higher_is_better": False,
                 "scaling": "weak", "vs_baseline": None, "dtype": dtype,
@@ -738,6 +797,7 @@ def main():
                            "jitter": JITTER, "tolerance": TOL, "iterations": iters,
                            "l2": "inputs larger than L2 (matrix 0.94 GB, vectors 134 MB each)",
                            "parallelism": f"replicas x{ws}"},
+                "comparison": head, "parity": parity,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
                 "gpu_launches": launches, "extra": extra}
         print(json.dumps(line), flush=True)

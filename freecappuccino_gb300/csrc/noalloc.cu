@@ -19,7 +19,12 @@
 //
 // Set-up: the first call on a device, with that device current, looks up the array's
 // device address with cudaGetSymbolAddress and caches it for that device.  Make that
-// first call before any stream capture begins.
+// first call before any stream capture begins.  With CUDA's default lazy module loading
+// that first call is also when this file's code and the array are loaded onto the
+// device: it takes about 6.4 MB plus the code's size once, and later calls take
+// nothing.  A caller that reserves the whole device for its own pool must make the first
+// call before the pool takes its memory, or run with CUDA_MODULE_LOADING=EAGER, which
+// loads the array when the library is loaded.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -219,13 +224,24 @@ __global__ void k_na_final(int n, const int *io, const int *ja, const double *a,
   }
 }
 
-bool on_device(const void *p) {
+// Device memory of the current device `dev`, or managed memory: arrays of another GPU
+// would be read over peer access, or fault without it.
+bool on_device(const void *p, int dev) {
   cudaPointerAttributes at;
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+  if (at.type == cudaMemoryTypeManaged) return true;
+  return at.type == cudaMemoryTypeDevice && at.device == dev;
+}
+
+// A launch that failed (no image for this GPU, bad configuration) leaves the solver
+// scalars unwritten: report it instead of reading them.
+bool launch_failed() {
+  if (cudaPeekAtLastError() == cudaSuccess) return false;
+  cudaGetLastError();
+  return true;
 }
 
 }  // namespace
@@ -236,11 +252,11 @@ extern "C" int fcg_dpcg_noalloc(int numCells, const int *ioffset, const int *ja,
                                 void *stream) {
   if (numCells <= 0 || numCells > kMaxCells) return FCG_ERR_ARG;  // beyond the static array
   if (nsw < 0 || !ioffset || !ja || !diag || !a || !su || !fi || !res) return FCG_ERR_ARG;
-  const void *arrays[] = {ioffset, ja, diag, a, su, fi, res};
-  for (const void *p : arrays)
-    if (!on_device(p)) return FCG_ERR_ARG;  // host arrays would need staging memory
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return FCG_ERR_CUDA;
+  const void *arrays[] = {ioffset, ja, diag, a, su, fi, res};
+  for (const void *p : arrays)
+    if (!on_device(p, dev)) return FCG_ERR_ARG;  // host arrays would need staging memory
   double *base;
   {
     std::lock_guard<std::mutex> lock(g_setup_mutex);
@@ -267,6 +283,7 @@ extern "C" int fcg_dpcg_noalloc(int numCells, const int *ioffset, const int *ja,
   const auto t0 = std::chrono::steady_clock::now();
   k_na_reset<<<1, 32, 0, st>>>(S, nsw, sor, (double)1e-20f, (double)1e-13f);
   k_na_init<<<G, kTPB, 0, st>>>(n, ioffset, ja, diag, a, su, fi, res, invd, pk, partials, S);
+  if (launch_failed()) return FCG_ERR_CUDA;
   int done = 0;
   for (int swept = 0; !done && swept <= nsw; swept += kSweepsPerCheck) {
     for (int j = 0; j < kSweepsPerCheck; ++j) {
@@ -274,6 +291,7 @@ extern "C" int fcg_dpcg_noalloc(int numCells, const int *ioffset, const int *ja,
       k_na_spmv<<<G, kTPB, 0, st>>>(n, ioffset, ja, a, pk, qk, partials, S);
       k_na_update<<<G, kTPB, 0, st>>>(n, fi, res, pk, qk, invd, partials, S);
     }
+    if (launch_failed()) return FCG_ERR_CUDA;
     if (cudaMemcpyAsync(&done, &S->done, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess) {
       cudaGetLastError();
@@ -281,6 +299,7 @@ extern "C" int fcg_dpcg_noalloc(int numCells, const int *ioffset, const int *ja,
     }
   }
   k_na_final<<<G, kTPB, 0, st>>>(n, ioffset, ja, a, su, fi, partials, S);
+  if (launch_failed()) return FCG_ERR_CUDA;
   NaScal h;
   if (cudaMemcpyAsync(&h, S, sizeof(NaScal), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess) {

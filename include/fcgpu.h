@@ -410,12 +410,16 @@ int fcg_get_solver_trace(fcg_context *ctx, double *resl_rsm, int max_count, int 
  * nothing: every array is the caller's DEVICE array (the reference's 1-based CSR
  * ioffset[numCells+1], ja[nnz], diag[numCells], values a[nnz], su[numCells], fi
  * in/out, res out), and the work vectors sit in one file-scope device array sized for
- * at most FCG_NOALLOC_MAX_CELLS cells (about 6.4 MB, held by every GPU that loads the
- * library until exit).  Larger systems and host arrays return FCG_ERR_ARG.  All calls
- * share that array: calls that overlap on the GPU race.  The first call on a device
- * looks up the array's address (cudaGetSymbolAddress) with that device current; make
- * it before any stream capture.  Work runs on cuda_stream (NULL = legacy stream); the
- * call returns when the solve is done. */
+ * at most FCG_NOALLOC_MAX_CELLS cells (about 6.4 MB, held until exit by every GPU it has
+ * been used on).  Larger systems, host arrays and arrays of another GPU return
+ * FCG_ERR_ARG.  All calls share that array: calls that overlap on the GPU race.  The
+ * first call on a device looks up the array's address (cudaGetSymbolAddress) with that
+ * device current; make it before any stream capture.  Under CUDA's default lazy module
+ * loading that first call also loads this code and the array onto the device (about
+ * 6.4 MB plus the code, once): a caller whose pool reserves the whole device must make
+ * it before the pool takes its memory, or set CUDA_MODULE_LOADING=EAGER.  Later calls
+ * allocate nothing.  Work runs on cuda_stream (NULL = legacy stream); the call returns
+ * when the solve is done. */
 #define FCG_NOALLOC_MAX_CELLS 262144
 int fcg_dpcg_noalloc(int numCells, const int *ioffset, const int *ja, const int *diag,
                      const double *a, const double *su, double *fi, double *res, double sor,

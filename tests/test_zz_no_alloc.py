@@ -30,17 +30,19 @@ def _system(N):
     return m, ctx, a, su, io, ja, dg
 
 
-def _noalloc(torch, io, ja, dg, a, su, sor, nsw):
+def _noalloc(torch, io, ja, dg, a, su, sor, nsw, fi0=None, stream=None):
     lib = _lib.load()
     d = lambda x: torch.from_numpy(np.ascontiguousarray(x)).cuda()
     tio, tja, tdg, ta, tsu = d(io), d(ja), d(dg), d(a), d(su)
-    fi = torch.zeros(len(dg), dtype=torch.float64, device="cuda")
+    fi = torch.zeros(len(dg), dtype=torch.float64, device="cuda") if fi0 is None else d(fi0)
     res = torch.empty_like(fi)
     resor = C.c_double(float("nan"))
     rep = _lib.SolveReport()
+    torch.cuda.synchronize()
     rc = lib.fcg_dpcg_noalloc(len(dg), tio.data_ptr(), tja.data_ptr(), tdg.data_ptr(),
                               ta.data_ptr(), tsu.data_ptr(), fi.data_ptr(), res.data_ptr(),
-                              float(sor), int(nsw), C.byref(resor), C.byref(rep), None)
+                              float(sor), int(nsw), C.byref(resor), C.byref(rep),
+                              None if stream is None else C.c_void_p(stream.cuda_stream))
     return rc, fi.cpu().numpy(), res.cpu().numpy(), rep, resor.value
 
 
@@ -87,3 +89,50 @@ def test_noalloc_rejects_oversize_and_host_arrays():
     rc = lib.fcg_dpcg_noalloc(4, p(i), p(i), p(i), h.ctypes.data, p(x), p(x), p(x), 1e-8, 10,
                               None, None, None)
     assert rc == big
+
+
+def test_noalloc_allocates_nothing_after_the_first_call():
+    """The first call on a device loads the code and the work array (lazy module
+    loading); every later call leaves the device's free memory unchanged."""
+    torch = pytest.importorskip("torch")
+    m, ctx, a, su, io, ja, dg = _system(16)
+    lib = _lib.load()
+    d = lambda x: torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    tio, tja, tdg, ta, tsu = d(io), d(ja), d(dg), d(a), d(su)
+    fi = torch.zeros(len(dg), dtype=torch.float64, device="cuda")
+    res = torch.empty_like(fi)
+    rep = _lib.SolveReport()
+    args = (len(dg), tio.data_ptr(), tja.data_ptr(), tdg.data_ptr(), ta.data_ptr(),
+            tsu.data_ptr(), fi.data_ptr(), res.data_ptr(), 1e-8, 500, None, C.byref(rep), None)
+    torch.cuda.synchronize()
+    assert lib.fcg_dpcg_noalloc(*args) == _lib.FCG_OK  # set-up call
+    free0, _ = torch.cuda.mem_get_info()
+    fi.zero_()
+    torch.cuda.synchronize()
+    assert lib.fcg_dpcg_noalloc(*args) == _lib.FCG_OK
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert rep.converged
+    ctx.close()
+
+
+def test_noalloc_zero_residual_and_side_stream():
+    """su = A fi: res0 = 0 < tol, no sweep and resor untouched (dpcg.f90:66-70); and the
+    same solve on a non-default stream as on the legacy stream."""
+    torch = pytest.importorskip("torch")
+    from oracle import oracle
+
+    m, ctx, a, su, io, ja, dg = _system(12)
+    x = 1e-3 * fcg.uniform(6, 1, m.numCells)  # small: rounding of A x stays far below tol
+    csr = oracle.create_csr(m.numCells, m.owner, m.neighbour)
+    b = oracle.spmv(csr, a, x)
+    rc, fi, res, rep, resor = _noalloc(torch, io, ja, dg, a, b, 1e-8, 100, fi0=x)
+    assert rc == _lib.FCG_OK
+    assert rep.iters == 0 and np.isnan(resor)
+    assert np.array_equal(fi, x)
+    s = torch.cuda.Stream()
+    rc0, fi0, _, rep0, _ = _noalloc(torch, io, ja, dg, a, su, 0.0, 20)
+    rc1, fi1, _, rep1, _ = _noalloc(torch, io, ja, dg, a, su, 0.0, 20, stream=s)
+    assert rc0 == rc1 == _lib.FCG_OK and rep0.iters == rep1.iters == 20
+    assert np.array_equal(fi0, fi1)  # same launches, same order of sums
+    ctx.close()
