@@ -454,6 +454,46 @@ def run_assembly(ctx, m, dev, stream, peak, reps=5, seed=SEED + 3):
             "kernels": out}
 
 
+def run_section(which, ctx, m, mu, phi, su, dev, stream):
+    """Profiling sections on the bench system (all arrays on the device), each kernel
+    launched a few times after one warm-up: "layer" = one forward pass of the network,
+    three times (rms, embedding, six layers, output); "solvers" = three FP64 products
+    A x, fixed sweep counts of FP64 DPCG (20), ICCG (20), BiCGStab (10) and mixed DPCG
+    (20), and the multi-RHS BiCGStab on the five transport systems of this mesh."""
+    import torch
+
+    from freecappuccino_gb300.learned import DEFAULT_WEIGHTS, LearnedPreconditioner
+    from freecappuccino_gb300.systems import transport_systems
+
+    with torch.cuda.stream(stream):
+        a, b = ctx.laplacian(torch.from_numpy(mu).to(dev), torch.from_numpy(phi).to(dev),
+                             torch.from_numpy(su).to(dev))
+        x0 = torch.zeros(m.numCells, dtype=torch.float64, device=dev)
+    stream.synchronize()
+    out = {}
+    if which == "layer":
+        lp = LearnedPreconditioner(device=dev.index or 0, path=DEFAULT_WEIGHTS)
+        lp.set_matrix(ctx, a)
+        dg = torch.from_numpy(ctx.create_csr()[2] - 1).to(dev)
+        r32 = (b / torch.sqrt(a[dg])).to(torch.float32)
+        out["forward_kernels_ms"] = lp.profile(ctx, r32, reps=3)
+        out["layer_form"] = lp.layer_form(ctx)
+        lp.close()
+        return out
+    y = torch.empty_like(x0)
+    for _ in range(3):
+        ctx.spmv(a, b, y)
+    for name, k in (("dpcg", 20), ("iccg", 20), ("bicgstab", 10), ("dpcg_mixed", 20)):
+        getattr(ctx, name)(a, b, x0, 0.0, k, want_res=False)
+        r = getattr(ctx, name)(a, b, x0, 0.0, k, want_res=False)
+        out[name] = {"sweeps": r.iters, "seconds": r.seconds}
+    ta, tsu, _ = transport_systems(m, ctx.create_csr())
+    ta, tsu = torch.from_numpy(ta).to(dev), torch.from_numpy(tsu).to(dev)
+    _, reps = ctx.bicgstab_multi(ta, tsu, torch.zeros_like(tsu), 1e-10, 2000)
+    out["bicgstab_multi"] = {"sweeps": [r.iters for r in reps], "seconds": reps[0].seconds}
+    return out
+
+
 def run_multi(dev, N=128, seed=SEED + 2):
     """The five transport systems (u, v, w, k, eps) on one pattern solved in one
     multi-RHS BiCGStab (FP32 DILU inner, FP64 correction to 1e-10) against the same
@@ -524,8 +564,10 @@ def main():
                     help="Jacobi sweeps per level of the coarse-grid correction (library default 2)")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven sweep loop instead of the CUDA-graph WHILE loop")
-    ap.add_argument("--only", choices=["assembly"], default=None,
-                    help="run one section alone on the --N mesh and print it (profiling)")
+    ap.add_argument("--only", choices=["assembly", "layer", "solvers"], default=None,
+                    help="run one section alone on the --N mesh and print it (profiling): "
+                         "the face-loop entry points, the network's forward kernels, or a "
+                         "fixed number of sweeps of each solver")
     args = ap.parse_args()
     if args.no_graph:
         os.environ["FCG_NO_GRAPH"] = "1"
@@ -554,6 +596,12 @@ def main():
         out = run_assembly(ctx, m, torch.device("cuda", local), stream, peaks()[0])
         if rank == 0:
             print(json.dumps({"section": "assembly", "N": N, **out}), flush=True)
+        ctx.close()
+        return
+    if args.only in ("layer", "solvers"):
+        out = run_section(args.only, ctx, m, mu, phi, su, torch.device("cuda", local), stream)
+        if rank == 0:
+            print(json.dumps({"section": args.only, "N": N, **out}), flush=True)
         ctx.close()
         return
     n, nnz = m.numCells, m.nnz

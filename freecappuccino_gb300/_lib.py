@@ -183,6 +183,7 @@ _PROTOS = {
     "fcg_lp_set_loss": (C.c_int, [_LP, C.c_int]),
     "fcg_lp_last_solve_stats": (C.c_int, [_LP, _ip, _ip]),
     "fcg_lp_profile": (C.c_int, [_LP, _CTX, _vp, C.c_int, _dp, C.c_int, _ip]),
+    "fcg_lp_layer_form": (C.c_int, [_LP, _CTX, _ip, _ip]),
     "fcg_lp_set_fcg_options": (C.c_int, [_LP, C.c_int, C.c_int, C.c_int, C.c_double]),
     "fcg_lp_set_multilevel": (C.c_int, [_LP, C.POINTER(Multilevel)]),
     "fcg_lp_get_multilevel": (C.c_int, [_LP, C.POINTER(Multilevel)]),

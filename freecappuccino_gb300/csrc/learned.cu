@@ -51,6 +51,8 @@
 #include "fcg_internal.h"
 #include "krylov_common.cuh"
 #include "launch.h"
+#include "lp_hex.h"
+#include "lp_tile.cuh"
 
 namespace fcg {
 namespace lp {
@@ -63,7 +65,7 @@ constexpr int P = oBout + 1;
 static_assert(P == FCG_LP_PARAMS, "parameter count must match the header");
 static_assert(oBin == oWin + C * F && oLayer0 == oBin + C, "parameter layout");
 constexpr int kBwdTile = 64;            // cells per shared-memory tile of the layer backward
-constexpr int kTileStride = 2 * C + 8;  // padded BF16 row of the [h; m] tile and of W_l
+static_assert(kTileC == C && kTileStride == 2 * C + 8, "tile layout of lp_tile.cuh");
 constexpr int kRed = 8;                 // reduction tickets
 constexpr int kMaxDir = 8;              // most previous directions the FCG keeps
 
@@ -121,6 +123,12 @@ struct fcg_learned {
   // coarse-grid correction of the flexible CG (coarse.cu, aggregation.cpp)
   fcg::ml::Options mlo;
   std::vector<fcg::ml::Hierarchy *> mlc;  // one per context, least recently used first
+  // plane-staged layer (learned_hex.cu) for the context and mesh it was detected on,
+  // and the stencil value planes of the matrix loaded last
+  fcg::lphex::HexGrid hex;
+  unsigned long long hex_uid = 0;
+  unsigned hex_gen = 0;
+  DBuf hexval;
 };
 
 namespace fcg {
@@ -250,22 +258,7 @@ __global__ void __launch_bounds__(kTPB)
   }
 }
 
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4],
-                                         const unsigned (&b)[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-      "{%8,%9}, {%0,%1,%2,%3};"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-
-// acc[0..7] += v * (8 BF16 values packed in q)
-__device__ __forceinline__ void fma8(float (&acc)[8], float v, const uint4 &q) {
-  const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(&q);
-#pragma unroll
-  for (int c = 0; c < 8; ++c) acc[c] += v * bf(e[c]);
-}
+using lp::fma8;
 
 // One message-passing layer.  Tiles are dealt to warps grid-stride, so all blocks work
 // on one narrow band of the mesh at a time and the rows at +-N^2 that a tile gathers were
@@ -295,7 +288,7 @@ __global__ void __launch_bounds__(kTPB, 4)
   if (threadIdx.x < C) bsm[threadIdx.x] = bl[threadIdx.x];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int g = lane >> 2, tg = lane & 3, qc = 8 * (lane & 3);
+  const int qc = 8 * (lane & 3);
   __nv_bfloat16 *tw = tile[warp];
   const int ntiles = (n + 15) / 16;
   const int nwarps = (int)(((long long)gridDim.x * blockDim.x) >> 5);
@@ -343,12 +336,8 @@ __global__ void __launch_bounds__(kTPB, 4)
         }
         own = __ldg(reinterpret_cast<const uint4 *>(hq + (long long)r * C));
       }
-      __nv_bfloat16 *row = tw + rloc * TS;
-      *reinterpret_cast<uint4 *>(row + qc) = own;
       __align__(16) __nv_bfloat16 mb[8];
-#pragma unroll
-      for (int c = 0; c < 8; ++c) mb[c] = __float2bfloat16(acc[c]);
-      *reinterpret_cast<uint4 *>(row + C + qc) = *reinterpret_cast<const uint4 *>(mb);
+      lp::tile_put_row(tw, rloc, qc, own, acc, mb);
       if (mout && r < n) {
         float4 *mo = reinterpret_cast<float4 *>(mout + (long long)r * C + qc);
         mo[0] = make_float4(bf(mb[0]), bf(mb[1]), bf(mb[2]), bf(mb[3]));
@@ -356,47 +345,11 @@ __global__ void __launch_bounds__(kTPB, 4)
       }
     }
     __syncwarp();
-    float d[4][4];
-#pragma unroll
-    for (int nt = 0; nt < 4; ++nt)
-#pragma unroll
-      for (int q = 0; q < 4; ++q) d[nt][q] = 0.f;
-#pragma unroll
-    for (int kb = 0; kb < 4; ++kb) {
-      const int k0 = kb * 16 + tg * 2;
-      unsigned a[4];
-      a[0] = *reinterpret_cast<const unsigned *>(tw + g * TS + k0);
-      a[1] = *reinterpret_cast<const unsigned *>(tw + (g + 8) * TS + k0);
-      a[2] = *reinterpret_cast<const unsigned *>(tw + g * TS + k0 + 8);
-      a[3] = *reinterpret_cast<const unsigned *>(tw + (g + 8) * TS + k0 + 8);
-#pragma unroll
-      for (int nt = 0; nt < 4; ++nt) {
-        const int oc = nt * 8 + g;  // output channel = column of B = row of W_l
-        unsigned b[2];
-        b[0] = *reinterpret_cast<const unsigned *>(wsm + oc * TS + k0);
-        b[1] = *reinterpret_cast<const unsigned *>(wsm + oc * TS + k0 + 8);
-        mma_bf16(d[nt], a, b);
-      }
-    }
-    __syncwarp();  // every lane has its fragments: the h part of the tile may change
-#pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-#pragma unroll
-      for (int hh = 0; hh < 2; ++hh) {
-        const int rr = g + 8 * hh, cell = tt * 16 + rr;
-        const int col = nt * 8 + tg * 2;
-        const float z0 = d[nt][2 * hh] + bsm[col], z1 = d[nt][2 * hh + 1] + bsm[col + 1];
-        __nv_bfloat162 *hp = reinterpret_cast<__nv_bfloat162 *>(tw + rr * TS + col);
-        const __nv_bfloat162 hold = *hp;
-        __nv_bfloat162 o;
-        o.x = __float2bfloat16(bf(hold.x) + fmaxf(z0, 0.f));
-        o.y = __float2bfloat16(bf(hold.y) + fmaxf(z1, 0.f));
-        *hp = o;
-        if (zout && cell < n)
-          *reinterpret_cast<float2 *>(zout + (long long)cell * C + col) = make_float2(z0, z1);
-      }
-    }
-    __syncwarp();
+    lp::tile_dense(tw, wsm, bsm, lane, [&](int rr, int col, float z0, float z1) {
+      const int cell = tt * 16 + rr;
+      if (zout && cell < n)
+        *reinterpret_cast<float2 *>(zout + (long long)cell * C + col) = make_float2(z0, z1);
+    });
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
       const int idx = lane + 32 * k, rr = idx >> 2, part = idx & 3;
@@ -474,7 +427,6 @@ __global__ void __launch_bounds__(kTPB, 4)
   if (threadIdx.x < C) bsm[threadIdx.x] = bl[threadIdx.x];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int g = lane >> 2, tg = lane & 3;
   __nv_bfloat16 *tw = tile[warp];
   const int ntiles = (n + 15) / 16;
   const int nwarps = (int)(((long long)gridDim.x * blockDim.x) >> 5);
@@ -494,44 +446,7 @@ __global__ void __launch_bounds__(kTPB, 4)
       *reinterpret_cast<uint4 *>(tw + rr * TS + 8 * part) = v;
     }
     __syncwarp();
-    float d[4][4];
-#pragma unroll
-    for (int nt = 0; nt < 4; ++nt)
-#pragma unroll
-      for (int q = 0; q < 4; ++q) d[nt][q] = 0.f;
-#pragma unroll
-    for (int kb = 0; kb < 4; ++kb) {
-      const int k0 = kb * 16 + tg * 2;
-      unsigned a[4];
-      a[0] = *reinterpret_cast<const unsigned *>(tw + g * TS + k0);
-      a[1] = *reinterpret_cast<const unsigned *>(tw + (g + 8) * TS + k0);
-      a[2] = *reinterpret_cast<const unsigned *>(tw + g * TS + k0 + 8);
-      a[3] = *reinterpret_cast<const unsigned *>(tw + (g + 8) * TS + k0 + 8);
-#pragma unroll
-      for (int nt = 0; nt < 4; ++nt) {
-        const int oc = nt * 8 + g;
-        unsigned b[2];
-        b[0] = *reinterpret_cast<const unsigned *>(wsm + oc * TS + k0);
-        b[1] = *reinterpret_cast<const unsigned *>(wsm + oc * TS + k0 + 8);
-        mma_bf16(d[nt], a, b);
-      }
-    }
-    __syncwarp();
-#pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-#pragma unroll
-      for (int hh = 0; hh < 2; ++hh) {
-        const int rr = g + 8 * hh, col = nt * 8 + tg * 2;
-        const float z0 = d[nt][2 * hh] + bsm[col], z1 = d[nt][2 * hh + 1] + bsm[col + 1];
-        __nv_bfloat162 *hp = reinterpret_cast<__nv_bfloat162 *>(tw + rr * TS + col);
-        const __nv_bfloat162 hold = *hp;
-        __nv_bfloat162 o;
-        o.x = __float2bfloat16(bf(hold.x) + fmaxf(z0, 0.f));
-        o.y = __float2bfloat16(bf(hold.y) + fmaxf(z1, 0.f));
-        *hp = o;
-      }
-    }
-    __syncwarp();
+    lp::tile_dense(tw, wsm, bsm, lane, lp::NoZ());
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
       const int idx = lane + 32 * k, rr = idx >> 2, part = idx & 3;
@@ -1217,6 +1132,53 @@ bool features_current(const fcg_learned *Lp, const fcg_context *c) {
          scaled32(c) != nullptr;
 }
 
+// Device ints of the scal buffer used by the plane-staged layer: scratch of the mesh
+// check, and the status a layer outside a solve reports a wait timeout to.
+constexpr int kHexFlag = 40, kHexStatus = 41;
+
+// The plane-staged layer serves inference on lexicographic hex meshes; FCG_LP_LAYER=gather
+// (or =split) keeps the sliced gather form everywhere.
+bool hex_allowed() {
+  const char *e = std::getenv("FCG_LP_LAYER");
+  return !(e && (std::strcmp(e, "gather") == 0 || std::strcmp(e, "split") == 0));
+}
+
+bool hex_on(const fcg_learned *Lp, const fcg_context *c) {
+  return Lp->hex.ok && Lp->hex_uid == c->uid && Lp->hex_gen == c->bind_gen && hex_allowed();
+}
+
+// Detects the block structure of c's mesh once per bound mesh, then writes the stencil
+// value planes of the scaled matrix loaded last.
+int hex_prepare(fcg_learned *Lp, fcg_context *c) {
+  if (Lp->hex_uid != c->uid || Lp->hex_gen != c->bind_gen) {
+    fcg::lphex::HexGrid g;
+    int rc = fcg::lphex::detect(c, Lp->scal.as<int>() + kHexFlag, &g);
+    if (rc) return lp_fail(Lp, rc, fcg_last_error(c));
+    if (g.ok) {
+      const size_t bytes = sizeof(float) * fcg::lphex::value_count(g);
+      LP_TRY(Lp, Lp->hexval.ensure(bytes));
+      LP_TRY(Lp, cudaMemsetAsync(Lp->hexval.p, 0, bytes, c->stream));  // padding columns
+    }
+    Lp->hex = g;
+    Lp->hex_uid = c->uid;
+    Lp->hex_gen = c->bind_gen;
+  }
+  if (Lp->hex.ok)
+    LP_TRY(Lp, fcg::lphex::values(c, Lp->hex, scaled32(c), Lp->hexval.as<float>(), c->stream));
+  return FCG_OK;
+}
+
+// Reads and clears the timeout status of the plane-staged layer (calls outside a solve).
+int hex_status(fcg_learned *Lp, fcg_context *c) {
+  int st = 0;
+  LP_TRY(Lp, cudaMemcpyAsync(&st, Lp->scal.as<int>() + kHexStatus, sizeof st,
+                             cudaMemcpyDeviceToHost, c->stream));
+  LP_TRY(Lp, cudaStreamSynchronize(c->stream));
+  if (st == 0) return FCG_OK;
+  LP_TRY(Lp, cudaMemsetAsync(Lp->scal.as<int>() + kHexStatus, 0, sizeof(int), c->stream));
+  return lp_fail(Lp, st, "plane-staged layer: a copy wait gave up");
+}
+
 // Features of the context's mesh and of the scaled matrix loaded into it.
 int compute_features(fcg_learned *Lp, fcg_context *c) {
   int rc = ensure_workspace(Lp, c, false);
@@ -1228,6 +1190,7 @@ int compute_features(fcg_learned *Lp, fcg_context *c) {
   k_lp_features<<<grid_for(c->n, c->num_sms), kTPB, 0, c->stream>>>(
       c->mv, scale64(c), red + lp::kMaxDir * kMaxBlocks, Lp->feat.as<float>());
   LP_TRY(Lp, cudaGetLastError());
+  if ((rc = hex_prepare(Lp, c))) return rc;
   Lp->fuid = c->uid;
   Lp->fgen = c->bind_gen;
   Lp->fmat = scaled32(c);
@@ -1243,9 +1206,11 @@ bool layer_split() {
 
 // Forward pass on r (device, FP32) up to h_L.  Training keeps h_0..h_L, m_1..m_L and the
 // pre-activations; inference ping-pongs two activation buffers.  `done` (device flag or
-// NULL) turns the launches into no-ops.
+// NULL) turns the launches into no-ops; `status` (device int or NULL) receives a wait
+// timeout of the plane-staged layer.  Inference on a lexicographic hex mesh runs that
+// layer (learned_hex.cu, the same bits as k_lp_layer).
 void enqueue_forward(fcg_learned *Lp, fcg_context *c, cudaStream_t st, const float *r, bool train,
-                     const int *done, unsigned *rms_ticket) {
+                     const int *done, unsigned *rms_ticket, int *status) {
   const int n = c->n;
   float *rms = Lp->scal.as<float>();
   const float *prm = Lp->params.as<float>();
@@ -1268,6 +1233,10 @@ void enqueue_forward(fcg_learned *Lp, fcg_context *c, cudaStream_t st, const flo
       k_lp_agg<<<grid_for(4LL * n, c->num_sms, 8), kTPB, 0, st>>>(c->sv, n, aval, hin, H + 2 * hs,
                                                                  done);
       k_lp_dense<<<lg, kTPB, 0, st>>>(n, hin, H + 2 * hs, hout, wl, bl, done);
+    } else if (!train && hex_on(Lp, c) &&
+               fcg::lphex::layer(Lp->hex, c->num_sms, hin, hout, Lp->hexval.as<float>(), wl, bl,
+                                 done, status, st) == cudaSuccess) {
+      // plane-staged form launched
     } else {
       k_lp_layer<<<lg, kTPB, 0, st>>>(c->sv, n, aval, hin, hout, wl, bl,
                                       train ? Lp->mbuf.as<float>() + l * hs : nullptr,
@@ -1335,7 +1304,7 @@ int loss_grad(fcg_learned *Lp, fcg_context *c, const float *r, const float *e) {
   const int n = c->n;
   cudaStream_t st = c->stream;
   unsigned *tk = Lp->scal.as<unsigned>() + 16;
-  enqueue_forward(Lp, c, st, r, true, nullptr, tk + 1);
+  enqueue_forward(Lp, c, st, r, true, nullptr, tk + 1, nullptr);
   float *rms = Lp->scal.as<float>();
   float *sums = rms + 2;
   const float *prm = Lp->params.as<float>();
@@ -1606,7 +1575,8 @@ extern "C" int fcg_lp_apply(fcg_learned *Lp, fcg_context *c, const float *r, flo
   bool hr, hz;
   if ((rc = stage_f32(Lp, c, r, 4, true, &dr, &hr))) return rc;
   if ((rc = stage_f32(Lp, c, z, 5, false, &dz, &hz))) return rc;
-  enqueue_forward(Lp, c, c->stream, dr, false, nullptr, Lp->scal.as<unsigned>() + 17);
+  enqueue_forward(Lp, c, c->stream, dr, false, nullptr, Lp->scal.as<unsigned>() + 17,
+                  Lp->scal.as<int>() + kHexStatus);
   k_lp_out<<<grid_for(c->n, c->num_sms), kTPB, 0, c->stream>>>(
       c->n, last_activation(Lp, c, false), Lp->params.as<float>(), Lp->scal.as<float>(), dr,
       nullptr, nullptr, nullptr, dz);
@@ -1614,6 +1584,7 @@ extern "C" int fcg_lp_apply(fcg_learned *Lp, fcg_context *c, const float *r, flo
   if ((rc = stage_out(c, z, dz, sizeof(float) * c->n, hz)))
     return lp_fail(Lp, rc, fcg_last_error(c));
   LP_TRY(Lp, cudaStreamSynchronize(c->stream));
+  if ((rc = hex_status(Lp, c))) return rc;
   return mark_done(Lp, c);
 }
 
@@ -1657,6 +1628,11 @@ extern "C" int fcg_lp_profile(fcg_learned *Lp, fcg_context *c, const float *r, i
             c->sv, n, scaled32(c), H + (l % 2) * hs, H + 2 * hs, nullptr);
         k_lp_dense<<<lg, kTPB, 0, st>>>(n, H + (l % 2) * hs, H + 2 * hs, H + ((l + 1) % 2) * hs,
                                         wl, bl, nullptr);
+      } else if (hex_on(Lp, c) &&
+                 fcg::lphex::layer(Lp->hex, c->num_sms, H + (l % 2) * hs,
+                                   H + ((l + 1) % 2) * hs, Lp->hexval.as<float>(), wl, bl,
+                                   nullptr, Lp->scal.as<int>() + kHexStatus, st) == cudaSuccess) {
+        // plane-staged form launched
       } else {
         k_lp_layer<<<lg, kTPB, 0, st>>>(c->sv, n, scaled32(c), H + (l % 2) * hs,
                                         H + ((l + 1) % 2) * hs, wl, bl, nullptr, nullptr, nullptr);
@@ -1677,10 +1653,26 @@ extern "C" int fcg_lp_profile(fcg_learned *Lp, fcg_context *c, const float *r, i
     }
   }
   for (auto &e : ev) cudaEventDestroy(e);
+  if ((rc = hex_status(Lp, c))) return rc;
   const int nu = std::min(U, max_units);
   for (int u = 0; u < nu; ++u) ms[u] = acc[u] / reps;
   if (units) *units = U;
   return mark_done(Lp, c);
+}
+
+extern "C" int fcg_lp_layer_form(fcg_learned *Lp, fcg_context *c, int *form, int *dims) {
+  int rc = check_ctx(Lp, c);
+  if (rc) return rc;
+  if (!form) return lp_fail(Lp, FCG_ERR_ARG, "NULL form");
+  if ((rc = matrix_ready(Lp, c))) return rc;
+  const bool on = hex_on(Lp, c);
+  *form = on ? FCG_LP_LAYER_PLANES : FCG_LP_LAYER_GATHER;
+  if (dims) {
+    dims[0] = on ? Lp->hex.nx : 0;
+    dims[1] = on ? Lp->hex.ny : 0;
+    dims[2] = on ? Lp->hex.nz : 0;
+  }
+  return FCG_OK;
 }
 
 // loss = ||N(r) - e||^2 / ||e||^2 and its gradient with respect to the FP32 weights.
@@ -1785,7 +1777,8 @@ void enqueue_preconditioner(fcg_learned *Lp, fcg_context *c, cudaStream_t st, co
     fcg::ml::enqueue_jacobi_cycle(*ml_for(Lp, c), c, Lp->mlo, st, r, z, done);
     return;
   }
-  enqueue_forward(Lp, c, st, r, false, done, rms_ticket);
+  enqueue_forward(Lp, c, st, r, false, done, rms_ticket,
+                  S ? &S->status : Lp->scal.as<int>() + kHexStatus);
   if (S)
     k_f_out<<<reduction_grid(c), kTPB, 0, st>>>(n, last_activation(Lp, c, false),
                                                 Lp->params.as<float>(), Lp->scal.as<float>(), r,
@@ -1805,7 +1798,7 @@ void enqueue_body_head(fcg_learned *Lp, fcg_context *c, cudaStream_t st, const F
   double *red = Lp->red.as<double>();
   const int *done = &Lp->S->done;
   if (!ml_on(Lp, c)) {
-    enqueue_forward(Lp, c, st, v.r, false, done, &Lp->S->ticket[6]);
+    enqueue_forward(Lp, c, st, v.r, false, done, &Lp->S->ticket[6], &Lp->S->status);
     k_f_out<<<G, kTPB, 0, st>>>(n, last_activation(Lp, c, false), Lp->params.as<float>(),
                                 Lp->scal.as<float>(), v.r, v.z, v.q, v.stride, Lp->S, red, 1);
   } else {
@@ -1838,7 +1831,8 @@ int build_fcg_graph(fcg_learned *Lp, fcg_context *c, const FcgVecs &v) {
                                    (const void *)(uintptr_t)Lp->mlo.sweeps,
                                    (const void *)(uintptr_t)(Lp->mlo.alpha * 1e6),
                                    (const void *)(uintptr_t)(Lp->mlo.omega * 1e6),
-                                   (const void *)(uintptr_t)Lp->mlo.smoothed};
+                                   (const void *)(uintptr_t)Lp->mlo.smoothed,
+                                   (const void *)(uintptr_t)hex_on(Lp, c), Lp->hexval.p};
   if (Lp->exec && key == Lp->graph_key) return FCG_OK;
   if (Lp->exec) cudaGraphExecDestroy(Lp->exec);
   if (Lp->graph) cudaGraphDestroy(Lp->graph);
@@ -2127,6 +2121,7 @@ extern "C" int fcg_lp_precondition(fcg_learned *Lp, fcg_context *c, const float 
   if ((rc = stage_out(c, z, dz, sizeof(float) * c->n, hz)))
     return lp_fail(Lp, rc, fcg_last_error(c));
   LP_TRY(Lp, cudaStreamSynchronize(c->stream));
+  if ((rc = hex_status(Lp, c))) return rc;
   return mark_done(Lp, c);
 }
 

@@ -152,6 +152,16 @@ class LearnedPreconditioner:
         names.append("k_lp_out")
         return {names[i]: ms[i] for i in range(nu.value)}
 
+    def layer_form(self, ctx: Context) -> dict:
+        """Which form of the layer kernel inference runs on ctx's mesh: "planes" (the
+        cells form a lexicographic hex block; planes staged by TMA copies) or "gather"
+        (the sliced gather, any mesh).  Both give the same bits."""
+        form = C.c_int()
+        dims = (C.c_int * 3)()
+        self._check(self.lib.fcg_lp_layer_form(self.h, ctx.h, C.byref(form), dims),
+                    "fcg_lp_layer_form")
+        return {"form": "planes" if form.value == 1 else "gather", "dims": tuple(dims)}
+
     def set_loss(self, kind: str = "residual"):
         """Training loss: "residual" (|Ahat N(r) - r|^2 / |r|^2, the default), "energy"
         ((N(r)-e).Ahat(N(r)-e) / e.Ahat e) or "cycle" ((M(r)-e).Ahat(M(r)-e) / e.Ahat e

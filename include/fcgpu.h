@@ -546,6 +546,15 @@ int fcg_lp_last_solve_stats(const fcg_learned *lp, int *iters, int *updates);
  * message-passing layers, 8 output (*units receives 9). */
 int fcg_lp_profile(fcg_learned *lp, fcg_context *ctx, const float *r, int reps, double *ms,
                    int max_units, int *units);
+/* Which form of the message-passing layer inference runs for ctx's mesh (no reference
+ * counterpart; valid after fcg_lp_set_matrix): *form = FCG_LP_LAYER_GATHER (the sliced
+ * gather over the CSR pattern, any mesh) or FCG_LP_LAYER_PLANES (the cells form a
+ * lexicographic nx x ny x nz hex block: planes staged by TMA copies; the same bits).
+ * dims (may be NULL) receives nx, ny, nz for the plane form.  The environment variable
+ * FCG_LP_LAYER=gather keeps the gather form on every mesh. */
+#define FCG_LP_LAYER_GATHER 0
+#define FCG_LP_LAYER_PLANES 1
+int fcg_lp_layer_form(fcg_learned *lp, fcg_context *ctx, int *form, int *dims);
 
 /* Coarse-grid correction of the flexible CG (on by default).  The preconditioner is
  *   M(r) = z + alpha P V(P^T (r - Ahat z)),  z = N(r),
