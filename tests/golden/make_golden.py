@@ -1,8 +1,9 @@
 """Regenerates the golden fixtures in this folder from the freeCappuccino source tree.
 
-Run once in a checkout that has the reference mounted (default ``/root/reference``):
+Run once with the root of a freeCappuccino source tree (the folder that holds ``src/``,
+``tests/`` and ``examples/``):
 
-    python tests/golden/make_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_golden.py REFERENCE_ROOT
 
 It writes
   * ``sparse_solvers.json``       -- the two 5x5 dense-as-CSR systems of
@@ -125,7 +126,9 @@ def meshes(ref: str):
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py REFERENCE_ROOT")
+    ref = sys.argv[1]
     sparse_solver_systems(ref)
     meshes(ref)
     print("golden fixtures written to", HERE)
