@@ -494,6 +494,41 @@ def run_section(which, ctx, m, mu, phi, su, dev, stream):
     return out
 
 
+def run_network_gain(dev, sizes=(64, 128), seed=SEED + 5):
+    """What the network gains inside the shipped cycle: the learned FCG (the network
+    followed by the coarse-grid correction) against the same FCG with Jacobi sweeps in
+    the network's place, on N^3 meshes jittered by 0.2 h with the smoothed log-uniform
+    diffusivity on [0.1, 10] of the learned-preconditioner configuration, with the
+    library's default cycle (2 sweeps per level).  Device arrays; each time is the
+    solve's own event-timed duration (rep.seconds) after one warm-up solve."""
+    import torch
+
+    from freecappuccino_gb300.learned import (DEFAULT_WEIGHTS, LearnedPreconditioner,
+                                              pressure_system)
+
+    out = {}
+    for N in sizes:
+        sysm = pressure_system(N, JITTER, seed, variable=True, device=dev.index or 0)
+        a = torch.from_numpy(sysm.a).to(dev)
+        su = torch.from_numpy(sysm.su).to(dev)
+        x0 = torch.zeros(sysm.ctx.n, dtype=torch.float64, device=dev)
+        lp = LearnedPreconditioner(device=dev.index or 0, path=DEFAULT_WEIGHTS)
+        row = {}
+        for sm in ("network", "jacobi"):
+            lp.set_multilevel(smoother=sm)
+            lp.solve(sysm.ctx, a, su, x0, TOL, NSW)
+            r = lp.solve(sysm.ctx, a, su, x0, TOL, NSW)
+            row[sm] = {"fcg_iterations": r.fcg_iters, "seconds": r.seconds, "l2_rel": r.l2_rel,
+                       "converged": r.converged}
+        row["iterations_jacobi_over_network"] = (row["jacobi"]["fcg_iterations"] /
+                                                 row["network"]["fcg_iterations"])
+        row["time_network_over_jacobi"] = row["network"]["seconds"] / row["jacobi"]["seconds"]
+        out[f"{N}^3"] = row
+        lp.close()
+        sysm.ctx.close()
+    return out
+
+
 def run_multi(dev, N=128, seed=SEED + 2):
     """The five transport systems (u, v, w, k, eps) on one pattern solved in one
     multi-RHS BiCGStab (FP32 DILU inner, FP64 correction to 1e-10) against the same
@@ -564,7 +599,7 @@ def main():
                     help="Jacobi sweeps per level of the coarse-grid correction (library default 2)")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven sweep loop instead of the CUDA-graph WHILE loop")
-    ap.add_argument("--only", choices=["assembly", "layer", "solvers"], default=None,
+    ap.add_argument("--only", choices=["assembly", "layer", "solvers", "gain"], default=None,
                     help="run one section alone on the --N mesh and print it (profiling): "
                          "the face-loop entry points, the network's forward kernels, or a "
                          "fixed number of sweeps of each solver")
@@ -596,6 +631,12 @@ def main():
         out = run_assembly(ctx, m, torch.device("cuda", local), stream, peaks()[0])
         if rank == 0:
             print(json.dumps({"section": "assembly", "N": N, **out}), flush=True)
+        ctx.close()
+        return
+    if args.only == "gain":
+        out = run_network_gain(torch.device("cuda", local))
+        if rank == 0:
+            print(json.dumps({"section": "gain", **out}), flush=True)
         ctx.close()
         return
     if args.only in ("layer", "solvers"):
@@ -701,9 +742,16 @@ def main():
         layers = [v for k, v in prof.items() if k.startswith("k_lp_layer")]
         t_dom = statistics.mean(layers) * 1e-3
         dom_bytes = 128 * n + 4 * nnz  # BF16 activations in and out, FP32 Ahat values
-        dom_desc = ("k_lp_layer (one message-passing layer: gather of BF16 neighbour rows "
-                    "through the FP32 scaled matrix, 16x64x32 mma.sync BF16 tiles, 256^3)")
-        dom = "k_lp_layer"
+        if lp.layer_form(ctx)["form"] == "planes":
+            dom = "k_lp_layer_hex"
+            dom_desc = ("k_lp_layer_hex (one message-passing layer on the hex block: 18x18-cell "
+                        "planes of BF16 activations and the stencil value planes streamed by "
+                        "TMA tensor copies into a 5-stage mbarrier ring, 16 consumer warps, "
+                        f"16x64x32 mma.sync BF16 tiles, {N}^3)")
+        else:
+            dom = "k_lp_layer"
+            dom_desc = ("k_lp_layer (one message-passing layer: gather of BF16 neighbour rows "
+                        f"through the FP32 scaled matrix, 16x64x32 mma.sync BF16 tiles, {N}^3)")
         prof_extra = {"forward_kernels_ms": prof, "forward_ms": sum(prof.values()),
                       "layer_tensor_TFLOPs": 4096.0 * n / t_dom / 1e12}
     else:
@@ -803,11 +851,12 @@ def main():
     batch = None
     if not args.no_batch:
         batch = run_batch(args, dev, peak)
-    calcp = multi = assembly = None
+    calcp = multi = assembly = gain = None
     if not args.no_configs:
         calcp = run_calcp(dev)
         multi = run_multi(dev)
         assembly = run_assembly(ctx, m, dev, stream, peak)
+        gain = run_network_gain(dev)
 
     cpu = parity = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -820,7 +869,8 @@ def main():
         extra = {"comparisons": comparisons, "spmv_fp64": spmv64,
                  "l2_rel_final": last.l2_rel, "resl_over_res0": last.resl / last.res0,
                  "mesh_setup_s": t_mesh, "bind_s": t_bind, "step_s": step_s, "batched": batch,
-                 "calcp_step": calcp, "multi_rhs": multi, "assembly": assembly}
+                 "calcp_step": calcp, "multi_rhs": multi, "assembly": assembly,
+                 "network_gain": gain}
         if method == "learned":
             extra["learned"] = {"fcg_iterations": last.fcg_iters, "fallback": last.fallback,
                                 "directions": 8, "weights": os.path.relpath(

@@ -385,6 +385,7 @@ extern "C" int fcg_bind_mesh(fcg_context *c, const fcg_mesh_desc *m) {
       rec(c->lb.pad, sizeof(int) * c->lb.pad_len);
     }
   }
+  if ((rc = detect_hex_block(c))) return rc;
   c->bound = true;
   c->bind_gen++;
   return FCG_OK;

@@ -70,6 +70,16 @@ struct SellView {
   const int *src;       // [len] CSR position of each value slot (-1: no entry)
 };
 
+// A mesh whose cells form a lexicographic nx x ny x nz hexahedral block: cell
+// r = i + nx j + nx ny k, and row r of the CSR pattern holds exactly the cell itself and
+// its face neighbours inside the block, so the lower entries of a row are (when present)
+// -nx ny, -nx, -1 and the upper ones +1, +nx, +nx ny, in that order.  Found at bind time
+// (hexblock.cu); kernels with a plane-staged or wavefront-tiled form use it.
+struct HexBlock {
+  int nx = 0, ny = 0, nz = 0;
+  bool ok = false;
+};
+
 struct Level {
   std::vector<int> ptr;  // host: level offsets into rows
   int *rows = nullptr;   // device: rows sorted by level, ascending inside a level
@@ -113,6 +123,7 @@ struct fcg_context {
   int sell_maxw = 0;
   long long sell_len = 0, sell_nuniform = 0;
   fcg::Level lf, lb;  // forward (lower) and backward (upper) level schedules
+  fcg::HexBlock hex;  // the block structure of the cell numbering, when it has one
   const int *tpos = nullptr;  // CSR position of the transpose entry of every entry
   // every topology array bound to the device (pointer, bytes), for fcg_topology_digest
   std::vector<std::pair<const void *, size_t>> topo;
@@ -165,6 +176,8 @@ int build_rest(const fcg_mesh_desc &m, const int cnt[B_NTYPES], const int fst[B_
 // the device copies (0-based) of owner / neighbour, own_host the 1-based host owner.
 // a[i] -= 1 on the device (1-based index arrays to 0-based), on c's stream.
 int to_zero_based(fcg_context *c, int *a, long long n);
+// Fills c->hex from the bound CSR pattern (hexblock.cu); synchronises c's stream.
+int detect_hex_block(fcg_context *c);
 int bind_topology_device(fcg_context *c, const int *own0, const int *nei0,
                          const std::vector<int> &own_host, const int cnt[B_NTYPES],
                          const int fst[B_NTYPES], const int bst[B_NTYPES], std::string &err);

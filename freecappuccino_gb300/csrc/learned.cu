@@ -1132,9 +1132,9 @@ bool features_current(const fcg_learned *Lp, const fcg_context *c) {
          scaled32(c) != nullptr;
 }
 
-// Device ints of the scal buffer used by the plane-staged layer: scratch of the mesh
-// check, and the status a layer outside a solve reports a wait timeout to.
-constexpr int kHexFlag = 40, kHexStatus = 41;
+// Device int of the scal buffer that a plane-staged layer outside a solve reports a wait
+// timeout to.
+constexpr int kHexStatus = 41;
 
 // The plane-staged layer serves inference on lexicographic hex meshes; FCG_LP_LAYER=gather
 // (or =split) keeps the sliced gather form everywhere.
@@ -1152,7 +1152,7 @@ bool hex_on(const fcg_learned *Lp, const fcg_context *c) {
 int hex_prepare(fcg_learned *Lp, fcg_context *c) {
   if (Lp->hex_uid != c->uid || Lp->hex_gen != c->bind_gen) {
     fcg::lphex::HexGrid g;
-    int rc = fcg::lphex::detect(c, Lp->scal.as<int>() + kHexFlag, &g);
+    int rc = fcg::lphex::detect(c, &g);
     if (rc) return lp_fail(Lp, rc, fcg_last_error(c));
     if (g.ok) {
       const size_t bytes = sizeof(float) * fcg::lphex::value_count(g);

@@ -16,7 +16,7 @@
 //     five shared-memory stages with TMA tensor copies (cp.async.bulk.tensor, 4-D
 //     tensor maps over this GPU's memory, zero fill outside the block), each stage
 //     signalled by an mbarrier with a transaction count;
-//   - eight consumer warps compute plane k from stages k-1, k and k+1: per cell
+//   - sixteen consumer warps compute plane k from stages k-1, k and k+1: per cell
 //     m = sum over the seven directions of val[d] * h[neighbour], summed in the CSR column
 //     order with the same fused multiply-adds as the gather form; then the per-warp
 //     16-cell tile [h; m] goes through the shared mma.sync product and epilogue
@@ -47,7 +47,7 @@ constexpr int BX = 16, BY = 16;          // cells of a tile in i and j
 constexpr int HX = BX + 2, HY = BY + 2;  // with the one-cell halo
 constexpr int S = 5;                     // ring stages (planes)
 constexpr int KC = 32;                   // planes computed by one block
-constexpr int kCons = 8;                 // consumer warps
+constexpr int kCons = 16;                // consumer warps, one j row of the tile each
 constexpr int kThreads = (kCons + 1) * 32;
 constexpr unsigned kHBytes = HY * HX * C * 2;
 constexpr unsigned kVBytes = 7 * BY * BX * 4;
@@ -242,24 +242,6 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
-// Row r of a lexicographic hex block: each entry must be the row itself or a face
-// neighbour inside the block.  Counts the rows that are not.
-__global__ void k_hex_check(int n, const int *__restrict__ io, const int *__restrict__ ja, int nx,
-                            int ny, int nz, int *bad) {
-  const long long nxy = (long long)nx * ny;
-  FCG_GRID_STRIDE(r, n) {
-    const int i = (int)(r % nx), j = (int)((r / nx) % ny), k = (int)(r / nxy);
-    bool good = true;
-    for (int e = io[r]; e < io[r + 1]; ++e) {
-      const long long d = (long long)ja[e] - r;
-      good = good && (d == 0 || (d == -1 && i > 0) || (d == 1 && i < nx - 1) ||
-                      (d == -nx && j > 0) || (d == nx && j < ny - 1) ||
-                      (d == -nxy && k > 0) || (d == nxy && k < nz - 1));
-    }
-    if (!good) atomicAdd(bad, 1);
-  }
-}
-
 // Stencil value planes from the sliced FP32 matrix (real entries only: pads are skipped).
 __global__ void k_hex_values(SellView s, int n, const float *__restrict__ aval, int nx, int ny,
                              int nz, int nxp, float *__restrict__ val) {
@@ -348,37 +330,15 @@ cudaError_t set_attributes(int dev) {
 
 }  // namespace
 
-int detect(fcg_context *c, int *dflag, HexGrid *g) {
+int detect(fcg_context *c, HexGrid *g) {
   *g = HexGrid();
-  const int n = c->n;
-  if (n < 8 || !encoder()) return FCG_OK;
-  int io[2] = {0, 0};
-  FCG_CUDA_TRY(c, cudaMemcpyAsync(io, c->mv.ioffset, sizeof io, cudaMemcpyDeviceToHost, c->stream));
-  FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-  if (io[1] - io[0] != 4) return FCG_OK;  // a corner cell has three face neighbours
-  int col[4];
-  FCG_CUDA_TRY(c, cudaMemcpyAsync(col, c->mv.ja + io[0], sizeof col, cudaMemcpyDeviceToHost,
-                                  c->stream));
-  FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-  const long long nx = col[2], nxy = col[3];
-  if (col[0] != 0 || col[1] != 1 || nx < 2 || nxy <= nx || nxy % nx != 0 || n % nxy != 0)
-    return FCG_OK;
-  const long long ny = nxy / nx, nz = n / nxy;
-  if (ny < 2 || nz < 2) return FCG_OK;
-  FCG_CUDA_TRY(c, cudaMemsetAsync(dflag, 0, sizeof(int), c->stream));
-  k_hex_check<<<grid_for(n, c->num_sms), kTPB, 0, c->stream>>>(n, c->mv.ioffset, c->mv.ja,
-                                                               (int)nx, (int)ny, (int)nz, dflag);
-  FCG_CHECK_LAUNCH(c, "k_hex_check");
-  int bad = -1;
-  FCG_CUDA_TRY(c, cudaMemcpyAsync(&bad, dflag, sizeof bad, cudaMemcpyDeviceToHost, c->stream));
-  FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-  if (bad != 0) return FCG_OK;
+  if (!c->hex.ok || !encoder()) return FCG_OK;
   FCG_CUDA_TRY(c, set_attributes(c->device));
   HexGrid t;
-  t.nx = (int)nx;
-  t.ny = (int)ny;
-  t.nz = (int)nz;
-  t.nxp = (int)((nx + 3) / 4 * 4);
+  t.nx = c->hex.nx;
+  t.ny = c->hex.ny;
+  t.nz = c->hex.nz;
+  t.nxp = (t.nx + 3) / 4 * 4;
   // a trial encoding on aligned placeholder addresses: maps that the driver refuses
   // (extents beyond its limits) leave the gather form in use
   CUtensorMap th, tv;

@@ -18,13 +18,11 @@ struct HexGrid {
   bool ok = false;
 };
 
-// Finds whether the bound mesh's CSR pattern is that of a lexicographic hex block: row 0
-// gives nx and nx*ny (its columns are 0, 1, nx, nx*ny), and a kernel then checks that
-// every entry of every row is the row itself or one of its six face neighbours inside the
-// block (dflag: one device int of scratch).  Synchronises c's stream.  g->ok is false for
-// any other mesh.  Call it outside stream capture: it also sets the layer kernel's
-// shared-memory limit on c's device.
-int detect(fcg_context *c, int *dflag, HexGrid *g);
+// The grid of the plane-staged layer for c's mesh: g->ok when the mesh is a lexicographic
+// hex block (c->hex, found at bind time) and the driver accepts the tensor maps.  Call
+// it outside stream capture: it also sets the layer kernel's shared-memory limit on c's
+// device.
+int detect(fcg_context *c, HexGrid *g);
 
 // Floats of the stencil value planes: 7 directions x nz x ny x nxp.
 inline size_t value_count(const HexGrid &g) { return 7ull * g.nz * g.ny * g.nxp; }

@@ -34,9 +34,16 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4],
 // for eight channels.  The explicit fused multiply-add fixes the rounding for every
 // kernel form.
 __device__ __forceinline__ void fma8(float (&acc)[8], float v, const uint4 &q) {
-  const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(&q);
+  const __nv_bfloat162 *e = reinterpret_cast<const __nv_bfloat162 *>(&q);
+  const float2 vv = make_float2(v, v);
 #pragma unroll
-  for (int c = 0; c < 8; ++c) acc[c] = __fmaf_rn(v, bf(e[c]), acc[c]);
+  for (int c = 0; c < 4; ++c) {
+    // packed FP32 FMA: each half is fma(v, h, acc), rounded to nearest
+    const float2 r =
+        __ffma2_rn(vv, __bfloat1622float2(e[c]), make_float2(acc[2 * c], acc[2 * c + 1]));
+    acc[2 * c] = r.x;
+    acc[2 * c + 1] = r.y;
+  }
 }
 
 // Stores row `row` of the warp's tile: own = the cell's h (8 channels at qc), acc = its

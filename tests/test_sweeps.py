@@ -1,7 +1,9 @@
-"""DIC / DILU triangular sweeps in one launch (rows waiting on the rows they read)
-against the level-by-level launches: the same row arithmetic, so the same bits.  And the
-timeout path of the dependency waits: a row that never announces its result makes the
-solve return FCG_ERR_TIMEOUT, and the context then solves normally."""
+"""DIC / DILU triangular sweeps in their three kernel forms against each other: one
+launch per level, one launch with rows waiting on the rows they read, and (on meshes
+that form a lexicographic hex block) the wavefront-tiled launch.  All use the same row
+arithmetic in the same entry order, so the same bits.  And the timeout path of the
+dependency waits: a row that never announces its result makes the solve return
+FCG_ERR_TIMEOUT, and the context then solves normally."""
 import os
 
 import numpy as np
@@ -15,12 +17,14 @@ from tests.meshes import fixture_mesh, hex_mesh, oracle_csr, poisson_system
 pytestmark = pytest.mark.gpu
 
 
-def _context(m, levels: bool):
+def _context(m, levels):
     """A context whose solver state (created at its first solve) uses the level
-    launches or the one-launch sweeps."""
+    launches (levels=True or "levels"), the row-claiming one-launch sweeps ("rows") or
+    the default (False: wavefront tiles on hex blocks, rows elsewhere)."""
     old = os.environ.get("FCG_SWEEP")
-    if levels:
-        os.environ["FCG_SWEEP"] = "levels"
+    mode = "levels" if levels is True else levels
+    if mode:
+        os.environ["FCG_SWEEP"] = mode
     else:
         os.environ.pop("FCG_SWEEP", None)
     try:
@@ -34,21 +38,24 @@ def _context(m, levels: bool):
     return c
 
 
-@pytest.mark.parametrize("name", ["hex12", "pitzdaily"])
+@pytest.mark.parametrize("name", ["hex12", "hex20", "hex33", "pitzdaily"])
 def test_one_launch_sweeps_equal_level_sweeps(name):
-    m = hex_mesh(12, 0.2) if name == "hex12" else fixture_mesh("pitzdaily")
-    a_ctx, b_ctx = _context(m, False), _context(m, True)
+    """hex12 is one 8 x 8 tile and a partial one, hex20 and hex33 cut tiles at the block
+    edge and have tiles that wait on several others; pitzDaily is not a block (no
+    wavefront form)."""
+    m = fixture_mesh("pitzdaily") if name == "pitzdaily" else hex_mesh(int(name[3:]), 0.2)
+    ctxs = [_context(m, mode) for mode in (False, "rows", "levels")]
     mu, phi, su0 = poisson_system(m)
-    a, su = a_ctx.laplacian(mu, phi, su0)
+    a, su = ctxs[0].laplacian(mu, phi, su0)
     x0 = np.zeros(m.numCells)
     for solver in ("iccg", "bicgstab"):
         for sor, nsw in ((0.0, 30), (1e-8, 3000)):
-            r1 = getattr(a_ctx, solver)(a, su, x0, sor, nsw)
-            r2 = getattr(b_ctx, solver)(a, su, x0, sor, nsw)
-            assert r1.iters == r2.iters and np.array_equal(r1.fi, r2.fi), (solver, sor)
-            assert r1.resl == r2.resl
-    a_ctx.close()
-    b_ctx.close()
+            r = [getattr(c, solver)(a, su, x0, sor, nsw) for c in ctxs]
+            for other in r[1:]:
+                assert other.iters == r[0].iters and np.array_equal(other.fi, r[0].fi), (solver, sor)
+                assert other.resl == r[0].resl
+    for c in ctxs:
+        c.close()
 
 
 def test_sweep_wait_runs_out_and_device_stays_usable():
