@@ -79,3 +79,24 @@ def test_other_meshes_use_the_gather_form():
         assert np.isfinite(z).all()
         lp.close()
         c.close()
+
+
+def test_tensor_memory_form_equals_mma_sync_form():
+    """The plane-staged layer with its tile product on tcgen05 (accumulator in tensor
+    memory, FCG_LP_HEX_MMA=tc) gives the same bits as with mma.sync."""
+    sysm = pressure_system(20, 0.2, 4, variable=True)
+    lp = LearnedPreconditioner(path=DEFAULT_WEIGHTS)
+    lp.set_matrix(sysm.ctx, sysm.a)
+    r = fcg.uniform(20, 3, sysm.ctx.n, -1.0, 1.0).astype(np.float32)
+    z_sync = lp.apply(sysm.ctx, r)
+    old = os.environ.get("FCG_LP_HEX_MMA")
+    os.environ["FCG_LP_HEX_MMA"] = "tc"
+    try:
+        z_tc = lp.apply(sysm.ctx, r)
+    finally:
+        if old is None:
+            os.environ.pop("FCG_LP_HEX_MMA", None)
+        else:
+            os.environ["FCG_LP_HEX_MMA"] = old
+    assert np.array_equal(z_sync, z_tc)
+    lp.close()
