@@ -22,16 +22,70 @@ using namespace fcg;
 namespace {
 
 // ---------------------------------------------------------------------------
+// Mesh-constant factors of the inner faces, computed once per bound mesh by the same
+// rounded operations the face loops use, so that the loops that read them give the same
+// bits as recomputing them (sqrt and divisions dominate those loops on this part's FP64
+// pipe).  Planar: plane q holds factor q of every inner face.
+// ---------------------------------------------------------------------------
+enum FaceGeo {
+  FG_NX, FG_NY, FG_NZ,    // unit normal S/|S|
+  FG_SFDPNR,              // 1/(arx xpn nx + ary ypn ny + arz zpn nz)   (facefluxmass.f90:94)
+  FG_SMDPN,               // |S|^2 sfdpnr                                (:95)
+  FG_DPPNNR,              // 1/(xpn nx + ypn ny + zpn nz)                (facefluxmass.f90:578)
+  FG_XPP, FG_YPP, FG_ZPP, // P' - P: (f - (f - P) n) - P                 (:155-172, :586-595)
+  FG_XEP, FG_YEP, FG_ZEP, // N' - N
+  FG_DXP, FG_DYP, FG_DZP, // face centre - P
+  FG_DXQ, FG_DYQ, FG_DZQ, // face centre - N
+  FG_XPN, FG_YPN, FG_ZPN, // N - P
+  FG_ARE,                 // |S|
+  FG_SMDPN_LAP,           // |S|^2 / (S . (N - P))                        (fvm_laplacian.f90:214)
+  FG_DPN,                 // |N - P|                                     (facefluxmass.f90:334)
+  FG_COUNT
+};
+
+__global__ void k_face_geo(MeshView m, double *__restrict__ g) {
+  const long long nin = m.nin;
+  FCG_GRID_STRIDE(f, nin) {
+    const int p = m.owner[f], q = m.neighbour[f];
+    const double xf = m.xf[f], yf = m.yf[f], zf = m.zf[f];
+    const double arx = m.arx[f], ary = m.ary[f], arz = m.arz[f];
+    const double xpn = m.xc[q] - m.xc[p], ypn = m.yc[q] - m.yc[p], zpn = m.zc[q] - m.zc[p];
+    const double are = sqrt(arx * arx + ary * ary + arz * arz);
+    const double nxx = arx / are, nyy = ary / are, nzz = arz / are;
+    const double sfdpnr = 1.0 / (arx * xpn * nxx + ary * ypn * nyy + arz * zpn * nzz);
+    double xpp = xf - (xf - m.xc[p]) * nxx, ypp = yf - (yf - m.yc[p]) * nyy,
+           zpp = zf - (zf - m.zc[p]) * nzz;
+    double xep = xf - (xf - m.xc[q]) * nxx, yep = yf - (yf - m.yc[q]) * nyy,
+           zep = zf - (zf - m.zc[q]) * nzz;
+    xpp = xpp - m.xc[p];
+    ypp = ypp - m.yc[p];
+    zpp = zpp - m.zc[p];
+    xep = xep - m.xc[q];
+    yep = yep - m.yc[q];
+    zep = zep - m.zc[q];
+    const double v[FG_COUNT] = {
+        nxx, nyy, nzz, sfdpnr, (arx * arx + ary * ary + arz * arz) * sfdpnr,
+        1.0 / ((xpn * nxx) + (ypn * nyy) + (zpn * nzz)), xpp, ypp, zpp, xep, yep, zep,
+        xf - m.xc[p], yf - m.yc[p], zf - m.zc[p], xf - m.xc[q], yf - m.yc[q], zf - m.zc[q],
+        xpn, ypn, zpn, are,
+        (arx * arx + ary * ary + arz * arz) / (arx * xpn + ary * ypn + arz * zpn),
+        sqrt(xpn * xpn + ypn * ypn + zpn * zpn)};
+#pragma unroll
+    for (int k = 0; k < FG_COUNT; ++k) g[k * nin + f] = v[k];
+  }
+}
+
+// ---------------------------------------------------------------------------
 // laplacian(mu,phi)
 // ---------------------------------------------------------------------------
-__global__ void k_lap_faces(MeshView m, const double *__restrict__ mu, double *__restrict__ a) {
-  FCG_GRID_STRIDE(f, m.nin) {
+__global__ void k_lap_faces(MeshView m, const double *__restrict__ g, const double *__restrict__ mu,
+                            double *__restrict__ a) {
+  const long long nin = m.nin;
+  FCG_GRID_STRIDE(f, nin) {
     int p = m.owner[f], q = m.neighbour[f];
-    double arx = m.arx[f], ary = m.ary[f], arz = m.arz[f];
     double fxn = m.facint[f];  // facefluxlaplacian :195-196
     double fxp = 1.0 - fxn;
-    double xpn = m.xc[q] - m.xc[p], ypn = m.yc[q] - m.yc[p], zpn = m.zc[q] - m.zc[p];
-    double smdpn = (arx * arx + ary * ary + arz * arz) / (arx * xpn + ary * ypn + arz * zpn);
+    double smdpn = g[FG_SMDPN_LAP * nin + f];  // :214
     double cap = (fxp * mu[p] + fxn * mu[q]) * smdpn;  // :218, can = cap
     a[m.slot_pn[f]] = cap;                              // :48-49
     a[m.slot_np[f]] = cap;                              // :52-53
@@ -66,52 +120,45 @@ struct FlowView {
   const double *u, *v, *w, *p, *dU, *dV, *dW, *dP, *apu, *apv, *apw, *den;
 };
 
-// face_value_central, interpolation.f90:145-199
-__device__ __forceinline__ double face_value_central(const MeshView &m, int p, int q, double xf,
-                                                     double yf, double zf,
-                                                     const double *__restrict__ fi,
+// face_value_central, interpolation.f90:145-199, with the face centre's offsets from P
+// (dxp..) and N (dxq..)
+__device__ __forceinline__ double face_value_central(int p, int q, double dxp, double dyp,
+                                                     double dzp, double dxq, double dyq,
+                                                     double dzq, const double *__restrict__ fi,
                                                      const double *__restrict__ g) {
-  double gradfidr = g[3 * p] * (xf - m.xc[p]) + g[3 * p + 1] * (yf - m.yc[p]) +
-                    g[3 * p + 2] * (zf - m.zc[p]) + g[3 * q] * (xf - m.xc[q]) +
-                    g[3 * q + 1] * (yf - m.yc[q]) + g[3 * q + 2] * (zf - m.zc[q]);
+  double gradfidr = g[3 * p] * dxp + g[3 * p + 1] * dyp + g[3 * p + 2] * dzp + g[3 * q] * dxq +
+                    g[3 * q + 1] * dyq + g[3 * q + 2] * dzq;
   return 0.5 * (fi[p] + fi[q] + gradfidr);
 }
 
-__global__ void k_ffm_faces(MeshView m, FlowView fl, double *__restrict__ a,
-                            double *__restrict__ flmass) {
-  FCG_GRID_STRIDE(f, m.nin) {
+__global__ void k_ffm_faces(MeshView m, const double *__restrict__ g, FlowView fl,
+                            double *__restrict__ a, double *__restrict__ flmass) {
+  const long long nin = m.nin;
+  FCG_GRID_STRIDE(f, nin) {
     int p = m.owner[f], q = m.neighbour[f];
-    double xf = m.xf[f], yf = m.yf[f], zf = m.zf[f];
     double arx = m.arx[f], ary = m.ary[f], arz = m.arz[f];
     double fxn = m.facint[f];
     double fxp = 1.0 - fxn;
-    double xpn = m.xc[q] - m.xc[p], ypn = m.yc[q] - m.yc[p], zpn = m.zc[q] - m.zc[p];
-    double are = sqrt(arx * arx + ary * ary + arz * arz);
-    double nxx = arx / are, nyy = ary / are, nzz = arz / are;
+    const double xpn = g[FG_XPN * nin + f], ypn = g[FG_YPN * nin + f], zpn = g[FG_ZPN * nin + f];
+    const double nxx = g[FG_NX * nin + f], nyy = g[FG_NY * nin + f], nzz = g[FG_NZ * nin + f];
     double Dpu = fxn * m.vol[q] * fl.apu[q] + fxp * m.vol[p] * fl.apu[p];  // :86-88
     double Dpv = fxn * m.vol[q] * fl.apv[q] + fxp * m.vol[p] * fl.apv[p];
     double Dpw = fxn * m.vol[q] * fl.apw[q] + fxp * m.vol[p] * fl.apw[p];
     double dene = fl.den[p] * fxp + fl.den[q] * fxn;
-    double sfdpnr = 1.0 / (arx * xpn * nxx + ary * ypn * nyy + arz * zpn * nzz);  // :94
-    double smdpn = (arx * arx + ary * ary + arz * arz) * sfdpnr;
+    const double sfdpnr = g[FG_SFDPNR * nin + f];  // :94
+    const double smdpn = g[FG_SMDPN * nin + f];
     double cap = -(dene * Dpu * smdpn);  // :96, can = cap
-    double ui = face_value_central(m, p, q, xf, yf, zf, fl.u, fl.dU);
-    double vi = face_value_central(m, p, q, xf, yf, zf, fl.v, fl.dV);
-    double wi = face_value_central(m, p, q, xf, yf, zf, fl.w, fl.dW);
+    const double dxp = g[FG_DXP * nin + f], dyp = g[FG_DYP * nin + f], dzp = g[FG_DZP * nin + f];
+    const double dxq = g[FG_DXQ * nin + f], dyq = g[FG_DYQ * nin + f], dzq = g[FG_DZQ * nin + f];
+    double ui = face_value_central(p, q, dxp, dyp, dzp, dxq, dyq, dzq, fl.u, fl.dU);
+    double vi = face_value_central(p, q, dxp, dyp, dzp, dxq, dyq, dzq, fl.v, fl.dV);
+    double wi = face_value_central(p, q, dxp, dyp, dzp, dxq, dyq, dzq, fl.w, fl.dW);
     const double *dP = fl.dP;
     double dpxi = Dpu * (fxn * dP[3 * q] + fxp * dP[3 * p]) * xpn * nxx;  // :145-147
     double dpyi = Dpv * (fxn * dP[3 * q + 1] + fxp * dP[3 * p + 1]) * ypn * nyy;
     double dpzi = Dpw * (fxn * dP[3 * q + 2] + fxp * dP[3 * p + 2]) * zpn * nzz;
-    double xpp = xf - (xf - m.xc[p]) * nxx, ypp = yf - (yf - m.yc[p]) * nyy,
-           zpp = zf - (zf - m.zc[p]) * nzz;
-    double xep = xf - (xf - m.xc[q]) * nxx, yep = yf - (yf - m.yc[q]) * nyy,
-           zep = zf - (zf - m.zc[q]) * nzz;
-    xpp = xpp - m.xc[p];
-    ypp = ypp - m.yc[p];
-    zpp = zpp - m.zc[p];
-    xep = xep - m.xc[q];
-    yep = yep - m.yc[q];
-    zep = zep - m.zc[q];
+    const double xpp = g[FG_XPP * nin + f], ypp = g[FG_YPP * nin + f], zpp = g[FG_ZPP * nin + f];
+    const double xep = g[FG_XEP * nin + f], yep = g[FG_YEP * nin + f], zep = g[FG_ZEP * nin + f];
     double dpe = fl.p[q] - fl.p[p];
     // :174-175 as written: only the first owner term carries the minus sign.
     double dpecorr = dP[3 * q] * xep + dP[3 * q + 1] * yep + dP[3 * q + 2] * zep - dP[3 * p] * xpp +
@@ -146,24 +193,25 @@ __global__ void k_ffm_cells(MeshView m, const double *__restrict__ flmass, doubl
 // ---------------------------------------------------------------------------
 // facefluxmass_piso inside the PISO corrector (PISO_multiple_correction.f90:116-148)
 // ---------------------------------------------------------------------------
-__global__ void k_ffp_faces(MeshView m, FlowView fl, double *__restrict__ a,
-                            double *__restrict__ flmass) {
-  FCG_GRID_STRIDE(f, m.nin) {
+__global__ void k_ffp_faces(MeshView m, const double *__restrict__ g, FlowView fl,
+                            double *__restrict__ a, double *__restrict__ flmass) {
+  const long long nin = m.nin;
+  FCG_GRID_STRIDE(f, nin) {
     int p = m.owner[f], q = m.neighbour[f];
-    double xf = m.xf[f], yf = m.yf[f], zf = m.zf[f];
     double arx = m.arx[f], ary = m.ary[f], arz = m.arz[f];
     double fxn = m.facint[f];  // facefluxmass.f90:325-326
     double fxp = 1.0 - fxn;
-    double xpn = m.xc[q] - m.xc[p], ypn = m.yc[q] - m.yc[p], zpn = m.zc[q] - m.zc[p];
-    double dpn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);  // :334
-    double are = sqrt(arx * arx + ary * ary + arz * arz);  // :337
+    const double dpn = g[FG_DPN * nin + f];  // :334
+    const double are = g[FG_ARE * nin + f];  // :337
     double dene = fl.den[p] * fxp + fl.den[q] * fxn;       // :340
     // :343, cap = -dene*(...)*are/dpn; can = cap
     double cap =
         -(dene * (fxp * m.vol[p] * fl.apu[p] + fxn * m.vol[q] * fl.apu[q]) * are / dpn);
-    double ui = face_value_central(m, p, q, xf, yf, zf, fl.u, fl.dU);  // :349-351
-    double vi = face_value_central(m, p, q, xf, yf, zf, fl.v, fl.dV);
-    double wi = face_value_central(m, p, q, xf, yf, zf, fl.w, fl.dW);
+    const double dxp = g[FG_DXP * nin + f], dyp = g[FG_DYP * nin + f], dzp = g[FG_DZP * nin + f];
+    const double dxq = g[FG_DXQ * nin + f], dyq = g[FG_DYQ * nin + f], dzq = g[FG_DZQ * nin + f];
+    double ui = face_value_central(p, q, dxp, dyp, dzp, dxq, dyq, dzq, fl.u, fl.dU);  // :349-351
+    double vi = face_value_central(p, q, dxp, dyp, dzp, dxq, dyq, dzq, fl.v, fl.dV);
+    double wi = face_value_central(p, q, dxp, dyp, dzp, dxq, dyq, dzq, fl.w, fl.dW);
     flmass[f] = dene * (ui * arx + vi * ary + wi * arz);  // :356
     a[m.slot_pn[f]] = cap;                                // PISO :126-131
     a[m.slot_np[f]] = cap;
@@ -173,29 +221,18 @@ __global__ void k_ffp_faces(MeshView m, FlowView fl, double *__restrict__ a,
 // ---------------------------------------------------------------------------
 // fluxmc inside calcp :193-206
 // ---------------------------------------------------------------------------
-__global__ void k_fmc_faces(MeshView m, const double *__restrict__ dP,
+__global__ void k_fmc_faces(MeshView m, const double *__restrict__ g, const double *__restrict__ dP,
                             const double *__restrict__ apu, const double *__restrict__ den,
                             double *__restrict__ flmass, double *__restrict__ fmcor_out) {
-  FCG_GRID_STRIDE(f, m.nin) {
+  const long long nin = m.nin;
+  FCG_GRID_STRIDE(f, nin) {
     int p = m.owner[f], q = m.neighbour[f];
-    double xf = m.xf[f], yf = m.yf[f], zf = m.zf[f];
-    double arx = m.arx[f], ary = m.ary[f], arz = m.arz[f];
     double fxn = m.facint[f];
     double fxp = 1.0 - fxn;
-    double xpn = m.xc[q] - m.xc[p], ypn = m.yc[q] - m.yc[p], zpn = m.zc[q] - m.zc[p];
-    double are = sqrt(arx * arx + ary * ary + arz * arz);
-    double nxx = arx / are, nyy = ary / are, nzz = arz / are;
-    double dppnnr = 1.0 / ((xpn * nxx) + (ypn * nyy) + (zpn * nzz));  // :578
-    double xpp = xf - (xf - m.xc[p]) * nxx, ypp = yf - (yf - m.yc[p]) * nyy,
-           zpp = zf - (zf - m.zc[p]) * nzz;
-    double xep = xf - (xf - m.xc[q]) * nxx, yep = yf - (yf - m.yc[q]) * nyy,
-           zep = zf - (zf - m.zc[q]) * nzz;
-    xpp = xpp - m.xc[p];
-    ypp = ypp - m.yc[p];
-    zpp = zpp - m.zc[p];
-    xep = xep - m.xc[q];
-    yep = yep - m.yc[q];
-    zep = zep - m.zc[q];
+    const double are = g[FG_ARE * nin + f];
+    const double dppnnr = g[FG_DPPNNR * nin + f];  // :578
+    const double xpp = g[FG_XPP * nin + f], ypp = g[FG_YPP * nin + f], zpp = g[FG_ZPP * nin + f];
+    const double xep = g[FG_XEP * nin + f], yep = g[FG_YEP * nin + f], zep = g[FG_ZEP * nin + f];
     double rapr = apu[p] * den[p] * m.vol[p] * fxp + apu[q] * den[q] * m.vol[q] * fxn;  // :599
     double fmcor = rapr * are *
                    ((dP[3 * q] * xep - dP[3 * p] * xpp) + (dP[3 * q + 1] * yep - dP[3 * p + 1] * ypp) +
@@ -222,6 +259,22 @@ __global__ void k_fmc_cells(MeshView m, const double *__restrict__ fmcor, double
 
 // ---------------------------------------------------------------------------
 // C ABI
+// The face factors of the bound mesh (built at the first face loop that needs them).
+int face_geo(fcg_context *c, const double **g) {
+  if (!c->fgeo_ready) {
+    const size_t nin = c->nin > 0 ? (size_t)c->nin : 1;
+    FCG_CUDA_TRY(c, c->fgeo.ensure(sizeof(double) * FG_COUNT * nin));
+    if (c->nin > 0) {
+      k_face_geo<<<grid_for(c->nin, c->num_sms), kTPB, 0, c->stream>>>(c->mv,
+                                                                       c->fgeo.as<double>());
+      FCG_CHECK_LAUNCH(c, "k_face_geo");
+    }
+    c->fgeo_ready = true;
+  }
+  *g = c->fgeo.as<double>();
+  return FCG_OK;
+}
+
 // ---------------------------------------------------------------------------
 extern "C" int fcg_laplacian(fcg_context *c, const double *mu, const double *phi, double *a,
                              double *su) {
@@ -236,8 +289,10 @@ extern "C" int fcg_laplacian(fcg_context *c, const double *mu, const double *phi
   if ((rc = stage_in(c, a, sizeof(double) * c->nnz, 2, false, &da, &ha))) return rc;
   if ((rc = stage_in(c, su, sizeof(double) * c->n, 3, true, &dsu, &hsu))) return rc;
   const MeshView &m = c->mv;
+  const double *g;
+  if ((rc = face_geo(c, &g))) return rc;
   if (m.nin > 0) {
-    k_lap_faces<<<grid_for(m.nin, c->num_sms), kTPB, 0, c->stream>>>(m, (const double *)dmu,
+    k_lap_faces<<<grid_for(m.nin, c->num_sms), kTPB, 0, c->stream>>>(m, g, (const double *)dmu,
                                                                         (double *)da);
     FCG_CHECK_LAUNCH(c, "k_lap_faces");
   }
@@ -275,8 +330,10 @@ extern "C" int fcg_facefluxmass(fcg_context *c, const fcg_flow_fields *f, double
               (const double *)dev[6], (const double *)dev[7], (const double *)dev[8],
               (const double *)dev[9], (const double *)dev[10], (const double *)dev[11]};
   const MeshView &m = c->mv;
+  const double *g;
+  if ((rc = face_geo(c, &g))) return rc;
   if (m.nin > 0) {
-    k_ffm_faces<<<grid_for(m.nin, c->num_sms), kTPB, 0, c->stream>>>(m, fl, (double *)da,
+    k_ffm_faces<<<grid_for(m.nin, c->num_sms), kTPB, 0, c->stream>>>(m, g, fl, (double *)da,
                                                                         (double *)dfm);
     FCG_CHECK_LAUNCH(c, "k_ffm_faces");
   }
@@ -314,8 +371,10 @@ extern "C" int fcg_facefluxmass_piso(fcg_context *c, const fcg_flow_fields *f, d
               (const double *)dev[3], (const double *)dev[4], (const double *)dev[5], nullptr,
               (const double *)dev[6], nullptr, nullptr, (const double *)dev[7]};
   const MeshView &m = c->mv;
+  const double *g;
+  if ((rc = face_geo(c, &g))) return rc;
   if (m.nin > 0) {
-    k_ffp_faces<<<grid_for(m.nin, c->num_sms), kTPB, 0, c->stream>>>(m, fl, (double *)da,
+    k_ffp_faces<<<grid_for(m.nin, c->num_sms), kTPB, 0, c->stream>>>(m, g, fl, (double *)da,
                                                                         (double *)dfm);
     FCG_CHECK_LAUNCH(c, "k_ffp_faces");
   }
@@ -347,9 +406,11 @@ extern "C" int fcg_fluxmc(fcg_context *c, const double *dPdxi, const double *apu
     return rc;
   FCG_CUDA_TRY(c, c->scratch.ensure(sizeof(double) * (c->nin > 0 ? c->nin : 1)));
   const MeshView &m = c->mv;
+  const double *g;
+  if ((rc = face_geo(c, &g))) return rc;
   if (m.nin > 0) {
     k_fmc_faces<<<grid_for(m.nin, c->num_sms), kTPB, 0, c->stream>>>(
-        m, (const double *)dP, (const double *)dapu, (const double *)dden, (double *)dfm,
+        m, g, (const double *)dP, (const double *)dapu, (const double *)dden, (double *)dfm,
         c->scratch.as<double>());
     FCG_CHECK_LAUNCH(c, "k_fmc_faces");
   }

@@ -131,6 +131,10 @@ struct fcg_context {
   // lazily built lsq matrices dmat(9,n)
   fcg::DBuf dmat;
   bool dmat_ready = false;
+  // lazily built mesh-constant factors of the inner faces (assembly.cu: laplacian,
+  // facefluxmass, fluxmc), planar [FG_COUNT][nin]
+  fcg::DBuf fgeo;
+  bool fgeo_ready = false;
 
   // per-call staging of host arrays and kernel scratch
   std::vector<fcg::DBuf> stage;
