@@ -14,6 +14,7 @@
 // bit-identical to the reference's loop on the same inputs.
 #include <algorithm>
 
+#include "face_geo.h"
 #include "fcg_internal.h"
 #include "launch.h"
 
@@ -22,27 +23,8 @@ using namespace fcg;
 namespace {
 
 // ---------------------------------------------------------------------------
-// Mesh-constant factors of the inner faces, computed once per bound mesh by the same
-// rounded operations the face loops use, so that the loops that read them give the same
-// bits as recomputing them (sqrt and divisions dominate those loops on this part's FP64
-// pipe).  Planar: plane q holds factor q of every inner face.
+// The face factors (face_geo.h).
 // ---------------------------------------------------------------------------
-enum FaceGeo {
-  FG_NX, FG_NY, FG_NZ,    // unit normal S/|S|
-  FG_SFDPNR,              // 1/(arx xpn nx + ary ypn ny + arz zpn nz)   (facefluxmass.f90:94)
-  FG_SMDPN,               // |S|^2 sfdpnr                                (:95)
-  FG_DPPNNR,              // 1/(xpn nx + ypn ny + zpn nz)                (facefluxmass.f90:578)
-  FG_XPP, FG_YPP, FG_ZPP, // P' - P: (f - (f - P) n) - P                 (:155-172, :586-595)
-  FG_XEP, FG_YEP, FG_ZEP, // N' - N
-  FG_DXP, FG_DYP, FG_DZP, // face centre - P
-  FG_DXQ, FG_DYQ, FG_DZQ, // face centre - N
-  FG_XPN, FG_YPN, FG_ZPN, // N - P
-  FG_ARE,                 // |S|
-  FG_SMDPN_LAP,           // |S|^2 / (S . (N - P))                        (fvm_laplacian.f90:214)
-  FG_DPN,                 // |N - P|                                     (facefluxmass.f90:334)
-  FG_COUNT
-};
-
 __global__ void k_face_geo(MeshView m, double *__restrict__ g) {
   const long long nin = m.nin;
   FCG_GRID_STRIDE(f, nin) {
@@ -63,15 +45,44 @@ __global__ void k_face_geo(MeshView m, double *__restrict__ g) {
     xep = xep - m.xc[q];
     yep = yep - m.yc[q];
     zep = zep - m.zc[q];
+    // sngrad's arx / vole with vole = xpn arx + ypn ary + zpn arz (gradients.f90:644, 666)
+    const double vole = xpn * arx + ypn * ary + zpn * arz;
+    // presFaceDivInner's interpolated centre xi = xc(P) fxp + xc(N) fxn
+    // (fieldManipulation.f90:429-431)
+    const double fxn = m.facint[f], fxp = 1.0 - fxn;
+    const double xi = m.xc[p] * fxp + m.xc[q] * fxn, yi = m.yc[p] * fxp + m.yc[q] * fxn,
+                 zi = m.zc[p] * fxp + m.zc[q] * fxn;
     const double v[FG_COUNT] = {
         nxx, nyy, nzz, sfdpnr, (arx * arx + ary * ary + arz * arz) * sfdpnr,
         1.0 / ((xpn * nxx) + (ypn * nyy) + (zpn * nzz)), xpp, ypp, zpp, xep, yep, zep,
         xf - m.xc[p], yf - m.yc[p], zf - m.zc[p], xf - m.xc[q], yf - m.yc[q], zf - m.zc[q],
         xpn, ypn, zpn, are,
         (arx * arx + ary * ary + arz * arz) / (arx * xpn + ary * ypn + arz * zpn),
-        sqrt(xpn * xpn + ypn * ypn + zpn * zpn)};
+        sqrt(xpn * xpn + ypn * ypn + zpn * zpn), arx / vole, ary / vole, arz / vole,
+        xf - xi, yf - yi, zf - zi};
 #pragma unroll
     for (int k = 0; k < FG_COUNT; ++k) g[k * nin + f] = v[k];
+  }
+}
+
+// Boundary-face factors (face_geo.h), one thread per cell over its boundary entries.
+__global__ void k_bnd_geo(MeshView m, long long ncb, double *__restrict__ b) {
+  FCG_GRID_STRIDE(c, m.n) {
+    for (int e = m.cb_ptr[c]; e < m.cb_ptr[c + 1]; ++e) {
+      const int f = m.cb_face[e];
+      const double arx = m.arx[f], ary = m.ary[f], arz = m.arz[f];
+      const double are = sqrt(arx * arx + ary * ary + arz * arz);
+      const double nxf = arx / are, nyf = ary / are, nzf = arz / are;
+      const double dn = (m.xf[f] - m.xc[c]) * nxf + (m.yf[f] - m.yc[c]) * nyf +
+                        (m.zf[f] - m.zc[c]) * nzf;
+      const double dx = m.xc[c] - m.xf[f], dy = m.yc[c] - m.yf[f], dz = m.zc[c] - m.zf[f];
+      b[BG_ARE * ncb + e] = are;
+      b[BG_DPB * ncb + e] = sqrt(dx * dx + dy * dy + dz * dz);
+      b[BG_NX * ncb + e] = nxf;
+      b[BG_NY * ncb + e] = nyf;
+      b[BG_NZ * ncb + e] = nzf;
+      b[BG_SRD * ncb + e] = are / dn;
+    }
   }
 }
 
@@ -260,7 +271,7 @@ __global__ void k_fmc_cells(MeshView m, const double *__restrict__ fmcor, double
 // ---------------------------------------------------------------------------
 // C ABI
 // The face factors of the bound mesh (built at the first face loop that needs them).
-int face_geo(fcg_context *c, const double **g) {
+int fcg::face_geo(fcg_context *c, const double **g) {
   if (!c->fgeo_ready) {
     const size_t nin = c->nin > 0 ? (size_t)c->nin : 1;
     FCG_CUDA_TRY(c, c->fgeo.ensure(sizeof(double) * FG_COUNT * nin));
@@ -272,6 +283,22 @@ int face_geo(fcg_context *c, const double **g) {
     c->fgeo_ready = true;
   }
   *g = c->fgeo.as<double>();
+  return FCG_OK;
+}
+
+int fcg::bnd_geo(fcg_context *c, const double **b) {
+  if (!c->bgeo_ready) {
+    long long ncb = 0;
+    for (int t = 0; t < B_NTYPES; ++t) ncb += c->cnt[t];
+    FCG_CUDA_TRY(c, c->bgeo.ensure(sizeof(double) * BG_COUNT * (ncb > 0 ? ncb : 1)));
+    if (ncb > 0) {
+      k_bnd_geo<<<grid_for(c->n, c->num_sms), kTPB, 0, c->stream>>>(c->mv, ncb,
+                                                                   c->bgeo.as<double>());
+      FCG_CHECK_LAUNCH(c, "k_bnd_geo");
+    }
+    c->bgeo_ready = true;
+  }
+  *b = c->bgeo.as<double>();
   return FCG_OK;
 }
 

@@ -12,6 +12,7 @@ fcg_context::~fcg_context() {
   for (auto &b : stage) b.release();
   dmat.release();
   fgeo.release();
+  bgeo.release();
   scratch.release();
   fcg::destroy_krylov(ks);
   fcg::destroy_multi(ms);
@@ -216,6 +217,7 @@ extern "C" int fcg_bind_mesh(fcg_context *c, const fcg_mesh_desc *m) {
   c->bound = false;
   c->dmat_ready = false;
   c->fgeo_ready = false;
+  c->bgeo_ready = false;
 
   const int n = m->numCells, nf = m->numFaces, nin = m->numInnerFaces, nb = nf - nin;
   int cnt[B_NTYPES] = {m->ninl, m->nout, m->nsym, m->nwal, m->npru};

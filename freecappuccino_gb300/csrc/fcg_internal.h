@@ -135,6 +135,9 @@ struct fcg_context {
   // facefluxmass, fluxmc), planar [FG_COUNT][nin]
   fcg::DBuf fgeo;
   bool fgeo_ready = false;
+  // and of the boundary faces (calcuvw's boundary loops), planar [BG_COUNT][ncb]
+  fcg::DBuf bgeo;
+  bool bgeo_ready = false;
 
   // per-call staging of host arrays and kernel scratch
   std::vector<fcg::DBuf> stage;

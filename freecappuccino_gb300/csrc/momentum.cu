@@ -11,6 +11,7 @@
 // Compiled with --fmad=false: bit-identical to the reference's loops on the same inputs.
 //
 // MIN and MAX keep the first argument on ties (only the sign of a zero can differ).
+#include "face_geo.h"
 #include "fcg_internal.h"
 #include "launch.h"
 
@@ -26,149 +27,157 @@ struct UvwView {
   const double *dU, *dV, *dW, *dP, *flmass, *fmi, *fmo;
 };
 
+// The face's offsets that face_value reads, with the upwind cell first: the face centre
+// minus the upwind cell's centre (du*) and minus the downwind cell's centre (dd*), from
+// the cached face factors.
+struct Offs {
+  double dux, duy, duz, ddx, ddy, ddz;
+};
+
 // face_value (interpolation.f90:20-60) with the first cell upwind: f is the first cell,
 // s the second, lam the weight of the second (the caller passes fxp or fxn as the
-// reference does).
-__device__ double face_value(const MeshView &m, int scheme, int limiter, int f, int s,
-                             double xf, double yf, double zf, double lam,
-                             const double *__restrict__ fi, const double *__restrict__ g) {
-  switch (scheme) {
-    case FCG_CONV_CDS: {  // :65-93
-      const double fxn = lam, fxp = 1.0 - lam;
-      return fi[f] * fxp + fi[s] * fxn;
+// reference does).  One instantiation per scheme: the scheme is fixed for a call.
+template <int S>
+__device__ __forceinline__ double face_value(const MeshView &m, int limiter, int f, int s,
+                                             double lam, long long fi_face, const Offs &o,
+                                             const double *__restrict__ fi,
+                                             const double *__restrict__ g) {
+  if constexpr (S == FCG_CONV_CDS) {  // :65-93
+    const double fxn = lam, fxp = 1.0 - lam;
+    return fi[f] * fxp + fi[s] * fxn;
+  } else if constexpr (S == FCG_CONV_CDS_CORRECTED) {  // :99-139
+    const double xf = m.xf[fi_face], yf = m.yf[fi_face], zf = m.zf[fi_face];
+    const double fxn = lam, fxp = 1.0 - lam;
+    const double xi = m.xc[f] * fxp + m.xc[s] * fxn, yi = m.yc[f] * fxp + m.yc[s] * fxn,
+                 zi = m.zc[f] * fxp + m.zc[s] * fxn;
+    const double dx = g[3 * f] * fxp + g[3 * s] * fxn, dy = g[3 * f + 1] * fxp + g[3 * s + 1] * fxn,
+                 dz = g[3 * f + 2] * fxp + g[3 * s + 2] * fxn;
+    return fi[f] * fxp + fi[s] * fxn + (dx * (xf - xi) + dy * (yf - yi) + dz * (zf - zi));
+  } else if constexpr (S == FCG_CONV_CENTRAL) {  // :145-199
+    const double r = g[3 * f] * o.dux + g[3 * f + 1] * o.duy + g[3 * f + 2] * o.duz +
+                     g[3 * s] * o.ddx + g[3 * s + 1] * o.ddy + g[3 * s + 2] * o.ddz;
+    return 0.5 * (fi[f] + fi[s] + r);
+  } else if constexpr (S == FCG_CONV_SECOND_UPWIND) {  // :204-249
+    const double r = g[3 * f] * o.dux + g[3 * f + 1] * o.duy + g[3 * f + 2] * o.duz;
+    return fi[f] + r;
+  } else if constexpr (S == FCG_CONV_FLUX_LIMITER) {  // :325-393
+    const double fxp = 1.0 - lam;
+    const double xpn = m.xc[s] - m.xc[f], ypn = m.yc[s] - m.yc[f], zpn = m.zc[s] - m.zc[f];
+    const double r = (2.0 * g[3 * f] * xpn + 2.0 * g[3 * f + 1] * ypn + 2.0 * g[3 * f + 2] * zpn) /
+                         (fi[s] - fi[f]) -
+                     1.0;
+    double psi;
+    switch (limiter) {
+      case FCG_LIM_SMART:
+        psi = rmax(0.0, rmin(rmin(2.0 * r, 0.75 * r + 0.25), 4.0));
+        break;
+      case FCG_LIM_AVL:
+        psi = rmax(0.0, rmin(rmin(1.5 * r, 0.75 * r + 0.25), 2.5));
+        break;
+      case FCG_LIM_MUSCL:
+        psi = rmax(0.0, rmin(rmin(2.0 * r, 0.5 * r + 0.5), 2.0));
+        break;
+      case FCG_LIM_UMIST:
+        psi = rmax(0.0, rmin(rmin(rmin(2.0 * r, 0.75 * r + 0.25), 0.25 * r + 0.75), 2.0));
+        break;
+      case FCG_LIM_KOREN:
+        psi = rmax(0.0, rmin(rmin(2.0 * r, 2.0 / 3.0 * r + 1.0 / 3.0), 2.0));
+        break;
+      case FCG_LIM_CHARM:
+        psi = (r + fabs(r)) * (3.0 * r + 1.0) / (2.0 * ((r + 1.0) * (r + 1.0)));
+        break;
+      case FCG_LIM_OSPRE:
+        psi = 1.5 * r * (r + 1.0) / (r * r + r + 1.0);
+        break;
+      default:
+        psi = 1.0;
     }
-    case FCG_CONV_CDS_CORRECTED: {  // :99-139
-      const double fxn = lam, fxp = 1.0 - lam;
-      const double xi = m.xc[f] * fxp + m.xc[s] * fxn, yi = m.yc[f] * fxp + m.yc[s] * fxn,
-                   zi = m.zc[f] * fxp + m.zc[s] * fxn;
-      const double dx = g[3 * f] * fxp + g[3 * s] * fxn, dy = g[3 * f + 1] * fxp + g[3 * s + 1] * fxn,
-                   dz = g[3 * f + 2] * fxp + g[3 * s + 2] * fxn;
-      return fi[f] * fxp + fi[s] * fxn + (dx * (xf - xi) + dy * (yf - yi) + dz * (zf - zi));
-    }
-    case FCG_CONV_CENTRAL: {  // :145-199
-      const double r = g[3 * f] * (xf - m.xc[f]) + g[3 * f + 1] * (yf - m.yc[f]) +
-                       g[3 * f + 2] * (zf - m.zc[f]) + g[3 * s] * (xf - m.xc[s]) +
-                       g[3 * s + 1] * (yf - m.yc[s]) + g[3 * s + 2] * (zf - m.zc[s]);
-      return 0.5 * (fi[f] + fi[s] + r);
-    }
-    case FCG_CONV_SECOND_UPWIND: {  // :204-249
-      const double r = g[3 * f] * (xf - m.xc[f]) + g[3 * f + 1] * (yf - m.yc[f]) +
-                       g[3 * f + 2] * (zf - m.zc[f]);
-      return fi[f] + r;
-    }
-    case FCG_CONV_FLUX_LIMITER: {  // :325-393
-      const double fxp = 1.0 - lam;
-      const double xpn = m.xc[s] - m.xc[f], ypn = m.yc[s] - m.yc[f], zpn = m.zc[s] - m.zc[f];
-      const double r = (2.0 * g[3 * f] * xpn + 2.0 * g[3 * f + 1] * ypn + 2.0 * g[3 * f + 2] * zpn) /
-                           (fi[s] - fi[f]) -
-                       1.0;
-      double psi;
-      switch (limiter) {
-        case FCG_LIM_SMART:
-          psi = rmax(0.0, rmin(rmin(2.0 * r, 0.75 * r + 0.25), 4.0));
-          break;
-        case FCG_LIM_AVL:
-          psi = rmax(0.0, rmin(rmin(1.5 * r, 0.75 * r + 0.25), 2.5));
-          break;
-        case FCG_LIM_MUSCL:
-          psi = rmax(0.0, rmin(rmin(2.0 * r, 0.5 * r + 0.5), 2.0));
-          break;
-        case FCG_LIM_UMIST:
-          psi = rmax(0.0, rmin(rmin(rmin(2.0 * r, 0.75 * r + 0.25), 0.25 * r + 0.75), 2.0));
-          break;
-        case FCG_LIM_KOREN:
-          psi = rmax(0.0, rmin(rmin(2.0 * r, 2.0 / 3.0 * r + 1.0 / 3.0), 2.0));
-          break;
-        case FCG_LIM_CHARM:
-          psi = (r + fabs(r)) * (3.0 * r + 1.0) / (2.0 * ((r + 1.0) * (r + 1.0)));
-          break;
-        case FCG_LIM_OSPRE:
-          psi = 1.5 * r * (r + 1.0) / (r * r + r + 1.0);
-          break;
-        default:
-          psi = 1.0;
-      }
-      return fi[f] + fxp * psi * (fi[s] - fi[f]);
-    }
-    default: {  // FCG_CONV_MUSCL, :254-320
-      const double theta = 0.125;
-      const double g2 = g[3 * f] * (xf - m.xc[f]) + g[3 * f + 1] * (yf - m.yc[f]) +
-                        g[3 * f + 2] * (zf - m.zc[f]);
-      const double gc = g[3 * f] * (xf - m.xc[f]) + g[3 * f + 1] * (yf - m.yc[f]) +
-                        g[3 * f + 2] * (zf - m.zc[f]) + g[3 * s] * (xf - m.xc[s]) +
-                        g[3 * s + 1] * (yf - m.yc[s]) + g[3 * s + 2] * (zf - m.zc[s]);
-      const double fv2 = fi[f] + g2;
-      const double fvc = 0.5 * (fi[f] + fi[s] + gc);
-      return theta * fvc + (1.0 - theta) * fv2;
-    }
+    return fi[f] + fxp * psi * (fi[s] - fi[f]);
+  } else {  // FCG_CONV_MUSCL, :254-320
+    const double theta = 0.125;
+    // the reference's central correction repeats the upwind one's three products first,
+    // so it continues from the same partial sum
+    const double g2 = g[3 * f] * o.dux + g[3 * f + 1] * o.duy + g[3 * f + 2] * o.duz;
+    const double gc = g2 + g[3 * s] * o.ddx + g[3 * s + 1] * o.ddy + g[3 * s + 2] * o.ddz;
+    const double fv2 = fi[f] + g2;
+    const double fvc = 0.5 * (fi[f] + fi[s] + gc);
+    return theta * fvc + (1.0 - theta) * fv2;
   }
 }
 
 // sngrad with nrelax = 0 and the skewness approach (gradients.f90:597-668): the face
-// gradient interpolated (dxi..) and corrected (dxii..).
+// gradient interpolated (dxi..) and corrected (dxii..).  costn = 1, so d1 = 1 and
+// d2 = (xpn, ypn, zpn) exactly; rv = (arx, ary, arz) / vole comes from the cached factors.
 struct SnGrad {
   double xi, yi, zi, xii, yii, zii;
 };
 
-__device__ __forceinline__ SnGrad sngrad(int p, int q, double arx, double ary, double arz,
+__device__ __forceinline__ SnGrad sngrad(int p, int q, double rvx, double rvy, double rvz,
                                          double fxp, double fxn, double xpn, double ypn,
-                                         double zpn, double vole,
-                                         const double *__restrict__ fi,
+                                         double zpn, const double *__restrict__ fi,
                                          const double *__restrict__ g) {
   SnGrad s;
   s.xi = g[3 * p] * fxp + g[3 * q] * fxn;
   s.yi = g[3 * p + 1] * fxp + g[3 * q + 1] * fxn;
   s.zi = g[3 * p + 2] * fxp + g[3 * q + 2] * fxn;
-  const double costn = 1.0;
-  const double d2x = xpn * costn, d2y = ypn * costn, d2z = zpn * costn;
-  s.xii = s.xi * costn + arx / vole * (fi[q] - fi[p] - s.xi * d2x - s.yi * d2y - s.zi * d2z);
-  s.yii = s.yi * costn + ary / vole * (fi[q] - fi[p] - s.xi * d2x - s.yi * d2y - s.zi * d2z);
-  s.zii = s.zi * costn + arz / vole * (fi[q] - fi[p] - s.xi * d2x - s.yi * d2y - s.zi * d2z);
+  const double r = fi[q] - fi[p] - s.xi * xpn - s.yi * ypn - s.zi * zpn;
+  s.xii = s.xi + rvx * r;
+  s.yii = s.yi + rvy * r;
+  s.zii = s.zi + rvz * r;
   return s;
 }
 
-__global__ void k_uvw_faces(MeshView m, fcg_uvw_params prm, UvwView F, double *__restrict__ a,
-                            double *__restrict__ fsrc, double *__restrict__ fdiv) {
+template <int S>
+__global__ void __launch_bounds__(kTPB)
+    k_uvw_faces(MeshView m, fcg_uvw_params prm, UvwView F, const double *__restrict__ geo,
+                double *__restrict__ a, double *__restrict__ fsrc, double *__restrict__ fdiv) {
   const long long nin = m.nin;
   FCG_GRID_STRIDE(f, nin) {
     const int p = m.owner[f], q = m.neighbour[f];
-    const double xf = m.xf[f], yf = m.yf[f], zf = m.zf[f];
     const double arx = m.arx[f], ary = m.ary[f], arz = m.arz[f];
     const double lambda = m.facint[f];
     const double flomass = F.flmass[f];
     // facefluxuvw (faceflux_velocity.f90:78-182)
     const double fxn = lambda, fxp = 1.0 - lambda;
-    const double xpn = m.xc[q] - m.xc[p], ypn = m.yc[q] - m.yc[p], zpn = m.zc[q] - m.zc[p];
-    const double dpn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
-    const double are = sqrt(arx * arx + ary * ary + arz * arz);
+    const double xpn = geo[FG_XPN * nin + f], ypn = geo[FG_YPN * nin + f],
+                 zpn = geo[FG_ZPN * nin + f];
+    const double dpn = geo[FG_DPN * nin + f];
+    const double are = geo[FG_ARE * nin + f];
     const double game = F.vis[p] * fxp + F.vis[q] * fxn;
     const double de = game * are / dpn;
     double can = -de + rmin(flomass, 0.0);
     double cap = -de - rmax(flomass, 0.0);
-    const double vole = xpn * arx + ypn * ary + zpn * arz;
-    const SnGrad du = sngrad(p, q, arx, ary, arz, fxp, fxn, xpn, ypn, zpn, vole, F.u, F.dU);
-    const SnGrad dv = sngrad(p, q, arx, ary, arz, fxp, fxn, xpn, ypn, zpn, vole, F.v, F.dV);
-    const SnGrad dw = sngrad(p, q, arx, ary, arz, fxp, fxn, xpn, ypn, zpn, vole, F.w, F.dW);
+    const double rvx = geo[FG_RVX * nin + f], rvy = geo[FG_RVY * nin + f],
+                 rvz = geo[FG_RVZ * nin + f];
+    const SnGrad du = sngrad(p, q, rvx, rvy, rvz, fxp, fxn, xpn, ypn, zpn, F.u, F.dU);
+    const SnGrad dv = sngrad(p, q, rvx, rvy, rvz, fxp, fxn, xpn, ypn, zpn, F.v, F.dV);
+    const SnGrad dw = sngrad(p, q, rvx, rvy, rvz, fxp, fxn, xpn, ypn, zpn, F.w, F.dW);
     const double fdue = game * ((du.xii + du.xii) * arx + (du.yii + dv.xii) * ary + (du.zii + dw.xii) * arz);
     const double fdve = game * ((du.yii + dv.xii) * arx + (dv.yii + dv.yii) * ary + (dv.zii + dw.yii) * arz);
     const double fdwe = game * ((du.zii + dw.xii) * arx + (dw.yii + dv.zii) * ary + (dw.zii + dw.zii) * arz);
-    const double fdui = game * are / dpn * (du.xi * xpn + du.yi * ypn + du.zi * zpn);
-    const double fdvi = game * are / dpn * (dv.xi * xpn + dv.yi * ypn + dv.zi * zpn);
-    const double fdwi = game * are / dpn * (dw.xi * xpn + dw.yi * ypn + dw.zi * zpn);
+    // game * are / dpn * (...) evaluates its first factor as de does
+    const double fdui = de * (du.xi * xpn + du.yi * ypn + du.zi * zpn);
+    const double fdvi = de * (dv.xi * xpn + dv.yi * ypn + dv.zi * zpn);
+    const double fdwi = de * (dw.xi * xpn + dw.yi * ypn + dw.zi * zpn);
     const double fpos = rmax(flomass, 0.0), fneg = rmin(flomass, 0.0);
     const double fuuds = fpos * F.u[p] + fneg * F.u[q];
     const double fvuds = fpos * F.v[p] + fneg * F.v[q];
     const double fwuds = fpos * F.w[p] + fneg * F.w[q];
-    double ue, ve, we;
-    if (flomass >= 0.0) {
-      ue = face_value(m, prm.scheme, prm.limiter, p, q, xf, yf, zf, fxp, F.u, F.dU);
-      ve = face_value(m, prm.scheme, prm.limiter, p, q, xf, yf, zf, fxp, F.v, F.dV);
-      we = face_value(m, prm.scheme, prm.limiter, p, q, xf, yf, zf, fxp, F.w, F.dW);
-    } else {
-      ue = face_value(m, prm.scheme, prm.limiter, q, p, xf, yf, zf, fxn, F.u, F.dU);
-      ve = face_value(m, prm.scheme, prm.limiter, q, p, xf, yf, zf, fxn, F.v, F.dV);
-      we = face_value(m, prm.scheme, prm.limiter, q, p, xf, yf, zf, fxn, F.w, F.dW);
+    // face_value from the upwind side (:129-150): one path for both signs of the flux
+    const bool fwd = flomass >= 0.0;
+    const int uc = fwd ? p : q, dc = fwd ? q : p;
+    const double lam = fwd ? fxp : fxn;
+    Offs o{};
+    if constexpr (S == FCG_CONV_CENTRAL || S == FCG_CONV_SECOND_UPWIND || S == FCG_CONV_MUSCL) {
+      const double dxp = geo[FG_DXP * nin + f], dyp = geo[FG_DYP * nin + f],
+                   dzp = geo[FG_DZP * nin + f];
+      const double dxq = geo[FG_DXQ * nin + f], dyq = geo[FG_DYQ * nin + f],
+                   dzq = geo[FG_DZQ * nin + f];
+      o = fwd ? Offs{dxp, dyp, dzp, dxq, dyq, dzq} : Offs{dxq, dyq, dzq, dxp, dyp, dzp};
     }
+    const double ue = face_value<S>(m, prm.limiter, uc, dc, lam, f, o, F.u, F.dU);
+    const double ve = face_value<S>(m, prm.limiter, uc, dc, lam, f, o, F.v, F.dV);
+    const double we = face_value<S>(m, prm.limiter, uc, dc, lam, f, o, F.w, F.dW);
     const double gam = prm.gds;
     fsrc[3 * f] = -gam * (flomass * ue - fuuds) + fdue - fdui;
     fsrc[3 * f + 1] = -gam * (flomass * ve - fvuds) + fdve - fdvi;
@@ -182,13 +191,11 @@ __global__ void k_uvw_faces(MeshView m, fcg_uvw_params prm, UvwView F, double *_
     // presFaceDivInner (fieldManipulation.f90:426-442).  The reference indexes its
     // (3,numCells) gradient argument as df(ijp,k): element ijp + 3(k-1) of the flat array.
     const double *dP = F.dP;
-    const double xi = m.xc[p] * fxp + m.xc[q] * fxn, yi = m.yc[p] * fxp + m.yc[q] * fxn,
-                 zi = m.zc[p] * fxp + m.zc[q] * fxn;
     const double dfxi = dP[p] * fxp + dP[q] * fxn;
     const double dfyi = dP[p + 3] * fxp + dP[q + 3] * fxn;
     const double dfzi = dP[p + 6] * fxp + dP[q + 6] * fxn;
-    const double fie =
-        F.p[p] * fxp + F.p[q] * fxn + dfxi * (xf - xi) + dfyi * (yf - yi) + dfzi * (zf - zi);
+    const double fie = F.p[p] * fxp + F.p[q] * fxn + dfxi * geo[FG_DXI * nin + f] +
+                       dfyi * geo[FG_DYI * nin + f] + dfzi * geo[FG_DZI * nin + f];
     fdiv[3 * f] = fie * arx;
     fdiv[3 * f + 1] = fie * ary;
     fdiv[3 * f + 2] = fie * arz;
@@ -205,7 +212,8 @@ __device__ __forceinline__ double row_sum(const MeshView &m, const double *__res
 }
 
 __global__ void k_uvw_cells(MeshView m, fcg_uvw_params prm, UvwView F, int bst_inl,
-                            int bst_out, int bst_sym, int bst_wal, double *__restrict__ a,
+                            int bst_out, const double *__restrict__ bg, long long ncb,
+                            double *__restrict__ a,
                             const double *__restrict__ fsrc, const double *__restrict__ fdiv,
                             double *__restrict__ diag_vw, double *__restrict__ rhs,
                             double *__restrict__ ap) {
@@ -286,14 +294,12 @@ __global__ void k_uvw_cells(MeshView m, fcg_uvw_params prm, UvwView F, int bst_i
     for (int e = b0; e < b1; ++e) {
       const int t = m.cb_type[e];
       if (t == B_PRESSOUT) continue;
-      const int f = m.cb_face[e], b = m.cb_slot[e];
-      const double arx = m.arx[f], ary = m.ary[f], arz = m.arz[f];
+      const int b = m.cb_slot[e];
+      const double are = bg[BG_ARE * ncb + e];
       if (t == B_INLET || t == B_OUTLET) {
         // facefluxuvw_boundary (faceflux_velocity.f90:403-468): only cb is used
         const double flomass = t == B_INLET ? F.fmi[b - bst_inl] : F.fmo[b - bst_out];
-        const double xpn = m.xf[f] - m.xc[c], ypn = m.yf[f] - m.yc[c], zpn = m.zf[f] - m.zc[c];
-        const double dpn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
-        const double are = sqrt(arx * arx + ary * ary + arz * arz);
+        const double dpn = bg[BG_DPB * ncb + e];
         const double de = F.vis[b] * are / dpn;
         const double cb = -de + rmin(flomass, 0.0);
         sp0 = sp0 - cb;
@@ -303,14 +309,11 @@ __global__ void k_uvw_cells(MeshView m, fcg_uvw_params prm, UvwView F, int bst_i
         s1 = s1 - cb * F.v[b];
         s2 = s2 - cb * F.w[b];
       } else {
-        const double are = sqrt(arx * arx + ary * ary + arz * arz);
-        const double nxf = arx / are, nyf = ary / are, nzf = arz / are;
+        const double nxf = bg[BG_NX * ncb + e], nyf = bg[BG_NY * ncb + e],
+                     nzf = bg[BG_NZ * ncb + e];
         // dns / dnw and srds / srdw (init.f90:1002-1027)
-        const double dn = (m.xf[f] - m.xc[c]) * nxf + (m.yf[f] - m.yc[c]) * nyf +
-                          (m.zf[f] - m.zc[c]) * nzf;
-        const double srd = are / dn;
-        const double dx = m.xc[c] - m.xf[f], dy = m.yc[c] - m.yf[f], dz = m.zc[c] - m.zf[f];
-        const double dpb = sqrt(dx * dx + dy * dy + dz * dz);
+        const double srd = bg[BG_SRD * ncb + e];
+        const double dpb = bg[BG_DPB * ncb + e];
         const double upb = F.u[c] - F.u[b], vpb = F.v[c] - F.v[b], wpb = F.w[c] - F.w[b];
         if (t == B_SYMMETRY) {  // :268-306
           const double vsi = F.vis[b];
@@ -343,6 +346,7 @@ __global__ void k_uvw_cells(MeshView m, fcg_uvw_params prm, UvwView F, int bst_i
     if (prm.cn) d_in = 0.5 * d_in;
     const double apotime = prm.cn ? F.den[c] * vol / prm.timestep : 0.0;
     // u (:392-438)
+    const double offu = row_sum(m, a, c, d_in) - d_in;
     if (prm.cn) {
       for (int e = e0; e < e1; ++e) {
         const int ent = m.cf_ent[e];
@@ -350,10 +354,10 @@ __global__ void k_uvw_cells(MeshView m, fcg_uvw_params prm, UvwView F, int bst_i
         const int o = ent > 0 ? m.neighbour[f] : m.owner[f];
         s0 = s0 - a[m.cf_slot[e]] * F.uo[o];
       }
-      s0 = s0 + (apotime + (row_sum(m, a, c, d_in) - d_in)) * F.uo[c];
+      s0 = s0 + (apotime + offu) * F.uo[c];
       sp0 = sp0 + apotime;
     }
-    double du = (sp0 - (row_sum(m, a, c, d_in) - d_in)) * prm.urfr[0];
+    double du = (sp0 - offu) * prm.urfr[0];
     rhs[c] = s0 + prm.urfm[0] * du * F.u[c];
     ap[c] = 1.0 / (du + small);
     // v (:447-495): its CN term sees the u diagonal; its diagonal assembly a zero one
@@ -367,7 +371,9 @@ __global__ void k_uvw_cells(MeshView m, fcg_uvw_params prm, UvwView F, int bst_i
       s1 = s1 + (apotime + (row_sum(m, a, c, du) - du)) * F.vo[c];
       sp1 = sp1 + apotime;
     }
-    const double dv = (sp1 - (row_sum(m, a, c, 0.0) - 0.0)) * prm.urfr[1];
+    // the v and w diagonals see a zero in place of the diagonal (x - 0.0 is x exactly)
+    const double rs0 = row_sum(m, a, c, 0.0);
+    const double dv = (sp1 - rs0) * prm.urfr[1];
     rhs[m.n + c] = s1 + prm.urfm[1] * dv * F.v[c];
     ap[m.n + c] = 1.0 / (dv + small);
     // w (:504-553): its CN term sees the v diagonal
@@ -381,7 +387,7 @@ __global__ void k_uvw_cells(MeshView m, fcg_uvw_params prm, UvwView F, int bst_i
       s2 = s2 + (apotime + (row_sum(m, a, c, dv) - dv)) * F.wo[c];
       sp2 = sp2 + apotime;
     }
-    const double dw = (sp2 - (row_sum(m, a, c, 0.0) - 0.0)) * prm.urfr[2];
+    const double dw = (sp2 - rs0) * prm.urfr[2];
     rhs[2 * m.n + c] = s2 + prm.urfm[2] * dw * F.w[c];
     ap[2 * m.n + c] = 1.0 / (dw + small);
     a[m.diag[c]] = du;
@@ -453,13 +459,28 @@ extern "C" int fcg_calcuvw(fcg_context *c, const fcg_uvw_params *prm, const fcg_
   double *fsrc = c->scratch.as<double>(), *fdiv = fsrc + 3 * (c->nin > 0 ? c->nin : 1);
   const MeshView &m = c->mv;
   if (m.nin > 0) {
-    k_uvw_faces<<<grid_for(m.nin, c->num_sms), kTPB, 0, c->stream>>>(m, *prm, V, (double *)da,
-                                                                        fsrc, fdiv);
+    const double *geo;
+    if ((rc = face_geo(c, &geo))) return rc;
+    auto faces = k_uvw_faces<FCG_CONV_MUSCL>;
+    switch (prm->scheme) {
+      case FCG_CONV_CDS: faces = k_uvw_faces<FCG_CONV_CDS>; break;
+      case FCG_CONV_CDS_CORRECTED: faces = k_uvw_faces<FCG_CONV_CDS_CORRECTED>; break;
+      case FCG_CONV_CENTRAL: faces = k_uvw_faces<FCG_CONV_CENTRAL>; break;
+      case FCG_CONV_SECOND_UPWIND: faces = k_uvw_faces<FCG_CONV_SECOND_UPWIND>; break;
+      case FCG_CONV_FLUX_LIMITER: faces = k_uvw_faces<FCG_CONV_FLUX_LIMITER>; break;
+      default: break;
+    }
+    faces<<<grid_for(m.nin, c->num_sms), kTPB, 0, c->stream>>>(m, *prm, V, geo, (double *)da,
+                                                                 fsrc, fdiv);
     FCG_CHECK_LAUNCH(c, "k_uvw_faces");
   }
+  const double *bg;
+  if ((rc = bnd_geo(c, &bg))) return rc;
+  long long ncb = 0;
+  for (int t = 0; t < B_NTYPES; ++t) ncb += c->cnt[t];
   k_uvw_cells<<<grid_for(m.n, c->num_sms), kTPB, 0, c->stream>>>(
-      m, *prm, V, c->bst[B_INLET], c->bst[B_OUTLET], c->bst[B_SYMMETRY], c->bst[B_WALL],
-      (double *)da, fsrc, fdiv, (double *)ddv, (double *)drhs, (double *)dap);
+      m, *prm, V, c->bst[B_INLET], c->bst[B_OUTLET], bg, ncb, (double *)da, fsrc, fdiv,
+      (double *)ddv, (double *)drhs, (double *)dap);
   FCG_CHECK_LAUNCH(c, "k_uvw_cells");
   if ((rc = stage_out(c, a, da, sizeof(double) * c->nnz, ha)) ||
       (rc = stage_out(c, diag_vw, ddv, 2 * n1, hdv)) ||
