@@ -102,6 +102,7 @@ struct KrylovState {
   int sf_spin = 1 << 20;     // polls before a dependency wait gives up
   int sf_absent_row = -1;    // test hook: this row never publishes its flag
   bool wave_on = true;       // wavefront-tiled sweeps on lexicographic hex blocks
+  bool wave_wide = true;     // tiles of 16 x 8 columns rather than 8 x 8
 };
 
 void destroy_krylov(KrylovState *k) {
@@ -682,6 +683,14 @@ __global__ void k_wave_coef(int nx, int ny, int nz, const int *__restrict__ ioff
 // are loaded kRing steps ahead into a register ring whose slot is the step modulo kRing,
 // so every slot index is a compile-time constant of the unrolled step loop.  An upstream
 // value that was still the sentinel when loaded is then waited for.
+//
+// The step is branch-free: a neighbour outside the block has coefficient +0 (k_wave_coef)
+// and value +0, and acc - (+0)(+0) is acc exactly, so every cell runs the same three
+// terms in CSR order and gives the bits of the level kernels.  On this part a dependent
+// FP64 operation takes about 64 cycles, so the step's length is its chain of FP64
+// operations: the term of the cell's own column (the previous step of the same thread)
+// is formed before the barrier, which leaves the two products and subtractions of the
+// in-tile neighbours and the scaling after it.
 template <int TX, int TY, bool BWD>
 __global__ void __launch_bounds__(TX * TY)
     k_wave_sweep(int nx, int ny, int nz, const double *__restrict__ coef,
@@ -695,6 +704,8 @@ __global__ void __launch_bounds__(TX * TY)
   const long long nxy = (long long)nx * ny, n = nxy * nz;
   const bool edge_q = t.q > 0 && t.dj == 0, edge_p = t.p > 0 && t.di == 0;
   auto row_of = [&](int s) { return t.col0 + nxy * (BWD ? nz - 1 - s : s); };
+  // Only loads here: an instruction that used a loaded value would hold the warp's
+  // in-order issue until the load returned.
   struct Cell {
     double c0, c1, c2, x, dd, sc, eq, ep;
   };
@@ -711,10 +722,23 @@ __global__ void __launch_bounds__(TX * TY)
     if (edge_q) cl.eq = ld_relaxed64(&out[r + t.step_j]);
     if (edge_p) cl.ep = ld_relaxed64(&out[r + t.step_i]);
   };
+  // The terms of the next step's cell that do not need the neighbours' values, formed
+  // before the barrier: forward x - c0 prev (k first in CSR order); backward y rdi and the
+  // product c2 prev (k last).
+  double part = 0.0, part2 = 0.0;
+  auto own = [&](const Cell &cl, double prev) {
+    if (BWD) {
+      part = cl.x * cl.sc;
+      part2 = __dmul_rn(cl.c2, prev);
+    } else {
+      part = __dsub_rn(cl.x, __dmul_rn(cl.c0, prev));
+    }
+  };
 #pragma unroll
   for (int u = 0; u < kRing; ++u) load(u - t.di - t.dj, ring[u]);
   const int nlev = TX + TY - 2 + nz;
-  double prev = 0.0;
+  double prev = 0.0;  // +0: the first cell of a column has no own-column neighbour
+  own(ring[0], prev);
   for (int L0 = 0; L0 < nlev; L0 += kRing) {
 #pragma unroll
     for (int u = 0; u < kRing; ++u) {
@@ -726,27 +750,21 @@ __global__ void __launch_bounds__(TX * TY)
           const long long r = row_of(s);
           const Cell cl = ring[u];
           bool ok = true;
-          double vq = 0.0, vp = 0.0;
-          if (t.q > 0)
-            vq = t.dj > 0 ? sm[(L - 1) & 1][t.dj - 1][t.di]
-                          : (is_sentinel(cl.eq) ? sf_value(&out[r + t.step_j], &ctl[3], spin, &ok)
-                                                : cl.eq);
-          if (t.p > 0)
-            vp = t.di > 0 ? sm[(L - 1) & 1][t.dj][t.di - 1]
-                          : (is_sentinel(cl.ep) ? sf_value(&out[r + t.step_i], &ctl[3], spin, &ok)
-                                                : cl.ep);
+          const double sq = sm[(L - 1) & 1][t.dj > 0 ? t.dj - 1 : 0][t.di];
+          const double sp = sm[(L - 1) & 1][t.dj][t.di > 0 ? t.di - 1 : 0];
+          double vq = t.dj > 0 ? sq : (edge_q ? cl.eq : 0.0);
+          double vp = t.di > 0 ? sp : (edge_p ? cl.ep : 0.0);
+          if (edge_q && is_sentinel(vq)) vq = sf_value(&out[r + t.step_j], &ctl[3], spin, &ok);
+          if (edge_p && is_sentinel(vp)) vp = sf_value(&out[r + t.step_i], &ctl[3], spin, &ok);
           if (!ok) sf_fail(&ctl[3], S);
           double acc;
           if (!BWD) {  // lower entries in CSR order: k, j, i
-            acc = cl.x;
-            if (s > 0) acc = __dsub_rn(acc, __dmul_rn(cl.c0, prev));
-            if (t.q > 0) acc = __dsub_rn(acc, __dmul_rn(cl.c1, vq));
-            if (t.p > 0) acc = __dsub_rn(acc, __dmul_rn(cl.c2, vp));
+            acc = __dsub_rn(part, __dmul_rn(cl.c1, vq));
+            acc = __dsub_rn(acc, __dmul_rn(cl.c2, vp));
           } else {  // upper entries in CSR order: i, j, k
-            acc = cl.x * cl.sc;
-            if (t.p > 0) acc = __dsub_rn(acc, __dmul_rn(cl.c0, vp));
-            if (t.q > 0) acc = __dsub_rn(acc, __dmul_rn(cl.c1, vq));
-            if (s > 0) acc = __dsub_rn(acc, __dmul_rn(cl.c2, prev));
+            acc = __dsub_rn(part, __dmul_rn(cl.c0, vp));
+            acc = __dsub_rn(acc, __dmul_rn(cl.c1, vq));
+            acc = __dsub_rn(acc, part2);
           }
           val = acc * cl.dd;
           st_relaxed64(&out[r], val);
@@ -754,6 +772,7 @@ __global__ void __launch_bounds__(TX * TY)
         }
         load(s + kRing, ring[u]);
         sm[L & 1][t.dj][t.di] = val;
+        own(ring[(u + 1) % kRing], prev);
         __syncthreads();
       }
     }
@@ -1199,6 +1218,11 @@ static int ensure_state(fcg_context *c, int nsw) {
       const char *e = std::getenv("FCG_SWEEP");
       k->sf_on = !(e && std::string(e) == "levels");
       k->wave_on = !(e && (std::string(e) == "levels" || std::string(e) == "rows"));
+      // 16 x 8 tiles while 8 x 8 ones would number fewer than two per SM; FCG_WAVE_TILE
+      // (8x8 or 16x8) overrides
+      const char *wt = std::getenv("FCG_WAVE_TILE");
+      const long long t88 = (long long)((c->hex.nx + 7) / 8) * ((c->hex.ny + 7) / 8);
+      k->wave_wide = wt ? std::string(wt) == "16x8" : t88 < 2LL * c->num_sms;
       // two blocks per SM: more resident warps only poll further ahead (measured)
       k->sf_grid = std::min(k->sf_grid, c->num_sms * 2);
     }
@@ -1301,12 +1325,40 @@ static bool wave_sweeps(const fcg_context *c) {
   return k->sf_on && k->wave_on && c->hex.ok && k->wlo && k->sf_absent_row < 0;
 }
 
-// Tiles of 8 x 8 columns: at 128^3 and 256^3 they spread the FP64 work of one wavefront
-// step over more SMs than 16 x 16 tiles (measured 1.0x and 1.2x faster).
-constexpr int kWaveTile = 8;
-
+// Tiles of 16 x 8 or 8 x 8 columns (64 or 128 threads per block).  Measured on 20 ICCG
+// sweeps: at 128^3 (256 tiles of 8 x 8) 16 x 8 tiles are 4% faster, at 256^3 (1024 tiles of
+// 8 x 8) 8 x 8 tiles are 11% faster, where enough tiles are in flight to keep the SMs'
+// FP64 units busy.
+template <int TX, int TY>
 static int wave_tiles(const fcg_context *c) {
-  return ((c->hex.nx + kWaveTile - 1) / kWaveTile) * ((c->hex.ny + kWaveTile - 1) / kWaveTile);
+  return ((c->hex.nx + TX - 1) / TX) * ((c->hex.ny + TY - 1) / TY);
+}
+
+template <int TX, int TY>
+static void launch_wave_sweep(fcg_context *c, cudaStream_t st, bool forward, const double *b,
+                              double *z) {
+  KrylovState *k = c->ks;
+  const HexBlock &h = c->hex;
+  if (forward)
+    k_wave_sweep<TX, TY, false><<<wave_tiles<TX, TY>(c), TX * TY, 0, st>>>(
+        h.nx, h.ny, h.nz, k->wlo, b, k->d, k->rdi, k->sf_y, k->sf_ctl, k->S, k->sf_spin);
+  else
+    k_wave_sweep<TX, TY, true><<<wave_tiles<TX, TY>(c), TX * TY, 0, st>>>(
+        h.nx, h.ny, h.nz, k->wup, k->sf_y, k->d, k->rdi, z, k->sf_ctl, k->S, k->sf_spin);
+}
+
+template <int TX, int TY>
+static void launch_wave_factor(fcg_context *c, bool dilu) {
+  KrylovState *k = c->ks;
+  const HexBlock &h = c->hex;
+  if (dilu)
+    k_wave_factor<TX, TY, true><<<wave_tiles<TX, TY>(c), TX * TY, 0, c->stream>>>(
+        h.nx, h.ny, h.nz, c->mv.ioffset, c->mv.diag, c->tpos, k->a, k->d, k->rdi, k->sf_ctl,
+        k->S, k->sf_spin);
+  else
+    k_wave_factor<TX, TY, false><<<wave_tiles<TX, TY>(c), TX * TY, 0, c->stream>>>(
+        h.nx, h.ny, h.nz, c->mv.ioffset, c->mv.diag, c->tpos, k->a, k->d, k->rdi, k->sf_ctl,
+        k->S, k->sf_spin);
 }
 
 static void launch_sweeps(fcg_context *c, cudaStream_t st, const Level &lv, bool forward,
@@ -1314,21 +1366,23 @@ static void launch_sweeps(fcg_context *c, cudaStream_t st, const Level &lv, bool
   KrylovState *k = c->ks;
   if (k->sf_on) {
     const bool wave = wave_sweeps(c);
-    const HexBlock &h = c->hex;
-    constexpr int T = kWaveTile;
+    auto wave_launch = [&](bool fwd) {
+      if (k->wave_wide)
+        launch_wave_sweep<16, 8>(c, st, fwd, b, z);
+      else
+        launch_wave_sweep<8, 8>(c, st, fwd, b, z);
+    };
     if (forward) {  // b -> sf_y, after the sentinel fill of sf_y and z
       k_sf_fill<<<grid_for(c->n, c->num_sms), kTPB, 0, st>>>(c->n, k->sf_y, z, k->sf_ctl);
       if (wave)
-        k_wave_sweep<T, T, false><<<wave_tiles(c), T * T, 0, st>>>(
-            h.nx, h.ny, h.nz, k->wlo, b, k->d, k->rdi, k->sf_y, k->sf_ctl, k->S, k->sf_spin);
+        wave_launch(true);
       else
         k_fwd_sf<<<k->sf_grid, kTPB, 0, st>>>(lv.pad, lv.pad_len, c->mv.ioffset, c->mv.ja,
                                               c->mv.diag, k->a, k->d, b, k->sf_y, k->sf_ctl,
                                               k->S, k->sf_spin, k->sf_absent_row);
     } else {  // sf_y -> z
       if (wave)
-        k_wave_sweep<T, T, true><<<wave_tiles(c), T * T, 0, st>>>(
-            h.nx, h.ny, h.nz, k->wup, k->sf_y, k->d, k->rdi, z, k->sf_ctl, k->S, k->sf_spin);
+        wave_launch(false);
       else
         k_bwd_sf<<<k->sf_grid, kTPB, 0, st>>>(lv.pad, lv.pad_len, c->mv.ioffset, c->mv.ja,
                                               c->mv.diag, k->a, k->d, k->rdi, k->sf_y, z,
@@ -1568,17 +1622,12 @@ static int run_solver(fcg_context *c, int kind, const double *a, const double *s
                                                                     k->sf_ctl);
     if (wave_sweeps(c)) {
       const HexBlock &h = c->hex;
-      constexpr int T = kWaveTile;
       k_wave_coef<<<grid_for(c->n, c->num_sms), kTPB, 0, c->stream>>>(
           h.nx, h.ny, h.nz, c->mv.ioffset, c->mv.diag, k->a, k->wlo, k->wup);
-      if (kind == SK_BICG)
-        k_wave_factor<T, T, true><<<wave_tiles(c), T * T, 0, c->stream>>>(
-            h.nx, h.ny, h.nz, c->mv.ioffset, c->mv.diag, c->tpos, k->a, k->d, k->rdi, k->sf_ctl,
-            k->S, k->sf_spin);
+      if (k->wave_wide)
+        launch_wave_factor<16, 8>(c, kind == SK_BICG);
       else
-        k_wave_factor<T, T, false><<<wave_tiles(c), T * T, 0, c->stream>>>(
-            h.nx, h.ny, h.nz, c->mv.ioffset, c->mv.diag, c->tpos, k->a, k->d, k->rdi, k->sf_ctl,
-            k->S, k->sf_spin);
+        launch_wave_factor<8, 8>(c, kind == SK_BICG);
     } else {
       k_factor_sf<<<k->sf_grid, kTPB, 0, c->stream>>>(
           c->lf.pad, c->lf.pad_len, c->mv.ioffset, c->mv.ja, c->mv.diag, c->tpos, k->a, k->d,

@@ -17,34 +17,41 @@ from tests.meshes import fixture_mesh, hex_mesh, oracle_csr, poisson_system
 pytestmark = pytest.mark.gpu
 
 
-def _context(m, levels):
+def _context(m, levels, tile=None):
     """A context whose solver state (created at its first solve) uses the level
     launches (levels=True or "levels"), the row-claiming one-launch sweeps ("rows") or
-    the default (False: wavefront tiles on hex blocks, rows elsewhere)."""
-    old = os.environ.get("FCG_SWEEP")
+    the default (False: wavefront tiles on hex blocks, rows elsewhere); tile="8x8"
+    selects 8 x 8 wavefront tiles instead of 16 x 8."""
+    saved = {k: os.environ.get(k) for k in ("FCG_SWEEP", "FCG_WAVE_TILE")}
     mode = "levels" if levels is True else levels
     if mode:
         os.environ["FCG_SWEEP"] = mode
     else:
         os.environ.pop("FCG_SWEEP", None)
+    if tile:
+        os.environ["FCG_WAVE_TILE"] = tile
+    else:
+        os.environ.pop("FCG_WAVE_TILE", None)
     try:
         c = fcg.Context(m)
         c.set_solver_options(float(np.float32(1e-20)), True)  # creates the solver state
     finally:
-        if old is None:
-            os.environ.pop("FCG_SWEEP", None)
-        else:
-            os.environ["FCG_SWEEP"] = old
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
     return c
 
 
 @pytest.mark.parametrize("name", ["hex12", "hex20", "hex33", "pitzdaily"])
 def test_one_launch_sweeps_equal_level_sweeps(name):
-    """hex12 is one 8 x 8 tile and a partial one, hex20 and hex33 cut tiles at the block
-    edge and have tiles that wait on several others; pitzDaily is not a block (no
-    wavefront form)."""
+    """hex12 is one 16 x 8 tile and a partial one (one 8 x 8 tile and partial ones in the
+    8 x 8 form), hex20 and hex33 cut tiles at the block edge and have tiles that wait on
+    several others; pitzDaily is not a block (no wavefront form)."""
     m = fixture_mesh("pitzdaily") if name == "pitzdaily" else hex_mesh(int(name[3:]), 0.2)
-    ctxs = [_context(m, mode) for mode in (False, "rows", "levels")]
+    ctxs = [_context(m, False), _context(m, False, "8x8"), _context(m, "rows"),
+            _context(m, "levels")]
     mu, phi, su0 = poisson_system(m)
     a, su = ctxs[0].laplacian(mu, phi, su0)
     x0 = np.zeros(m.numCells)
