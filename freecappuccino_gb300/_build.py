@@ -20,7 +20,7 @@ LIB = os.path.join(OUT, "libfcgpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Translation units that must round like the reference (no contraction into FMA).
-NO_FMA = {"assembly.cu", "gradients.cu", "momentum.cu", "piso.cu", "setup.cu"}
+NO_FMA = {"aggregation_gpu.cu", "assembly.cu", "gradients.cu", "momentum.cu", "piso.cu", "setup.cu"}
 
 
 def _nvcc() -> str:

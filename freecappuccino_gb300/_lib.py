@@ -188,6 +188,7 @@ _PROTOS = {
     "fcg_lp_set_multilevel": (C.c_int, [_LP, C.POINTER(Multilevel)]),
     "fcg_lp_get_multilevel": (C.c_int, [_LP, C.POINTER(Multilevel)]),
     "fcg_lp_hierarchy_info": (C.c_int, [_LP, _CTX, _ip, _ip, C.POINTER(C.c_longlong), _dp]),
+    "fcg_lp_hierarchy_built_on": (C.c_int, [_LP, _CTX, _ip]),
     "fcg_lp_hierarchy_level": (C.c_int, [_LP, _CTX, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
     "fcg_lp_precondition": (C.c_int, [_LP, _CTX, _vp, _vp]),
     "fcg_lp_coarse_correct": (C.c_int, [_LP, _CTX, _vp, _vp, _vp]),

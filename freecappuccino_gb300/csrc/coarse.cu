@@ -593,9 +593,145 @@ void Hierarchy::release() {
   uid = 0;
 }
 
-int build(Hierarchy &H, fcg_context *c, const Options &o, std::string &err) {
-  const auto t0 = std::chrono::steady_clock::now();
-  H.release();
+namespace {
+
+// The arrays of one level below the fine one, on the host or on the device.
+struct LevelSrc {
+  int n = 0, np = 0;  // rows, rows of the level above
+  long long nnz = 0;
+  const int *ptr = nullptr, *mptr = nullptr, *col = nullptr, *agg = nullptr, *mem = nullptr;
+};
+
+// The smoothed first level's patterns.
+struct SmoothSrc {
+  long long p_nnz = 0, ap_nnz = 0;
+  const int *p_ptr = nullptr, *ap_ptr = nullptr, *p_col = nullptr, *t_row = nullptr,
+            *t_pos = nullptr, *t_ptr = nullptr, *ap_col = nullptr;
+};
+
+// Allocates H's levels and copies the patterns in (kind: host or device sources).
+int fill(Hierarchy &H, fcg_context *c, const Options &o, const std::vector<LevelSrc> &ls,
+         const SmoothSrc *sm, cudaMemcpyKind kind, std::string &err) {
+  const int n = c->n;
+  cudaError_t e;
+  auto cp = [&](void *dst, const void *src, size_t bytes) {
+    return cudaMemcpyAsync(dst, src, bytes, kind, c->stream);
+  };
+  H.lv.resize(ls.size());
+  for (size_t l = 0; l < ls.size(); ++l) {
+    const LevelSrc &h = ls[l];
+    DevLevel &L = H.lv[l];
+    const int np = h.np;
+    L.n = h.n;
+    L.nnz = h.nnz;
+    const size_t ib = pad256(sizeof(int) * (h.n + 1)) * 2 + pad256(sizeof(int) * L.nnz) +
+                      pad256(sizeof(int) * np) * 2;
+    const size_t vb = pad256(sizeof(float) * L.nnz) + pad256(sizeof(float) * h.n);
+    const size_t xb = 3 * pad256(sizeof(float) * h.n);
+    if ((e = L.ints.ensure(ib)) || (e = L.vals.ensure(vb)) || (e = L.vecs.ensure(xb))) {
+      err = std::string("hierarchy allocation: ") + cudaGetErrorString(e);
+      return FCG_ERR_CUDA;
+    }
+    char *p = (char *)L.ints.p;
+    L.ptr = carve<int>(p, h.n + 1);
+    L.mptr = carve<int>(p, h.n + 1);
+    L.col = carve<int>(p, L.nnz);
+    L.agg = carve<int>(p, np);
+    L.mem = carve<int>(p, np);
+    p = (char *)L.vals.p;
+    L.a32 = carve<float>(p, L.nnz);
+    L.dinv = carve<float>(p, h.n);
+    p = (char *)L.vecs.p;
+    L.b = carve<float>(p, h.n);
+    L.x = carve<float>(p, h.n);
+    L.y = carve<float>(p, h.n);
+    if ((e = cp(L.ptr, h.ptr, sizeof(int) * (h.n + 1))) ||
+        (e = cp(L.mptr, h.mptr, sizeof(int) * (h.n + 1))) ||
+        (e = cp(L.col, h.col, sizeof(int) * L.nnz)) || (e = cp(L.agg, h.agg, sizeof(int) * np)) ||
+        (e = cp(L.mem, h.mem, sizeof(int) * np))) {
+      err = std::string("hierarchy upload: ") + cudaGetErrorString(e);
+      return FCG_ERR_CUDA;
+    }
+  }
+  if (sm) {
+    H.p_nnz = sm->p_nnz;
+    H.ap_nnz = sm->ap_nnz;
+    const int n1 = ls[0].n;
+    const size_t ib = pad256(sizeof(int) * (n + 1)) * 2 + pad256(sizeof(int) * H.p_nnz) * 3 +
+                      pad256(sizeof(int) * (n1 + 1)) + pad256(sizeof(int) * H.ap_nnz);
+    const size_t vb = pad256(sizeof(float) * H.p_nnz) + pad256(sizeof(float) * H.ap_nnz);
+    if ((e = H.sa_ints.ensure(ib)) || (e = H.sa_vals.ensure(vb))) {
+      err = std::string("hierarchy allocation: ") + cudaGetErrorString(e);
+      return FCG_ERR_CUDA;
+    }
+    char *p = (char *)H.sa_ints.p;
+    H.p_ptr = carve<int>(p, n + 1);
+    H.ap_ptr = carve<int>(p, n + 1);
+    H.p_col = carve<int>(p, H.p_nnz);
+    H.t_row = carve<int>(p, H.p_nnz);
+    H.t_pos = carve<int>(p, H.p_nnz);
+    H.t_ptr = carve<int>(p, n1 + 1);
+    H.ap_col = carve<int>(p, H.ap_nnz);
+    p = (char *)H.sa_vals.p;
+    H.p_val = carve<float>(p, H.p_nnz);
+    H.ap_val = carve<float>(p, H.ap_nnz);
+    if ((e = cp(H.p_ptr, sm->p_ptr, sizeof(int) * (n + 1))) ||
+        (e = cp(H.ap_ptr, sm->ap_ptr, sizeof(int) * (n + 1))) ||
+        (e = cp(H.p_col, sm->p_col, sizeof(int) * H.p_nnz)) ||
+        (e = cp(H.t_row, sm->t_row, sizeof(int) * H.p_nnz)) ||
+        (e = cp(H.t_pos, sm->t_pos, sizeof(int) * H.p_nnz)) ||
+        (e = cp(H.t_ptr, sm->t_ptr, sizeof(int) * (n1 + 1))) ||
+        (e = cp(H.ap_col, sm->ap_col, sizeof(int) * H.ap_nnz))) {
+      err = std::string("hierarchy upload: ") + cudaGetErrorString(e);
+      return FCG_ERR_CUDA;
+    }
+  }
+  if ((e = cudaStreamSynchronize(c->stream))) {
+    err = std::string("hierarchy upload: ") + cudaGetErrorString(e);
+    return FCG_ERR_CUDA;
+  }
+  (void)o;
+  return FCG_OK;
+}
+
+// The levels built on the device (aggregation_gpu.cu) from the scaled fine matrix.
+// Returns FCG_OK, FCG_ERR_CUDA, or another code when the host should build instead.
+int build_on_device(Hierarchy &H, fcg_context *c, const Options &o, int dmax, std::string &err) {
+  const int n = c->n;
+  const long long nnz = c->nnz;
+  DevMat fine;
+  cudaError_t e;
+  if ((e = fine.val.ensure(sizeof(double) * (nnz > 0 ? nnz : 1)))) {
+    err = std::string("hierarchy allocation: ") + cudaGetErrorString(e);
+    return FCG_ERR_CUDA;
+  }
+  fine_values(c, sliced64(c), c->sv.src, c->sell_len, scale64(c), fine.val.as<double>());
+  const DevCsr fv{n, nnz, c->mv.ioffset, c->mv.ja, fine.val.as<double>()};
+  std::vector<DevBuiltLevel> dl;
+  int rc = build_levels_device(c, fv, std::max(2, o.max_levels), dmax, H.passes,
+                               o.smoothed ? o.omega : 0.0, dl, err);
+  fine.release();
+  if (rc == FCG_OK) {
+    std::vector<LevelSrc> ls(dl.size());
+    for (size_t l = 0; l < dl.size(); ++l) {
+      const DevBuiltLevel &d = dl[l];
+      ls[l] = {d.n, d.np, d.A.nnz, d.A.ptr.as<int>(), d.mptr.as<int>(), d.A.col.as<int>(),
+               d.agg.as<int>(), d.mem.as<int>()};
+    }
+    SmoothSrc sm;
+    const bool smooth = !dl.empty() && o.smoothed;
+    if (smooth) {
+      const DevBuiltLevel &d = dl[0];
+      sm = {d.p_nnz, d.ap_nnz, d.p_ptr.as<int>(), d.ap_ptr.as<int>(), d.p_col.as<int>(),
+            d.t_row.as<int>(), d.t_pos.as<int>(), d.t_ptr.as<int>(), d.ap_col.as<int>()};
+    }
+    rc = fill(H, c, o, ls, smooth ? &sm : nullptr, cudaMemcpyDeviceToDevice, err);
+  }
+  for (auto &d : dl) d.release();
+  return rc;
+}
+
+int build_on_host(Hierarchy &H, fcg_context *c, const Options &o, int dmax, std::string &err) {
   const int n = c->n;
   const long long nnz = c->nnz, len = c->sell_len;
   HostCsr fine;
@@ -628,85 +764,57 @@ int build(Hierarchy &H, fcg_context *c, const Options &o, std::string &err) {
     for (int k = fine.ptr[i]; k < fine.ptr[i + 1]; ++k)
       fine.val[k] = (fine.val[k] * s[i]) * s[fine.col[k]];
   std::vector<HostLevel> hl;
-  const int dmax = std::min(std::max(o.dense_max, 1), kDenseMaxRows);
   build_levels(fine, std::max(2, o.max_levels), dmax, H.passes, hl, o.smoothed ? o.omega : 0.0);
   fine = HostCsr();
-  H.lv.resize(hl.size());
-  int np = n;  // rows of the parent level
+  std::vector<LevelSrc> ls(hl.size());
+  int np = n;
   for (size_t l = 0; l < hl.size(); ++l) {
     const HostLevel &h = hl[l];
-    DevLevel &L = H.lv[l];
-    L.n = h.n;
-    L.nnz = (long long)h.A.col.size();
-    const size_t ib = pad256(sizeof(int) * (h.n + 1)) * 2 + pad256(sizeof(int) * L.nnz) +
-                      pad256(sizeof(int) * np) * 2;
-    const size_t vb = pad256(sizeof(float) * L.nnz) + pad256(sizeof(float) * h.n);
-    const size_t xb = 3 * pad256(sizeof(float) * h.n);
-    if ((e = L.ints.ensure(ib)) || (e = L.vals.ensure(vb)) || (e = L.vecs.ensure(xb))) {
-      err = std::string("hierarchy allocation: ") + cudaGetErrorString(e);
-      H.release();
-      return FCG_ERR_CUDA;
-    }
-    char *p = (char *)L.ints.p;
-    L.ptr = carve<int>(p, h.n + 1);
-    L.mptr = carve<int>(p, h.n + 1);
-    L.col = carve<int>(p, L.nnz);
-    L.agg = carve<int>(p, np);
-    L.mem = carve<int>(p, np);
-    p = (char *)L.vals.p;
-    L.a32 = carve<float>(p, L.nnz);
-    L.dinv = carve<float>(p, h.n);
-    p = (char *)L.vecs.p;
-    L.b = carve<float>(p, h.n);
-    L.x = carve<float>(p, h.n);
-    L.y = carve<float>(p, h.n);
-    if ((e = cudaMemcpy(L.ptr, h.A.ptr.data(), sizeof(int) * (h.n + 1), cudaMemcpyHostToDevice)) ||
-        (e = cudaMemcpy(L.mptr, h.mptr.data(), sizeof(int) * (h.n + 1), cudaMemcpyHostToDevice)) ||
-        (e = cudaMemcpy(L.col, h.A.col.data(), sizeof(int) * L.nnz, cudaMemcpyHostToDevice)) ||
-        (e = cudaMemcpy(L.agg, h.agg.data(), sizeof(int) * np, cudaMemcpyHostToDevice)) ||
-        (e = cudaMemcpy(L.mem, h.mem.data(), sizeof(int) * np, cudaMemcpyHostToDevice))) {
-      err = std::string("hierarchy upload: ") + cudaGetErrorString(e);
-      H.release();
-      return FCG_ERR_CUDA;
-    }
+    ls[l] = {h.n, np, (long long)h.A.col.size(), h.A.ptr.data(), h.mptr.data(), h.A.col.data(),
+             h.agg.data(), h.mem.data()};
     np = h.n;
   }
-  if (!hl.empty() && o.smoothed) {
+  SmoothSrc sm;
+  const bool smooth = !hl.empty() && o.smoothed;
+  if (smooth) {
     const HostLevel &h = hl[0];
-    H.p_nnz = (long long)h.p_col.size();
-    H.ap_nnz = (long long)h.ap_col.size();
-    const int n1 = h.n;
-    const size_t ib = pad256(sizeof(int) * (n + 1)) * 2 + pad256(sizeof(int) * H.p_nnz) * 3 +
-                      pad256(sizeof(int) * (n1 + 1)) + pad256(sizeof(int) * H.ap_nnz);
-    const size_t vb = pad256(sizeof(float) * H.p_nnz) + pad256(sizeof(float) * H.ap_nnz);
-    if ((e = H.sa_ints.ensure(ib)) || (e = H.sa_vals.ensure(vb))) {
-      err = std::string("hierarchy allocation: ") + cudaGetErrorString(e);
+    sm = {(long long)h.p_col.size(), (long long)h.ap_col.size(), h.p_ptr.data(),
+          h.ap_ptr.data(), h.p_col.data(), h.t_row.data(), h.t_pos.data(), h.t_ptr.data(),
+          h.ap_col.data()};
+  }
+  return fill(H, c, o, ls, smooth ? &sm : nullptr, cudaMemcpyHostToDevice, err);
+}
+
+}  // namespace
+
+int build(Hierarchy &H, fcg_context *c, const Options &o, std::string &err) {
+  const auto t0 = std::chrono::steady_clock::now();
+  H.release();
+  const int n = c->n;
+  const int dmax = std::min(std::max(o.dense_max, 1), kDenseMaxRows);
+  // FCG_AGG=host builds the levels on the host (aggregation.cpp); the device build gives
+  // the same arrays and falls back to the host when a matching wait gives up or a coarse
+  // row outgrows its accumulation table
+  const char *where = std::getenv("FCG_AGG");
+  int rc = FCG_ERR_UNSUPPORTED;
+  H.built_on_device = false;
+  if (!(where && std::string(where) == "host")) {
+    rc = build_on_device(H, c, o, dmax, err);
+    if (rc == FCG_ERR_CUDA) {
       H.release();
-      return FCG_ERR_CUDA;
+      return rc;
     }
-    char *p = (char *)H.sa_ints.p;
-    H.p_ptr = carve<int>(p, n + 1);
-    H.ap_ptr = carve<int>(p, n + 1);
-    H.p_col = carve<int>(p, H.p_nnz);
-    H.t_row = carve<int>(p, H.p_nnz);
-    H.t_pos = carve<int>(p, H.p_nnz);
-    H.t_ptr = carve<int>(p, n1 + 1);
-    H.ap_col = carve<int>(p, H.ap_nnz);
-    p = (char *)H.sa_vals.p;
-    H.p_val = carve<float>(p, H.p_nnz);
-    H.ap_val = carve<float>(p, H.ap_nnz);
-    if ((e = cudaMemcpy(H.p_ptr, h.p_ptr.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice)) ||
-        (e = cudaMemcpy(H.ap_ptr, h.ap_ptr.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice)) ||
-        (e = cudaMemcpy(H.p_col, h.p_col.data(), sizeof(int) * H.p_nnz, cudaMemcpyHostToDevice)) ||
-        (e = cudaMemcpy(H.t_row, h.t_row.data(), sizeof(int) * H.p_nnz, cudaMemcpyHostToDevice)) ||
-        (e = cudaMemcpy(H.t_pos, h.t_pos.data(), sizeof(int) * H.p_nnz, cudaMemcpyHostToDevice)) ||
-        (e = cudaMemcpy(H.t_ptr, h.t_ptr.data(), sizeof(int) * (n1 + 1), cudaMemcpyHostToDevice)) ||
-        (e = cudaMemcpy(H.ap_col, h.ap_col.data(), sizeof(int) * H.ap_nnz, cudaMemcpyHostToDevice))) {
-      err = std::string("hierarchy upload: ") + cudaGetErrorString(e);
+    H.built_on_device = rc == FCG_OK;
+  }
+  if (rc != FCG_OK) {
+    H.release();
+    err.clear();
+    if ((rc = build_on_host(H, c, o, dmax, err))) {
       H.release();
-      return FCG_ERR_CUDA;
+      return rc;
     }
   }
+  cudaError_t e;
   H.smoothed = o.smoothed;
   H.sa_omega = o.omega;
   if (!H.lv.empty()) {

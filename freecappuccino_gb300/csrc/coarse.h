@@ -49,6 +49,51 @@ int build_levels(const HostCsr &fine, int max_levels, int dense_max, int passes,
 // The smoothed first level (sa_omega > 0 in build_levels): patterns and FP64 values.
 void smoothed_level(const HostCsr &A, double omega, HostLevel &lv);
 
+// A CSR matrix on the device, 0-based, columns ascending in every row.
+struct DevCsr {
+  int n = 0;
+  long long nnz = 0;
+  const int *ptr = nullptr, *col = nullptr;
+  const double *val = nullptr;
+};
+
+// A device CSR that owns its arrays.
+struct DevMat {
+  int n = 0;
+  long long nnz = 0;
+  DBuf ptr, col, val;
+  DevCsr view() const { return {n, nnz, ptr.as<int>(), col.as<int>(), val.as<double>()}; }
+  void release() {
+    ptr.release();
+    col.release();
+    val.release();
+  }
+};
+
+// A HostLevel built on the device (aggregation_gpu.cu): the same arrays, on c's device;
+// np is the row count of the level above.  Owns its buffers until release().
+struct DevBuiltLevel {
+  int n = 0, np = 0;
+  DBuf agg, mptr, mem;
+  DevMat A;
+  long long p_nnz = 0, ap_nnz = 0;
+  DBuf p_ptr, p_col, t_ptr, t_row, t_pos, ap_ptr, ap_col;
+  void release();
+};
+
+// The scaled fine matrix's CSR values on the device: the sliced FP64 values scattered to
+// CSR order through src (len slots, -1 for padding), then (a_ik s_i) s_k, as build() forms
+// them on the host.
+void fine_values(fcg_context *c, const double *sval, const int *src, long long len,
+                 const double *s, double *val);
+
+// build_levels on the device, element for element the host's result.  Returns FCG_OK,
+// FCG_ERR_TIMEOUT when a dependency wait of the matching gave up, FCG_ERR_UNSUPPORTED when
+// a coarse row outgrows the accumulation tables, or FCG_ERR_CUDA; err says which.
+int build_levels_device(fcg_context *c, const DevCsr &fine, int max_levels, int dense_max,
+                        int passes, double sa_omega, std::vector<DevBuiltLevel> &levels,
+                        std::string &err);
+
 // Options of the correction (fcg_lp_set_multilevel).
 struct Options {
   int enabled = 1;
@@ -88,6 +133,7 @@ struct Hierarchy {
   bool has_dense = false;
   DBuf fine_tmp;                // two FP32 vectors of the fine level
   double setup_seconds = 0.0;
+  bool built_on_device = false;  // the levels came from aggregation_gpu.cu
   unsigned long long build_id = 0;  // bumped at every build (keys captured graphs)
   bool built_for(const fcg_context *c, const struct Options &o) const {
     return uid == c->uid && gen == c->bind_gen && max_levels == o.max_levels &&

@@ -177,14 +177,17 @@ int validate_topology(const fcg_mesh_desc &m, const int cnt[B_NTYPES], const int
 int build_csr(const fcg_mesh_desc &m, HostTopology &t, std::string &err);
 int build_rest(const fcg_mesh_desc &m, const int cnt[B_NTYPES], const int fst[B_NTYPES],
                const int bst[B_NTYPES], HostTopology &t);
-// The whole topology built on c's device (setup.cu), 0-based and owned by the bound
-// mesh, element for element the host construction: fills c->mv's CSR, slot maps and
-// incidence lists, c->tpos, c->sv, c->lf / c->lb, c->nnz and c->topo.  own0 / nei0 are
-// the device copies (0-based) of owner / neighbour, own_host the 1-based host owner.
+// Exclusive scan of n ints on the context's stream: out[0..n], out[n] the total (setup.cu);
+// tmp holds the block sums.
+int scan_ints(fcg_context *c, const int *in, int *out, int n, DBuf &tmp);
 // a[i] -= 1 on the device (1-based index arrays to 0-based), on c's stream.
 int to_zero_based(fcg_context *c, int *a, long long n);
 // Fills c->hex from the bound CSR pattern (hexblock.cu); synchronises c's stream.
 int detect_hex_block(fcg_context *c);
+// The whole topology built on c's device (setup.cu), 0-based and owned by the bound
+// mesh, element for element the host construction: fills c->mv's CSR, slot maps and
+// incidence lists, c->tpos, c->sv, c->lf / c->lb, c->nnz and c->topo.  own0 / nei0 are
+// the device copies (0-based) of owner / neighbour, own_host the 1-based host owner.
 int bind_topology_device(fcg_context *c, const int *own0, const int *nei0,
                          const std::vector<int> &own_host, const int cnt[B_NTYPES],
                          const int fst[B_NTYPES], const int bst[B_NTYPES], std::string &err);

@@ -2084,6 +2084,14 @@ extern "C" int fcg_lp_hierarchy_info(fcg_learned *Lp, fcg_context *c, int *level
   return mark_done(Lp, c);
 }
 
+extern "C" int fcg_lp_hierarchy_built_on(fcg_learned *Lp, fcg_context *c, int *on_device) {
+  if (!on_device) return FCG_ERR_ARG;
+  int rc = ml_ready(Lp, c);
+  if (rc) return rc;
+  *on_device = ml_for(Lp, c)->built_on_device ? 1 : 0;
+  return mark_done(Lp, c);
+}
+
 extern "C" int fcg_lp_hierarchy_level(fcg_learned *Lp, fcg_context *c, int level, int *agg,
                                       int *mptr, int *mem, int *ptr, int *col, float *val) {
   int rc = ml_ready(Lp, c);

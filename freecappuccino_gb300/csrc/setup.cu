@@ -112,18 +112,22 @@ struct Tmp {
   ~Tmp() { b.release(); }
 };
 
-int scan_exclusive(fcg_context *c, const int *in, int *out, int n, Tmp &tmp) {
+int scan_into(fcg_context *c, const int *in, int *out, int n, DBuf &tmp) {
   const int nb = (n + kScanChunk - 1) / kScanChunk;
-  FCG_CUDA_TRY(c, tmp.b.ensure(sizeof(int) * (nb > 0 ? nb : 1)));
+  FCG_CUDA_TRY(c, tmp.ensure(sizeof(int) * (nb > 0 ? nb : 1)));
   if (n == 0) {
     FCG_CUDA_TRY(c, cudaMemsetAsync(out, 0, sizeof(int), c->stream));
     return FCG_OK;
   }
-  k_scan_local<<<nb, kScanThreads, 0, c->stream>>>(in, out, n, tmp.b.as<int>());
-  k_scan_sums<<<1, kScanThreads, 0, c->stream>>>(tmp.b.as<int>(), nb);
-  k_scan_add<<<grid_for(n, c->num_sms), kTPB, 0, c->stream>>>(out, in, n, tmp.b.as<int>());
+  k_scan_local<<<nb, kScanThreads, 0, c->stream>>>(in, out, n, tmp.as<int>());
+  k_scan_sums<<<1, kScanThreads, 0, c->stream>>>(tmp.as<int>(), nb);
+  k_scan_add<<<grid_for(n, c->num_sms), kTPB, 0, c->stream>>>(out, in, n, tmp.as<int>());
   FCG_CHECK_LAUNCH(c, "scan_exclusive");
   return FCG_OK;
+}
+
+int scan_exclusive(fcg_context *c, const int *in, int *out, int n, Tmp &tmp) {
+  return scan_into(c, in, out, n, tmp.b);
 }
 
 __global__ void k_fill_int(int *__restrict__ a, long long n, int v) {
@@ -475,6 +479,10 @@ int read_flag(fcg_context *c, const int *dflag, int *out) {
 }
 
 }  // namespace
+
+int fcg::scan_ints(fcg_context *c, const int *in, int *out, int n, DBuf &tmp) {
+  return scan_into(c, in, out, n, tmp);
+}
 
 extern "C" int fcg_csr_build_gpu(fcg_context *c, int numCells, int numInnerFaces,
                                  const int *owner, const int *neighbour, int *ioffset, int *ja,

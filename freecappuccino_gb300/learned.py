@@ -204,16 +204,19 @@ class LearnedPreconditioner:
         self._check(self.lib.fcg_lp_set_multilevel(self.h, C.byref(o)), "fcg_lp_set_multilevel")
 
     def hierarchy(self, ctx: Context) -> dict:
-        """Levels (the fine one first): cells and entries of each, and the seconds the
-        host construction took."""
+        """Levels (the fine one first): cells and entries of each, the seconds the
+        construction took and where it ran ("device" or "host")."""
         nl = C.c_int()
         cells = (C.c_int * _lib.MAX_LEVELS)()
         ent = (C.c_longlong * _lib.MAX_LEVELS)()
         sec = C.c_double()
+        dev = C.c_int()
         self._check(self.lib.fcg_lp_hierarchy_info(self.h, ctx.h, C.byref(nl), cells, ent,
                                                    C.byref(sec)), "fcg_lp_hierarchy_info")
+        self._check(self.lib.fcg_lp_hierarchy_built_on(self.h, ctx.h, C.byref(dev)),
+                    "fcg_lp_hierarchy_built_on")
         return {"cells": list(cells[:nl.value]), "entries": list(ent[:nl.value]),
-                "setup_seconds": sec.value}
+                "setup_seconds": sec.value, "built_on": "device" if dev.value else "host"}
 
     def hierarchy_level(self, ctx: Context, level: int) -> dict:
         """Arrays of coarse level `level` (1-based below the fine one), 0-based."""

@@ -588,9 +588,14 @@ int fcg_lp_set_multilevel(fcg_learned *lp, const fcg_lp_multilevel *opt);
 int fcg_lp_get_multilevel(const fcg_learned *lp, fcg_lp_multilevel *opt);
 /* The hierarchy for ctx's mesh and the matrix last set (built if needed): *levels
  * counting the fine one, cells[l] and entries[l] of every level (arrays of
- * FCG_LP_MAX_LEVELS, may be NULL), and the seconds its host construction took. */
+ * FCG_LP_MAX_LEVELS, may be NULL), and the seconds its construction took. */
 int fcg_lp_hierarchy_info(fcg_learned *lp, fcg_context *ctx, int *levels, int *cells,
                           long long *entries, double *setup_seconds);
+/* Where that hierarchy was built: *on_device = 1 on the GPU (the default), 0 on the host
+ * (FCG_AGG=host in the environment, or after the GPU build gave up: a matching wait that
+ * ran out or a coarse row too wide for its accumulation table).  Both give the same
+ * arrays element for element. */
+int fcg_lp_hierarchy_built_on(fcg_learned *lp, fcg_context *ctx, int *on_device);
 /* Arrays of coarse level `level` (1..levels-1), 0-based, each may be NULL: agg[n_above]
  * (row of the level above -> row of this level), mptr[n+1] and mem[n_above] (rows above
  * of every row, ascending), ptr[n+1] and col[entries] (pattern, columns ascending) and

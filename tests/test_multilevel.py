@@ -245,6 +245,7 @@ def test_hierarchy_matches_oracle(name, smoothed):
     m, csr, a, su, ctx, lp = _gpu(name)
     lp.set_multilevel(smoothed=bool(smoothed))
     info = lp.hierarchy(ctx)
+    assert info["built_on"] == "device"
     fine = mo.scaled_csr(csr.ioffset, csr.ja, csr.diag, a)
     levels = mo.build_levels(*fine, sa_omega=0.67 if smoothed else 0.0)
     values = mo.level_values(levels, fine)
@@ -281,6 +282,98 @@ def test_correction_matches_oracle(name, smoothed):
     assert np.array_equal(lp.precondition(ctx, r), lp.coarse_correct(ctx, r, zn))
     ctx.close()
     lp.close()
+
+
+class _host_build:
+    """FCG_AGG=host while a hierarchy is built: aggregation.cpp instead of the device."""
+
+    def __enter__(self):
+        import os
+
+        self.old = os.environ.get("FCG_AGG")
+        os.environ["FCG_AGG"] = "host"
+
+    def __exit__(self, *exc):
+        import os
+
+        if self.old is None:
+            os.environ.pop("FCG_AGG", None)
+        else:
+            os.environ["FCG_AGG"] = self.old
+
+
+def _levels(lp, ctx):
+    info = lp.hierarchy(ctx)
+    return info, [lp.hierarchy_level(ctx, l) for l in range(1, len(info["cells"]))]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,smoothed", [("hex32", 1), ("hex32", 0), ("pitzdaily", 1),
+                                           ("hexmix8", 1), ("cavity", 0)])
+def test_device_hierarchy_equals_host_hierarchy(name, smoothed):
+    """The hierarchy built on the device (aggregation_gpu.cu) against the host build
+    (aggregation.cpp) on the same matrix: every level's aggregates, members, pattern and
+    FP32 values, and (through the smoothed prolongation's patterns) the correction and a
+    whole learned solve, bit for bit."""
+    from freecappuccino_gb300.learned import DEFAULT_WEIGHTS, LearnedPreconditioner
+
+    m, csr, a, su, ctx, lp = _gpu(name)
+    lp.set_multilevel(smoothed=bool(smoothed))
+    info_d, lev_d = _levels(lp, ctx)
+    rng = np.random.default_rng(2)
+    r = rng.standard_normal(m.numCells).astype(np.float32)
+    z = (0.5 * rng.standard_normal(m.numCells)).astype(np.float32)
+    corr_d = lp.coarse_correct(ctx, r, z)
+    x0 = np.zeros(m.numCells)
+    sol_d = lp.solve(ctx, a, su, x0, 1e-8, 5000)
+    lp.close()
+    with _host_build():
+        lp = LearnedPreconditioner(path=DEFAULT_WEIGHTS)
+        lp.set_matrix(ctx, a)
+        lp.set_multilevel(smoothed=bool(smoothed))
+        info_h, lev_h = _levels(lp, ctx)
+    assert info_d["built_on"] == "device" and info_h["built_on"] == "host"
+    assert info_d["cells"] == info_h["cells"] and info_d["entries"] == info_h["entries"]
+    for l, (gd, gh) in enumerate(zip(lev_d, lev_h), start=1):
+        for k in ("agg", "mptr", "mem", "ptr", "col", "val"):
+            assert np.array_equal(gd[k], gh[k]), (name, l, k)
+    assert np.array_equal(lp.coarse_correct(ctx, r, z), corr_d)
+    sol_h = lp.solve(ctx, a, su, x0, 1e-8, 5000)
+    assert sol_h.fcg_iters == sol_d.fcg_iters and np.array_equal(sol_h.fi, sol_d.fi)
+    print(f"\n{name}: levels {info_d['cells']}, set-up device {info_d['setup_seconds']:.3f} s, "
+          f"host {info_h['setup_seconds']:.3f} s")
+    ctx.close()
+    lp.close()
+
+
+@pytest.mark.gpu
+def test_device_hierarchy_equals_host_hierarchy_128():
+    """The same at 128^3 (jittered, variable diffusivity): every level element for
+    element, and the set-up times of both builds."""
+    from freecappuccino_gb300.learned import DEFAULT_WEIGHTS, LearnedPreconditioner, pressure_system
+
+    sysm = pressure_system(128, 0.2, 2029, variable=True)
+    ctx = sysm.ctx
+    out = []
+    for host in (False, True):
+        lp = LearnedPreconditioner(path=DEFAULT_WEIGHTS)
+        if host:
+            with _host_build():
+                lp.set_matrix(ctx, sysm.a)
+                out.append(_levels(lp, ctx))
+        else:
+            lp.set_matrix(ctx, sysm.a)
+            out.append(_levels(lp, ctx))
+        lp.close()
+    (info_d, lev_d), (info_h, lev_h) = out
+    assert info_d["built_on"] == "device" and info_h["built_on"] == "host"
+    assert info_d["cells"] == info_h["cells"] and info_d["entries"] == info_h["entries"]
+    for l, (gd, gh) in enumerate(zip(lev_d, lev_h), start=1):
+        for k in ("agg", "mptr", "mem", "ptr", "col", "val"):
+            assert np.array_equal(gd[k], gh[k]), (l, k)
+    print(f"\n128^3: levels {info_d['cells']}, set-up device {info_d['setup_seconds']:.3f} s, "
+          f"host {info_h['setup_seconds']:.3f} s")
+    ctx.close()
 
 
 @pytest.mark.gpu
