@@ -175,7 +175,7 @@ __device__ int decide_blocking(int i, const int *__restrict__ ptr, const int *__
 }
 
 constexpr int kMaxCand = 48;  // candidates of a row in the two-phase form
-constexpr int kMaxPend = 24;  // earlier rows still undecided when the row starts
+constexpr int kMaxPend = 96;  // earlier rows still undecided when the row starts
 
 // The decisions form a chain (a row waits for its predecessor when they are neighbours),
 // so a row first gathers everything already decided: whether an earlier row took it, and
@@ -686,7 +686,8 @@ int acc_rows(Ctx &x, int nrows, const Gen &gen, DBuf &ptr, DBuf &col, DBuf *val,
   int *ctl = x.ctl.as<int>();
   if ((rc = ints(x, x.cnt, nrows))) return rc;
   for (;;) {
-    // threads: enough for the rows, at most 256 MB of slabs
+    // threads: enough for the rows, at most 256 MB of slabs (more threads measured slower:
+    // the tables then spill out of L1)
     const long long budget = (256LL << 20) / (16LL * x.cap);
     long long thr = std::min<long long>({(long long)nrows, (long long)c->num_sms * 512, budget});
     thr = std::max<long long>(kAccThreads, (thr + kAccThreads - 1) / kAccThreads * kAccThreads);
