@@ -563,10 +563,14 @@ struct Ctx {
   }
   DBuf scan_tmp, ctl, cnt;
   DBuf skey, sval, sused;  // accumulation slabs
+  DBuf m_pick, m_leader, m_join, m_picker, m_lrank, m_used, m_id;  // matching scratch
+  DBuf p_agg, p_mptr, p_mem;  // one pass's aggregates and members
   int cap = 64;
   long long slab_threads = 0;
   void release() {
-    for (DBuf *b : {&scan_tmp, &ctl, &cnt, &skey, &sval, &sused}) b->release();
+    for (DBuf *b : {&scan_tmp, &ctl, &cnt, &skey, &sval, &sused, &m_pick, &m_leader, &m_join,
+                    &m_picker, &m_lrank, &m_used, &m_id, &p_agg, &p_mptr, &p_mem})
+      b->release();
   }
 };
 
@@ -626,13 +630,9 @@ int members(Ctx &x, int n, int m, const int *agg, DBuf &mptr, DBuf &mem) {
 int match(Ctx &x, const DevCsr &a, DBuf &agg, int *m) {
   fcg_context *c = x.c;
   const int n = a.n;
-  DBuf pick, leader, join, picker, lrank, used, id;
-  struct Rel {
-    DBuf *b[7];
-    ~Rel() {
-      for (DBuf *p : b) p->release();
-    }
-  } rel{{&pick, &leader, &join, &picker, &lrank, &used, &id}};
+  // scratch kept across passes (the first pass is the largest)
+  DBuf &pick = x.m_pick, &leader = x.m_leader, &join = x.m_join, &picker = x.m_picker,
+       &lrank = x.m_lrank, &used = x.m_used, &id = x.m_id;
   int rc;
   if ((rc = ints(x, pick, n)) || (rc = ints(x, leader, n)) || (rc = ints(x, join, n)) ||
       (rc = ints(x, picker, n)) || (rc = ints(x, agg, n)))
@@ -820,13 +820,10 @@ int levels_impl(Ctx &x, const DevCsr &fine, int max_levels, int dense_max, int p
     DevCsr a = cur;
     int nc = n0;
     for (int p = 0; p < passes; ++p) {
-      DBuf agg, mptr, mem;
+      DBuf &agg = x.p_agg, &mptr = x.p_mptr, &mem = x.p_mem;
       int m = 0;
       rc = match(x, a, agg, &m);
-      if (!rc && m == a.n) {  // no pair formed: this matrix does not coarsen
-        agg.release();
-        break;
-      }
+      if (!rc && m == a.n) break;  // no pair formed: this matrix does not coarsen
       x.mark("matching", a.n);
       if (!rc) rc = members(x, a.n, m, agg.as<int>(), mptr, mem);
       DevMat &dst = work[wi];
@@ -836,9 +833,6 @@ int levels_impl(Ctx &x, const DevCsr &fine, int max_levels, int dense_max, int p
       if (!rc) k_compose<<<grid_for(n0, c->num_sms), kTPB, 0, c->stream>>>(n0, agg.as<int>(),
                                                                           lv.agg.as<int>());
       if (!rc) rc = cudaStreamSynchronize(c->stream) == cudaSuccess ? FCG_OK : FCG_ERR_CUDA;
-      agg.release();
-      mptr.release();
-      mem.release();
       if (rc) {
         lv.release();
         return rc;
