@@ -206,14 +206,22 @@ __global__ void __launch_bounds__(kTPB, 8)
 // lanes fall in distinct banks) and stores it as 2 KB of contiguous 16-byte writes.
 constexpr int kEmbRow = 40;  // BF16 elements per staged row (32 + 8 padding)
 
-__global__ void __launch_bounds__(kTPB)
+// Four blocks per SM (at most 64 registers): with two, the six feature loads of a cell
+// were not hidden.
+__global__ void __launch_bounds__(kTPB, 4)
     k_lp_embed(int n, const float *__restrict__ r, const float *__restrict__ rms,
                float *__restrict__ feat, const float *__restrict__ prm,
                __nv_bfloat16 *__restrict__ h0, float *__restrict__ z0, const int *done) {
   if (stopped(done)) return;
-  __shared__ float w[C * F + C];
+  // weights of output channels 2p and 2p+1 side by side: w2[p * F + k], biases after them
+  __shared__ float2 w2[C / 2 * F + C / 2];
   __shared__ __align__(16) __nv_bfloat16 tile[kTPB / 32][32 * kEmbRow];
-  for (int t = threadIdx.x; t < C * F + C; t += blockDim.x) w[t] = prm[lp::oWin + t];
+  for (int t = threadIdx.x; t < C / 2 * F; t += blockDim.x) {
+    const int pr = t / F, k = t % F;
+    w2[t] = make_float2(prm[lp::oWin + 2 * pr * F + k], prm[lp::oWin + (2 * pr + 1) * F + k]);
+  }
+  for (int pr = threadIdx.x; pr < C / 2; pr += blockDim.x)
+    w2[C / 2 * F + pr] = make_float2(prm[lp::oWin + C * F + 2 * pr], prm[lp::oWin + C * F + 2 * pr + 1]);
   __syncthreads();
   const float inv = 1.0f / rms[0];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -232,13 +240,17 @@ __global__ void __launch_bounds__(kTPB)
       for (int g = 0; g < C / 8; ++g) {
         __align__(16) __nv_bfloat16 hv[8];
 #pragma unroll
-        for (int o = 0; o < 8; ++o) {
-          const int oc = g * 8 + o;
-          float z = w[C * F + oc];
+        for (int o = 0; o < 4; ++o) {  // channels 2p, 2p+1: z = fma(w, f, z) for k in order
+          const int pr = g * 4 + o;
+          float2 z = w2[C / 2 * F + pr];
 #pragma unroll
-          for (int k = 0; k < F; ++k) z += w[oc * F + k] * f[k];
-          if (z0) z0[i * C + oc] = z;
-          hv[o] = __float2bfloat16(fmaxf(z, 0.f));
+          for (int k = 0; k < F; ++k) z = __ffma2_rn(w2[pr * F + k], make_float2(f[k], f[k]), z);
+          if (z0) {
+            z0[i * C + 2 * pr] = z.x;
+            z0[i * C + 2 * pr + 1] = z.y;
+          }
+          hv[2 * o] = __float2bfloat16(fmaxf(z.x, 0.f));
+          hv[2 * o + 1] = __float2bfloat16(fmaxf(z.y, 0.f));
         }
         *reinterpret_cast<uint4 *>(my + lane * kEmbRow + g * 8) =
             *reinterpret_cast<const uint4 *>(hv);
