@@ -237,7 +237,7 @@ def learned_launches(stats, ml=None):
     + 1 (loop close) + 2 per FP64 residual replacement + final check 1; matrix set-up 4.
     With the coarse-grid correction (ml: levels counting the fine one, sweeps, dense
     coarsest): per solve one Galerkin launch per coarse level, the dense inverse and, for
-    the smoothed first level, the P and A P kernels; per
+    the smoothed first level, the P, transposed-P and A P kernels; per
     iteration the fine residual, restriction and prolongation, per inner level the
     pre-sweeps, residual, restriction, prolongation and post-sweeps, the coarsest solve,
     and the dot products the network's output kernel no longer does."""
@@ -248,7 +248,7 @@ def learned_launches(stats, ml=None):
     coarse = L - 1
     last = 1 if ml["dense"] else 2 * nu + 2
     per_it = 3 + (2 * nu + 3) * (coarse - 1) + last + 1
-    setup = coarse + (1 if ml["dense"] else 0) + (2 if ml["options"]["smoothed"] else 0)
+    setup = coarse + (1 if ml["dense"] else 0) + (3 if ml["options"]["smoothed"] else 0)
     return base + setup + per_it * stats["iters"]
 
 

@@ -769,6 +769,7 @@ int smoothed(Ctx &x, const DevCsr &A, double omega, DevBuiltLevel &lv) {
   if ((rc = acc_rows<GenAP, true>(x, n, ga, lv.ap_ptr, lv.ap_col, &apv, &lv.ap_nnz))) return rc;
   GenPtAP gc{lv.t_ptr.as<int>(), lv.t_row.as<int>(), lv.t_pos.as<int>(), lv.ap_ptr.as<int>(),
              lv.ap_col.as<int>(), pv.as<double>(), apv.as<double>()};
+  x.cap = std::max(x.cap, 128);  // P^T A P rows hold about 45 columns on hex meshes
   lv.A.n = nc;
   if ((rc = acc_rows<GenPtAP, true>(x, nc, gc, lv.A.ptr, lv.A.col, &lv.A.val, &lv.A.nnz)))
     return rc;

@@ -403,15 +403,26 @@ __global__ void __launch_bounds__(kTPB)
   }
 }
 
-// P^T (A P): one warp per coarse row, two coarse entries per lane; the rows holding the
-// aggregate in ascending order, each row's (A P) entries in column order
-__global__ void __launch_bounds__(kTPB)
+// P^T (A P): one warp per coarse row, two coarse entries per lane (entry e of a 64-entry
+// chunk of the row belongs to lane e mod 32); the rows holding the aggregate in ascending
+// order, each row's (A P) entries in column order.  The contributions come 32 at a time,
+// one per lane.  Each lane finds its entry by binary search in the row's columns, the
+// lanes with the same entry are grouped, and the entry's owner adds the group's values in
+// lane order: the same FP32 sums in the same order as adding every contribution in turn.
+constexpr int kA1Warps = kTPB / 32;
+
+__global__ void __launch_bounds__(kTPB, 4)
     k_sa_a1(int nc, const int *__restrict__ cptr, const int *__restrict__ ccol,
             const int *__restrict__ t_ptr, const int *__restrict__ t_row,
-            const int *__restrict__ t_pos, const float *__restrict__ p_val,
+            const float *__restrict__ pt_val,
             const int *__restrict__ ap_ptr, const int *__restrict__ ap_col,
             const float *__restrict__ ap_val, float *__restrict__ a, float *__restrict__ dinv) {
-  const int lane = threadIdx.x & 31;
+  __shared__ unsigned gmask[kA1Warps][64];  // lanes holding a contribution to each entry
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  unsigned *gm = gmask[wib];
+  gm[lane] = 0u;
+  gm[lane + 32] = 0u;
+  __syncwarp();
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   for (long long I = warp; I < nc; I += nwarps) {
@@ -419,7 +430,7 @@ __global__ void __launch_bounds__(kTPB)
     const int mb = t_ptr[I], me = t_ptr[I + 1];
     for (int sb = cb; sb < ce; sb += 64) {  // two coarse entries per lane
       const int my0 = sb + lane, my1 = sb + 32 + lane;
-      const int c0 = my0 < ce ? ccol[my0] : -1, c1 = my1 < ce ? ccol[my1] : -1;
+      const int send = min(sb + 64, ce);
       float acc0 = 0.f, acc1 = 0.f;
       // up to 32 supporting rows at a time, one per lane; their (A P) entries are
       // numbered consecutively (row by row, entries in column order) and taken in full
@@ -431,7 +442,7 @@ __global__ void __launch_bounds__(kTPB)
         float p = 0.f;
         if (m < me) {
           const int i = t_row[m];
-          p = p_val[t_pos[m]];
+          p = pt_val[m];
           st = ap_ptr[i];
           len = ap_ptr[i + 1] - st;
         }
@@ -455,27 +466,49 @@ __global__ void __launch_bounds__(kTPB)
           const int oinc = __shfl_sync(0xffffffffu, inc, src);
           const int olen = __shfl_sync(0xffffffffu, len, src);
           const float op = __shfl_sync(0xffffffffu, p, src);
-          int J = -1;
+          int e = -1;  // entry of this chunk that the contribution adds to
           float v = 0.f;
           if (f < total) {
             const int q = ost + (f - (oinc - olen));
-            J = ap_col[q];
+            const int J = ap_col[q];
             v = __fmul_rn(op, ap_val[q]);
+            int l = sb, h = send - 1;
+            while (l < h) {
+              const int mid = (l + h) >> 1;
+              if (ccol[mid] < J) l = mid + 1;
+              else h = mid;
+            }
+            if (l < send && ccol[l] == J) e = l - sb;
           }
-          const int cnt = min(32, total - fb);
-          for (int e = 0; e < cnt; ++e) {
-            const int Je = __shfl_sync(0xffffffffu, J, e);
-            const float ve = __shfl_sync(0xffffffffu, v, e);
-            if (Je == c0) acc0 = __fadd_rn(acc0, ve);
-            else if (Je == c1) acc1 = __fadd_rn(acc1, ve);
+          const unsigned grp = __match_any_sync(0xffffffffu, e);
+          if (e >= 0 && lane == __ffs(grp) - 1) gm[e] = grp;
+          __syncwarp();
+          unsigned g0 = gm[lane], g1 = gm[lane + 32];
+          while (__any_sync(0xffffffffu, (g0 | g1) != 0u)) {
+            const int s0 = g0 ? __ffs(g0) - 1 : lane, s1 = g1 ? __ffs(g1) - 1 : lane;
+            const float v0 = __shfl_sync(0xffffffffu, v, s0);
+            const float v1 = __shfl_sync(0xffffffffu, v, s1);
+            if (g0) {
+              acc0 = __fadd_rn(acc0, v0);
+              g0 &= g0 - 1;
+            }
+            if (g1) {
+              acc1 = __fadd_rn(acc1, v1);
+              g1 &= g1 - 1;
+            }
           }
+          gm[lane] = 0u;
+          gm[lane + 32] = 0u;
+          __syncwarp();
         }
       }
       if (my0 < ce) {
+        const int c0 = ccol[my0];
         a[my0] = acc0;
         if (c0 == (int)I) dinv[I] = acc0 > 0.f ? 1.f / acc0 : 0.f;
       }
       if (my1 < ce) {
+        const int c1 = ccol[my1];
         a[my1] = acc1;
         if (c1 == (int)I) dinv[I] = acc1 > 0.f ? 1.f / acc1 : 0.f;
       }
@@ -483,15 +516,22 @@ __global__ void __launch_bounds__(kTPB)
   }
 }
 
+// P's values in the order of its transpose lists (once per solve): pt_val[m] = p_val[t_pos[m]]
+__global__ void __launch_bounds__(kTPB)
+    k_sa_pt(long long nnz, const int *__restrict__ t_pos, const float *__restrict__ p_val,
+            float *__restrict__ pt_val) {
+  FCG_GRID_STRIDE(m, nnz) pt_val[m] = p_val[t_pos[m]];
+}
+
 // b1 = P^T t
 __global__ void __launch_bounds__(kTPB)
     k_sa_restrict(int nc, const int *__restrict__ t_ptr, const int *__restrict__ t_row,
-                  const int *__restrict__ t_pos, const float *__restrict__ p_val,
-                  const float *__restrict__ t, float *__restrict__ bc, const int *done) {
+                  const float *__restrict__ pt_val, const float *__restrict__ t,
+                  float *__restrict__ bc, const int *done) {
   if (stopped(done)) return;
   FCG_GRID_STRIDE(I, nc) {
     float acc = 0.f;
-    for (int m = t_ptr[I]; m < t_ptr[I + 1]; ++m) acc += p_val[t_pos[m]] * t[t_row[m]];
+    for (int m = t_ptr[I]; m < t_ptr[I + 1]; ++m) acc += pt_val[m] * t[t_row[m]];
     bc[I] = acc;
   }
 }
@@ -549,8 +589,8 @@ float *enqueue_vcycle(Hierarchy &H, int num_sms, const Options &o, cudaStream_t 
 void fine_restrict(Hierarchy &H, int num_sms, cudaStream_t st, const float *t, const int *done) {
   DevLevel &L1 = H.lv[0];
   if (H.smoothed)
-    k_sa_restrict<<<grid_for(L1.n, num_sms, 8), kTPB, 0, st>>>(L1.n, H.t_ptr, H.t_row, H.t_pos,
-                                                              H.p_val, t, L1.b, done);
+    k_sa_restrict<<<grid_for(L1.n, num_sms, 8), kTPB, 0, st>>>(L1.n, H.t_ptr, H.t_row,
+                                                              H.pt_val, t, L1.b, done);
   else
     k_ml_restrict<<<grid_for(L1.n, num_sms, 8), kTPB, 0, st>>>(L1.n, L1.mptr, L1.mem, t, L1.b,
                                                               done);
@@ -659,7 +699,7 @@ int fill(Hierarchy &H, fcg_context *c, const Options &o, const std::vector<Level
     const int n1 = ls[0].n;
     const size_t ib = pad256(sizeof(int) * (n + 1)) * 2 + pad256(sizeof(int) * H.p_nnz) * 3 +
                       pad256(sizeof(int) * (n1 + 1)) + pad256(sizeof(int) * H.ap_nnz);
-    const size_t vb = pad256(sizeof(float) * H.p_nnz) + pad256(sizeof(float) * H.ap_nnz);
+    const size_t vb = 2 * pad256(sizeof(float) * H.p_nnz) + pad256(sizeof(float) * H.ap_nnz);
     if ((e = H.sa_ints.ensure(ib)) || (e = H.sa_vals.ensure(vb))) {
       err = std::string("hierarchy allocation: ") + cudaGetErrorString(e);
       return FCG_ERR_CUDA;
@@ -674,6 +714,7 @@ int fill(Hierarchy &H, fcg_context *c, const Options &o, const std::vector<Level
     H.ap_col = carve<int>(p, H.ap_nnz);
     p = (char *)H.sa_vals.p;
     H.p_val = carve<float>(p, H.p_nnz);
+    H.pt_val = carve<float>(p, H.p_nnz);
     H.ap_val = carve<float>(p, H.ap_nnz);
     if ((e = cp(H.p_ptr, sm->p_ptr, sizeof(int) * (n + 1))) ||
         (e = cp(H.ap_ptr, sm->ap_ptr, sizeof(int) * (n + 1))) ||
@@ -855,8 +896,9 @@ int values(Hierarchy &H, fcg_context *c, cudaStream_t st) {
                                   (float)H.sa_omega, H.p_val);
       k_sa_ap<<<gn, kTPB, 0, st>>>(c->sv, c->n, scaled32(c), H.p_ptr, H.p_col, H.p_val, H.ap_ptr,
                                    H.ap_col, H.ap_val);
-      k_sa_a1<<<g, kTPB, 0, st>>>(L.n, L.ptr, L.col, H.t_ptr, H.t_row, H.t_pos, H.p_val,
-                                  H.ap_ptr, H.ap_col, H.ap_val, L.a32, L.dinv);
+      k_sa_pt<<<grid_for(H.p_nnz, ns, 8), kTPB, 0, st>>>(H.p_nnz, H.t_pos, H.p_val, H.pt_val);
+      k_sa_a1<<<g, kTPB, 0, st>>>(L.n, L.ptr, L.col, H.t_ptr, H.t_row, H.pt_val, H.ap_ptr,
+                                  H.ap_col, H.ap_val, L.a32, L.dinv);
     } else if (l == 0) {
       k_ml_galerkin0<<<g, kTPB, 0, st>>>(L.n, L.ptr, L.col, L.mptr, L.mem, c->sv, c->n,
                                          scaled32(c), L.agg, L.a32, L.dinv);

@@ -126,7 +126,7 @@ struct Hierarchy {
   DBuf sa_ints, sa_vals;
   int *p_ptr = nullptr, *p_col = nullptr, *t_ptr = nullptr, *t_row = nullptr, *t_pos = nullptr;
   int *ap_ptr = nullptr, *ap_col = nullptr;
-  float *p_val = nullptr, *ap_val = nullptr;
+  float *p_val = nullptr, *pt_val = nullptr, *ap_val = nullptr;  // pt_val: P in t-list order
   long long p_nnz = 0, ap_nnz = 0;
   std::vector<DevLevel> lv;     // levels 1..L (lv[0] is level 1)
   DBuf dense;                   // inverse of the coarsest matrix (row-major)
