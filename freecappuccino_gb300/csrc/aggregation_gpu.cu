@@ -145,14 +145,16 @@ __global__ void k_fine_scale(int n, const int *__restrict__ ptr, const int *__re
 // pick[i]: the row leader i paired with, -1 for a row taken by an earlier leader or a
 // leader left single; leader[i] = 1 for rows that start an aggregate.  ctl = {claim
 // counter, error}.
+constexpr int kTaken = -3;  // decide_blocking: an earlier row took row i
+
 // Row i's decision by waiting in column order (the form for rows with more candidates or
-// pending rows than the two-phase form holds).
+// pending rows than the two-phase form holds): the row it pairs with, -1, or kTaken.
 __device__ int decide_blocking(int i, const int *__restrict__ ptr, const int *__restrict__ col,
                                const double *__restrict__ val, const Chunk &ch) {
   const int k0 = ptr[i], k1 = ptr[i + 1];
   for (int k = k0; k < k1; ++k) {
     const int j = col[k];
-    if (j < i && ch.get(j) == i) return -2 - 1;  // taken
+    if (j < i && ch.get(j) == i) return kTaken;
   }
   int best = -1;
   double bv = 0.0;
@@ -261,7 +263,7 @@ __global__ void __launch_bounds__(kTPB)
     int d = -1;
     if (full) {
       d = decide_blocking(i, ptr, col, val, ch);
-      if (d == -3) d = -1, taken = true;
+      if (d == kTaken) d = -1, taken = true;
     } else {
       for (int q = 0; q < nt && !taken; ++q) taken = ch.get(prow[q]) == i;
       for (int o = 0; o < nc && !taken; ++o) {
