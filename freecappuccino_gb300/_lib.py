@@ -129,6 +129,7 @@ _PROTOS = {
     "fcg_correct_fields": (C.c_int, [_CTX, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_int, _vp,
                                      _vp, _vp, _vp]),
     "fcg_set_sweep_wait_test": (C.c_int, [_CTX, C.c_int, C.c_int]),
+    "fcg_set_aggregation_wait_test": (C.c_int, [_CTX, C.c_int, C.c_int]),
     "fcg_calcuvw": (C.c_int, [_CTX, C.POINTER(UvwParams), C.POINTER(UvwFields), _vp, _vp, _vp,
                               _vp]),
     "fcg_piso_hbya": (C.c_int, [_CTX, C.POINTER(HbyaParams), C.POINTER(HbyaFields), _vp, _vp,

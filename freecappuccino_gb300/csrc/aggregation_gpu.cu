@@ -55,7 +55,8 @@ __device__ __forceinline__ void st_relaxed32(int *p, int v) {
 // has given up), records the failure in *err and returns -1.  A decision changes once,
 // from kUndecided to its value, so a plain (L1-cached) load that sees a value sees the
 // final one; only kUndecided is polled again, at L2.  The polls back off up to about a
-// microsecond apart, so that waiting blocks do not crowd the L2.
+// microsecond apart, so that waiting blocks do not crowd the L2 (a quarter of a
+// microsecond measured slower).
 __device__ int wait_decided(const int *p, int *err, int spin) {
   int v = *p;
   if (v != kUndecided) return v;
@@ -189,7 +190,7 @@ constexpr int kMaxPend = 96;  // earlier rows still undecided when the row start
 __global__ void __launch_bounds__(kTPB)
     k_pm_greedy(int n, const int *__restrict__ ptr, const int *__restrict__ col,
                 const double *__restrict__ val, int *pick, int *__restrict__ leader, int *ctl,
-                int spin) {
+                int spin, int absent) {
   __shared__ int s_base;
   __shared__ int s_pick[kTPB];
   for (;;) {
@@ -276,9 +277,10 @@ __global__ void __launch_bounds__(kTPB)
         }
       }
     }
+    leader[i] = taken ? 0 : 1;
+    if (i == absent) continue;  // diagnostics: this decision is never announced
     ((volatile int *)s_pick)[threadIdx.x] = d;
     st_relaxed32(&pick[i], d);
-    leader[i] = taken ? 0 : 1;
   }
 }
 
@@ -554,6 +556,7 @@ struct Ctx {
   fcg_context *c;
   std::string &err;
   bool trace = false;  // FCG_AGG_TRACE=1: seconds of every stage on stderr
+  bool first_pass = true;
   std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
   void mark(const char *what, long long rows) {
     if (!trace) return;
@@ -642,13 +645,15 @@ int match(Ctx &x, const DevCsr &a, DBuf &agg, int *m) {
   int *ctl = x.ctl.as<int>();
   const int g = grid_for(n, c->num_sms);
   const int gw = std::max(1, std::min((n + kTPB - 1) / kTPB, c->num_sms * 8));
-  const int spin = 1 << 22;
+  const int spin = c->agg_test_polls > 0 ? c->agg_test_polls : 1 << 22;
+  const int absent = x.first_pass ? c->agg_test_row : -1;
+  x.first_pass = false;
   int fail = 0;
   k_fill<<<g, kTPB, 0, c->stream>>>(pick.as<int>(), n, kUndecided);
   k_fill<<<g, kTPB, 0, c->stream>>>(join.as<int>(), n, kUndecided);
   AG_TRY(cudaMemsetAsync(ctl, 0, 2 * sizeof(int), c->stream), "matching");
   k_pm_greedy<<<gw, kTPB, 0, c->stream>>>(n, a.ptr, a.col, a.val, pick.as<int>(),
-                                         leader.as<int>(), ctl, spin);
+                                         leader.as<int>(), ctl, spin, absent);
   AG_TRY(cudaGetLastError(), "matching");
   if ((rc = read_int(x, ctl + 1, &fail))) return rc;
   if (fail) {
@@ -828,11 +833,17 @@ int levels_impl(Ctx &x, const DevCsr &fine, int max_levels, int dense_max, int p
       rc = match(x, a, agg, &m);
       if (!rc && m == a.n) break;  // no pair formed: this matrix does not coarsen
       x.mark("matching", a.n);
-      if (!rc) rc = members(x, a.n, m, agg.as<int>(), mptr, mem);
+      // the last pass of a smoothed first level needs no Galerkin product: that level's
+      // matrix is P^T A P
+      const bool last = p == passes - 1 || m <= dense_max;
+      const bool need_a = !(levels.empty() && sa_omega > 0.0 && last);
       DevMat &dst = work[wi];
-      wi ^= 1;
-      if (!rc) rc = galerkin(x, a, agg.as<int>(), m, mptr.as<int>(), mem.as<int>(), dst);
-      x.mark("galerkin", m);
+      if (need_a) {
+        wi ^= 1;
+        if (!rc) rc = members(x, a.n, m, agg.as<int>(), mptr, mem);
+        if (!rc) rc = galerkin(x, a, agg.as<int>(), m, mptr.as<int>(), mem.as<int>(), dst);
+        x.mark("galerkin", m);
+      }
       if (!rc) k_compose<<<grid_for(n0, c->num_sms), kTPB, 0, c->stream>>>(n0, agg.as<int>(),
                                                                           lv.agg.as<int>());
       if (!rc) rc = cudaStreamSynchronize(c->stream) == cudaSuccess ? FCG_OK : FCG_ERR_CUDA;
@@ -840,7 +851,7 @@ int levels_impl(Ctx &x, const DevCsr &fine, int max_levels, int dense_max, int p
         lv.release();
         return rc;
       }
-      a = dst.view();
+      if (need_a) a = dst.view();
       nc = m;
       if (nc <= dense_max) break;
     }
@@ -903,3 +914,14 @@ int build_levels_device(fcg_context *c, const DevCsr &fine, int max_levels, int 
 
 }  // namespace ml
 }  // namespace fcg
+
+extern "C" int fcg_set_aggregation_wait_test(fcg_context *c, int polls, int absent_row) {
+  if (!c) return FCG_ERR_ARG;
+  if (!c->bound)
+    return fcg::set_error(c, FCG_ERR_STATE, "fcg_set_aggregation_wait_test before fcg_bind_mesh");
+  if (absent_row < 0 || absent_row > c->n)
+    return fcg::set_error(c, FCG_ERR_INDEX, "absent_row out of range");
+  c->agg_test_polls = polls > 0 ? polls : 0;
+  c->agg_test_row = absent_row - 1;
+  return FCG_OK;
+}

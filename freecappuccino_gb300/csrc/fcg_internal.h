@@ -138,6 +138,8 @@ struct fcg_context {
   // and of the boundary faces (calcuvw's boundary loops), planar [BG_COUNT][ncb]
   fcg::DBuf bgeo;
   bool bgeo_ready = false;
+  // diagnostics of the GPU hierarchy build (fcg_set_aggregation_wait_test)
+  int agg_test_polls = 0, agg_test_row = -1;
 
   // per-call staging of host arrays and kernel scratch
   std::vector<fcg::DBuf> stage;

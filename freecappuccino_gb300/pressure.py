@@ -442,6 +442,14 @@ class Context:
         self._check(self.lib.fcg_set_sweep_wait_test(self.h, int(polls), int(absent_row)),
                     "fcg_set_sweep_wait_test")
 
+    def set_aggregation_wait_test(self, polls: int = 0, absent_row: int = 0):
+        """Timeout diagnostics of the GPU build of the learned FCG's coarse hierarchy:
+        every matching wait gives up after `polls` polls and row `absent_row` (1-based) of
+        the first pass never announces its decision, so the build falls back to the host.
+        (0, 0) restores normal runs."""
+        self._check(self.lib.fcg_set_aggregation_wait_test(self.h, int(polls), int(absent_row)),
+                    "fcg_set_aggregation_wait_test")
+
     def profile_sweeps(self, reps: int = 10) -> dict:
         """Mean milliseconds per kernel unit of the last solve's sweep (changes its state)."""
         ms = (C.c_double * 32)()

@@ -398,6 +398,15 @@ int fcg_set_solver_options(fcg_context *ctx, double small, int early_exit);
  * returns FCG_ERR_TIMEOUT with the device still usable.  (0, 0) restores normal runs. */
 int fcg_set_sweep_wait_test(fcg_context *ctx, int polls, int absent_row);
 
+/* Diagnostics for the timeout path of the GPU build of the learned FCG's coarse
+ * hierarchy, whose matching decides every row in one launch with each row waiting on the
+ * decisions it reads: every wait gives up after `polls` polls (<= 0: the default), and
+ * row absent_row (1-based; 0: none) of the first matching pass never announces its
+ * decision, so the waits that read it run out, the GPU build gives up and the hierarchy
+ * is built on the host (fcg_lp_hierarchy_built_on then reports 0).  Read when a
+ * hierarchy is built; (0, 0) restores normal runs. */
+int fcg_set_aggregation_wait_test(fcg_context *ctx, int polls, int absent_row);
+
 /* Per-sweep (resl, rsm) pairs of the last solve -- what the reference prints per
  * sweep when ltest is set (dpcg.f90:141); for fcg_dpcg_mixed one pair per FP64 residual
  * replacement (the true residual).  *count receives the number available; at most

@@ -347,6 +347,36 @@ def test_device_hierarchy_equals_host_hierarchy(name, smoothed):
 
 
 @pytest.mark.gpu
+def test_device_hierarchy_wait_runs_out_and_host_builds():
+    """A matching row that never announces its decision (fcg_set_aggregation_wait_test):
+    the waits that read it give up after their poll bound, the GPU build returns without
+    hanging, the hierarchy is built on the host instead, and the next build runs on the
+    device again with the same arrays."""
+    from freecappuccino_gb300.learned import DEFAULT_WEIGHTS, LearnedPreconditioner
+
+    m, csr, a, su, ctx, lp = _gpu("hex16")
+    lp.close()
+    ctx.set_aggregation_wait_test(polls=4096, absent_row=1)
+    lp = LearnedPreconditioner(path=DEFAULT_WEIGHTS)
+    lp.set_matrix(ctx, a)
+    info_h, lev_h = _levels(lp, ctx)
+    lp.close()
+    assert info_h["built_on"] == "host"
+    ctx.set_aggregation_wait_test(0, 0)
+    lp = LearnedPreconditioner(path=DEFAULT_WEIGHTS)
+    lp.set_matrix(ctx, a)
+    info_d, lev_d = _levels(lp, ctx)
+    assert info_d["built_on"] == "device" and info_d["cells"] == info_h["cells"]
+    for l, (gd, gh) in enumerate(zip(lev_d, lev_h), start=1):
+        for k in ("agg", "mptr", "mem", "ptr", "col", "val"):
+            assert np.array_equal(gd[k], gh[k]), (l, k)
+    r = lp.solve(ctx, a, su, np.zeros(m.numCells), 1e-8, 5000)
+    assert r.converged and not r.fallback
+    ctx.close()
+    lp.close()
+
+
+@pytest.mark.gpu
 def test_device_hierarchy_equals_host_hierarchy_128():
     """The same at 128^3 (jittered, variable diffusivity): every level element for
     element, and the set-up times of both builds."""
