@@ -190,7 +190,7 @@ constexpr int kMaxPend = 96;  // earlier rows still undecided when the row start
 __global__ void __launch_bounds__(kTPB)
     k_pm_greedy(int n, const int *__restrict__ ptr, const int *__restrict__ col,
                 const double *__restrict__ val, int *pick, int *__restrict__ leader, int *ctl,
-                int spin, int absent) {
+                int spin, int absent, bool count_full) {
   __shared__ int s_base;
   __shared__ int s_pick[kTPB];
   for (;;) {
@@ -263,6 +263,7 @@ __global__ void __launch_bounds__(kTPB)
     }
     int d = -1;
     if (full) {
+      if (count_full) atomicAdd(&ctl[2], 1);
       d = decide_blocking(i, ptr, col, val, ch);
       if (d == kTaken) d = -1, taken = true;
     } else {
@@ -652,13 +653,19 @@ int match(Ctx &x, const DevCsr &a, DBuf &agg, int *m) {
   k_fill<<<g, kTPB, 0, c->stream>>>(pick.as<int>(), n, kUndecided);
   k_fill<<<g, kTPB, 0, c->stream>>>(join.as<int>(), n, kUndecided);
   AG_TRY(cudaMemsetAsync(ctl, 0, 2 * sizeof(int), c->stream), "matching");
+  AG_TRY(cudaMemsetAsync(ctl + 2, 0, sizeof(int), c->stream), "matching");
   k_pm_greedy<<<gw, kTPB, 0, c->stream>>>(n, a.ptr, a.col, a.val, pick.as<int>(),
-                                         leader.as<int>(), ctl, spin, absent);
+                                         leader.as<int>(), ctl, spin, absent, x.trace);
   AG_TRY(cudaGetLastError(), "matching");
   if ((rc = read_int(x, ctl + 1, &fail))) return rc;
   if (fail) {
     x.err = "aggregation: a matching wait gave up";
     return FCG_ERR_TIMEOUT;
+  }
+  if (x.trace) {
+    int nfull = 0;
+    if ((rc = read_int(x, ctl + 2, &nfull))) return rc;
+    std::fprintf(stderr, "aggregation: %d of %d rows decided by the blocking form\n", nfull, n);
   }
   AG_TRY(cudaMemsetAsync(ctl, 0, 2 * sizeof(int), c->stream), "matching");
   k_pm_join<<<gw, kTPB, 0, c->stream>>>(n, a.ptr, a.col, a.val, pick.as<int>(), leader.as<int>(),
