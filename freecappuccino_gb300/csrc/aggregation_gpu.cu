@@ -10,10 +10,11 @@
 // launch: blocks claim 256 rows at a time in ascending order and each row waits for the
 // decisions it reads (a value-as-flag wait with an iteration bound, as in the one-launch
 // triangular sweeps), in shared memory for rows of its own block.  A row only waits for
-// rows claimed before it, by blocks that are running, so the waits end.  The second loop (a row left single joins the pair it is
-// most negatively coupled to, as matched, or the pair an earlier single joined) reads the
-// earlier singles' joins the same way.  The pattern must be structurally symmetric, as a
-// mesh's CSR and its Galerkin products are: who may take row i is read from row i.
+// rows claimed before it, by blocks that are running, so the waits end.  The second loop
+// (a row left single joins the pair it is most negatively coupled to, as matched, or the
+// pair an earlier single joined) reads the earlier singles' joins the same way.  The
+// pattern must be structurally symmetric, as a mesh's CSR and its Galerkin products are:
+// who may take row i is read from row i.
 //
 // Galerkin products and the smoothed level.  One thread per output row enumerates the
 // row's contributions in the host's order into an open-addressing table (its own slab of
