@@ -21,13 +21,22 @@ constexpr int kTileStride = 2 * kTileC + 8;  // padded BF16 row of the [h; m] ti
 
 __device__ __forceinline__ float bf(const __nv_bfloat16 v) { return __bfloat162float(v); }
 
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4],
-                                         const unsigned (&b)[2]) {
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4], unsigned b0,
+                                         unsigned b1) {
   asm volatile(
       "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
       "{%8,%9}, {%0,%1,%2,%3};"
       : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Four 8x8 BF16 matrices from shared memory, one 16-byte row address per lane (lanes
+// 8m..8m+7 give the rows of matrix m); register m of each lane gets the lane's pair
+// (row lane/4, columns 2(lane%4), +1) of matrix m: the mma.m16n8k16 fragment layout.
+__device__ __forceinline__ void ldsm_x4(unsigned (&r)[4], const __nv_bfloat16 *p) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"((unsigned)__cvta_generic_to_shared(p)));
 }
 
 // acc[0..7] = fma(v, 8 BF16 values packed in q, acc): one neighbour's term of m = Ahat h
@@ -70,22 +79,21 @@ __device__ __forceinline__ void tile_dense(__nv_bfloat16 *tw, const __nv_bfloat1
   for (int nt = 0; nt < 4; ++nt)
 #pragma unroll
     for (int q = 0; q < 4; ++q) d[nt][q] = 0.f;
+  // fragment rows by ldmatrix: A, matrices (rows 0-7 | 8-15) x (k 0-7 | 8-15) of the
+  // k-step; B, for two n-blocks at a time, (n-block) x (k 0-7 | 8-15) of W_l's rows
+  const int mi = lane >> 3, mr = lane & 7;
+  const __nv_bfloat16 *pa = tw + (mr + 8 * (mi & 1)) * TS + 8 * (mi >> 1);
+  const __nv_bfloat16 *pb = wsm + (8 * (mi >> 1) + mr) * TS + 8 * (mi & 1);
 #pragma unroll
   for (int kb = 0; kb < 4; ++kb) {
-    const int k0 = kb * 16 + tg * 2;
-    unsigned a[4];
-    a[0] = *reinterpret_cast<const unsigned *>(tw + g * TS + k0);
-    a[1] = *reinterpret_cast<const unsigned *>(tw + (g + 8) * TS + k0);
-    a[2] = *reinterpret_cast<const unsigned *>(tw + g * TS + k0 + 8);
-    a[3] = *reinterpret_cast<const unsigned *>(tw + (g + 8) * TS + k0 + 8);
-#pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-      const int oc = nt * 8 + g;  // output channel = column of B = row of W_l
-      unsigned b[2];
-      b[0] = *reinterpret_cast<const unsigned *>(wsm + oc * TS + k0);
-      b[1] = *reinterpret_cast<const unsigned *>(wsm + oc * TS + k0 + 8);
-      mma_bf16(d[nt], a, b);
-    }
+    unsigned a[4], b[4];
+    ldsm_x4(a, pa + kb * 16);
+    ldsm_x4(b, pb + kb * 16);
+    mma_bf16(d[0], a, b[0], b[1]);
+    mma_bf16(d[1], a, b[2], b[3]);
+    ldsm_x4(b, pb + 16 * TS + kb * 16);
+    mma_bf16(d[2], a, b[0], b[1]);
+    mma_bf16(d[3], a, b[2], b[3]);
   }
   __syncwarp();  // every lane has its fragments: the h part of the tile may change
 #pragma unroll
