@@ -286,6 +286,204 @@ __global__ void __launch_bounds__(kTPB)
   }
 }
 
+// --- pair matching in order, for the coarse levels ----------------------------------
+// On a Galerkin level consecutive rows are neighbours, so the decisions above form one
+// chain through almost every row and each row spends its turn rescanning its neighbours'
+// decisions.  There the pass runs as the host's loop itself: k_pm_cands lists every
+// row's candidates in the order the host prefers them (most negative coupling first, the
+// lower column on ties), and k_pm_seq walks the rows in ascending order in one warp with
+// the taken flags of the rows ahead in shared memory.  A row takes the first candidate
+// of its list that no earlier row took, so the decisions are the host's.
+constexpr int kSeqCand = 8;          // candidates of a row kept in order
+constexpr int kSeqRing = 1 << 17;    // taken flags of the rows i .. i + kSeqRing - 1 (bytes)
+constexpr int kSeqMargin = 8;        // candidates lie this far inside the ring
+constexpr int kSeqBatch = 512;       // candidate lists staged per batch
+constexpr int kSeqThreads = 128;     // warp 0 decides, warps 1-3 stage the next batch
+constexpr size_t kSeqSmem = kSeqRing + 2 * kSeqBatch * (kSeqCand + 2) * sizeof(int);
+constexpr int kNoCand = -2;          // an empty slot of a candidate list
+
+// cand[8 i ..]: the first kSeqCand candidates of row i (j > i, a_ij < 0) in order of
+// preference, kNoCand after the last; ncand[i] their number; ctl[3] = the largest j - i.
+__global__ void k_pm_cands(int n, const int *__restrict__ ptr, const int *__restrict__ col,
+                           const double *__restrict__ val, int *__restrict__ cand,
+                           int *__restrict__ ncand, int *ctl) {
+  int far = 0;
+  FCG_GRID_STRIDE(i, n) {
+    double kv[kSeqCand];
+    int kc[kSeqCand];
+#pragma unroll
+    for (int s = 0; s < kSeqCand; ++s) kv[s] = 0.0, kc[s] = kNoCand;
+    int cnt = 0;
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+      const int j = col[k];
+      const double v = val[k];
+      if (j <= (int)i || !(v < 0.0)) continue;
+      ++cnt;
+      far = max(far, j - (int)i);
+      // insertion into the ordered list; an empty slot (value 0) never precedes an entry
+      double cv = v;
+      int cc = j;
+#pragma unroll
+      for (int s = 0; s < kSeqCand; ++s) {
+        const bool first = kc[s] == kNoCand || cv < kv[s] || (cv == kv[s] && cc < kc[s]);
+        const double tv = first ? kv[s] : cv;
+        const int tc = first ? kc[s] : cc;
+        kv[s] = first ? cv : kv[s];
+        kc[s] = first ? cc : kc[s];
+        cv = tv;
+        cc = tc;
+      }
+    }
+    int4 *o = reinterpret_cast<int4 *>(cand + (long long)kSeqCand * i);
+    o[0] = make_int4(kc[0], kc[1], kc[2], kc[3]);
+    o[1] = make_int4(kc[4], kc[5], kc[6], kc[7]);
+    ncand[i] = cnt;
+  }
+  far = __reduce_max_sync(0xffffffffu, far);
+  if ((threadIdx.x & 31) == 0 && far > 0) atomicMax(&ctl[3], far);
+}
+
+// Row i's choice when all of its first kSeqCand candidates are taken and it has more:
+// the whole warp scans the row against the flags (every earlier decision is in them).
+// Not inlined: its row loads must not be hoisted into the decision loop.
+__device__ __noinline__ int seq_scan_row(int i, const int *__restrict__ ptr, const int *__restrict__ col,
+                            const double *__restrict__ val, const unsigned char *ring,
+                            int lane) {
+  double bv = 0.0;
+  int bj = -1;
+  for (int k = ptr[i] + lane; k < ptr[i + 1]; k += 32) {
+    const int j = col[k];
+    const double v = val[k];
+    if (j <= i || !(v < 0.0) || ring[j & (kSeqRing - 1)]) continue;
+    if (bj < 0 || v < bv || (v == bv && j < bj)) bv = v, bj = j;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const double ov = __shfl_xor_sync(0xffffffffu, bv, off);
+    const int oj = __shfl_xor_sync(0xffffffffu, bj, off);
+    if (oj >= 0 && (bj < 0 || ov < bv || (ov == bv && oj < bj))) bv = ov, bj = oj;
+  }
+  return bj;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ unsigned lds_u8(uint32_t a) {
+  unsigned v;
+  asm volatile("ld.shared.u8 %0, [%1];" : "=r"(v) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ int lds_s32(uint32_t a) {
+  int v;
+  asm volatile("ld.shared.s32 %0, [%1];" : "=r"(v) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ void sts_u8_if(bool p, uint32_t a, unsigned v) {
+  asm volatile("{\n .reg .pred q;\n setp.ne.u32 q, %0, 0;\n @q st.shared.u8 [%1], %2;\n}" ::"r"(
+                   (unsigned)p),
+               "r"(a), "r"(v));
+}
+__device__ __forceinline__ void sts_s32_if(bool p, uint32_t a, int v) {
+  asm volatile("{\n .reg .pred q;\n setp.ne.u32 q, %0, 0;\n @q st.shared.s32 [%1], %2;\n}" ::"r"(
+                   (unsigned)p),
+               "r"(a), "r"(v));
+}
+
+// One block.  Batches of kSeqBatch candidate lists are staged in shared memory by warps
+// 1-3 while warp 0 decides the batch before; they also write out the decisions of the
+// batch before that.  The decision loop touches shared memory only.  Warp 0 decides row i
+// with lanes 0-7 on the
+// row's candidate slots and lane 8 on the row itself: each lane reads its taken flag,
+// one ballot gives which are free, and the first free candidate is chosen.  The flags
+// of row i + 1 are read while row i is decided, so they miss only row i's decision,
+// which is compared in.  ring[r mod kSeqRing] is the flag of row r; a decided row
+// clears its own, which then stands for row r + kSeqRing (candidates lie less than
+// kSeqRing - kSeqMargin rows ahead: k_pm_cands checks).  Nothing waits: each row is
+// decided after the rows before it, by the same warp.
+__global__ void __launch_bounds__(kSeqThreads, 1)
+    k_pm_seq(int n, const int *__restrict__ cand, const int *__restrict__ ncand,
+             const int *__restrict__ ptr, const int *__restrict__ col,
+             const double *__restrict__ val, int *__restrict__ pick, int *__restrict__ leader) {
+  extern __shared__ __align__(16) unsigned char seq_smem[];
+  unsigned char *ring = seq_smem;
+  int *buf = reinterpret_cast<int *>(seq_smem + kSeqRing);
+  int *dec = buf + 2 * kSeqBatch * kSeqCand;  // decisions of two batches (kTaken: taken)
+  int *cnb = dec + 2 * kSeqBatch;             // candidate counts of two batches
+  constexpr int M = kSeqRing - 1;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int t = threadIdx.x; t < kSeqRing / 16; t += blockDim.x)
+    reinterpret_cast<uint4 *>(ring)[t] = make_uint4(0, 0, 0, 0);
+  const int nb = (n + kSeqBatch - 1) / kSeqBatch;
+  auto stage = [&](int b, int t0, int nt) {
+    const int r0 = b * kSeqBatch, rows = min(kSeqBatch, n - r0);
+    const int4 *src = reinterpret_cast<const int4 *>(cand + (long long)kSeqCand * r0);
+    int4 *dst = reinterpret_cast<int4 *>(buf + (b & 1) * kSeqBatch * kSeqCand);
+    for (int t = t0; t < 2 * rows; t += nt) dst[t] = src[t];
+    for (int t = t0; t < rows; t += nt) cnb[(b & 1) * kSeqBatch + t] = ncand[r0 + t];
+  };
+  auto flush = [&](int b, int t0, int nt) {
+    const int r0 = b * kSeqBatch, rows = min(kSeqBatch, n - r0);
+    const int *src = dec + (b & 1) * kSeqBatch;
+    for (int t = t0; t < rows; t += nt) {
+      const int v = src[t];
+      pick[r0 + t] = v == kTaken ? -1 : v;
+      leader[r0 + t] = v == kTaken ? 0 : 1;
+    }
+  };
+  if (nb > 0) stage(0, threadIdx.x, blockDim.x);
+  __syncthreads();
+  for (int b = 0; b < nb; ++b) {
+    if (warp != 0) {
+      if (b + 1 < nb) stage(b + 1, threadIdx.x - 32, blockDim.x - 32);
+      if (b > 0) flush(b - 1, threadIdx.x - 32, blockDim.x - 32);
+    } else {
+      const int r0 = b * kSeqBatch, r1 = min(n, r0 + kSeqBatch);
+      const uint32_t ring_s = smem_u32(ring);
+      // this lane's id in a row's list: its candidate slot (lanes 0-7), the row (lane 8);
+      // the two rows after a batch read the staged words that follow it (in bounds of the
+      // shared buffer; their flags are read but never used)
+      const uint32_t cb_s = smem_u32(buf + (b & 1) * kSeqBatch * kSeqCand + lane);
+      const uint32_t db_s = smem_u32(dec + (b & 1) * kSeqBatch);
+      const uint32_t nb_s = smem_u32(cnb + (b & 1) * kSeqBatch);
+      const bool slot = lane < kSeqCand, self = lane == kSeqCand;
+      auto id_of = [&](int r) -> int {
+        return slot ? lds_s32(cb_s + 4u * (uint32_t)((r - r0) * kSeqCand)) : (self ? r : kNoCand);
+      };
+      auto flag_of = [&](int id) -> unsigned {
+        return id >= 0 ? lds_u8(ring_s + ((uint32_t)id & M)) : 0u;
+      };
+      int mine = id_of(r0);
+      unsigned f = flag_of(mine);
+      int mine1 = id_of(r0 + 1);
+      int dprev = -1;  // the flags of row r0 miss no decision
+#pragma unroll 2
+      for (int i = r0; i < r1; ++i) {
+        // flags of row i + 1 (every decision before row i is in the ring), ids of i + 2
+        const unsigned f1 = flag_of(mine1);
+        const int mine2 = id_of(i + 2);
+        const bool t = f != 0u || mine == dprev;
+        const unsigned bal = __ballot_sync(0xffffffffu, slot ? (mine >= 0 && !t) : (self && t));
+        const unsigned fr = bal & 0xffu;
+        const bool taken = (bal >> kSeqCand) & 1u;
+        int d = __shfl_sync(0xffffffffu, mine, (__ffs(fr) - 1) & 31);
+        if (taken || !fr) d = -1;
+        if (!taken && !fr && lds_s32(nb_s + 4u * (uint32_t)(i - r0)) > kSeqCand)
+          d = seq_scan_row(i, ptr, col, val, ring, lane);
+        const bool l0 = lane == 0;
+        sts_u8_if(l0 && d >= 0, ring_s + ((uint32_t)d & M), 1u);
+        sts_u8_if(l0, ring_s + ((uint32_t)i & M), 0u);
+        sts_s32_if(l0, db_s + 4u * (uint32_t)(i - r0), taken ? kTaken : d);
+        __syncwarp();
+        mine = mine1, f = f1, mine1 = mine2;
+        dprev = d;
+      }
+    }
+    __syncthreads();
+  }
+  if (nb > 0) flush(nb - 1, threadIdx.x, blockDim.x);
+}
+
 // join[i] for a leader left single: the row whose aggregate it joins, or -1.  A neighbour
 // j counts as paired when it is in a pair of the first loop, or is an earlier single that
 // joined one.
@@ -571,12 +769,15 @@ struct Ctx {
   DBuf scan_tmp, ctl, cnt;
   DBuf skey, sval, sused;  // accumulation slabs
   DBuf m_pick, m_leader, m_join, m_picker, m_lrank, m_used, m_id;  // matching scratch
+  DBuf m_cand, m_ncand;  // candidate lists of the in-order form
+  bool seq_on = true;    // FCG_AGG_SEQ=0: the coarse levels match with the chained form too
   DBuf p_agg, p_mptr, p_mem;  // one pass's aggregates and members
   int cap = 64;
   long long slab_threads = 0;
   void release() {
     for (DBuf *b : {&scan_tmp, &ctl, &cnt, &skey, &sval, &sused, &m_pick, &m_leader, &m_join,
-                    &m_picker, &m_lrank, &m_used, &m_id, &p_agg, &p_mptr, &p_mem})
+                    &m_picker, &m_lrank, &m_used, &m_id, &m_cand, &m_ncand, &p_agg, &p_mptr,
+                    &p_mem})
       b->release();
   }
 };
@@ -633,8 +834,33 @@ int members(Ctx &x, int n, int m, const int *agg, DBuf &mptr, DBuf &mem) {
   return FCG_OK;
 }
 
+// The in-order form of one pass (pick, leader as k_pm_greedy gives them); *done = false
+// when a candidate lies beyond the flag ring (the caller then runs the chained form).
+int match_in_order(Ctx &x, const DevCsr &a, int *pick, int *leader, bool *done) {
+  fcg_context *c = x.c;
+  const int n = a.n;
+  int *ctl = x.ctl.as<int>();
+  int rc, far = 0;
+  *done = false;
+  if ((rc = ints(x, x.m_cand, (long long)kSeqCand * n)) || (rc = ints(x, x.m_ncand, n))) return rc;
+  AG_TRY(cudaMemsetAsync(ctl + 3, 0, sizeof(int), c->stream), "matching");
+  k_pm_cands<<<grid_for(n, c->num_sms), kTPB, 0, c->stream>>>(
+      n, a.ptr, a.col, a.val, x.m_cand.as<int>(), x.m_ncand.as<int>(), ctl);
+  AG_TRY(cudaGetLastError(), "matching");
+  if ((rc = read_int(x, ctl + 3, &far))) return rc;
+  if (far >= kSeqRing - kSeqMargin) return FCG_OK;
+  AG_TRY(cudaFuncSetAttribute(k_pm_seq, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)kSeqSmem), "matching");
+  k_pm_seq<<<1, kSeqThreads, kSeqSmem, c->stream>>>(n, x.m_cand.as<int>(), x.m_ncand.as<int>(),
+                                                   a.ptr, a.col, a.val, pick, leader);
+  AG_TRY(cudaGetLastError(), "matching");
+  *done = true;
+  return FCG_OK;
+}
+
 // One pass of pairwise matching on a; agg (a.n) gets the aggregates, *m their count.
-int match(Ctx &x, const DevCsr &a, DBuf &agg, int *m) {
+// in_order: decide the pairs with the in-order form (coarse levels), else the chained one.
+int match(Ctx &x, const DevCsr &a, DBuf &agg, int *m, bool in_order) {
   fcg_context *c = x.c;
   const int n = a.n;
   // scratch kept across passes (the first pass is the largest)
@@ -651,22 +877,30 @@ int match(Ctx &x, const DevCsr &a, DBuf &agg, int *m) {
   const int absent = x.first_pass ? c->agg_test_row : -1;
   x.first_pass = false;
   int fail = 0;
-  k_fill<<<g, kTPB, 0, c->stream>>>(pick.as<int>(), n, kUndecided);
+  bool done = false;
   k_fill<<<g, kTPB, 0, c->stream>>>(join.as<int>(), n, kUndecided);
-  AG_TRY(cudaMemsetAsync(ctl, 0, 2 * sizeof(int), c->stream), "matching");
-  AG_TRY(cudaMemsetAsync(ctl + 2, 0, sizeof(int), c->stream), "matching");
-  k_pm_greedy<<<gw, kTPB, 0, c->stream>>>(n, a.ptr, a.col, a.val, pick.as<int>(),
-                                         leader.as<int>(), ctl, spin, absent, x.trace);
-  AG_TRY(cudaGetLastError(), "matching");
-  if ((rc = read_int(x, ctl + 1, &fail))) return rc;
-  if (fail) {
-    x.err = "aggregation: a matching wait gave up";
-    return FCG_ERR_TIMEOUT;
-  }
-  if (x.trace) {
-    int nfull = 0;
-    if ((rc = read_int(x, ctl + 2, &nfull))) return rc;
-    std::fprintf(stderr, "aggregation: %d of %d rows decided by the blocking form\n", nfull, n);
+  if (in_order && absent < 0 && x.seq_on &&
+      (rc = match_in_order(x, a, pick.as<int>(), leader.as<int>(), &done)))
+    return rc;
+  if (done) {
+    if (x.trace) std::fprintf(stderr, "aggregation: %d rows decided in order\n", n);
+  } else {
+    k_fill<<<g, kTPB, 0, c->stream>>>(pick.as<int>(), n, kUndecided);
+    AG_TRY(cudaMemsetAsync(ctl, 0, 2 * sizeof(int), c->stream), "matching");
+    AG_TRY(cudaMemsetAsync(ctl + 2, 0, sizeof(int), c->stream), "matching");
+    k_pm_greedy<<<gw, kTPB, 0, c->stream>>>(n, a.ptr, a.col, a.val, pick.as<int>(),
+                                           leader.as<int>(), ctl, spin, absent, x.trace);
+    AG_TRY(cudaGetLastError(), "matching");
+    if ((rc = read_int(x, ctl + 1, &fail))) return rc;
+    if (fail) {
+      x.err = "aggregation: a matching wait gave up";
+      return FCG_ERR_TIMEOUT;
+    }
+    if (x.trace) {
+      int nfull = 0;
+      if ((rc = read_int(x, ctl + 2, &nfull))) return rc;
+      std::fprintf(stderr, "aggregation: %d of %d rows decided by the blocking form\n", nfull, n);
+    }
   }
   AG_TRY(cudaMemsetAsync(ctl, 0, 2 * sizeof(int), c->stream), "matching");
   k_pm_join<<<gw, kTPB, 0, c->stream>>>(n, a.ptr, a.col, a.val, pick.as<int>(), leader.as<int>(),
@@ -838,7 +1072,7 @@ int levels_impl(Ctx &x, const DevCsr &fine, int max_levels, int dense_max, int p
     for (int p = 0; p < passes; ++p) {
       DBuf &agg = x.p_agg, &mptr = x.p_mptr, &mem = x.p_mem;
       int m = 0;
-      rc = match(x, a, agg, &m);
+      rc = match(x, a, agg, &m, !levels.empty());
       if (!rc && m == a.n) break;  // no pair formed: this matrix does not coarsen
       x.mark("matching", a.n);
       // the last pass of a smoothed first level needs no Galerkin product: that level's
@@ -910,6 +1144,8 @@ int build_levels_device(fcg_context *c, const DevCsr &fine, int max_levels, int 
   Ctx x{c, err};
   const char *tr = std::getenv("FCG_AGG_TRACE");
   x.trace = tr && tr[0] == '1';
+  const char *sq = std::getenv("FCG_AGG_SEQ");
+  x.seq_on = !(sq && sq[0] == '0');
   levels.clear();
   const int rc = levels_impl(x, fine, max_levels, dense_max, passes, sa_omega, levels);
   x.release();

@@ -347,6 +347,42 @@ def test_device_hierarchy_equals_host_hierarchy(name, smoothed):
 
 
 @pytest.mark.gpu
+def test_device_hierarchy_in_order_form(monkeypatch, capfd):
+    """The coarse levels' passes run in the in-order form (k_pm_cands, k_pm_seq), the fine
+    level's in the chained form, and the in-order form's levels equal those of the
+    chained form everywhere (FCG_AGG_SEQ=0) element for element."""
+    from freecappuccino_gb300.learned import DEFAULT_WEIGHTS, LearnedPreconditioner
+
+    m = mesh_by_name("hex32")
+    csr, a, su = _system(m, True)
+    ctx = fcg.Context(m)
+    out = []
+    for seq in ("1", "0"):
+        monkeypatch.setenv("FCG_AGG_SEQ", seq)
+        monkeypatch.setenv("FCG_AGG_TRACE", "1")
+        capfd.readouterr()
+        lp = LearnedPreconditioner(path=DEFAULT_WEIGHTS)
+        lp.set_matrix(ctx, a)
+        out.append(_levels(lp, ctx))
+        lp.close()
+        err = capfd.readouterr().err
+        in_order = [ln for ln in err.splitlines() if "decided in order" in ln]
+        chained = [ln for ln in err.splitlines() if "by the blocking form" in ln]
+        if seq == "1":
+            # three passes on the fine matrix chained, every later pass in order
+            assert len(chained) == 3 and len(in_order) >= 3, err
+        else:
+            assert not in_order and len(chained) >= 6, err
+    (info_s, lev_s), (info_c, lev_c) = out
+    assert info_s["built_on"] == "device" and info_c["built_on"] == "device"
+    assert info_s["cells"] == info_c["cells"] and info_s["entries"] == info_c["entries"]
+    for l, (gs, gc) in enumerate(zip(lev_s, lev_c), start=1):
+        for k in ("agg", "mptr", "mem", "ptr", "col", "val"):
+            assert np.array_equal(gs[k], gc[k]), (l, k)
+    ctx.close()
+
+
+@pytest.mark.gpu
 def test_device_hierarchy_wait_runs_out_and_host_builds():
     """A matching row that never announces its decision (fcg_set_aggregation_wait_test):
     the waits that read it give up after their poll bound, the GPU build returns without
