@@ -379,6 +379,13 @@ __device__ __forceinline__ int lds_s32(uint32_t a) {
   asm volatile("ld.shared.s32 %0, [%1];" : "=r"(v) : "r"(a));
   return v;
 }
+__device__ __forceinline__ int4 lds_v4(uint32_t a) {
+  int4 v;
+  asm volatile("ld.shared.v4.s32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "r"(a));
+  return v;
+}
 __device__ __forceinline__ void sts_u8_if(bool p, uint32_t a, unsigned v) {
   asm volatile("{\n .reg .pred q;\n setp.ne.u32 q, %0, 0;\n @q st.shared.u8 [%1], %2;\n}" ::"r"(
                    (unsigned)p),
@@ -443,7 +450,8 @@ __global__ void __launch_bounds__(kSeqThreads, 1)
       // this lane's id in a row's list: its candidate slot (lanes 0-7), the row (lane 8);
       // the two rows after a batch read the staged words that follow it (in bounds of the
       // shared buffer; their flags are read but never used)
-      const uint32_t cb_s = smem_u32(buf + (b & 1) * kSeqBatch * kSeqCand + lane);
+      const int *cb = buf + (b & 1) * kSeqBatch * kSeqCand;
+      const uint32_t cb_s = smem_u32(cb + lane);
       const uint32_t db_s = smem_u32(dec + (b & 1) * kSeqBatch);
       const uint32_t nb_s = smem_u32(cnb + (b & 1) * kSeqBatch);
       const bool slot = lane < kSeqCand, self = lane == kSeqCand;
@@ -453,30 +461,68 @@ __global__ void __launch_bounds__(kSeqThreads, 1)
       auto flag_of = [&](int id) -> unsigned {
         return id >= 0 ? lds_u8(ring_s + ((uint32_t)id & M)) : 0u;
       };
+      // a row's whole list in every lane
+      const uint32_t cl_s = smem_u32(cb);
+      auto list_of = [&](int r, int4 &lo, int4 &hi) {
+        const uint32_t a = cl_s + 4u * (uint32_t)((r - r0) * kSeqCand);
+        lo = lds_v4(a);
+        hi = lds_v4(a + 16u);
+      };
+      // the slots of a list that hold id (bit k for slot k)
+      auto eq_of = [](int id, const int4 &lo, const int4 &hi) -> unsigned {
+        return (lo.x == id ? 1u : 0u) | (lo.y == id ? 2u : 0u) | (lo.z == id ? 4u : 0u) |
+               (lo.w == id ? 8u : 0u) | (hi.x == id ? 16u : 0u) | (hi.y == id ? 32u : 0u) |
+               (hi.z == id ? 64u : 0u) | (hi.w == id ? 128u : 0u);
+      };
+      int4 lo, hi;
+      list_of(r0, lo, hi);
       int mine = id_of(r0);
       unsigned f = flag_of(mine);
       int mine1 = id_of(r0 + 1);
-      int dprev = -1;  // the flags of row r0 miss no decision
+      unsigned eq = 0, selp = 0;  // row r0's flags miss no decision
+      // Row i is decided from its flags, read after every decision up to row i - 2 was
+      // stored, and from row i - 1's choice: a lane's id is taken if its flag is set or
+      // if it is the candidate row i - 1 chose (its slot bit selp, against eq, the slots
+      // of row i - 1 that hold the id).  The chosen slot's own lane then flags and
+      // records it, so no lane waits for the choice to be broadcast.
 #pragma unroll 2
       for (int i = r0; i < r1; ++i) {
-        // flags of row i + 1 (every decision before row i is in the ring), ids of i + 2
+        // flags of row i + 1 (every decision before row i is in the ring), its eq against
+        // row i, the ids of row i + 2 and the list of row i + 1
         const unsigned f1 = flag_of(mine1);
+        const unsigned eq1 = eq_of(mine1, lo, hi);
         const int mine2 = id_of(i + 2);
-        const bool t = f != 0u || mine == dprev;
+        int4 lo1, hi1;
+        list_of(i + 1, lo1, hi1);
+        const bool t = f != 0u || (eq & selp) != 0u;
         const unsigned bal = __ballot_sync(0xffffffffu, slot ? (mine >= 0 && !t) : (self && t));
         const unsigned fr = bal & 0xffu;
         const bool taken = (bal >> kSeqCand) & 1u;
-        int d = __shfl_sync(0xffffffffu, mine, (__ffs(fr) - 1) & 31);
-        if (taken || !fr) d = -1;
-        if (!taken && !fr && lds_s32(nb_s + 4u * (uint32_t)(i - r0)) > kSeqCand)
-          d = seq_scan_row(i, ptr, col, val, ring, lane);
-        const bool l0 = lane == 0;
-        sts_u8_if(l0 && d >= 0, ring_s + ((uint32_t)d & M), 1u);
-        sts_u8_if(l0, ring_s + ((uint32_t)i & M), 0u);
-        sts_s32_if(l0, db_s + 4u * (uint32_t)(i - r0), taken ? kTaken : d);
+        const unsigned sel = taken ? 0u : (fr & (0u - fr));
+        // the chosen slot's lane flags its candidate and records it; the row's lane
+        // clears the row's flag (it now stands for row i + kSeqRing) and records a row
+        // left single or taken
+        const bool chosen = slot && ((sel >> lane) & 1u);
+        const uint32_t da = db_s + 4u * (uint32_t)(i - r0);
+        sts_u8_if(chosen, ring_s + ((uint32_t)mine & M), 1u);
+        sts_s32_if(chosen, da, mine);
+        sts_s32_if(self && sel == 0u, da, taken ? kTaken : -1);
+        sts_u8_if(self, ring_s + ((uint32_t)i & M), 0u);
+        unsigned f1c = f1;
+        if (!taken && fr == 0u && lds_s32(nb_s + 4u * (uint32_t)(i - r0)) > kSeqCand) {
+          // every listed candidate taken: scan the row; row i + 1 then rereads its flags,
+          // which hold every decision up to this one (selp stays 0)
+          __syncwarp();
+          const int d = seq_scan_row(i, ptr, col, val, ring, lane);
+          sts_u8_if(lane == 0 && d >= 0, ring_s + ((uint32_t)d & M), 1u);
+          sts_s32_if(lane == 0, da, d);
+          __syncwarp();
+          f1c = flag_of(mine1);
+        }
         __syncwarp();
-        mine = mine1, f = f1, mine1 = mine2;
-        dprev = d;
+        lo = lo1, hi = hi1, mine = mine1, f = f1c, eq = eq1;
+        mine1 = mine2;
+        selp = sel;
       }
     }
     __syncthreads();
