@@ -14,7 +14,10 @@
 // (a row left single joins the pair it is most negatively coupled to, as matched, or the
 // pair an earlier single joined) reads the earlier singles' joins the same way.  The
 // pattern must be structurally symmetric, as a mesh's CSR and its Galerkin products are:
-// who may take row i is read from row i.
+// who may take row i is read from row i.  That chained form serves the fine level, whose
+// chains are short; the passes on a coarse level, where consecutive rows are neighbours
+// and the chain runs through almost every row, walk the rows in order in one warp
+// (k_pm_cands, k_pm_seq below).
 //
 // Galerkin products and the smoothed level.  One thread per output row enumerates the
 // row's contributions in the host's order into an open-addressing table (its own slab of
