@@ -44,6 +44,7 @@ class MeshDesc(C.Structure):
         ("owner", _vp), ("neighbour", _vp),
         ("arx", _vp), ("ary", _vp), ("arz", _vp), ("xf", _vp), ("yf", _vp), ("zf", _vp),
         ("xc", _vp), ("yc", _vp), ("zc", _vp), ("vol", _vp), ("facint", _vp),
+        ("ncyc", C.c_int), ("iOCFacesStart", C.c_int), ("ijlFace", _vp), ("ijrFace", _vp),
     ]
 
 

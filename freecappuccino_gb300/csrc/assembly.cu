@@ -86,6 +86,43 @@ __global__ void k_bnd_geo(MeshView m, long long ncb, double *__restrict__ b) {
   }
 }
 
+// foc and srdoc of the O-C and cyclic pairs (mesh_geometry_and_topology.f90:1083-1152):
+// the distances of the left cell's centre to its face (djn) and of the right cell's
+// centre to the friend face (dpn); a cyclic pair takes foc = 1/2 (:1149).
+__global__ void k_oc_geo(MeshView m, double *__restrict__ foc, double *__restrict__ srdoc) {
+  const int nreg = m.noc - m.ncyc;
+  FCG_GRID_STRIDE(i, m.noc) {
+    const int f = m.oc_fl[i], g = m.oc_fr[i], p = m.oc_l[i], q = m.oc_r[i];
+    double xpn = m.xc[q] - m.xf[g], ypn = m.yc[q] - m.yf[g], zpn = m.zc[q] - m.zf[g];
+    const double dpn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
+    xpn = m.xf[f] - m.xc[p];
+    ypn = m.yf[f] - m.yc[p];
+    zpn = m.zf[f] - m.zc[p];
+    const double djn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
+    foc[i] = (int)i < nreg ? djn / (djn + dpn) : 0.5;
+    const double are = sqrt(m.arx[f] * m.arx[f] + m.ary[f] * m.ary[f] + m.arz[f] * m.arz[f]);
+    srdoc[i] = are / (djn + dpn);
+  }
+}
+
+}  // namespace
+
+int fcg::oc_geometry(fcg_context *c) {
+  MeshView &m = c->mv;
+  c->bound_allocs.emplace_back();
+  DBuf &b = c->bound_allocs.back();
+  FCG_CUDA_TRY(c, b.ensure(2 * sizeof(double) * (size_t)m.noc));
+  double *foc = b.as<double>(), *srdoc = foc + m.noc;
+  k_oc_geo<<<grid_for(m.noc, c->num_sms), kTPB, 0, c->stream>>>(m, foc, srdoc);
+  FCG_CHECK_LAUNCH(c, "k_oc_geo");
+  FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  m.oc_foc = foc;
+  m.oc_srdoc = srdoc;
+  return FCG_OK;
+}
+
+namespace {
+
 // ---------------------------------------------------------------------------
 // laplacian(mu,phi)
 // ---------------------------------------------------------------------------
@@ -103,12 +140,30 @@ __global__ void k_lap_faces(MeshView m, const double *__restrict__ g, const doub
   }
 }
 
+// The O-C pairs (:67-86): facefluxlaplacian(ijl, ijr, area of face iOCFacesStart + i,
+// foc(i), mu, al(i), ar(i)), ar and al stored after the CSR values of a.
+__global__ void k_lap_oc(MeshView m, const double *__restrict__ mu, double *__restrict__ a) {
+  FCG_GRID_STRIDE(i, m.noc) {
+    const int p = m.oc_l[i], q = m.oc_r[i], f = m.oc_start + (int)i;
+    const double arx = m.arx[f], ary = m.ary[f], arz = m.arz[f];
+    const double fxn = m.oc_foc[i];
+    const double fxp = 1.0 - fxn;
+    const double xpn = m.xc[q] - m.xc[p], ypn = m.yc[q] - m.yc[p], zpn = m.zc[q] - m.zc[p];
+    const double smdpn = (arx * arx + ary * ary + arz * arz) / (arx * xpn + ary * ypn + arz * zpn);
+    const double cap = (fxp * mu[p] + fxn * mu[q]) * smdpn;
+    a[m.nnz + i] = cap;          // ar(i) = can
+    a[m.nnz + m.noc + i] = cap;  // al(i) = cap
+  }
+}
+
 __global__ void k_lap_cells(MeshView m, const double *__restrict__ mu,
                             const double *__restrict__ phi, double *__restrict__ a,
                             double *__restrict__ su) {
   FCG_GRID_STRIDE(c, m.n) {
     double acc = 0.0;  // a = 0 (:33), then a(diag) -= can/cap in face order (:58-63)
     for (int e = m.cf_ptr[c]; e < m.cf_ptr[c + 1]; ++e) acc = acc - a[m.cf_slot[e]];
+    if (m.noc)  // then ar / al of the cell's O-C pairs in pair order (:79-84)
+      for (int e = m.oc_cptr[c]; e < m.oc_cptr[c + 1]; ++e) acc = acc - a[m.nnz + m.oc_vix[e]];
     double s = su[c];
     for (int e = m.cb_ptr[c]; e < m.cb_ptr[c + 1]; ++e) {  // wall faces :140-154
       if (m.cb_type[e] != B_WALL) continue;
@@ -313,7 +368,8 @@ extern "C" int fcg_laplacian(fcg_context *c, const double *mu, const double *phi
   int rc;
   if ((rc = stage_in(c, mu, sizeof(double) * c->n, 0, true, &dmu, &hmu))) return rc;
   if ((rc = stage_in(c, phi, sizeof(double) * c->ntot, 1, true, &dphi, &hphi))) return rc;
-  if ((rc = stage_in(c, a, sizeof(double) * c->nnz, 2, false, &da, &ha))) return rc;
+  const size_t alen = sizeof(double) * (size_t)a_len(c);
+  if ((rc = stage_in(c, a, alen, 2, false, &da, &ha))) return rc;
   if ((rc = stage_in(c, su, sizeof(double) * c->n, 3, true, &dsu, &hsu))) return rc;
   const MeshView &m = c->mv;
   const double *g;
@@ -323,10 +379,15 @@ extern "C" int fcg_laplacian(fcg_context *c, const double *mu, const double *phi
                                                                         (double *)da);
     FCG_CHECK_LAUNCH(c, "k_lap_faces");
   }
+  if (m.noc > 0) {
+    k_lap_oc<<<grid_for(m.noc, c->num_sms), kTPB, 0, c->stream>>>(m, (const double *)dmu,
+                                                                     (double *)da);
+    FCG_CHECK_LAUNCH(c, "k_lap_oc");
+  }
   k_lap_cells<<<grid_for(m.n, c->num_sms), kTPB, 0, c->stream>>>(
       m, (const double *)dmu, (const double *)dphi, (double *)da, (double *)dsu);
   FCG_CHECK_LAUNCH(c, "k_lap_cells");
-  if ((rc = stage_out(c, a, da, sizeof(double) * c->nnz, ha))) return rc;
+  if ((rc = stage_out(c, a, da, alen, ha))) return rc;
   if ((rc = stage_out(c, su, dsu, sizeof(double) * c->n, hsu))) return rc;
   if (ha || hsu) FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return FCG_OK;
@@ -336,6 +397,7 @@ extern "C" int fcg_facefluxmass(fcg_context *c, const fcg_flow_fields *f, double
                                 double *flmass) {
   if (!c || !f) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_facefluxmass before fcg_bind_mesh");
+  if (c->mv.noc) return refuse_oc(c, "fcg_facefluxmass");
   FCG_CUDA_TRY(c, cudaSetDevice(c->device));
   const size_t nt = sizeof(double) * c->ntot, n1 = sizeof(double) * c->n, n3 = 3 * n1;
   const double *src[12] = {f->u, f->v, f->w, f->p, f->dUdxi, f->dVdxi, f->dWdxi, f->dPdxi,
@@ -378,6 +440,7 @@ extern "C" int fcg_facefluxmass_piso(fcg_context *c, const fcg_flow_fields *f, d
                                      double *su, double *flmass) {
   if (!c || !f) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_facefluxmass_piso before fcg_bind_mesh");
+  if (c->mv.noc) return refuse_oc(c, "fcg_facefluxmass_piso");
   FCG_CUDA_TRY(c, cudaSetDevice(c->device));
   const size_t nt = sizeof(double) * c->ntot, n1 = sizeof(double) * c->n, n3 = 3 * n1;
   // the fields facefluxmass_piso reads (facefluxmass.f90:300-302)
@@ -420,6 +483,7 @@ extern "C" int fcg_fluxmc(fcg_context *c, const double *dPdxi, const double *apu
                           const double *den, double *su, double *flmass) {
   if (!c) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_fluxmc before fcg_bind_mesh");
+  if (c->mv.noc) return refuse_oc(c, "fcg_fluxmc");
   FCG_CUDA_TRY(c, cudaSetDevice(c->device));
   void *dP, *dapu, *dden, *dsu, *dfm;
   bool h0, h1, h2, hsu, hfm;
@@ -614,6 +678,7 @@ extern "C" int fcg_correct_bc_velocity(fcg_context *c, const double *den, double
                                        double *u, double *v, double *w, double *fmo) {
   if (!c) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_correct_bc_velocity before fcg_bind_mesh");
+  if (c->mv.noc) return refuse_oc(c, "fcg_correct_bc_velocity");
   if (!den || !u || !v || !w || (!fmo && c->cnt[B_OUTLET] > 0))
     return set_error(c, FCG_ERR_ARG, "NULL array");
   FCG_CUDA_TRY(c, cudaSetDevice(c->device));
@@ -649,6 +714,7 @@ extern "C" int fcg_continuity_errors(fcg_context *c, const double *flmass, const
                                      double *global) {
   if (!c) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_continuity_errors before fcg_bind_mesh");
+  if (c->mv.noc) return refuse_oc(c, "fcg_continuity_errors");
   if (!flmass || (!fmi && c->cnt[B_INLET] > 0) || (!fmo && c->cnt[B_OUTLET] > 0))
     return set_error(c, FCG_ERR_ARG, "NULL array");
   if (c->n > c->nin)
@@ -691,6 +757,7 @@ extern "C" int fcg_flux_correct(fcg_context *c, const double *a, const double *p
                                 double *flmass) {
   if (!c) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_flux_correct before fcg_bind_mesh");
+  if (c->mv.noc) return refuse_oc(c, "fcg_flux_correct");
   if (!a || !pp || !flmass) return set_error(c, FCG_ERR_ARG, "NULL a, pp or flmass");
   FCG_CUDA_TRY(c, cudaSetDevice(c->device));
   void *da, *dpp, *dfm;
@@ -716,6 +783,7 @@ extern "C" int fcg_correct_fields(fcg_context *c, const double *dPdxi, const dou
                                   double *p) {
   if (!c) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_correct_fields before fcg_bind_mesh");
+  if (c->mv.noc) return refuse_oc(c, "fcg_correct_fields");
   if (!dPdxi || !apu || !apv || !apw || !pp || !u || !v || !w || !p)
     return set_error(c, FCG_ERR_ARG, "NULL array");
   if (pRefCell < 1 || pRefCell > c->n) return set_error(c, FCG_ERR_INDEX, "pRefCell out of range");

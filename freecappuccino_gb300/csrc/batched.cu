@@ -485,6 +485,7 @@ extern "C" int fcg_batch_create(fcg_context *const *ctxs, int nsys, fcg_batch **
   std::set<fcg_context *> seen;
   for (int k = 0; k < nsys; ++k) {
     if (!ctxs[k] || !ctxs[k]->bound || ctxs[k]->device != ctxs[0]->device) return FCG_ERR_ARG;
+    if (ctxs[k]->mv.noc) return FCG_ERR_UNSUPPORTED;  // O-C grid cuts: one system at a time
     if (!seen.insert(ctxs[k]).second) return FCG_ERR_ARG;  // systems share solver vectors
   }
   if (cudaSetDevice(ctxs[0]->device) != cudaSuccess) return FCG_ERR_CUDA;

@@ -104,6 +104,57 @@ static int upload_any(fcg_context *c, const T *user, size_t count, const T **out
   return FCG_OK;
 }
 
+// The O-C pairs of a mesh (mesh_geometry_and_topology.f90:800-845): the two cells of
+// every pair from the owners of its faces, every cell's pair entries in pair order (the
+// left cell's before the right cell's within a pair, as the reference's loops update
+// ijl(i) before ijr(i)), and foc / srdoc computed on the device (oc_geometry).
+static int bind_oc(fcg_context *c, const fcg_mesh_desc &m, const std::vector<int> &own) {
+  const int noc = m.noc, n = m.numCells;
+  std::vector<int> fl, fr;
+  int rc;
+  if ((rc = host_copy(c, m.ijlFace, (size_t)noc, fl)) || (rc = host_copy(c, m.ijrFace, (size_t)noc, fr)))
+    return rc;
+  std::vector<int> l(noc), r(noc);
+  for (int i = 0; i < noc; ++i) {
+    if (fl[i] <= m.numInnerFaces || fl[i] > m.numFaces || fr[i] <= m.numInnerFaces ||
+        fr[i] > m.numFaces)
+      return set_error(c, FCG_ERR_INDEX, "an O-C pair names a face that is not a boundary face");
+    fl[i] -= 1;
+    fr[i] -= 1;
+    l[i] = own[fl[i]] - 1;
+    r[i] = own[fr[i]] - 1;
+    if (l[i] == r[i]) return set_error(c, FCG_ERR_INDEX, "an O-C pair couples a cell to itself");
+  }
+  std::vector<int> ptr((size_t)n + 1, 0), col(2 * (size_t)noc), vix(2 * (size_t)noc);
+  for (int i = 0; i < noc; ++i) {
+    ++ptr[(size_t)l[i] + 1];
+    ++ptr[(size_t)r[i] + 1];
+  }
+  for (int k = 0; k < n; ++k) ptr[(size_t)k + 1] += ptr[k];
+  std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+  for (int i = 0; i < noc; ++i) {
+    int e = fill[l[i]]++;  // row ijl(i): ar(i) * x(ijr(i))
+    col[e] = r[i];
+    vix[e] = i;
+    e = fill[r[i]]++;  // row ijr(i): al(i) * x(ijl(i))
+    col[e] = l[i];
+    vix[e] = noc + i;
+  }
+  MeshView &v = c->mv;
+  if ((rc = upload(c, l.data(), (size_t)noc, &v.oc_l)) ||
+      (rc = upload(c, r.data(), (size_t)noc, &v.oc_r)) ||
+      (rc = upload(c, fl.data(), (size_t)noc, &v.oc_fl)) ||
+      (rc = upload(c, fr.data(), (size_t)noc, &v.oc_fr)) ||
+      (rc = upload(c, ptr.data(), ptr.size(), &v.oc_cptr)) ||
+      (rc = upload(c, col.data(), col.size(), &v.oc_col)) ||
+      (rc = upload(c, vix.data(), vix.size(), &v.oc_vix)))
+    return rc;
+  v.noc = noc;
+  v.ncyc = m.ncyc;
+  v.oc_start = m.iOCFacesStart;
+  return oc_geometry(c);
+}
+
 }  // namespace fcg
 
 using namespace fcg;
@@ -204,8 +255,13 @@ extern "C" int fcg_bind_mesh(fcg_context *c, const fcg_mesh_desc *m) {
   if (m->numCells <= 0 || m->numFaces <= 0 || m->numInnerFaces < 0 ||
       m->numInnerFaces > m->numFaces)
     return set_error(c, FCG_ERR_ARG, "mesh sizes out of range");
-  if (m->noc != 0)
-    return set_error(c, FCG_ERR_UNSUPPORTED, "O-C grid cuts (noc > 0) are not supported");
+  if (m->noc < 0 || m->ncyc < 0 || m->ncyc > m->noc)
+    return set_error(c, FCG_ERR_ARG, "noc or ncyc out of range");
+  if (m->noc > 0 && (!m->ijlFace || !m->ijrFace))
+    return set_error(c, FCG_ERR_ARG, "noc > 0 without ijlFace / ijrFace");
+  if (m->noc > 0 && (m->iOCFacesStart < m->numInnerFaces ||
+                     (long long)m->iOCFacesStart + m->noc > m->numFaces))
+    return set_error(c, FCG_ERR_INDEX, "iOCFacesStart + noc is outside the boundary faces");
   const double *dp[] = {m->arx, m->ary, m->arz, m->xf, m->yf, m->zf, m->xc, m->yc, m->zc, m->vol};
   for (const double *p : dp)
     if (!p) return set_error(c, FCG_ERR_ARG, "NULL geometry array in fcg_mesh_desc");
@@ -389,6 +445,7 @@ extern "C" int fcg_bind_mesh(fcg_context *c, const fcg_mesh_desc *m) {
       rec(c->lb.pad, sizeof(int) * c->lb.pad_len);
     }
   }
+  if (m->noc > 0 && (rc = bind_oc(c, *m, own))) return rc;
   if ((rc = detect_hex_block(c))) return rc;
   c->bound = true;
   c->bind_gen++;

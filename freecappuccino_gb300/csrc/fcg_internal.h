@@ -52,6 +52,24 @@ struct MeshView {
   const int *cb_ptr, *cb_face, *cb_slot, *cb_type;
   // boundary faces per cell in face order (grad_lsq.f90:116-130)
   const int *cbf_ptr, *cbf_face;
+  // O-C grid cuts and cyclic faces (mesh_geometry_and_topology.f90:453-462, 800-845):
+  // noc pairs, the last ncyc cyclic; pair i couples cell oc_l[i] (owner of its left
+  // face oc_fl[i]) to oc_r[i] (owner of the friend face oc_fr[i]), with the area of
+  // face oc_start + i (fvm_laplacian.f90:70).  Per cell, its pair entries in pair order
+  // (oc_cptr): the coupled cell oc_col and the position oc_vix of the coefficient after
+  // the CSR values of a matrix (ar(i) at i for the left cell, al(i) at noc + i for the
+  // right).  noc = 0 and null pointers for a mesh without them.
+  int noc, ncyc, oc_start;
+  const int *oc_l, *oc_r, *oc_fl, *oc_fr;
+  const double *oc_foc, *oc_srdoc;
+  const int *oc_cptr, *oc_col, *oc_vix;
+};
+
+// The O-C couplings of one matrix for the solver kernels (the per-cell lists of the
+// MeshView and the coefficients after the CSR values); ptr == nullptr: none.
+struct OcView {
+  const int *ptr, *col, *vix;
+  const double *val;
 };
 
 // Sliced-ELL copy of the CSR pattern used by the solvers: slices of 32 rows stored
@@ -153,6 +171,22 @@ struct fcg_context {
 namespace fcg {
 
 int set_error(fcg_context *c, int status, const std::string &msg);
+
+// Values of a matrix `a` on the bound mesh: the CSR values, then ar and al of the O-C
+// pairs (2 noc more when the mesh has them).
+inline long long a_len(const fcg_context *c) { return c->nnz + 2LL * c->mv.noc; }
+
+// foc and srdoc of the bound mesh's O-C pairs (assembly.cu), computed at bind.
+int oc_geometry(fcg_context *c);
+
+// FCG_ERR_UNSUPPORTED for the entry points that do not take the O-C pairs into account.
+inline int refuse_oc(fcg_context *c, const char *what) {
+  return c->mv.noc ? set_error(c, FCG_ERR_UNSUPPORTED,
+                               std::string(what) + ": O-C grid cuts and cyclic faces (noc > 0)"
+                                                   " are supported by fcg_laplacian, fcg_dpcg,"
+                                                   " fcg_iccg, fcg_bicgstab and fcg_spmv only")
+                   : FCG_OK;
+}
 int cuda_fail(fcg_context *c, cudaError_t e, const char *where);
 
 // Host-side construction of the topology (topology.cpp).  Returns a status code.

@@ -167,6 +167,7 @@ int ensure_lsq_matrix(fcg_context *c) {
 extern "C" int fcg_grad_lsq_matrix(fcg_context *c, double *dmat) {
   if (!c) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_grad_lsq_matrix before fcg_bind_mesh");
+  if (c->mv.noc) return refuse_oc(c, "fcg_grad_lsq_matrix");
   FCG_CUDA_TRY(c, cudaSetDevice(c->device));
   c->dmat_ready = false;
   int rc = ensure_lsq_matrix(c);
@@ -183,6 +184,7 @@ extern "C" int fcg_grad(fcg_context *c, const double *phi, double *dPhidxi, int 
                         int nigrad) {
   if (!c) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_grad before fcg_bind_mesh");
+  if (c->mv.noc) return refuse_oc(c, "fcg_grad");
   if (method != FCG_GRAD_GAUSS && method != FCG_GRAD_GAUSS_CORRECTED && method != FCG_GRAD_LSQ)
     return set_error(c, FCG_ERR_ARG, "unknown gradient method");
   if (method == FCG_GRAD_GAUSS && nigrad < 1)
@@ -234,6 +236,7 @@ extern "C" int fcg_grad(fcg_context *c, const double *phi, double *dPhidxi, int 
 extern "C" int fcg_bpres(fcg_context *c, double *p, const double *dPdxi, int istage) {
   if (!c) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_bpres before fcg_bind_mesh");
+  if (c->mv.noc) return refuse_oc(c, "fcg_bpres");
   if (istage < 1) return set_error(c, FCG_ERR_ARG, "istage must be >= 1");
   FCG_CUDA_TRY(c, cudaSetDevice(c->device));
   void *dp, *dg = nullptr;

@@ -175,12 +175,26 @@ __global__ void k_sell_fill(SellView s, int n, const int *__restrict__ diag,
   }
 }
 
+// Row r's O-C couplings in pair order, added to or subtracted from acc after the row's
+// CSR terms, as the reference's loops over i = 1..noc follow its row loops
+// (dpcg.f90:58-61 and 113-116).
+__device__ __forceinline__ double oc_add(const OcView &o, int r, double acc,
+                                         const double *__restrict__ x) {
+  for (int e = o.ptr[r]; e < o.ptr[r + 1]; ++e) acc = acc + o.val[o.vix[e]] * x[o.col[e]];
+  return acc;
+}
+__device__ __forceinline__ double oc_sub(const OcView &o, int r, double acc,
+                                         const double *__restrict__ x) {
+  for (int e = o.ptr[r]; e < o.ptr[r + 1]; ++e) acc = acc - o.val[o.vix[e]] * x[o.col[e]];
+  return acc;
+}
+
 __global__ void __launch_bounds__(kTPB, 8) k_spmv(SellView s, int n, const double *__restrict__ val,
-                       const double *__restrict__ x, double *__restrict__ y) {
+                       const double *__restrict__ x, double *__restrict__ y, OcView o) {
   FCG_SLICE_LOOP(slice, lane, s) {
     int r = slice * 32 + lane;
     double acc = sell_row(s, n, val, x, slice, lane);
-    if (r < n) y[r] = acc;
+    if (r < n) y[r] = o.ptr ? oc_add(o, r, acc, x) : acc;
   }
 }
 
@@ -191,13 +205,14 @@ __global__ void __launch_bounds__(kTPB, 8) k_spmv(SellView s, int n, const doubl
 __global__ void __launch_bounds__(kTPB, 8) k_init(SellView s, int n, const double *__restrict__ val,
                        const double *__restrict__ su, const double *__restrict__ x,
                        double *__restrict__ res, const double *__restrict__ invd, Scal *S,
-                       double *partials, int kind) {
+                       double *partials, int kind, OcView o) {
   double v[2] = {0.0, 0.0};
   FCG_SLICE_LOOP(slice, lane, s) {
     int r = slice * 32 + lane;
     double ax = sell_row(s, n, val, x, slice, lane);
     if (r < n) {
       double rr = su[r] - ax;
+      if (o.ptr) rr = oc_sub(o, r, rr, x);  // every solver's residual (bicgstab.f90:49-52)
       res[r] = rr;
       v[0] += fabs(rr);
       if (kind == SK_DPCG) v[1] += rr * (rr * invd[r]);
@@ -276,13 +291,14 @@ __global__ void __launch_bounds__(kTPB, 8) k_cg_p(int n, const double *__restric
 // qk = A pk, pkapk = sum pk*qk, alf = sk/pkapk (dpcg.f90:105-121).
 __global__ void __launch_bounds__(kTPB, 8) k_cg_spmv(SellView s, int n, const double *__restrict__ val,
                           const double *__restrict__ pk, double *__restrict__ qk, Scal *S,
-                          double *partials) {
+                          double *partials, OcView o) {
   if (solve_done(S)) return;
   double v[1] = {0.0};
   FCG_SLICE_LOOP(slice, lane, s) {
     int r = slice * 32 + lane;
     double q = sell_row(s, n, val, pk, slice, lane);
     if (r < n) {
+      if (o.ptr) q = oc_add(o, r, q, pk);  // block boundaries (dpcg.f90:113-116)
       qk[r] = q;
       v[0] += pk[r] * q;
     }
@@ -1107,13 +1123,14 @@ __global__ void __launch_bounds__(kTPB, 6)
 // Final FP64 check: ||su - A x||^2 and ||su||^2.
 __global__ void __launch_bounds__(kTPB, 8) k_final(SellView s, int n, const double *__restrict__ val,
                         const double *__restrict__ su, const double *__restrict__ x, Scal *S,
-                        double *partials) {
+                        double *partials, OcView o) {
   double v[2] = {0.0, 0.0};
   FCG_SLICE_LOOP(slice, lane, s) {
     int r = slice * 32 + lane;
     double ax = sell_row(s, n, val, x, slice, lane);
     if (r < n) {
       double rr = su[r] - ax;
+      if (o.ptr) rr = oc_sub(o, r, rr, x);
       v[0] += rr * rr;
       v[1] += su[r] * su[r];
     }
@@ -1150,7 +1167,7 @@ static int ensure_state(fcg_context *c, int nsw) {
       k->graph[i] = nullptr;
     }
     const size_t n = c->n;
-    size_t total = 14 * n + (size_t)c->nnz + (size_t)c->sell_len + 8 * (size_t)G + 64;
+    size_t total = 14 * n + (size_t)a_len(c) + (size_t)c->sell_len + 8 * (size_t)G + 64;
     FCG_CUDA_TRY(c, k->vec.ensure(total * sizeof(double)));
     FCG_CUDA_TRY(c, cudaMemset(k->vec.p, 0, total * sizeof(double)));
     if (c->hex.ok) {
@@ -1169,8 +1186,8 @@ static int ensure_state(fcg_context *c, int nsw) {
       p += n;
     }
     p += n;  // guard
-    k->a = p;
-    p += c->nnz;
+    k->a = p;  // the CSR values, then the O-C pairs' ar and al
+    p += a_len(c);
     k->sval = p;
     p += c->sell_len;
     k->partials = p;
@@ -1244,9 +1261,16 @@ static int ensure_state(fcg_context *c, int nsw) {
 }
 
 // Loads CSR values a (device pointer) into the solver copies.
+// The O-C couplings of the matrix load_matrix() placed in the state (none: ptr null).
+static OcView oc_view(const fcg_context *c) {
+  const MeshView &m = c->mv;
+  if (!m.noc) return OcView{nullptr, nullptr, nullptr, nullptr};
+  return OcView{m.oc_cptr, m.oc_col, m.oc_vix, c->ks->a + c->nnz};
+}
+
 static int load_matrix(fcg_context *c, const double *da) {
   KrylovState *k = c->ks;
-  FCG_CUDA_TRY(c, cudaMemcpyAsync(k->a, da, sizeof(double) * c->nnz, cudaMemcpyDeviceToDevice,
+  FCG_CUDA_TRY(c, cudaMemcpyAsync(k->a, da, sizeof(double) * a_len(c), cudaMemcpyDeviceToDevice,
                                   c->stream));
   k_sell_fill<<<grid_for((long long)c->sv.nslices * 32, c->num_sms), kTPB, 0, c->stream>>>(
       c->sv, c->n, c->mv.diag, k->a, k->sval, k->invd);
@@ -1448,7 +1472,8 @@ static void enqueue_unit(fcg_context *c, cudaStream_t st, int kind, int u,
         k_cg_p<<<k->gr.p, kTPB, 0, st>>>(n, k->res, k->invd, k->zk, k->pk, k->S, kind);
         break;
       case 4:
-        k_cg_spmv<<<k->gr.spmv, kTPB, 0, st>>>(s, n, k->sval, k->pk, k->qk, k->S, k->partials);
+        k_cg_spmv<<<k->gr.spmv, kTPB, 0, st>>>(s, n, k->sval, k->pk, k->qk, k->S, k->partials,
+                                               oc_view(c));
         break;
       case 5:
         k_cg_update<<<k->gr.update, kTPB, 0, st>>>(n, k->x, k->res, k->pk, k->qk, k->invd, k->S,
@@ -1578,6 +1603,7 @@ static int run_solver(fcg_context *c, int kind, const double *a, const double *s
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "solver called before fcg_bind_mesh");
   if (!a || !su || !fi) return set_error(c, FCG_ERR_ARG, "NULL a, su or fi");
   if (nsw < 0) return set_error(c, FCG_ERR_ARG, "nsw must be >= 0");
+  if (kind == SK_MIXED && c->mv.noc) return refuse_oc(c, "fcg_dpcg_mixed");
   FCG_CUDA_TRY(c, cudaSetDevice(c->device));
   int rc = ensure_state(c, nsw > 0 ? nsw : 1);
   if (rc) return rc;
@@ -1585,7 +1611,7 @@ static int run_solver(fcg_context *c, int kind, const double *a, const double *s
   const size_t n1 = sizeof(double) * c->n;
   void *da, *dsu, *dfi;
   bool ha, hsu, hfi;
-  if ((rc = stage_in(c, a, sizeof(double) * c->nnz, 0, true, &da, &ha))) return rc;
+  if ((rc = stage_in(c, a, sizeof(double) * a_len(c), 0, true, &da, &ha))) return rc;
   if ((rc = stage_in(c, su, n1, 1, true, &dsu, &hsu))) return rc;
   if ((rc = stage_in(c, fi, n1, 2, true, &dfi, &hfi))) return rc;
   FCG_CUDA_TRY(c, cudaEventRecord(k->ev0, c->stream));
@@ -1607,7 +1633,7 @@ static int run_solver(fcg_context *c, int kind, const double *a, const double *s
   *k->hS = init;
   FCG_CUDA_TRY(c, cudaMemcpyAsync(k->S, k->hS, sizeof(Scal), cudaMemcpyHostToDevice, c->stream));
   k_init<<<k->gr.init, kTPB, 0, c->stream>>>(c->sv, c->n, k->sval, k->su, k->x, k->res, k->invd, k->S,
-                                    k->partials, kind);
+                                    k->partials, kind, oc_view(c));
   FCG_CHECK_LAUNCH(c, "k_init");
   if (kind == SK_BICG)
     FCG_CUDA_TRY(c, cudaMemcpyAsync(k->reso, k->res, n1, cudaMemcpyDeviceToDevice, c->stream));
@@ -1657,7 +1683,8 @@ static int run_solver(fcg_context *c, int kind, const double *a, const double *s
       done = k->hS->done;
     }
   }
-  k_final<<<k->gr.fin, kTPB, 0, c->stream>>>(c->sv, c->n, k->sval, k->su, k->x, k->S, k->partials);
+  k_final<<<k->gr.fin, kTPB, 0, c->stream>>>(c->sv, c->n, k->sval, k->su, k->x, k->S, k->partials,
+                                             oc_view(c));
   FCG_CHECK_LAUNCH(c, "k_final");
   FCG_CUDA_TRY(c, cudaEventRecord(k->ev1, c->stream));
   FCG_CUDA_TRY(c, cudaMemcpyAsync(dfi, k->x, n1, cudaMemcpyDeviceToDevice, c->stream));
@@ -1827,7 +1854,7 @@ extern "C" int fcg_spmv(fcg_context *c, const double *a, const double *x, double
   if (a) {
     void *da;
     bool ha;
-    if ((rc = stage_in(c, a, sizeof(double) * c->nnz, 0, true, &da, &ha))) return rc;
+    if ((rc = stage_in(c, a, sizeof(double) * a_len(c), 0, true, &da, &ha))) return rc;
     if ((rc = load_matrix(c, (const double *)da))) return rc;
   } else if (!k->matrix_loaded) {
     return set_error(c, FCG_ERR_STATE, "fcg_spmv with a == NULL before any matrix was loaded");
@@ -1836,7 +1863,8 @@ extern "C" int fcg_spmv(fcg_context *c, const double *a, const double *x, double
   bool hx, hy;
   if ((rc = stage_in(c, x, n1, 1, true, &dx, &hx))) return rc;
   if ((rc = stage_in(c, y, n1, 2, false, &dy, &hy))) return rc;
-  k_spmv<<<k->gr.plain, kTPB, 0, c->stream>>>(c->sv, c->n, k->sval, (const double *)dx, (double *)dy);
+  k_spmv<<<k->gr.plain, kTPB, 0, c->stream>>>(c->sv, c->n, k->sval, (const double *)dx, (double *)dy,
+                                              oc_view(c));
   FCG_CHECK_LAUNCH(c, "k_spmv");
   if ((rc = stage_out(c, y, dy, n1, hy))) return rc;
   if (hy) FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));

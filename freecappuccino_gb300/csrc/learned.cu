@@ -1133,6 +1133,9 @@ int mark_done(fcg_learned *Lp, fcg_context *c) {
 int check_ctx(fcg_learned *Lp, fcg_context *c) {
   if (!Lp || !c) return FCG_ERR_ARG;
   if (!c->bound) return lp_fail(Lp, FCG_ERR_STATE, "context has no mesh (fcg_bind_mesh)");
+  if (c->mv.noc)
+    return lp_fail(Lp, FCG_ERR_UNSUPPORTED,
+                   "the learned preconditioner does not take O-C grid cuts (noc > 0)");
   if (c->device != Lp->device)
     return lp_fail(Lp, FCG_ERR_ARG, "context and learned preconditioner on different devices");
   LP_TRY(Lp, cudaSetDevice(c->device));

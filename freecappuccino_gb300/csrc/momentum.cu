@@ -402,6 +402,7 @@ extern "C" int fcg_calcuvw(fcg_context *c, const fcg_uvw_params *prm, const fcg_
                            double *a, double *diag_vw, double *rhs, double *ap) {
   if (!c || !prm || !f) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_calcuvw before fcg_bind_mesh");
+  if (c->mv.noc) return refuse_oc(c, "fcg_calcuvw");
   const bool need_old = prm->bdf || prm->cn;
   const bool need_oo = prm->bdf && prm->btime > (double)0.99f;
   const bool need_t = prm->buoyancy && prm->boussinesq;

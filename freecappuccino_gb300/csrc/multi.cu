@@ -835,6 +835,7 @@ extern "C" int fcg_bicgstab_multi(fcg_context *c, int nsys, const double *a, con
                                   fcg_solve_report *rep) {
   if (!c) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_bicgstab_multi before fcg_bind_mesh");
+  if (c->mv.noc) return refuse_oc(c, "fcg_bicgstab_multi");
   if (nsys < 1 || nsys > kMaxSys) return set_error(c, FCG_ERR_ARG, "nsys must be 1..8");
   if (!a || !su || !fi || nsw < 0) return set_error(c, FCG_ERR_ARG, "bad argument");
   FCG_CUDA_TRY(c, cudaSetDevice(c->device));

@@ -45,6 +45,15 @@ class Mesh:
     points: np.ndarray | None = None
     face_ptr: np.ndarray | None = None
     face_nodes: np.ndarray | None = None
+    # O-C grid cut and cyclic pairs (mesh_geometry_and_topology.f90:453-462, 800-845):
+    # pair i joins the owners of boundary faces ijlFace[i] and ijrFace[i] (1-based); the
+    # last ncyc pairs are cyclic; the O-C loops take pair i's area from face
+    # iOCFacesStart + i (0-based start, i 1-based)
+    noc: int = 0
+    ncyc: int = 0
+    iOCFacesStart: int = 0
+    ijlFace: np.ndarray | None = None
+    ijrFace: np.ndarray | None = None
 
     @property
     def numTotal(self) -> int:
@@ -53,6 +62,11 @@ class Mesh:
     @property
     def nnz(self) -> int:
         return self.numCells + 2 * self.numInnerFaces
+
+    @property
+    def a_len(self) -> int:
+        """Values of a matrix on this mesh: the CSR values, then ar and al of the O-C pairs."""
+        return self.nnz + 2 * self.noc
 
     def boundary_slot_start(self, btype: str) -> int:
         """0-based offset of a boundary type's slots in a numTotal field (:593-605)."""
@@ -71,10 +85,14 @@ class Mesh:
         for k in ("iInletFacesStart", "iOutletFacesStart", "iSymmetryFacesStart",
                   "iWallFacesStart", "iPressOutletFacesStart"):
             setattr(d, k, int(self.starts.get(k, 0)))
-        d.noc = 0
+        d.noc, d.ncyc, d.iOCFacesStart = int(self.noc), int(self.ncyc), int(self.iOCFacesStart)
         for k in ("owner", "neighbour", "arx", "ary", "arz", "xf", "yf", "zf", "xc", "yc", "zc",
                   "vol", "facint"):
             setattr(d, k, getattr(self, k).ctypes.data)
+        if self.noc:
+            self.ijlFace = np.ascontiguousarray(self.ijlFace, dtype=np.int32)
+            self.ijrFace = np.ascontiguousarray(self.ijrFace, dtype=np.int32)
+            d.ijlFace, d.ijrFace = self.ijlFace.ctypes.data, self.ijrFace.ctypes.data
         return d
 
     def oracle_kwargs(self) -> dict:
@@ -84,6 +102,9 @@ class Mesh:
                                              "xc", "yc", "zc", "vol", "facint")}
         kw.update(self.counts)
         kw.update(self.starts)
+        if self.noc:
+            kw.update(noc=self.noc, ncyc=self.ncyc, iOCFacesStart=self.iOCFacesStart,
+                      ijlFace=self.ijlFace, ijrFace=self.ijrFace)
         return kw
 
 

@@ -156,7 +156,7 @@ class Context:
         self._follow(mu, phi, su)
         mu, phi = _host(mu), _host(phi)
         su = su.clone() if _is_torch(su) else np.array(su, dtype=np.float64)
-        a = _like(mu, self.nnz)
+        a = _like(mu, self.mesh.a_len)  # with O-C pairs: ar and al after the CSR values
         self._check(self.lib.fcg_laplacian(self.h, _ptr(mu), _ptr(phi), _ptr(a), _ptr(su)),
                     "fcg_laplacian")
         return a, su

@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define FCG_ABI_VERSION 1
+#define FCG_ABI_VERSION 2  /* 2: fcg_mesh_desc gained the O-C pair fields */
 
 /* Status codes. */
 #define FCG_OK 0
@@ -40,7 +40,7 @@ extern "C" {
 #define FCG_ERR_PIVOT (-5)       /* zero or non-finite pivot in a DIC/DILU factor */
 #define FCG_ERR_STALL (-6)       /* a preconditioned iteration stalled (learned FCG) */
 #define FCG_ERR_TIMEOUT (-7)     /* a bounded device-side wait gave up */
-#define FCG_ERR_UNSUPPORTED (-8) /* O-C grid cuts and cyclic faces are not supported */
+#define FCG_ERR_UNSUPPORTED (-8) /* an entry point that does not take O-C grid cuts */
 #define FCG_ERR_NOMEM (-9)       /* device allocation failed */
 #define FCG_ERR_NONFINITE (-10)  /* NaN/Inf reached a reduction */
 
@@ -71,12 +71,26 @@ typedef struct fcg_mesh_desc {
   int ninl, nout, nsym, nwal, npru;
   int iInletFacesStart, iOutletFacesStart, iSymmetryFacesStart, iWallFacesStart,
       iPressOutletFacesStart;
-  int noc; /* O-C grid cut faces: must be 0 (FCG_ERR_UNSUPPORTED otherwise) */
+  /* O-C grid cut and cyclic face pairs after `noc = noc + ncyc`
+   * (mesh_geometry_and_topology.f90:1163); 0 for none.  See the fields at the end. */
+  int noc;
   const int *owner;                             /* [numFaces], 1-based */
   const int *neighbour;                         /* [numInnerFaces], 1-based */
   const double *arx, *ary, *arz, *xf, *yf, *zf; /* [numFaces] */
   const double *xc, *yc, *zc, *vol;             /* [numCells] */
   const double *facint;                         /* [numInnerFaces] */
+  /* The O-C pairs ('domain' and 'cyclic' patches, mesh_geometry_and_topology.f90:
+   * 453-462, 800-845), read when noc > 0: pair i couples the owner of boundary face
+   * ijlFace[i] (ijl) to the owner of its friend face ijrFace[i] (ijr), both 1-based;
+   * the last ncyc pairs are cyclic (interpolation factor 1/2, :1149).  The O-C loops
+   * take the area of pair i from face iOCFacesStart + i (0-based start, i 1-based;
+   * fvm_laplacian.f90:70).  With noc > 0 a matrix `a` holds nnz + 2 noc values: the
+   * CSR values, then ar(1..noc), then al(1..noc) (module sparse_matrix's al, ar).
+   * fcg_laplacian, fcg_dpcg, fcg_iccg, fcg_bicgstab and fcg_spmv take the pairs; every
+   * other entry point returns FCG_ERR_UNSUPPORTED on such a mesh. */
+  int ncyc;
+  int iOCFacesStart;
+  const int *ijlFace, *ijrFace; /* [noc] */
 } fcg_mesh_desc;
 
 /* Uploads the mesh and builds, once, everything the kernels need: the CSR pattern

@@ -241,6 +241,29 @@ static int iPressOutletStart(const orc_mesh *m) {
 /* a2: fvm_laplacian.f90                                                      */
 /* ------------------------------------------------------------------------- */
 
+int orc_oc_geometry(const orc_mesh *m, int *ijl, int *ijr, double *foc, double *srdoc) {
+  int nreg = m->noc - m->ncyc;
+  for (int i = 1; i <= m->noc; ++i) {
+    int iface = F(m->ijlFace, i), ifaceFriend = F(m->ijrFace, i); /* :820-824 */
+    int inp = F(m->owner, iface), inn = F(m->owner, ifaceFriend);
+    F(ijl, i) = inp;
+    F(ijr, i) = inn;
+    double xpn = F(m->xc, inn) - F(m->xf, ifaceFriend); /* :1094-1100 */
+    double ypn = F(m->yc, inn) - F(m->yf, ifaceFriend);
+    double zpn = F(m->zc, inn) - F(m->zf, ifaceFriend);
+    double dpn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
+    xpn = F(m->xf, iface) - F(m->xc, inp); /* :1103-1107 */
+    ypn = F(m->yf, iface) - F(m->yc, inp);
+    zpn = F(m->zf, iface) - F(m->zc, inp);
+    double djn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
+    F(foc, i) = i <= nreg ? djn / (djn + dpn) : 0.5; /* :1109, cyclic :1149 */
+    double are = sqrt(F(m->arx, iface) * F(m->arx, iface) + F(m->ary, iface) * F(m->ary, iface) +
+                      F(m->arz, iface) * F(m->arz, iface));
+    F(srdoc, i) = are / (djn + dpn); /* :1115 */
+  }
+  return 0;
+}
+
 int orc_laplacian(const orc_mesh *m, const int *ioffset, const int *diag, const int *slot_pn,
                   const int *slot_np, const double *mu, const double *phi, double *a,
                   double *su) {
@@ -262,6 +285,33 @@ int orc_laplacian(const orc_mesh *m, const int *ioffset, const int *diag, const 
     F(a, F(slot_np, i)) = cap;
     F(a, F(diag, ijp)) = F(a, F(diag, ijp)) - can;
     F(a, F(diag, ijn)) = F(a, F(diag, ijn)) - cap;
+  }
+  if (m->noc > 0) { /* o- and c-grid cuts (:67-86) */
+    int noc = m->noc;
+    int *ijl = malloc(sizeof(int) * (size_t)noc), *ijr = malloc(sizeof(int) * (size_t)noc);
+    double *foc = malloc(sizeof(double) * (size_t)noc);
+    double *srdoc = malloc(sizeof(double) * (size_t)noc);
+    if (!ijl || !ijr || !foc || !srdoc) return -1;
+    orc_oc_geometry(m, ijl, ijr, foc, srdoc);
+    double *ar = a + nnz, *al = a + nnz + noc;
+    for (int i = 1; i <= noc; ++i) {
+      int iface = m->iOCFacesStart + i;
+      int ijp = F(ijl, i), ijn = F(ijr, i);
+      double arx = F(m->arx, iface), ary = F(m->ary, iface), arz = F(m->arz, iface);
+      /* facefluxlaplacian(ijp, ijn, arx(iface), .., foc(i), mu, al(i), ar(i)) */
+      double fxn = F(foc, i);
+      double fxp = 1.0 - fxn;
+      double xpn = F(m->xc, ijn) - F(m->xc, ijp);
+      double ypn = F(m->yc, ijn) - F(m->yc, ijp);
+      double zpn = F(m->zc, ijn) - F(m->zc, ijp);
+      double smdpn = (arx * arx + ary * ary + arz * arz) / (arx * xpn + ary * ypn + arz * zpn);
+      double cap = (fxp * F(mu, ijp) + fxn * F(mu, ijn)) * smdpn;
+      F(al, i) = cap;
+      F(ar, i) = cap;
+      F(a, F(diag, ijp)) = F(a, F(diag, ijp)) - F(ar, i);
+      F(a, F(diag, ijn)) = F(a, F(diag, ijn)) - F(al, i);
+    }
+    free(ijl), free(ijr), free(foc), free(srdoc);
   }
   /* Wall faces (:140-154); inlet/outlet/symmetry add nothing (their loops are commented out). */
   for (int i = 1; i <= m->nwal; ++i) {
@@ -644,13 +694,19 @@ int orc_spmv(int n, const int *ioffset, const int *ja, const double *a, const do
   return 0;
 }
 
-/* res = su - A fi and its L1 norm (dpcg.f90:51-64). */
+/* res = su - A fi and its L1 norm (dpcg.f90:51-64), the O-C couplings after the rows
+ * (:58-61). */
 static double initial_residual(int n, const int *ioffset, const int *ja, const double *a,
-                               const double *su, const double *fi, double *res) {
+                               const double *su, const double *fi, double *res,
+                               const orc_solver_opts *o) {
   for (int i = 1; i <= n; ++i) {
     double r = F(su, i);
     for (int k = F(ioffset, i); k <= F(ioffset, i + 1) - 1; ++k) r = r - F(a, k) * F(fi, F(ja, k));
     F(res, i) = r;
+  }
+  for (int i = 1; i <= o->noc; ++i) {
+    F(res, F(o->ijl, i)) = F(res, F(o->ijl, i)) - F(o->ar, i) * F(fi, F(o->ijr, i));
+    F(res, F(o->ijr, i)) = F(res, F(o->ijr, i)) - F(o->al, i) * F(fi, F(o->ijl, i));
   }
   double res0 = 0.0;
   for (int i = 0; i < n; ++i) res0 = res0 + fabs(res[i]);
@@ -690,7 +746,7 @@ static int pcg(int n, const int *ioffset, const int *ja, const int *diag, const 
   double *zk = (double *)calloc((size_t)n + 1, sizeof(double));
   double *d = (double *)calloc((size_t)n + 1, sizeof(double));
   if (!pk || !zk || !d) return -1;
-  double res0 = initial_residual(n, ioffset, ja, a, su, fi, res);
+  double res0 = initial_residual(n, ioffset, ja, a, su, fi, res, o);
   if (o->early_exit && res0 < orc_const_tol()) { /* dpcg.f90:66-70 */
     fill_out(out, res0, res0, 0, 0);
     free(pk), free(zk), free(d);
@@ -717,6 +773,10 @@ static int pcg(int n, const int *ioffset, const int *ja, const int *diag, const 
     double bet = sk / s0;
     for (int i = 0; i < n; ++i) pk[i] = zk[i] + bet * pk[i];
     orc_spmv(n, ioffset, ja, a, pk, zk);
+    for (int i = 1; i <= o->noc; ++i) { /* block boundaries, dpcg.f90:113-116 */
+      F(zk, F(o->ijl, i)) = F(zk, F(o->ijl, i)) + F(o->ar, i) * F(pk, F(o->ijr, i));
+      F(zk, F(o->ijr, i)) = F(zk, F(o->ijr, i)) + F(o->al, i) * F(pk, F(o->ijl, i));
+    }
     double pkapk = 0.0;
     for (int i = 0; i < n; ++i) pkapk = pkapk + pk[i] * zk[i];
     double alf = sk / pkapk;
@@ -760,7 +820,7 @@ int orc_bicgstab(int n, const int *ioffset, const int *ja, const int *diag, cons
   double *uk = calloc(sz, sizeof(double)), *zk = calloc(sz, sizeof(double));
   double *vk = calloc(sz, sizeof(double)), *d = calloc(sz, sizeof(double));
   if (!reso || !pk || !uk || !zk || !vk || !d) return -1;
-  double res0 = initial_residual(n, ioffset, ja, a, su, fi, res);
+  double res0 = initial_residual(n, ioffset, ja, a, su, fi, res, o);
   if (o->early_exit && res0 < orc_const_tol()) {
     fill_out(out, res0, res0, 0, 0);
     free(reso), free(pk), free(uk), free(zk), free(vk), free(d);

@@ -35,7 +35,18 @@ typedef struct orc_mesh {
   const double *arx, *ary, *arz, *xf, *yf, *zf; /* [numFaces] */
   const double *xc, *yc, *zc, *vol;             /* [numCells] */
   const double *facint;                         /* [numInnerFaces] */
+  /* O-C grid cuts and cyclic faces (mesh_geometry_and_topology.f90:453-462, 800-845):
+   * noc face pairs after `noc = noc + ncyc` (:1163), the last ncyc of them cyclic.
+   * Pair i joins the owner of face ijlFace(i) (ijl) to the owner of its friend
+   * ijrFace(i) (ijr); the O-C loops take the pair's area from face iOCFacesStart + i
+   * (fvm_laplacian.f90:70). */
+  int noc, ncyc, iOCFacesStart;
+  const int *ijlFace, *ijrFace; /* [noc] 1-based face indices */
 } orc_mesh;
+
+/* ijl, ijr (1-based cells), foc and srdoc of the noc pairs
+ * (mesh_geometry_and_topology.f90:814-845, 1083-1152; cyclic pairs take foc = 1/2). */
+int orc_oc_geometry(const orc_mesh *m, int *ijl, int *ijr, double *foc, double *srdoc);
 
 /* Float-literal constants of the reference: default-REAL literals promoted to real(dp). */
 double orc_const_small_src(void);  /* parameters::small = 1e-20 (modules_allocatable.f90:27) */
@@ -57,6 +68,8 @@ int orc_create_csr(int numCells, int numInnerFaces, const int *owner, const int 
                    int *slot_pn /*[nin]*/, int *slot_np /*[nin]*/);
 
 /* --- a2: fvm_laplacian.f90:1-163 (+ facefluxlaplacian :171-221) --- */
+/* fvm_laplacian.f90:1-163.  With m->noc > 0, a holds nnz + 2 noc values: the CSR
+ * values, then ar(1..noc), then al(1..noc) of the O-C faces (:67-86). */
 int orc_laplacian(const orc_mesh *m, const int *ioffset, const int *diag,
                   const int *slot_pn, const int *slot_np,
                   const double *mu /*[n]*/, const double *phi /*[numTotal]*/,
@@ -159,6 +172,13 @@ typedef struct orc_solver_opts {
   double small;    /* parameters::small (1e-20) or the test copies' 1e-30 */
   int early_exit;  /* 1: src/ variant returns when res0 < tol; 0: test copies never do */
   double *trace;   /* optional [2*nsw]: per sweep (resl, rsm) */
+  /* O-C couplings (module sparse_matrix's al, ar): row ijl(i) couples to ijr(i) with
+   * ar(i), row ijr(i) to ijl(i) with al(i); noc = 0 for none.  dpcg and iccg apply them
+   * in the initial residual and in every A p (dpcg.f90:58-61,113-116; iccg.f90:59-62,
+   * 137-140); bicgstab in the initial residual only (bicgstab.f90:49-52). */
+  int noc;
+  const int *ijl, *ijr; /* [noc] 1-based cells */
+  const double *ar, *al; /* [noc] */
 } orc_solver_opts;
 
 typedef struct orc_solver_out {

@@ -46,12 +46,15 @@ class _Mesh(C.Structure):
         ("owner", _ip), ("neighbour", _ip),
         ("arx", _dp), ("ary", _dp), ("arz", _dp), ("xf", _dp), ("yf", _dp), ("zf", _dp),
         ("xc", _dp), ("yc", _dp), ("zc", _dp), ("vol", _dp), ("facint", _dp),
+        ("noc", C.c_int), ("ncyc", C.c_int), ("iOCFacesStart", C.c_int),
+        ("ijlFace", _ip), ("ijrFace", _ip),
     ]
 
 
 class _Opts(C.Structure):
     _fields_ = [("resmax", C.c_double), ("nsw", C.c_int), ("small", C.c_double),
-                ("early_exit", C.c_int), ("trace", _dp)]
+                ("early_exit", C.c_int), ("trace", _dp),
+                ("noc", C.c_int), ("ijl", _ip), ("ijr", _ip), ("ar", _dp), ("al", _dp)]
 
 
 class _Out(C.Structure):
@@ -103,7 +106,8 @@ class Mesh:
     def __init__(self, numCells, numFaces, numInnerFaces, owner, neighbour, arx, ary, arz,
                  xf, yf, zf, xc, yc, zc, vol, facint, ninl=0, nout=0, nsym=0, nwal=0, npru=0,
                  iInletFacesStart=0, iOutletFacesStart=0, iSymmetryFacesStart=0,
-                 iWallFacesStart=0, iPressOutletFacesStart=0):
+                 iWallFacesStart=0, iPressOutletFacesStart=0, noc=0, ncyc=0, iOCFacesStart=0,
+                 ijlFace=None, ijrFace=None):
         self.numCells, self.numFaces, self.numInnerFaces = numCells, numFaces, numInnerFaces
         self.numTotal = numCells + numFaces - numInnerFaces
         self.arrays = dict(owner=_i32(owner), neighbour=_i32(neighbour), arx=_f64(arx),
@@ -120,6 +124,12 @@ class Mesh:
             setattr(s, k, int(v))
         for k, v in self.arrays.items():
             setattr(s, k, _i(v) if v.dtype == np.int32 else _d(v))
+        # O-C grid cuts and cyclic pairs (1-based face indices of each pair's two faces)
+        self.noc, self.ncyc, self.iOCFacesStart = int(noc), int(ncyc), int(iOCFacesStart)
+        if self.noc:
+            self.arrays["ijlFace"], self.arrays["ijrFace"] = _i32(ijlFace), _i32(ijrFace)
+            s.ijlFace, s.ijrFace = _i(self.arrays["ijlFace"]), _i(self.arrays["ijrFace"])
+        s.noc, s.ncyc, s.iOCFacesStart = self.noc, self.ncyc, self.iOCFacesStart
         self.struct = s
 
     def __getattr__(self, k):
@@ -173,10 +183,20 @@ def create_csr(numCells, owner, neighbour) -> CSR:
     return c
 
 
+def oc_geometry(m: Mesh):
+    """ijl, ijr (1-based cells), foc and srdoc of the mesh's O-C and cyclic pairs
+    (mesh_geometry_and_topology.f90:814-845, 1083-1152)."""
+    ijl, ijr = np.zeros(max(m.noc, 1), np.int32), np.zeros(max(m.noc, 1), np.int32)
+    foc, srdoc = np.zeros(max(m.noc, 1)), np.zeros(max(m.noc, 1))
+    assert lib().orc_oc_geometry(C.byref(m.struct), _i(ijl), _i(ijr), _d(foc), _d(srdoc)) == 0
+    return ijl[: m.noc], ijr[: m.noc], foc[: m.noc], srdoc[: m.noc]
+
+
 def laplacian(m: Mesh, csr: CSR, mu, phi, su):
-    """fvm_laplacian.f90:1-163. Returns (a, su) with su updated by the wall terms."""
+    """fvm_laplacian.f90:1-163. Returns (a, su) with su updated by the wall terms; with O-C
+    pairs a holds nnz + 2 noc values (the CSR values, then ar, then al)."""
     mu, phi, su = _f64(mu), _f64(phi), _f64(su).copy()
-    a = np.zeros(csr.nnz)
+    a = np.zeros(csr.nnz + 2 * m.noc)
     assert lib().orc_laplacian(C.byref(m.struct), _i(csr.ioffset), _i(csr.diag), _i(csr.slot_pn),
                                _i(csr.slot_np), _d(mu), _d(phi), _d(a), _d(su)) == 0
     return a, su
@@ -378,7 +398,9 @@ class SolveResult:
     trace: np.ndarray
 
 
-def _solve(fn, csr: CSR, a, su, fi, sor, nsw, small=None, early_exit=True) -> SolveResult:
+def _solve(fn, csr: CSR, a, su, fi, sor, nsw, small=None, early_exit=True,
+           oc=None) -> SolveResult:
+    """oc = (ijl, ijr), 1-based: the O-C pairs, whose ar and al follow the CSR values in a."""
     n = len(csr.diag)
     a, su = _f64(a), _f64(su)
     fi = _f64(fi).copy()
@@ -386,6 +408,13 @@ def _solve(fn, csr: CSR, a, su, fi, sor, nsw, small=None, early_exit=True) -> So
     trace = np.zeros(2 * max(nsw, 1))
     o = _Opts(float(sor), int(nsw), small_src() if small is None else float(small),
               int(bool(early_exit)), _d(trace))
+    if oc is not None and len(oc[0]):
+        ijl, ijr = _i32(oc[0]), _i32(oc[1])
+        noc, nnz = len(ijl), csr.nnz
+        ar, al = np.ascontiguousarray(a[nnz:nnz + noc]), np.ascontiguousarray(a[nnz + noc:nnz + 2 * noc])
+        assert len(a) == nnz + 2 * noc
+        o.noc, o.ijl, o.ijr, o.ar, o.al = noc, _i(ijl), _i(ijr), _d(ar), _d(al)
+        keep = (ijl, ijr, ar, al)  # noqa: F841 (alive across the call)
     out = _Out()
     assert fn(n, _i(csr.ioffset), _i(csr.ja), _i(csr.diag), _d(a), _d(su), _d(fi), _d(res),
               C.byref(o), C.byref(out)) == 0

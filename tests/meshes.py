@@ -27,6 +27,39 @@ def hex_mesh(N: int, jitter: float = 0.2, seed: int = 7) -> fcg.Mesh:
 
 
 @functools.lru_cache(maxsize=None)
+def oc_split_mesh(N: int, kc: int | None = None, jitter: float = 0.0, seed: int = 7,
+                  cyclic: bool = False) -> fcg.Mesh:
+    """The N^3 hex mesh with the inner faces between planes kc - 1 and kc (default N/2)
+    made O-C pairs, as a mesh cut into two blocks reads them ('domain' patches, or
+    'cyclic' with cyclic=True): every cut face becomes a left face owned by the cell
+    below and a friend face owned by the cell above (area reversed), both after the other
+    boundary faces, left faces first (iOCFacesStart)."""
+    m = fcg.hex_mesh(N, jitter=jitter, seed=seed)
+    nin, nf = m.numInnerFaces, m.numFaces
+    own0, nb0 = m.owner[:nin] - 1, m.neighbour - 1
+    kc = N // 2 if kc is None else kc
+    cut = (own0 // (N * N) == kc - 1) & (nb0 // (N * N) == kc)
+    keep = np.flatnonzero(~cut)
+    ci = np.flatnonzero(cut)
+    bnd = np.arange(nin, nf)
+    noc = len(ci)
+    src = np.concatenate([keep, bnd, ci, ci])  # the old face each new face copies
+    flip = np.concatenate([np.ones(len(keep) + len(bnd) + noc), -np.ones(noc)])
+    owner = np.concatenate([m.owner[keep], m.owner[bnd], m.owner[ci], m.neighbour[ci]])
+    geo = {k: getattr(m, k)[src] * (flip if k.startswith("ar") else 1.0)
+           for k in ("arx", "ary", "arz", "xf", "yf", "zf")}
+    start = nf - noc  # 0-based: the left faces follow the old boundary faces
+    out = fcg.Mesh(m.numCells, nf + noc, nin - noc, owner.astype(np.int32),
+                   m.neighbour[keep].astype(np.int32), xc=m.xc, yc=m.yc, zc=m.zc, vol=m.vol,
+                   facint=m.facint[keep], counts=dict(m.counts),
+                   starts={k: v - noc for k, v in m.starts.items()}, **geo)
+    out.noc, out.ncyc, out.iOCFacesStart = noc, noc if cyclic else 0, start
+    out.ijlFace = (start + 1 + np.arange(noc)).astype(np.int32)
+    out.ijrFace = (start + 1 + noc + np.arange(noc)).astype(np.int32)
+    return out
+
+
+@functools.lru_cache(maxsize=None)
 def mixed_patch_mesh(N: int = 8) -> fcg.Mesh:
     """A jittered N^3 hex mesh whose boundary faces carry all five boundary types: the
     symmetry faces relabelled in four runs as inlet, outlet, pressure outlet and symmetry,

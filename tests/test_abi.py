@@ -39,7 +39,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_abi_version_and_status_strings():
     lib = _lib.load()
-    assert lib.fcg_abi_version() == 1
+    assert lib.fcg_abi_version() == 2
     assert lib.fcg_status_string(0) == b"ok"
     assert lib.fcg_status_string(_lib.FCG_ERR_PIVOT) == b"zero or non-finite pivot"
 

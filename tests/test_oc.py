@@ -1,0 +1,195 @@
+"""O-C grid cuts and cyclic faces (noc > 0; mesh_geometry_and_topology.f90:453-462, 800-845,
+1083-1163; fvm_laplacian.f90:67-86; dpcg.f90:58-61,113-116; iccg.f90:59-62,137-140;
+bicgstab.f90:49-52).
+
+The test mesh is an N^3 hex mesh cut into two blocks: the inner faces between two planes
+become O-C pairs (tests/meshes.py oc_split_mesh).  The operator of the cut mesh, its CSR
+values plus the pairs' ar and al, is then the operator of the uncut mesh up to the
+rounding of the pairs' interpolation factor (from the face centres) against the inner
+faces' (from the plane intersection), so both meshes give the same solution.
+
+CPU: the oracle's pair geometry, operator and solvers.  GPU: fcg_laplacian bit for bit
+against the oracle, fcg_dpcg / fcg_iccg / fcg_bicgstab and fcg_spmv against it (within
+the solvers' usual 1e-10), the same solution as on the uncut mesh, and the entry points
+that do not take the pairs refusing the mesh."""
+import numpy as np
+import pytest
+
+import freecappuccino_gb300 as fcg
+from oracle import oracle
+from tests.meshes import oc_split_mesh, oracle_csr, oracle_mesh
+
+
+def _fields(m, seed=5):
+    mu = -(1.0 + 0.5 * fcg.uniform(seed, 5, m.numCells))
+    su = fcg.uniform(seed, 7, m.numCells) * m.vol
+    return mu, np.zeros(m.numTotal), su
+
+
+def _operator(m, csr, a):
+    """Dense operator of a (CSR values, then ar and al of the pairs)."""
+    n = m.numCells
+    A = np.zeros((n, n))
+    for i in range(n):
+        for k in range(csr.ioffset[i] - 1, csr.ioffset[i + 1] - 1):
+            A[i, csr.ja[k] - 1] += a[k]
+    if m.noc:
+        ijl, ijr, _, _ = oracle.oc_geometry(oracle_mesh(m))
+        ar, al = a[csr.nnz:csr.nnz + m.noc], a[csr.nnz + m.noc:]
+        for i in range(m.noc):
+            A[ijl[i] - 1, ijr[i] - 1] += ar[i]
+            A[ijr[i] - 1, ijl[i] - 1] += al[i]
+    return A
+
+
+def _oc(m):
+    ijl, ijr, _, _ = oracle.oc_geometry(oracle_mesh(m))
+    return ijl, ijr
+
+
+# ----------------------------------------------------------------------------- CPU
+@pytest.mark.parametrize("cyclic", [False, True])
+def test_oracle_pair_geometry(cyclic):
+    """ijl / ijr are the owners of each pair's faces; foc is the cut faces' interpolation
+    factor (1/2 for cyclic pairs) and srdoc |S| / (djn + dpn)."""
+    N = 8
+    m, u = oc_split_mesh(N, cyclic=cyclic), fcg.hex_mesh(N)
+    ijl, ijr, foc, srdoc = oracle.oc_geometry(oracle_mesh(m))
+    assert m.noc == N * N
+    assert np.array_equal(ijl, m.owner[m.ijlFace - 1]) and np.array_equal(ijr, m.owner[m.ijrFace - 1])
+    assert np.all(ijr - ijl == N * N)
+    nin = u.numInnerFaces
+    cut = ((u.owner[:nin] - 1) // (N * N) == N // 2 - 1) & ((u.neighbour - 1) // (N * N) == N // 2)
+    if cyclic:
+        assert np.all(foc == 0.5)
+    else:
+        assert np.abs(foc - u.facint[cut]).max() < 1e-13
+    f = np.flatnonzero(cut)
+    are = np.sqrt(u.arx[f] ** 2 + u.ary[f] ** 2 + u.arz[f] ** 2)
+    assert np.allclose(srdoc, are * N, rtol=1e-12)
+
+
+@pytest.mark.parametrize("N", [6, 8])
+def test_oracle_laplacian_of_the_cut_mesh_is_the_uncut_operator(N):
+    m, u = oc_split_mesh(N), fcg.hex_mesh(N)
+    mu, phi, su = _fields(m)
+    a, su_m = oracle.laplacian(oracle_mesh(m), oracle_csr(m), mu, phi, su)
+    b, su_u = oracle.laplacian(oracle_mesh(u), oracle_csr(u), mu, np.zeros(u.numTotal), su)
+    assert len(a) == m.nnz + 2 * m.noc
+    assert np.array_equal(a[m.nnz:m.nnz + m.noc], a[m.nnz + m.noc:])  # al = ar (:218-219)
+    A, B = _operator(m, oracle_csr(m), a), _operator(u, oracle_csr(u), b)
+    assert np.abs(A - B).max() <= 1e-13 * np.abs(B).max()
+    assert np.array_equal(su_m, su_u)
+
+
+def test_oracle_solvers_take_the_pairs_where_the_reference_does():
+    """dpcg and iccg solve the cut operator; all three start from its residual
+    (res0 = sum |su - A fi| with the pairs); bicgstab's sweeps use the CSR part only."""
+    m = oc_split_mesh(6)
+    csr = oracle_csr(m)
+    mu, phi, su = _fields(m)
+    a, su = oracle.laplacian(oracle_mesh(m), csr, mu, phi, su)
+    A = _operator(m, csr, a)
+    fi0 = fcg.uniform(9, 0, m.numCells)
+    r0 = np.abs(su - A @ fi0).sum()
+    x = np.linalg.solve(A, su)
+    for solve in (oracle.dpcg, oracle.iccg):
+        r = solve(csr, a, su, fi0, 1e-13, 2000, oc=_oc(m))
+        assert r.res0 == pytest.approx(r0, rel=1e-12)
+        assert np.abs(r.fi - x).max() <= 1e-8 * np.abs(x).max()
+    r = oracle.bicgstab(csr, a, su, fi0, 1e-13, 3, oc=_oc(m))
+    assert r.res0 == pytest.approx(r0, rel=1e-12)
+    # without the pairs the first residual differs (the pairs carry the cut's couplings)
+    r_csr = oracle.bicgstab(csr, a[: m.nnz], su, fi0, 1e-13, 3)
+    assert abs(r_csr.res0 - r0) > 1e-6 * r0
+
+
+def test_oracle_dpcg_on_the_cut_mesh_gives_the_uncut_solution():
+    N = 8
+    m, u = oc_split_mesh(N), fcg.hex_mesh(N)
+    mu, phi, su = _fields(m)
+    a, su_m = oracle.laplacian(oracle_mesh(m), oracle_csr(m), mu, phi, su)
+    b, su_u = oracle.laplacian(oracle_mesh(u), oracle_csr(u), mu, np.zeros(u.numTotal), su)
+    x0 = np.zeros(m.numCells)
+    rm = oracle.dpcg(oracle_csr(m), a, su_m, x0, 1e-12, 5000, oc=_oc(m))
+    ru = oracle.dpcg(oracle_csr(u), b, su_u, x0, 1e-12, 5000)
+    assert abs(rm.iters - ru.iters) <= 2
+    assert np.abs(rm.fi - ru.fi).max() <= 1e-9 * np.abs(ru.fi).max()
+
+
+# ----------------------------------------------------------------------------- GPU
+def _gpu(N=8, cyclic=False):
+    m = oc_split_mesh(N, cyclic=cyclic)
+    return m, fcg.Context(m)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cyclic", [False, True])
+def test_laplacian_with_pairs_bit_exact(cyclic):
+    m, c = _gpu(8, cyclic)
+    mu, _, su = _fields(m)
+    phi = fcg.uniform(1, 6, m.numTotal)
+    a, su_g = c.laplacian(mu, phi, su)
+    a_o, su_o = oracle.laplacian(oracle_mesh(m), oracle_csr(m), mu, phi, su)
+    assert len(a) == m.nnz + 2 * m.noc
+    assert np.array_equal(a, a_o)
+    assert np.array_equal(su_g, su_o)
+    c.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method", ["dpcg", "iccg", "bicgstab"])
+def test_solvers_with_pairs_against_the_oracle(method):
+    """Fixed sweeps from a nonzero start: the solution and the residual norms within
+    1e-10 of the oracle's (which applies the pairs where the reference does)."""
+    m, c = _gpu(8)
+    mu, phi, su = _fields(m)
+    a, su = oracle.laplacian(oracle_mesh(m), oracle_csr(m), mu, phi, su)
+    fi0 = fcg.uniform(9, 0, m.numCells)
+    nsw = 12
+    g = getattr(c, method)(a, su, fi0, 0.0, nsw)
+    o = getattr(oracle, method)(oracle_csr(m), a, su, fi0, 0.0, nsw, oc=_oc(m))
+    assert g.iters == o.iters == nsw
+    assert g.res0 == pytest.approx(o.res0, rel=1e-12)
+    assert g.resl == pytest.approx(o.resl, rel=1e-8)
+    assert np.abs(g.fi - o.fi).max() <= 1e-10 * np.abs(o.fi).max()
+    c.close()
+
+
+@pytest.mark.gpu
+def test_dpcg_on_the_cut_mesh_gives_the_uncut_solution_and_spmv():
+    N = 16
+    m, c = _gpu(N)
+    u = fcg.hex_mesh(N)
+    cu = fcg.Context(u)
+    mu, phi, su = _fields(m)
+    a, su_m = c.laplacian(mu, phi, su)
+    b, su_u = cu.laplacian(mu, np.zeros(u.numTotal), su)
+    x0 = np.zeros(m.numCells)
+    rm = c.dpcg(a, su_m, x0, 1e-12, 20000)
+    ru = cu.dpcg(b, su_u, x0, 1e-12, 20000)
+    assert rm.converged and ru.converged and abs(rm.iters - ru.iters) <= 3
+    assert np.abs(rm.fi - ru.fi).max() <= 1e-8 * np.abs(ru.fi).max()
+    # y = A x with the pairs, against the operator of the oracle's restatement
+    x = fcg.uniform(3, 1, m.numCells)
+    y = c.spmv(a, x)
+    A = _operator(m, oracle_csr(m), a)
+    assert np.abs(y - A @ x).max() <= 1e-13 * np.abs(A @ x).max()
+    c.close()
+    cu.close()
+
+
+@pytest.mark.gpu
+def test_entry_points_without_pairs_refuse_the_mesh():
+    from freecappuccino_gb300._lib import FcgError
+
+    m, c = _gpu(6)
+    mu, phi, su = _fields(m)
+    a, su = c.laplacian(mu, phi, su)
+    with pytest.raises(FcgError) as e:
+        c.dpcg_mixed(a, su, np.zeros(m.numCells), 1e-8, 100)
+    assert e.value.status == -8
+    with pytest.raises(FcgError) as e:
+        c.grad(np.zeros(m.numTotal))
+    assert e.value.status == -8
+    c.close()
