@@ -18,7 +18,9 @@
 !   bicgstab(fi,ifi)    bicgstab.f90:1
 ! The reference's own files for these routines then drop out of its build.  Every call
 ! returns a status: a non-zero status stops the run with the library's message, which is
-! the reference's own reaction to bad input.
+! the reference's own reaction to bad input.  On a mesh with O-C grid cuts (noc > 0)
+! laplacian, dpcg, iccg and bicgstab carry the pairs (ar, al through the array aoc);
+! bpres and the other entry points stop the run with FCG_ERR_UNSUPPORTED.
 module fcgpu
   use iso_c_binding
   implicit none
@@ -35,7 +37,13 @@ module fcgpu
     integer(c_int) :: iInletFacesStart, iOutletFacesStart, iSymmetryFacesStart, &
                       iWallFacesStart, iPressOutletFacesStart, noc
     type(c_ptr) :: owner, neighbour, arx, ary, arz, xf, yf, zf, xc, yc, zc, vol, facint
+    integer(c_int) :: ncyc, iOCFacesStart
+    type(c_ptr) :: ijlFace, ijrFace
   end type
+
+  ! With O-C grid cuts (noc > 0) the library takes a matrix as one array: the CSR values
+  ! a(1:nnz), then ar(1:noc), then al(1:noc) (module sparse_matrix's ar, al).
+  real(c_double), allocatable, save :: aoc(:)
 
   ! include/fcgpu.h: fcg_solve_report
   type, bind(c) :: fcg_solve_report
@@ -156,14 +164,22 @@ contains
     integer, intent(in), optional :: device
     type(fcg_mesh_desc), target, save :: m
     integer(c_int) :: dev
+    type(c_ptr) :: pl, pr
     dev = 0
     if (present(device)) dev = device
     call fcg_check(fcg_create(fcg_ctx, dev), 'fcg_create')
+    pl = c_null_ptr
+    pr = c_null_ptr
+    if (noc > 0) then  ! noc = noc + ncyc after mesh_geometry (:1163)
+      pl = c_loc(ijlFace)
+      pr = c_loc(ijrFace)
+      allocate(aoc(nnz + 2*noc))
+    end if
     m = fcg_mesh_desc(numCells, numFaces, numInnerFaces, ninl, nout, nsym, nwal, npru, &
         iInletFacesStart, iOutletFacesStart, iSymmetryFacesStart, iWallFacesStart,     &
         iPressOutletFacesStart, noc, c_loc(owner), c_loc(neighbour), c_loc(arx),       &
         c_loc(ary), c_loc(arz), c_loc(xf), c_loc(yf), c_loc(zf), c_loc(xc), c_loc(yc), &
-        c_loc(zc), c_loc(vol), c_loc(facint))
+        c_loc(zc), c_loc(vol), c_loc(facint), ncyc, iOCFacesStart, pl, pr)
     call fcg_check(fcg_bind_mesh(fcg_ctx, m), 'fcg_bind_mesh')
     allocate(ioffset(numCells+1), ja(nnz), diag(numCells), a(nnz))
     allocate(icell_jcell_csr_value_index(numInnerFaces), jcell_icell_csr_value_index(numInnerFaces))
@@ -174,14 +190,32 @@ contains
   subroutine fcg_finish
     if (c_associated(fcg_ctx)) call fcg_check(fcg_destroy(fcg_ctx), 'fcg_destroy')
     fcg_ctx = c_null_ptr
+    if (allocated(aoc)) deallocate(aoc)
   end subroutine
 
   ! laplacian(mu,phi) (fvm_laplacian.f90:1-163): writes the module arrays a and su.
+  ! With O-C pairs also ar and al (:67-86).
   subroutine laplacian(mu, phi)
-    use types; use geometry, only: numCells, numTotal; use sparse_matrix, only: a, su
+    use types; use geometry, only: numCells, numTotal, noc
+    use sparse_matrix, only: a, su, ar, al, nnz
     real(dp), dimension(numCells), intent(in) :: mu
     real(dp), dimension(numTotal), intent(in) :: phi
-    call fcg_check(fcg_laplacian(fcg_ctx, mu, phi, a, su), 'laplacian')
+    if (noc == 0) then
+      call fcg_check(fcg_laplacian(fcg_ctx, mu, phi, a, su), 'laplacian')
+    else
+      call fcg_check(fcg_laplacian(fcg_ctx, mu, phi, aoc, su), 'laplacian')
+      a(1:nnz) = aoc(1:nnz)
+      ar(1:noc) = aoc(nnz+1:nnz+noc)
+      al(1:noc) = aoc(nnz+noc+1:nnz+2*noc)
+    end if
+  end subroutine
+
+  ! aoc = [a, ar, al] for a solve on a mesh with O-C pairs.
+  subroutine pack_oc
+    use geometry, only: noc; use sparse_matrix, only: a, ar, al, nnz
+    aoc(1:nnz) = a(1:nnz)
+    aoc(nnz+1:nnz+noc) = ar(1:noc)
+    aoc(nnz+noc+1:nnz+2*noc) = al(1:noc)
   end subroutine
 
   ! bpres(p,istage) (bpres.f90:3-152), with the module gradient dPdxi(3,numCells).
@@ -195,32 +229,50 @@ contains
   ! The solvers: same arguments and module state as dpcg/iccg/bicgstab, same stop test
   ! resl/(res0+small) < sor(ifi), resor(ifi) set, and the reference's log line.
   subroutine dpcg(fi, ifi)
-    use types; use parameters; use sparse_matrix; use title_mod
+    use types; use parameters; use sparse_matrix; use title_mod; use geometry, only: noc
     real(dp), intent(inout) :: fi(*)
     integer, intent(in) :: ifi
     type(fcg_solve_report) :: rep
-    call fcg_check(fcg_dpcg(fcg_ctx, a, su, fi, res, sor(ifi), int(nsw(ifi), c_int), &
-                            resor(ifi), rep), 'dpcg')
+    if (noc == 0) then
+      call fcg_check(fcg_dpcg(fcg_ctx, a, su, fi, res, sor(ifi), int(nsw(ifi), c_int), &
+                              resor(ifi), rep), 'dpcg')
+    else
+      call pack_oc
+      call fcg_check(fcg_dpcg(fcg_ctx, aoc, su, fi, res, sor(ifi), int(nsw(ifi), c_int), &
+                              resor(ifi), rep), 'dpcg')
+    end if
     call solver_log('PCG(Jacobi):  ', ifi, rep)
   end subroutine
 
   subroutine iccg(fi, ifi)
-    use types; use parameters; use sparse_matrix; use title_mod
+    use types; use parameters; use sparse_matrix; use title_mod; use geometry, only: noc
     real(dp), intent(inout) :: fi(*)
     integer, intent(in) :: ifi
     type(fcg_solve_report) :: rep
-    call fcg_check(fcg_iccg(fcg_ctx, a, su, fi, res, sor(ifi), int(nsw(ifi), c_int), &
-                            resor(ifi), rep), 'iccg')
+    if (noc == 0) then
+      call fcg_check(fcg_iccg(fcg_ctx, a, su, fi, res, sor(ifi), int(nsw(ifi), c_int), &
+                              resor(ifi), rep), 'iccg')
+    else
+      call pack_oc
+      call fcg_check(fcg_iccg(fcg_ctx, aoc, su, fi, res, sor(ifi), int(nsw(ifi), c_int), &
+                              resor(ifi), rep), 'iccg')
+    end if
     call solver_log('  PCG(IC0):  ', ifi, rep)
   end subroutine
 
   subroutine bicgstab(fi, ifi)
-    use types; use parameters; use sparse_matrix; use title_mod
+    use types; use parameters; use sparse_matrix; use title_mod; use geometry, only: noc
     real(dp), intent(inout) :: fi(*)
     integer, intent(in) :: ifi
     type(fcg_solve_report) :: rep
-    call fcg_check(fcg_bicgstab(fcg_ctx, a, su, fi, res, sor(ifi), int(nsw(ifi), c_int), &
-                                resor(ifi), rep), 'bicgstab')
+    if (noc == 0) then
+      call fcg_check(fcg_bicgstab(fcg_ctx, a, su, fi, res, sor(ifi), int(nsw(ifi), c_int), &
+                                  resor(ifi), rep), 'bicgstab')
+    else
+      call pack_oc
+      call fcg_check(fcg_bicgstab(fcg_ctx, aoc, su, fi, res, sor(ifi), int(nsw(ifi), c_int), &
+                                  resor(ifi), rep), 'bicgstab')
+    end if
     call solver_log('  BiCGStab(ILU(0)):  ', ifi, rep)
   end subroutine
 
