@@ -259,9 +259,10 @@ extern "C" int fcg_bind_mesh(fcg_context *c, const fcg_mesh_desc *m) {
     return set_error(c, FCG_ERR_ARG, "noc or ncyc out of range");
   if (m->noc > 0 && (!m->ijlFace || !m->ijrFace))
     return set_error(c, FCG_ERR_ARG, "noc > 0 without ijlFace / ijrFace");
-  if (m->noc > 0 && (m->iOCFacesStart < m->numInnerFaces ||
-                     (long long)m->iOCFacesStart + m->noc > m->numFaces))
-    return set_error(c, FCG_ERR_INDEX, "iOCFacesStart + noc is outside the boundary faces");
+  // faces iOCFacesStart + 1 .. + noc give the pairs' areas (fvm_laplacian.f90:70); with
+  // cyclic pairs only the start stays 0, as the reference leaves it
+  if (m->noc > 0 && (m->iOCFacesStart < 0 || (long long)m->iOCFacesStart + m->noc > m->numFaces))
+    return set_error(c, FCG_ERR_INDEX, "iOCFacesStart + noc is outside the faces");
   const double *dp[] = {m->arx, m->ary, m->arz, m->xf, m->yf, m->zf, m->xc, m->yc, m->zc, m->vol};
   for (const double *p : dp)
     if (!p) return set_error(c, FCG_ERR_ARG, "NULL geometry array in fcg_mesh_desc");

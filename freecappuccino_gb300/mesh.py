@@ -250,21 +250,48 @@ def polymesh_mesh(points, face_ptr, face_nodes, owner, neighbour, numCells, patc
            "symmetry": ("nsym", "iSymmetryFacesStart"), "prOutlet": ("npru", "iPressOutletFacesStart")}
     for t in _WALL_ALIASES:
         key[t] = ("nwal", "iWallFacesStart")
+    # 'domain' (O-C grid cut) and 'cyclic' patches come in pairs of lines, a patch and its
+    # friend of as many faces; face k of one is matched with face k of the other
+    # (mesh_geometry_and_topology.f90:453-462, 800-845).  The O-C pairs come first, then
+    # the cyclic ones (:1163); iOCFacesStart is the start of the first 'domain' patch.
+    pairs = {"domain": [], "cyclic": []}
+    pend, oc_start = None, None
     for t, cnt, st in zip(patch_type, patch_nfaces, patch_start):
         t = str(t)
+        if t in pairs:
+            if pend is None:
+                pend = (t, int(cnt), int(st))
+                if t == "domain" and oc_start is None:
+                    oc_start = int(st)
+            else:
+                if pend[0] != t or pend[1] != int(cnt):
+                    raise ValueError(f"a {pend[0]!r} patch of {pend[1]} faces is followed by "
+                                     f"{t!r} of {int(cnt)}, not by its friend")
+                pairs[t].append((pend[2], int(st), pend[1]))
+                pend = None
+            continue
         if t not in key:
-            raise ValueError(f"boundary type {t!r} is not supported (O-C and cyclic faces)")
+            raise ValueError(f"boundary type {t!r} is not supported")
         c, s = key[t]
         if counts[c] == 0:
             starts[s] = int(st)
         counts[c] += int(cnt)
+    if pend is not None:
+        raise ValueError(f"a {pend[0]!r} patch without its friend")
+    runs = pairs["domain"] + pairs["cyclic"]
+    ijl = [s0 + 1 + k for s0, _, c in runs for k in range(c)]
+    ijr = [s1 + 1 + k for _, s1, c in runs for k in range(c)]
     geo = compute_geometry if device is None else (
         lambda *a: compute_geometry_gpu(*a, device=device))
     g = geo(points, face_ptr, face_nodes, owner, neighbour, int(numCells))
     return Mesh(int(numCells), len(face_ptr) - 1, len(neighbour),
                 np.ascontiguousarray(owner, np.int32), np.ascontiguousarray(neighbour, np.int32),
                 **g, counts=counts, starts=starts, points=np.asarray(points),
-                face_ptr=np.asarray(face_ptr, np.int32), face_nodes=np.asarray(face_nodes, np.int32))
+                face_ptr=np.asarray(face_ptr, np.int32), face_nodes=np.asarray(face_nodes, np.int32),
+                noc=len(ijl), ncyc=sum(c for _, _, c in pairs["cyclic"]),
+                iOCFacesStart=oc_start or 0,
+                ijlFace=np.array(ijl, np.int32) if ijl else None,
+                ijrFace=np.array(ijr, np.int32) if ijr else None)
 
 
 def uniform(seed: int, stream: int, count: int, lo: float = -1.0, hi: float = 1.0) -> np.ndarray:

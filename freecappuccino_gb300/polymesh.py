@@ -195,3 +195,24 @@ def write_polymesh(m: Mesh, path: str):
         f.write("# type nFaces startFace\n")
         for st, t, c in rows:
             f.write(f"{t} {c} {st}\n")
+        for t, st, st_friend, c in _pair_patches(m):
+            f.write(f"{t} {c} {st}\n{t} {c} {st_friend}\n")
+
+
+def _pair_patches(m: Mesh):
+    """The O-C and cyclic pairs of a mesh as patch pairs (type, start, friend start, count):
+    runs of pairs whose faces and friend faces are both consecutive."""
+    if not getattr(m, "noc", 0):
+        return []
+    ijl = np.asarray(m.ijlFace, np.int64) - 1
+    ijr = np.asarray(m.ijrFace, np.int64) - 1
+    out, i = [], 0
+    while i < m.noc:
+        t = "domain" if i < m.noc - m.ncyc else "cyclic"
+        j = i + 1
+        while (j < m.noc and (j < m.noc - m.ncyc) == (i < m.noc - m.ncyc)
+               and ijl[j] == ijl[j - 1] + 1 and ijr[j] == ijr[j - 1] + 1):
+            j += 1
+        out.append((t, int(ijl[i]), int(ijr[i]), j - i))
+        i = j
+    return out

@@ -34,7 +34,7 @@ def oc_split_mesh(N: int, kc: int | None = None, jitter: float = 0.0, seed: int 
     'cyclic' with cyclic=True): every cut face becomes a left face owned by the cell
     below and a friend face owned by the cell above (area reversed), both after the other
     boundary faces, left faces first (iOCFacesStart)."""
-    m = fcg.hex_mesh(N, jitter=jitter, seed=seed)
+    m = fcg.hex_mesh(N, jitter=jitter, seed=seed, keep_topology=True)
     nin, nf = m.numInnerFaces, m.numFaces
     own0, nb0 = m.owner[:nin] - 1, m.neighbour - 1
     kc = N // 2 if kc is None else kc
@@ -56,6 +56,12 @@ def oc_split_mesh(N: int, kc: int | None = None, jitter: float = 0.0, seed: int 
     out.noc, out.ncyc, out.iOCFacesStart = noc, noc if cyclic else 0, start
     out.ijlFace = (start + 1 + np.arange(noc)).astype(np.int32)
     out.ijrFace = (start + 1 + noc + np.arange(noc)).astype(np.int32)
+    # the faces' nodes in the new order, the friend faces' reversed
+    fp, fn = m.face_ptr, m.face_nodes
+    rows = [fn[fp[f]:fp[f + 1]][::int(s)] for f, s in zip(src, flip)]
+    out.points = m.points
+    out.face_ptr = np.concatenate([[0], np.cumsum([len(r) for r in rows])]).astype(np.int32)
+    out.face_nodes = np.concatenate(rows).astype(np.int32)
     return out
 
 
