@@ -19,8 +19,8 @@
 ! The reference's own files for these routines then drop out of its build.  Every call
 ! returns a status: a non-zero status stops the run with the library's message, which is
 ! the reference's own reaction to bad input.  On a mesh with O-C grid cuts (noc > 0)
-! laplacian, dpcg, iccg and bicgstab carry the pairs (ar, al through the array aoc);
-! bpres and the other entry points stop the run with FCG_ERR_UNSUPPORTED.
+! laplacian, bpres, dpcg, iccg and bicgstab carry the pairs (ar, al through the array
+! aoc); the face-flux entry points stop the run with FCG_ERR_UNSUPPORTED.
 module fcgpu
   use iso_c_binding
   implicit none

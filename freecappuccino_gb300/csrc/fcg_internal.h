@@ -183,7 +183,8 @@ int oc_geometry(fcg_context *c);
 inline int refuse_oc(fcg_context *c, const char *what) {
   return c->mv.noc ? set_error(c, FCG_ERR_UNSUPPORTED,
                                std::string(what) + ": O-C grid cuts and cyclic faces (noc > 0)"
-                                                   " are supported by fcg_laplacian, fcg_dpcg,"
+                                                   " are supported by fcg_laplacian, fcg_grad,"
+                                                   " fcg_grad_lsq_matrix, fcg_bpres, fcg_dpcg,"
                                                    " fcg_iccg, fcg_bicgstab and fcg_spmv only")
                    : FCG_OK;
 }

@@ -36,8 +36,30 @@ __global__ void k_gauss_faces(MeshView m, const double *__restrict__ fi,
   }
 }
 
+// The same on the O-C pairs (grad_gauss.f90:60-67): face ijlFace(i), factor foc(i).
+__global__ void k_gauss_oc(MeshView m, const double *__restrict__ fi,
+                           const double *__restrict__ gold, double *__restrict__ dfo) {
+  FCG_GRID_STRIDE(i, m.noc) {
+    const int p = m.oc_l[i], q = m.oc_r[i], f = m.oc_fl[i];
+    double fxn = m.oc_foc[i];
+    double fxp = 1.0 - fxn;
+    double xi = m.xc[p] * fxp + m.xc[q] * fxn;
+    double yi = m.yc[p] * fxp + m.yc[q] * fxn;
+    double zi = m.zc[p] * fxp + m.zc[q] * fxn;
+    double dfxi = gold[3 * p] * fxp + gold[3 * q] * fxn;
+    double dfyi = gold[3 * p + 1] * fxp + gold[3 * q + 1] * fxn;
+    double dfzi = gold[3 * p + 2] * fxp + gold[3 * q + 2] * fxn;
+    double fie = fi[p] * fxp + fi[q] * fxn + dfxi * (m.xf[f] - xi) + dfyi * (m.yf[f] - yi) +
+                 dfzi * (m.zf[f] - zi);
+    dfo[i] = fie * m.arx[f];
+    dfo[m.noc + i] = fie * m.ary[f];
+    dfo[2LL * m.noc + i] = fie * m.arz[f];
+  }
+}
+
 __global__ void k_gauss_cells(MeshView m, const double *__restrict__ fi,
-                              const double *__restrict__ dfe, double *__restrict__ g) {
+                              const double *__restrict__ dfe, const double *__restrict__ dfo,
+                              double *__restrict__ g) {
   FCG_GRID_STRIDE(c, m.n) {
     double gx = 0.0, gy = 0.0, gz = 0.0;
     for (int e = m.cf_ptr[c]; e < m.cf_ptr[c + 1]; ++e) {
@@ -54,6 +76,21 @@ __global__ void k_gauss_cells(MeshView m, const double *__restrict__ fi,
         gz = gz - ez;
       }
     }
+    if (m.noc)  // the O-C pairs after the inner faces, + on the left cell, - on the right
+      for (int e = m.oc_cptr[c]; e < m.oc_cptr[c + 1]; ++e) {
+        const int v = m.oc_vix[e];
+        const long long i = v < m.noc ? v : v - m.noc;
+        double ex = dfo[i], ey = dfo[m.noc + i], ez = dfo[2LL * m.noc + i];
+        if (v < m.noc) {
+          gx = gx + ex;
+          gy = gy + ey;
+          gz = gz + ez;
+        } else {
+          gx = gx - ex;
+          gy = gy - ey;
+          gz = gz - ez;
+        }
+      }
     for (int e = m.cb_ptr[c]; e < m.cb_ptr[c + 1]; ++e) {
       int f = m.cb_face[e];
       double fb = fi[m.cb_slot[e]];
@@ -85,6 +122,18 @@ __global__ void k_lsq_matrix(MeshView m, double *__restrict__ dmat) {
       d13 = d13 + Dx * Dz;
       d23 = d23 + Dy * Dz;
     }
+    if (m.noc)  // the O-C pairs (:85-108)
+      for (int e = m.oc_cptr[c]; e < m.oc_cptr[c + 1]; ++e) {
+        const int v = m.oc_vix[e], i = v < m.noc ? v : v - m.noc;
+        const int p = m.oc_l[i], q = m.oc_r[i];
+        double Dx = m.xc[q] - m.xc[p], Dy = m.yc[q] - m.yc[p], Dz = m.zc[q] - m.zc[p];
+        d11 = d11 + Dx * Dx;
+        d22 = d22 + Dy * Dy;
+        d33 = d33 + Dz * Dz;
+        d12 = d12 + Dx * Dy;
+        d13 = d13 + Dx * Dz;
+        d23 = d23 + Dy * Dz;
+      }
     for (int e = m.cbf_ptr[c]; e < m.cbf_ptr[c + 1]; ++e) {
       int f = m.cbf_face[e];
       double Dx = m.xf[f] - m.xc[c], Dy = m.yf[f] - m.yc[c], Dz = m.zf[f] - m.zc[c];
@@ -125,6 +174,15 @@ __global__ void k_lsq_cells(MeshView m, const double *__restrict__ fi,
       b2 = b2 + (m.yc[q] - m.yc[p]) * df;
       b3 = b3 + (m.zc[q] - m.zc[p]) * df;
     }
+    if (m.noc)  // the O-C pairs (:198-214)
+      for (int e = m.oc_cptr[c]; e < m.oc_cptr[c + 1]; ++e) {
+        const int v = m.oc_vix[e], i = v < m.noc ? v : v - m.noc;
+        const int p = m.oc_l[i], q = m.oc_r[i];
+        double df = fi[q] - fi[p];
+        b1 = b1 + (m.xc[q] - m.xc[p]) * df;
+        b2 = b2 + (m.yc[q] - m.yc[p]) * df;
+        b3 = b3 + (m.zc[q] - m.zc[p]) * df;
+      }
     for (int e = m.cb_ptr[c]; e < m.cb_ptr[c + 1]; ++e) {
       int f = m.cb_face[e];
       double df = fi[m.cb_slot[e]] - fi[c];
@@ -153,6 +211,22 @@ __global__ void k_bpres(MeshView m, long long nbent, double *__restrict__ p,
   }
 }
 
+// bpres on the O-C slots (:89-95, :134-148): slot s0 + i takes the value of the owner of
+// face iOCFacesStart + i; from stage 2 on, extrapolated over the distance from the
+// centre of face i, as :140-142 write it.
+__global__ void k_bpres_oc(MeshView m, long long s0, double *__restrict__ p,
+                           const double *__restrict__ dP, int istage) {
+  FCG_GRID_STRIDE(i, m.noc) {
+    const int c = m.owner[m.oc_start + i];
+    if (istage == 1) {
+      p[s0 + i] = p[c];
+    } else {
+      double xpb = m.xf[i] - m.xc[c], ypb = m.yf[i] - m.yc[c], zpb = m.zf[i] - m.zc[c];
+      p[s0 + i] = p[c] + dP[3 * c] * xpb + dP[3 * c + 1] * ypb + dP[3 * c + 2] * zpb;
+    }
+  }
+}
+
 int ensure_lsq_matrix(fcg_context *c) {
   if (c->dmat_ready) return FCG_OK;
   FCG_CUDA_TRY(c, c->dmat.ensure(sizeof(double) * 9 * (size_t)c->n));
@@ -167,7 +241,6 @@ int ensure_lsq_matrix(fcg_context *c) {
 extern "C" int fcg_grad_lsq_matrix(fcg_context *c, double *dmat) {
   if (!c) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_grad_lsq_matrix before fcg_bind_mesh");
-  if (c->mv.noc) return refuse_oc(c, "fcg_grad_lsq_matrix");
   FCG_CUDA_TRY(c, cudaSetDevice(c->device));
   c->dmat_ready = false;
   int rc = ensure_lsq_matrix(c);
@@ -184,7 +257,6 @@ extern "C" int fcg_grad(fcg_context *c, const double *phi, double *dPhidxi, int 
                         int nigrad) {
   if (!c) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_grad before fcg_bind_mesh");
-  if (c->mv.noc) return refuse_oc(c, "fcg_grad");
   if (method != FCG_GRAD_GAUSS && method != FCG_GRAD_GAUSS_CORRECTED && method != FCG_GRAD_LSQ)
     return set_error(c, FCG_ERR_ARG, "unknown gradient method");
   if (method == FCG_GRAD_GAUSS && nigrad < 1)
@@ -204,11 +276,12 @@ extern "C" int fcg_grad(fcg_context *c, const double *phi, double *dPhidxi, int 
                                             (double *)dg);
     FCG_CHECK_LAUNCH(c, "k_lsq_cells");
   } else {
-    // scratch: dfe[3*nin] | old gradient [3n] | new gradient [3n]
-    size_t nin3 = 3 * (size_t)(m.nin > 0 ? m.nin : 1);
-    FCG_CUDA_TRY(c, c->scratch.ensure(sizeof(double) * nin3 + 2 * n3));
+    // scratch: dfe[3*nin] | old gradient [3n] | new gradient [3n] | O-C terms [3*noc]
+    size_t nin3 = 3 * (size_t)(m.nin > 0 ? m.nin : 1), noc3 = 3 * (size_t)m.noc;
+    FCG_CUDA_TRY(c, c->scratch.ensure(sizeof(double) * (nin3 + noc3) + 2 * n3));
     double *dfe = c->scratch.as<double>();
     double *gA = dfe + nin3, *gB = gA + 3 * (size_t)m.n;
+    double *dfo = gB + 3 * (size_t)m.n;
     int passes = method == FCG_GRAD_GAUSS_CORRECTED ? 1 : nigrad;
     const double *gold = gA;
     if (method == FCG_GRAD_GAUSS_CORRECTED) {
@@ -222,7 +295,12 @@ extern "C" int fcg_grad(fcg_context *c, const double *phi, double *dPhidxi, int 
         k_gauss_faces<<<gf, kTPB, 0, c->stream>>>(m, (const double *)dphi, gold, dfe);
         FCG_CHECK_LAUNCH(c, "k_gauss_faces");
       }
-      k_gauss_cells<<<gc, kTPB, 0, c->stream>>>(m, (const double *)dphi, dfe, gnew);
+      if (m.noc > 0) {
+        k_gauss_oc<<<grid_for(m.noc, c->num_sms), kTPB, 0, c->stream>>>(m, (const double *)dphi,
+                                                                         gold, dfo);
+        FCG_CHECK_LAUNCH(c, "k_gauss_oc");
+      }
+      k_gauss_cells<<<gc, kTPB, 0, c->stream>>>(m, (const double *)dphi, dfe, dfo, gnew);
       FCG_CHECK_LAUNCH(c, "k_gauss_cells");
       gold = gnew;  // :116-120
     }
@@ -236,7 +314,6 @@ extern "C" int fcg_grad(fcg_context *c, const double *phi, double *dPhidxi, int 
 extern "C" int fcg_bpres(fcg_context *c, double *p, const double *dPdxi, int istage) {
   if (!c) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_bpres before fcg_bind_mesh");
-  if (c->mv.noc) return refuse_oc(c, "fcg_bpres");
   if (istage < 1) return set_error(c, FCG_ERR_ARG, "istage must be >= 1");
   FCG_CUDA_TRY(c, cudaSetDevice(c->device));
   void *dp, *dg = nullptr;
@@ -252,6 +329,11 @@ extern "C" int fcg_bpres(fcg_context *c, double *p, const double *dPdxi, int ist
     k_bpres<<<grid_for(nbent, c->num_sms), kTPB, 0, c->stream>>>(c->mv, nbent, (double *)dp,
                                                                    (const double *)dg, istage);
     FCG_CHECK_LAUNCH(c, "k_bpres");
+  }
+  if (c->mv.noc > 0) {  // the O-C slots follow the typed ones (iOCStart, :603)
+    k_bpres_oc<<<grid_for(c->mv.noc, c->num_sms), kTPB, 0, c->stream>>>(
+        c->mv, (long long)c->n + nbent, (double *)dp, (const double *)dg, istage);
+    FCG_CHECK_LAUNCH(c, "k_bpres_oc");
   }
   if ((rc = stage_out(c, p, dp, sizeof(double) * c->ntot, hp))) return rc;
   if (hp) FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));

@@ -86,8 +86,9 @@ typedef struct fcg_mesh_desc {
    * take the area of pair i from face iOCFacesStart + i (0-based start, i 1-based;
    * fvm_laplacian.f90:70): the start of the first 'domain' patch, 0 without one.  With noc > 0 a matrix `a` holds nnz + 2 noc values: the
    * CSR values, then ar(1..noc), then al(1..noc) (module sparse_matrix's al, ar).
-   * fcg_laplacian, fcg_dpcg, fcg_iccg, fcg_bicgstab and fcg_spmv take the pairs; every
-   * other entry point returns FCG_ERR_UNSUPPORTED on such a mesh. */
+   * fcg_laplacian, fcg_grad, fcg_grad_lsq_matrix, fcg_bpres, fcg_dpcg, fcg_iccg,
+   * fcg_bicgstab and fcg_spmv take the pairs; every other entry point returns
+   * FCG_ERR_UNSUPPORTED on such a mesh. */
   int ncyc;
   int iOCFacesStart;
   const int *ijlFace, *ijrFace; /* [noc] */

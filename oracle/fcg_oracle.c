@@ -241,6 +241,19 @@ static int iPressOutletStart(const orc_mesh *m) {
 /* a2: fvm_laplacian.f90                                                      */
 /* ------------------------------------------------------------------------- */
 
+/* The pairs' cells and interpolation factors in freshly allocated arrays (free_oc). */
+typedef struct { int *ijl, *ijr; double *foc, *srdoc; } oc_pairs;
+int orc_oc_geometry(const orc_mesh *m, int *ijl, int *ijr, double *foc, double *srdoc);
+static int get_oc(const orc_mesh *m, oc_pairs *o) {
+  size_t k = (size_t)(m->noc > 0 ? m->noc : 1);
+  o->ijl = malloc(sizeof(int) * k), o->ijr = malloc(sizeof(int) * k);
+  o->foc = malloc(sizeof(double) * k), o->srdoc = malloc(sizeof(double) * k);
+  if (!o->ijl || !o->ijr || !o->foc || !o->srdoc) return -1;
+  if (m->noc > 0) orc_oc_geometry(m, o->ijl, o->ijr, o->foc, o->srdoc);
+  return 0;
+}
+static void free_oc(oc_pairs *o) { free(o->ijl), free(o->ijr), free(o->foc), free(o->srdoc); }
+
 int orc_oc_geometry(const orc_mesh *m, int *ijl, int *ijr, double *foc, double *srdoc) {
   int nreg = m->noc - m->ncyc;
   for (int i = 1; i <= m->noc; ++i) {
@@ -490,6 +503,32 @@ static void gauss_pass(const orc_mesh *m, const double *fi, const double *dfxo,
     F(dfy, ijn) = F(dfy, ijn) - dfye;
     F(dfz, ijn) = F(dfz, ijn) - dfze;
   }
+  if (m->noc > 0) { /* O- and C-grid cuts (:60-67): gradco on face ijlFace(i) with foc(i) */
+    oc_pairs oc;
+    if (get_oc(m, &oc)) return;
+    for (int i = 1; i <= m->noc; ++i) {
+      int iface = F(m->ijlFace, i), ijp = F(oc.ijl, i), ijn = F(oc.ijr, i);
+      double fxn = F(oc.foc, i);
+      double fxp = 1.0 - fxn;
+      double xi = F(m->xc, ijp) * fxp + F(m->xc, ijn) * fxn;
+      double yi = F(m->yc, ijp) * fxp + F(m->yc, ijn) * fxn;
+      double zi = F(m->zc, ijp) * fxp + F(m->zc, ijn) * fxn;
+      double dfxi = F(dfxo, ijp) * fxp + F(dfxo, ijn) * fxn;
+      double dfyi = F(dfyo, ijp) * fxp + F(dfyo, ijn) * fxn;
+      double dfzi = F(dfzo, ijp) * fxp + F(dfzo, ijn) * fxn;
+      double fie = F(fi, ijp) * fxp + F(fi, ijn) * fxn + dfxi * (F(m->xf, iface) - xi) +
+                   dfyi * (F(m->yf, iface) - yi) + dfzi * (F(m->zf, iface) - zi);
+      double dfxe = fie * F(m->arx, iface), dfye = fie * F(m->ary, iface),
+             dfze = fie * F(m->arz, iface);
+      F(dfx, ijp) = F(dfx, ijp) + dfxe;
+      F(dfy, ijp) = F(dfy, ijp) + dfye;
+      F(dfz, ijp) = F(dfz, ijp) + dfze;
+      F(dfx, ijn) = F(dfx, ijn) - dfxe;
+      F(dfy, ijn) = F(dfy, ijn) - dfye;
+      F(dfz, ijn) = F(dfz, ijn) - dfze;
+    }
+    free_oc(&oc);
+  }
   /* Boundary loops :70-103 in patch-type order; gradbc :194-211. */
   const int cnt[5] = {m->ninl, m->nout, m->nsym, m->nwal, m->npru};
   const int fst[5] = {m->iInletFacesStart, m->iOutletFacesStart, m->iSymmetryFacesStart,
@@ -575,6 +614,29 @@ int orc_grad_lsq_matrix(const orc_mesh *m, double *dmat) {
     DM(5, ijp) += Dy * Dz;
     DM(5, ijn) += Dy * Dz;
   }
+  if (m->noc > 0) { /* faces along O-C grid cuts (:85-108) */
+    oc_pairs oc;
+    if (get_oc(m, &oc)) return -1;
+    for (int i = 1; i <= m->noc; ++i) {
+      int ijp = F(oc.ijl, i), ijn = F(oc.ijr, i);
+      double Dx = F(m->xc, ijn) - F(m->xc, ijp);
+      double Dy = F(m->yc, ijn) - F(m->yc, ijp);
+      double Dz = F(m->zc, ijn) - F(m->zc, ijp);
+      DM(1, ijp) += Dx * Dx;
+      DM(1, ijn) += Dx * Dx;
+      DM(4, ijp) += Dy * Dy;
+      DM(4, ijn) += Dy * Dy;
+      DM(6, ijp) += Dz * Dz;
+      DM(6, ijn) += Dz * Dz;
+      DM(2, ijp) += Dx * Dy;
+      DM(2, ijn) += Dx * Dy;
+      DM(3, ijp) += Dx * Dz;
+      DM(3, ijn) += Dx * Dz;
+      DM(5, ijp) += Dy * Dz;
+      DM(5, ijn) += Dy * Dz;
+    }
+    free_oc(&oc);
+  }
   int nbf = m->numFaces - m->numInnerFaces;
   for (int i = 1; i <= nbf; ++i) { /* :116-130 */
     int iface = m->numInnerFaces + i;
@@ -625,6 +687,23 @@ int orc_grad_lsq(const orc_mesh *m, const double *fi, const double *dmat, double
     F(b3, ijp) += Dz;
     F(b3, ijn) += Dz;
   }
+  if (m->noc > 0) { /* faces along O-C grid cuts (:198-214) */
+    oc_pairs oc;
+    if (get_oc(m, &oc)) return -1;
+    for (int i = 1; i <= m->noc; ++i) {
+      int ijp = F(oc.ijl, i), ijn = F(oc.ijr, i);
+      double Dx = (F(m->xc, ijn) - F(m->xc, ijp)) * (F(fi, ijn) - F(fi, ijp));
+      double Dy = (F(m->yc, ijn) - F(m->yc, ijp)) * (F(fi, ijn) - F(fi, ijp));
+      double Dz = (F(m->zc, ijn) - F(m->zc, ijp)) * (F(fi, ijn) - F(fi, ijp));
+      F(b1, ijp) += Dx;
+      F(b1, ijn) += Dx;
+      F(b2, ijp) += Dy;
+      F(b2, ijn) += Dy;
+      F(b3, ijp) += Dz;
+      F(b3, ijn) += Dz;
+    }
+    free_oc(&oc);
+  }
   const int cnt[5] = {m->ninl, m->nout, m->nsym, m->nwal, m->npru};
   const int fst[5] = {m->iInletFacesStart, m->iOutletFacesStart, m->iSymmetryFacesStart,
                       m->iWallFacesStart, m->iPressOutletFacesStart};
@@ -662,9 +741,13 @@ int orc_bpres(const orc_mesh *m, double *p, const double *dPdxi, int istage) {
                       m->iWallFacesStart, m->iPressOutletFacesStart};
   const int bst[5] = {iInletStart(m), iOutletStart(m), iSymmetryStart(m), iWallStart(m),
                       iPressOutletStart(m)};
+  /* the O-C slots follow the pressure-outlet ones (iOCStart, :603) */
+  const int ocst = iPressOutletStart(m) + m->npru;
   if (istage == 1) { /* :37-96: every boundary slot takes its owner value */
     for (int t = 0; t < 5; ++t)
       for (int i = 1; i <= cnt[t]; ++i) F(p, bst[t] + i) = F(p, F(m->owner, fst[t] + i));
+    for (int i = 1; i <= m->noc; ++i) /* :89-95 */
+      F(p, ocst + i) = F(p, F(m->owner, m->iOCFacesStart + i));
   } else { /* :98-148: wall and pressure-outlet slots are extrapolated */
     for (int t = 3; t < 5; ++t)
       for (int i = 1; i <= cnt[t]; ++i) {
@@ -676,6 +759,15 @@ int orc_bpres(const orc_mesh *m, double *p, const double *dPdxi, int istage) {
         F(p, bst[t] + i) = F(p, ijp) + G3(dPdxi, 1, ijp) * xpb + G3(dPdxi, 2, ijp) * ypb +
                            G3(dPdxi, 3, ijp) * zpb;
       }
+    for (int i = 1; i <= m->noc; ++i) { /* O-C grid cuts :134-148 */
+      int ijp = F(m->owner, m->iOCFacesStart + i);
+      /* the distance is taken from face i's centre, as :140-142 write it */
+      double xpb = F(m->xf, i) - F(m->xc, ijp);
+      double ypb = F(m->yf, i) - F(m->yc, ijp);
+      double zpb = F(m->zf, i) - F(m->zc, ijp);
+      F(p, ocst + i) = F(p, ijp) + G3(dPdxi, 1, ijp) * xpb + G3(dPdxi, 2, ijp) * ypb +
+                       G3(dPdxi, 3, ijp) * zpb;
+    }
   }
   return 0;
 }

@@ -117,6 +117,26 @@ def test_oracle_dpcg_on_the_cut_mesh_gives_the_uncut_solution():
     assert np.abs(rm.fi - ru.fi).max() <= 1e-9 * np.abs(ru.fi).max()
 
 
+def test_oracle_gauss_gradient_of_the_cut_mesh_is_the_uncut_one():
+    """The pairs carry the cut faces' Gauss terms (grad_gauss.f90:60-67): the gradient of a
+    field on the cut mesh is the uncut mesh's up to the rounding of foc; the O-C slots of
+    bpres take the owner values (stage 1)."""
+    N = 8
+    m, u = oc_split_mesh(N), fcg.hex_mesh(N)
+    phi_c = fcg.uniform(2, 1, m.numCells)
+    pm = np.concatenate([phi_c, np.zeros(m.numTotal - m.numCells)])
+    pu = np.concatenate([phi_c, np.zeros(u.numTotal - u.numCells)])
+    # boundary values as bpres stage 1 gives them, on both meshes
+    pm = oracle.bpres(oracle_mesh(m), pm, None, 1)
+    pu = oracle.bpres(oracle_mesh(u), pu, None, 1)
+    ocs = m.boundary_slot_start("prOutlet") + m.counts.get("npru", 0)
+    assert np.array_equal(pm[ocs:ocs + m.noc], phi_c[m.owner[m.iOCFacesStart:m.iOCFacesStart + m.noc] - 1])
+    for nigrad in (1, 2):
+        gm = oracle.grad_gauss(oracle_mesh(m), pm, nigrad=nigrad)
+        gu = oracle.grad_gauss(oracle_mesh(u), pu, nigrad=nigrad)
+        assert np.abs(gm - gu).max() <= 1e-12 * np.abs(gu).max()
+
+
 # ----------------------------------------------------------------------------- GPU
 def _gpu(N=8, cyclic=False):
     m = oc_split_mesh(N, cyclic=cyclic)
@@ -180,8 +200,33 @@ def test_dpcg_on_the_cut_mesh_gives_the_uncut_solution_and_spmv():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("cyclic", [False, True])
+def test_gradients_and_bpres_with_pairs_bit_exact(cyclic):
+    """Gauss (1 and 2 passes), corrected Gauss, least squares and both bpres stages on the
+    cut mesh, bit for bit against the oracle."""
+    m, c = _gpu(8, cyclic)
+    om = oracle_mesh(m)
+    phi = fcg.uniform(2, 1, m.numTotal)
+    for nigrad in (1, 2):
+        assert np.array_equal(c.grad(phi, "gauss", nigrad=nigrad),
+                              oracle.grad_gauss(om, phi, nigrad=nigrad))
+    g0 = fcg.uniform(2, 3, 3 * m.numCells).reshape(-1, 3)
+    assert np.array_equal(c.grad(phi, "gauss_corrected", dphidxi=g0),
+                          oracle.grad_gauss(om, phi, corrected=True, dphidxi_in=g0))
+    d_o = oracle.grad_lsq_matrix(om)
+    assert np.array_equal(c.grad_lsq_matrix(), d_o)
+    assert np.array_equal(c.grad(phi, "lsq"), oracle.grad_lsq(om, phi, d_o))
+    p = fcg.uniform(3, 1, m.numTotal)
+    g = fcg.uniform(3, 2, 3 * m.numCells).reshape(-1, 3)
+    for stage in (1, 2):
+        assert np.array_equal(c.bpres(p, g, stage), oracle.bpres(om, p, g, stage))
+    c.close()
+
+
+@pytest.mark.gpu
 def test_entry_points_without_pairs_refuse_the_mesh():
     from freecappuccino_gb300._lib import FcgError
+    from tests.meshes import seeded_fields
 
     m, c = _gpu(6)
     mu, phi, su = _fields(m)
@@ -190,7 +235,7 @@ def test_entry_points_without_pairs_refuse_the_mesh():
         c.dpcg_mixed(a, su, np.zeros(m.numCells), 1e-8, 100)
     assert e.value.status == -8
     with pytest.raises(FcgError) as e:
-        c.grad(np.zeros(m.numTotal))
+        c.facefluxmass(**seeded_fields(m))
     assert e.value.status == -8
     c.close()
 
