@@ -20,7 +20,7 @@
 ! returns a status: a non-zero status stops the run with the library's message, which is
 ! the reference's own reaction to bad input.  On a mesh with O-C grid cuts (noc > 0)
 ! laplacian, bpres, dpcg, iccg and bicgstab carry the pairs (ar, al through the array
-! aoc); the face-flux entry points stop the run with FCG_ERR_UNSUPPORTED.
+! aoc); the face-flux calls take flmass followed by fmoc in one array.
 module fcgpu
   use iso_c_binding
   implicit none

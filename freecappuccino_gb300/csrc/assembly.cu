@@ -239,8 +239,74 @@ __global__ void k_ffm_faces(MeshView m, const double *__restrict__ g, FlowView f
   }
 }
 
+// facefluxmass.f90:34-199 on the face between p and q with centre (xf, yf, zf), area
+// (arx, ary, arz) and factor lambda, computed in place (the O-C pairs have no cached face
+// factors): cap, can and the mass flux, with the operations of k_ffm_faces and the
+// factors k_face_geo caches.
+__device__ void ffm_face(const MeshView &m, const FlowView &fl, int p, int q, double xf,
+                         double yf, double zf, double arx, double ary, double arz,
+                         double lambda, double &cap, double &can, double &fm) {
+  double fxn = lambda;
+  double fxp = 1.0 - fxn;
+  double xpn = m.xc[q] - m.xc[p], ypn = m.yc[q] - m.yc[p], zpn = m.zc[q] - m.zc[p];
+  double are = sqrt(arx * arx + ary * ary + arz * arz);
+  double nxx = arx / are, nyy = ary / are, nzz = arz / are;
+  double Dpu = fxn * m.vol[q] * fl.apu[q] + fxp * m.vol[p] * fl.apu[p];
+  double Dpv = fxn * m.vol[q] * fl.apv[q] + fxp * m.vol[p] * fl.apv[p];
+  double Dpw = fxn * m.vol[q] * fl.apw[q] + fxp * m.vol[p] * fl.apw[p];
+  double dene = fl.den[p] * fxp + fl.den[q] * fxn;
+  double sfdpnr = 1.0 / (arx * xpn * nxx + ary * ypn * nyy + arz * zpn * nzz);
+  double smdpn = (arx * arx + ary * ary + arz * arz) * sfdpnr;
+  cap = -(dene * Dpu * smdpn);
+  can = cap;
+  const double dxp = xf - m.xc[p], dyp = yf - m.yc[p], dzp = zf - m.zc[p];
+  const double dxq = xf - m.xc[q], dyq = yf - m.yc[q], dzq = zf - m.zc[q];
+  double ui = face_value_central(p, q, dxp, dyp, dzp, dxq, dyq, dzq, fl.u, fl.dU);
+  double vi = face_value_central(p, q, dxp, dyp, dzp, dxq, dyq, dzq, fl.v, fl.dV);
+  double wi = face_value_central(p, q, dxp, dyp, dzp, dxq, dyq, dzq, fl.w, fl.dW);
+  const double *dP = fl.dP;
+  double dpxi = Dpu * (fxn * dP[3 * q] + fxp * dP[3 * p]) * xpn * nxx;
+  double dpyi = Dpv * (fxn * dP[3 * q + 1] + fxp * dP[3 * p + 1]) * ypn * nyy;
+  double dpzi = Dpw * (fxn * dP[3 * q + 2] + fxp * dP[3 * p + 2]) * zpn * nzz;
+  double xpp = xf - (xf - m.xc[p]) * nxx, ypp = yf - (yf - m.yc[p]) * nyy;
+  double zpp = zf - (zf - m.zc[p]) * nzz;
+  double xep = xf - (xf - m.xc[q]) * nxx, yep = yf - (yf - m.yc[q]) * nyy;
+  double zep = zf - (zf - m.zc[q]) * nzz;
+  xpp = xpp - m.xc[p];
+  ypp = ypp - m.yc[p];
+  zpp = zpp - m.zc[p];
+  xep = xep - m.xc[q];
+  yep = yep - m.yc[q];
+  zep = zep - m.zc[q];
+  double dpe = fl.p[q] - fl.p[p];
+  // :174-175 as written: only the first owner term carries the minus sign.
+  double dpecorr = dP[3 * q] * xep + dP[3 * q + 1] * yep + dP[3 * q + 2] * zep - dP[3 * p] * xpp +
+                   dP[3 * p + 1] * ypp + dP[3 * p + 2] * zpp;
+  dpe = dpe + dpecorr;
+  double dpex = Dpu * dpe * sfdpnr * arx, dpey = Dpv * dpe * sfdpnr * ary,
+         dpez = Dpw * dpe * sfdpnr * arz;
+  double ue = ui - dpex + dpxi, ve = vi - dpey + dpyi, we = wi - dpez + dpzi;
+  fm = dene * (ue * arx + ve * ary + we * arz);
+}
+
+// The O-C pairs (calcp :81-100): facefluxmass on face ijlFace(i) with foc(i); al(i) = cap,
+// ar(i) = can after the CSR values of a, fmoc(i) after the inner faces' fluxes.
+__global__ void k_ffm_oc(MeshView m, FlowView fl, double *__restrict__ a,
+                         double *__restrict__ flmass) {
+  FCG_GRID_STRIDE(i, m.noc) {
+    const int f = m.oc_fl[i];
+    double cap, can, fm;
+    ffm_face(m, fl, m.oc_l[i], m.oc_r[i], m.xf[f], m.yf[f], m.zf[f], m.arx[f], m.ary[f],
+             m.arz[f], m.oc_foc[i], cap, can, fm);
+    a[m.nnz + m.noc + i] = cap;
+    a[m.nnz + i] = can;
+    flmass[m.nin + i] = fm;
+  }
+}
+
 // Diagonal from the cell's own off-diagonal slots and su from the face fluxes, both in
-// face order (calcp :65-75).
+// face order (calcp :65-75), then the cell's O-C pairs in pair order (:89-99): ar / al
+// off the diagonal and fmoc off / onto su.
 __global__ void k_ffm_cells(MeshView m, const double *__restrict__ flmass, double *__restrict__ a,
                             double *__restrict__ su) {
   FCG_GRID_STRIDE(c, m.n) {
@@ -251,6 +317,13 @@ __global__ void k_ffm_cells(MeshView m, const double *__restrict__ flmass, doubl
       double fm = flmass[(ent > 0 ? ent : -ent) - 1];
       s = ent > 0 ? s - fm : s + fm;
     }
+    if (m.noc)
+      for (int e = m.oc_cptr[c]; e < m.oc_cptr[c + 1]; ++e) {
+        const int v = m.oc_vix[e];
+        acc = acc - a[m.nnz + v];
+        const double fm = flmass[m.nin + (v < m.noc ? v : v - m.noc)];
+        s = v < m.noc ? s - fm : s + fm;
+      }
     a[m.diag[c]] = acc;
     su[c] = s;
   }
@@ -309,6 +382,42 @@ __global__ void k_fmc_faces(MeshView m, const double *__restrict__ g, const doub
   }
 }
 
+// fluxmc (facefluxmass.f90:520-607) on the O-C pairs (calcp :206-215), computed in place
+// with the operations of k_fmc_faces and the factors k_face_geo caches: fmoc(i) += fmcor,
+// and fmcor kept after the inner faces' for the cells' sums.
+__global__ void k_fmc_oc(MeshView m, const double *__restrict__ dP, const double *__restrict__ apu,
+                         const double *__restrict__ den, double *__restrict__ flmass,
+                         double *__restrict__ fmcor_out) {
+  FCG_GRID_STRIDE(i, m.noc) {
+    const int p = m.oc_l[i], q = m.oc_r[i], f = m.oc_fl[i];
+    const double xf = m.xf[f], yf = m.yf[f], zf = m.zf[f];
+    const double arx = m.arx[f], ary = m.ary[f], arz = m.arz[f];
+    double fxn = m.oc_foc[i];
+    double fxp = 1.0 - fxn;
+    double xpn = m.xc[q] - m.xc[p], ypn = m.yc[q] - m.yc[p], zpn = m.zc[q] - m.zc[p];
+    double are = sqrt(arx * arx + ary * ary + arz * arz);
+    double nxx = arx / are, nyy = ary / are, nzz = arz / are;
+    double dppnnr = 1.0 / ((xpn * nxx) + (ypn * nyy) + (zpn * nzz));
+    double xpp = xf - (xf - m.xc[p]) * nxx, ypp = yf - (yf - m.yc[p]) * nyy;
+    double zpp = zf - (zf - m.zc[p]) * nzz;
+    double xep = xf - (xf - m.xc[q]) * nxx, yep = yf - (yf - m.yc[q]) * nyy;
+    double zep = zf - (zf - m.zc[q]) * nzz;
+    xpp = xpp - m.xc[p];
+    ypp = ypp - m.yc[p];
+    zpp = zpp - m.zc[p];
+    xep = xep - m.xc[q];
+    yep = yep - m.yc[q];
+    zep = zep - m.zc[q];
+    double rapr = apu[p] * den[p] * m.vol[p] * fxp + apu[q] * den[q] * m.vol[q] * fxn;
+    double fmcor = rapr * are *
+                   ((dP[3 * q] * xep - dP[3 * p] * xpp) + (dP[3 * q + 1] * yep - dP[3 * p + 1] * ypp) +
+                    (dP[3 * q + 2] * zep - dP[3 * p + 2] * zpp)) *
+                   dppnnr;
+    flmass[m.nin + i] = flmass[m.nin + i] + fmcor;
+    fmcor_out[m.nin + i] = fmcor;
+  }
+}
+
 __global__ void k_fmc_cells(MeshView m, const double *__restrict__ fmcor, double *__restrict__ su) {
   FCG_GRID_STRIDE(c, m.n) {
     double s = 0.0;  // su = 0 (:193), then -= / += fmcor in face order (:203-204)
@@ -317,6 +426,12 @@ __global__ void k_fmc_cells(MeshView m, const double *__restrict__ fmcor, double
       double fm = fmcor[(ent > 0 ? ent : -ent) - 1];
       s = ent > 0 ? s - fm : s + fm;
     }
+    if (m.noc)  // then the cell's O-C pairs in pair order (:212-213)
+      for (int e = m.oc_cptr[c]; e < m.oc_cptr[c + 1]; ++e) {
+        const int v = m.oc_vix[e];
+        const double fm = fmcor[m.nin + (v < m.noc ? v : v - m.noc)];
+        s = v < m.noc ? s - fm : s + fm;
+      }
     su[c] = s;
   }
 }
@@ -397,7 +512,6 @@ extern "C" int fcg_facefluxmass(fcg_context *c, const fcg_flow_fields *f, double
                                 double *flmass) {
   if (!c || !f) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_facefluxmass before fcg_bind_mesh");
-  if (c->mv.noc) return refuse_oc(c, "fcg_facefluxmass");
   FCG_CUDA_TRY(c, cudaSetDevice(c->device));
   const size_t nt = sizeof(double) * c->ntot, n1 = sizeof(double) * c->n, n3 = 3 * n1;
   const double *src[12] = {f->u, f->v, f->w, f->p, f->dUdxi, f->dVdxi, f->dWdxi, f->dPdxi,
@@ -410,9 +524,12 @@ extern "C" int fcg_facefluxmass(fcg_context *c, const fcg_flow_fields *f, double
     if ((rc = stage_in(c, src[i], bytes[i], i, true, &dev[i], &host[i]))) return rc;
   void *da, *dsu, *dfm;
   bool ha, hsu, hfm;
-  if ((rc = stage_in(c, a, sizeof(double) * c->nnz, 12, false, &da, &ha))) return rc;
+  // with O-C pairs: ar, al after the CSR values and fmoc after the inner faces' fluxes
+  const size_t alen = sizeof(double) * (size_t)a_len(c);
+  const size_t flen = sizeof(double) * (size_t)(c->nin + c->mv.noc);
+  if ((rc = stage_in(c, a, alen, 12, false, &da, &ha))) return rc;
   if ((rc = stage_in(c, su, n1, 13, false, &dsu, &hsu))) return rc;
-  if ((rc = stage_in(c, flmass, sizeof(double) * (c->nin > 0 ? c->nin : 1), 14, false, &dfm, &hfm)))
+  if ((rc = stage_in(c, flmass, flen > 0 ? flen : sizeof(double), 14, false, &dfm, &hfm)))
     return rc;
   FlowView fl{(const double *)dev[0], (const double *)dev[1], (const double *)dev[2],
               (const double *)dev[3], (const double *)dev[4], (const double *)dev[5],
@@ -426,12 +543,17 @@ extern "C" int fcg_facefluxmass(fcg_context *c, const fcg_flow_fields *f, double
                                                                         (double *)dfm);
     FCG_CHECK_LAUNCH(c, "k_ffm_faces");
   }
+  if (m.noc > 0) {
+    k_ffm_oc<<<grid_for(m.noc, c->num_sms), kTPB, 0, c->stream>>>(m, fl, (double *)da,
+                                                                     (double *)dfm);
+    FCG_CHECK_LAUNCH(c, "k_ffm_oc");
+  }
   k_ffm_cells<<<grid_for(m.n, c->num_sms), kTPB, 0, c->stream>>>(m, (const double *)dfm,
                                                                     (double *)da, (double *)dsu);
   FCG_CHECK_LAUNCH(c, "k_ffm_cells");
-  if ((rc = stage_out(c, a, da, sizeof(double) * c->nnz, ha))) return rc;
+  if ((rc = stage_out(c, a, da, alen, ha))) return rc;
   if ((rc = stage_out(c, su, dsu, n1, hsu))) return rc;
-  if ((rc = stage_out(c, flmass, dfm, sizeof(double) * c->nin, hfm))) return rc;
+  if ((rc = stage_out(c, flmass, dfm, flen, hfm))) return rc;
   if (ha || hsu || hfm) FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return FCG_OK;
 }
@@ -483,7 +605,6 @@ extern "C" int fcg_fluxmc(fcg_context *c, const double *dPdxi, const double *apu
                           const double *den, double *su, double *flmass) {
   if (!c) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_fluxmc before fcg_bind_mesh");
-  if (c->mv.noc) return refuse_oc(c, "fcg_fluxmc");
   FCG_CUDA_TRY(c, cudaSetDevice(c->device));
   void *dP, *dapu, *dden, *dsu, *dfm;
   bool h0, h1, h2, hsu, hfm;
@@ -493,9 +614,11 @@ extern "C" int fcg_fluxmc(fcg_context *c, const double *dPdxi, const double *apu
   if ((rc = stage_in(c, apu, n1, 1, true, &dapu, &h1))) return rc;
   if ((rc = stage_in(c, den, sizeof(double) * c->ntot, 2, true, &dden, &h2))) return rc;
   if ((rc = stage_in(c, su, n1, 3, false, &dsu, &hsu))) return rc;
-  if ((rc = stage_in(c, flmass, sizeof(double) * (c->nin > 0 ? c->nin : 1), 4, true, &dfm, &hfm)))
+  // with O-C pairs flmass holds fmoc after the inner faces' fluxes
+  const size_t flen = sizeof(double) * (size_t)(c->nin + c->mv.noc);
+  if ((rc = stage_in(c, flmass, flen > 0 ? flen : sizeof(double), 4, true, &dfm, &hfm)))
     return rc;
-  FCG_CUDA_TRY(c, c->scratch.ensure(sizeof(double) * (c->nin > 0 ? c->nin : 1)));
+  FCG_CUDA_TRY(c, c->scratch.ensure(flen > 0 ? flen : sizeof(double)));
   const MeshView &m = c->mv;
   const double *g;
   if ((rc = face_geo(c, &g))) return rc;
@@ -505,11 +628,17 @@ extern "C" int fcg_fluxmc(fcg_context *c, const double *dPdxi, const double *apu
         c->scratch.as<double>());
     FCG_CHECK_LAUNCH(c, "k_fmc_faces");
   }
+  if (m.noc > 0) {
+    k_fmc_oc<<<grid_for(m.noc, c->num_sms), kTPB, 0, c->stream>>>(
+        m, (const double *)dP, (const double *)dapu, (const double *)dden, (double *)dfm,
+        c->scratch.as<double>());
+    FCG_CHECK_LAUNCH(c, "k_fmc_oc");
+  }
   k_fmc_cells<<<grid_for(m.n, c->num_sms), kTPB, 0, c->stream>>>(m, c->scratch.as<double>(),
                                                                     (double *)dsu);
   FCG_CHECK_LAUNCH(c, "k_fmc_cells");
   if ((rc = stage_out(c, su, dsu, n1, hsu))) return rc;
-  if ((rc = stage_out(c, flmass, dfm, sizeof(double) * c->nin, hfm))) return rc;
+  if ((rc = stage_out(c, flmass, dfm, flen, hfm))) return rc;
   if (hsu || hfm) FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return FCG_OK;
 }
@@ -526,6 +655,14 @@ __global__ void k_flux_correct(MeshView m, const double *__restrict__ a,
   FCG_GRID_STRIDE(f, m.nin) {
     const int P = m.owner[f], N = m.neighbour[f];
     flmass[f] = flmass[f] + a[m.slot_pn[f]] * (pp[N] - pp[P]);
+  }
+}
+
+// fmoc(i) += ar(i) * (pp(ijr(i)) - pp(ijl(i))) (calcp :166-171)
+__global__ void k_flux_correct_oc(MeshView m, const double *__restrict__ a,
+                                  const double *__restrict__ pp, double *__restrict__ flmass) {
+  FCG_GRID_STRIDE(i, m.noc) {
+    flmass[m.nin + i] = flmass[m.nin + i] + a[m.nnz + i] * (pp[m.oc_r[i]] - pp[m.oc_l[i]]);
   }
 }
 
@@ -607,6 +744,12 @@ __global__ void k_contin_cells(MeshView m, const double *__restrict__ flmass,
       else
         r = r + flmass[m.owner[-ent - 1]];
     }
+    if (m.noc)  // faces along O-C grid cuts (:22-28), fmoc after the inner faces' fluxes
+      for (int e = m.oc_cptr[c]; e < m.oc_cptr[c + 1]; ++e) {
+        const int v = m.oc_vix[e];
+        const double fm = flmass[m.nin + (v < m.noc ? v : v - m.noc)];
+        r = v < m.noc ? r - fm : r + fm;
+      }
     for (int e = m.cb_ptr[c]; e < m.cb_ptr[c + 1]; ++e) {
       const int t = m.cb_type[e];
       if (t == B_INLET) r = r - fmi[m.cb_slot[e] - bst_inl];
@@ -678,7 +821,6 @@ extern "C" int fcg_correct_bc_velocity(fcg_context *c, const double *den, double
                                        double *u, double *v, double *w, double *fmo) {
   if (!c) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_correct_bc_velocity before fcg_bind_mesh");
-  if (c->mv.noc) return refuse_oc(c, "fcg_correct_bc_velocity");
   if (!den || !u || !v || !w || (!fmo && c->cnt[B_OUTLET] > 0))
     return set_error(c, FCG_ERR_ARG, "NULL array");
   FCG_CUDA_TRY(c, cudaSetDevice(c->device));
@@ -714,7 +856,6 @@ extern "C" int fcg_continuity_errors(fcg_context *c, const double *flmass, const
                                      double *global) {
   if (!c) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_continuity_errors before fcg_bind_mesh");
-  if (c->mv.noc) return refuse_oc(c, "fcg_continuity_errors");
   if (!flmass || (!fmi && c->cnt[B_INLET] > 0) || (!fmo && c->cnt[B_OUTLET] > 0))
     return set_error(c, FCG_ERR_ARG, "NULL array");
   if (c->n > c->nin)
@@ -725,7 +866,8 @@ extern "C" int fcg_continuity_errors(fcg_context *c, const double *flmass, const
   void *dfm, *dfmi = nullptr, *dfmo = nullptr, *dres;
   bool h0, h1 = false, h2 = false, hres = false;
   int rc;
-  if ((rc = stage_in(c, flmass, sizeof(double) * c->nin, 0, true, &dfm, &h0))) return rc;
+  if ((rc = stage_in(c, flmass, sizeof(double) * (size_t)(c->nin + c->mv.noc), 0, true, &dfm, &h0)))
+    return rc;
   if (nin_ > 0 && (rc = stage_in(c, fmi, sizeof(double) * nin_, 1, true, &dfmi, &h1))) return rc;
   if (nout > 0 && (rc = stage_in(c, fmo, sizeof(double) * nout, 2, true, &dfmo, &h2))) return rc;
   const size_t n1 = sizeof(double) * c->n;
@@ -757,14 +899,15 @@ extern "C" int fcg_flux_correct(fcg_context *c, const double *a, const double *p
                                 double *flmass) {
   if (!c) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_flux_correct before fcg_bind_mesh");
-  if (c->mv.noc) return refuse_oc(c, "fcg_flux_correct");
   if (!a || !pp || !flmass) return set_error(c, FCG_ERR_ARG, "NULL a, pp or flmass");
   FCG_CUDA_TRY(c, cudaSetDevice(c->device));
   void *da, *dpp, *dfm;
   bool ha, hpp, hfm;
   int rc;
-  const size_t nf = sizeof(double) * (c->nin > 0 ? c->nin : 1);
-  if ((rc = stage_in(c, a, sizeof(double) * c->nnz, 0, true, &da, &ha))) return rc;
+  // with O-C pairs: ar, al after the CSR values, fmoc after the inner faces' fluxes
+  const size_t flen = sizeof(double) * (size_t)(c->nin + c->mv.noc);
+  const size_t nf = flen > 0 ? flen : sizeof(double);
+  if ((rc = stage_in(c, a, sizeof(double) * (size_t)a_len(c), 0, true, &da, &ha))) return rc;
   if ((rc = stage_in(c, pp, sizeof(double) * c->ntot, 1, true, &dpp, &hpp))) return rc;
   if ((rc = stage_in(c, flmass, nf, 2, true, &dfm, &hfm))) return rc;
   if (c->nin > 0) {
@@ -772,7 +915,12 @@ extern "C" int fcg_flux_correct(fcg_context *c, const double *a, const double *p
         c->mv, (const double *)da, (const double *)dpp, (double *)dfm);
     FCG_CHECK_LAUNCH(c, "k_flux_correct");
   }
-  if ((rc = stage_out(c, flmass, dfm, sizeof(double) * c->nin, hfm))) return rc;
+  if (c->mv.noc > 0) {
+    fcg::corr::k_flux_correct_oc<<<grid_for(c->mv.noc, c->num_sms), kTPB, 0, c->stream>>>(
+        c->mv, (const double *)da, (const double *)dpp, (double *)dfm);
+    FCG_CHECK_LAUNCH(c, "k_flux_correct_oc");
+  }
+  if ((rc = stage_out(c, flmass, dfm, flen, hfm))) return rc;
   if (hfm) FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return FCG_OK;
 }
@@ -783,7 +931,6 @@ extern "C" int fcg_correct_fields(fcg_context *c, const double *dPdxi, const dou
                                   double *p) {
   if (!c) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_correct_fields before fcg_bind_mesh");
-  if (c->mv.noc) return refuse_oc(c, "fcg_correct_fields");
   if (!dPdxi || !apu || !apv || !apw || !pp || !u || !v || !w || !p)
     return set_error(c, FCG_ERR_ARG, "NULL array");
   if (pRefCell < 1 || pRefCell > c->n) return set_error(c, FCG_ERR_INDEX, "pRefCell out of range");

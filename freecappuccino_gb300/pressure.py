@@ -166,12 +166,14 @@ class Context:
         self._follow(u, v, w, p, dUdxi, dVdxi, dWdxi, dPdxi, apu, apv, apw, den)
         arrs = [_host(t) for t in (u, v, w, p, dUdxi, dVdxi, dWdxi, dPdxi, apu, apv, apw, den)]
         ff = _lib.FlowFields(*[_ptr(t) for t in arrs])
-        a = _like(arrs[0], self.nnz)
+        # with O-C pairs: ar, al after the CSR values, fmoc after the inner faces' fluxes
+        nfl = self.mesh.numInnerFaces + self.mesh.noc
+        a = _like(arrs[0], self.mesh.a_len)
         su = _like(arrs[0], self.n)
-        fm = _like(arrs[0], max(self.mesh.numInnerFaces, 1))
+        fm = _like(arrs[0], max(nfl, 1))
         self._check(self.lib.fcg_facefluxmass(self.h, C.byref(ff), _ptr(a), _ptr(su), _ptr(fm)),
                     "fcg_facefluxmass")
-        return a, su, fm[: self.mesh.numInnerFaces]
+        return a, su, fm[:nfl]
 
     def fluxmc(self, dPdxi, apu, den, flmass):
         """calcp's non-orthogonal corrector with fluxmc: returns (su, flmass)."""

@@ -360,6 +360,65 @@ static double face_value_central(const orc_mesh *m, int inp, int inn, double xf,
   return 0.5 * (F(fi, inp) + F(fi, inn) + gradfidr);
 }
 
+/* facefluxmass.f90:34-199 on the face between ijp and ijn with centre (xf, yf, zf), area
+ * (arx, ary, arz) and interpolation factor lambda: cap, can and the face mass flux. */
+static void ffm_face(const orc_mesh *m, int ijp, int ijn, double xf, double yf, double zf,
+                     double arx, double ary, double arz, double lambda, const double *u,
+                     const double *v, const double *w, const double *p, const double *dUdxi,
+                     const double *dVdxi, const double *dWdxi, const double *dPdxi,
+                     const double *apu, const double *apv, const double *apw,
+                     const double *den, double *cap_out, double *can_out, double *fm_out) {
+  double fxn = lambda;
+  double fxp = 1.0 - fxn;
+  double xpn = F(m->xc, ijn) - F(m->xc, ijp);
+  double ypn = F(m->yc, ijn) - F(m->yc, ijp);
+  double zpn = F(m->zc, ijn) - F(m->zc, ijp);
+  double are = sqrt(arx * arx + ary * ary + arz * arz);
+  double nxx = arx / are, nyy = ary / are, nzz = arz / are;
+  double Dpu = fxn * F(m->vol, ijn) * F(apu, ijn) + fxp * F(m->vol, ijp) * F(apu, ijp);
+  double Dpv = fxn * F(m->vol, ijn) * F(apv, ijn) + fxp * F(m->vol, ijp) * F(apv, ijp);
+  double Dpw = fxn * F(m->vol, ijn) * F(apw, ijn) + fxp * F(m->vol, ijp) * F(apw, ijp);
+  double dene = F(den, ijp) * fxp + F(den, ijn) * fxn;
+  double sfdpnr = 1.0 / (arx * xpn * nxx + ary * ypn * nyy + arz * zpn * nzz);
+  double smdpn = (arx * arx + ary * ary + arz * arz) * sfdpnr;
+  double cap = -(dene * Dpu * smdpn);
+  double can = cap;
+  double ui = face_value_central(m, ijp, ijn, xf, yf, zf, u, dUdxi);
+  double vi = face_value_central(m, ijp, ijn, xf, yf, zf, v, dVdxi);
+  double wi = face_value_central(m, ijp, ijn, xf, yf, zf, w, dWdxi);
+  double dpxi = Dpu * (fxn * G3(dPdxi, 1, ijn) + fxp * G3(dPdxi, 1, ijp)) * xpn * nxx;
+  double dpyi = Dpv * (fxn * G3(dPdxi, 2, ijn) + fxp * G3(dPdxi, 2, ijp)) * ypn * nyy;
+  double dpzi = Dpw * (fxn * G3(dPdxi, 3, ijn) + fxp * G3(dPdxi, 3, ijp)) * zpn * nzz;
+  double xpp = xf - (xf - F(m->xc, ijp)) * nxx;
+  double ypp = yf - (yf - F(m->yc, ijp)) * nyy;
+  double zpp = zf - (zf - F(m->zc, ijp)) * nzz;
+  double xep = xf - (xf - F(m->xc, ijn)) * nxx;
+  double yep = yf - (yf - F(m->yc, ijn)) * nyy;
+  double zep = zf - (zf - F(m->zc, ijn)) * nzz;
+  xpp = xpp - F(m->xc, ijp);
+  ypp = ypp - F(m->yc, ijp);
+  zpp = zpp - F(m->zc, ijp);
+  xep = xep - F(m->xc, ijn);
+  yep = yep - F(m->yc, ijn);
+  zep = zep - F(m->zc, ijn);
+  double dpe = F(p, ijn) - F(p, ijp);
+  /* :174-175, including the reference's sign pattern (only the first P term is subtracted). */
+  double dpecorr = G3(dPdxi, 1, ijn) * xep + G3(dPdxi, 2, ijn) * yep + G3(dPdxi, 3, ijn) * zep -
+                   G3(dPdxi, 1, ijp) * xpp + G3(dPdxi, 2, ijp) * ypp + G3(dPdxi, 3, ijp) * zpp;
+  dpe = dpe + dpecorr;
+  double dpex = Dpu * dpe * sfdpnr * arx;
+  double dpey = Dpv * dpe * sfdpnr * ary;
+  double dpez = Dpw * dpe * sfdpnr * arz;
+  double ue = ui - dpex + dpxi;
+  double ve = vi - dpey + dpyi;
+  double we = wi - dpez + dpzi;
+  *cap_out = cap;
+  *can_out = can;
+  *fm_out = dene * (ue * arx + ve * ary + we * arz);
+}
+
+/* calcp :34-100.  With O-C pairs a holds ar, al after the nnz CSR values and flmass the
+ * pairs' fluxes fmoc after the numInnerFaces inner-face fluxes. */
 int orc_facefluxmass(const orc_mesh *m, const int *diag, const int *slot_pn, const int *slot_np,
                      const double *u, const double *v, const double *w, const double *p,
                      const double *dUdxi, const double *dVdxi, const double *dWdxi,
@@ -370,53 +429,10 @@ int orc_facefluxmass(const orc_mesh *m, const int *diag, const int *slot_pn, con
   for (int i = 0; i < m->numCells; ++i) su[i] = 0.0;     /* calcp :35 */
   for (int i = 1; i <= m->numInnerFaces; ++i) {
     int ijp = F(m->owner, i), ijn = F(m->neighbour, i);
-    double xf = F(m->xf, i), yf = F(m->yf, i), zf = F(m->zf, i);
-    double arx = F(m->arx, i), ary = F(m->ary, i), arz = F(m->arz, i);
-    double fxn = F(m->facint, i);
-    double fxp = 1.0 - fxn;
-    double xpn = F(m->xc, ijn) - F(m->xc, ijp);
-    double ypn = F(m->yc, ijn) - F(m->yc, ijp);
-    double zpn = F(m->zc, ijn) - F(m->zc, ijp);
-    double are = sqrt(arx * arx + ary * ary + arz * arz);
-    double nxx = arx / are, nyy = ary / are, nzz = arz / are;
-    double Dpu = fxn * F(m->vol, ijn) * F(apu, ijn) + fxp * F(m->vol, ijp) * F(apu, ijp);
-    double Dpv = fxn * F(m->vol, ijn) * F(apv, ijn) + fxp * F(m->vol, ijp) * F(apv, ijp);
-    double Dpw = fxn * F(m->vol, ijn) * F(apw, ijn) + fxp * F(m->vol, ijp) * F(apw, ijp);
-    double dene = F(den, ijp) * fxp + F(den, ijn) * fxn;
-    double sfdpnr = 1.0 / (arx * xpn * nxx + ary * ypn * nyy + arz * zpn * nzz);
-    double smdpn = (arx * arx + ary * ary + arz * arz) * sfdpnr;
-    double cap = -(dene * Dpu * smdpn);
-    double can = cap;
-    double ui = face_value_central(m, ijp, ijn, xf, yf, zf, u, dUdxi);
-    double vi = face_value_central(m, ijp, ijn, xf, yf, zf, v, dVdxi);
-    double wi = face_value_central(m, ijp, ijn, xf, yf, zf, w, dWdxi);
-    double dpxi = Dpu * (fxn * G3(dPdxi, 1, ijn) + fxp * G3(dPdxi, 1, ijp)) * xpn * nxx;
-    double dpyi = Dpv * (fxn * G3(dPdxi, 2, ijn) + fxp * G3(dPdxi, 2, ijp)) * ypn * nyy;
-    double dpzi = Dpw * (fxn * G3(dPdxi, 3, ijn) + fxp * G3(dPdxi, 3, ijp)) * zpn * nzz;
-    double xpp = xf - (xf - F(m->xc, ijp)) * nxx;
-    double ypp = yf - (yf - F(m->yc, ijp)) * nyy;
-    double zpp = zf - (zf - F(m->zc, ijp)) * nzz;
-    double xep = xf - (xf - F(m->xc, ijn)) * nxx;
-    double yep = yf - (yf - F(m->yc, ijn)) * nyy;
-    double zep = zf - (zf - F(m->zc, ijn)) * nzz;
-    xpp = xpp - F(m->xc, ijp);
-    ypp = ypp - F(m->yc, ijp);
-    zpp = zpp - F(m->zc, ijp);
-    xep = xep - F(m->xc, ijn);
-    yep = yep - F(m->yc, ijn);
-    zep = zep - F(m->zc, ijn);
-    double dpe = F(p, ijn) - F(p, ijp);
-    /* :174-175, including the reference's sign pattern (only the first P term is subtracted). */
-    double dpecorr = G3(dPdxi, 1, ijn) * xep + G3(dPdxi, 2, ijn) * yep + G3(dPdxi, 3, ijn) * zep -
-                     G3(dPdxi, 1, ijp) * xpp + G3(dPdxi, 2, ijp) * ypp + G3(dPdxi, 3, ijp) * zpp;
-    dpe = dpe + dpecorr;
-    double dpex = Dpu * dpe * sfdpnr * arx;
-    double dpey = Dpv * dpe * sfdpnr * ary;
-    double dpez = Dpw * dpe * sfdpnr * arz;
-    double ue = ui - dpex + dpxi;
-    double ve = vi - dpey + dpyi;
-    double we = wi - dpez + dpzi;
-    double fm = dene * (ue * arx + ve * ary + we * arz);
+    double cap, can, fm;
+    ffm_face(m, ijp, ijn, F(m->xf, i), F(m->yf, i), F(m->zf, i), F(m->arx, i), F(m->ary, i),
+             F(m->arz, i), F(m->facint, i), u, v, w, p, dUdxi, dVdxi, dWdxi, dPdxi, apu, apv,
+             apw, den, &cap, &can, &fm);
     F(flmass, i) = fm;
     F(a, F(slot_pn, i)) = can;
     F(a, F(slot_np, i)) = cap;
@@ -425,6 +441,23 @@ int orc_facefluxmass(const orc_mesh *m, const int *diag, const int *slot_pn, con
     F(su, ijp) = F(su, ijp) - fm;
     F(su, ijn) = F(su, ijn) + fm;
   }
+  if (m->noc > 0) { /* o- and c-grid cuts (:81-100) */
+    oc_pairs oc;
+    if (get_oc(m, &oc)) return -1;
+    double *ar = a + nnz, *al = a + nnz + m->noc, *fmoc = flmass + m->numInnerFaces;
+    for (int i = 1; i <= m->noc; ++i) {
+      int iface = F(m->ijlFace, i), ijp = F(oc.ijl, i), ijn = F(oc.ijr, i);
+      ffm_face(m, ijp, ijn, F(m->xf, iface), F(m->yf, iface), F(m->zf, iface),
+               F(m->arx, iface), F(m->ary, iface), F(m->arz, iface), F(oc.foc, i), u, v, w, p,
+               dUdxi, dVdxi, dWdxi, dPdxi, apu, apv, apw, den, &F(al, i), &F(ar, i),
+               &F(fmoc, i));
+      F(a, F(diag, ijp)) = F(a, F(diag, ijp)) - F(ar, i);
+      F(a, F(diag, ijn)) = F(a, F(diag, ijn)) - F(al, i);
+      F(su, ijp) = F(su, ijp) - F(fmoc, i);
+      F(su, ijn) = F(su, ijn) + F(fmoc, i);
+    }
+    free_oc(&oc);
+  }
   return 0;
 }
 
@@ -432,43 +465,65 @@ int orc_facefluxmass(const orc_mesh *m, const int *diag, const int *slot_pn, con
 /* a4: fluxmc, facefluxmass.f90:520-607, driven by calcp :193-206             */
 /* ------------------------------------------------------------------------- */
 
+/* fluxmc, facefluxmass.f90:520-607, on the face between ijp and ijn (centre, area, factor). */
+static double fmc_face(const orc_mesh *m, int ijp, int ijn, double xf, double yf, double zf,
+                       double arx, double ary, double arz, double lambda, const double *dPdxi,
+                       const double *apu, const double *den) {
+  double fxn = lambda;
+  double fxp = 1.0 - fxn;
+  double xpn = F(m->xc, ijn) - F(m->xc, ijp);
+  double ypn = F(m->yc, ijn) - F(m->yc, ijp);
+  double zpn = F(m->zc, ijn) - F(m->zc, ijp);
+  double are = sqrt(arx * arx + ary * ary + arz * arz);
+  double nxx = arx / are, nyy = ary / are, nzz = arz / are;
+  double dppnnr = 1.0 / ((xpn * nxx) + (ypn * nyy) + (zpn * nzz));
+  double xpp = xf - (xf - F(m->xc, ijp)) * nxx;
+  double ypp = yf - (yf - F(m->yc, ijp)) * nyy;
+  double zpp = zf - (zf - F(m->zc, ijp)) * nzz;
+  double xep = xf - (xf - F(m->xc, ijn)) * nxx;
+  double yep = yf - (yf - F(m->yc, ijn)) * nyy;
+  double zep = zf - (zf - F(m->zc, ijn)) * nzz;
+  xpp = xpp - F(m->xc, ijp);
+  ypp = ypp - F(m->yc, ijp);
+  zpp = zpp - F(m->zc, ijp);
+  xep = xep - F(m->xc, ijn);
+  yep = yep - F(m->yc, ijn);
+  zep = zep - F(m->zc, ijn);
+  double rapr = F(apu, ijp) * F(den, ijp) * F(m->vol, ijp) * fxp +
+                F(apu, ijn) * F(den, ijn) * F(m->vol, ijn) * fxn;
+  return rapr * are *
+         ((G3(dPdxi, 1, ijn) * xep - G3(dPdxi, 1, ijp) * xpp) +
+          (G3(dPdxi, 2, ijn) * yep - G3(dPdxi, 2, ijp) * ypp) +
+          (G3(dPdxi, 3, ijn) * zep - G3(dPdxi, 3, ijp) * zpp)) *
+         dppnnr;
+}
+
+/* calcp :193-215; with O-C pairs flmass holds fmoc after the inner-face fluxes. */
 int orc_fluxmc(const orc_mesh *m, const double *dPdxi, const double *apu, const double *den,
                double *su, double *flmass) {
   for (int i = 0; i < m->numCells; ++i) su[i] = 0.0; /* calcp :193 */
   for (int i = 1; i <= m->numInnerFaces; ++i) {
     int ijp = F(m->owner, i), ijn = F(m->neighbour, i);
-    double xf = F(m->xf, i), yf = F(m->yf, i), zf = F(m->zf, i);
-    double arx = F(m->arx, i), ary = F(m->ary, i), arz = F(m->arz, i);
-    double fxn = F(m->facint, i);
-    double fxp = 1.0 - fxn;
-    double xpn = F(m->xc, ijn) - F(m->xc, ijp);
-    double ypn = F(m->yc, ijn) - F(m->yc, ijp);
-    double zpn = F(m->zc, ijn) - F(m->zc, ijp);
-    double are = sqrt(arx * arx + ary * ary + arz * arz);
-    double nxx = arx / are, nyy = ary / are, nzz = arz / are;
-    double dppnnr = 1.0 / ((xpn * nxx) + (ypn * nyy) + (zpn * nzz));
-    double xpp = xf - (xf - F(m->xc, ijp)) * nxx;
-    double ypp = yf - (yf - F(m->yc, ijp)) * nyy;
-    double zpp = zf - (zf - F(m->zc, ijp)) * nzz;
-    double xep = xf - (xf - F(m->xc, ijn)) * nxx;
-    double yep = yf - (yf - F(m->yc, ijn)) * nyy;
-    double zep = zf - (zf - F(m->zc, ijn)) * nzz;
-    xpp = xpp - F(m->xc, ijp);
-    ypp = ypp - F(m->yc, ijp);
-    zpp = zpp - F(m->zc, ijp);
-    xep = xep - F(m->xc, ijn);
-    yep = yep - F(m->yc, ijn);
-    zep = zep - F(m->zc, ijn);
-    double rapr = F(apu, ijp) * F(den, ijp) * F(m->vol, ijp) * fxp +
-                  F(apu, ijn) * F(den, ijn) * F(m->vol, ijn) * fxn;
-    double fmcor = rapr * are *
-                   ((G3(dPdxi, 1, ijn) * xep - G3(dPdxi, 1, ijp) * xpp) +
-                    (G3(dPdxi, 2, ijn) * yep - G3(dPdxi, 2, ijp) * ypp) +
-                    (G3(dPdxi, 3, ijn) * zep - G3(dPdxi, 3, ijp) * zpp)) *
-                   dppnnr;
+    double fmcor = fmc_face(m, ijp, ijn, F(m->xf, i), F(m->yf, i), F(m->zf, i), F(m->arx, i),
+                            F(m->ary, i), F(m->arz, i), F(m->facint, i), dPdxi, apu, den);
     F(flmass, i) = F(flmass, i) + fmcor;
     F(su, ijp) = F(su, ijp) - fmcor;
     F(su, ijn) = F(su, ijn) + fmcor;
+  }
+  if (m->noc > 0) { /* faces along O-C grid cuts (:206-215) */
+    oc_pairs oc;
+    if (get_oc(m, &oc)) return -1;
+    double *fmoc = flmass + m->numInnerFaces;
+    for (int i = 1; i <= m->noc; ++i) {
+      int iface = F(m->ijlFace, i), ijp = F(oc.ijl, i), ijn = F(oc.ijr, i);
+      double fmcor = fmc_face(m, ijp, ijn, F(m->xf, iface), F(m->yf, iface), F(m->zf, iface),
+                              F(m->arx, iface), F(m->ary, iface), F(m->arz, iface),
+                              F(oc.foc, i), dPdxi, apu, den);
+      F(fmoc, i) = F(fmoc, i) + fmcor;
+      F(su, ijp) = F(su, ijp) - fmcor;
+      F(su, ijn) = F(su, ijn) + fmcor;
+    }
+    free_oc(&oc);
   }
   return 0;
 }
@@ -979,6 +1034,15 @@ int orc_flux_correct(const orc_mesh *m, const int *slot_pn, const double *a, con
   for (int i = 0; i < m->numInnerFaces; ++i) {
     const int ijp = m->owner[i] - 1, ijn = m->neighbour[i] - 1;
     flmass[i] = flmass[i] + a[slot_pn[i] - 1] * (pp[ijn] - pp[ijp]);
+  }
+  if (m->noc > 0) { /* faces along O-C grid cuts (calcp :166-171) */
+    oc_pairs oc;
+    if (get_oc(m, &oc)) return -1;
+    const double *ar = a + m->numCells + 2L * m->numInnerFaces;
+    double *fmoc = flmass + m->numInnerFaces;
+    for (int i = 1; i <= m->noc; ++i)
+      F(fmoc, i) = F(fmoc, i) + F(ar, i) * (F(pp, F(oc.ijr, i)) - F(pp, F(oc.ijl, i)));
+    free_oc(&oc);
   }
   return 0;
 }
@@ -1616,6 +1680,16 @@ int orc_continuity_errors(const orc_mesh *m, const double *flmass, const double 
     const int ijp = F(m->owner, i), ijn = F(m->neighbour, i);
     F(res, ijp) = F(res, ijp) - F(flmass, ijp);
     F(res, ijn) = F(res, ijn) + F(flmass, ijp);
+  }
+  if (m->noc > 0) { /* faces along O-C grid cuts (continuityErrors.h:22-28) */
+    oc_pairs oc;
+    if (get_oc(m, &oc)) return -1;
+    const double *fmoc = flmass + m->numInnerFaces;
+    for (int i = 1; i <= m->noc; ++i) {
+      F(res, F(oc.ijl, i)) = F(res, F(oc.ijl, i)) - F(fmoc, i);
+      F(res, F(oc.ijr, i)) = F(res, F(oc.ijr, i)) + F(fmoc, i);
+    }
+    free_oc(&oc);
   }
   for (int i = 1; i <= m->ninl; ++i) {
     const int ijp = F(m->owner, m->iInletFacesStart + i);

@@ -203,14 +203,16 @@ def laplacian(m: Mesh, csr: CSR, mu, phi, su):
 
 
 def facefluxmass(m: Mesh, csr: CSR, u, v, w, p, dUdxi, dVdxi, dWdxi, dPdxi, apu, apv, apw, den):
-    """calcp-multiple_correction_SIMPLE.f90:34-77 with facefluxmass.f90:34-199."""
+    """calcp-multiple_correction_SIMPLE.f90:34-100 with facefluxmass.f90:34-199.  With O-C
+    pairs a holds ar, al after the CSR values and flmass the pairs' fmoc after the inner
+    faces' fluxes."""
     args = [_f64(t) for t in (u, v, w, p, dUdxi, dVdxi, dWdxi, dPdxi, apu, apv, apw, den)]
-    a = np.zeros(csr.nnz)
+    a = np.zeros(csr.nnz + 2 * m.noc)
     su = np.zeros(m.numCells)
-    flmass = np.zeros(max(m.numInnerFaces, 1))
+    flmass = np.zeros(max(m.numInnerFaces + m.noc, 1))
     assert lib().orc_facefluxmass(C.byref(m.struct), _i(csr.diag), _i(csr.slot_pn), _i(csr.slot_np),
                                   *[_d(t) for t in args], csr.nnz, _d(a), _d(su), _d(flmass)) == 0
-    return a, su, flmass[:m.numInnerFaces]
+    return a, su, flmass[:m.numInnerFaces + m.noc]
 
 
 def fluxmc(m: Mesh, dPdxi, apu, den, flmass):

@@ -137,6 +137,50 @@ def test_oracle_gauss_gradient_of_the_cut_mesh_is_the_uncut_one():
         assert np.abs(gm - gu).max() <= 1e-12 * np.abs(gu).max()
 
 
+def _cell_fields(m, seed=3):
+    """Flow fields from cell values only (boundary slots 0), so that the cut and the uncut
+    mesh see the same fields."""
+    n, nt = m.numCells, m.numTotal
+    pad = lambda x: np.concatenate([x, np.zeros(nt - n)])
+    f = {k: pad(fcg.uniform(seed, i, n)) for i, k in enumerate(("u", "v", "w", "p"), start=1)}
+    for k, name in enumerate(("dUdxi", "dVdxi", "dWdxi", "dPdxi")):
+        f[name] = fcg.uniform(seed, 10 + k, 3 * n).reshape(n, 3)
+    for k, name in enumerate(("apu", "apv", "apw")):
+        f[name] = 1.0 / m.vol * (1.0 + 0.1 * fcg.uniform(seed, 20 + k, n))
+    f["den"] = pad(1.0 + 0.2 * fcg.uniform(seed, 30, n))
+    return f
+
+
+def test_oracle_face_fluxes_of_the_cut_mesh_are_the_uncut_ones():
+    """calcp on the cut mesh (:34-100, 159-171, 193-215): the pairs' ar / al and fmoc are the
+    cut inner faces' coefficients and fluxes, so the p' operator, its source and the mass
+    fluxes are the uncut mesh's up to the rounding of foc."""
+    N = 8
+    m, u = oc_split_mesh(N), fcg.hex_mesh(N)
+    fm_, fu_ = _cell_fields(m), _cell_fields(u)
+    a, su_m, fl_m = oracle.facefluxmass(oracle_mesh(m), oracle_csr(m), *fm_.values())
+    b, su_u, fl_u = oracle.facefluxmass(oracle_mesh(u), oracle_csr(u), *fu_.values())
+    assert len(a) == m.nnz + 2 * m.noc and len(fl_m) == m.numInnerFaces + m.noc
+    A, B = _operator(m, oracle_csr(m), a), _operator(u, oracle_csr(u), b)
+    assert np.abs(A - B).max() <= 1e-12 * np.abs(B).max()
+    assert np.abs(su_m - su_u).max() <= 1e-12 * np.abs(su_u).max()
+    nin = u.numInnerFaces
+    cut = ((u.owner[:nin] - 1) // (N * N) == N // 2 - 1) & ((u.neighbour - 1) // (N * N) == N // 2)
+    keep = ~cut
+    assert np.abs(fl_m[m.numInnerFaces:] - fl_u[cut]).max() <= 1e-12 * np.abs(fl_u).max()
+    assert np.array_equal(fl_m[: m.numInnerFaces], fl_u[keep])
+    # the non-orthogonal corrector and the flux correction follow the same faces
+    su2_m, fl2_m = oracle.fluxmc(oracle_mesh(m), fm_["dPdxi"], fm_["apu"], fm_["den"], fl_m)
+    su2_u, fl2_u = oracle.fluxmc(oracle_mesh(u), fu_["dPdxi"], fu_["apu"], fu_["den"], fl_u)
+    assert np.abs(fl2_m[m.numInnerFaces:] - fl2_u[cut]).max() <= 1e-12 * np.abs(fl2_u).max()
+    assert np.abs(su2_m - su2_u).max() <= 1e-12 * np.abs(su2_u).max()
+    pp_m = np.concatenate([fcg.uniform(6, 1, m.numCells), np.zeros(m.numTotal - m.numCells)])
+    pp_u = np.concatenate([pp_m[: m.numCells], np.zeros(u.numTotal - u.numCells)])
+    fc_m = oracle.flux_correct(oracle_mesh(m), oracle_csr(m), a, pp_m, fl_m)
+    fc_u = oracle.flux_correct(oracle_mesh(u), oracle_csr(u), b, pp_u, fl_u)
+    assert np.abs(fc_m[m.numInnerFaces:] - fc_u[cut]).max() <= 1e-12 * np.abs(fc_u).max()
+
+
 # ----------------------------------------------------------------------------- GPU
 def _gpu(N=8, cyclic=False):
     m = oc_split_mesh(N, cyclic=cyclic)
@@ -224,6 +268,32 @@ def test_gradients_and_bpres_with_pairs_bit_exact(cyclic):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("cyclic", [False, True])
+def test_calcp_face_fluxes_with_pairs_bit_exact(cyclic):
+    """facefluxmass, fluxmc, the flux correction and the continuity errors on the cut mesh,
+    bit for bit against the oracle (ar, al after the CSR values, fmoc after the inner
+    faces' fluxes)."""
+    from tests.meshes import seeded_fields
+
+    m, c = _gpu(8, cyclic)
+    om, csr = oracle_mesh(m), oracle_csr(m)
+    f = seeded_fields(m)
+    a, su, fm = c.facefluxmass(**f)
+    a_o, su_o, fm_o = oracle.facefluxmass(om, csr, *f.values())
+    assert len(fm) == m.numInnerFaces + m.noc
+    assert np.array_equal(a, a_o) and np.array_equal(su, su_o) and np.array_equal(fm, fm_o)
+    su2, fm2 = c.fluxmc(f["dPdxi"], f["apu"], f["den"], fm)
+    su2_o, fm2_o = oracle.fluxmc(om, f["dPdxi"], f["apu"], f["den"], fm_o)
+    assert np.array_equal(su2, su2_o) and np.array_equal(fm2, fm2_o)
+    pp = fcg.uniform(6, 1, m.numTotal)
+    assert np.array_equal(c.flux_correct(a, pp, fm2), oracle.flux_correct(om, csr, a_o, pp, fm2_o))
+    r, sl, sg = c.continuity_errors(fm2, np.zeros(0), np.zeros(0))
+    r_o, sl_o, sg_o = oracle.continuity_errors(om, fm2_o, np.zeros(0), np.zeros(0))
+    assert np.array_equal(r, r_o)
+    c.close()
+
+
+@pytest.mark.gpu
 def test_entry_points_without_pairs_refuse_the_mesh():
     from freecappuccino_gb300._lib import FcgError
     from tests.meshes import seeded_fields
@@ -235,7 +305,8 @@ def test_entry_points_without_pairs_refuse_the_mesh():
         c.dpcg_mixed(a, su, np.zeros(m.numCells), 1e-8, 100)
     assert e.value.status == -8
     with pytest.raises(FcgError) as e:
-        c.facefluxmass(**seeded_fields(m))
+        c.facefluxmass_piso(**{k: v for k, v in seeded_fields(m).items()
+                               if k in ("u", "v", "w", "dUdxi", "dVdxi", "dWdxi", "apu", "den")})
     assert e.value.status == -8
     c.close()
 
