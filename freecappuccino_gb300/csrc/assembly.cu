@@ -304,6 +304,34 @@ __global__ void k_ffm_oc(MeshView m, FlowView fl, double *__restrict__ a,
   }
 }
 
+// The O-C pairs of the PISO assembly (PISO_multiple_correction.f90:151-174):
+// facefluxmass_piso (facefluxmass.f90:294-358) on face ijlFace(i) with foc(i), computed in
+// place with the operations of k_ffp_faces.
+__global__ void k_ffp_oc(MeshView m, FlowView fl, double *__restrict__ a,
+                         double *__restrict__ flmass) {
+  FCG_GRID_STRIDE(i, m.noc) {
+    const int p = m.oc_l[i], q = m.oc_r[i], f = m.oc_fl[i];
+    const double xf = m.xf[f], yf = m.yf[f], zf = m.zf[f];
+    const double arx = m.arx[f], ary = m.ary[f], arz = m.arz[f];
+    const double fxn = m.oc_foc[i];
+    const double fxp = 1.0 - fxn;
+    const double xpn = m.xc[q] - m.xc[p], ypn = m.yc[q] - m.yc[p], zpn = m.zc[q] - m.zc[p];
+    const double dpn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
+    const double are = sqrt(arx * arx + ary * ary + arz * arz);
+    const double dene = fl.den[p] * fxp + fl.den[q] * fxn;
+    const double cap =
+        -(dene * (fxp * m.vol[p] * fl.apu[p] + fxn * m.vol[q] * fl.apu[q]) * are / dpn);
+    const double dxp = xf - m.xc[p], dyp = yf - m.yc[p], dzp = zf - m.zc[p];
+    const double dxq = xf - m.xc[q], dyq = yf - m.yc[q], dzq = zf - m.zc[q];
+    const double ui = face_value_central(p, q, dxp, dyp, dzp, dxq, dyq, dzq, fl.u, fl.dU);
+    const double vi = face_value_central(p, q, dxp, dyp, dzp, dxq, dyq, dzq, fl.v, fl.dV);
+    const double wi = face_value_central(p, q, dxp, dyp, dzp, dxq, dyq, dzq, fl.w, fl.dW);
+    a[m.nnz + m.noc + i] = cap;  // al = cap
+    a[m.nnz + i] = cap;          // ar = can = cap
+    flmass[m.nin + i] = dene * (ui * arx + vi * ary + wi * arz);
+  }
+}
+
 // Diagonal from the cell's own off-diagonal slots and su from the face fluxes, both in
 // face order (calcp :65-75), then the cell's O-C pairs in pair order (:89-99): ar / al
 // off the diagonal and fmoc off / onto su.
@@ -562,7 +590,6 @@ extern "C" int fcg_facefluxmass_piso(fcg_context *c, const fcg_flow_fields *f, d
                                      double *su, double *flmass) {
   if (!c || !f) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_facefluxmass_piso before fcg_bind_mesh");
-  if (c->mv.noc) return refuse_oc(c, "fcg_facefluxmass_piso");
   FCG_CUDA_TRY(c, cudaSetDevice(c->device));
   const size_t nt = sizeof(double) * c->ntot, n1 = sizeof(double) * c->n, n3 = 3 * n1;
   // the fields facefluxmass_piso reads (facefluxmass.f90:300-302)
@@ -575,9 +602,12 @@ extern "C" int fcg_facefluxmass_piso(fcg_context *c, const fcg_flow_fields *f, d
     if ((rc = stage_in(c, src[i], bytes[i], i, true, &dev[i], &host[i]))) return rc;
   void *da, *dsu, *dfm;
   bool ha, hsu, hfm;
-  if ((rc = stage_in(c, a, sizeof(double) * c->nnz, 12, false, &da, &ha))) return rc;
+  // with O-C pairs: ar, al after the CSR values and fmoc after the inner faces' fluxes
+  const size_t alen = sizeof(double) * (size_t)a_len(c);
+  const size_t flen = sizeof(double) * (size_t)(c->nin + c->mv.noc);
+  if ((rc = stage_in(c, a, alen, 12, false, &da, &ha))) return rc;
   if ((rc = stage_in(c, su, n1, 13, false, &dsu, &hsu))) return rc;
-  if ((rc = stage_in(c, flmass, sizeof(double) * (c->nin > 0 ? c->nin : 1), 14, false, &dfm, &hfm)))
+  if ((rc = stage_in(c, flmass, flen > 0 ? flen : sizeof(double), 14, false, &dfm, &hfm)))
     return rc;
   FlowView fl{(const double *)dev[0], (const double *)dev[1], (const double *)dev[2], nullptr,
               (const double *)dev[3], (const double *)dev[4], (const double *)dev[5], nullptr,
@@ -590,13 +620,19 @@ extern "C" int fcg_facefluxmass_piso(fcg_context *c, const fcg_flow_fields *f, d
                                                                         (double *)dfm);
     FCG_CHECK_LAUNCH(c, "k_ffp_faces");
   }
-  // a = 0, su = 0 (PISO :109-110), then the diagonal and su in face order (:133-146)
+  if (m.noc > 0) {
+    k_ffp_oc<<<grid_for(m.noc, c->num_sms), kTPB, 0, c->stream>>>(m, fl, (double *)da,
+                                                                     (double *)dfm);
+    FCG_CHECK_LAUNCH(c, "k_ffp_oc");
+  }
+  // a = 0, su = 0 (PISO :109-110), then the diagonal and su in face order (:133-146) and the
+  // O-C pairs (:162-173)
   k_ffm_cells<<<grid_for(m.n, c->num_sms), kTPB, 0, c->stream>>>(m, (const double *)dfm,
                                                                     (double *)da, (double *)dsu);
   FCG_CHECK_LAUNCH(c, "k_ffm_cells");
-  if ((rc = stage_out(c, a, da, sizeof(double) * c->nnz, ha))) return rc;
+  if ((rc = stage_out(c, a, da, alen, ha))) return rc;
   if ((rc = stage_out(c, su, dsu, n1, hsu))) return rc;
-  if ((rc = stage_out(c, flmass, dfm, sizeof(double) * c->nin, hfm))) return rc;
+  if ((rc = stage_out(c, flmass, dfm, flen, hfm))) return rc;
   if (ha || hsu || hfm) FCG_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return FCG_OK;
 }

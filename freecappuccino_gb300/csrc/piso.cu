@@ -149,7 +149,6 @@ extern "C" int fcg_piso_hbya(fcg_context *c, const fcg_hbya_params *prm, const f
                              double *sv, double *sw) {
   if (!c || !prm || !f) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_piso_hbya before fcg_bind_mesh");
-  if (c->mv.noc) return refuse_oc(c, "fcg_piso_hbya");
   const bool need_old = prm->bdf || prm->cn;
   const bool need_oo = prm->bdf && prm->btime > (double)0.99f;
   const bool need_t = prm->buoyancy && prm->boussinesq;
@@ -232,7 +231,6 @@ extern "C" int fcg_adjust_mass_flow(fcg_context *c, const double *den, double fl
                                     double *fmo, double *su) {
   if (!c) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_adjust_mass_flow before fcg_bind_mesh");
-  if (c->mv.noc) return refuse_oc(c, "fcg_adjust_mass_flow");
   const int ninl = c->cnt[B_INLET], nout = c->cnt[B_OUTLET];
   if (!den || !u || !v || !w || !su || (ninl > 0 && !fmi) || (nout > 0 && !fmo))
     return set_error(c, FCG_ERR_ARG, "NULL array");
@@ -271,7 +269,6 @@ extern "C" int fcg_set_reference_pressure(fcg_context *c, int pRefCell, const do
   if (!c) return FCG_ERR_ARG;
   if (!c->bound)
     return set_error(c, FCG_ERR_STATE, "fcg_set_reference_pressure before fcg_bind_mesh");
-  if (c->mv.noc) return refuse_oc(c, "fcg_set_reference_pressure");
   if (!p || !a || !su) return set_error(c, FCG_ERR_ARG, "NULL array");
   if (pRefCell < 1 || pRefCell > c->n) return set_error(c, FCG_ERR_INDEX, "pRefCell out of range");
   FCG_CUDA_TRY(c, cudaSetDevice(c->device));
@@ -298,7 +295,6 @@ extern "C" int fcg_correct_velocity_piso(fcg_context *c, const double *dPdxi, co
   if (!c) return FCG_ERR_ARG;
   if (!c->bound)
     return set_error(c, FCG_ERR_STATE, "fcg_correct_velocity_piso before fcg_bind_mesh");
-  if (c->mv.noc) return refuse_oc(c, "fcg_correct_velocity_piso");
   if (!dPdxi || !apu || !apv || !apw || !u || !v || !w)
     return set_error(c, FCG_ERR_ARG, "NULL array");
   FCG_CUDA_TRY(c, cudaSetDevice(c->device));

@@ -311,12 +311,13 @@ class Context:
                                                             den))
         ff = _lib.FlowFields(_ptr(u), _ptr(v), _ptr(w), None, _ptr(dU), _ptr(dV), _ptr(dW), None,
                              _ptr(apu), None, None, _ptr(den))
-        a = _like(u, self.nnz)
+        nfl = self.mesh.numInnerFaces + self.mesh.noc  # fmoc after the inner faces' fluxes
+        a = _like(u, self.mesh.a_len)
         su = _like(u, self.n)
-        fm = _like(u, max(self.mesh.numInnerFaces, 1))
+        fm = _like(u, max(nfl, 1))
         self._check(self.lib.fcg_facefluxmass_piso(self.h, C.byref(ff), _ptr(a), _ptr(su),
                                                    _ptr(fm)), "fcg_facefluxmass_piso")
-        return a, su, fm[: self.mesh.numInnerFaces]
+        return a, su, fm[:nfl]
 
     def adjust_mass_flow(self, den, flomas, fmi, u, v, w, su):
         """adjustMassFlow: returns (u, v, w, fmo, su)."""

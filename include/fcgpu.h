@@ -87,11 +87,13 @@ typedef struct fcg_mesh_desc {
    * fvm_laplacian.f90:70): the start of the first 'domain' patch, 0 without one.  With noc > 0 a matrix `a` holds nnz + 2 noc values: the
    * CSR values, then ar(1..noc), then al(1..noc) (module sparse_matrix's al, ar), and
    * a mass-flux array flmass holds numInnerFaces + noc values: the inner faces', then
-   * the pairs' fmoc(1..noc) (module variables' fmoc).  The pressure-correction path
-   * takes the pairs: fcg_laplacian, fcg_facefluxmass, fcg_fluxmc, fcg_flux_correct,
-   * fcg_continuity_errors, fcg_correct_fields, fcg_correct_bc_velocity, fcg_grad,
-   * fcg_grad_lsq_matrix, fcg_bpres, fcg_dpcg, fcg_iccg, fcg_bicgstab and fcg_spmv; the
-   * momentum, PISO, mixed, multi-RHS, batched and learned entry points return
+   * the pairs' fmoc(1..noc) (module variables' fmoc).  The SIMPLE and PISO pressure-
+   * correction paths take the pairs: fcg_laplacian, fcg_facefluxmass, fcg_fluxmc,
+   * fcg_flux_correct, fcg_continuity_errors, fcg_correct_fields, fcg_correct_bc_velocity,
+   * fcg_facefluxmass_piso, fcg_piso_hbya, fcg_adjust_mass_flow,
+   * fcg_set_reference_pressure, fcg_correct_velocity_piso, fcg_grad, fcg_grad_lsq_matrix,
+   * fcg_bpres, fcg_dpcg, fcg_iccg, fcg_bicgstab and fcg_spmv; the momentum assembly
+   * (fcg_calcuvw) and the mixed, multi-RHS, batched and learned solvers return
    * FCG_ERR_UNSUPPORTED on such a mesh. */
   int ncyc;
   int iOCFacesStart;

@@ -1524,6 +1524,34 @@ int orc_piso_hbya(const orc_mesh *m, const int *ioffset, const int *diag, const 
 }
 
 /* PISO_multiple_correction.f90:109-148 with facefluxmass_piso (facefluxmass.f90:294-358). */
+/* facefluxmass_piso, facefluxmass.f90:294-358, on the face between ijp and ijn (centre,
+ * area, factor): cap, can and the face mass flux. */
+static void ffp_face(const orc_mesh *m, int ijp, int ijn, double xf, double yf, double zf,
+                     double arx, double ary, double arz, double lambda, const double *u,
+                     const double *v, const double *w, const double *dUdxi,
+                     const double *dVdxi, const double *dWdxi, const double *apu,
+                     const double *den, double *cap_out, double *can_out, double *fm_out) {
+  const double fxn = lambda;
+  const double fxp = 1.0 - fxn;
+  const double xpn = F(m->xc, ijn) - F(m->xc, ijp);
+  const double ypn = F(m->yc, ijn) - F(m->yc, ijp);
+  const double zpn = F(m->zc, ijn) - F(m->zc, ijp);
+  const double dpn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
+  const double are = sqrt(arx * arx + ary * ary + arz * arz);
+  const double dene = F(den, ijp) * fxp + F(den, ijn) * fxn;
+  const double cap = -(dene *
+                       (fxp * F(m->vol, ijp) * F(apu, ijp) + fxn * F(m->vol, ijn) * F(apu, ijn)) *
+                       are / dpn);
+  const double ui = face_value_central(m, ijp, ijn, xf, yf, zf, u, dUdxi);
+  const double vi = face_value_central(m, ijp, ijn, xf, yf, zf, v, dVdxi);
+  const double wi = face_value_central(m, ijp, ijn, xf, yf, zf, w, dWdxi);
+  *cap_out = cap;
+  *can_out = cap;
+  *fm_out = dene * (ui * arx + vi * ary + wi * arz);
+}
+
+/* PISO :109-174; with O-C pairs a holds ar, al after the CSR values and flmass the
+ * pairs' fmoc after the inner faces' fluxes. */
 int orc_facefluxmass_piso(const orc_mesh *m, const int *diag, const int *slot_pn,
                           const int *slot_np, const double *u, const double *v, const double *w,
                           const double *dUdxi, const double *dVdxi, const double *dWdxi,
@@ -1533,24 +1561,10 @@ int orc_facefluxmass_piso(const orc_mesh *m, const int *diag, const int *slot_pn
   for (int i = 0; i < m->numCells; ++i) su[i] = 0.0; /* :110 */
   for (int i = 1; i <= m->numInnerFaces; ++i) {
     const int ijp = F(m->owner, i), ijn = F(m->neighbour, i);
-    const double xf = F(m->xf, i), yf = F(m->yf, i), zf = F(m->zf, i);
-    const double arx = F(m->arx, i), ary = F(m->ary, i), arz = F(m->arz, i);
-    const double fxn = F(m->facint, i);
-    const double fxp = 1.0 - fxn;
-    const double xpn = F(m->xc, ijn) - F(m->xc, ijp);
-    const double ypn = F(m->yc, ijn) - F(m->yc, ijp);
-    const double zpn = F(m->zc, ijn) - F(m->zc, ijp);
-    const double dpn = sqrt(xpn * xpn + ypn * ypn + zpn * zpn);
-    const double are = sqrt(arx * arx + ary * ary + arz * arz);
-    const double dene = F(den, ijp) * fxp + F(den, ijn) * fxn;
-    const double cap = -(dene *
-                         (fxp * F(m->vol, ijp) * F(apu, ijp) + fxn * F(m->vol, ijn) * F(apu, ijn)) *
-                         are / dpn);
-    const double can = cap;
-    const double ui = face_value_central(m, ijp, ijn, xf, yf, zf, u, dUdxi);
-    const double vi = face_value_central(m, ijp, ijn, xf, yf, zf, v, dVdxi);
-    const double wi = face_value_central(m, ijp, ijn, xf, yf, zf, w, dWdxi);
-    const double fm = dene * (ui * arx + vi * ary + wi * arz);
+    double cap, can, fm;
+    ffp_face(m, ijp, ijn, F(m->xf, i), F(m->yf, i), F(m->zf, i), F(m->arx, i), F(m->ary, i),
+             F(m->arz, i), F(m->facint, i), u, v, w, dUdxi, dVdxi, dWdxi, apu, den, &cap, &can,
+             &fm);
     F(flmass, i) = fm;
     F(a, F(slot_pn, i)) = can;
     F(a, F(slot_np, i)) = cap;
@@ -1558,6 +1572,22 @@ int orc_facefluxmass_piso(const orc_mesh *m, const int *diag, const int *slot_pn
     F(a, F(diag, ijn)) = F(a, F(diag, ijn)) - cap;
     F(su, ijp) = F(su, ijp) - fm;
     F(su, ijn) = F(su, ijn) + fm;
+  }
+  if (m->noc > 0) { /* O- and C-grid cuts (:151-174) */
+    oc_pairs oc;
+    if (get_oc(m, &oc)) return -1;
+    double *ar = a + nnz, *al = a + nnz + m->noc, *fmoc = flmass + m->numInnerFaces;
+    for (int i = 1; i <= m->noc; ++i) {
+      int iface = F(m->ijlFace, i), ijp = F(oc.ijl, i), ijn = F(oc.ijr, i);
+      ffp_face(m, ijp, ijn, F(m->xf, iface), F(m->yf, iface), F(m->zf, iface),
+               F(m->arx, iface), F(m->ary, iface), F(m->arz, iface), F(oc.foc, i), u, v, w,
+               dUdxi, dVdxi, dWdxi, apu, den, &F(al, i), &F(ar, i), &F(fmoc, i));
+      F(a, F(diag, ijp)) = F(a, F(diag, ijp)) - F(ar, i);
+      F(a, F(diag, ijn)) = F(a, F(diag, ijn)) - F(al, i);
+      F(su, ijp) = F(su, ijp) - F(fmoc, i);
+      F(su, ijn) = F(su, ijn) + F(fmoc, i);
+    }
+    free_oc(&oc);
   }
   return 0;
 }

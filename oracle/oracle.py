@@ -302,13 +302,13 @@ def facefluxmass_piso(m: Mesh, csr: CSR, u, v, w, dUdxi, dVdxi, dWdxi, apu, den)
     """PISO_multiple_correction.f90:109-148 with facefluxmass_piso (facefluxmass.f90:294-358).
     Returns (a, su, flmass)."""
     args = [_f64(t) for t in (u, v, w, dUdxi, dVdxi, dWdxi, apu, den)]
-    a = np.zeros(csr.nnz)
+    a = np.zeros(csr.nnz + 2 * m.noc)
     su = np.zeros(m.numCells)
-    flmass = np.zeros(max(m.numInnerFaces, 1))
+    flmass = np.zeros(max(m.numInnerFaces + m.noc, 1))
     assert lib().orc_facefluxmass_piso(C.byref(m.struct), _i(csr.diag), _i(csr.slot_pn),
                                        _i(csr.slot_np), *[_d(t) for t in args], csr.nnz, _d(a),
                                        _d(su), _d(flmass)) == 0
-    return a, su, flmass[:m.numInnerFaces]
+    return a, su, flmass[:m.numInnerFaces + m.noc]
 
 
 def adjust_mass_flow(m: Mesh, den, flomas, fmi, u, v, w, su):
