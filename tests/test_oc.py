@@ -340,3 +340,24 @@ def test_polymesh_round_trip_keeps_the_pairs(tmp_path):
             b, _ = oracle.laplacian(oracle_mesh(r), oracle_csr(r), mu, phi, su)
             A, B = _operator(m, oracle_csr(m), a), _operator(r, oracle_csr(r), b)
             assert np.abs(A - B).max() <= 1e-12 * np.abs(A).max()
+
+
+@pytest.mark.gpu
+def test_cyclic_only_polymesh_binds_as_the_reference_reads_it(tmp_path):
+    """A polyMesh whose only pairs are 'cyclic' keeps iOCFacesStart = 0, as the reference
+    leaves it, so the pairs' areas come from faces 1..noc: the library binds it and its
+    Laplacian and gradients are the oracle's bit for bit."""
+    from freecappuccino_gb300.polymesh import read_polymesh, write_polymesh
+
+    write_polymesh(oc_split_mesh(6, cyclic=True), str(tmp_path))
+    m = read_polymesh(str(tmp_path))
+    assert m.noc == m.ncyc > 0 and m.iOCFacesStart == 0
+    c = fcg.Context(m)
+    mu, phi, su = _fields(m)
+    a, su_g = c.laplacian(mu, phi, su)
+    a_o, su_o = oracle.laplacian(oracle_mesh(m), oracle_csr(m), mu, phi, su)
+    assert np.array_equal(a, a_o) and np.array_equal(su_g, su_o)
+    ph = fcg.uniform(2, 1, m.numTotal)
+    assert np.array_equal(c.grad(ph, "gauss", nigrad=2),
+                          oracle.grad_gauss(oracle_mesh(m), ph, nigrad=2))
+    c.close()
