@@ -183,10 +183,10 @@ int oc_geometry(fcg_context *c);
 inline int refuse_oc(fcg_context *c, const char *what) {
   return c->mv.noc ? set_error(c, FCG_ERR_UNSUPPORTED,
                                std::string(what) + ": O-C grid cuts and cyclic faces (noc > 0)"
-                                                   " are supported by the SIMPLE and PISO"
-                                                   " pressure-correction paths only (assembly,"
-                                                   " corrections, gradients, bpres, dpcg, iccg,"
-                                                   " bicgstab, spmv)")
+                                                   " are supported by the reference's routines"
+                                                   " only (assembly, gradients, bpres, dpcg,"
+                                                   " iccg, bicgstab, spmv), not by the mixed,"
+                                                   " multi-RHS, batched or learned solvers")
                    : FCG_OK;
 }
 int cuda_fail(fcg_context *c, cudaError_t e, const char *where);

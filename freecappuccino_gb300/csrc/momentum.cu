@@ -202,6 +202,75 @@ __global__ void __launch_bounds__(kTPB)
   }
 }
 
+// The O-C pairs (calcuvw.f90:186-215, fieldManipulation.f90:110-125): facefluxuvw_cyclic
+// (faceflux_velocity.f90:189-354, what the generic facefluxuvw resolves to for the
+// pairs) and presFaceDivInner on face ijlFace(i) with foc(i), the pair's mass flux fmoc(i)
+// after the inner faces' fluxes, computed in place: the distance is |S| / srdoc(i) and
+// the vector dpn S / |S|, sngrad keeps the cell centres.  ar = can and al = cap go after
+// the CSR values of a (not halved for Crank-Nicolson: :380 halves a only).
+template <int S>
+__global__ void __launch_bounds__(kTPB)
+    k_uvw_oc(MeshView m, fcg_uvw_params prm, UvwView F, double *__restrict__ a,
+             double *__restrict__ osrc, double *__restrict__ odiv) {
+  FCG_GRID_STRIDE(i, m.noc) {
+    const int p = m.oc_l[i], q = m.oc_r[i], f = m.oc_fl[i];
+    const double arx = m.arx[f], ary = m.ary[f], arz = m.arz[f];
+    const double xf = m.xf[f], yf = m.yf[f], zf = m.zf[f];
+    const double lambda = m.oc_foc[i];
+    const double flomass = F.flmass[m.nin + i];
+    const double fxn = lambda, fxp = 1.0 - lambda;
+    const double are = sqrt(arx * arx + ary * ary + arz * arz);
+    const double dpn = are / m.oc_srdoc[i];
+    const double xpn = dpn * arx / are, ypn = dpn * ary / are, zpn = dpn * arz / are;
+    const double game = F.vis[p] * fxp + F.vis[q] * fxn;
+    const double de = game * are / dpn;
+    const double can = -de + rmin(flomass, 0.0);
+    const double cap = -de - rmax(flomass, 0.0);
+    const double cxpn = m.xc[q] - m.xc[p], cypn = m.yc[q] - m.yc[p], czpn = m.zc[q] - m.zc[p];
+    const double vole = cxpn * arx + cypn * ary + czpn * arz;
+    const double rvx = arx / vole, rvy = ary / vole, rvz = arz / vole;
+    const SnGrad du = sngrad(p, q, rvx, rvy, rvz, fxp, fxn, cxpn, cypn, czpn, F.u, F.dU);
+    const SnGrad dv = sngrad(p, q, rvx, rvy, rvz, fxp, fxn, cxpn, cypn, czpn, F.v, F.dV);
+    const SnGrad dw = sngrad(p, q, rvx, rvy, rvz, fxp, fxn, cxpn, cypn, czpn, F.w, F.dW);
+    const double fdue = game * ((du.xii + du.xii) * arx + (du.yii + dv.xii) * ary + (du.zii + dw.xii) * arz);
+    const double fdve = game * ((du.yii + dv.xii) * arx + (dv.yii + dv.yii) * ary + (dv.zii + dw.yii) * arz);
+    const double fdwe = game * ((du.zii + dw.xii) * arx + (dw.yii + dv.zii) * ary + (dw.zii + dw.zii) * arz);
+    const double fdui = de * (du.xi * xpn + du.yi * ypn + du.zi * zpn);
+    const double fdvi = de * (dv.xi * xpn + dv.yi * ypn + dv.zi * zpn);
+    const double fdwi = de * (dw.xi * xpn + dw.yi * ypn + dw.zi * zpn);
+    const double fpos = rmax(flomass, 0.0), fneg = rmin(flomass, 0.0);
+    const double fuuds = fpos * F.u[p] + fneg * F.u[q];
+    const double fvuds = fpos * F.v[p] + fneg * F.v[q];
+    const double fwuds = fpos * F.w[p] + fneg * F.w[q];
+    const bool fwd = flomass >= 0.0;
+    const int uc = fwd ? p : q, dc = fwd ? q : p;
+    const double lam = fwd ? fxp : fxn;
+    const double dxp = xf - m.xc[p], dyp = yf - m.yc[p], dzp = zf - m.zc[p];
+    const double dxq = xf - m.xc[q], dyq = yf - m.yc[q], dzq = zf - m.zc[q];
+    const Offs o = fwd ? Offs{dxp, dyp, dzp, dxq, dyq, dzq} : Offs{dxq, dyq, dzq, dxp, dyp, dzp};
+    const double ue = face_value<S>(m, prm.limiter, uc, dc, lam, f, o, F.u, F.dU);
+    const double ve = face_value<S>(m, prm.limiter, uc, dc, lam, f, o, F.v, F.dV);
+    const double we = face_value<S>(m, prm.limiter, uc, dc, lam, f, o, F.w, F.dW);
+    const double gam = prm.gds;
+    osrc[3 * i] = -gam * (flomass * ue - fuuds) + fdue - fdui;
+    osrc[3 * i + 1] = -gam * (flomass * ve - fvuds) + fdve - fdvi;
+    osrc[3 * i + 2] = -gam * (flomass * we - fwuds) + fdwe - fdwi;
+    a[m.nnz + i] = can;          // ar(i)
+    a[m.nnz + m.noc + i] = cap;  // al(i)
+    const double *dP = F.dP;  // presFaceDivInner, df(ijp,k) on the flat (3,n) array
+    const double dfxi = dP[p] * fxp + dP[q] * fxn;
+    const double dfyi = dP[p + 3] * fxp + dP[q + 3] * fxn;
+    const double dfzi = dP[p + 6] * fxp + dP[q + 6] * fxn;
+    const double xi = m.xc[p] * fxp + m.xc[q] * fxn, yi = m.yc[p] * fxp + m.yc[q] * fxn,
+                 zi = m.zc[p] * fxp + m.zc[q] * fxn;
+    const double fie = F.p[p] * fxp + F.p[q] * fxn + dfxi * (xf - xi) + dfyi * (yf - yi) +
+                       dfzi * (zf - zi);
+    odiv[3 * i] = fie * arx;
+    odiv[3 * i + 1] = fie * ary;
+    odiv[3 * i + 2] = fie * arz;
+  }
+}
+
 // Sum of the row's values in row order with `dv` in place of the diagonal (Fortran SUM).
 __device__ __forceinline__ double row_sum(const MeshView &m, const double *__restrict__ a,
                                           int c, double dv) {
@@ -215,6 +284,7 @@ __global__ void k_uvw_cells(MeshView m, fcg_uvw_params prm, UvwView F, int bst_i
                             int bst_out, const double *__restrict__ bg, long long ncb,
                             double *__restrict__ a,
                             const double *__restrict__ fsrc, const double *__restrict__ fdiv,
+                            const double *__restrict__ osrc, const double *__restrict__ odiv,
                             double *__restrict__ diag_vw, double *__restrict__ rhs,
                             double *__restrict__ ap) {
   const double small = (double)1e-20f;  // parameters::small, modules_allocatable.f90:27
@@ -239,6 +309,19 @@ __global__ void k_uvw_cells(MeshView m, fcg_uvw_params prm, UvwView F, int bst_i
         s2 = s2 + fdiv[3 * f + 2];
       }
     }
+    if (m.noc)  // the O-C pairs (fieldManipulation.f90:110-125)
+      for (int e = m.oc_cptr[c]; e < m.oc_cptr[c + 1]; ++e) {
+        const int v = m.oc_vix[e], i = v < m.noc ? v : v - m.noc;
+        if (v < m.noc) {
+          s0 = s0 - odiv[3 * i];
+          s1 = s1 - odiv[3 * i + 1];
+          s2 = s2 - odiv[3 * i + 2];
+        } else {
+          s0 = s0 + odiv[3 * i];
+          s1 = s1 + odiv[3 * i + 1];
+          s2 = s2 + odiv[3 * i + 2];
+        }
+      }
     for (int e = b0; e < b1; ++e) {
       const int f = m.cb_face[e];
       const double pb = F.p[m.cb_slot[e]];
@@ -290,6 +373,23 @@ __global__ void k_uvw_cells(MeshView m, fcg_uvw_params prm, UvwView F, int bst_i
         s2 = s2 - fsrc[3 * f + 2];
       }
     }
+    if (m.noc)  // the O-C pairs (:186-215): ar (left cell) or al (right) off sp, the sources
+      for (int e = m.oc_cptr[c]; e < m.oc_cptr[c + 1]; ++e) {
+        const int v = m.oc_vix[e], i = v < m.noc ? v : v - m.noc;
+        const double co = a[m.nnz + v];
+        sp0 = sp0 - co;
+        sp1 = sp1 - co;
+        sp2 = sp2 - co;
+        if (v < m.noc) {
+          s0 = s0 + osrc[3 * i];
+          s1 = s1 + osrc[3 * i + 1];
+          s2 = s2 + osrc[3 * i + 2];
+        } else {
+          s0 = s0 - osrc[3 * i];
+          s1 = s1 - osrc[3 * i + 1];
+          s2 = s2 - osrc[3 * i + 2];
+        }
+      }
     // boundary loops (:223-378): inlet, outlet, symmetry, wall
     for (int e = b0; e < b1; ++e) {
       const int t = m.cb_type[e];
@@ -402,7 +502,6 @@ extern "C" int fcg_calcuvw(fcg_context *c, const fcg_uvw_params *prm, const fcg_
                            double *a, double *diag_vw, double *rhs, double *ap) {
   if (!c || !prm || !f) return FCG_ERR_ARG;
   if (!c->bound) return set_error(c, FCG_ERR_STATE, "fcg_calcuvw before fcg_bind_mesh");
-  if (c->mv.noc) return refuse_oc(c, "fcg_calcuvw");
   const bool need_old = prm->bdf || prm->cn;
   const bool need_oo = prm->bdf && prm->btime > (double)0.99f;
   const bool need_t = prm->buoyancy && prm->boussinesq;
@@ -423,6 +522,8 @@ extern "C" int fcg_calcuvw(fcg_context *c, const fcg_uvw_params *prm, const fcg_
   FCG_CUDA_TRY(c, cudaSetDevice(c->device));
   const size_t nt = sizeof(double) * c->ntot, n1 = sizeof(double) * c->n, n3 = 3 * n1;
   const size_t fb = sizeof(double) * (c->nin > 0 ? c->nin : 1);
+  // flmass with the O-C pairs' fmoc after the inner faces' fluxes
+  const size_t fbo = sizeof(double) * (c->nin + c->mv.noc > 0 ? c->nin + c->mv.noc : 1);
   struct In {
     const double *src;
     size_t bytes;
@@ -432,7 +533,8 @@ extern "C" int fcg_calcuvw(fcg_context *c, const fcg_uvw_params *prm, const fcg_
              {f->t, n1, need_t},    {f->uo, n1, need_old},   {f->vo, n1, need_old},
              {f->wo, n1, need_old}, {f->uoo, n1, need_oo},   {f->voo, n1, need_oo},
              {f->woo, n1, need_oo}, {f->dUdxi, n3, true},    {f->dVdxi, n3, true},
-             {f->dWdxi, n3, true},  {f->dPdxi, n3, true},    {f->flmass, fb, c->nin > 0},
+             {f->dWdxi, n3, true},  {f->dPdxi, n3, true},
+             {f->flmass, fbo, c->nin + c->mv.noc > 0},
              {f->fmi, sizeof(double) * (ninl > 0 ? ninl : 1), ninl > 0},
              {f->fmo, sizeof(double) * (nout > 0 ? nout : 1), nout > 0}};
   const int NI = (int)(sizeof(ins) / sizeof(ins[0]));
@@ -450,15 +552,32 @@ extern "C" int fcg_calcuvw(fcg_context *c, const fcg_uvw_params *prm, const fcg_
             dev[14], dev[15], dev[16], dev[17], dev[18], dev[19]};
   void *da, *ddv, *drhs, *dap;
   bool ha, hdv, hrhs, hap;
-  if ((rc = stage_in(c, a, sizeof(double) * c->nnz, NI, true, &da, &ha)) ||
+  const size_t alen = sizeof(double) * (size_t)a_len(c);  // with ar, al of the O-C pairs
+  if ((rc = stage_in(c, a, alen, NI, true, &da, &ha)) ||
       (rc = stage_in(c, diag_vw, 2 * n1, NI + 1, false, &ddv, &hdv)) ||
       (rc = stage_in(c, rhs, n3, NI + 2, false, &drhs, &hrhs)) ||
       (rc = stage_in(c, ap, n3, NI + 3, false, &dap, &hap)))
     return rc;
-  // face terms: 3 sources + 3 pressure-divergence terms per inner face
-  FCG_CUDA_TRY(c, c->scratch.ensure(6 * fb));
+  // face terms: 3 sources + 3 pressure-divergence terms per inner face and per O-C pair
+  const size_t noc = (size_t)c->mv.noc;
+  FCG_CUDA_TRY(c, c->scratch.ensure(6 * fb + 6 * sizeof(double) * (noc > 0 ? noc : 1)));
   double *fsrc = c->scratch.as<double>(), *fdiv = fsrc + 3 * (c->nin > 0 ? c->nin : 1);
+  double *osrc = fdiv + 3 * (c->nin > 0 ? c->nin : 1), *odiv = osrc + 3 * (noc > 0 ? noc : 1);
   const MeshView &m = c->mv;
+  if (m.noc > 0) {
+    auto pairs = k_uvw_oc<FCG_CONV_MUSCL>;
+    switch (prm->scheme) {
+      case FCG_CONV_CDS: pairs = k_uvw_oc<FCG_CONV_CDS>; break;
+      case FCG_CONV_CDS_CORRECTED: pairs = k_uvw_oc<FCG_CONV_CDS_CORRECTED>; break;
+      case FCG_CONV_CENTRAL: pairs = k_uvw_oc<FCG_CONV_CENTRAL>; break;
+      case FCG_CONV_SECOND_UPWIND: pairs = k_uvw_oc<FCG_CONV_SECOND_UPWIND>; break;
+      case FCG_CONV_FLUX_LIMITER: pairs = k_uvw_oc<FCG_CONV_FLUX_LIMITER>; break;
+      default: break;
+    }
+    pairs<<<grid_for(m.noc, c->num_sms), kTPB, 0, c->stream>>>(m, *prm, V, (double *)da, osrc,
+                                                                 odiv);
+    FCG_CHECK_LAUNCH(c, "k_uvw_oc");
+  }
   if (m.nin > 0) {
     const double *geo;
     if ((rc = face_geo(c, &geo))) return rc;
@@ -480,10 +599,10 @@ extern "C" int fcg_calcuvw(fcg_context *c, const fcg_uvw_params *prm, const fcg_
   long long ncb = 0;
   for (int t = 0; t < B_NTYPES; ++t) ncb += c->cnt[t];
   k_uvw_cells<<<grid_for(m.n, c->num_sms), kTPB, 0, c->stream>>>(
-      m, *prm, V, c->bst[B_INLET], c->bst[B_OUTLET], bg, ncb, (double *)da, fsrc, fdiv,
-      (double *)ddv, (double *)drhs, (double *)dap);
+      m, *prm, V, c->bst[B_INLET], c->bst[B_OUTLET], bg, ncb, (double *)da, fsrc, fdiv, osrc,
+      odiv, (double *)ddv, (double *)drhs, (double *)dap);
   FCG_CHECK_LAUNCH(c, "k_uvw_cells");
-  if ((rc = stage_out(c, a, da, sizeof(double) * c->nnz, ha)) ||
+  if ((rc = stage_out(c, a, da, alen, ha)) ||
       (rc = stage_out(c, diag_vw, ddv, 2 * n1, hdv)) ||
       (rc = stage_out(c, rhs, drhs, n3, hrhs)) || (rc = stage_out(c, ap, dap, n3, hap)))
     return rc;

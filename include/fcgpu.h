@@ -91,10 +91,10 @@ typedef struct fcg_mesh_desc {
    * correction paths take the pairs: fcg_laplacian, fcg_facefluxmass, fcg_fluxmc,
    * fcg_flux_correct, fcg_continuity_errors, fcg_correct_fields, fcg_correct_bc_velocity,
    * fcg_facefluxmass_piso, fcg_piso_hbya, fcg_adjust_mass_flow,
-   * fcg_set_reference_pressure, fcg_correct_velocity_piso, fcg_grad, fcg_grad_lsq_matrix,
-   * fcg_bpres, fcg_dpcg, fcg_iccg, fcg_bicgstab and fcg_spmv; the momentum assembly
-   * (fcg_calcuvw) and the mixed, multi-RHS, batched and learned solvers return
-   * FCG_ERR_UNSUPPORTED on such a mesh. */
+   * fcg_set_reference_pressure, fcg_correct_velocity_piso, the momentum assembly
+   * fcg_calcuvw, fcg_grad, fcg_grad_lsq_matrix, fcg_bpres, fcg_dpcg, fcg_iccg,
+   * fcg_bicgstab and fcg_spmv; the mixed, multi-RHS, batched and learned solvers (no
+   * reference counterpart) return FCG_ERR_UNSUPPORTED on such a mesh. */
   int ncyc;
   int iOCFacesStart;
   const int *ijlFace, *ijrFace; /* [noc] */

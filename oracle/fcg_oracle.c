@@ -1211,6 +1211,55 @@ static void facefluxuvw(const orc_mesh *m, const orc_uvw_params *prm, int ijp, i
   *swp = -gam * (fwhigh - fwuds) + fdwe - fdwi;
 }
 
+/* facefluxuvw_cyclic (faceflux_velocity.f90:189-354), which the generic facefluxuvw
+ * resolves to for the O-C pairs (calcuvw.f90:193-194): facefluxuvw with the distance
+ * dpn = |S| / srd and the vector (xpn, ypn, zpn) = dpn S / |S| (sngrad keeps the cell
+ * centres). */
+static void facefluxuvw_cyclic(const orc_mesh *m, const orc_uvw_params *prm, int ijp, int ijn,
+                               double xf, double yf, double zf, double arx, double ary,
+                               double arz, double flomass, double lambda, double gam,
+                               double srd, const double *u, const double *v, const double *w,
+                               const double *vis, const double *dUdxi, const double *dVdxi,
+                               const double *dWdxi, double *cap, double *can, double *sup,
+                               double *svp, double *swp) {
+  const double fxn = lambda, fxp = 1.0 - lambda;
+  const double are = sqrt(arx * arx + ary * ary + arz * arz);
+  const double dpn = are / srd;
+  const double xpn = dpn * arx / are, ypn = dpn * ary / are, zpn = dpn * arz / are;
+  const double game = F(vis, ijp) * fxp + F(vis, ijn) * fxn;
+  const double de = game * are / dpn;
+  *can = -de + rmin(flomass, 0.0);
+  *cap = -de - rmax(flomass, 0.0);
+  double duxi, duyi, duzi, duxii, duyii, duzii, dvxi, dvyi, dvzi, dvxii, dvyii, dvzii;
+  double dwxi, dwyi, dwzi, dwxii, dwyii, dwzii;
+  sngrad(m, ijp, ijn, arx, ary, arz, lambda, u, dUdxi, &duxi, &duyi, &duzi, &duxii, &duyii, &duzii);
+  sngrad(m, ijp, ijn, arx, ary, arz, lambda, v, dVdxi, &dvxi, &dvyi, &dvzi, &dvxii, &dvyii, &dvzii);
+  sngrad(m, ijp, ijn, arx, ary, arz, lambda, w, dWdxi, &dwxi, &dwyi, &dwzi, &dwxii, &dwyii, &dwzii);
+  const double fdue = game * ((duxii + duxii) * arx + (duyii + dvxii) * ary + (duzii + dwxii) * arz);
+  const double fdve = game * ((duyii + dvxii) * arx + (dvyii + dvyii) * ary + (dvzii + dwyii) * arz);
+  const double fdwe = game * ((duzii + dwxii) * arx + (dwyii + dvzii) * ary + (dwzii + dwzii) * arz);
+  const double fdui = game * are / dpn * (duxi * xpn + duyi * ypn + duzi * zpn);
+  const double fdvi = game * are / dpn * (dvxi * xpn + dvyi * ypn + dvzi * zpn);
+  const double fdwi = game * are / dpn * (dwxi * xpn + dwyi * ypn + dwzi * zpn);
+  const double fuuds = rmax(flomass, 0.0) * F(u, ijp) + rmin(flomass, 0.0) * F(u, ijn);
+  const double fvuds = rmax(flomass, 0.0) * F(v, ijp) + rmin(flomass, 0.0) * F(v, ijn);
+  const double fwuds = rmax(flomass, 0.0) * F(w, ijp) + rmin(flomass, 0.0) * F(w, ijn);
+  double ue, ve, we;
+  if (flomass >= 0.0) {
+    ue = face_value(m, prm, ijp, ijn, xf, yf, zf, fxp, u, dUdxi);
+    ve = face_value(m, prm, ijp, ijn, xf, yf, zf, fxp, v, dVdxi);
+    we = face_value(m, prm, ijp, ijn, xf, yf, zf, fxp, w, dWdxi);
+  } else {
+    ue = face_value(m, prm, ijn, ijp, xf, yf, zf, fxn, u, dUdxi);
+    ve = face_value(m, prm, ijn, ijp, xf, yf, zf, fxn, v, dVdxi);
+    we = face_value(m, prm, ijn, ijp, xf, yf, zf, fxn, w, dWdxi);
+  }
+  const double fuhigh = flomass * ue, fvhigh = flomass * ve, fwhigh = flomass * we;
+  *sup = -gam * (fuhigh - fuuds) + fdue - fdui;
+  *svp = -gam * (fvhigh - fvuds) + fdve - fdvi;
+  *swp = -gam * (fwhigh - fwuds) + fdwe - fdwi;
+}
+
 /* The cb coefficient of facefluxuvw_boundary (faceflux_velocity.f90:403-468): the only
  * result calcuvw's inlet and outlet loops use. */
 static double boundary_cb(const orc_mesh *m, int ijp, int ijb, int iface, double flomass,
@@ -1264,6 +1313,28 @@ int orc_calcuvw(const orc_mesh *m, const int *ioffset, const int *diag, const in
     const double fie = F(p, ijp) * fxp + F(p, ijn) * fxn + dfxi * (F(m->xf, i) - xi) +
                        dfyi * (F(m->yf, i) - yi) + dfzi * (F(m->zf, i) - zi);
     const double dfxe = fie * F(m->arx, i), dfye = fie * F(m->ary, i), dfze = fie * F(m->arz, i);
+    F(su, ijp) = F(su, ijp) - dfxe;
+    F(sv, ijp) = F(sv, ijp) - dfye;
+    F(sw, ijp) = F(sw, ijp) - dfze;
+    F(su, ijn) = F(su, ijn) + dfxe;
+    F(sv, ijn) = F(sv, ijn) + dfye;
+    F(sw, ijn) = F(sw, ijn) + dfze;
+  }
+  oc_pairs oc;
+  if (get_oc(m, &oc)) return -9;
+  for (int i = 1; i <= m->noc; ++i) { /* O- and C-grid cuts (fieldManipulation.f90:110-125) */
+    const int iface = F(m->ijlFace, i), ijp = F(oc.ijl, i), ijn = F(oc.ijr, i);
+    const double fxn = F(oc.foc, i), fxp = 1.0 - fxn;
+    const double xi = F(m->xc, ijp) * fxp + F(m->xc, ijn) * fxn;
+    const double yi = F(m->yc, ijp) * fxp + F(m->yc, ijn) * fxn;
+    const double zi = F(m->zc, ijp) * fxp + F(m->zc, ijn) * fxn;
+    const double dfxi = dPdxi[ijp - 1] * fxp + dPdxi[ijn - 1] * fxn;
+    const double dfyi = dPdxi[ijp - 1 + 3] * fxp + dPdxi[ijn - 1 + 3] * fxn;
+    const double dfzi = dPdxi[ijp - 1 + 6] * fxp + dPdxi[ijn - 1 + 6] * fxn;
+    const double fie = F(p, ijp) * fxp + F(p, ijn) * fxn + dfxi * (F(m->xf, iface) - xi) +
+                       dfyi * (F(m->yf, iface) - yi) + dfzi * (F(m->zf, iface) - zi);
+    const double dfxe = fie * F(m->arx, iface), dfye = fie * F(m->ary, iface),
+                 dfze = fie * F(m->arz, iface);
     F(su, ijp) = F(su, ijp) - dfxe;
     F(sv, ijp) = F(sv, ijp) - dfye;
     F(sw, ijp) = F(sw, ijp) - dfze;
@@ -1332,6 +1403,31 @@ int orc_calcuvw(const orc_mesh *m, const int *ioffset, const int *diag, const in
     F(sv, ijn) = F(sv, ijn) - svp;
     F(sw, ijn) = F(sw, ijn) - swp;
   }
+  if (m->noc > 0) { /* O- and C-grid cuts (:186-215): ar, al after the CSR values */
+    double *ar = a + nnz, *al = a + nnz + m->noc;
+    const double *fmoc = flmass + m->numInnerFaces;
+    for (int i = 1; i <= m->noc; ++i) {
+      const int iface = F(m->ijlFace, i), ijp = F(oc.ijl, i), ijn = F(oc.ijr, i);
+      double sup, svp, swp;
+      facefluxuvw_cyclic(m, prm, ijp, ijn, F(m->xf, iface), F(m->yf, iface), F(m->zf, iface),
+                         F(m->arx, iface), F(m->ary, iface), F(m->arz, iface), F(fmoc, i),
+                         F(oc.foc, i), prm->gds, F(oc.srdoc, i), u, v, w, vis, dUdxi, dVdxi,
+                         dWdxi, &F(al, i), &F(ar, i), &sup, &svp, &swp);
+      F(spu, ijp) = F(spu, ijp) - F(ar, i);
+      F(spv, ijp) = F(spv, ijp) - F(ar, i);
+      F(sp, ijp) = F(sp, ijp) - F(ar, i);
+      F(spu, ijn) = F(spu, ijn) - F(al, i);
+      F(spv, ijn) = F(spv, ijn) - F(al, i);
+      F(sp, ijn) = F(sp, ijn) - F(al, i);
+      F(su, ijp) = F(su, ijp) + sup;
+      F(sv, ijp) = F(sv, ijp) + svp;
+      F(sw, ijp) = F(sw, ijp) + swp;
+      F(su, ijn) = F(su, ijn) - sup;
+      F(sv, ijn) = F(sv, ijn) - svp;
+      F(sw, ijn) = F(sw, ijn) - swp;
+    }
+  }
+  free_oc(&oc);
   /* inlet and outlet (:223-264) */
   for (int pass = 0; pass < 2; ++pass) {
     const int cnt = pass == 0 ? m->ninl : m->nout;

@@ -300,8 +300,8 @@ def test_calcp_face_fluxes_with_pairs_bit_exact(cyclic):
 
 @pytest.mark.gpu
 def test_entry_points_without_pairs_refuse_the_mesh():
-    """The momentum assembly and the mixed, multi-RHS and learned solvers do not take the
-    pairs: FCG_ERR_UNSUPPORTED (-8), the context still usable."""
+    """The mixed and multi-RHS solvers, which have no reference counterpart, do not take
+    the pairs: FCG_ERR_UNSUPPORTED (-8), the context still usable."""
     from freecappuccino_gb300._lib import FcgError
 
     m, c = _gpu(6)
@@ -346,7 +346,9 @@ def test_polymesh_round_trip_keeps_the_pairs(tmp_path):
 def test_cyclic_only_polymesh_binds_as_the_reference_reads_it(tmp_path):
     """A polyMesh whose only pairs are 'cyclic' keeps iOCFacesStart = 0, as the reference
     leaves it, so the pairs' areas come from faces 1..noc: the library binds it and its
-    Laplacian and gradients are the oracle's bit for bit."""
+    Laplacian and gradients are the oracle's bit for bit. Those inner faces lie across the
+    pairs' direction, so ar and al come out infinite and the wall cells among the pairs' get
+    NaN sources, in the oracle as in the library: NaN compares equal here."""
     from freecappuccino_gb300.polymesh import read_polymesh, write_polymesh
 
     write_polymesh(oc_split_mesh(6, cyclic=True), str(tmp_path))
@@ -356,8 +358,73 @@ def test_cyclic_only_polymesh_binds_as_the_reference_reads_it(tmp_path):
     mu, phi, su = _fields(m)
     a, su_g = c.laplacian(mu, phi, su)
     a_o, su_o = oracle.laplacian(oracle_mesh(m), oracle_csr(m), mu, phi, su)
-    assert np.array_equal(a, a_o) and np.array_equal(su_g, su_o)
+    assert np.isinf(a_o).any() and np.isnan(su_o).any()
+    assert np.array_equal(a, a_o) and np.array_equal(su_g, su_o, equal_nan=True)
     ph = fcg.uniform(2, 1, m.numTotal)
     assert np.array_equal(c.grad(ph, "gauss", nigrad=2),
                           oracle.grad_gauss(oracle_mesh(m), ph, nigrad=2))
+    c.close()
+
+
+def _uvw_fields(m, flmass, seed=5):
+    """Momentum inputs from cell values (boundary slots 0) and the given face fluxes."""
+    n, nt = m.numCells, m.numTotal
+    pad = lambda x: np.concatenate([x, np.zeros(nt - n)])
+    f = {k: pad(fcg.uniform(seed, i, n)) for i, k in enumerate(("u", "v", "w", "p"), start=1)}
+    f["vis"] = pad(1e-3 * (1.0 + 0.5 * fcg.uniform(seed, 50, n, 0.0, 1.0)))
+    f["den"] = 1.0 + 0.2 * fcg.uniform(seed, 30, n)
+    for k, name in enumerate(("dUdxi", "dVdxi", "dWdxi", "dPdxi")):
+        f[name] = fcg.uniform(seed, 10 + k, 3 * n).reshape(n, 3)
+    for k, s in (("t", 54), ("uo", 55), ("vo", 56), ("wo", 57), ("uoo", 58), ("voo", 59),
+                 ("woo", 60)):
+        f[k] = fcg.uniform(seed, s, n) + (290.0 if k == "t" else 0.0)
+    f["flmass"], f["fmi"], f["fmo"] = flmass, np.zeros(0), np.zeros(0)
+    return f
+
+
+def _uvw_oracle(m, kw, f, a):
+    from tests.test_momentum import _oracle
+
+    return _oracle(m, oracle_csr(m), kw, f, a)
+
+
+def test_oracle_momentum_of_the_cut_mesh_is_the_uncut_one():
+    """calcuvw's pairs (facefluxuvw_cyclic and presFaceDivInner, calcuvw.f90:186-215,
+    fieldManipulation.f90:110-125) carry the cut faces' terms: on the unjittered cut mesh
+    the momentum operators, diagonals, sources and ap are the uncut mesh's."""
+    N = 6
+    m, u = oc_split_mesh(N), fcg.hex_mesh(N)
+    nin = u.numInnerFaces
+    cut = ((u.owner[:nin] - 1) // (N * N) == N // 2 - 1) & ((u.neighbour - 1) // (N * N) == N // 2)
+    fl = 0.05 * fcg.uniform(5, 51, nin)
+    fu = _uvw_fields(u, fl)
+    fm = _uvw_fields(m, np.concatenate([fl[~cut], fl[cut]]))
+    for kw in (dict(scheme="central"), dict(scheme="muscl", bdf=True, timestep=0.01),
+               dict(scheme="flux_limiter", limiter="smart")):
+        am, dm, rm, pm = _uvw_oracle(m, kw, fm, np.zeros(m.nnz + 2 * m.noc))
+        au, du, ru, pu = _uvw_oracle(u, kw, fu, np.zeros(u.nnz))
+        A, B = _operator(m, oracle_csr(m), am), _operator(u, oracle_csr(u), au)
+        assert np.abs(A - B).max() <= 1e-11 * np.abs(B).max(), kw
+        for x, y in ((dm, du), (rm, ru), (pm, pu)):
+            assert np.abs(x - y).max() <= 1e-11 * np.abs(y).max(), kw
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cyclic", [False, True])
+def test_calcuvw_with_pairs_bit_exact(cyclic):
+    """fcg_calcuvw on the cut mesh with every option set of the momentum tests, bit for bit
+    against the oracle (ar, al after the CSR values; the pairs' fmoc after the inner
+    faces' fluxes)."""
+    from tests.test_momentum import OPTS
+
+    m, c = _gpu(8, cyclic)
+    f = _uvw_fields(m, 0.05 * fcg.uniform(5, 51, m.numInnerFaces + m.noc))
+    a = fcg.uniform(5, 70, m.nnz + 2 * m.noc)
+    keys = ("u", "v", "w", "p", "vis", "den", "dUdxi", "dVdxi", "dWdxi", "dPdxi", "flmass")
+    for kw in OPTS:
+        got = c.calcuvw(*[f[k] for k in keys], a, f["fmi"], f["fmo"], t=f["t"], uo=f["uo"],
+                        vo=f["vo"], wo=f["wo"], uoo=f["uoo"], voo=f["voo"], woo=f["woo"], **kw)
+        ref = _uvw_oracle(m, kw, f, a)
+        for key, r in zip(("a", "diag_vw", "rhs", "ap"), ref):
+            assert np.array_equal(got[key], r), (kw, key)
     c.close()
