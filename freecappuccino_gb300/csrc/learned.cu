@@ -1,5 +1,5 @@
 // Learned preconditioner and flexible CG (no counterpart in the reference; it builds on
-// the DPCG of dpcg.f90, which stays the fallback and the judge of the result).
+// the DPCG of dpcg.f90, which stays the fallback and the check on the result).
 //
 // The network maps the residual of the Jacobi-scaled pressure system,
 // r^ = D^-1/2 r with Ahat = D^-1/2 A D^-1/2, to an approximation of its error

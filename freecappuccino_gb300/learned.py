@@ -4,7 +4,7 @@ No reference counterpart: the reference solves the pressure equation with dpcg/i
 (dpcg.f90, iccg.f90).  Here a small message-passing network (libfcgpu.so, learned.cu)
 approximates the inverse of the Jacobi-scaled pressure matrix and serves as the
 preconditioner of a flexible CG; plain FP64 DPCG stays the fallback (taken when the
-FCG stalls) and the judge of the result (the stop test is dpcg.f90's L1 test on the
+FCG stalls) and the check on the result (the stop test is dpcg.f90's L1 test on the
 FP64 residual).  Training data are (residual, error) pairs of DPCG iterates on seeded
 jittered meshes with a smoothed log-uniform diffusivity; training runs on the GPU
 through the library's own forward, backward and Adam kernels.
