@@ -474,15 +474,10 @@ __global__ void __launch_bounds__(kTPB, 4)
 __device__ __forceinline__ float out_dot(const __nv_bfloat16 *__restrict__ h, long long i,
                                          const float *w) {
   const uint4 *hp = reinterpret_cast<const uint4 *>(h + i * C);
-  float acc = w[C];
+  uint4 v[4];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const uint4 v = __ldg(hp + q);
-    const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(&v);
-#pragma unroll
-    for (int c = 0; c < 8; ++c) acc += w[q * 8 + c] * bf(e[c]);
-  }
-  return acc;
+  for (int q = 0; q < 4; ++q) v[q] = __ldg(hp + q);
+  return lp::out_dot_vals(v, w);
 }
 
 // Output with the Jacobi skip: y = r/rms + w_out . h_L + b_out (the normalised output),
@@ -1224,8 +1219,13 @@ bool layer_split() {
 // NULL) turns the launches into no-ops; `status` (device int or NULL) receives a wait
 // timeout of the plane-staged layer.  Inference on a lexicographic hex mesh runs that
 // layer (learned_hex.cu, the same bits as k_lp_layer).
+// The forward pass of the network on r.  With `out` given (inference), the plane-staged
+// form writes the output z of lphex::OutFuse from its last layer and sets *fused; the
+// caller runs the output kernel itself when *fused stays false.
 void enqueue_forward(fcg_learned *Lp, fcg_context *c, cudaStream_t st, const float *r, bool train,
-                     const int *done, unsigned *rms_ticket, int *status) {
+                     const int *done, unsigned *rms_ticket, int *status,
+                     const fcg::lphex::OutFuse *out = nullptr, bool *fused = nullptr) {
+  if (fused) *fused = false;
   const int n = c->n;
   float *rms = Lp->scal.as<float>();
   const float *prm = Lp->params.as<float>();
@@ -1250,7 +1250,8 @@ void enqueue_forward(fcg_learned *Lp, fcg_context *c, cudaStream_t st, const flo
       k_lp_dense<<<lg, kTPB, 0, st>>>(n, hin, H + 2 * hs, hout, wl, bl, done);
     } else if (!train && hex_on(Lp, c) &&
                fcg::lphex::layer(Lp->hex, c->num_sms, hin, hout, Lp->hexval.as<float>(), wl, bl,
-                                 done, status, st) == cudaSuccess) {
+                                 done, status, st, l + 1 == lp::L ? out : nullptr,
+                                 l + 1 == lp::L ? fused : nullptr) == cudaSuccess) {
       // plane-staged form launched
     } else {
       k_lp_layer<<<lg, kTPB, 0, st>>>(c->sv, n, aval, hin, hout, wl, bl,
@@ -1792,13 +1793,17 @@ void enqueue_preconditioner(fcg_learned *Lp, fcg_context *c, cudaStream_t st, co
     fcg::ml::enqueue_jacobi_cycle(*ml_for(Lp, c), c, Lp->mlo, st, r, z, done);
     return;
   }
+  // in the flexible CG the plane-staged last layer writes z itself (the same bits as
+  // k_f_out on h_L, which is then not stored)
+  const fcg::lphex::OutFuse of{r, Lp->scal.as<float>(), Lp->params.as<float>() + lp::oWout, z};
+  bool fused = false;
   enqueue_forward(Lp, c, st, r, false, done, rms_ticket,
-                  S ? &S->status : Lp->scal.as<int>() + kHexStatus);
-  if (S)
+                  S ? &S->status : Lp->scal.as<int>() + kHexStatus, S ? &of : nullptr, &fused);
+  if (S && !fused)
     k_f_out<<<reduction_grid(c), kTPB, 0, st>>>(n, last_activation(Lp, c, false),
                                                 Lp->params.as<float>(), Lp->scal.as<float>(), r,
                                                 z, nullptr, 0, S, nullptr, 0);
-  else
+  else if (!S)
     k_lp_out<<<grid_for(n, c->num_sms), kTPB, 0, st>>>(n, last_activation(Lp, c, false),
                                                        Lp->params.as<float>(),
                                                        Lp->scal.as<float>(), r, nullptr, nullptr,

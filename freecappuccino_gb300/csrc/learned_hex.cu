@@ -30,6 +30,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <cstddef>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -63,11 +64,13 @@ struct __align__(128) Smem {
   float v[S][7][BY][BX];
   __nv_bfloat16 w[C * TS];
   float b[C];
+  float wo[C + 4];  // w_out, b_out of a fused output (padded to 16 bytes)
   __nv_bfloat16 tile[kCons][16 * TS];
   unsigned long long full[S], empty[S];
   int abort, issued;
 };
 constexpr size_t kSmemBytes = sizeof(Smem) + 128;  // + alignment of the dynamic base
+static_assert(offsetof(Smem, tile) % 16 == 0, "the tile rows take 16-byte accesses");
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -128,7 +131,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     k_lp_layer_hex(const __grid_constant__ CUtensorMap tm_h, const __grid_constant__ CUtensorMap tm_v,
                    int nx, int ny, int nz, __nv_bfloat16 *__restrict__ hout,
                    const __nv_bfloat16 *__restrict__ wl, const float *__restrict__ bl,
-                   const int *done, int *status) {
+                   const int *done, int *status, OutFuse of) {
   if (done && __ldcg(done) != 0) return;
   extern __shared__ unsigned char smem_raw[];
   Smem &sm = *reinterpret_cast<Smem *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) &
@@ -141,6 +144,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   for (int t = threadIdx.x; t < C * 2 * C; t += blockDim.x)
     sm.w[(t / (2 * C)) * TS + t % (2 * C)] = wl[t];
   if (threadIdx.x < C) sm.b[threadIdx.x] = bl[threadIdx.x];
+  if (of.z && threadIdx.x <= C) sm.wo[threadIdx.x] = of.wout[threadIdx.x];
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
       mbar_init(&sm.full[s], 1);
@@ -172,6 +176,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else {
     const int g = lane >> 2, qc = 8 * (lane & 3);
     __nv_bfloat16 *tw = sm.tile[warp];
+    const float osc = of.z ? *of.rms : 0.f;
     // every decision to stop is taken by the whole warp (__all_sync / __any_sync), so
     // the warp never splits around its __syncwarp calls
     bool ok = __all_sync(0xffffffffu, mbar_wait(&sm.full[0], 0, abort) &&
@@ -214,14 +219,25 @@ __global__ void __launch_bounds__(kThreads, 1)
         __syncwarp();
         lp::tile_dense(tw, sm.w, sm.b, lane, lp::NoZ());
         const int jg = j0 + jr;
+        if (of.z) {
+          // the output instead of h': lane ri < 16 takes cell ri of the row, with the
+          // operations of the output kernel on the stored h'
+          const int ig = i0 + lane;
+          if (lane < 16 && ig < nx && jg < ny) {
+            const long long cell = ((long long)k * ny + jg) * nx + ig;
+            const float acc = lp::out_dot_row(tw + lane * TS, sm.wo);
+            of.z[cell] = of.r[cell] + osc * acc;
+          }
+        } else {
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          const int e = lane + 32 * q, ri = e >> 2, part = e & 3;
-          const int ig = i0 + ri;
-          if (ig < nx && jg < ny)
-            *reinterpret_cast<uint4 *>(
-                hout + (((long long)k * ny + jg) * nx + ig) * C + 8 * part) =
-                *reinterpret_cast<const uint4 *>(tw + ri * TS + 8 * part);
+          for (int q = 0; q < 2; ++q) {
+            const int e = lane + 32 * q, ri = e >> 2, part = e & 3;
+            const int ig = i0 + ri;
+            if (ig < nx && jg < ny)
+              *reinterpret_cast<uint4 *>(
+                  hout + (((long long)k * ny + jg) * nx + ig) * C + 8 * part) =
+                  *reinterpret_cast<const uint4 *>(tw + ri * TS + 8 * part);
+          }
         }
         __syncwarp();
       }
@@ -630,8 +646,9 @@ cudaError_t values(const fcg_context *c, const HexGrid &g, const float *aval, fl
 
 cudaError_t layer(const HexGrid &g, int num_sms, const __nv_bfloat16 *hin, __nv_bfloat16 *hout,
                   const float *val, const __nv_bfloat16 *wl, const float *bl, const int *done,
-                  int *status, cudaStream_t st) {
+                  int *status, cudaStream_t st, const OutFuse *out, bool *fused) {
   (void)num_sms;
+  if (fused) *fused = false;
   CUtensorMap th, tv;
   if (!encode_maps(g, hin, val, &th, &tv)) return cudaErrorInvalidValue;
   const int ntx = (g.nx + BX - 1) / BX, nty = (g.ny + BY - 1) / BY;
@@ -642,9 +659,11 @@ cudaError_t layer(const HexGrid &g, int num_sms, const __nv_bfloat16 *hin, __nv_
   if (mm && std::strcmp(mm, "tc") == 0)
     k_lp_layer_hex_tc<<<grid, kThreads, kSmemTcBytes, st>>>(th, tv, g.nx, g.ny, g.nz, hout, wl,
                                                             bl, done, status);
-  else
+  else {
     k_lp_layer_hex<<<grid, kThreads, kSmemBytes, st>>>(th, tv, g.nx, g.ny, g.nz, hout, wl, bl,
-                                                       done, status);
+                                                       done, status, out ? *out : OutFuse{});
+    if (out && fused) *fused = true;
+  }
   return cudaPeekAtLastError();  // left set for the caller's launch check
 }
 

@@ -34,14 +34,27 @@ inline size_t value_count(const HexGrid &g) { return 7ull * g.nz * g.ny * g.nxp;
 cudaError_t values(const fcg_context *c, const HexGrid &g, const float *aval, float *val,
                    cudaStream_t st);
 
+// The network's output fused into its last layer: z = r + rms (w_out . h_L + b_out) per
+// cell, with wout = [w_out (C values), b_out] and rms a device scalar.  h_L itself is
+// then not stored.
+struct OutFuse {
+  const float *r, *rms, *wout;
+  float *z;
+};
+
 // One layer h_out = h_in + relu(W_l [h_in; Ahat h_in] + b_l) for all cells, the same
-// bits as the sliced gather form.  Returns cudaErrorInvalidValue without launching when
-// the driver refuses the tensor maps (the caller then runs the gather form), else the
-// launch error, which stays set for the caller's own check.  An mbarrier wait that
-// gives up (after 1 s) stores FCG_ERR_TIMEOUT into *status (when status is not NULL).
+// bits as the sliced gather form.  With `out` given, the kernel writes the output z of
+// OutFuse from the layer's tiles instead of h_out, the same bits as the output kernel
+// on h_out, and sets *fused; *fused stays false when the form launched cannot fuse it
+// (the caller then runs the output kernel).  Returns cudaErrorInvalidValue without
+// launching when the driver refuses the tensor maps (the caller then runs the gather
+// form), else the launch error, which stays set for the caller's own check.  An
+// mbarrier wait that gives up (after 1 s) stores FCG_ERR_TIMEOUT into *status (when
+// status is not NULL).
 cudaError_t layer(const HexGrid &g, int num_sms, const __nv_bfloat16 *hin, __nv_bfloat16 *hout,
                   const float *val, const __nv_bfloat16 *wl, const float *bl, const int *done,
-                  int *status, cudaStream_t st);
+                  int *status, cudaStream_t st, const OutFuse *out = nullptr,
+                  bool *fused = nullptr);
 
 }  // namespace lphex
 }  // namespace fcg

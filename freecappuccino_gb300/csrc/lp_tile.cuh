@@ -55,6 +55,27 @@ __device__ __forceinline__ void fma8(float (&acc)[8], float v, const uint4 &q) {
   }
 }
 
+// The network's output before its scaling, w_out . h + b_out, over one BF16 row of
+// kTileC channels held in v, in channel order (w = [w_out, b_out]).
+__device__ __forceinline__ float out_dot_vals(const uint4 (&v)[4], const float *w) {
+  float acc = w[kTileC];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(&v[q]);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) acc += w[q * 8 + c] * bf(e[c]);
+  }
+  return acc;
+}
+
+// out_dot_vals of a row in shared memory (16-byte aligned).
+__device__ __forceinline__ float out_dot_row(const __nv_bfloat16 *row, const float *w) {
+  uint4 v[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) v[q] = reinterpret_cast<const uint4 *>(row)[q];
+  return out_dot_vals(v, w);
+}
+
 // Stores row `row` of the warp's tile: own = the cell's h (8 channels at qc), acc = its
 // m (FP32 sums, rounded to BF16 here).
 __device__ __forceinline__ void tile_put_row(__nv_bfloat16 *tw, int row, int qc, const uint4 &own,
