@@ -224,51 +224,58 @@ __global__ void __launch_bounds__(kTPB)
   if (lane == 0) x[r] = acc;
 }
 
-// Row products of the coarse levels: four lanes per row (eight rows per warp), each
-// lane summing every fourth entry, then a shuffle sum.  Loops are warp-uniform.
-__device__ __forceinline__ float row4(const int *ptr, const int *col, const float *a,
-                                     const float *x, int row, int n, int q) {
+// Row products of the coarse levels: LPR lanes per row (32 / LPR rows per warp), each
+// lane summing every LPR-th entry, then a shuffle sum.  Four lanes on the sparse levels;
+// eight on the first level of the smoothed hierarchy (about 45 entries per row), so that
+// a row's lanes read whole 32-byte sectors of values and columns.  Loops are warp-uniform.
+template <int LPR>
+__device__ __forceinline__ float row_lanes(const int *ptr, const int *col, const float *a,
+                                          const float *x, int row, int n, int q) {
   float acc = 0.f;
   if (row < n)
-    for (int k = ptr[row] + q; k < ptr[row + 1]; k += 4) acc += a[k] * x[col[k]];
-  acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-  acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+    for (int k = ptr[row] + q; k < ptr[row + 1]; k += LPR) acc += a[k] * x[col[k]];
+#pragma unroll
+  for (int o = 1; o < LPR; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   return acc;
 }
 
 // y = x + omega dinv (b - A x); x == NULL stands for x = 0
+template <int LPR>
 __global__ void __launch_bounds__(kTPB)
     k_ml_jacobi(int n, const int *__restrict__ ptr, const int *__restrict__ col,
                 const float *__restrict__ a, const float *__restrict__ dinv,
                 const float *__restrict__ b, const float *__restrict__ x, float *__restrict__ y,
                 float omega, const int *done) {
   if (stopped(done)) return;
-  const int lane = threadIdx.x & 31, q = lane & 3;
+  constexpr int RPW = 32 / LPR;  // rows per warp
+  const int lane = threadIdx.x & 31, q = lane & (LPR - 1);
   const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long base = w0 * 8; base < n; base += nw * 8) {
-    const int row = (int)base + (lane >> 2);
+  for (long long base = w0 * RPW; base < n; base += nw * RPW) {
+    const int row = (int)base + lane / LPR;
     if (!x) {
       if (q == 0 && row < n) y[row] = omega * dinv[row] * b[row];
       continue;
     }
-    const float ax = row4(ptr, col, a, x, row, n, q);
+    const float ax = row_lanes<LPR>(ptr, col, a, x, row, n, q);
     if (q == 0 && row < n) y[row] = x[row] + omega * dinv[row] * (b[row] - ax);
   }
 }
 
 // t = b - A x
+template <int LPR>
 __global__ void __launch_bounds__(kTPB)
     k_ml_resid(int n, const int *__restrict__ ptr, const int *__restrict__ col,
                const float *__restrict__ a, const float *__restrict__ b,
                const float *__restrict__ x, float *__restrict__ t, const int *done) {
   if (stopped(done)) return;
-  const int lane = threadIdx.x & 31, q = lane & 3;
+  constexpr int RPW = 32 / LPR;
+  const int lane = threadIdx.x & 31, q = lane & (LPR - 1);
   const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long base = w0 * 8; base < n; base += nw * 8) {
-    const int row = (int)base + (lane >> 2);
-    const float ax = row4(ptr, col, a, x, row, n, q);
+  for (long long base = w0 * RPW; base < n; base += nw * RPW) {
+    const int row = (int)base + lane / LPR;
+    const float ax = row_lanes<LPR>(ptr, col, a, x, row, n, q);
     if (q == 0 && row < n) t[row] = b[row] - ax;
   }
 }
@@ -556,7 +563,11 @@ float *enqueue_vcycle(Hierarchy &H, int num_sms, const Options &o, cudaStream_t 
   DevLevel &L = H.lv[k];
   const float om = (float)o.omega, al = (float)o.alpha;
   const int g = grid_for(L.n, num_sms, 8);
-  const int g4 = grid_for(4LL * L.n, num_sms, 8);  // four lanes per row
+  // eight lanes per row on a level of 24 or more entries per row, else four
+  const bool wide = L.nnz >= 24LL * L.n;
+  const int g4 = grid_for((wide ? 8LL : 4LL) * L.n, num_sms, 8);
+  auto jacobi = wide ? k_ml_jacobi<8> : k_ml_jacobi<4>;
+  auto resid = wide ? k_ml_resid<8> : k_ml_resid<4>;
   const bool last = k + 1 == (int)H.lv.size();
   if (last && H.has_dense) {
     const int blocks = (L.n * 32 + kTPB - 1) / kTPB;
@@ -564,21 +575,21 @@ float *enqueue_vcycle(Hierarchy &H, int num_sms, const Options &o, cudaStream_t 
     return L.x;
   }
   float *cur = L.x, *oth = L.y;
-  k_ml_jacobi<<<g4, kTPB, 0, st>>>(L.n, L.ptr, L.col, L.a32, L.dinv, L.b, nullptr, cur, om, done);
+  jacobi<<<g4, kTPB, 0, st>>>(L.n, L.ptr, L.col, L.a32, L.dinv, L.b, nullptr, cur, om, done);
   const int pre = last ? 2 * o.sweeps + 2 : o.sweeps;  // coarsest without a dense inverse
   for (int s = 1; s < pre; ++s) {
-    k_ml_jacobi<<<g4, kTPB, 0, st>>>(L.n, L.ptr, L.col, L.a32, L.dinv, L.b, cur, oth, om, done);
+    jacobi<<<g4, kTPB, 0, st>>>(L.n, L.ptr, L.col, L.a32, L.dinv, L.b, cur, oth, om, done);
     std::swap(cur, oth);
   }
   if (last) return cur;
   DevLevel &Lc = H.lv[k + 1];
-  k_ml_resid<<<g4, kTPB, 0, st>>>(L.n, L.ptr, L.col, L.a32, L.b, cur, oth, done);
+  resid<<<g4, kTPB, 0, st>>>(L.n, L.ptr, L.col, L.a32, L.b, cur, oth, done);
   k_ml_restrict<<<grid_for(Lc.n, num_sms, 8), kTPB, 0, st>>>(Lc.n, Lc.mptr, Lc.mem, oth, Lc.b,
                                                             done);
   const float *e = enqueue_vcycle(H, num_sms, o, st, k + 1, done);
   k_ml_prolong<<<g, kTPB, 0, st>>>(L.n, Lc.agg, e, cur, al, done);
   for (int s = 0; s < o.sweeps; ++s) {
-    k_ml_jacobi<<<g4, kTPB, 0, st>>>(L.n, L.ptr, L.col, L.a32, L.dinv, L.b, cur, oth, om, done);
+    jacobi<<<g4, kTPB, 0, st>>>(L.n, L.ptr, L.col, L.a32, L.dinv, L.b, cur, oth, om, done);
     std::swap(cur, oth);
   }
   return cur;
