@@ -893,7 +893,11 @@ def main():
                            "method": method, "N": N, "cells": n, "nnz": nnz,
                            "coarse_sweeps": args.ml_sweeps if method == "learned" else None,
                            "jitter": JITTER, "tolerance": TOL, "iterations": iters,
-                           "l2": "inputs larger than L2 (matrix 0.94 GB, vectors 134 MB each)",
+                           "l2": (f"inputs larger than L2 (matrix {8 * nnz / 1e9:.2f} GB, "
+                                  f"vectors {8 * n / 1e6:.0f} MB each)"
+                                  if 8 * nnz > 129e6 else
+                                  f"matrix ({8 * nnz / 1e6:.0f} MB) within the 129 MB L2: "
+                                  "steps reuse it from L2"),
                            "parallelism": f"replicas x{ws}"},
                 "comparison": head, "parity": parity,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
